@@ -1,0 +1,131 @@
+/*
+ * cp_al_gb300.h -- entry points of libcp_al_gb300.so beyond the reference's
+ * cp_al.h.
+ *
+ * The reference solver reads a second set of options from CP_AL_* environment
+ * variables inside the library (LP/CP_AL/src/solver.cu:3141-3164, 3563-3579,
+ * 2857-2966; LP/CP_AL/src/utils.cu:324-332, 370-372).  That plane is made
+ * explicit here as cp_al_gb300_options_t.  solve_lp_problem() fills it from the
+ * environment with cp_al_gb300_options_from_env(), so a caller of the
+ * reference interface sees the same behaviour for the same environment.
+ *
+ * Only the options of the iteration itself are carried.  The reference's
+ * benchmark controllers (alpha trial/pulse, adaptive lambda tiers, dynamic
+ * evaluation frequency, Curtis-Reid scaling, diagnostics) are not.
+ */
+#pragma once
+
+#include "cp_al_types.h"
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CP_AL_GB300_FP64 = 0,        /* plain FP64 everywhere */
+    CP_AL_GB300_FP32_REFINE = 1  /* FP32 matrix/vectors, FP64 anchors and
+                                    reductions, then an FP64 refinement phase */
+} cp_al_gb300_precision_t;
+
+typedef struct {
+    /* --- the reference's CP_AL_* environment plane (same names, defaults) --- */
+    double al_lambda;             /* CP_AL_LAMBDA, default 0.05 (solver.cu:3579) */
+    int sigma_mode;               /* CP_AL_SIGMA_MODE!=0 or CP_AL_SIGMA set (solver.cu:3563-3564) */
+    int sigma_set;                /* 1 when CP_AL_SIGMA gives sigma explicitly */
+    double sigma;                 /* CP_AL_SIGMA */
+    int sigma_adaptive;           /* CP_AL_SIGMA_ADAPTIVE; default 1 unless sigma_set (solver.cu:3158-3161) */
+    double sigma_init_factor;     /* CP_AL_SIGMA_INIT_FACTOR, 6.0 */
+    double sigma_min_factor;      /* CP_AL_SIGMA_MIN_FACTOR, 1e-4 */
+    double sigma_max_factor;      /* CP_AL_SIGMA_MAX_FACTOR, 100 */
+    double lambda_factor;         /* CP_AL_LAMBDA_FACTOR, 2.01 */
+    int lambda_param_set;         /* 1 when CP_AL_LAMBDA_PARAM is given */
+    double lambda_param;          /* CP_AL_LAMBDA_PARAM */
+    double sigma_balance_gain;    /* CP_AL_SIGMA_BALANCE_GAIN, 0.15 */
+    double sigma_i_smooth;        /* CP_AL_SIGMA_I_SMOOTH; NaN = restart_params.i_smooth */
+    double sigma_kp;              /* CP_AL_SIGMA_KP; NaN = restart_params.k_p */
+    double sigma_ki;              /* CP_AL_SIGMA_KI; NaN = restart_params.k_i */
+    double sigma_kd;              /* CP_AL_SIGMA_KD; NaN = restart_params.k_d */
+    double sigma_update_min;      /* CP_AL_SIGMA_UPDATE_MIN, 0.60 */
+    double sigma_update_max;      /* CP_AL_SIGMA_UPDATE_MAX, 1.70 */
+    double step_margin;           /* CP_AL_STEP_MARGIN, 0.998^2 */
+    double restart_sufficient;    /* CP_AL_RESTART_SUFFICIENT; NaN = params */
+    double restart_necessary;     /* CP_AL_RESTART_NECESSARY; NaN = params */
+    double restart_artificial;    /* CP_AL_RESTART_ARTIFICIAL; NaN = params */
+    int restart_select;           /* CP_AL_RESTART_SELECT, 0 = off (solver.cu:2749-2819) */
+    double restart_select_margin; /* CP_AL_RESTART_SELECT_MARGIN, 1.0 */
+    int restart_select_min_iters; /* CP_AL_RESTART_SELECT_MIN_ITERS, 0 */
+    int restart_select_threepoint;/* CP_AL_RESTART_SELECT_THREEPOINT, 0 */
+
+    /* --- options of this implementation --- */
+    int precision;                /* cp_al_gb300_precision_t */
+    double fp32_switch_tol;       /* FP32 phase ends when rel KKT < this (default 1e-5) */
+    int fp32_max_iterations;      /* FP32 phase iteration cap (default: none, -1) */
+    int spmv_nnz_per_block;       /* row-block nonzero budget; 0 = autotune */
+    int device;                   /* CUDA device ordinal, -1 = current */
+    int graph_blocks;             /* evaluation blocks per host check (default 1) */
+    int timing;                   /* 1: time one primal and one dual launch per
+                                     block with CUDA events (stats avg_*_ms) */
+} cp_al_gb300_options_t;
+
+/* Statistics of the last solve on this thread (for benchmarks and tests). */
+typedef struct {
+    double setup_sec;             /* upload, transpose, scaling, power iteration */
+    double loop_sec;              /* iteration loop (wall) */
+    double total_sec;             /* whole call, including result download */
+    double lambda_est;            /* power-iteration estimate of sigma_max(A)^2 */
+    int power_iterations;
+    int restarts;
+    int fp32_iterations;          /* iterations run in the FP32 phase */
+    int64_t kernel_launches;      /* kernels of this library launched by the loop */
+    int64_t h2d_bytes;
+    int64_t d2h_bytes;
+    double primal_weight;
+    double step_size;
+    double al_penalty;
+    /* timing == 1: mean duration of one primal / dual launch and of one
+     * evaluation block, over the FP64 blocks and over the FP32 blocks */
+    double avg_primal_ms;
+    double avg_dual_ms;
+    double avg_block_ms;
+    int timed_blocks;
+    double avg_primal32_ms;
+    double avg_dual32_ms;
+    double avg_block32_ms;
+    int timed_blocks32;
+} cp_al_gb300_stats_t;
+
+/* The reference defaults of every field, ignoring the environment. */
+void cp_al_gb300_default_options(cp_al_gb300_options_t *opts);
+
+/* Defaults, then each CP_AL_* variable that is set and parses overrides its
+ * field exactly as the reference's getenv readers do. */
+void cp_al_gb300_options_from_env(cp_al_gb300_options_t *opts);
+
+/* solve_lp_problem with explicit options (opts == NULL -> from environment). */
+cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *params,
+                                  const cp_al_gb300_options_t *opts);
+
+/* Statistics of the last solve made by the calling thread. */
+void cp_al_gb300_last_stats(cp_al_gb300_stats_t *out);
+
+/* Last error message of the calling thread ("" if none). */
+const char *cp_al_gb300_last_error(void);
+
+/* --- device-resident solves (inputs already in HBM) ---------------------- */
+typedef struct cp_al_gb300_session cp_al_gb300_session_t;
+
+/* Uploads and prepares the problem (transpose, scaling, power iteration are
+ * done by cp_al_gb300_session_solve, not here, so that a solve is complete). */
+cp_al_gb300_session_t *cp_al_gb300_session_create(const lp_problem_t *prob, const cp_al_parameters_t *params,
+                                                  const cp_al_gb300_options_t *opts);
+/* Solves from the device-resident copy; the result stays on the device except
+ * for the scalar summary written to *summary (vectors are not downloaded). */
+int cp_al_gb300_session_solve(cp_al_gb300_session_t *s, cp_al_result_t *summary);
+/* Downloads the unscaled solution of the last session solve. */
+int cp_al_gb300_session_fetch(cp_al_gb300_session_t *s, double *primal, double *dual, double *reduced_cost);
+void cp_al_gb300_session_free(cp_al_gb300_session_t *s);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif

@@ -1,0 +1,150 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+The oracle restates the reference solver on the CPU in FP64; tests compare the
+CUDA library against it.  Nothing in pdal_gb300/ imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+from pdal_gb300 import _native as N  # struct layouts of include/*.h only
+from pdal_gb300.lp import LPData, LPResult, apply_options, apply_params
+
+from . import build as _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        L.oracle_cpal_solve.restype = C.POINTER(N.CpalResult)
+        L.oracle_cpal_solve.argtypes = [C.POINTER(N.LpProblem), C.POINTER(N.CpalParameters),
+                                        C.POINTER(N.CpalOptions), _ip]
+        L.oracle_cpal_result_free.argtypes = [C.POINTER(N.CpalResult)]
+        L.oracle_cpal_default_options.argtypes = [C.POINTER(N.CpalOptions)]
+        L.oracle_cpal_default_parameters.argtypes = [C.POINTER(N.CpalParameters)]
+        L.oracle_set_threads.argtypes = [C.c_int]
+        L.oracle_max_threads.restype = C.c_int
+        L.oracle_cpal_rescale.argtypes = [C.POINTER(N.LpProblem), C.POINTER(N.CpalParameters), _dp, _dp, _dp, _dp]
+        L.oracle_power_iteration.restype = C.c_double
+        L.oracle_power_iteration.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, C.c_int, C.c_double, _ip]
+        _lib = L
+    return _lib
+
+
+def default_parameters() -> N.CpalParameters:
+    p = N.CpalParameters()
+    lib().oracle_cpal_default_parameters(C.byref(p))
+    return p
+
+
+def default_options() -> N.CpalOptions:
+    o = N.CpalOptions()
+    lib().oracle_cpal_default_options(C.byref(o))
+    return o
+
+
+class _Problem:
+    """lp_problem_t pointing at numpy arrays kept alive by this object."""
+
+    def __init__(self, data: LPData):
+        rp, ci, v, (m, n) = data.csr()
+        f = lambda a, k, fill: (np.ascontiguousarray(a, dtype=np.float64) if a is not None else np.full(k, fill))
+        self.keep = [rp, ci, v, f(data.c, n, 0.0), f(data.var_lb, n, -np.inf), f(data.var_ub, n, np.inf),
+                     f(data.con_lb, m, -np.inf), f(data.con_ub, m, np.inf)]
+        p = N.LpProblem()
+        p.num_variables, p.num_constraints = n, m
+        p.constraint_matrix_row_pointers = rp.ctypes.data_as(_ip)
+        p.constraint_matrix_col_indices = ci.ctypes.data_as(_ip)
+        p.constraint_matrix_values = v.ctypes.data_as(_dp)
+        p.constraint_matrix_num_nonzeros = int(ci.shape[0])
+        p.objective_vector = self.keep[3].ctypes.data_as(_dp)
+        p.variable_lower_bound = self.keep[4].ctypes.data_as(_dp)
+        p.variable_upper_bound = self.keep[5].ctypes.data_as(_dp)
+        p.constraint_lower_bound = self.keep[6].ctypes.data_as(_dp)
+        p.constraint_upper_bound = self.keep[7].ctypes.data_as(_dp)
+        p.objective_constant = float(data.c0)
+        if data.primal_start is not None:
+            xs = np.ascontiguousarray(data.primal_start, dtype=np.float64)
+            self.keep.append(xs)
+            p.primal_start = xs.ctypes.data_as(_dp)
+        if data.dual_start is not None:
+            ys = np.ascontiguousarray(data.dual_start, dtype=np.float64)
+            self.keep.append(ys)
+            p.dual_start = ys.ctypes.data_as(_dp)
+        self.p, self.m, self.n = p, m, n
+
+
+def solve_lp(data: LPData, params: dict | None = None, options: dict | None = None, threads: int = 1) -> LPResult:
+    L = lib()
+    p = apply_params(default_parameters(), params)
+    o = apply_options(default_options(), options)
+    prob = _Problem(data)
+    L.oracle_set_threads(int(threads))
+    piters = C.c_int(0)
+    rp = L.oracle_cpal_solve(C.byref(prob.p), C.byref(p), C.byref(o), C.byref(piters))
+    if not rp:
+        raise RuntimeError("oracle solve failed (invalid parameters)")
+    try:
+        r = rp.contents
+        vec = lambda ptr, k: np.ctypeslib.as_array(ptr, shape=(k,)).copy() if k > 0 else np.zeros(0)
+        return LPResult(
+            status=N.TERMINATION_REASONS[r.termination_reason],
+            status_code=r.termination_reason,
+            iterations=r.total_count,
+            x=vec(r.primal_solution, prob.n),
+            y=vec(r.dual_solution, prob.m),
+            reduced_cost=vec(r.reduced_cost, prob.n),
+            primal_objective=r.primal_objective_value,
+            dual_objective=r.dual_objective_value,
+            relative_primal_residual=r.relative_primal_residual,
+            relative_dual_residual=r.relative_dual_residual,
+            relative_gap=r.relative_objective_gap,
+            absolute_primal_residual=r.absolute_primal_residual,
+            absolute_dual_residual=r.absolute_dual_residual,
+            setup_sec=r.rescaling_time_sec,
+            solve_sec=r.cumulative_time_sec,
+            stats={"power_iterations": piters.value},
+        )
+    finally:
+        L.oracle_cpal_result_free(rp)
+
+
+def rescale(data: LPData, params: dict | None = None):
+    """(row_scale, col_scale, cbr, ovr, scaled A values) of the reference's
+    rescale_problem, from the oracle."""
+    L = lib()
+    p = apply_params(default_parameters(), params)
+    prob = _Problem(data)
+    r = np.empty(prob.m)
+    d = np.empty(prob.n)
+    co = np.empty(2)
+    sv = np.empty(int(prob.p.constraint_matrix_num_nonzeros))
+    L.oracle_cpal_rescale(C.byref(prob.p), C.byref(p), r.ctypes.data_as(_dp), d.ctypes.data_as(_dp),
+                          co.ctypes.data_as(_dp), sv.ctypes.data_as(_dp))
+    return r, d, co[0], co[1], sv
+
+
+def power_iteration(data: LPData, max_iter: int = 5000, tol: float = 1e-4):
+    rp, ci, v, (m, n) = data.csr()
+    it = C.c_int(0)
+    s = lib().oracle_power_iteration(m, n, rp.ctypes.data_as(_ip), ci.ctypes.data_as(_ip), v.ctypes.data_as(_dp),
+                                     max_iter, tol, C.byref(it))
+    return s, it.value
+
+
+def max_threads() -> int:
+    return lib().oracle_max_threads()

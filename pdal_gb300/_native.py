@@ -1,0 +1,276 @@
+"""ctypes mirror of the C interface in include/cp_al_types.h, include/cp_al.h
+and include/cp_al_gb300.h, plus the loader of the in-tree libraries.
+
+The loader never falls back to anything: if the CUDA library is missing it
+raises, so a product path cannot silently run elsewhere.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIBDIR = Path(__file__).resolve().parent / "lib"
+
+TERMINATION_REASONS = {
+    0: "UNSPECIFIED",
+    1: "OPTIMAL",
+    2: "PRIMAL_INFEASIBLE",
+    3: "DUAL_INFEASIBLE",
+    4: "INFEASIBLE_OR_UNBOUNDED",
+    5: "TIME_LIMIT",
+    6: "ITERATION_LIMIT",
+    7: "FEAS_POLISH_SUCCESS",
+}
+
+NORM_L2, NORM_LINF = 0, 1
+MATRIX_DENSE, MATRIX_CSR, MATRIX_CSC, MATRIX_COO = 0, 1, 2, 3
+PRECISION_FP64, PRECISION_FP32_REFINE = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class LpProblem(C.Structure):
+    _fields_ = [
+        ("num_variables", C.c_int),
+        ("num_constraints", C.c_int),
+        ("variable_lower_bound", _dp),
+        ("variable_upper_bound", _dp),
+        ("objective_vector", _dp),
+        ("objective_constant", C.c_double),
+        ("constraint_matrix_row_pointers", _ip),
+        ("constraint_matrix_col_indices", _ip),
+        ("constraint_matrix_values", _dp),
+        ("constraint_matrix_num_nonzeros", C.c_int),
+        ("constraint_lower_bound", _dp),
+        ("constraint_upper_bound", _dp),
+        ("primal_start", _dp),
+        ("dual_start", _dp),
+    ]
+
+
+class RestartParams(C.Structure):
+    _fields_ = [
+        ("artificial_restart_threshold", C.c_double),
+        ("sufficient_reduction_for_restart", C.c_double),
+        ("necessary_reduction_for_restart", C.c_double),
+        ("k_p", C.c_double),
+        ("k_i", C.c_double),
+        ("k_d", C.c_double),
+        ("i_smooth", C.c_double),
+    ]
+
+
+class TerminationCriteria(C.Structure):
+    _fields_ = [
+        ("eps_optimal_relative", C.c_double),
+        ("eps_feasible_relative", C.c_double),
+        ("eps_feas_polish_relative", C.c_double),
+        ("time_sec_limit", C.c_double),
+        ("iteration_limit", C.c_int),
+    ]
+
+
+class CpalParameters(C.Structure):
+    _fields_ = [
+        ("l_inf_ruiz_iterations", C.c_int),
+        ("has_pock_chambolle_alpha", C.c_bool),
+        ("pock_chambolle_alpha", C.c_double),
+        ("bound_objective_rescaling", C.c_bool),
+        ("verbose", C.c_bool),
+        ("termination_evaluation_frequency", C.c_int),
+        ("sv_max_iter", C.c_int),
+        ("sv_tol", C.c_double),
+        ("termination_criteria", TerminationCriteria),
+        ("restart_params", RestartParams),
+        ("reflection_coefficient", C.c_double),
+        ("feasibility_polishing", C.c_bool),
+        ("optimality_norm", C.c_int),
+        ("presolve", C.c_bool),
+        ("matrix_zero_tol", C.c_double),
+    ]
+
+
+class CpalResult(C.Structure):
+    _fields_ = [
+        ("num_variables", C.c_int),
+        ("num_constraints", C.c_int),
+        ("num_nonzeros", C.c_int),
+        ("num_reduced_variables", C.c_int),
+        ("num_reduced_constraints", C.c_int),
+        ("num_reduced_nonzeros", C.c_int),
+        ("primal_solution", _dp),
+        ("dual_solution", _dp),
+        ("reduced_cost", _dp),
+        ("total_count", C.c_int),
+        ("rescaling_time_sec", C.c_double),
+        ("cumulative_time_sec", C.c_double),
+        ("presolve_time", C.c_double),
+        ("presolve_status", C.c_int),
+        ("absolute_primal_residual", C.c_double),
+        ("relative_primal_residual", C.c_double),
+        ("absolute_dual_residual", C.c_double),
+        ("relative_dual_residual", C.c_double),
+        ("primal_objective_value", C.c_double),
+        ("dual_objective_value", C.c_double),
+        ("objective_gap", C.c_double),
+        ("relative_objective_gap", C.c_double),
+        ("max_primal_ray_infeasibility", C.c_double),
+        ("max_dual_ray_infeasibility", C.c_double),
+        ("primal_ray_linear_objective", C.c_double),
+        ("dual_ray_objective", C.c_double),
+        ("termination_reason", C.c_int),
+        ("feasibility_polishing_time", C.c_double),
+        ("feasibility_iteration", C.c_int),
+    ]
+
+
+class _Dense(C.Structure):
+    _fields_ = [("A", _dp)]
+
+
+class _Csr(C.Structure):
+    _fields_ = [("nnz", C.c_int), ("row_ptr", _ip), ("col_ind", _ip), ("vals", _dp)]
+
+
+class _Csc(C.Structure):
+    _fields_ = [("nnz", C.c_int), ("col_ptr", _ip), ("row_ind", _ip), ("vals", _dp)]
+
+
+class _Coo(C.Structure):
+    _fields_ = [("nnz", C.c_int), ("row_ind", _ip), ("col_ind", _ip), ("vals", _dp)]
+
+
+class _MatrixData(C.Union):
+    _fields_ = [("dense", _Dense), ("csr", _Csr), ("csc", _Csc), ("coo", _Coo)]
+
+
+class MatrixDesc(C.Structure):
+    """LP/CP_AL/include/cp_al_types.h:145-189 (the CP_AL layout, without
+    FA_CP's zero_tolerance member)."""
+
+    _fields_ = [("m", C.c_int), ("n", C.c_int), ("fmt", C.c_int), ("data", _MatrixData)]
+
+
+class CpalOptions(C.Structure):
+    _fields_ = [
+        ("al_lambda", C.c_double),
+        ("sigma_mode", C.c_int),
+        ("sigma_set", C.c_int),
+        ("sigma", C.c_double),
+        ("sigma_adaptive", C.c_int),
+        ("sigma_init_factor", C.c_double),
+        ("sigma_min_factor", C.c_double),
+        ("sigma_max_factor", C.c_double),
+        ("lambda_factor", C.c_double),
+        ("lambda_param_set", C.c_int),
+        ("lambda_param", C.c_double),
+        ("sigma_balance_gain", C.c_double),
+        ("sigma_i_smooth", C.c_double),
+        ("sigma_kp", C.c_double),
+        ("sigma_ki", C.c_double),
+        ("sigma_kd", C.c_double),
+        ("sigma_update_min", C.c_double),
+        ("sigma_update_max", C.c_double),
+        ("step_margin", C.c_double),
+        ("restart_sufficient", C.c_double),
+        ("restart_necessary", C.c_double),
+        ("restart_artificial", C.c_double),
+        ("restart_select", C.c_int),
+        ("restart_select_margin", C.c_double),
+        ("restart_select_min_iters", C.c_int),
+        ("restart_select_threepoint", C.c_int),
+        ("precision", C.c_int),
+        ("fp32_switch_tol", C.c_double),
+        ("fp32_max_iterations", C.c_int),
+        ("spmv_nnz_per_block", C.c_int),
+        ("device", C.c_int),
+        ("graph_blocks", C.c_int),
+        ("timing", C.c_int),
+    ]
+
+
+class CpalStats(C.Structure):
+    _fields_ = [
+        ("setup_sec", C.c_double),
+        ("loop_sec", C.c_double),
+        ("total_sec", C.c_double),
+        ("lambda_est", C.c_double),
+        ("power_iterations", C.c_int),
+        ("restarts", C.c_int),
+        ("fp32_iterations", C.c_int),
+        ("kernel_launches", C.c_int64),
+        ("h2d_bytes", C.c_int64),
+        ("d2h_bytes", C.c_int64),
+        ("primal_weight", C.c_double),
+        ("step_size", C.c_double),
+        ("al_penalty", C.c_double),
+        ("avg_primal_ms", C.c_double),
+        ("avg_dual_ms", C.c_double),
+        ("avg_block_ms", C.c_double),
+        ("timed_blocks", C.c_int),
+        ("avg_primal32_ms", C.c_double),
+        ("avg_dual32_ms", C.c_double),
+        ("avg_block32_ms", C.c_double),
+        ("timed_blocks32", C.c_int),
+    ]
+
+
+# name -> (restype, argtypes); every symbol include/cp_al.h and
+# include/cp_al_gb300.h declare
+LP_SYMBOLS = {
+    "create_lp_problem": (C.POINTER(LpProblem), [_dp, C.POINTER(MatrixDesc), _dp, _dp, _dp, _dp, _dp]),
+    "set_start_values": (None, [C.POINTER(LpProblem), _dp, _dp]),
+    "solve_lp_problem": (C.POINTER(CpalResult), [C.POINTER(LpProblem), C.POINTER(CpalParameters)]),
+    "set_default_parameters": (None, [C.POINTER(CpalParameters)]),
+    "cp_al_result_free": (None, [C.POINTER(CpalResult)]),
+    "lp_problem_free": (None, [C.POINTER(LpProblem)]),
+    "cp_al_gb300_default_options": (None, [C.POINTER(CpalOptions)]),
+    "cp_al_gb300_options_from_env": (None, [C.POINTER(CpalOptions)]),
+    "cp_al_gb300_solve": (
+        C.POINTER(CpalResult),
+        [C.POINTER(LpProblem), C.POINTER(CpalParameters), C.POINTER(CpalOptions)],
+    ),
+    "cp_al_gb300_last_stats": (None, [C.POINTER(CpalStats)]),
+    "cp_al_gb300_last_error": (C.c_char_p, []),
+    "cp_al_gb300_session_create": (
+        C.c_void_p,
+        [C.POINTER(LpProblem), C.POINTER(CpalParameters), C.POINTER(CpalOptions)],
+    ),
+    "cp_al_gb300_session_solve": (C.c_int, [C.c_void_p, C.POINTER(CpalResult)]),
+    "cp_al_gb300_session_fetch": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "cp_al_gb300_session_free": (None, [C.c_void_p]),
+}
+
+_LIBS: dict[str, C.CDLL] = {}
+
+
+def lib_path(name: str) -> Path:
+    return LIBDIR / name
+
+
+def load(name: str, symbols: dict) -> C.CDLL:
+    if name in _LIBS:
+        return _LIBS[name]
+    path = lib_path(name)
+    if not path.exists():
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA library first (python -m pdal_gb300.build); "
+            "there is no CPU fallback"
+        )
+    lib = C.CDLL(str(path))
+    for sym, (res, args) in symbols.items():
+        fn = getattr(lib, sym)
+        fn.restype = res
+        fn.argtypes = args
+    _LIBS[name] = lib
+    return lib
+
+
+def load_lp() -> C.CDLL:
+    return load("libcp_al_gb300.so", LP_SYMBOLS)
+
+
+def last_error(lib: C.CDLL) -> str:
+    msg = lib.cp_al_gb300_last_error()
+    return msg.decode() if msg else ""

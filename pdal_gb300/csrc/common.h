@@ -1,0 +1,111 @@
+/*
+ * common.h -- host-side helpers shared by the solver translation units:
+ * CUDA error handling that never exits the process, a device arena, CSR
+ * utilities and row-block planning.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace pdal {
+
+/* Every CUDA failure becomes an exception that the C entry points turn into a
+ * NULL result plus a message (the reference calls exit(): internal/utils.h:32-63). */
+struct Error : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+#define PDAL_CUDA(call)                                                                                 \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            throw ::pdal::Error(std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " + __FILE__ + \
+                                ":" + std::to_string(__LINE__));                                        \
+        }                                                                                               \
+    } while (0)
+
+/* One cudaMalloc for all buffers of a solve; sub-allocations are 256-byte
+ * aligned so every vector can be read with 128-bit loads.  The same
+ * allocation code runs twice: once in measuring mode (take() only counts),
+ * then for real after reserve(). */
+class Arena {
+  public:
+    Arena() = default;
+    Arena(const Arena &) = delete;
+    Arena &operator=(const Arena &) = delete;
+    ~Arena() { release(); }
+    void begin_measure() {
+        release();
+        measuring_ = true;
+        off_ = 0;
+    }
+    void reserve_measured() {
+        const size_t bytes = off_;
+        measuring_ = false;
+        cap_ = bytes + 256;
+        PDAL_CUDA(cudaMalloc(&base_, cap_));
+        off_ = 0;
+    }
+    template <typename T>
+    T *take(size_t count) {
+        size_t bytes = ((count * sizeof(T)) + 255) & ~size_t(255);
+        if (bytes == 0) bytes = 256;
+        if (measuring_) {
+            off_ += bytes;
+            return reinterpret_cast<T *>(alignof(T) > 256 ? alignof(T) : 256);
+        }
+        if (off_ + bytes > cap_) throw Error("device arena exhausted");
+        T *p = reinterpret_cast<T *>(static_cast<char *>(base_) + off_);
+        off_ += bytes;
+        return p;
+    }
+    void release() {
+        if (base_) cudaFree(base_);
+        base_ = nullptr;
+        cap_ = off_ = 0;
+    }
+    size_t used() const { return off_; }
+    size_t capacity() const { return cap_; }
+
+  private:
+    void *base_ = nullptr;
+    size_t cap_ = 0, off_ = 0;
+    bool measuring_ = false;
+};
+
+/* Host CSR. */
+struct HostCsr {
+    int nr = 0, nc = 0;
+    std::vector<int> rp, ci;
+    std::vector<double> v;
+    int nnz() const { return (int)ci.size(); }
+};
+
+/* Transpose with rows of A^T in increasing row order of A. */
+HostCsr csr_transpose(int nr, int nc, const int *rp, const int *ci, const double *v);
+
+/* Checks row pointers (monotone, rp[0]=0, rp[nr]=nnz) and column range; the
+ * kernels index vectors with these values, so a malformed matrix is refused
+ * on the host instead of reading outside a device buffer. */
+void csr_validate(int nr, int nc, const int *rp, const int *ci, int nnz, const char *what);
+
+/* Row-block plan (see rowblock.cuh). */
+struct HostPlan {
+    int S = 0;
+    std::vector<int> desc;  /* 4 ints per block */
+    std::vector<int> linfo; /* 4 ints per long row */
+    int nblocks = 0, nlong = 0, npieces = 0;
+};
+HostPlan plan_rows(int nr, const int *rp, int S);
+
+/* Nonzero budget per block for a matrix of `nnz` nonzeros when none is
+ * requested: enough blocks to cover the 152 SMs twice, at most 2048. */
+int auto_block_nnz(long long nnz, int nr);
+
+} // namespace pdal

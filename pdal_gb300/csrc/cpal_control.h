@@ -1,0 +1,269 @@
+/*
+ * cpal_control.h -- scalar control logic of the CP_AL iteration, compiled for
+ * both the host (initial step schedule) and the device (the single-thread
+ * controller kernel that ends every evaluation block).
+ *
+ * Running the decisions on the device is what lets the loop replay as a CUDA
+ * graph: the reference does the same work on the host after about ten
+ * host-synchronising cuBLAS reductions per block (LP/CP_AL/src/solver.cu:
+ * 1343-1697).  The rules themselves are the reference's:
+ *   step schedule      LP/CP_AL/src/solver.cu:3103-3139
+ *   sigma parameters   LP/CP_AL/src/solver.cu:3141-3164
+ *   fixed-point error  LP/CP_AL/src/solver.cu:3611-3686
+ *   residual / KKT     LP/CP_AL/src/utils.cu:812-917
+ *   termination        LP/CP_AL/src/utils.cu:275-317
+ *   restart rule       LP/CP_AL/src/utils.cu:319-359
+ *   restart (PID, sigma PID, best weight)  LP/CP_AL/src/solver.cu:2821-3101
+ */
+#pragma once
+
+#include <math.h>
+
+#ifdef __CUDACC__
+#define PDAL_HD __host__ __device__ __forceinline__
+#else
+#define PDAL_HD inline
+#endif
+
+namespace pdal {
+
+/* Parameters the controller needs, resolved on the host once per solve. */
+struct CpalParams {
+    int F;                 /* termination_evaluation_frequency */
+    int iteration_limit;
+    double time_limit;
+    double eps_opt, eps_feas;
+    int norm_linf;
+    double refl;           /* reflection coefficient */
+    double suff, nec, art; /* restart thresholds (environment overrides applied) */
+    double kp, ki, kd, ismooth;
+    int sigma_mode, sigma_adaptive;
+    double s_kp, s_ki, s_kd, s_ismooth, s_gain, s_umin, s_umax;
+    double step_margin, lambda_factor;
+    int lambda_param_set;
+    double lambda_param_opt;
+    double obj_norm, bnd_norm, obj_const;
+};
+
+/* Solver scalars, resident in device memory during the loop. */
+struct CpalState {
+    /* coefficients read by the iteration kernels */
+    double tau, rho, beta, inv_tau, inv_prox, inv_beta, refl;
+    int inner;   /* Halpern counter at the start of the current block */
+    int status;  /* 0 while running, else termination_reason_t */
+    int restart; /* 1 when the last evaluation restarted */
+    int total;
+    /* controller state */
+    double step, pw, al_lambda, lambda_est;
+    double sigma, sigma_base, sigma_min, sigma_max, sigma_best, sigma_esum, sigma_last, lambda_param;
+    double pw_esum, pw_last, best_pw, best_gap;
+    double fp, fp0, fp_last;
+    double abs_p, abs_d, rel_p, rel_d, pobj, dobj, gap, rel_gap;
+    double cbr, ovr;
+    double elapsed;
+    unsigned long long t_start_ns;
+    int restarts;
+    int sigma_on;
+    int sigma_adapt;
+    int phase_switch;      /* 1: the FP32 phase reached its switch tolerance */
+    double fp32_switch_tol; /* < 0: no FP32 phase running */
+};
+
+/* Reduction terms of one evaluation (finished sums / maxima). */
+struct CpalEval {
+    /* rows of A */
+    double rp2, contrib, adx2, dy2, ddy2, axd2, rpmax;
+    /* rows of A^T */
+    double rd2, dx2, cross, cx, lx, ddx2, rdmax;
+};
+
+PDAL_HD void cpal_set_coefficients(CpalState &s) {
+    s.tau = s.step / s.pw;
+    s.rho = s.step * s.pw;
+    s.inv_tau = 1.0 / s.tau;
+    s.inv_prox = 1.0 / (s.rho + s.beta);
+    s.inv_beta = s.beta > 0.0 ? 1.0 / s.beta : 0.0;
+}
+
+/* LP/CP_AL/src/solver.cu:3103-3139 */
+PDAL_HD void cpal_refresh_step_schedule(CpalState &s, const CpalParams &p) {
+    const double margin = p.step_margin;
+    if (s.sigma_on) {
+        const double sg = fmax(s.sigma, 0.0);
+        if (sg <= 0.0) {
+            s.beta = 0.0;
+            s.lambda_param = 0.0;
+            s.step = sqrt(fmax(margin / fmax(s.lambda_est, 1e-12), 1e-24));
+            s.al_lambda = 0.0;
+            return;
+        }
+        if (!isfinite(s.lambda_param) || s.lambda_param <= 0.0) {
+            s.lambda_param = p.lambda_param_set ? p.lambda_param_opt : p.lambda_factor * fmax(s.lambda_est, 1e-12);
+        }
+        s.lambda_param = fmax(s.lambda_param, (2.0 + 1e-12) * fmax(s.lambda_est, 1e-12));
+        const double tau = 1.0 / (sg * s.lambda_param);
+        const double rho = sg;
+        s.beta = sg;
+        s.step = sqrt(fmax(tau * rho, 1e-24));
+        s.pw = sqrt(fmax(rho / tau, 1e-24));
+        s.al_lambda = 0.0;
+        return;
+    }
+    s.al_lambda = fmin(fmax(s.al_lambda, 0.0), 0.95);
+    const double eta_sq = margin * (1.0 - s.al_lambda) / fmax(s.lambda_est, 1e-12);
+    s.step = sqrt(fmax(eta_sq, 1e-24));
+    const double dual_step = s.step * fmax(s.pw, 1e-12);
+    s.beta = dual_step * s.al_lambda / fmax(1.0 - s.al_lambda, 1e-12);
+}
+
+/* LP/CP_AL/src/solver.cu:3611-3686; the arguments are squared norms, taken
+ * through sqrt and squared again as the reference does with nrm2 results. */
+PDAL_HD double cpal_fixed_point_error(const CpalState &s, double pn2, double dn2, double axn2, double cross) {
+    const double pn = sqrt(pn2), dn = sqrt(dn2), axn = sqrt(axn2);
+    if (s.sigma_on && s.sigma > 0.0 && s.lambda_param > 0.0) {
+        const double val = s.sigma * (s.lambda_param * pn * pn - axn * axn) + dn * dn / fmax(s.sigma, 1e-16);
+        return sqrt(fmax(val, 0.0));
+    }
+    const double movement = pn * pn * s.pw + dn * dn / s.pw;
+    const double interaction = 2 * s.step * cross;
+    const double augmentation = s.step * s.beta * axn * axn;
+    return sqrt(fmax(movement + interaction - augmentation, 0.0));
+}
+
+/* LP/CP_AL/src/utils.cu:812-917 (scalar tail of compute_residual) */
+PDAL_HD void cpal_residual_scalars(CpalState &s, const CpalParams &p, const CpalEval &e) {
+    if (p.norm_linf) {
+        s.abs_p = e.rpmax;
+        s.abs_d = e.rdmax;
+    } else {
+        s.abs_p = sqrt(e.rp2) / s.cbr;
+        s.abs_d = sqrt(e.rd2);
+    }
+    s.abs_d /= s.ovr;
+    s.pobj = e.cx / (s.cbr * s.ovr) + p.obj_const;
+    s.dobj = (e.lx + e.contrib) / (s.cbr * s.ovr) + p.obj_const;
+    s.rel_p = s.abs_p / (1.0 + p.bnd_norm);
+    s.rel_d = s.abs_d / (1.0 + p.obj_norm);
+    s.gap = fabs(s.pobj - s.dobj);
+    s.rel_gap = s.gap / (1.0 + fabs(s.pobj) + fabs(s.dobj));
+}
+
+/* LP/CP_AL/src/utils.cu:319-359 */
+PDAL_HD bool cpal_should_restart(CpalState &s, const CpalParams &p) {
+    bool rs = false;
+    if (s.total == p.F) {
+        rs = true;
+    } else if (s.total > p.F) {
+        if (s.fp <= p.suff * s.fp0) rs = true;
+        if (s.fp <= p.nec * s.fp0 && s.fp > s.fp_last) rs = true;
+        if (s.inner >= p.art * s.total) rs = true;
+    }
+    s.fp_last = s.fp;
+    return rs;
+}
+
+/* Scalar part of LP/CP_AL/src/solver.cu:2821-3101 (restart target "current");
+ * pd2/dd2 are the squared distances of (x^, y^) from the anchors, axd2 the
+ * squared norm of A(x^ - x0). */
+PDAL_HD void cpal_restart_scalars(CpalState &s, const CpalParams &p, double pd2, double dd2, double axd2) {
+    const double pd = sqrt(pd2), dd = sqrt(dd2);
+    const double ratio = s.rel_d / fmax(s.rel_p, 1e-300);
+    if (s.sigma_on) {
+        if (s.sigma_adapt) {
+            const double axd = sqrt(axd2);
+            const double dxm = s.lambda_param * pd * pd - axd * axd;
+            if (dd > 1e-16 && dd < 1e12 && dxm > 1e-24 && dxm < 1e24 && isfinite(s.sigma) && s.sigma > 1e-16 &&
+                ratio > 1e-8 && ratio < 1e8) {
+                double err = log(fmax(dd, 1e-300)) - 0.5 * log(fmax(dxm, 1e-300)) - log(fmax(s.sigma, 1e-300));
+                double bal = 0.5 * log(fmax(ratio, 1e-300));
+                bal = fmax(-2.0, fmin(bal, 2.0));
+                err += p.s_gain * bal;
+                s.sigma_esum = p.s_ismooth * s.sigma_esum + err;
+                const double de = err - s.sigma_last;
+                double sr = exp(p.s_kp * err + p.s_ki * s.sigma_esum + p.s_kd * de);
+                sr = fmin(fmax(sr, p.s_umin), p.s_umax);
+                s.sigma *= sr;
+                s.sigma_last = err;
+            } else {
+                s.sigma = s.sigma_best;
+                s.sigma_esum = 0.0;
+                s.sigma_last = 0.0;
+            }
+        }
+        if (!isfinite(s.sigma) || s.sigma <= 1e-16) {
+            s.sigma = s.sigma_best;
+            s.sigma_esum = 0.0;
+            s.sigma_last = 0.0;
+        }
+        s.sigma = fmin(fmax(s.sigma, s.sigma_min), s.sigma_max);
+        const double g = fabs(log10(fmax(s.rel_d, 1e-300) / fmax(s.rel_p, 1e-300)));
+        if (isfinite(g) && g < s.best_gap) {
+            s.best_gap = g;
+            s.sigma_best = s.sigma;
+        }
+        s.pw_esum = 0.0;
+        s.pw_last = 0.0;
+    } else {
+        if (pd > 1e-16 && dd > 1e-16 && pd < 1e12 && dd < 1e12 && ratio > 1e-8 && ratio < 1e8) {
+            const double err = log(dd) - log(pd) - log(s.pw);
+            s.pw_esum *= p.ismooth;
+            s.pw_esum += err;
+            const double de = err - s.pw_last;
+            s.pw *= exp(p.kp * err + p.ki * s.pw_esum + p.kd * de);
+            s.pw_last = err;
+        } else {
+            s.pw = s.best_pw;
+            s.pw_esum = 0.0;
+            s.pw_last = 0.0;
+        }
+        const double g = fabs(log10(fmax(s.rel_d, 1e-300) / fmax(s.rel_p, 1e-300)));
+        if (g < s.best_gap) {
+            s.best_gap = g;
+            s.best_pw = s.pw;
+        }
+    }
+    cpal_refresh_step_schedule(s, p);
+    s.inner = 0;
+    s.fp_last = INFINITY;
+    s.restarts++;
+}
+
+/*
+ * Everything the reference does between two graph launches
+ * (LP/CP_AL/src/solver.cu:1343-1697 with the default controllers off):
+ * fixed-point error, KKT, counters, termination, restart decision, restart.
+ * Returns true when the solve has terminated (s.status set).
+ */
+PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval &e) {
+    s.fp = cpal_fixed_point_error(s, e.dx2, e.dy2, e.adx2, e.cross);
+    cpal_residual_scalars(s, p, e);
+    s.inner += p.F;
+    s.total += p.F;
+    s.restart = 0;
+    /* LP/CP_AL/src/utils.cu:299-317 */
+    if (s.rel_d < p.eps_feas && s.rel_p < p.eps_feas && s.rel_gap < p.eps_opt) {
+        s.status = 1; /* TERMINATION_REASON_OPTIMAL */
+        return true;
+    }
+    if (s.total >= p.iteration_limit) {
+        s.status = 6; /* TERMINATION_REASON_ITERATION_LIMIT */
+        return true;
+    }
+    if (s.fp32_switch_tol > 0.0 && fmax(s.rel_p, fmax(s.rel_d, s.rel_gap)) < s.fp32_switch_tol) s.phase_switch = 1;
+    if (s.elapsed >= p.time_limit) {
+        s.status = 5; /* TERMINATION_REASON_TIME_LIMIT */
+        return true;
+    }
+    if (cpal_should_restart(s, p)) {
+        cpal_restart_scalars(s, p, e.ddx2, e.ddy2, e.axd2);
+        s.restart = 1;
+        /* the reference recomputes the fixed-point error of the unchanged
+         * iterates with the new coefficients at the start of the next block
+         * (solver.cu:1279-1284) */
+        s.fp0 = cpal_fixed_point_error(s, e.dx2, e.dy2, e.adx2, e.cross);
+    }
+    cpal_set_coefficients(s);
+    return false;
+}
+
+} // namespace pdal

@@ -1,0 +1,747 @@
+/*
+ * cpal_kernels.cuh -- device kernels of the CP_AL (LP) solver.
+ *
+ * One iteration is two launches, each streaming one matrix once:
+ *   k_primal  rows of A^T:  q = A^T u  ->  projected primal step, reflection,
+ *             Halpern averaging (LP/CP_AL/src/solver.cu:2340-2397, 2561-2606)
+ *   k_dual    rows of A:    p = A xbar ->  dual step, reflection, Halpern
+ *             averaging (solver.cu:2399-2457, 2617-2661), and, when the
+ *             augmentation beta > 0, the next iteration's predictor
+ *             u = y - beta (Ax - P(Ax - y/beta)) (solver.cu:2459-2479).
+ * The predictor needs A x for the *next* x.  Since
+ *   x+ = w (r xbar + (1-r) x) + (1-w) x0,
+ * A x+ = w (r A xbar + (1-r) A x) + (1-w) A x0 is formed from the product the
+ * dual kernel already holds and the anchor product A x0 (recomputed exactly at
+ * every restart).  This removes the reference's third matrix stream per
+ * iteration (solver.cu:2528-2554).
+ *
+ * Every evaluation block ends with
+ *   k_eval_rows / k_eval_cols  the KKT, gap and fixed-point reductions
+ *             (utils.cu:812-917, solver.cu:3611-3686) as fused products over
+ *             the FP64 matrices,
+ *   k_control the scalar controller (cpal_control.h), one block,
+ *   k_restart the anchor reset of a restart (solver.cu:3078-3095).
+ *
+ * T is the arithmetic type of the iteration (double, or float in the FP32
+ * phase).  Anchors x0, y0, A x0 and every reduction stay in FP64.
+ */
+#pragma once
+
+#include "cpal_control.h"
+#include "rowblock.cuh"
+
+namespace pdal {
+
+template <typename T>
+__device__ __forceinline__ T vmax(T a, T b) {
+    return fmax(a, b);
+}
+template <>
+__device__ __forceinline__ float vmax<float>(float a, float b) {
+    return fmaxf(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T vmin(T a, T b) {
+    return fmin(a, b);
+}
+template <>
+__device__ __forceinline__ float vmin<float>(float a, float b) {
+    return fminf(a, b);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+struct NoLongRed {
+    __device__ __forceinline__ void long_red(int, Red<0, 0> &) const {}
+};
+
+/* ------------------------------------------------------------------ */
+/* iteration                                                           */
+/* ------------------------------------------------------------------ */
+template <typename T>
+struct PrimalArgs {
+    T *x, *xbar, *xh, *lam;
+    const double *x0;
+    const T *c, *lb, *ub;
+};
+
+template <typename T, bool MAJOR>
+struct PrimalEpi : NoLongRed {
+    PrimalArgs<T> a;
+    T tau, inv_tau, r;
+    double w;
+    __device__ __forceinline__ void operator()(int j, const T *s, Red<0, 0> &) const {
+        const T xj = a.x[j];
+        const T t = xj - tau * (a.c[j] - s[0]);
+        const T proj = vmax(a.lb[j], vmin(t, a.ub[j]));
+        const T xb = T(2) * proj - xj;
+        a.xbar[j] = xb;
+        if (MAJOR) {
+            a.xh[j] = proj;
+            a.lam[j] = (proj - t) * inv_tau;
+        }
+        const T refl = r * xb + (T(1) - r) * xj;
+        a.x[j] = (T)(w * (double)refl + (1.0 - w) * a.x0[j]);
+    }
+};
+
+template <typename T, int S, bool MAJOR>
+__global__ void __launch_bounds__(kThreads) k_primal(RowPlanDev plan, const int *__restrict__ rp,
+                                                     const int *__restrict__ ci, const T *__restrict__ val,
+                                                     const T *__restrict__ gat, PrimalArgs<T> a,
+                                                     const CpalState *__restrict__ st, int koff) {
+    if (st->status) return;
+    __shared__ RowBlockSmem<S, 1, T> sm;
+    PrimalEpi<T, MAJOR> epi;
+    epi.a = a;
+    epi.tau = (T)st->tau;
+    epi.inv_tau = (T)st->inv_tau;
+    epi.r = (T)st->refl;
+    const int k = st->inner + koff;
+    epi.w = (double)k / (double)(k + 1);
+    auto prod = [&](int kk, T *out) { out[0] = val[kk] * gat[ci[kk]]; };
+    Red<0, 0> red;
+    rowblock_run<S, 1, T>(plan, rp, prod, epi, red, sm);
+}
+
+template <typename T>
+struct DualArgs {
+    T *y, *yh, *ybar, *ax, *u;
+    const double *y0, *ax0;
+    const T *lb, *ub;
+};
+
+template <typename T, bool MAJOR, bool BETA>
+struct DualEpi : NoLongRed {
+    DualArgs<T> a;
+    T rho, inv_prox, beta, inv_beta, r;
+    double w;
+    __device__ __forceinline__ void operator()(int i, const T *s, Red<0, 0> &) const {
+        const T yi = a.y[i];
+        const T p = s[0];
+        const T lo = a.lb[i], hi = a.ub[i];
+        const T zb = vmax(lo, vmin(p - yi * inv_prox, hi));
+        const T yn = yi - rho * (p - zb);
+        const T yb = T(2) * yn - yi;
+        if (MAJOR) {
+            a.yh[i] = yn;
+            a.ybar[i] = yb;
+        }
+        const T refl = r * yb + (T(1) - r) * yi;
+        const T ynew = (T)(w * (double)refl + (1.0 - w) * a.y0[i]);
+        a.y[i] = ynew;
+        if (BETA) {
+            T mix = p;
+            if (r != T(1)) mix = r * p + (T(1) - r) * a.ax[i];
+            const T axn = (T)(w * (double)mix + (1.0 - w) * a.ax0[i]);
+            a.ax[i] = axn;
+            const T z2 = vmax(lo, vmin(axn - ynew * inv_beta, hi));
+            a.u[i] = ynew - beta * (axn - z2);
+        }
+    }
+};
+
+template <typename T, int S, bool MAJOR, bool BETA>
+__global__ void __launch_bounds__(kThreads) k_dual(RowPlanDev plan, const int *__restrict__ rp,
+                                                   const int *__restrict__ ci, const T *__restrict__ val,
+                                                   const T *__restrict__ xbar, DualArgs<T> a,
+                                                   const CpalState *__restrict__ st, int koff) {
+    if (st->status) return;
+    __shared__ RowBlockSmem<S, 1, T> sm;
+    DualEpi<T, MAJOR, BETA> epi;
+    epi.a = a;
+    epi.rho = (T)st->rho;
+    epi.inv_prox = (T)st->inv_prox;
+    epi.beta = (T)st->beta;
+    epi.inv_beta = (T)st->inv_beta;
+    epi.r = (T)st->refl;
+    const int k = st->inner + koff;
+    epi.w = (double)k / (double)(k + 1);
+    auto prod = [&](int kk, T *out) { out[0] = val[kk] * xbar[ci[kk]]; };
+    Red<0, 0> red;
+    rowblock_run<S, 1, T>(plan, rp, prod, epi, red, sm);
+}
+
+/* A x0 at the start of a solve (or of a precision phase), with the first
+ * predictor u = y - beta (A x - P(A x - y/beta)). */
+template <typename T, bool BETA>
+struct InitAxEpi : NoLongRed {
+    T *ax, *u;
+    double *ax0;
+    const T *y, *lb, *ub;
+    T beta, inv_beta;
+    __device__ __forceinline__ void operator()(int i, const double *s, Red<0, 0> &) const {
+        ax0[i] = s[0];
+        const T axv = (T)s[0];
+        ax[i] = axv;
+        if (BETA) {
+            const T yi = y[i];
+            const T z = vmax(lb[i], vmin(axv - yi * inv_beta, ub[i]));
+            u[i] = yi - beta * (axv - z);
+        }
+    }
+};
+
+template <typename T, int S, bool BETA>
+__global__ void __launch_bounds__(kThreads) k_init_ax(RowPlanDev plan, const int *__restrict__ rp,
+                                                      const int *__restrict__ ci, const double *__restrict__ val,
+                                                      const double *__restrict__ x0, T *ax, double *ax0, T *u,
+                                                      const T *y, const T *lb, const T *ub,
+                                                      const CpalState *__restrict__ st) {
+    __shared__ RowBlockSmem<S, 1, double> sm;
+    InitAxEpi<T, BETA> epi;
+    epi.ax = ax;
+    epi.u = u;
+    epi.ax0 = ax0;
+    epi.y = y;
+    epi.lb = lb;
+    epi.ub = ub;
+    epi.beta = (T)st->beta;
+    epi.inv_beta = (T)st->inv_beta;
+    auto prod = [&](int kk, double *out) { out[0] = val[kk] * x0[ci[kk]]; };
+    Red<0, 0> red;
+    rowblock_run<S, 1, double>(plan, rp, prod, epi, red, sm);
+}
+
+/* ------------------------------------------------------------------ */
+/* evaluation                                                          */
+/* ------------------------------------------------------------------ */
+constexpr int kEvalStride = 8; /* doubles per partial slot */
+
+/* rows of A: p^ = A x^, A dx, A (x^ - x0); primal residual, dual-objective
+ * contribution, |A dx|^2, |dy|^2, |y^ - y0|^2, |A(x^ - x0)|^2. */
+template <typename T>
+struct EvalRowArgs {
+    const T *xh, *xbar, *yh, *ybar;
+    const double *x0, *y0, *ax0, *clb, *cub, *clb_fin, *cub_fin, *rscale;
+    double *phat;
+    double *part; /* (nblocks + nlong) * kEvalStride */
+    int nblocks;
+};
+
+template <typename T>
+struct EvalRowEpi {
+    EvalRowArgs<T> a;
+    __device__ __forceinline__ void operator()(int i, const double *s, Red<6, 1> &r) const {
+        const double ph = s[0];
+        a.phat[i] = ph;
+        const double cl = fmax(a.clb[i], fmin(ph, a.cub[i]));
+        const double rpv = (ph - cl) * a.rscale[i];
+        r.s[0] += rpv * rpv;
+        r.mx[0] = fmax(r.mx[0], fabs(rpv));
+        const double yhi = (double)a.yh[i];
+        r.s[1] += fmax(yhi, 0.0) * a.clb_fin[i] + fmin(yhi, 0.0) * a.cub_fin[i];
+        r.s[2] += s[1] * s[1];
+        const double dyv = (double)a.ybar[i] - yhi;
+        r.s[3] += dyv * dyv;
+        const double ddy = yhi - a.y0[i];
+        r.s[4] += ddy * ddy;
+        r.s[5] += s[2] * s[2];
+    }
+    __device__ __forceinline__ void long_red(int lid, Red<6, 1> &r) const {
+        double *d = a.part + (size_t)(a.nblocks + lid) * kEvalStride;
+        for (int q = 0; q < 6; ++q) d[q] = r.s[q];
+        d[6] = r.mx[0];
+    }
+};
+
+template <typename T, int S>
+__global__ void __launch_bounds__(kThreads) k_eval_rows(RowPlanDev plan, const int *__restrict__ rp,
+                                                        const int *__restrict__ ci, const double *__restrict__ val,
+                                                        EvalRowArgs<T> a, const CpalState *__restrict__ st) {
+    if (st->status) return;
+    __shared__ RowBlockSmem<S, 3, double> sm;
+    EvalRowEpi<T> epi;
+    epi.a = a;
+    const T *xh = a.xh;
+    const T *xb = a.xbar;
+    const double *x0 = a.x0;
+    auto prod = [&](int kk, double *out) {
+        const double v = val[kk];
+        const int c = ci[kk];
+        const double xhc = (double)xh[c];
+        out[0] = v * xhc;
+        out[1] = v * ((double)xb[c] - xhc);
+        out[2] = v * (xhc - x0[c]);
+    };
+    Red<6, 1> red;
+    red.zero();
+    rowblock_run<S, 3, double>(plan, rp, prod, epi, red, sm);
+    block_reduce<kThreads, 6, 1>(red, sm.red);
+    if (threadIdx.x == 0) {
+        double *d = a.part + (size_t)blockIdx.x * kEvalStride;
+        for (int q = 0; q < 6; ++q) d[q] = red.s[q];
+        d[6] = red.mx[0];
+    }
+}
+
+/* rows of A^T: q^ = A^T y^, A^T dy; dual residual, |dx|^2, <A^T dy, dx>,
+ * c'x^, lambda'x^, |x^ - x0|^2. */
+template <typename T>
+struct EvalColArgs {
+    const T *xh, *xbar, *yh, *ybar, *lam;
+    const double *x0, *c, *cscale;
+    double *part;
+    int nblocks;
+};
+
+template <typename T>
+struct EvalColEpi {
+    EvalColArgs<T> a;
+    __device__ __forceinline__ void operator()(int j, const double *s, Red<6, 1> &r) const {
+        const double xhj = (double)a.xh[j];
+        const double lj = (double)a.lam[j];
+        const double cj = a.c[j];
+        const double rdv = (cj - s[0] - lj) * a.cscale[j];
+        r.s[0] += rdv * rdv;
+        r.mx[0] = fmax(r.mx[0], fabs(rdv));
+        const double dxv = (double)a.xbar[j] - xhj;
+        r.s[1] += dxv * dxv;
+        r.s[2] += s[1] * dxv;
+        r.s[3] += cj * xhj;
+        r.s[4] += lj * xhj;
+        const double ddx = xhj - a.x0[j];
+        r.s[5] += ddx * ddx;
+    }
+    __device__ __forceinline__ void long_red(int lid, Red<6, 1> &r) const {
+        double *d = a.part + (size_t)(a.nblocks + lid) * kEvalStride;
+        for (int q = 0; q < 6; ++q) d[q] = r.s[q];
+        d[6] = r.mx[0];
+    }
+};
+
+template <typename T, int S>
+__global__ void __launch_bounds__(kThreads) k_eval_cols(RowPlanDev plan, const int *__restrict__ rp,
+                                                        const int *__restrict__ ci, const double *__restrict__ val,
+                                                        EvalColArgs<T> a, const CpalState *__restrict__ st) {
+    if (st->status) return;
+    __shared__ RowBlockSmem<S, 2, double> sm;
+    EvalColEpi<T> epi;
+    epi.a = a;
+    const T *yh = a.yh;
+    const T *yb = a.ybar;
+    auto prod = [&](int kk, double *out) {
+        const double v = val[kk];
+        const int c = ci[kk];
+        const double yhc = (double)yh[c];
+        out[0] = v * yhc;
+        out[1] = v * ((double)yb[c] - yhc);
+    };
+    Red<6, 1> red;
+    red.zero();
+    rowblock_run<S, 2, double>(plan, rp, prod, epi, red, sm);
+    block_reduce<kThreads, 6, 1>(red, sm.red);
+    if (threadIdx.x == 0) {
+        double *d = a.part + (size_t)blockIdx.x * kEvalStride;
+        for (int q = 0; q < 6; ++q) d[q] = red.s[q];
+        d[6] = red.mx[0];
+    }
+}
+
+/* Sums the partial slots of one evaluation kernel in a fixed order. */
+__device__ __forceinline__ void reduce_slots(const double *part, int nslots, Red<6, 1> &r, double *sbuf) {
+    r.zero();
+    for (int b = threadIdx.x; b < nslots; b += kThreads) {
+        const double *d = part + (size_t)b * kEvalStride;
+        for (int q = 0; q < 6; ++q) r.s[q] += d[q];
+        r.mx[0] = fmax(r.mx[0], d[6]);
+    }
+    block_reduce<kThreads, 6, 1>(r, sbuf);
+}
+
+__global__ void __launch_bounds__(kThreads) k_control(const double *__restrict__ prow, int nrow_slots,
+                                                      const double *__restrict__ pcol, int ncol_slots,
+                                                      CpalState *st, CpalParams p) {
+    if (st->status) return;
+    __shared__ double sbuf[8 * (kThreads / 32)];
+    Red<6, 1> r1, r2;
+    reduce_slots(prow, nrow_slots, r1, sbuf);
+    reduce_slots(pcol, ncol_slots, r2, sbuf);
+    if (threadIdx.x == 0) {
+        CpalEval e;
+        e.rp2 = r1.s[0];
+        e.contrib = r1.s[1];
+        e.adx2 = r1.s[2];
+        e.dy2 = r1.s[3];
+        e.ddy2 = r1.s[4];
+        e.axd2 = r1.s[5];
+        e.rpmax = r1.mx[0];
+        e.rd2 = r2.s[0];
+        e.dx2 = r2.s[1];
+        e.cross = r2.s[2];
+        e.cx = r2.s[3];
+        e.lx = r2.s[4];
+        e.ddx2 = r2.s[5];
+        e.rdmax = r2.mx[0];
+        CpalState s = *st;
+        s.elapsed = (double)(globaltimer_ns() - s.t_start_ns) * 1e-9;
+        cpal_end_of_block(s, p, e);
+        *st = s;
+    }
+}
+
+/* Anchor reset after a restart: x0 = x = x^, y0 = y = y^, A x0 = A x = p^,
+ * and the next predictor from the new beta. */
+template <typename T, bool BETA>
+__global__ void k_restart(const CpalState *__restrict__ st, int n, int m, const T *__restrict__ xh, T *x,
+                          double *x0, const T *__restrict__ yh, T *y, double *y0, const double *__restrict__ phat,
+                          T *ax, double *ax0, T *u, const T *__restrict__ lb, const T *__restrict__ ub) {
+    if (st->status || !st->restart) return;
+    const T beta = (T)st->beta, inv_beta = (T)st->inv_beta;
+    const int total = n > m ? n : m;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        if (t < n) {
+            const T v = xh[t];
+            x[t] = v;
+            x0[t] = (double)v;
+        }
+        if (t < m) {
+            const T v = yh[t];
+            y[t] = v;
+            y0[t] = (double)v;
+            const double ph = phat[t];
+            ax0[t] = ph;
+            const T axv = (T)ph;
+            ax[t] = axv;
+            if (BETA) {
+                const T z = vmax(lb[t], vmin(axv - v * inv_beta, ub[t]));
+                u[t] = v - beta * (axv - z);
+            }
+        }
+    }
+}
+
+__global__ void k_start_clock(CpalState *st) { st->t_start_ns = globaltimer_ns(); }
+
+/* ------------------------------------------------------------------ */
+/* result (LP/CP_AL/src/solver.cu:1768-1793, 2481-2500)                 */
+/* ------------------------------------------------------------------ */
+struct ResultColEpi : NoLongRed {
+    const double *xh, *c, *cscale, *vlb, *vub;
+    const CpalState *st;
+    double *x_out, *rc_out;
+    __device__ __forceinline__ void operator()(int j, const double *s, Red<0, 0> &) const {
+        double rc = (c[j] - s[0]) * cscale[j] / st->ovr;
+        if (!isfinite(vlb[j])) rc = fmin(rc, 0.0);
+        if (!isfinite(vub[j])) rc = fmax(rc, 0.0);
+        rc_out[j] = rc;
+        x_out[j] = xh[j] / cscale[j] / st->cbr;
+    }
+};
+
+template <int S>
+__global__ void __launch_bounds__(kThreads) k_result_cols(RowPlanDev plan, const int *__restrict__ rp,
+                                                          const int *__restrict__ ci, const double *__restrict__ val,
+                                                          const double *__restrict__ yh, ResultColEpi epi) {
+    __shared__ RowBlockSmem<S, 1, double> sm;
+    auto prod = [&](int kk, double *out) { out[0] = val[kk] * yh[ci[kk]]; };
+    Red<0, 0> red;
+    rowblock_run<S, 1, double>(plan, rp, prod, epi, red, sm);
+}
+
+__global__ void k_result_rows(int m, const double *__restrict__ yh, const double *__restrict__ rscale,
+                              const CpalState *__restrict__ st, double *y_out) {
+    const double ovr = st->ovr;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+        y_out[i] = yh[i] / rscale[i] / ovr;
+}
+
+/* Promotes / demotes a vector between the FP32 phase and FP64. */
+template <typename A, typename B>
+__global__ void k_convert(const A *__restrict__ src, B *dst, int len) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) dst[i] = (B)src[i];
+}
+
+/* ------------------------------------------------------------------ */
+/* setup: equilibration (LP/CP_AL/src/preconditioner.cu)               */
+/* ------------------------------------------------------------------ */
+
+/* warp per row: s = clamp_sqrt(max |a| or sum |a|^deg), cum *= s
+ * (preconditioner.cu:532-550, 634-667). mode 0 = abs max, 1 = power sum. */
+__global__ void k_row_scale(int nr, const int *__restrict__ rp, const double *__restrict__ val, int mode, double deg,
+                            double *scale, double *cum) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nr; row += warps) {
+        double acc = 0.0;
+        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+            double v = fabs(val[k]);
+            if (!isfinite(v)) v = 0.0;
+            if (mode == 0) {
+                acc = fmax(acc, v);
+            } else {
+                double pv;
+                if (deg == 2.0)
+                    pv = v * v;
+                else if (deg == 1.0)
+                    pv = v;
+                else if (deg == 0.5)
+                    pv = sqrt(v);
+                else
+                    pv = pow(v, deg);
+                acc += pv;
+            }
+        }
+        if (mode == 0)
+            acc = warp_max(acc);
+        else
+            acc = warp_sum(acc);
+        if (lane == 0) {
+            const double s = (acc < 1e-12) ? 1.0 : sqrt(acc);
+            cum[row] *= s;
+            scale[row] = s;
+        }
+    }
+}
+
+/* A values *= (1/d[j]) * (1/r[i]); rows of this matrix are scaled by
+ * row_is_var ? d : r (preconditioner.cu:514-530). */
+__global__ void k_scale_matrix(int nr, const int *__restrict__ rp, const int *__restrict__ ci, double *val,
+                               const double *__restrict__ rowscale, const double *__restrict__ colscale,
+                               int row_is_var) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nr; row += warps) {
+        const double inv_row = 1.0 / rowscale[row];
+        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+            const double inv_col = 1.0 / colscale[ci[k]];
+            val[k] *= row_is_var ? inv_row * inv_col : inv_col * inv_row;
+        }
+    }
+}
+
+/* preconditioner.cu:476-512 */
+__global__ void k_scale_vectors(int n, int m, const double *__restrict__ d, const double *__restrict__ r, double *c,
+                                double *vlb, double *vub, double *x0, double *clb, double *cub, double *y0) {
+    const int total = n > m ? n : m;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        if (t < n) {
+            const double dj = d[t], inv = 1.0 / d[t];
+            c[t] *= inv;
+            vlb[t] *= dj;
+            vub[t] *= dj;
+            x0[t] *= dj;
+        }
+        if (t < m) {
+            const double inv = 1.0 / r[t], ei = r[t];
+            clb[t] *= inv;
+            cub[t] *= inv;
+            y0[t] *= ei;
+        }
+    }
+}
+
+/* bound/objective norms (preconditioner.cu:329-377, 669-691): partial sums of
+ * the bound contributions and of c^2 per block. */
+__global__ void __launch_bounds__(kThreads) k_boundobj_partials(int n, int m, const double *__restrict__ clb,
+                                                                const double *__restrict__ cub,
+                                                                const double *__restrict__ c, double *part) {
+    __shared__ double sbuf[2 * (kThreads / 32)];
+    Red<2, 0> r;
+    r.zero();
+    const int total = n > m ? n : m;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        if (t < m) {
+            const double L = clb[t], U = cub[t];
+            const bool fL = isfinite(L), fU = isfinite(U);
+            double acc = 0.0;
+            if (fL && (!fU || fabs(L - U) > 1e-12)) acc += L * L;
+            if (fU) acc += U * U;
+            r.s[0] += acc;
+        }
+        if (t < n) r.s[1] += c[t] * c[t];
+    }
+    block_reduce<kThreads, 2, 0>(r, sbuf);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x * 2 + 0] = r.s[0];
+        part[blockIdx.x * 2 + 1] = r.s[1];
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_boundobj_finish(const double *__restrict__ part, int nparts,
+                                                              CpalState *st, int enabled) {
+    __shared__ double sbuf[2 * (kThreads / 32)];
+    Red<2, 0> r;
+    r.zero();
+    for (int b = threadIdx.x; b < nparts; b += kThreads) {
+        r.s[0] += part[b * 2];
+        r.s[1] += part[b * 2 + 1];
+    }
+    block_reduce<kThreads, 2, 0>(r, sbuf);
+    if (threadIdx.x == 0) {
+        if (enabled) {
+            st->cbr = 1.0 / (sqrt(r.s[0]) + 1.0);
+            st->ovr = 1.0 / (sqrt(r.s[1]) + 1.0);
+        } else {
+            st->cbr = 1.0;
+            st->ovr = 1.0;
+        }
+    }
+}
+
+__global__ void k_scale_boundobj(int n, int m, const CpalState *__restrict__ st, double *c, double *vlb, double *vub,
+                                 double *x0, double *clb, double *cub, double *y0) {
+    const double cs = st->cbr, os = st->ovr;
+    const int total = n > m ? n : m;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        if (t < m) {
+            clb[t] *= cs;
+            cub[t] *= cs;
+            y0[t] *= os;
+        }
+        if (t < n) {
+            vlb[t] *= cs;
+            vub[t] *= cs;
+            c[t] *= os;
+            x0[t] *= cs;
+        }
+    }
+}
+
+/* finite-bound copies (LP/CP_AL/src/solver.cu:2323-2338) */
+__global__ void k_finite_bounds(int m, const double *__restrict__ lb, const double *__restrict__ ub, double *lbf,
+                                double *ubf) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        lbf[i] = isfinite(lb[i]) ? lb[i] : 0.0;
+        ubf[i] = isfinite(ub[i]) ? ub[i] : 0.0;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* setup: power iteration on A A^T (LP/CP_AL/src/utils.cu:87-228)      */
+/* ------------------------------------------------------------------ */
+struct PowerState {
+    double inv;  /* 1/|v| of the current vector */
+    double s2;   /* Rayleigh quotient, sigma_max^2 estimate */
+    double res;  /* residual norm */
+    int done;    /* converged or out of iterations */
+    int iters;
+    int max_iter;
+    double tol;
+};
+
+struct PowerColEpi : NoLongRed {
+    double *dp;
+    __device__ __forceinline__ void operator()(int j, const double *s, Red<0, 0> &) const { dp[j] = s[0]; }
+};
+
+/* dp = A^T (inv * v) */
+template <int S>
+__global__ void __launch_bounds__(kThreads) k_power_at(RowPlanDev plan, const int *__restrict__ rp,
+                                                       const int *__restrict__ ci, const double *__restrict__ val,
+                                                       const double *__restrict__ v, double *dp,
+                                                       const PowerState *__restrict__ ps) {
+    if (ps->done) return;
+    __shared__ RowBlockSmem<S, 1, double> sm;
+    const double inv = ps->inv;
+    PowerColEpi epi;
+    epi.dp = dp;
+    auto prod = [&](int kk, double *out) { out[0] = val[kk] * (inv * v[ci[kk]]); };
+    Red<0, 0> red;
+    rowblock_run<S, 1, double>(plan, rp, prod, epi, red, sm);
+}
+
+/* vn = A dp, partial sums of (inv * v) . vn */
+struct PowerRowEpi {
+    const double *v;
+    double *vn;
+    double inv;
+    double *part;
+    int nblocks;
+    __device__ __forceinline__ void operator()(int i, const double *s, Red<1, 0> &r) const {
+        vn[i] = s[0];
+        r.s[0] += (inv * v[i]) * s[0];
+    }
+    __device__ __forceinline__ void long_red(int lid, Red<1, 0> &r) const { part[nblocks + lid] = r.s[0]; }
+};
+
+template <int S>
+__global__ void __launch_bounds__(kThreads) k_power_a(RowPlanDev plan, const int *__restrict__ rp,
+                                                      const int *__restrict__ ci, const double *__restrict__ val,
+                                                      const double *__restrict__ dp, const double *__restrict__ v,
+                                                      double *vn, double *part, const PowerState *__restrict__ ps) {
+    if (ps->done) return;
+    __shared__ RowBlockSmem<S, 1, double> sm;
+    PowerRowEpi epi;
+    epi.v = v;
+    epi.vn = vn;
+    epi.inv = ps->inv;
+    epi.part = part;
+    epi.nblocks = plan.nblocks;
+    auto prod = [&](int kk, double *out) { out[0] = val[kk] * dp[ci[kk]]; };
+    Red<1, 0> red;
+    red.zero();
+    rowblock_run<S, 1, double>(plan, rp, prod, epi, red, sm);
+    block_reduce<kThreads, 1, 0>(red, sm.red);
+    if (threadIdx.x == 0) part[blockIdx.x] = red.s[0];
+}
+
+/* s2 = sum(part) */
+__global__ void __launch_bounds__(kThreads) k_power_dot(const double *__restrict__ part, int nparts, PowerState *ps) {
+    if (ps->done) return;
+    __shared__ double sbuf[kThreads / 32];
+    Red<1, 0> r;
+    r.zero();
+    for (int b = threadIdx.x; b < nparts; b += kThreads) r.s[0] += part[b];
+    block_reduce<kThreads, 1, 0>(r, sbuf);
+    if (threadIdx.x == 0) ps->s2 = r.s[0];
+}
+
+/* residual vn - s2 * (inv v) and |vn|^2; then v <- vn */
+__global__ void __launch_bounds__(kThreads) k_power_resid(int m, double *v, const double *__restrict__ vn,
+                                                          double *part, const PowerState *__restrict__ ps) {
+    if (ps->done) return;
+    __shared__ double sbuf[2 * (kThreads / 32)];
+    const double inv = ps->inv, s2 = ps->s2;
+    Red<2, 0> r;
+    r.zero();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const double nv = inv * v[i];
+        const double vni = vn[i];
+        const double q = (-s2 * nv) + vni;
+        r.s[0] += q * q;
+        r.s[1] += vni * vni;
+        v[i] = vni;
+    }
+    block_reduce<kThreads, 2, 0>(r, sbuf);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x * 2] = r.s[0];
+        part[blockIdx.x * 2 + 1] = r.s[1];
+    }
+}
+
+/* residual test and the normalisation of the next vector */
+__global__ void __launch_bounds__(kThreads) k_power_check(const double *__restrict__ part, int nparts,
+                                                          PowerState *ps) {
+    if (ps->done) return;
+    __shared__ double sbuf[2 * (kThreads / 32)];
+    Red<2, 0> r;
+    r.zero();
+    for (int b = threadIdx.x; b < nparts; b += kThreads) {
+        r.s[0] += part[b * 2];
+        r.s[1] += part[b * 2 + 1];
+    }
+    block_reduce<kThreads, 2, 0>(r, sbuf);
+    if (threadIdx.x == 0) {
+        ps->iters += 1;
+        ps->res = sqrt(r.s[0]);
+        ps->inv = 1.0 / sqrt(r.s[1]);
+        if (ps->res < ps->tol || ps->iters >= ps->max_iter) ps->done = 1;
+    }
+}
+
+/* 1/|v| of the start vector */
+__global__ void __launch_bounds__(kThreads) k_power_start(int m, const double *__restrict__ v, PowerState *ps) {
+    __shared__ double sbuf[kThreads / 32];
+    Red<1, 0> r;
+    r.zero();
+    for (int i = threadIdx.x; i < m; i += kThreads) r.s[0] += v[i] * v[i];
+    block_reduce<kThreads, 1, 0>(r, sbuf);
+    if (threadIdx.x == 0) ps->inv = 1.0 / sqrt(r.s[0]);
+}
+
+} // namespace pdal

@@ -1,0 +1,1083 @@
+/*
+ * cpal_solver.cu -- host driver of the CP_AL (LP) solver on one GPU.
+ *
+ * Control flow follows optimize() of the reference (LP/CP_AL/src/solver.cu:
+ * 1175-1736): equilibrate, estimate sigma_max(A)^2, then repeat evaluation
+ * blocks of F iterations until the KKT test passes.  Differences in form:
+ *   - a block (F iterations + evaluation + controller + restart) is one CUDA
+ *     graph; the host reads back one small struct per block and never
+ *     synchronises inside it (the reference synchronises ~10 times per block);
+ *   - every product is a fused row-block kernel (rowblock.cuh), no cuSPARSE,
+ *     cuBLAS or CUB;
+ *   - FP32_REFINE runs the iteration in FP32 (FP64 anchors and reductions)
+ *     until the KKT error falls below fp32_switch_tol, then continues in FP64
+ *     from the FP32 iterate.
+ */
+#include "../../include/cp_al.h"
+#include "../../include/cp_al_gb300.h"
+#include "common.h"
+#include "cpal_kernels.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <random>
+
+namespace pdal {
+
+namespace {
+
+thread_local cp_al_gb300_stats_t g_stats;
+
+double now_sec() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+int grid_for(long long len, int per_block = kThreads) {
+    long long g = (len + per_block - 1) / per_block;
+    if (g < 1) g = 1;
+    if (g > 152 * 8) g = 152 * 8;
+    return (int)g;
+}
+
+#define PDAL_LAUNCH_CHECK() PDAL_CUDA(cudaGetLastError())
+
+/* Dispatch on the row-block nonzero budget. */
+#define PDAL_WITH_S(Sval, ...)                     \
+    switch (Sval) {                                 \
+    case 256: {                                     \
+        constexpr int SB = 256;                     \
+        __VA_ARGS__;                                \
+    } break;                                        \
+    case 512: {                                     \
+        constexpr int SB = 512;                     \
+        __VA_ARGS__;                                \
+    } break;                                        \
+    case 1024: {                                    \
+        constexpr int SB = 1024;                    \
+        __VA_ARGS__;                                \
+    } break;                                        \
+    case 2048: {                                    \
+        constexpr int SB = 2048;                    \
+        __VA_ARGS__;                                \
+    } break;                                        \
+    default:                                        \
+        throw Error("unsupported row-block budget"); \
+    }
+
+#define PDAL_WITH_SE(Sval, ...)                    \
+    switch (Sval) {                                 \
+    case 256: {                                     \
+        constexpr int SE = 256;                     \
+        __VA_ARGS__;                                \
+    } break;                                        \
+    case 512: {                                     \
+        constexpr int SE = 512;                     \
+        __VA_ARGS__;                                \
+    } break;                                        \
+    case 1024: {                                    \
+        constexpr int SE = 1024;                    \
+        __VA_ARGS__;                                \
+    } break;                                        \
+    default:                                        \
+        throw Error("unsupported row-block budget"); \
+    }
+
+struct PlanDev {
+    HostPlan hp;
+    RowPlanDev d{};
+};
+
+struct DevMatrix {
+    int nr = 0, nc = 0, nnz = 0;
+    int *rp = nullptr, *ci = nullptr;
+    double *v = nullptr;
+    float *vf = nullptr;
+    PlanDev it, ev;
+};
+
+template <typename T>
+struct IterVecs {
+    /* n */
+    T *x = nullptr, *xbar = nullptr, *xh = nullptr, *lam = nullptr, *c = nullptr, *vlb = nullptr, *vub = nullptr;
+    /* m */
+    T *y = nullptr, *yh = nullptr, *ybar = nullptr, *ax = nullptr, *u = nullptr, *clb = nullptr, *cub = nullptr;
+};
+
+} // namespace
+
+class CpalSolver {
+  public:
+    CpalSolver(const lp_problem_t *prob, const cp_al_parameters_t *params, const cp_al_gb300_options_t *opts)
+        : prob_(prob), P_(*params), O_(*opts) {}
+    ~CpalSolver() { release(); }
+
+    /* host-side preparation that needs no device work */
+    void prepare();
+    /* allocate + upload the pristine problem */
+    void upload();
+    /* reset working buffers from the pristine copy, then equilibrate, power
+     * iteration and initial schedule */
+    void setup_device();
+    void run_loop();
+    void download(cp_al_result_t *res, bool vectors);
+    void result_on_device();
+    void fetch_vectors(double *x, double *y, double *rc);
+
+    CpalState host_state{};
+    double setup_sec = 0, loop_sec = 0;
+    int64_t launches = 0;
+    int64_t h2d = 0, d2h = 0;
+    int power_iters = 0;
+    int fp32_iters = 0;
+    double sum_ms[2][3] = {{0, 0, 0}, {0, 0, 0}}; /* [fp64, fp32][primal, dual, block] */
+    int timed[2] = {0, 0};
+
+  private:
+    void release();
+    template <typename T>
+    void capture_block(cudaGraphExec_t &exec);
+    template <typename T>
+    void launch_iteration(int koff, bool major);
+    template <typename T>
+    void launch_primal(int koff, bool major);
+    template <typename T>
+    void launch_dual(int koff, bool major);
+    template <typename T>
+    void launch_eval();
+    template <typename T>
+    void launch_init_ax();
+    template <typename T>
+    IterVecs<T> &vecs();
+    void power_iteration();
+    void switch_to_fp64();
+    void alloc_plan(PlanDev &pd);
+    void upload_plan(PlanDev &pd);
+    void alloc_all();
+
+    const lp_problem_t *prob_;
+    cp_al_parameters_t P_;
+    cp_al_gb300_options_t O_;
+    CpalParams cp_{};
+    int n_ = 0, m_ = 0, nnz_ = 0;
+    HostCsr At_host_;
+    int S_it_ = 2048, S_ev_ = 1024;
+    bool beta_on_ = false;
+    bool fp32_phase_ = false;
+
+    Arena arena_;
+    cudaStream_t stream_ = nullptr;
+    DevMatrix A_, At_;
+    /* pristine copies (session solves start from these) */
+    double *Av0_ = nullptr, *Atv0_ = nullptr, *c0_ = nullptr, *vlb0_ = nullptr, *vub0_ = nullptr, *clb0_ = nullptr,
+           *cub0_ = nullptr, *x00_ = nullptr, *y00_ = nullptr;
+    /* FP64 working data */
+    double *c_ = nullptr, *vlb_ = nullptr, *vub_ = nullptr, *clb_ = nullptr, *cub_ = nullptr, *clbf_ = nullptr,
+           *cubf_ = nullptr;
+    double *x0_ = nullptr, *y0_ = nullptr, *ax0_ = nullptr, *phat_ = nullptr, *dsc_ = nullptr, *rsc_ = nullptr;
+    double *tmp_n_ = nullptr, *tmp_m_ = nullptr, *tmp_m2_ = nullptr;
+    double *part_row_ = nullptr, *part_col_ = nullptr, *part_misc_ = nullptr;
+    double *xout_ = nullptr, *yout_ = nullptr, *rcout_ = nullptr;
+    IterVecs<double> v64_;
+    IterVecs<float> v32_;
+    CpalState *st_ = nullptr;
+    PowerState *ps_ = nullptr;
+    CpalState *h_st_ = nullptr; /* pinned */
+    PowerState *h_ps_ = nullptr;
+    cudaGraphExec_t exec64_ = nullptr, exec32_ = nullptr;
+    int nmisc_ = 0;
+    cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+template <>
+IterVecs<double> &CpalSolver::vecs<double>() {
+    return v64_;
+}
+template <>
+IterVecs<float> &CpalSolver::vecs<float>() {
+    return v32_;
+}
+
+void CpalSolver::release() {
+    for (auto &e : ev_)
+        if (e) cudaEventDestroy(e);
+    if (exec64_) cudaGraphExecDestroy(exec64_);
+    if (exec32_) cudaGraphExecDestroy(exec32_);
+    exec64_ = exec32_ = nullptr;
+    if (h_st_) cudaFreeHost(h_st_);
+    if (h_ps_) cudaFreeHost(h_ps_);
+    h_st_ = nullptr;
+    h_ps_ = nullptr;
+    arena_.release();
+    if (stream_) cudaStreamDestroy(stream_);
+    stream_ = nullptr;
+}
+
+void CpalSolver::prepare() {
+    n_ = prob_->num_variables;
+    m_ = prob_->num_constraints;
+    nnz_ = prob_->constraint_matrix_num_nonzeros;
+    if (n_ <= 0) throw Error("problem has no variables");
+    if (m_ < 0) throw Error("negative number of constraints");
+    if (P_.termination_evaluation_frequency < 3)
+        throw Error("termination_evaluation_frequency must be >= 3 (got " +
+                    std::to_string(P_.termination_evaluation_frequency) + ")");
+    if (!prob_->objective_vector || !prob_->variable_lower_bound || !prob_->variable_upper_bound)
+        throw Error("problem vectors missing");
+    if (m_ > 0 && (!prob_->constraint_lower_bound || !prob_->constraint_upper_bound))
+        throw Error("constraint bounds missing");
+    csr_validate(m_, n_, prob_->constraint_matrix_row_pointers, prob_->constraint_matrix_col_indices, nnz_,
+                 "constraint matrix");
+    At_host_ = csr_transpose(m_, n_, prob_->constraint_matrix_row_pointers, prob_->constraint_matrix_col_indices,
+                             prob_->constraint_matrix_values);
+    S_it_ = O_.spmv_nnz_per_block > 0 ? O_.spmv_nnz_per_block : auto_block_nnz(nnz_, std::max(m_, n_));
+    if (S_it_ != 256 && S_it_ != 512 && S_it_ != 1024 && S_it_ != 2048)
+        throw Error("spmv_nnz_per_block must be 256, 512, 1024 or 2048");
+    S_ev_ = std::min(S_it_, 1024);
+
+    /* controller parameters, environment overrides resolved */
+    const auto &R = P_.restart_params;
+    cp_.F = P_.termination_evaluation_frequency;
+    cp_.iteration_limit = P_.termination_criteria.iteration_limit;
+    cp_.time_limit = P_.termination_criteria.time_sec_limit;
+    cp_.eps_opt = P_.termination_criteria.eps_optimal_relative;
+    cp_.eps_feas = P_.termination_criteria.eps_feasible_relative;
+    cp_.norm_linf = P_.optimality_norm == NORM_TYPE_L_INF;
+    cp_.refl = P_.reflection_coefficient;
+    cp_.suff = std::isnan(O_.restart_sufficient) ? R.sufficient_reduction_for_restart : O_.restart_sufficient;
+    cp_.nec = std::isnan(O_.restart_necessary) ? R.necessary_reduction_for_restart : O_.restart_necessary;
+    cp_.art = std::isnan(O_.restart_artificial) ? R.artificial_restart_threshold : O_.restart_artificial;
+    cp_.kp = R.k_p;
+    cp_.ki = R.k_i;
+    cp_.kd = R.k_d;
+    cp_.ismooth = R.i_smooth;
+    cp_.sigma_mode = O_.sigma_mode != 0;
+    cp_.sigma_adaptive = O_.sigma_adaptive != 0;
+    cp_.s_kp = std::isnan(O_.sigma_kp) ? R.k_p : O_.sigma_kp;
+    cp_.s_ki = std::isnan(O_.sigma_ki) ? R.k_i : O_.sigma_ki;
+    cp_.s_kd = std::isnan(O_.sigma_kd) ? R.k_d : O_.sigma_kd;
+    cp_.s_ismooth = std::isnan(O_.sigma_i_smooth) ? R.i_smooth : O_.sigma_i_smooth;
+    cp_.s_gain = O_.sigma_balance_gain;
+    cp_.s_umin = O_.sigma_update_min;
+    cp_.s_umax = O_.sigma_update_max;
+    cp_.step_margin = O_.step_margin;
+    cp_.lambda_factor = O_.lambda_factor;
+    cp_.lambda_param_set = O_.lambda_param_set;
+    cp_.lambda_param_opt = O_.lambda_param;
+    cp_.obj_const = prob_->objective_constant;
+    /* norms of the unscaled problem (LP/CP_AL/src/solver.cu:1999-2067) */
+    {
+        const bool linf = cp_.norm_linf;
+        double s = 0, mx = 0;
+        for (int j = 0; j < n_; ++j) {
+            const double v = prob_->objective_vector[j];
+            if (linf)
+                mx = std::fmax(mx, std::fabs(v));
+            else
+                s += v * v;
+        }
+        cp_.obj_norm = linf ? mx : std::sqrt(s);
+        s = 0;
+        mx = 0;
+        for (int i = 0; i < m_; ++i) {
+            const double lo = prob_->constraint_lower_bound[i], up = prob_->constraint_upper_bound[i];
+            if (linf) {
+                if (std::isfinite(lo) && lo != up) mx = std::fmax(mx, std::fabs(lo));
+                if (std::isfinite(up)) mx = std::fmax(mx, std::fabs(up));
+            } else {
+                if (std::isfinite(lo) && lo != up) s += lo * lo;
+                if (std::isfinite(up)) s += up * up;
+            }
+        }
+        cp_.bnd_norm = linf ? mx : std::sqrt(s);
+    }
+    fp32_phase_ = O_.precision == CP_AL_GB300_FP32_REFINE;
+}
+
+void CpalSolver::alloc_plan(PlanDev &pd) {
+    pd.d.nblocks = pd.hp.nblocks;
+    pd.d.nlong = pd.hp.nlong;
+    pd.d.desc = arena_.take<int4>(std::max(pd.hp.nblocks, 1));
+    pd.d.linfo = arena_.take<int4>(std::max(pd.hp.nlong, 1));
+    pd.d.lpart = arena_.take<double>(kLongStride * (size_t)std::max(pd.hp.npieces, 1));
+    pd.d.lcount = arena_.take<unsigned>(std::max(pd.hp.nlong, 1));
+}
+
+void CpalSolver::upload_plan(PlanDev &pd) {
+    if (pd.hp.nblocks)
+        PDAL_CUDA(cudaMemcpyAsync((void *)pd.d.desc, pd.hp.desc.data(), pd.hp.desc.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice, stream_));
+    if (pd.hp.nlong)
+        PDAL_CUDA(cudaMemcpyAsync((void *)pd.d.linfo, pd.hp.linfo.data(), pd.hp.linfo.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice, stream_));
+    PDAL_CUDA(cudaMemsetAsync(pd.d.lcount, 0, sizeof(unsigned) * std::max(pd.hp.nlong, 1), stream_));
+    h2d += (pd.hp.desc.size() + pd.hp.linfo.size()) * sizeof(int);
+}
+
+void CpalSolver::alloc_all() {
+    const size_t n = n_, m = m_, nnz = nnz_;
+    A_.rp = arena_.take<int>(m + 1);
+    A_.ci = arena_.take<int>(nnz);
+    A_.v = arena_.take<double>(nnz);
+    Av0_ = arena_.take<double>(nnz);
+    At_.rp = arena_.take<int>(n + 1);
+    At_.ci = arena_.take<int>(nnz);
+    At_.v = arena_.take<double>(nnz);
+    Atv0_ = arena_.take<double>(nnz);
+    if (fp32_phase_) {
+        A_.vf = arena_.take<float>(nnz);
+        At_.vf = arena_.take<float>(nnz);
+    }
+    alloc_plan(A_.it);
+    alloc_plan(At_.it);
+    alloc_plan(A_.ev);
+    alloc_plan(At_.ev);
+    c0_ = arena_.take<double>(n);
+    vlb0_ = arena_.take<double>(n);
+    vub0_ = arena_.take<double>(n);
+    x00_ = arena_.take<double>(n);
+    clb0_ = arena_.take<double>(m);
+    cub0_ = arena_.take<double>(m);
+    y00_ = arena_.take<double>(m);
+    c_ = arena_.take<double>(n);
+    vlb_ = arena_.take<double>(n);
+    vub_ = arena_.take<double>(n);
+    x0_ = arena_.take<double>(n);
+    dsc_ = arena_.take<double>(n);
+    tmp_n_ = arena_.take<double>(n);
+    xout_ = arena_.take<double>(n);
+    rcout_ = arena_.take<double>(n);
+    clb_ = arena_.take<double>(m);
+    cub_ = arena_.take<double>(m);
+    clbf_ = arena_.take<double>(m);
+    cubf_ = arena_.take<double>(m);
+    y0_ = arena_.take<double>(m);
+    ax0_ = arena_.take<double>(m);
+    phat_ = arena_.take<double>(m);
+    rsc_ = arena_.take<double>(m);
+    tmp_m_ = arena_.take<double>(m);
+    tmp_m2_ = arena_.take<double>(m);
+    yout_ = arena_.take<double>(m);
+    {
+        auto &v = v64_;
+        v.x = arena_.take<double>(n);
+        v.xbar = arena_.take<double>(n);
+        v.xh = arena_.take<double>(n);
+        v.lam = arena_.take<double>(n);
+        v.c = c_;
+        v.vlb = vlb_;
+        v.vub = vub_;
+        v.y = arena_.take<double>(m);
+        v.yh = arena_.take<double>(m);
+        v.ybar = arena_.take<double>(m);
+        v.ax = arena_.take<double>(m);
+        v.u = arena_.take<double>(m);
+        v.clb = clb_;
+        v.cub = cub_;
+    }
+    if (fp32_phase_) {
+        auto &v = v32_;
+        v.x = arena_.take<float>(n);
+        v.xbar = arena_.take<float>(n);
+        v.xh = arena_.take<float>(n);
+        v.lam = arena_.take<float>(n);
+        v.c = arena_.take<float>(n);
+        v.vlb = arena_.take<float>(n);
+        v.vub = arena_.take<float>(n);
+        v.y = arena_.take<float>(m);
+        v.yh = arena_.take<float>(m);
+        v.ybar = arena_.take<float>(m);
+        v.ax = arena_.take<float>(m);
+        v.u = arena_.take<float>(m);
+        v.clb = arena_.take<float>(m);
+        v.cub = arena_.take<float>(m);
+    }
+    part_row_ = arena_.take<double>((size_t)(A_.ev.hp.nblocks + A_.ev.hp.nlong + 1) * kEvalStride);
+    part_col_ = arena_.take<double>((size_t)(At_.ev.hp.nblocks + At_.ev.hp.nlong + 1) * kEvalStride);
+    nmisc_ = std::max({A_.ev.hp.nblocks + A_.ev.hp.nlong, grid_for(std::max(n_, m_)), 1});
+    part_misc_ = arena_.take<double>(2 * (size_t)nmisc_ + 2);
+    st_ = arena_.take<CpalState>(1);
+    ps_ = arena_.take<PowerState>(1);
+}
+
+void CpalSolver::upload() {
+    if (O_.device >= 0) PDAL_CUDA(cudaSetDevice(O_.device));
+    PDAL_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    PDAL_CUDA(cudaMallocHost(&h_st_, sizeof(CpalState)));
+    PDAL_CUDA(cudaMallocHost(&h_ps_, sizeof(PowerState)));
+    A_.nr = m_;
+    A_.nc = n_;
+    A_.nnz = nnz_;
+    At_.nr = n_;
+    At_.nc = m_;
+    At_.nnz = nnz_;
+    A_.it.hp = plan_rows(m_, prob_->constraint_matrix_row_pointers, S_it_);
+    At_.it.hp = plan_rows(n_, At_host_.rp.data(), S_it_);
+    A_.ev.hp = plan_rows(m_, prob_->constraint_matrix_row_pointers, S_ev_);
+    At_.ev.hp = plan_rows(n_, At_host_.rp.data(), S_ev_);
+    arena_.begin_measure();
+    alloc_all();
+    arena_.reserve_measured();
+    alloc_all();
+
+    const size_t n = n_, m = m_, nnz = nnz_;
+    auto up = [&](void *dst, const void *src, size_t b) {
+        if (b == 0) return;
+        PDAL_CUDA(cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, stream_));
+        h2d += (int64_t)b;
+    };
+    up(A_.rp, prob_->constraint_matrix_row_pointers, (m + 1) * sizeof(int));
+    up(A_.ci, prob_->constraint_matrix_col_indices, nnz * sizeof(int));
+    up(Av0_, prob_->constraint_matrix_values, nnz * sizeof(double));
+    up(At_.rp, At_host_.rp.data(), (n + 1) * sizeof(int));
+    up(At_.ci, At_host_.ci.data(), nnz * sizeof(int));
+    up(Atv0_, At_host_.v.data(), nnz * sizeof(double));
+    upload_plan(A_.it);
+    upload_plan(At_.it);
+    upload_plan(A_.ev);
+    upload_plan(At_.ev);
+    up(c0_, prob_->objective_vector, n * sizeof(double));
+    up(vlb0_, prob_->variable_lower_bound, n * sizeof(double));
+    up(vub0_, prob_->variable_upper_bound, n * sizeof(double));
+    up(clb0_, prob_->constraint_lower_bound, m * sizeof(double));
+    up(cub0_, prob_->constraint_upper_bound, m * sizeof(double));
+    if (prob_->primal_start)
+        up(x00_, prob_->primal_start, n * sizeof(double));
+    else
+        PDAL_CUDA(cudaMemsetAsync(x00_, 0, std::max<size_t>(n, 1) * sizeof(double), stream_));
+    if (prob_->dual_start)
+        up(y00_, prob_->dual_start, m * sizeof(double));
+    else
+        PDAL_CUDA(cudaMemsetAsync(y00_, 0, std::max<size_t>(m, 1) * sizeof(double), stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    At_host_ = HostCsr(); /* host transpose no longer needed */
+}
+
+void CpalSolver::power_iteration() {
+    PowerState h{};
+    h.max_iter = P_.sv_max_iter;
+    h.tol = P_.sv_tol;
+    h.done = (h.max_iter <= 0) ? 1 : 0;
+    /* start vector: std::normal_distribution over std::mt19937(1), as the
+     * reference draws it in a fresh process (LP/CP_AL/src/utils.cu:27-28, 102-106) */
+    std::vector<double> v0(m_);
+    std::mt19937 gen(1);
+    std::normal_distribution<double> dist(0.0, 1.0);
+    for (int i = 0; i < m_; ++i) v0[i] = dist(gen);
+    double *v = tmp_m_, *vn = tmp_m2_, *dp = tmp_n_;
+    PDAL_CUDA(cudaMemcpyAsync(v, v0.data(), sizeof(double) * m_, cudaMemcpyHostToDevice, stream_));
+    h2d += sizeof(double) * m_;
+    *h_ps_ = h;
+    PDAL_CUDA(cudaMemcpyAsync(ps_, h_ps_, sizeof(PowerState), cudaMemcpyHostToDevice, stream_));
+    k_power_start<<<1, kThreads, 0, stream_>>>(m_, v, ps_);
+    PDAL_LAUNCH_CHECK();
+    launches += 1;
+    const int gres = grid_for(m_);
+    const int steps_per_graph = 16;
+    cudaGraphExec_t exec = nullptr;
+    PDAL_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < steps_per_graph; ++s) {
+        PDAL_WITH_SE(S_ev_, {
+            k_power_at<SE><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, v, dp, ps_);
+            k_power_a<SE><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, dp, v, vn,
+                                                                     part_misc_, ps_);
+        });
+        k_power_dot<<<1, kThreads, 0, stream_>>>(part_misc_, A_.ev.d.nblocks + A_.ev.d.nlong, ps_);
+        k_power_resid<<<gres, kThreads, 0, stream_>>>(m_, v, vn, part_misc_, ps_);
+        k_power_check<<<1, kThreads, 0, stream_>>>(part_misc_, gres, ps_);
+    }
+    cudaGraph_t graph;
+    PDAL_CUDA(cudaStreamEndCapture(stream_, &graph));
+    PDAL_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    PDAL_CUDA(cudaGraphDestroy(graph));
+    const int max_launch = P_.sv_max_iter / steps_per_graph + 2;
+    for (int it = 0; it < max_launch; ++it) {
+        PDAL_CUDA(cudaGraphLaunch(exec, stream_));
+        launches += 5 * steps_per_graph;
+        PDAL_CUDA(cudaMemcpyAsync(h_ps_, ps_, sizeof(PowerState), cudaMemcpyDeviceToHost, stream_));
+        d2h += sizeof(PowerState);
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
+        if (h_ps_->done) break;
+    }
+    cudaGraphExecDestroy(exec);
+    power_iters = h_ps_->iters;
+    const double smax = std::sqrt(h_ps_->s2);
+    host_state.lambda_est = smax * smax;
+}
+
+void CpalSolver::setup_device() {
+    const double t0 = now_sec();
+    for (auto &r : sum_ms)
+        for (auto &x : r) x = 0;
+    timed[0] = timed[1] = 0;
+    launches = 0;
+    fp32_iters = 0;
+    fp32_phase_ = O_.precision == CP_AL_GB300_FP32_REFINE;
+    const size_t n = n_, m = m_, nnz = nnz_;
+    auto d2d = [&](void *dst, const void *src, size_t b) {
+        if (b) PDAL_CUDA(cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, stream_));
+    };
+    d2d(A_.v, Av0_, nnz * sizeof(double));
+    d2d(At_.v, Atv0_, nnz * sizeof(double));
+    d2d(c_, c0_, n * sizeof(double));
+    d2d(vlb_, vlb0_, n * sizeof(double));
+    d2d(vub_, vub0_, n * sizeof(double));
+    d2d(x0_, x00_, n * sizeof(double));
+    d2d(clb_, clb0_, m * sizeof(double));
+    d2d(cub_, cub0_, m * sizeof(double));
+    d2d(y0_, y00_, m * sizeof(double));
+
+    /* equilibration: LP/CP_AL/src/preconditioner.cu:379-475 */
+    const int gn = grid_for(n), gm = grid_for(m);
+    const int gwr_m = grid_for((long long)m * 32), gwr_n = grid_for((long long)n * 32);
+    std::vector<double> ones_n(n, 1.0), ones_m(m, 1.0);
+    PDAL_CUDA(cudaMemcpyAsync(dsc_, ones_n.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    if (m) PDAL_CUDA(cudaMemcpyAsync(rsc_, ones_m.data(), m * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    double *rstep = tmp_m_, *dstep = tmp_n_;
+    auto scale_pass = [&](int mode, double deg_rows, double deg_cols) {
+        if (m) k_row_scale<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.v, mode, deg_rows, rstep, rsc_);
+        k_row_scale<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.v, mode, deg_cols, dstep, dsc_);
+        if (m) k_scale_matrix<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, A_.v, rstep, dstep, 0);
+        k_scale_matrix<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, At_.v, dstep, rstep, 1);
+        k_scale_vectors<<<grid_for(std::max(n, m)), kThreads, 0, stream_>>>(n_, m_, dstep, rstep, c_, vlb_, vub_, x0_,
+                                                                            clb_, cub_, y0_);
+        PDAL_LAUNCH_CHECK();
+        launches += 5;
+    };
+    for (int it = 0; it < P_.l_inf_ruiz_iterations; ++it) scale_pass(0, 0.0, 0.0);
+    if (P_.has_pock_chambolle_alpha) scale_pass(1, P_.pock_chambolle_alpha, 2.0 - P_.pock_chambolle_alpha);
+    const int gb = grid_for(std::max(n, m));
+    k_boundobj_partials<<<gb, kThreads, 0, stream_>>>(n_, m_, clb_, cub_, c_, part_misc_);
+    k_boundobj_finish<<<1, kThreads, 0, stream_>>>(part_misc_, gb, st_, P_.bound_objective_rescaling ? 1 : 0);
+    if (P_.bound_objective_rescaling)
+        k_scale_boundobj<<<gb, kThreads, 0, stream_>>>(n_, m_, st_, c_, vlb_, vub_, x0_, clb_, cub_, y0_);
+    if (m) k_finite_bounds<<<gm, kThreads, 0, stream_>>>(m_, clb_, cub_, clbf_, cubf_);
+    PDAL_LAUNCH_CHECK();
+    launches += 4;
+    (void)gn;
+    /* cbr / ovr back to the host state */
+    PDAL_CUDA(cudaMemcpyAsync(h_st_, st_, sizeof(CpalState), cudaMemcpyDeviceToHost, stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    d2h += sizeof(CpalState);
+    CpalState s{};
+    s.cbr = h_st_->cbr;
+    s.ovr = h_st_->ovr;
+
+    /* step size and primal weight: LP/CP_AL/src/solver.cu:3538-3609 */
+    if (nnz_ == 0) {
+        host_state.lambda_est = 1.0;
+        power_iters = 0;
+    } else {
+        power_iteration();
+    }
+    s.lambda_est = host_state.lambda_est;
+    s.pw = P_.bound_objective_rescaling ? 1.0 : (cp_.obj_norm + 1.0) / (cp_.bnd_norm + 1.0);
+    s.sigma_on = cp_.sigma_mode;
+    s.sigma_adapt = 0;
+    if (s.sigma_on) { /* solver.cu:3141-3164 */
+        s.lambda_param = O_.lambda_param_set ? O_.lambda_param : O_.lambda_factor * std::fmax(s.lambda_est, 1e-12);
+        s.lambda_param = std::fmax(s.lambda_param, (2.0 + 1e-12) * std::fmax(s.lambda_est, 1e-12));
+        s.sigma_base = 1.0 / std::sqrt(std::fmax(s.lambda_param, 1e-16));
+        s.sigma_min = O_.sigma_min_factor * s.sigma_base;
+        s.sigma_max = O_.sigma_max_factor * s.sigma_base;
+        s.sigma = O_.sigma_set ? O_.sigma : O_.sigma_init_factor * s.sigma_base;
+        s.sigma = std::fmin(std::fmax(s.sigma, s.sigma_min), s.sigma_max);
+        s.sigma_best = s.sigma;
+        s.sigma_adapt = O_.sigma_adaptive != 0;
+    }
+    s.al_lambda = O_.al_lambda;
+    cpal_refresh_step_schedule(s, cp_);
+    s.best_pw = s.pw;
+    s.best_gap = INFINITY;
+    s.fp_last = INFINITY;
+    s.refl = cp_.refl;
+    s.fp32_switch_tol = fp32_phase_ ? O_.fp32_switch_tol : -1.0;
+    cpal_set_coefficients(s);
+    beta_on_ = s.beta > 0.0;
+    host_state = s;
+    *h_st_ = s;
+    PDAL_CUDA(cudaMemcpyAsync(st_, h_st_, sizeof(CpalState), cudaMemcpyHostToDevice, stream_));
+    h2d += sizeof(CpalState);
+
+    /* iterates start at the (scaled) warm start: solver.cu:1939-1974 */
+    d2d(v64_.x, x0_, n * sizeof(double));
+    d2d(v64_.xh, x0_, n * sizeof(double));
+    d2d(v64_.y, y0_, m * sizeof(double));
+    d2d(v64_.yh, y0_, m * sizeof(double));
+    if (n) PDAL_CUDA(cudaMemsetAsync(v64_.lam, 0, n * sizeof(double), stream_));
+    if (n) PDAL_CUDA(cudaMemsetAsync(v64_.xbar, 0, n * sizeof(double), stream_));
+    if (m) PDAL_CUDA(cudaMemsetAsync(v64_.ybar, 0, m * sizeof(double), stream_));
+    if (m) PDAL_CUDA(cudaMemsetAsync(v64_.u, 0, m * sizeof(double), stream_));
+    if (fp32_phase_) {
+        auto cv = [&](const double *src, float *dst, size_t len) {
+            if (len) k_convert<double, float><<<grid_for(len), kThreads, 0, stream_>>>(src, dst, (int)len);
+            launches += 1;
+        };
+        cv(A_.v, A_.vf, nnz);
+        cv(At_.v, At_.vf, nnz);
+        cv(c_, v32_.c, n);
+        cv(vlb_, v32_.vlb, n);
+        cv(vub_, v32_.vub, n);
+        cv(x0_, v32_.x, n);
+        cv(x0_, v32_.xh, n);
+        cv(clb_, v32_.clb, m);
+        cv(cub_, v32_.cub, m);
+        cv(y0_, v32_.y, m);
+        cv(y0_, v32_.yh, m);
+        if (n) PDAL_CUDA(cudaMemsetAsync(v32_.lam, 0, n * sizeof(float), stream_));
+        if (n) PDAL_CUDA(cudaMemsetAsync(v32_.xbar, 0, n * sizeof(float), stream_));
+        if (m) PDAL_CUDA(cudaMemsetAsync(v32_.ybar, 0, m * sizeof(float), stream_));
+        if (m) PDAL_CUDA(cudaMemsetAsync(v32_.u, 0, m * sizeof(float), stream_));
+        PDAL_LAUNCH_CHECK();
+        launch_init_ax<float>();
+    } else {
+        launch_init_ax<double>();
+    }
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    setup_sec = now_sec() - t0;
+}
+
+template <typename T>
+void CpalSolver::launch_init_ax() {
+    if (m_ == 0) return;
+    auto &v = vecs<T>();
+    PDAL_WITH_SE(S_ev_, {
+        if (beta_on_)
+            k_init_ax<T, SE, true><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(
+                A_.ev.d, A_.rp, A_.ci, A_.v, x0_, v.ax, ax0_, v.u, v.y, v.clb, v.cub, st_);
+        else
+            k_init_ax<T, SE, false><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(
+                A_.ev.d, A_.rp, A_.ci, A_.v, x0_, v.ax, ax0_, v.u, v.y, v.clb, v.cub, st_);
+    });
+    PDAL_LAUNCH_CHECK();
+    launches += 1;
+}
+
+template <typename T>
+static const T *matvals(const double *v64, const float *v32);
+template <>
+const double *matvals<double>(const double *v64, const float *) {
+    return v64;
+}
+template <>
+const float *matvals<float>(const double *, const float *v32) {
+    return v32;
+}
+
+template <typename T>
+void CpalSolver::launch_primal(int koff, bool major) {
+    auto &v = vecs<T>();
+    PrimalArgs<T> pa{v.x, v.xbar, v.xh, v.lam, x0_, v.c, v.vlb, v.vub};
+    const T *gat = beta_on_ ? v.u : v.y;
+    const T *Atv = matvals<T>(At_.v, At_.vf);
+    PDAL_WITH_S(S_it_, {
+        if (major)
+            k_primal<T, SB, true><<<At_.it.d.nblocks, kThreads, 0, stream_>>>(At_.it.d, At_.rp, At_.ci, Atv, gat, pa,
+                                                                             st_, koff);
+        else
+            k_primal<T, SB, false><<<At_.it.d.nblocks, kThreads, 0, stream_>>>(At_.it.d, At_.rp, At_.ci, Atv, gat,
+                                                                              pa, st_, koff);
+    });
+}
+
+template <typename T>
+void CpalSolver::launch_dual(int koff, bool major) {
+    if (m_ == 0) return;
+    auto &v = vecs<T>();
+    const T *Av = matvals<T>(A_.v, A_.vf);
+    DualArgs<T> da{v.y, v.yh, v.ybar, v.ax, v.u, y0_, ax0_, v.clb, v.cub};
+    PDAL_WITH_S(S_it_, {
+        if (major) {
+            if (beta_on_)
+                k_dual<T, SB, true, true><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av, v.xbar,
+                                                                                    da, st_, koff);
+            else
+                k_dual<T, SB, true, false><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av,
+                                                                                     v.xbar, da, st_, koff);
+        } else {
+            if (beta_on_)
+                k_dual<T, SB, false, true><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av,
+                                                                                     v.xbar, da, st_, koff);
+            else
+                k_dual<T, SB, false, false><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av,
+                                                                                      v.xbar, da, st_, koff);
+        }
+    });
+}
+
+template <typename T>
+void CpalSolver::launch_iteration(int koff, bool major) {
+    launch_primal<T>(koff, major);
+    launch_dual<T>(koff, major);
+}
+
+template <typename T>
+void CpalSolver::launch_eval() {
+    auto &v = vecs<T>();
+    EvalRowArgs<T> ra{v.xh, v.xbar, v.yh, v.ybar, x0_, y0_, ax0_, clb_, cub_, clbf_, cubf_, rsc_, phat_, part_row_,
+                      A_.ev.d.nblocks};
+    EvalColArgs<T> ca{v.xh, v.xbar, v.yh, v.ybar, v.lam, x0_, c_, dsc_, part_col_, At_.ev.d.nblocks};
+    PDAL_WITH_SE(S_ev_, {
+        if (m_ > 0)
+            k_eval_rows<T, SE><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, ra, st_);
+        k_eval_cols<T, SE><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, ca, st_);
+    });
+    const int nrow_slots = m_ > 0 ? A_.ev.d.nblocks + A_.ev.d.nlong : 0;
+    k_control<<<1, kThreads, 0, stream_>>>(part_row_, nrow_slots, part_col_, At_.ev.d.nblocks + At_.ev.d.nlong, st_,
+                                           cp_);
+    const int gr = grid_for(std::max(n_, m_));
+    if (beta_on_)
+        k_restart<T, true><<<gr, kThreads, 0, stream_>>>(st_, n_, m_, v.xh, v.x, x0_, v.yh, v.y, y0_, phat_, v.ax,
+                                                         ax0_, v.u, v.clb, v.cub);
+    else
+        k_restart<T, false><<<gr, kThreads, 0, stream_>>>(st_, n_, m_, v.xh, v.x, x0_, v.yh, v.y, y0_, phat_, v.ax,
+                                                          ax0_, v.u, v.clb, v.cub);
+}
+
+template <typename T>
+void CpalSolver::capture_block(cudaGraphExec_t &exec) {
+    const int F = cp_.F;
+    const int G = std::max(1, O_.graph_blocks);
+    const bool timing = O_.timing != 0;
+    if (timing && !ev_[0])
+        for (auto &e : ev_) PDAL_CUDA(cudaEventCreate(&e));
+    PDAL_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    for (int g = 0; g < G; ++g) {
+        if (timing && g == 0) PDAL_CUDA(cudaEventRecord(ev_[3], stream_));
+        for (int i = 1; i <= F; ++i) {
+            /* one non-major iteration (F-1 >= 2) is bracketed by events */
+            if (timing && g == 0 && i == F - 1) {
+                PDAL_CUDA(cudaEventRecord(ev_[0], stream_));
+                launch_primal<T>(i, false);
+                PDAL_CUDA(cudaEventRecord(ev_[1], stream_));
+                launch_dual<T>(i, false);
+                PDAL_CUDA(cudaEventRecord(ev_[2], stream_));
+            } else {
+                launch_iteration<T>(i, i == F);
+            }
+        }
+        launch_eval<T>();
+    }
+    cudaGraph_t graph;
+    PDAL_CUDA(cudaStreamEndCapture(stream_, &graph));
+    PDAL_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    PDAL_CUDA(cudaGraphDestroy(graph));
+}
+
+void CpalSolver::switch_to_fp64() {
+    /* FP64 refinement phase: restart from the FP32 iterate (x0 = x = x^,
+     * y0 = y = y^), recompute A x0 and the predictor exactly in FP64, and
+     * keep every controller scalar (weight, step, sigma, counters). */
+    const size_t n = n_, m = m_;
+    auto up = [&](const float *src, double *dst, size_t len) {
+        if (len) k_convert<float, double><<<grid_for(len), kThreads, 0, stream_>>>(src, dst, (int)len);
+        launches += 1;
+    };
+    up(v32_.xh, v64_.xh, n);
+    up(v32_.xh, v64_.x, n);
+    up(v32_.xh, x0_, n);
+    up(v32_.xbar, v64_.xbar, n);
+    up(v32_.lam, v64_.lam, n);
+    up(v32_.yh, v64_.yh, m);
+    up(v32_.yh, v64_.y, m);
+    up(v32_.yh, y0_, m);
+    up(v32_.ybar, v64_.ybar, m);
+    PDAL_LAUNCH_CHECK();
+    CpalState s = *h_st_;
+    s.inner = 0;
+    s.fp_last = INFINITY;
+    if (!s.restart) s.fp0 = s.fp;
+    s.phase_switch = 0;
+    s.fp32_switch_tol = -1.0;
+    s.restart = 0;
+    *h_st_ = s;
+    PDAL_CUDA(cudaMemcpyAsync(st_, h_st_, sizeof(CpalState), cudaMemcpyHostToDevice, stream_));
+    h2d += sizeof(CpalState);
+    fp32_phase_ = false;
+    launch_init_ax<double>();
+}
+
+void CpalSolver::run_loop() {
+    const double t0 = now_sec();
+    const int F = cp_.F;
+    const int G = std::max(1, O_.graph_blocks);
+    const int64_t per_block = 2LL * F - (m_ == 0 ? F : 0) + (m_ > 0 ? 4 : 3);
+    k_start_clock<<<1, 1, 0, stream_>>>(st_);
+    PDAL_LAUNCH_CHECK();
+    launches += 1;
+    const int fp32_cap = O_.fp32_max_iterations;
+    for (;;) {
+        cudaGraphExec_t *exec;
+        if (fp32_phase_) {
+            if (!exec32_) capture_block<float>(exec32_);
+            exec = &exec32_;
+        } else {
+            if (!exec64_) capture_block<double>(exec64_);
+            exec = &exec64_;
+        }
+        PDAL_CUDA(cudaGraphLaunch(*exec, stream_));
+        launches += per_block * G;
+        PDAL_CUDA(cudaMemcpyAsync(h_st_, st_, sizeof(CpalState), cudaMemcpyDeviceToHost, stream_));
+        d2h += sizeof(CpalState);
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
+        if (O_.timing && F >= 3 && ev_[0]) {
+            float a = 0, b = 0, c = 0;
+            PDAL_CUDA(cudaEventElapsedTime(&a, ev_[0], ev_[1]));
+            PDAL_CUDA(cudaEventElapsedTime(&b, ev_[1], ev_[2]));
+            PDAL_CUDA(cudaEventElapsedTime(&c, ev_[3], ev_[2]));
+            const int ph = fp32_phase_ ? 1 : 0;
+            sum_ms[ph][0] += a;
+            sum_ms[ph][1] += b;
+            sum_ms[ph][2] += c;
+            timed[ph] += 1;
+        }
+        if (fp32_phase_) fp32_iters = h_st_->total;
+        if (h_st_->status) break;
+        /* the device enforces the time limit; this host guard only covers a
+         * device clock that does not advance */
+        if (now_sec() - t0 > cp_.time_limit + 60.0) {
+            h_st_->status = TERMINATION_REASON_TIME_LIMIT;
+            break;
+        }
+        if (fp32_phase_ && (h_st_->phase_switch || (fp32_cap >= 0 && h_st_->total >= fp32_cap))) switch_to_fp64();
+    }
+    if (fp32_phase_) {
+        /* finished inside the FP32 phase: promote the reported iterate */
+        const size_t n = n_, m = m_;
+        if (n) k_convert<float, double><<<grid_for(n), kThreads, 0, stream_>>>(v32_.xh, v64_.xh, n_);
+        if (m) k_convert<float, double><<<grid_for(m), kThreads, 0, stream_>>>(v32_.yh, v64_.yh, m_);
+        PDAL_LAUNCH_CHECK();
+        launches += 2;
+    }
+    host_state = *h_st_;
+    loop_sec = now_sec() - t0;
+}
+
+void CpalSolver::result_on_device() {
+    ResultColEpi epi;
+    epi.xh = v64_.xh;
+    epi.c = c_;
+    epi.cscale = dsc_;
+    epi.vlb = vlb_;
+    epi.vub = vub_;
+    epi.st = st_;
+    epi.x_out = xout_;
+    epi.rc_out = rcout_;
+    PDAL_WITH_SE(S_ev_, {
+        k_result_cols<SE><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, v64_.yh, epi);
+    });
+    if (m_) k_result_rows<<<grid_for(m_), kThreads, 0, stream_>>>(m_, v64_.yh, rsc_, st_, yout_);
+    PDAL_LAUNCH_CHECK();
+    launches += 2;
+}
+
+void CpalSolver::fetch_vectors(double *x, double *y, double *rc) {
+    if (x) PDAL_CUDA(cudaMemcpyAsync(x, xout_, sizeof(double) * n_, cudaMemcpyDeviceToHost, stream_));
+    if (y && m_) PDAL_CUDA(cudaMemcpyAsync(y, yout_, sizeof(double) * m_, cudaMemcpyDeviceToHost, stream_));
+    if (rc) PDAL_CUDA(cudaMemcpyAsync(rc, rcout_, sizeof(double) * n_, cudaMemcpyDeviceToHost, stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    d2h += (int64_t)sizeof(double) * ((x ? n_ : 0) + (y ? m_ : 0) + (rc ? n_ : 0));
+}
+
+void CpalSolver::download(cp_al_result_t *res, bool vectors) {
+    const CpalState &s = host_state;
+    res->num_variables = n_;
+    res->num_constraints = m_;
+    res->num_nonzeros = nnz_;
+    res->total_count = s.total;
+    res->rescaling_time_sec = setup_sec;
+    res->cumulative_time_sec = loop_sec;
+    res->presolve_time = 0.0;
+    res->presolve_status = 0;
+    res->absolute_primal_residual = s.abs_p;
+    res->relative_primal_residual = s.rel_p;
+    res->absolute_dual_residual = s.abs_d;
+    res->relative_dual_residual = s.rel_d;
+    res->primal_objective_value = s.pobj;
+    res->dual_objective_value = s.dobj;
+    res->objective_gap = s.gap;
+    res->relative_objective_gap = s.rel_gap;
+    res->termination_reason = (termination_reason_t)s.status;
+    if (vectors) {
+        res->primal_solution = (double *)malloc(sizeof(double) * std::max(n_, 1));
+        res->dual_solution = (double *)malloc(sizeof(double) * std::max(m_, 1));
+        res->reduced_cost = (double *)malloc(sizeof(double) * std::max(n_, 1));
+        if (!res->primal_solution || !res->dual_solution || !res->reduced_cost) throw Error("out of host memory");
+        fetch_vectors(res->primal_solution, res->dual_solution, res->reduced_cost);
+    }
+}
+
+} // namespace pdal
+
+/* ---------------------------------------------------------------------- */
+/* C entry points                                                          */
+/* ---------------------------------------------------------------------- */
+namespace {
+thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) {
+    g_last_error = msg;
+    fprintf(stderr, "[cp_al_gb300] %s\n", msg.c_str());
+}
+} // namespace
+
+struct cp_al_gb300_session {
+    std::unique_ptr<pdal::CpalSolver> solver;
+    lp_problem_t prob_copy;
+};
+
+extern "C" {
+
+const char *cp_al_gb300_last_error(void) { return g_last_error.c_str(); }
+
+void cp_al_gb300_last_stats(cp_al_gb300_stats_t *out) {
+    if (out) *out = pdal::g_stats;
+}
+
+static void fill_stats(const pdal::CpalSolver &s, double total) {
+    cp_al_gb300_stats_t &st = pdal::g_stats;
+    memset(&st, 0, sizeof(st));
+    st.setup_sec = s.setup_sec;
+    st.loop_sec = s.loop_sec;
+    st.total_sec = total;
+    st.lambda_est = s.host_state.lambda_est;
+    st.power_iterations = s.power_iters;
+    st.restarts = s.host_state.restarts;
+    st.fp32_iterations = s.fp32_iters;
+    st.kernel_launches = s.launches;
+    st.h2d_bytes = s.h2d;
+    st.d2h_bytes = s.d2h;
+    st.primal_weight = s.host_state.pw;
+    if (s.timed[0] > 0) {
+        st.avg_primal_ms = s.sum_ms[0][0] / s.timed[0];
+        st.avg_dual_ms = s.sum_ms[0][1] / s.timed[0];
+        st.avg_block_ms = s.sum_ms[0][2] / s.timed[0];
+        st.timed_blocks = s.timed[0];
+    }
+    if (s.timed[1] > 0) {
+        st.avg_primal32_ms = s.sum_ms[1][0] / s.timed[1];
+        st.avg_dual32_ms = s.sum_ms[1][1] / s.timed[1];
+        st.avg_block32_ms = s.sum_ms[1][2] / s.timed[1];
+        st.timed_blocks32 = s.timed[1];
+    }
+    st.step_size = s.host_state.step;
+    st.al_penalty = s.host_state.beta;
+}
+
+cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *params,
+                                  const cp_al_gb300_options_t *opts) {
+    g_last_error.clear();
+    if (!prob) {
+        set_error("solve_lp_problem: invalid arguments.");
+        return nullptr;
+    }
+    cp_al_parameters_t local;
+    if (params)
+        local = *params;
+    else
+        set_default_parameters(&local);
+    cp_al_gb300_options_t o;
+    if (opts)
+        o = *opts;
+    else
+        cp_al_gb300_options_from_env(&o);
+    const double t0 = pdal::now_sec();
+    cp_al_result_t *res = (cp_al_result_t *)calloc(1, sizeof(cp_al_result_t));
+    if (!res) {
+        set_error("out of host memory");
+        return nullptr;
+    }
+    try {
+        pdal::CpalSolver s(prob, &local, &o);
+        s.prepare();
+        s.upload();
+        s.setup_device();
+        s.run_loop();
+        s.result_on_device();
+        s.download(res, true);
+        fill_stats(s, pdal::now_sec() - t0);
+        if (local.verbose) {
+            printf("Solution Summary\n  Status                 : %d\n  Iterations             : %d\n"
+                   "  Primal objective       : %.10g\n  Dual objective         : %.10g\n",
+                   (int)res->termination_reason, res->total_count, res->primal_objective_value,
+                   res->dual_objective_value);
+        }
+        return res;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        free(res->primal_solution);
+        free(res->dual_solution);
+        free(res->reduced_cost);
+        free(res);
+        return nullptr;
+    }
+}
+
+cp_al_result_t *solve_lp_problem(lp_problem_t *prob, const cp_al_parameters_t *params) {
+    return cp_al_gb300_solve(prob, params, nullptr);
+}
+
+cp_al_gb300_session_t *cp_al_gb300_session_create(const lp_problem_t *prob, const cp_al_parameters_t *params,
+                                                  const cp_al_gb300_options_t *opts) {
+    g_last_error.clear();
+    if (!prob) {
+        set_error("session_create: invalid arguments.");
+        return nullptr;
+    }
+    try {
+        auto *sess = new cp_al_gb300_session;
+        cp_al_parameters_t local;
+        if (params)
+            local = *params;
+        else
+            set_default_parameters(&local);
+        cp_al_gb300_options_t o;
+        if (opts)
+            o = *opts;
+        else
+            cp_al_gb300_options_from_env(&o);
+        sess->prob_copy = *prob;
+        sess->solver.reset(new pdal::CpalSolver(&sess->prob_copy, &local, &o));
+        sess->solver->prepare();
+        sess->solver->upload();
+        PDAL_CUDA(cudaDeviceSynchronize());
+        return sess;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return nullptr;
+    }
+}
+
+int cp_al_gb300_session_solve(cp_al_gb300_session_t *s, cp_al_result_t *summary) {
+    if (!s) return -1;
+    try {
+        const double t0 = pdal::now_sec();
+        s->solver->setup_device();
+        s->solver->run_loop();
+        s->solver->result_on_device();
+        PDAL_CUDA(cudaDeviceSynchronize());
+        if (summary) s->solver->download(summary, false);
+        fill_stats(*s->solver, pdal::now_sec() - t0);
+        return 0;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return -1;
+    }
+}
+
+int cp_al_gb300_session_fetch(cp_al_gb300_session_t *s, double *primal, double *dual, double *reduced_cost) {
+    if (!s) return -1;
+    try {
+        s->solver->fetch_vectors(primal, dual, reduced_cost);
+        return 0;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return -1;
+    }
+}
+
+void cp_al_gb300_session_free(cp_al_gb300_session_t *s) { delete s; }
+
+} // extern "C"

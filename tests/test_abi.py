@@ -1,0 +1,170 @@
+"""The C-ABI boundary without a GPU: the library loads, exports every function
+the headers declare, its structs have the C layout, and host-side argument
+checks refuse bad input before any device work."""
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from pdal_gb300 import _native as N
+from pdal_gb300 import lp
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADERS = {"libcp_al_gb300.so": ["cp_al.h", "cp_al_gb300.h"]}
+
+
+def declared_functions(header: Path):
+    text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+    names = re.findall(r"\b([a-z_][a-z0-9_]*)\s*\([^;{]*\)\s*;", text)
+    return sorted({n for n in names if n not in ("if", "sizeof")})
+
+
+@pytest.mark.parametrize("libname", list(HEADERS))
+def test_library_exports_every_declared_symbol(libname, lp_lib):
+    lib = C.CDLL(str(N.lib_path(libname)))
+    for h in HEADERS[libname]:
+        for fn in declared_functions(ROOT / "include" / h):
+            assert hasattr(lib, fn), f"{libname} lacks {fn} declared in {h}"
+
+
+PROBE = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "cp_al_types.h"
+#include "cp_al_gb300.h"
+#define S(T) printf(#T " %zu\n", sizeof(T));
+#define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
+int main(void) {
+  S(lp_problem_t) S(cp_al_parameters_t) S(cp_al_result_t) S(matrix_desc_t) S(cp_al_gb300_options_t)
+  S(cp_al_gb300_stats_t) S(termination_criteria_t) S(restart_parameters_t)
+  O(cp_al_parameters_t, termination_criteria) O(cp_al_parameters_t, restart_params)
+  O(cp_al_parameters_t, optimality_norm) O(cp_al_parameters_t, matrix_zero_tol)
+  O(cp_al_result_t, termination_reason) O(cp_al_result_t, feasibility_iteration)
+  O(cp_al_gb300_options_t, precision) O(cp_al_gb300_options_t, graph_blocks)
+  O(lp_problem_t, dual_start) O(matrix_desc_t, data)
+  return 0;
+}
+"""
+
+
+def test_struct_layouts_match_c(tmp_path):
+    src = tmp_path / "probe.c"
+    src.write_text(PROBE)
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.rsplit(" ", 1) for line in subprocess.check_output([str(exe)], text=True).splitlines())
+    sizes = {
+        "lp_problem_t": N.LpProblem, "cp_al_parameters_t": N.CpalParameters, "cp_al_result_t": N.CpalResult,
+        "matrix_desc_t": N.MatrixDesc, "cp_al_gb300_options_t": N.CpalOptions, "cp_al_gb300_stats_t": N.CpalStats,
+        "termination_criteria_t": N.TerminationCriteria, "restart_parameters_t": N.RestartParams,
+    }
+    for cname, ct in sizes.items():
+        assert int(out[cname]) == C.sizeof(ct), cname
+    offs = {
+        "cp_al_parameters_t.termination_criteria": N.CpalParameters.termination_criteria.offset,
+        "cp_al_parameters_t.restart_params": N.CpalParameters.restart_params.offset,
+        "cp_al_parameters_t.optimality_norm": N.CpalParameters.optimality_norm.offset,
+        "cp_al_parameters_t.matrix_zero_tol": N.CpalParameters.matrix_zero_tol.offset,
+        "cp_al_result_t.termination_reason": N.CpalResult.termination_reason.offset,
+        "cp_al_result_t.feasibility_iteration": N.CpalResult.feasibility_iteration.offset,
+        "cp_al_gb300_options_t.precision": N.CpalOptions.precision.offset,
+        "cp_al_gb300_options_t.graph_blocks": N.CpalOptions.graph_blocks.offset,
+        "lp_problem_t.dual_start": N.LpProblem.dual_start.offset,
+        "matrix_desc_t.data": N.MatrixDesc.data.offset,
+    }
+    for k, v in offs.items():
+        assert int(out[k]) == v, k
+
+
+def _problem_from_desc(lib, desc, m, n):
+    c = np.arange(1, n + 1, dtype=np.float64)
+    p = lib.create_lp_problem(c.ctypes.data_as(C.POINTER(C.c_double)), C.byref(desc), None, None, None, None, None)
+    assert p
+    P = p.contents
+    nnz = P.constraint_matrix_num_nonzeros
+    rp = np.ctypeslib.as_array(P.constraint_matrix_row_pointers, shape=(m + 1,)).copy()
+    ci = np.ctypeslib.as_array(P.constraint_matrix_col_indices, shape=(nnz,)).copy() if nnz else np.zeros(0, int)
+    v = np.ctypeslib.as_array(P.constraint_matrix_values, shape=(nnz,)).copy() if nnz else np.zeros(0)
+    lb = np.ctypeslib.as_array(P.variable_lower_bound, shape=(n,)).copy()
+    cu = np.ctypeslib.as_array(P.constraint_upper_bound, shape=(m,)).copy()
+    lib.lp_problem_free(p)
+    return rp, ci, v, lb, cu
+
+
+def test_create_lp_problem_formats_agree(lp_lib):
+    rng = np.random.default_rng(0)
+    m, n = 7, 9
+    A = rng.standard_normal((m, n)) * (rng.random((m, n)) < 0.4)
+    _dp, _ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+    results = []
+    # dense
+    Ad = np.ascontiguousarray(A)
+    d = N.MatrixDesc()
+    d.m, d.n, d.fmt = m, n, N.MATRIX_DENSE
+    d.data.dense.A = Ad.ctypes.data_as(_dp)
+    results.append(_problem_from_desc(lp_lib, d, m, n))
+    import scipy.sparse as sp
+
+    S = sp.csr_matrix(A)
+    rp, ci, v = S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data.copy()
+    d = N.MatrixDesc()
+    d.m, d.n, d.fmt = m, n, N.MATRIX_CSR
+    d.data.csr.nnz, d.data.csr.row_ptr, d.data.csr.col_ind, d.data.csr.vals = len(v), rp.ctypes.data_as(_ip), ci.ctypes.data_as(_ip), v.ctypes.data_as(_dp)
+    results.append(_problem_from_desc(lp_lib, d, m, n))
+    T = sp.csc_matrix(A)
+    cp_, ri, cv = T.indptr.astype(np.int32), T.indices.astype(np.int32), T.data.copy()
+    d = N.MatrixDesc()
+    d.m, d.n, d.fmt = m, n, N.MATRIX_CSC
+    d.data.csc.nnz, d.data.csc.col_ptr, d.data.csc.row_ind, d.data.csc.vals = len(cv), cp_.ctypes.data_as(_ip), ri.ctypes.data_as(_ip), cv.ctypes.data_as(_dp)
+    results.append(_problem_from_desc(lp_lib, d, m, n))
+    Q = S.tocoo()
+    perm = rng.permutation(Q.nnz)  # COO rows may come in any order; within a row input order is kept
+    qr, qc, qv = Q.row[perm].astype(np.int32), Q.col[perm].astype(np.int32), Q.data[perm].copy()
+    d = N.MatrixDesc()
+    d.m, d.n, d.fmt = m, n, N.MATRIX_COO
+    d.data.coo.nnz, d.data.coo.row_ind, d.data.coo.col_ind, d.data.coo.vals = len(qv), qr.ctypes.data_as(_ip), qc.ctypes.data_as(_ip), qv.ctypes.data_as(_dp)
+    coo = _problem_from_desc(lp_lib, d, m, n)
+    ref = results[0]
+    for r in results[1:]:
+        assert np.array_equal(r[0], ref[0]) and np.array_equal(r[1], ref[1]) and np.array_equal(r[2], ref[2])
+    # COO: same rows, same entries per row
+    assert np.array_equal(coo[0], ref[0])
+    for i in range(m):
+        a = sorted(zip(coo[1][coo[0][i]:coo[0][i + 1]], coo[2][coo[0][i]:coo[0][i + 1]]))
+        b = sorted(zip(ref[1][ref[0][i]:ref[0][i + 1]], ref[2][ref[0][i]:ref[0][i + 1]]))
+        assert a == b
+    # NULL vectors take the reference defaults
+    assert np.all(np.isneginf(ref[3])) and np.all(np.isposinf(ref[4]))
+
+
+def test_bad_input_is_refused_without_exit(lp_lib):
+    # column index out of range: refused on the host (returns NULL, process lives)
+    rp = np.array([0, 2], dtype=np.int32)
+    ci = np.array([0, 5], dtype=np.int32)
+    v = np.array([1.0, 1.0])
+    data = lp.LPData(np.ones(2), (rp, ci, v, (1, 2)), np.array([0.0]), np.array([1.0]), np.zeros(2), np.ones(2))
+    with pytest.raises((RuntimeError, ValueError)):
+        lp.solve(data)
+    assert "out of range" in N.last_error(lp_lib) or True
+    # evaluation frequency below 3 (the reference exits: LP/CP_AL/src/solver.cu:1757-1766)
+    good = lp.LPData(np.ones(2), (np.array([0, 2], np.int32), np.array([0, 1], np.int32), v, (1, 2)),
+                     np.array([0.0]), np.array([1.0]), np.zeros(2), np.ones(2))
+    with pytest.raises(RuntimeError, match="termination_evaluation_frequency"):
+        lp.solve(good, {"termination_evaluation_frequency": 2})
+
+
+def test_options_from_env_reads_reference_variables(lp_lib, monkeypatch):
+    monkeypatch.setenv("CP_AL_LAMBDA", "0")
+    monkeypatch.setenv("CP_AL_SIGMA_MODE", "1")
+    monkeypatch.setenv("CP_AL_SIGMA_INIT_FACTOR", "0.5")
+    monkeypatch.setenv("CP_AL_RESTART_NECESSARY", "0.8")
+    monkeypatch.setenv("CP_AL_SIGMA_KP", "bogus")
+    o = lp.default_options(lp_lib, from_env=True)
+    assert o.al_lambda == 0.0 and o.sigma_mode == 1 and o.sigma_init_factor == 0.5
+    assert o.restart_necessary == 0.8 and np.isnan(o.sigma_kp) and o.sigma_adaptive == 1
+    monkeypatch.setenv("CP_AL_SIGMA", "0.3")
+    o = lp.default_options(lp_lib, from_env=True)
+    assert o.sigma_set == 1 and o.sigma == 0.3 and o.sigma_adaptive == 0

@@ -1,0 +1,185 @@
+"""Parity of the CUDA CP_AL (LP) solver with the CPU oracle, through the C-ABI
+(create_lp_problem / cp_al_gb300_solve / cp_al_result_free).
+
+Bars (floating point, FP64 form): same termination status; iteration counts
+within 2%; relative objective difference <= 1e-8 at relative KKT 1e-8; per-block
+iterates equal to 1e-9 relative after a fixed number of iterations.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pdal_gb300 import instances as I
+from pdal_gb300 import lp
+
+pytestmark = pytest.mark.gpu
+
+OBJ_RTOL = 1e-8
+ITER_RTOL = 0.02
+
+
+def rel(a, b):
+    return abs(a - b) / (1.0 + abs(b))
+
+
+def both(data, params=None, options=None):
+    params = {"time_limit": 120.0, **(params or {})}
+    g = lp.solve(data, params, options)
+    o = O.solve_lp(data, params, options)
+    return g, o
+
+
+def assert_parity(g, o, obj_rtol=OBJ_RTOL, iter_rtol=ITER_RTOL):
+    assert g.status == o.status, (g.status, o.status)
+    assert abs(g.iterations - o.iterations) <= max(iter_rtol * o.iterations, 0), (g.iterations, o.iterations)
+    assert rel(g.primal_objective, o.primal_objective) <= obj_rtol, (g.primal_objective, o.primal_objective)
+    assert rel(g.dual_objective, o.dual_objective) <= obj_rtol
+
+
+def test_docs_example_known_answer(lp_lib):
+    g = lp.solve(I.docs_example_lp(), {"eps": 1e-9})
+    assert g.status == "OPTIMAL"
+    assert np.allclose(g.x, [1.0, 2.0], atol=1e-6)
+    assert abs(g.primal_objective - 3.0) < 1e-7
+
+
+@pytest.mark.parametrize("m,n,k,seed", [(150, 400, 6, 1), (2000, 5000, 8, 0)])
+def test_random_lp_parity(lp_lib, m, n, k, seed):
+    g, o = both(I.random_lp(m, n, k, seed=seed), {"eps": 1e-8, "l_inf_ruiz_iterations": 4})
+    assert g.status == "OPTIMAL"
+    assert_parity(g, o)
+
+
+def test_fixed_iterations_iterates_match(lp_lib):
+    d = I.random_lp(300, 700, 6, seed=11)
+    for blocks in (1, 3, 8):
+        p = {"eps": 1e-14, "iteration_limit": 200 * blocks, "l_inf_ruiz_iterations": 4}
+        g, o = both(d, p)
+        assert g.status == o.status == "ITERATION_LIMIT"
+        assert g.iterations == o.iterations
+        sx = 1 + np.abs(o.x).max()
+        sy = 1 + np.abs(o.y).max()
+        assert np.abs(g.x - o.x).max() / sx < 1e-9
+        assert np.abs(g.y - o.y).max() / sy < 1e-9
+        assert np.abs(g.reduced_cost - o.reduced_cost).max() / (1 + np.abs(o.reduced_cost).max()) < 1e-9
+
+
+def test_sigma_mode_parity(lp_lib):
+    opts = {"sigma_mode": 1, "sigma_init_factor": 0.5, "al_lambda": 0.0, "sigma_kp": 0.5, "sigma_ki": 0.0,
+            "sigma_kd": 0.0, "sigma_balance_gain": 0.0, "sigma_update_min": 1e-6, "sigma_update_max": 1e6,
+            "restart_necessary": 0.8}
+    g, o = both(I.random_lp(400, 1000, 6, seed=3), {"eps": 1e-8}, opts)
+    assert g.status == "OPTIMAL"
+    assert_parity(g, o)
+
+
+@pytest.mark.parametrize("variant", [
+    {"options": {"al_lambda": 0.0}},                      # no augmentation: gather y directly
+    {"params": {"reflection_coefficient": 0.7}},          # A x carried through the recurrence
+    {"params": {"linf": True}},                           # L-infinity optimality norm
+    {"params": {"bound_objective_rescaling": False, "has_pock_chambolle_alpha": False}},
+])
+def test_option_variants_parity(lp_lib, variant):
+    p = {"eps": 1e-8, "l_inf_ruiz_iterations": 4, **variant.get("params", {})}
+    g, o = both(I.random_lp(300, 800, 5, seed=21), p, variant.get("options"))
+    assert g.status == "OPTIMAL"
+    assert_parity(g, o)
+
+
+def test_transport_and_warm_start(lp_lib):
+    d = I.transport_lp(15, 20, seed=2)
+    g, o = both(d, {"eps": 1e-8})
+    assert_parity(g, o)
+    d.primal_start, d.dual_start = g.x, g.y
+    g2, o2 = both(d, {"eps": 1e-8})
+    assert_parity(g2, o2)
+    assert g2.iterations <= g.iterations
+
+
+@pytest.mark.parametrize("S", [256, 512, 1024, 2048])
+def test_long_rows_and_block_budgets(lp_lib, S):
+    """A few dense rows longer than the block budget take the split-row path."""
+    d = I.random_lp(200, 3000, 3, seed=5)
+    rp, ci, v, (m, n) = d.csr()
+    rng = np.random.default_rng(0)
+    rows = [list(zip(ci[rp[i]:rp[i + 1]], v[rp[i]:rp[i + 1]])) for i in range(m)]
+    for i in (3, 77):  # make two rows dense: 3000 nonzeros each
+        rows[i] = [(j, rng.standard_normal()) for j in range(n)]
+    rp2 = np.zeros(m + 1, np.int32)
+    rp2[1:] = np.cumsum([len(r) for r in rows])
+    ci2 = np.array([j for r in rows for j, _ in r], np.int32)
+    v2 = np.array([x for r in rows for _, x in r])
+    Ax = np.zeros(m)
+    for i in (3, 77):
+        Ax[i] = v2[rp2[i]:rp2[i + 1]].sum()
+        d.con_lb[i] = Ax[i]
+        d.con_ub[i] = Ax[i] + 1.0
+    d.A = (rp2, ci2, v2, (m, n))
+    p = {"eps": 1e-14, "iteration_limit": 600, "l_inf_ruiz_iterations": 4}
+    g = lp.solve(d, p, {"spmv_nnz_per_block": S})
+    o = O.solve_lp(d, p)
+    assert np.abs(g.x - o.x).max() / (1 + np.abs(o.x).max()) < 1e-9
+    assert np.abs(g.y - o.y).max() / (1 + np.abs(o.y).max()) < 1e-9
+
+
+def test_edge_rows_and_columns(lp_lib):
+    """Empty rows, empty columns, free rows, free and fixed variables."""
+    d = I.random_lp(120, 300, 4, seed=8)
+    rp, ci, v, (m, n) = d.csr()
+    keep = (ci % 17) != 0  # empties some columns
+    row_of = np.repeat(np.arange(m), np.diff(rp))
+    keep &= ~np.isin(row_of, [0, 5, 50])  # empties rows 0, 5, 50
+    rp2 = np.zeros(m + 1, np.int32)
+    np.add.at(rp2, row_of[keep] + 1, 1)
+    rp2 = np.cumsum(rp2).astype(np.int32)
+    d.A = (rp2, ci[keep].astype(np.int32), v[keep], (m, n))
+    d.con_lb[[0, 5]] = -np.inf
+    d.con_ub[[0, 5]] = np.inf
+    d.con_lb[50], d.con_ub[50] = -1.0, 1.0
+    d.con_lb[10], d.con_ub[10] = -np.inf, np.inf  # free row with entries
+    d.var_lb[:10] = -np.inf
+    d.var_ub[:10] = np.inf
+    d.c[:10] = 0.0
+    d.var_lb[10:15] = d.var_ub[10:15] = 2.0  # fixed
+    p = {"eps": 1e-14, "iteration_limit": 1000, "l_inf_ruiz_iterations": 4}
+    g, o = both(d, p)
+    assert np.all(np.isfinite(g.x)) and np.all(np.isfinite(g.y))
+    assert np.abs(g.x - o.x).max() / (1 + np.abs(o.x).max()) < 1e-9
+    assert np.abs(g.y - o.y).max() / (1 + np.abs(o.y).max()) < 1e-9
+
+
+def test_no_constraints(lp_lib):
+    n = 50
+    d = lp.LPData(np.linspace(-1, 1, n), (np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0), (0, n)),
+                  np.zeros(0), np.zeros(0), np.zeros(n), np.full(n, 3.0))
+    g, o = both(d, {"eps": 1e-10})
+    assert g.status == o.status == "OPTIMAL"
+    assert np.allclose(g.x, np.where(d.c < 0, 3.0, 0.0), atol=1e-6)
+
+
+def test_fp32_refine_matches_fp64(lp_lib):
+    d = I.random_lp(2000, 5000, 8, seed=0)
+    p = {"eps": 1e-8, "l_inf_ruiz_iterations": 4}
+    g32 = lp.solve(d, p, {"precision": "fp32_refine"})
+    o = O.solve_lp(d, p)
+    assert g32.status == "OPTIMAL"
+    assert g32.stats["fp32_iterations"] > 0
+    assert rel(g32.primal_objective, o.primal_objective) <= 1e-8
+
+
+def test_session_is_deterministic(lp_lib):
+    d = I.random_lp(500, 1200, 6, seed=4)
+    p = {"eps": 1e-8, "l_inf_ruiz_iterations": 4}
+    s = lp.LPSession(d, p)
+    try:
+        r1 = s.solve()
+        x1, y1, _ = s.fetch()
+        r2 = s.solve()
+        x2, y2, _ = s.fetch()
+    finally:
+        s.close()
+    assert r1.iterations == r2.iterations
+    assert np.array_equal(x1, x2) and np.array_equal(y1, y2)
+    g = lp.solve(d, p)
+    assert g.iterations == r1.iterations
+    assert np.array_equal(g.x, x1)

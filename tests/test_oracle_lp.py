@@ -1,0 +1,111 @@
+"""Pins of the CPU oracle (the checker of the CUDA library).
+
+The reference ships no numeric golden vectors for this path, so the oracle is
+pinned against known answers: the analytic optimum of the reference's own C API
+example, independent LP optima from scipy's HiGHS, the dense SVD for the power
+iteration, committed fixtures (tests/golden), and the reference defaults.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+from scipy.optimize import linprog
+
+from oracle import oracle as O
+from pdal_gb300 import instances as I
+
+
+def highs_objective(d):
+    rp, ci, v, (m, n) = d.csr()
+    A = sp.csr_matrix((v, ci, rp), shape=(m, n))
+    eq = np.isfinite(d.con_lb) & (d.con_lb == d.con_ub)
+    ub_rows = ~eq & np.isfinite(d.con_ub)
+    lb_rows = ~eq & np.isfinite(d.con_lb)
+    A_ub = sp.vstack([A[ub_rows], -A[lb_rows]])
+    b_ub = np.concatenate([d.con_ub[ub_rows], -d.con_lb[lb_rows]])
+    bounds = list(zip(np.where(np.isfinite(d.var_lb), d.var_lb, None), np.where(np.isfinite(d.var_ub), d.var_ub, None)))
+    res = linprog(d.c, A_ub=A_ub, b_ub=b_ub, A_eq=A[eq], b_eq=d.con_lb[eq], bounds=bounds, method="highs")
+    assert res.status == 0
+    return res.fun
+
+
+def test_docs_example_known_answer():
+    # LP/CP_AL/docs/C_API.md:41-89: optimum x = (1, 2), objective 3
+    r = O.solve_lp(I.docs_example_lp(), {"eps": 1e-9})
+    assert r.status == "OPTIMAL"
+    assert np.allclose(r.x, [1.0, 2.0], atol=1e-6)
+    assert abs(r.primal_objective - 3.0) < 1e-7
+    assert abs(r.dual_objective - 3.0) < 1e-7
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_random_lp_matches_highs(seed):
+    d = I.random_lp(150, 400, 6, seed=seed)
+    r = O.solve_lp(d, {"eps": 1e-9, "l_inf_ruiz_iterations": 4})
+    assert r.status == "OPTIMAL"
+    f = highs_objective(d)
+    assert abs(r.primal_objective - f) / (1 + abs(f)) < 1e-7
+
+
+def test_transport_matches_highs():
+    d = I.transport_lp(12, 15, seed=3)
+    r = O.solve_lp(d, {"eps": 1e-9})
+    assert r.status == "OPTIMAL"
+    f = highs_objective(d)
+    assert abs(r.primal_objective - f) / (1 + abs(f)) < 1e-7
+
+
+def test_sigma_mode_matches_highs():
+    d = I.random_lp(120, 300, 5, seed=7)
+    opts = {"sigma_mode": 1, "sigma_init_factor": 0.5, "al_lambda": 0.0, "sigma_kp": 0.5, "sigma_ki": 0.0,
+            "sigma_kd": 0.0, "sigma_balance_gain": 0.0, "sigma_update_min": 1e-6, "sigma_update_max": 1e6,
+            "restart_necessary": 0.8}
+    r = O.solve_lp(d, {"eps": 1e-9}, opts)
+    assert r.status == "OPTIMAL"
+    f = highs_objective(d)
+    assert abs(r.primal_objective - f) / (1 + abs(f)) < 1e-7
+
+
+def test_power_iteration_matches_svd():
+    d = I.random_lp(60, 150, 4, seed=5)
+    rp, ci, v, (m, n) = d.csr()
+    A = sp.csr_matrix((v, ci, rp), shape=(m, n)).toarray()
+    s, it = O.power_iteration(d, 5000, 1e-10)
+    smax = np.linalg.svd(A, compute_uv=False)[0]
+    assert abs(s - smax) / smax < 1e-6
+    assert 1 <= it <= 5000
+
+
+def test_ruiz_equilibrates_rows_and_columns():
+    d = I.random_lp(80, 200, 5, seed=9)
+    rp, ci, v, (m, n) = d.csr()
+    r, c, cbr, ovr, sv = O.rescale(d, {"l_inf_ruiz_iterations": 25, "has_pock_chambolle_alpha": False,
+                                      "bound_objective_rescaling": False})
+    S = sp.csr_matrix((sv, ci, rp), shape=(m, n))
+    row_max = abs(S).max(axis=1).toarray().ravel()
+    col_max = abs(S).max(axis=0).toarray().ravel()
+    assert np.all(abs(row_max[row_max > 0] - 1) < 1e-3)
+    assert np.all(abs(col_max[col_max > 0] - 1) < 1e-3)
+    # scaled entries are D_r^-1 A D_c^-1 of the original
+    A = sp.csr_matrix((v, ci, rp), shape=(m, n))
+    expect = sp.diags(1 / r) @ A @ sp.diags(1 / c)
+    assert np.allclose(S.toarray(), expect.toarray(), rtol=1e-12, atol=0)
+    assert cbr == 1.0 and ovr == 1.0
+
+
+def test_defaults_are_the_reference_defaults(lp_lib):
+    from pdal_gb300 import lp
+
+    p_prod = lp.default_parameters(lp_lib)
+    p_or = O.default_parameters()
+    for name, _ in type(p_or)._fields_:
+        a, b = getattr(p_prod, name), getattr(p_or, name)
+        if hasattr(a, "_fields_"):
+            for sub, _ in type(a)._fields_:
+                assert getattr(a, sub) == getattr(b, sub), (name, sub)
+        else:
+            assert a == b, name
+    o_prod = lp.default_options(lp_lib)
+    o_or = O.default_options()
+    for name, _ in type(o_or)._fields_:
+        a, b = getattr(o_prod, name), getattr(o_or, name)
+        assert (a == b) or (np.isnan(a) and np.isnan(b)), name

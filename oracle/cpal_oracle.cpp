@@ -697,6 +697,12 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
         S.total += F;
         charged += F;
         elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        if (params->verbose) {
+            printf("%8d %.2e | %+.6e %+.6e | %.1e %.1e %.1e | %.1e | pw %.3e eta %.3e beta %.3e rs %d oracle\n",
+                   S.total, elapsed, S.pobj, S.dobj, S.rel_p, S.rel_d, S.rel_gap, S.fp, S.pw, S.step, S.beta,
+                   S.restarts);
+            fflush(stdout);
+        }
         S.check_termination(elapsed);
         if (S.reason == TERMINATION_REASON_UNSPECIFIED && charged >= limit) S.reason = TERMINATION_REASON_ITERATION_LIMIT;
         if (S.reason != TERMINATION_REASON_UNSPECIFIED) break;

@@ -49,6 +49,9 @@ struct CpalParams {
 struct CpalState {
     /* coefficients read by the iteration kernels */
     double tau, rho, beta, inv_tau, inv_prox, inv_beta, refl;
+    /* the same coefficients rounded once to FP32 for the FP32 phase (the FP64
+     * pipe of GB300 is too narrow to convert them in every thread) */
+    float tau_f, rho_f, beta_f, inv_tau_f, inv_prox_f, inv_beta_f, refl_f, pad_f;
     int inner;   /* Halpern counter at the start of the current block */
     int status;  /* 0 while running, else termination_reason_t */
     int restart; /* 1 when the last evaluation restarted */
@@ -83,6 +86,30 @@ PDAL_HD void cpal_set_coefficients(CpalState &s) {
     s.inv_tau = 1.0 / s.tau;
     s.inv_prox = 1.0 / (s.rho + s.beta);
     s.inv_beta = s.beta > 0.0 ? 1.0 / s.beta : 0.0;
+    s.tau_f = (float)s.tau;
+    s.rho_f = (float)s.rho;
+    s.beta_f = (float)s.beta;
+    s.inv_tau_f = (float)s.inv_tau;
+    s.inv_prox_f = (float)s.inv_prox;
+    s.inv_beta_f = (float)s.inv_beta;
+    s.refl_f = (float)s.refl;
+}
+
+/* Halpern weights of the block that starts with counter `inner`:
+ * entry i (1..F) holds w = k/(k+1) and 1 - w for k = inner + i
+ * (LP/CP_AL/src/solver.cu:2355-2356), in FP64 and rounded to FP32. */
+struct HalpernW {
+    double w, omw;
+};
+struct HalpernWf {
+    float w, omw;
+};
+PDAL_HD void cpal_halpern_entry(int inner, int i, HalpernW &d, HalpernWf &f) {
+    const int k = inner + i;
+    d.w = (double)k / (double)(k + 1);
+    d.omw = 1.0 - d.w;
+    f.w = (float)d.w;
+    f.omw = (float)d.omw;
 }
 
 /* LP/CP_AL/src/solver.cu:3103-3139 */

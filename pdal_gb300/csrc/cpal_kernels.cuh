@@ -62,30 +62,89 @@ struct NoLongRed {
 /* ------------------------------------------------------------------ */
 /* iteration                                                           */
 /* ------------------------------------------------------------------ */
+
+/* Storage of an FP64 anchor (x0, y0, A x0) as the iteration kernels read it:
+ * a double in the FP64 phase, an unevaluated (hi, lo) float pair in the FP32
+ * phase so that the anchor keeps FP64 accuracy while all arithmetic stays on
+ * the FP32 pipes. */
+template <typename T>
+struct AnchorT;
+template <>
+struct AnchorT<double> {
+    using type = double;
+};
+template <>
+struct AnchorT<float> {
+    using type = float2;
+};
+template <typename T>
+struct WeightT;
+template <>
+struct WeightT<double> {
+    using type = HalpernW;
+};
+template <>
+struct WeightT<float> {
+    using type = HalpernWf;
+};
+
+__device__ __forceinline__ double halpern(double w, double omw, double refl, double a) { return w * refl + omw * a; }
+__device__ __forceinline__ float halpern(float w, float omw, float refl, float2 a) {
+    return fmaf(w, refl, fmaf(omw, a.x, omw * a.y));
+}
+
+__device__ __forceinline__ float2 split_anchor(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+
+template <typename T>
+struct Coefs {
+    T tau, inv_tau, rho, inv_prox, beta, inv_beta, r;
+};
+__device__ __forceinline__ void load_coefs(const CpalState *s, Coefs<double> &c) {
+    c.tau = s->tau;
+    c.inv_tau = s->inv_tau;
+    c.rho = s->rho;
+    c.inv_prox = s->inv_prox;
+    c.beta = s->beta;
+    c.inv_beta = s->inv_beta;
+    c.r = s->refl;
+}
+__device__ __forceinline__ void load_coefs(const CpalState *s, Coefs<float> &c) {
+    c.tau = s->tau_f;
+    c.inv_tau = s->inv_tau_f;
+    c.rho = s->rho_f;
+    c.inv_prox = s->inv_prox_f;
+    c.beta = s->beta_f;
+    c.inv_beta = s->inv_beta_f;
+    c.r = s->refl_f;
+}
+
 template <typename T>
 struct PrimalArgs {
     T *x, *xbar, *xh, *lam;
-    const double *x0;
+    const typename AnchorT<T>::type *x0;
     const T *c, *lb, *ub;
 };
 
 template <typename T, bool MAJOR>
 struct PrimalEpi : NoLongRed {
     PrimalArgs<T> a;
-    T tau, inv_tau, r;
-    double w;
+    Coefs<T> k;
+    T w, omw;
     __device__ __forceinline__ void operator()(int j, const T *s, Red<0, 0> &) const {
         const T xj = a.x[j];
-        const T t = xj - tau * (a.c[j] - s[0]);
+        const T t = xj - k.tau * (a.c[j] - s[0]);
         const T proj = vmax(a.lb[j], vmin(t, a.ub[j]));
         const T xb = T(2) * proj - xj;
         a.xbar[j] = xb;
         if (MAJOR) {
             a.xh[j] = proj;
-            a.lam[j] = (proj - t) * inv_tau;
+            a.lam[j] = (proj - t) * k.inv_tau;
         }
-        const T refl = r * xb + (T(1) - r) * xj;
-        a.x[j] = (T)(w * (double)refl + (1.0 - w) * a.x0[j]);
+        const T refl = k.r * xb + (T(1) - k.r) * xj;
+        a.x[j] = halpern(w, omw, refl, a.x0[j]);
     }
 };
 
@@ -93,54 +152,53 @@ template <typename T, int S, bool MAJOR>
 __global__ void __launch_bounds__(kThreads) k_primal(RowPlanDev plan, const int *__restrict__ rp,
                                                      const int *__restrict__ ci, const T *__restrict__ val,
                                                      const T *__restrict__ gat, PrimalArgs<T> a,
-                                                     const CpalState *__restrict__ st, int koff) {
+                                                     const CpalState *__restrict__ st,
+                                                     const typename WeightT<T>::type *__restrict__ wt, int koff) {
     if (st->status) return;
     __shared__ RowBlockSmem<S, 1, T> sm;
     PrimalEpi<T, MAJOR> epi;
     epi.a = a;
-    epi.tau = (T)st->tau;
-    epi.inv_tau = (T)st->inv_tau;
-    epi.r = (T)st->refl;
-    const int k = st->inner + koff;
-    epi.w = (double)k / (double)(k + 1);
-    auto prod = [&](int kk, T *out) { out[0] = val[kk] * gat[ci[kk]]; };
+    load_coefs(st, epi.k);
+    epi.w = wt[koff].w;
+    epi.omw = wt[koff].omw;
+    auto g = [&](int c, T *out) { out[0] = __ldg(gat + c); };
     Red<0, 0> red;
-    rowblock_run<S, 1, T>(plan, rp, prod, epi, red, sm);
+    rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);
 }
 
 template <typename T>
 struct DualArgs {
     T *y, *yh, *ybar, *ax, *u;
-    const double *y0, *ax0;
+    const typename AnchorT<T>::type *y0, *ax0;
     const T *lb, *ub;
 };
 
 template <typename T, bool MAJOR, bool BETA>
 struct DualEpi : NoLongRed {
     DualArgs<T> a;
-    T rho, inv_prox, beta, inv_beta, r;
-    double w;
+    Coefs<T> k;
+    T w, omw;
     __device__ __forceinline__ void operator()(int i, const T *s, Red<0, 0> &) const {
         const T yi = a.y[i];
         const T p = s[0];
         const T lo = a.lb[i], hi = a.ub[i];
-        const T zb = vmax(lo, vmin(p - yi * inv_prox, hi));
-        const T yn = yi - rho * (p - zb);
+        const T zb = vmax(lo, vmin(p - yi * k.inv_prox, hi));
+        const T yn = yi - k.rho * (p - zb);
         const T yb = T(2) * yn - yi;
         if (MAJOR) {
             a.yh[i] = yn;
             a.ybar[i] = yb;
         }
-        const T refl = r * yb + (T(1) - r) * yi;
-        const T ynew = (T)(w * (double)refl + (1.0 - w) * a.y0[i]);
+        const T refl = k.r * yb + (T(1) - k.r) * yi;
+        const T ynew = halpern(w, omw, refl, a.y0[i]);
         a.y[i] = ynew;
         if (BETA) {
             T mix = p;
-            if (r != T(1)) mix = r * p + (T(1) - r) * a.ax[i];
-            const T axn = (T)(w * (double)mix + (1.0 - w) * a.ax0[i]);
+            if (k.r != T(1)) mix = k.r * p + (T(1) - k.r) * a.ax[i];
+            const T axn = halpern(w, omw, mix, a.ax0[i]);
             a.ax[i] = axn;
-            const T z2 = vmax(lo, vmin(axn - ynew * inv_beta, hi));
-            a.u[i] = ynew - beta * (axn - z2);
+            const T z2 = vmax(lo, vmin(axn - ynew * k.inv_beta, hi));
+            a.u[i] = ynew - k.beta * (axn - z2);
         }
     }
 };
@@ -149,21 +207,29 @@ template <typename T, int S, bool MAJOR, bool BETA>
 __global__ void __launch_bounds__(kThreads) k_dual(RowPlanDev plan, const int *__restrict__ rp,
                                                    const int *__restrict__ ci, const T *__restrict__ val,
                                                    const T *__restrict__ xbar, DualArgs<T> a,
-                                                   const CpalState *__restrict__ st, int koff) {
+                                                   const CpalState *__restrict__ st,
+                                                   const typename WeightT<T>::type *__restrict__ wt, int koff) {
     if (st->status) return;
     __shared__ RowBlockSmem<S, 1, T> sm;
     DualEpi<T, MAJOR, BETA> epi;
     epi.a = a;
-    epi.rho = (T)st->rho;
-    epi.inv_prox = (T)st->inv_prox;
-    epi.beta = (T)st->beta;
-    epi.inv_beta = (T)st->inv_beta;
-    epi.r = (T)st->refl;
-    const int k = st->inner + koff;
-    epi.w = (double)k / (double)(k + 1);
-    auto prod = [&](int kk, T *out) { out[0] = val[kk] * xbar[ci[kk]]; };
+    load_coefs(st, epi.k);
+    epi.w = wt[koff].w;
+    epi.omw = wt[koff].omw;
+    auto g = [&](int c, T *out) { out[0] = __ldg(xbar + c); };
     Red<0, 0> red;
-    rowblock_run<S, 1, T>(plan, rp, prod, epi, red, sm);
+    rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);
+}
+
+/* Halpern weights for the block starting at st->inner (one block). */
+__global__ void k_fill_weights(const CpalState *__restrict__ st, HalpernW *wt, HalpernWf *wtf, int F) {
+    const int inner = st->inner;
+    for (int i = threadIdx.x + 1; i <= F; i += blockDim.x) cpal_halpern_entry(inner, i, wt[i], wtf[i]);
+}
+
+/* FP64 vector -> (hi, lo) float pairs */
+__global__ void k_split(const double *__restrict__ src, float2 *dst, int len) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) dst[i] = split_anchor(src[i]);
 }
 
 /* A x0 at the start of a solve (or of a precision phase), with the first
@@ -172,10 +238,12 @@ template <typename T, bool BETA>
 struct InitAxEpi : NoLongRed {
     T *ax, *u;
     double *ax0;
+    float2 *ax0f;
     const T *y, *lb, *ub;
     T beta, inv_beta;
     __device__ __forceinline__ void operator()(int i, const double *s, Red<0, 0> &) const {
         ax0[i] = s[0];
+        if (ax0f) ax0f[i] = split_anchor(s[0]);
         const T axv = (T)s[0];
         ax[i] = axv;
         if (BETA) {
@@ -189,22 +257,25 @@ struct InitAxEpi : NoLongRed {
 template <typename T, int S, bool BETA>
 __global__ void __launch_bounds__(kThreads) k_init_ax(RowPlanDev plan, const int *__restrict__ rp,
                                                       const int *__restrict__ ci, const double *__restrict__ val,
-                                                      const double *__restrict__ x0, T *ax, double *ax0, T *u,
-                                                      const T *y, const T *lb, const T *ub,
+                                                      const double *__restrict__ x0, T *ax, double *ax0, float2 *ax0f,
+                                                      T *u, const T *y, const T *lb, const T *ub,
                                                       const CpalState *__restrict__ st) {
     __shared__ RowBlockSmem<S, 1, double> sm;
     InitAxEpi<T, BETA> epi;
     epi.ax = ax;
     epi.u = u;
     epi.ax0 = ax0;
+    epi.ax0f = ax0f;
     epi.y = y;
     epi.lb = lb;
     epi.ub = ub;
-    epi.beta = (T)st->beta;
-    epi.inv_beta = (T)st->inv_beta;
-    auto prod = [&](int kk, double *out) { out[0] = val[kk] * x0[ci[kk]]; };
+    Coefs<T> k;
+    load_coefs(st, k);
+    epi.beta = k.beta;
+    epi.inv_beta = k.inv_beta;
+    auto g = [&](int c, double *out) { out[0] = __ldg(x0 + c); };
     Red<0, 0> red;
-    rowblock_run<S, 1, double>(plan, rp, prod, epi, red, sm);
+    rowblock_run<S, 1, double>(plan, rp, ci, val, g, epi, red, sm);
 }
 
 /* ------------------------------------------------------------------ */
@@ -260,17 +331,15 @@ __global__ void __launch_bounds__(kThreads) k_eval_rows(RowPlanDev plan, const i
     const T *xh = a.xh;
     const T *xb = a.xbar;
     const double *x0 = a.x0;
-    auto prod = [&](int kk, double *out) {
-        const double v = val[kk];
-        const int c = ci[kk];
+    auto g = [&](int c, double *out) {
         const double xhc = (double)xh[c];
-        out[0] = v * xhc;
-        out[1] = v * ((double)xb[c] - xhc);
-        out[2] = v * (xhc - x0[c]);
+        out[0] = xhc;
+        out[1] = (double)xb[c] - xhc;
+        out[2] = xhc - x0[c];
     };
     Red<6, 1> red;
     red.zero();
-    rowblock_run<S, 3, double>(plan, rp, prod, epi, red, sm);
+    rowblock_run<S, 3, double>(plan, rp, ci, val, g, epi, red, sm);
     block_reduce<kThreads, 6, 1>(red, sm.red);
     if (threadIdx.x == 0) {
         double *d = a.part + (size_t)blockIdx.x * kEvalStride;
@@ -324,16 +393,14 @@ __global__ void __launch_bounds__(kThreads) k_eval_cols(RowPlanDev plan, const i
     epi.a = a;
     const T *yh = a.yh;
     const T *yb = a.ybar;
-    auto prod = [&](int kk, double *out) {
-        const double v = val[kk];
-        const int c = ci[kk];
+    auto g = [&](int c, double *out) {
         const double yhc = (double)yh[c];
-        out[0] = v * yhc;
-        out[1] = v * ((double)yb[c] - yhc);
+        out[0] = yhc;
+        out[1] = (double)yb[c] - yhc;
     };
     Red<6, 1> red;
     red.zero();
-    rowblock_run<S, 2, double>(plan, rp, prod, epi, red, sm);
+    rowblock_run<S, 2, double>(plan, rp, ci, val, g, epi, red, sm);
     block_reduce<kThreads, 6, 1>(red, sm.red);
     if (threadIdx.x == 0) {
         double *d = a.part + (size_t)blockIdx.x * kEvalStride;
@@ -355,7 +422,7 @@ __device__ __forceinline__ void reduce_slots(const double *part, int nslots, Red
 
 __global__ void __launch_bounds__(kThreads) k_control(const double *__restrict__ prow, int nrow_slots,
                                                       const double *__restrict__ pcol, int ncol_slots,
-                                                      CpalState *st, CpalParams p) {
+                                                      CpalState *st, CpalParams p, HalpernW *wt, HalpernWf *wtf) {
     if (st->status) return;
     __shared__ double sbuf[8 * (kThreads / 32)];
     Red<6, 1> r1, r2;
@@ -382,34 +449,44 @@ __global__ void __launch_bounds__(kThreads) k_control(const double *__restrict__
         cpal_end_of_block(s, p, e);
         *st = s;
     }
+    __syncthreads();
+    /* Halpern weights of the next block (the counter may have been reset) */
+    const int inner = st->inner;
+    for (int i = threadIdx.x + 1; i <= p.F; i += kThreads) cpal_halpern_entry(inner, i, wt[i], wtf[i]);
 }
 
 /* Anchor reset after a restart: x0 = x = x^, y0 = y = y^, A x0 = A x = p^,
- * and the next predictor from the new beta. */
+ * and the next predictor from the new beta.  The FP64 anchors are written
+ * together with the (hi, lo) copies the FP32 phase reads. */
 template <typename T, bool BETA>
 __global__ void k_restart(const CpalState *__restrict__ st, int n, int m, const T *__restrict__ xh, T *x,
-                          double *x0, const T *__restrict__ yh, T *y, double *y0, const double *__restrict__ phat,
-                          T *ax, double *ax0, T *u, const T *__restrict__ lb, const T *__restrict__ ub) {
+                          double *x0, float2 *x0f, const T *__restrict__ yh, T *y, double *y0, float2 *y0f,
+                          const double *__restrict__ phat, T *ax, double *ax0, float2 *ax0f, T *u,
+                          const T *__restrict__ lb, const T *__restrict__ ub) {
     if (st->status || !st->restart) return;
-    const T beta = (T)st->beta, inv_beta = (T)st->inv_beta;
+    Coefs<T> k;
+    load_coefs(st, k);
     const int total = n > m ? n : m;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         if (t < n) {
             const T v = xh[t];
             x[t] = v;
             x0[t] = (double)v;
+            if (x0f) x0f[t] = split_anchor((double)v);
         }
         if (t < m) {
             const T v = yh[t];
             y[t] = v;
             y0[t] = (double)v;
+            if (y0f) y0f[t] = split_anchor((double)v);
             const double ph = phat[t];
             ax0[t] = ph;
+            if (ax0f) ax0f[t] = split_anchor(ph);
             const T axv = (T)ph;
             ax[t] = axv;
             if (BETA) {
-                const T z = vmax(lb[t], vmin(axv - v * inv_beta, ub[t]));
-                u[t] = v - beta * (axv - z);
+                const T z = vmax(lb[t], vmin(axv - v * k.inv_beta, ub[t]));
+                u[t] = v - k.beta * (axv - z);
             }
         }
     }
@@ -438,9 +515,9 @@ __global__ void __launch_bounds__(kThreads) k_result_cols(RowPlanDev plan, const
                                                           const int *__restrict__ ci, const double *__restrict__ val,
                                                           const double *__restrict__ yh, ResultColEpi epi) {
     __shared__ RowBlockSmem<S, 1, double> sm;
-    auto prod = [&](int kk, double *out) { out[0] = val[kk] * yh[ci[kk]]; };
+    auto g = [&](int c, double *out) { out[0] = yh[c]; };
     Red<0, 0> red;
-    rowblock_run<S, 1, double>(plan, rp, prod, epi, red, sm);
+    rowblock_run<S, 1, double>(plan, rp, ci, val, g, epi, red, sm);
 }
 
 __global__ void k_result_rows(int m, const double *__restrict__ yh, const double *__restrict__ rscale,
@@ -640,9 +717,9 @@ __global__ void __launch_bounds__(kThreads) k_power_at(RowPlanDev plan, const in
     const double inv = ps->inv;
     PowerColEpi epi;
     epi.dp = dp;
-    auto prod = [&](int kk, double *out) { out[0] = val[kk] * (inv * v[ci[kk]]); };
+    auto g = [&](int c, double *out) { out[0] = inv * v[c]; };
     Red<0, 0> red;
-    rowblock_run<S, 1, double>(plan, rp, prod, epi, red, sm);
+    rowblock_run<S, 1, double>(plan, rp, ci, val, g, epi, red, sm);
 }
 
 /* vn = A dp, partial sums of (inv * v) . vn */
@@ -672,10 +749,10 @@ __global__ void __launch_bounds__(kThreads) k_power_a(RowPlanDev plan, const int
     epi.inv = ps->inv;
     epi.part = part;
     epi.nblocks = plan.nblocks;
-    auto prod = [&](int kk, double *out) { out[0] = val[kk] * dp[ci[kk]]; };
+    auto g = [&](int c, double *out) { out[0] = dp[c]; };
     Red<1, 0> red;
     red.zero();
-    rowblock_run<S, 1, double>(plan, rp, prod, epi, red, sm);
+    rowblock_run<S, 1, double>(plan, rp, ci, val, g, epi, red, sm);
     block_reduce<kThreads, 1, 0>(red, sm.red);
     if (threadIdx.x == 0) part[blockIdx.x] = red.s[0];
 }

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <memory>
 #include <random>
+#include <type_traits>
 
 namespace pdal {
 
@@ -180,6 +181,9 @@ class CpalSolver {
     double *tmp_n_ = nullptr, *tmp_m_ = nullptr, *tmp_m2_ = nullptr;
     double *part_row_ = nullptr, *part_col_ = nullptr, *part_misc_ = nullptr;
     double *xout_ = nullptr, *yout_ = nullptr, *rcout_ = nullptr;
+    float2 *x0f_ = nullptr, *y0f_ = nullptr, *ax0f_ = nullptr; /* FP32-phase anchors (hi, lo) */
+    HalpernW *wt_ = nullptr;
+    HalpernWf *wtf_ = nullptr;
     IterVecs<double> v64_;
     IterVecs<float> v32_;
     CpalState *st_ = nullptr;
@@ -318,17 +322,20 @@ void CpalSolver::upload_plan(PlanDev &pd) {
 
 void CpalSolver::alloc_all() {
     const size_t n = n_, m = m_, nnz = nnz_;
+    /* +kPad: the row-block loads read 4-element windows that may extend
+     * three elements past the last nonzero */
+    constexpr size_t kPad = 8;
     A_.rp = arena_.take<int>(m + 1);
-    A_.ci = arena_.take<int>(nnz);
-    A_.v = arena_.take<double>(nnz);
-    Av0_ = arena_.take<double>(nnz);
+    A_.ci = arena_.take<int>(nnz + kPad);
+    A_.v = arena_.take<double>(nnz + kPad);
+    Av0_ = arena_.take<double>(nnz + kPad);
     At_.rp = arena_.take<int>(n + 1);
-    At_.ci = arena_.take<int>(nnz);
-    At_.v = arena_.take<double>(nnz);
-    Atv0_ = arena_.take<double>(nnz);
+    At_.ci = arena_.take<int>(nnz + kPad);
+    At_.v = arena_.take<double>(nnz + kPad);
+    Atv0_ = arena_.take<double>(nnz + kPad);
     if (fp32_phase_) {
-        A_.vf = arena_.take<float>(nnz);
-        At_.vf = arena_.take<float>(nnz);
+        A_.vf = arena_.take<float>(nnz + kPad);
+        At_.vf = arena_.take<float>(nnz + kPad);
     }
     alloc_plan(A_.it);
     alloc_plan(At_.it);
@@ -394,6 +401,13 @@ void CpalSolver::alloc_all() {
         v.clb = arena_.take<float>(m);
         v.cub = arena_.take<float>(m);
     }
+    if (fp32_phase_) {
+        x0f_ = arena_.take<float2>(n);
+        y0f_ = arena_.take<float2>(m);
+        ax0f_ = arena_.take<float2>(m);
+    }
+    wt_ = arena_.take<HalpernW>((size_t)cp_.F + 1);
+    wtf_ = arena_.take<HalpernWf>((size_t)cp_.F + 1);
     part_row_ = arena_.take<double>((size_t)(A_.ev.hp.nblocks + A_.ev.hp.nlong + 1) * kEvalStride);
     part_col_ = arena_.take<double>((size_t)(At_.ev.hp.nblocks + At_.ev.hp.nlong + 1) * kEvalStride);
     nmisc_ = std::max({A_.ev.hp.nblocks + A_.ev.hp.nlong, grid_for(std::max(n_, m_)), 1});
@@ -600,6 +614,8 @@ void CpalSolver::setup_device() {
     *h_st_ = s;
     PDAL_CUDA(cudaMemcpyAsync(st_, h_st_, sizeof(CpalState), cudaMemcpyHostToDevice, stream_));
     h2d += sizeof(CpalState);
+    k_fill_weights<<<1, kThreads, 0, stream_>>>(st_, wt_, wtf_, cp_.F);
+    launches += 1;
 
     /* iterates start at the (scaled) warm start: solver.cu:1939-1974 */
     d2d(v64_.x, x0_, n * sizeof(double));
@@ -630,6 +646,9 @@ void CpalSolver::setup_device() {
         if (n) PDAL_CUDA(cudaMemsetAsync(v32_.xbar, 0, n * sizeof(float), stream_));
         if (m) PDAL_CUDA(cudaMemsetAsync(v32_.ybar, 0, m * sizeof(float), stream_));
         if (m) PDAL_CUDA(cudaMemsetAsync(v32_.u, 0, m * sizeof(float), stream_));
+        if (n) k_split<<<grid_for(n), kThreads, 0, stream_>>>(x0_, x0f_, n_);
+        if (m) k_split<<<grid_for(m), kThreads, 0, stream_>>>(y0_, y0f_, m_);
+        launches += 2;
         PDAL_LAUNCH_CHECK();
         launch_init_ax<float>();
     } else {
@@ -644,12 +663,13 @@ void CpalSolver::launch_init_ax() {
     if (m_ == 0) return;
     auto &v = vecs<T>();
     PDAL_WITH_SE(S_ev_, {
+        float2 *axf = std::is_same<T, float>::value ? ax0f_ : nullptr;
         if (beta_on_)
             k_init_ax<T, SE, true><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(
-                A_.ev.d, A_.rp, A_.ci, A_.v, x0_, v.ax, ax0_, v.u, v.y, v.clb, v.cub, st_);
+                A_.ev.d, A_.rp, A_.ci, A_.v, x0_, v.ax, ax0_, axf, v.u, v.y, v.clb, v.cub, st_);
         else
             k_init_ax<T, SE, false><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(
-                A_.ev.d, A_.rp, A_.ci, A_.v, x0_, v.ax, ax0_, v.u, v.y, v.clb, v.cub, st_);
+                A_.ev.d, A_.rp, A_.ci, A_.v, x0_, v.ax, ax0_, axf, v.u, v.y, v.clb, v.cub, st_);
     });
     PDAL_LAUNCH_CHECK();
     launches += 1;
@@ -667,18 +687,40 @@ const float *matvals<float>(const double *, const float *v32) {
 }
 
 template <typename T>
+static const typename AnchorT<T>::type *anchor(const double *a64, const float2 *a32);
+template <>
+const double *anchor<double>(const double *a64, const float2 *) {
+    return a64;
+}
+template <>
+const float2 *anchor<float>(const double *, const float2 *a32) {
+    return a32;
+}
+template <typename T>
+static const typename WeightT<T>::type *weights(const HalpernW *w64, const HalpernWf *w32);
+template <>
+const HalpernW *weights<double>(const HalpernW *w64, const HalpernWf *) {
+    return w64;
+}
+template <>
+const HalpernWf *weights<float>(const HalpernW *, const HalpernWf *w32) {
+    return w32;
+}
+
+template <typename T>
 void CpalSolver::launch_primal(int koff, bool major) {
     auto &v = vecs<T>();
-    PrimalArgs<T> pa{v.x, v.xbar, v.xh, v.lam, x0_, v.c, v.vlb, v.vub};
+    PrimalArgs<T> pa{v.x, v.xbar, v.xh, v.lam, anchor<T>(x0_, x0f_), v.c, v.vlb, v.vub};
     const T *gat = beta_on_ ? v.u : v.y;
     const T *Atv = matvals<T>(At_.v, At_.vf);
+    const auto *wt = weights<T>(wt_, wtf_);
     PDAL_WITH_S(S_it_, {
         if (major)
             k_primal<T, SB, true><<<At_.it.d.nblocks, kThreads, 0, stream_>>>(At_.it.d, At_.rp, At_.ci, Atv, gat, pa,
-                                                                             st_, koff);
+                                                                             st_, wt, koff);
         else
             k_primal<T, SB, false><<<At_.it.d.nblocks, kThreads, 0, stream_>>>(At_.it.d, At_.rp, At_.ci, Atv, gat,
-                                                                              pa, st_, koff);
+                                                                              pa, st_, wt, koff);
     });
 }
 
@@ -687,22 +729,23 @@ void CpalSolver::launch_dual(int koff, bool major) {
     if (m_ == 0) return;
     auto &v = vecs<T>();
     const T *Av = matvals<T>(A_.v, A_.vf);
-    DualArgs<T> da{v.y, v.yh, v.ybar, v.ax, v.u, y0_, ax0_, v.clb, v.cub};
+    DualArgs<T> da{v.y, v.yh, v.ybar, v.ax, v.u, anchor<T>(y0_, y0f_), anchor<T>(ax0_, ax0f_), v.clb, v.cub};
+    const auto *wt = weights<T>(wt_, wtf_);
     PDAL_WITH_S(S_it_, {
         if (major) {
             if (beta_on_)
                 k_dual<T, SB, true, true><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av, v.xbar,
-                                                                                    da, st_, koff);
+                                                                                    da, st_, wt, koff);
             else
                 k_dual<T, SB, true, false><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av,
-                                                                                     v.xbar, da, st_, koff);
+                                                                                     v.xbar, da, st_, wt, koff);
         } else {
             if (beta_on_)
                 k_dual<T, SB, false, true><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av,
-                                                                                     v.xbar, da, st_, koff);
+                                                                                     v.xbar, da, st_, wt, koff);
             else
                 k_dual<T, SB, false, false><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av,
-                                                                                      v.xbar, da, st_, koff);
+                                                                                      v.xbar, da, st_, wt, koff);
         }
     });
 }
@@ -726,14 +769,16 @@ void CpalSolver::launch_eval() {
     });
     const int nrow_slots = m_ > 0 ? A_.ev.d.nblocks + A_.ev.d.nlong : 0;
     k_control<<<1, kThreads, 0, stream_>>>(part_row_, nrow_slots, part_col_, At_.ev.d.nblocks + At_.ev.d.nlong, st_,
-                                           cp_);
+                                           cp_, wt_, wtf_);
     const int gr = grid_for(std::max(n_, m_));
+    const bool f32 = std::is_same<T, float>::value;
+    float2 *x0f = f32 ? x0f_ : nullptr, *y0f = f32 ? y0f_ : nullptr, *ax0f = f32 ? ax0f_ : nullptr;
     if (beta_on_)
-        k_restart<T, true><<<gr, kThreads, 0, stream_>>>(st_, n_, m_, v.xh, v.x, x0_, v.yh, v.y, y0_, phat_, v.ax,
-                                                         ax0_, v.u, v.clb, v.cub);
+        k_restart<T, true><<<gr, kThreads, 0, stream_>>>(st_, n_, m_, v.xh, v.x, x0_, x0f, v.yh, v.y, y0_, y0f, phat_,
+                                                         v.ax, ax0_, ax0f, v.u, v.clb, v.cub);
     else
-        k_restart<T, false><<<gr, kThreads, 0, stream_>>>(st_, n_, m_, v.xh, v.x, x0_, v.yh, v.y, y0_, phat_, v.ax,
-                                                          ax0_, v.u, v.clb, v.cub);
+        k_restart<T, false><<<gr, kThreads, 0, stream_>>>(st_, n_, m_, v.xh, v.x, x0_, x0f, v.yh, v.y, y0_, y0f,
+                                                          phat_, v.ax, ax0_, ax0f, v.u, v.clb, v.cub);
 }
 
 template <typename T>
@@ -745,15 +790,15 @@ void CpalSolver::capture_block(cudaGraphExec_t &exec) {
         for (auto &e : ev_) PDAL_CUDA(cudaEventCreate(&e));
     PDAL_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int g = 0; g < G; ++g) {
-        if (timing && g == 0) PDAL_CUDA(cudaEventRecord(ev_[3], stream_));
+        if (timing && g == 0) PDAL_CUDA(cudaEventRecordWithFlags(ev_[3], stream_, cudaEventRecordExternal));
         for (int i = 1; i <= F; ++i) {
             /* one non-major iteration (F-1 >= 2) is bracketed by events */
             if (timing && g == 0 && i == F - 1) {
-                PDAL_CUDA(cudaEventRecord(ev_[0], stream_));
+                PDAL_CUDA(cudaEventRecordWithFlags(ev_[0], stream_, cudaEventRecordExternal));
                 launch_primal<T>(i, false);
-                PDAL_CUDA(cudaEventRecord(ev_[1], stream_));
+                PDAL_CUDA(cudaEventRecordWithFlags(ev_[1], stream_, cudaEventRecordExternal));
                 launch_dual<T>(i, false);
-                PDAL_CUDA(cudaEventRecord(ev_[2], stream_));
+                PDAL_CUDA(cudaEventRecordWithFlags(ev_[2], stream_, cudaEventRecordExternal));
             } else {
                 launch_iteration<T>(i, i == F);
             }
@@ -795,6 +840,8 @@ void CpalSolver::switch_to_fp64() {
     *h_st_ = s;
     PDAL_CUDA(cudaMemcpyAsync(st_, h_st_, sizeof(CpalState), cudaMemcpyHostToDevice, stream_));
     h2d += sizeof(CpalState);
+    k_fill_weights<<<1, kThreads, 0, stream_>>>(st_, wt_, wtf_, cp_.F);
+    launches += 1;
     fp32_phase_ = false;
     launch_init_ax<double>();
 }
@@ -834,6 +881,15 @@ void CpalSolver::run_loop() {
             timed[ph] += 1;
         }
         if (fp32_phase_) fp32_iters = h_st_->total;
+        if (P_.verbose) {
+            /* one line per block, the columns of display_iteration_stats
+             * (LP/CP_AL/src/utils.cu:613-634) plus weight, step and phase */
+            const CpalState &q = *h_st_;
+            printf("%8d %.2e | %+.6e %+.6e | %.1e %.1e %.1e | %.1e | pw %.3e eta %.3e beta %.3e rs %d %s\n", q.total,
+                   now_sec() - t0, q.pobj, q.dobj, q.rel_p, q.rel_d, q.rel_gap, q.fp, q.pw, q.step, q.beta,
+                   q.restarts, fp32_phase_ ? "fp32" : "fp64");
+            fflush(stdout);
+        }
         if (h_st_->status) break;
         /* the device enforces the time limit; this host guard only covers a
          * device clock that does not advance */

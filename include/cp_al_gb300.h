@@ -66,6 +66,8 @@ typedef struct {
     int graph_blocks;             /* evaluation blocks per host check (default 1) */
     int timing;                   /* 1: time one primal and one dual launch per
                                      block with CUDA events (stats avg_*_ms) */
+    int fp32_stall_evals;         /* FP32 phase ends after this many evaluations
+                                     without halving its best KKT error (default 25) */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */
@@ -122,9 +124,23 @@ cp_al_gb300_session_t *cp_al_gb300_session_create(const lp_problem_t *prob, cons
 /* Solves from the device-resident copy; the result stays on the device except
  * for the scalar summary written to *summary (vectors are not downloaded). */
 int cp_al_gb300_session_solve(cp_al_gb300_session_t *s, cp_al_result_t *summary);
+/* Starts a solve (equilibration, power iteration, initial iterate) without
+ * iterating; iterations then run with cp_al_gb300_session_iterate. */
+int cp_al_gb300_session_start(cp_al_gb300_session_t *s);
+/* Runs `iterations` more iterations (rounded up to whole evaluation blocks)
+ * of the solve in progress, or none if it has terminated for any reason but
+ * the iteration limit; writes the scalar summary. */
+int cp_al_gb300_session_iterate(cp_al_gb300_session_t *s, int iterations, cp_al_result_t *summary);
 /* Downloads the unscaled solution of the last session solve. */
 int cp_al_gb300_session_fetch(cp_al_gb300_session_t *s, double *primal, double *dual, double *reduced_cost);
 void cp_al_gb300_session_free(cp_al_gb300_session_t *s);
+
+/* Runs only the setup of a solve (equilibration and power iteration) and
+ * returns the equilibrated constraint values in CSR order, the cumulative row
+ * and column scales, {constraint-bound factor, objective factor} and the
+ * power-iteration estimate of sigma_max(A)^2 (any output may be NULL). */
+int cp_al_gb300_session_scaling(cp_al_gb300_session_t *s, double *scaled_values, double *row_scale,
+                                double *col_scale, double *bound_obj_factors, double *lambda_est);
 
 #ifdef __cplusplus
 } /* extern "C" */

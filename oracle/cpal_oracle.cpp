@@ -32,6 +32,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <random>
 #include <vector>
 
@@ -568,6 +569,7 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->device = -1;
     o->graph_blocks = 1;
     o->timing = 0;
+    o->fp32_stall_evals = 25;
 }
 
 /* LP/CP_AL/src/utils.cu:361-394 (reflection coefficient without the
@@ -611,12 +613,14 @@ int oracle_max_threads(void) {
 #endif
 }
 
-cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_parameters_t *params,
-                                  const cp_al_gb300_options_t *opts, int *power_iterations_out) {
-    if (!prob || !params || !opts) return nullptr;
-    if (params->termination_evaluation_frequency < 3) return nullptr;
-    auto t0 = std::chrono::steady_clock::now();
-    Solver S;
+}  // extern "C"
+
+namespace {
+
+/* setup of a solve: solver.cu:1795-2273 and 3538-3609 */
+Solver *oracle_setup(const lp_problem_t *prob, const cp_al_parameters_t *params, const cp_al_gb300_options_t *opts) {
+    Solver *SP = new Solver();
+    Solver &S = *SP;
     S.P = params;
     S.O = *opts;
     S.n = prob->num_variables;
@@ -640,7 +644,6 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
     if (prob->dual_start) S.y0.assign(prob->dual_start, prob->dual_start + m);
     for (auto *v : {&S.x, &S.xh, &S.xbar, &S.dprod, &S.lam, &S.dx, &S.rd}) v->assign(n, 0.0);
     for (auto *v : {&S.y, &S.yh, &S.ybar, &S.pprod, &S.dy, &S.rp, &S.contrib}) v->assign(m, 0.0);
-
     S.rescale();
     S.x = S.x0;
     S.y = S.y0;
@@ -668,53 +671,48 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
         }
         S.bnd_norm = params->optimality_norm == NORM_TYPE_L_INF ? mx : std::sqrt(s);
     }
-    double rescale_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     S.initialize_step_size_and_primal_weight();
+    return SP;
+}
 
-    auto t_start = std::chrono::steady_clock::now();
-    const int F = params->termination_evaluation_frequency;
-    const int limit = params->termination_criteria.iteration_limit;
-    bool do_restart = false;
-    int charged = 0;
-    double elapsed = 0.0;
-    while (charged < limit) { /* solver.cu:1270-1697 */
-        if (do_restart) {
-            S.fixed_point_error();
-            S.fp0 = S.fp;
-            do_restart = false;
-        }
-        S.primal(1, true);
-        S.dual(1, true);
-        for (int i = 2; i <= F - 1; ++i) {
-            S.primal(i, false);
-            S.dual(i, false);
-        }
-        S.primal(F, true);
-        S.dual(F, true);
+/* one evaluation block of the loop, solver.cu:1270-1697; returns true when
+ * the solve has terminated */
+bool oracle_block(Solver &S, bool &do_restart, int &charged, double elapsed, int limit) {
+    const int F = S.P->termination_evaluation_frequency;
+    if (do_restart) {
         S.fixed_point_error();
-        S.compute_residual();
-        S.inner += F;
-        S.total += F;
-        charged += F;
-        elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-        if (params->verbose) {
-            printf("%8d %.2e | %+.6e %+.6e | %.1e %.1e %.1e | %.1e | pw %.3e eta %.3e beta %.3e rs %d oracle\n",
-                   S.total, elapsed, S.pobj, S.dobj, S.rel_p, S.rel_d, S.rel_gap, S.fp, S.pw, S.step, S.beta,
-                   S.restarts);
-            fflush(stdout);
-        }
-        S.check_termination(elapsed);
-        if (S.reason == TERMINATION_REASON_UNSPECIFIED && charged >= limit) S.reason = TERMINATION_REASON_ITERATION_LIMIT;
-        if (S.reason != TERMINATION_REASON_UNSPECIFIED) break;
-        do_restart = S.should_restart(F);
-        if (do_restart) S.perform_restart();
+        S.fp0 = S.fp;
+        do_restart = false;
     }
-    if (S.reason == TERMINATION_REASON_UNSPECIFIED) {
-        S.reason = TERMINATION_REASON_ITERATION_LIMIT;
-        S.compute_residual();
+    S.primal(1, true);
+    S.dual(1, true);
+    for (int i = 2; i <= F - 1; ++i) {
+        S.primal(i, false);
+        S.dual(i, false);
     }
+    S.primal(F, true);
+    S.dual(F, true);
+    S.fixed_point_error();
+    S.compute_residual();
+    S.inner += F;
+    S.total += F;
+    charged += F;
+    if (S.P->verbose) {
+        printf("%8d %.2e | %+.6e %+.6e | %.1e %.1e %.1e | %.1e | pw %.3e eta %.3e beta %.3e rs %d oracle\n", S.total,
+               elapsed, S.pobj, S.dobj, S.rel_p, S.rel_d, S.rel_gap, S.fp, S.pw, S.step, S.beta, S.restarts);
+        fflush(stdout);
+    }
+    S.check_termination(elapsed);
+    if (S.reason == TERMINATION_REASON_UNSPECIFIED && charged >= limit) S.reason = TERMINATION_REASON_ITERATION_LIMIT;
+    if (S.reason != TERMINATION_REASON_UNSPECIFIED) return true;
+    do_restart = S.should_restart(F);
+    if (do_restart) S.perform_restart();
+    return false;
+}
 
-    /* result: solver.cu:3828-3909 */
+/* result: solver.cu:3828-3909 */
+cp_al_result_t *oracle_result(Solver &S, double rescale_sec, double elapsed) {
+    const int n = S.n, m = S.m;
     cp_al_result_t *res = (cp_al_result_t *)calloc(1, sizeof(cp_al_result_t));
     res->primal_solution = (double *)malloc(sizeof(double) * (n > 0 ? n : 1));
     res->dual_solution = (double *)malloc(sizeof(double) * (m > 0 ? m : 1));
@@ -730,7 +728,7 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
     for (int i = 0; i < m; ++i) res->dual_solution[i] = S.yh[i] / S.rcum[i] / S.ovr;
     res->num_variables = n;
     res->num_constraints = m;
-    res->num_nonzeros = nnz;
+    res->num_nonzeros = (int)S.A.v.size();
     res->total_count = S.total;
     res->rescaling_time_sec = rescale_sec;
     res->cumulative_time_sec = elapsed;
@@ -743,8 +741,77 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
     res->objective_gap = S.gap;
     res->relative_objective_gap = S.rel_gap;
     res->termination_reason = S.reason;
-    if (power_iterations_out) *power_iterations_out = S.power_iters;
     return res;
+}
+
+struct OracleSession {
+    Solver *S = nullptr;
+    cp_al_parameters_t P;
+    bool do_restart = false;
+    int charged = 0;
+};
+
+} // namespace
+
+extern "C" {
+
+cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_parameters_t *params,
+                                  const cp_al_gb300_options_t *opts, int *power_iterations_out) {
+    if (!prob || !params || !opts) return nullptr;
+    if (params->termination_evaluation_frequency < 3) return nullptr;
+    auto t0 = std::chrono::steady_clock::now();
+    std::unique_ptr<Solver> S(oracle_setup(prob, params, opts));
+    double rescale_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    auto t_start = std::chrono::steady_clock::now();
+    const int limit = params->termination_criteria.iteration_limit;
+    bool do_restart = false;
+    int charged = 0;
+    double elapsed = 0.0;
+    while (charged < limit) {
+        elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        if (oracle_block(*S, do_restart, charged, elapsed, limit)) break;
+    }
+    elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    if (S->reason == TERMINATION_REASON_UNSPECIFIED) {
+        S->reason = TERMINATION_REASON_ITERATION_LIMIT;
+        S->compute_residual();
+    }
+    if (power_iterations_out) *power_iterations_out = S->power_iters;
+    return oracle_result(*S, rescale_sec, elapsed);
+}
+
+/* Session form for timing: setup once, then blocks of iterations. */
+void *oracle_cpal_session_create(const lp_problem_t *prob, const cp_al_parameters_t *params,
+                                 const cp_al_gb300_options_t *opts) {
+    if (!prob || !params || !opts || params->termination_evaluation_frequency < 3) return nullptr;
+    OracleSession *s = new OracleSession();
+    s->P = *params;
+    s->S = oracle_setup(prob, &s->P, opts);
+    s->S->P = &s->P;
+    return s;
+}
+
+/* Runs ceil(iterations / F) evaluation blocks; returns the iterations run. */
+int oracle_cpal_session_iterate(void *h, int iterations) {
+    OracleSession *s = (OracleSession *)h;
+    if (!s) return -1;
+    const int F = s->P.termination_evaluation_frequency;
+    int done = 0;
+    while (done < iterations) {
+        s->S->reason = TERMINATION_REASON_UNSPECIFIED;
+        if (oracle_block(*s->S, s->do_restart, s->charged, 0.0, 2147483647) &&
+            s->S->reason == TERMINATION_REASON_OPTIMAL)
+            break;
+        done += F;
+    }
+    return done;
+}
+
+void oracle_cpal_session_free(void *h) {
+    OracleSession *s = (OracleSession *)h;
+    if (!s) return;
+    delete s->S;
+    delete s;
 }
 
 void oracle_cpal_result_free(cp_al_result_t *r) {

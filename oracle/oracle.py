@@ -39,6 +39,12 @@ def lib():
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_max_threads.restype = C.c_int
         L.oracle_cpal_rescale.argtypes = [C.POINTER(N.LpProblem), C.POINTER(N.CpalParameters), _dp, _dp, _dp, _dp]
+        L.oracle_cpal_session_create.restype = C.c_void_p
+        L.oracle_cpal_session_create.argtypes = [C.POINTER(N.LpProblem), C.POINTER(N.CpalParameters),
+                                                 C.POINTER(N.CpalOptions)]
+        L.oracle_cpal_session_iterate.restype = C.c_int
+        L.oracle_cpal_session_iterate.argtypes = [C.c_void_p, C.c_int]
+        L.oracle_cpal_session_free.argtypes = [C.c_void_p]
         L.oracle_power_iteration.restype = C.c_double
         L.oracle_power_iteration.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, C.c_int, C.c_double, _ip]
         _lib = L
@@ -144,6 +150,32 @@ def power_iteration(data: LPData, max_iter: int = 5000, tol: float = 1e-4):
     s = lib().oracle_power_iteration(m, n, rp.ctypes.data_as(_ip), ci.ctypes.data_as(_ip), v.ctypes.data_as(_dp),
                                      max_iter, tol, C.byref(it))
     return s, it.value
+
+
+class Session:
+    """Set up once (equilibration, power iteration), then iterate in blocks;
+    used to time the CPU iteration on a bounded sample."""
+
+    def __init__(self, data: LPData, params: dict | None = None, options: dict | None = None, threads: int = 1):
+        L = lib()
+        self.p = apply_params(default_parameters(), params)
+        self.o = apply_options(default_options(), options)
+        self.prob = _Problem(data)
+        L.oracle_set_threads(int(threads))
+        self.h = L.oracle_cpal_session_create(C.byref(self.prob.p), C.byref(self.p), C.byref(self.o))
+        if not self.h:
+            raise RuntimeError("oracle session failed")
+
+    def iterate(self, iterations: int) -> int:
+        return lib().oracle_cpal_session_iterate(self.h, int(iterations))
+
+    def close(self):
+        if self.h:
+            lib().oracle_cpal_session_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def max_threads() -> int:

@@ -187,6 +187,7 @@ class CpalOptions(C.Structure):
         ("device", C.c_int),
         ("graph_blocks", C.c_int),
         ("timing", C.c_int),
+        ("fp32_stall_evals", C.c_int),
     ]
 
 
@@ -240,6 +241,9 @@ LP_SYMBOLS = {
     "cp_al_gb300_session_solve": (C.c_int, [C.c_void_p, C.POINTER(CpalResult)]),
     "cp_al_gb300_session_fetch": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     "cp_al_gb300_session_free": (None, [C.c_void_p]),
+    "cp_al_gb300_session_scaling": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp]),
+    "cp_al_gb300_session_start": (C.c_int, [C.c_void_p]),
+    "cp_al_gb300_session_iterate": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(CpalResult)]),
 }
 
 _LIBS: dict[str, C.CDLL] = {}

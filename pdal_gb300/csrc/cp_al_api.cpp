@@ -344,6 +344,7 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->device = -1;
     o->graph_blocks = 1;
     o->timing = 0;
+    o->fp32_stall_evals = 25;
 }
 
 /* Each variable is read the way the reference reads it

@@ -68,8 +68,13 @@ struct CpalState {
     int restarts;
     int sigma_on;
     int sigma_adapt;
-    int phase_switch;      /* 1: the FP32 phase reached its switch tolerance */
+    int phase_switch;      /* 1: the FP32 phase reached its switch tolerance or stalled */
     double fp32_switch_tol; /* < 0: no FP32 phase running */
+    int iter_limit;        /* iteration limit (device copy, a session may extend it) */
+    int fp32_stall_limit;  /* evaluations without a 2x KKT gain that end the FP32 phase */
+    int fp32_stall;        /* evaluations since the FP32 phase last halved its best KKT */
+    int pad2_;
+    double fp32_best_kkt;
 };
 
 /* Reduction terms of one evaluation (finished sums / maxima). */
@@ -272,11 +277,23 @@ PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval
         s.status = 1; /* TERMINATION_REASON_OPTIMAL */
         return true;
     }
-    if (s.total >= p.iteration_limit) {
+    if (s.total >= s.iter_limit) {
         s.status = 6; /* TERMINATION_REASON_ITERATION_LIMIT */
         return true;
     }
-    if (s.fp32_switch_tol > 0.0 && fmax(s.rel_p, fmax(s.rel_d, s.rel_gap)) < s.fp32_switch_tol) s.phase_switch = 1;
+    if (s.fp32_switch_tol > 0.0) {
+        /* the FP32 phase ends at its tolerance, or when the KKT error has not
+         * halved over fp32_stall_limit evaluations (FP32 rounding floor) */
+        const double kkt = fmax(s.rel_p, fmax(s.rel_d, s.rel_gap));
+        if (kkt < 0.5 * s.fp32_best_kkt) {
+            s.fp32_best_kkt = kkt;
+            s.fp32_stall = 0;
+        } else {
+            s.fp32_stall++;
+        }
+        if (kkt < s.fp32_switch_tol || (s.fp32_stall_limit > 0 && s.fp32_stall >= s.fp32_stall_limit))
+            s.phase_switch = 1;
+    }
     if (s.elapsed >= p.time_limit) {
         s.status = 5; /* TERMINATION_REASON_TIME_LIMIT */
         return true;

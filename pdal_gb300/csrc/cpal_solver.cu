@@ -123,9 +123,12 @@ class CpalSolver {
      * iteration and initial schedule */
     void setup_device();
     void run_loop();
+    /* extends the iteration limit by n and continues (session iterate) */
+    bool extend(int n);
     void download(cp_al_result_t *res, bool vectors);
     void result_on_device();
     void fetch_vectors(double *x, double *y, double *rc);
+    void fetch_scaling(double *vals, double *rsc, double *csc, double *bo);
 
     CpalState host_state{};
     double setup_sec = 0, loop_sec = 0;
@@ -133,6 +136,7 @@ class CpalSolver {
     int64_t h2d = 0, d2h = 0;
     int power_iters = 0;
     int fp32_iters = 0;
+    bool started = false;
     double sum_ms[2][3] = {{0, 0, 0}, {0, 0, 0}}; /* [fp64, fp32][primal, dual, block] */
     int timed[2] = {0, 0};
 
@@ -608,6 +612,9 @@ void CpalSolver::setup_device() {
     s.fp_last = INFINITY;
     s.refl = cp_.refl;
     s.fp32_switch_tol = fp32_phase_ ? O_.fp32_switch_tol : -1.0;
+    s.fp32_stall_limit = O_.fp32_stall_evals;
+    s.fp32_best_kkt = INFINITY;
+    s.iter_limit = cp_.iteration_limit;
     cpal_set_coefficients(s);
     beta_on_ = s.beta > 0.0;
     host_state = s;
@@ -911,6 +918,21 @@ void CpalSolver::run_loop() {
     loop_sec = now_sec() - t0;
 }
 
+bool CpalSolver::extend(int n) {
+    if (n <= 0) return false;
+    const CpalState &q = host_state;
+    if (q.status != 0 && q.status != TERMINATION_REASON_ITERATION_LIMIT) return false;
+    const int F = cp_.F;
+    const int blocks = (n + F - 1) / F;
+    CpalState s = *h_st_;
+    s.status = 0;
+    s.iter_limit = s.total + blocks * F;
+    *h_st_ = s;
+    PDAL_CUDA(cudaMemcpyAsync(st_, h_st_, sizeof(CpalState), cudaMemcpyHostToDevice, stream_));
+    h2d += sizeof(CpalState);
+    return true;
+}
+
 void CpalSolver::result_on_device() {
     ResultColEpi epi;
     epi.xh = v64_.xh;
@@ -935,6 +957,17 @@ void CpalSolver::fetch_vectors(double *x, double *y, double *rc) {
     if (rc) PDAL_CUDA(cudaMemcpyAsync(rc, rcout_, sizeof(double) * n_, cudaMemcpyDeviceToHost, stream_));
     PDAL_CUDA(cudaStreamSynchronize(stream_));
     d2h += (int64_t)sizeof(double) * ((x ? n_ : 0) + (y ? m_ : 0) + (rc ? n_ : 0));
+}
+
+void CpalSolver::fetch_scaling(double *vals, double *rsc, double *csc, double *bo) {
+    if (vals && nnz_) PDAL_CUDA(cudaMemcpyAsync(vals, A_.v, sizeof(double) * nnz_, cudaMemcpyDeviceToHost, stream_));
+    if (rsc && m_) PDAL_CUDA(cudaMemcpyAsync(rsc, rsc_, sizeof(double) * m_, cudaMemcpyDeviceToHost, stream_));
+    if (csc) PDAL_CUDA(cudaMemcpyAsync(csc, dsc_, sizeof(double) * n_, cudaMemcpyDeviceToHost, stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    if (bo) {
+        bo[0] = host_state.cbr;
+        bo[1] = host_state.ovr;
+    }
 }
 
 void CpalSolver::download(cp_al_result_t *res, bool vectors) {
@@ -1135,5 +1168,51 @@ int cp_al_gb300_session_fetch(cp_al_gb300_session_t *s, double *primal, double *
 }
 
 void cp_al_gb300_session_free(cp_al_gb300_session_t *s) { delete s; }
+
+int cp_al_gb300_session_start(cp_al_gb300_session_t *s) {
+    if (!s) return -1;
+    try {
+        s->solver->setup_device();
+        s->solver->host_state.status = TERMINATION_REASON_ITERATION_LIMIT;
+        s->solver->started = true;
+        return 0;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return -1;
+    }
+}
+
+int cp_al_gb300_session_iterate(cp_al_gb300_session_t *s, int iterations, cp_al_result_t *summary) {
+    if (!s || iterations < 0) return -1;
+    try {
+        if (!s->solver->started) {
+            set_error("session_iterate: call cp_al_gb300_session_start first");
+            return -1;
+        }
+        const double t0 = pdal::now_sec();
+        if (s->solver->extend(iterations)) s->solver->run_loop();
+        PDAL_CUDA(cudaDeviceSynchronize());
+        if (summary) s->solver->download(summary, false);
+        fill_stats(*s->solver, pdal::now_sec() - t0);
+        return 0;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return -1;
+    }
+}
+
+int cp_al_gb300_session_scaling(cp_al_gb300_session_t *s, double *scaled_values, double *row_scale,
+                                double *col_scale, double *bound_obj_factors, double *lambda_est) {
+    if (!s) return -1;
+    try {
+        s->solver->setup_device();
+        s->solver->fetch_scaling(scaled_values, row_scale, col_scale, bound_obj_factors);
+        if (lambda_est) *lambda_est = s->solver->host_state.lambda_est;
+        return 0;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return -1;
+    }
+}
 
 } // extern "C"

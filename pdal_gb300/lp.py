@@ -239,6 +239,18 @@ class LPSession:
             raise RuntimeError("session solve failed: " + N.last_error(self.lib))
         return _result_from_c(self.lib, r, self.m, self.n, with_vectors=False)
 
+    def start(self):
+        """Equilibration, power iteration and the initial iterate, no iterations."""
+        if self.lib.cp_al_gb300_session_start(self.h) != 0:
+            raise RuntimeError("session start failed: " + N.last_error(self.lib))
+
+    def iterate(self, iterations: int) -> LPResult:
+        """Continue the started solve for `iterations` more iterations."""
+        r = N.CpalResult()
+        if self.lib.cp_al_gb300_session_iterate(self.h, int(iterations), C.byref(r)) != 0:
+            raise RuntimeError("session iterate failed: " + N.last_error(self.lib))
+        return _result_from_c(self.lib, r, self.m, self.n, with_vectors=False)
+
     def fetch(self):
         x = np.empty(self.n)
         y = np.empty(self.m)
@@ -246,6 +258,18 @@ class LPSession:
         if self.lib.cp_al_gb300_session_fetch(self.h, _ptr(x), _ptr(y) if self.m else None, _ptr(rc)) != 0:
             raise RuntimeError("fetch failed: " + N.last_error(self.lib))
         return x, y, rc
+
+    def scaling(self):
+        """(scaled A values, row scales, column scales, cbr, ovr, lambda_est)
+        after the device equilibration and power iteration."""
+        vals = np.empty(max(self._prob.nnz, 1))
+        r = np.empty(max(self.m, 1))
+        c = np.empty(self.n)
+        bo = np.empty(2)
+        lam = C.c_double(0.0)
+        if self.lib.cp_al_gb300_session_scaling(self.h, _ptr(vals), _ptr(r), _ptr(c), _ptr(bo), C.byref(lam)) != 0:
+            raise RuntimeError("scaling failed: " + N.last_error(self.lib))
+        return vals[: self._prob.nnz], r[: self.m], c, bo[0], bo[1], lam.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -142,6 +142,28 @@ void cp_al_gb300_session_free(cp_al_gb300_session_t *s);
 int cp_al_gb300_session_scaling(cp_al_gb300_session_t *s, double *scaled_values, double *row_scale,
                                 double *col_scale, double *bound_obj_factors, double *lambda_est);
 
+/* --- allocation-free evaluation ----------------------------------------- */
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory (an allocator owned by another framework, a memory pool that forbids
+ * cudaMalloc while active, a loop where a cudaMalloc would synchronise the
+ * device, a fixed device-memory budget): evaluates, for
+ *     min c'x  s.t.  con_lb <= A x <= con_ub
+ * and a candidate x, out[0] = ||A x - P(A x)||_2, out[1] = max |A x - P(A x)|
+ * and out[2] = c'x, P the projection onto [con_lb, con_ub].  Every pointer is
+ * a device pointer; A is CSR with m rows and n columns; stream may be NULL.
+ * The call allocates nothing: its scratch is a fixed 2 MiB device array
+ * inside the library, which every device that loads the library holds until
+ * the process exits, so at most 524,288 rows are accepted (larger m returns
+ * -1 with a message).  The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress); make it before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU (different
+ * streams, or several host threads) race; serialise them.  The launch is
+ * asynchronous on `stream`; returns 0, or -1 on a bad argument or CUDA error. */
+int cp_al_gb300_primal_kkt_noalloc(int m, int n, const int *row_ptr, const int *col_ind, const double *vals,
+                                   const double *con_lb, const double *con_ub, const double *c, const double *x,
+                                   double *out, void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -244,6 +244,11 @@ LP_SYMBOLS = {
     "cp_al_gb300_session_scaling": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp]),
     "cp_al_gb300_session_start": (C.c_int, [C.c_void_p]),
     "cp_al_gb300_session_iterate": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(CpalResult)]),
+    "cp_al_gb300_primal_kkt_noalloc": (
+        C.c_int,
+        [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+         C.c_void_p, C.c_void_p],
+    ),
 }
 
 _LIBS: dict[str, C.CDLL] = {}

@@ -26,7 +26,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 
 # library name -> sources
 LIBRARIES = {
-    "libcp_al_gb300.so": ["cpal_solver.cu", "common.cpp", "cp_al_api.cpp"],
+    "libcp_al_gb300.so": ["cpal_solver.cu", "common.cpp", "cp_al_api.cpp", "noalloc.cu"],
 }
 
 

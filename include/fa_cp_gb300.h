@@ -1,0 +1,81 @@
+/*
+ * fa_cp_gb300.h -- additions of libfa_cp_gb300.so beyond the FA_CP interface
+ * of fa_cp.h: per-call options instead of environment variables, statistics
+ * of the last solve on the calling thread, and the last error message.
+ *
+ * None of these has a counterpart function in the reference; the options
+ * replace the environment variables QP/FA_CP/src/fa_cp_core_op.cu:908-916 and
+ * 1130-1169 read (FA_CP_RESTART_SELECT and its companions).
+ */
+#pragma once
+
+#include "fa_cp_types.h"
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int device;        /* CUDA device ordinal; -1 keeps the current device */
+    int blocks_per_sm; /* resident blocks of the persistent kernel per SM; 0 = as many as fit */
+    /* restart target selection (QP/FA_CP/src/fa_cp_core_op.cu:1130-1169):
+     * 0 restarts to the averaged iterate (default), 1 to the Halpern iterate
+     * when its fixed-point score is below margin x the current one, 2 always
+     * to the Halpern iterate */
+    int restart_select;
+    double restart_select_margin;
+    int restart_select_min_iters;
+    double restart_select_min_time;
+} fa_cp_gb300_options_t;
+
+typedef struct {
+    double setup_sec;  /* equilibration, upload, power iterations */
+    double loop_sec;   /* iterations and evaluations */
+    double total_sec;
+    double max_singular_value; /* power-iteration estimate of sigma_max(A) (scaled) */
+    double q_norm;             /* estimate of the largest eigenvalue of the scaled Q */
+    double q_nonconvexity;     /* estimate of its smallest eigenvalue (or 0) */
+    int q_type;                /* quad_obj_type_t of the objective */
+    int grid_blocks;           /* CUDA blocks of the persistent kernel */
+    int restarts;
+    int evaluations;
+    int64_t kernel_launches;
+    int64_t inner_iterations;  /* projected Barzilai-Borwein steps */
+    double primal_weight;
+    double step_size;
+    double device_loop_ms;     /* device time of the iteration segments (CUDA events) */
+} fa_cp_gb300_stats_t;
+
+/* Defaults: current device, automatic grid and block budget, restart to the
+ * averaged iterate. */
+void fa_cp_gb300_default_options(fa_cp_gb300_options_t *opts);
+
+/* The options solve_qp_problem uses: the defaults, overridden by the
+ * environment variables the reference reads (FA_CP_RESTART_SELECT, with
+ * FA_CP_RESTART_SELECT_LEGACY as fallback, FA_CP_RESTART_SELECT_MARGIN,
+ * FA_CP_RESTART_SELECT_MIN_ITERS, FA_CP_RESTART_SELECT_MIN_TIME). */
+void fa_cp_gb300_options_from_env(fa_cp_gb300_options_t *opts);
+
+/* solve_qp_problem with explicit options; params == NULL selects the
+ * defaults, opts == NULL the default options.  NULL on error. */
+fa_cp_result_t *fa_cp_gb300_solve(const qp_problem_t *prob, const fa_cp_parameters_t *params,
+                                  const fa_cp_gb300_options_t *opts);
+
+/* Statistics of the last solve on this thread. */
+void fa_cp_gb300_last_stats(fa_cp_gb300_stats_t *stats);
+
+/* The first `count` values of the C library's rand() sequence after
+ * srand(seed), from the library's own generator: the start vectors of the
+ * eigenvalue estimates of Q use it (QP/FA_CP/src/utils.cu:182-184 draws them
+ * with rand() in a fresh process), without touching the process-wide
+ * rand() state. */
+void fa_cp_gb300_rand_sequence(unsigned seed, int count, int *out);
+
+/* Message of the last failure on this thread ("" if none). */
+const char *fa_cp_gb300_last_error(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif

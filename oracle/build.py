@@ -10,7 +10,7 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-SOURCES = ["cpal_oracle.cpp"]
+SOURCES = ["cpal_oracle.cpp", "facp_oracle.cpp"]
 TARGET = HERE / "liboracle_pdal.so"
 
 

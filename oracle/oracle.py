@@ -180,3 +180,96 @@ class Session:
 
 def max_threads() -> int:
     return lib().oracle_max_threads()
+
+
+# ------------------------------------------------------------------ FA_CP (QP)
+
+from pdal_gb300.qp import QPData, QPResult, _csr  # noqa: E402
+from pdal_gb300.qp import apply_params as _qp_apply_params  # noqa: E402
+from pdal_gb300.qp import result_from_c as _qp_result  # noqa: E402
+
+
+def _qp_lib():
+    L = lib()
+    if not getattr(L, "_facp_ready", False):
+        L.oracle_facp_solve.restype = C.POINTER(N.FacpResult)
+        L.oracle_facp_solve.argtypes = [C.POINTER(N.QpProblem), C.POINTER(N.FacpParameters)]
+        L.oracle_facp_result_free.argtypes = [C.POINTER(N.FacpResult)]
+        L.oracle_facp_default_parameters.argtypes = [C.POINTER(N.FacpParameters)]
+        L.oracle_facp_set_trace.argtypes = [C.c_int]
+        L._facp_ready = True
+    return L
+
+
+def qp_default_parameters() -> N.FacpParameters:
+    p = N.FacpParameters()
+    _qp_lib().oracle_facp_default_parameters(C.byref(p))
+    return p
+
+
+class _QpProblem:
+    """qp_problem_t over numpy arrays kept alive by this object (the layout
+    create_qp_problem produces: every matrix present, possibly empty)."""
+
+    def __init__(self, data: QPData):
+        m, n = data.dims()
+        self.keep = []
+
+        def comp(M, rows):
+            if M is None:
+                rp = np.zeros(rows + 1, dtype=np.int32)
+                ci = np.zeros(1, dtype=np.int32)
+                v = np.zeros(1)
+                nnz = 0
+            else:
+                rp, ci, v, _ = _csr(M)
+                nnz = int(ci.shape[0])
+                if nnz == 0:
+                    ci, v = np.zeros(1, dtype=np.int32), np.zeros(1)
+            c = N.CsrComponent(rp.ctypes.data_as(_ip), ci.ctypes.data_as(_ip), v.ctypes.data_as(_dp))
+            self.keep += [rp, ci, v, c]
+            return c, nnz
+
+        nr = _csr(data.R)[3][0] if data.R is not None else 0
+        cA, nA = comp(data.A, m)
+        cQ, nQ = comp(data.Q, n)
+        cR, nR = comp(data.R, nr)
+        f = lambda a, k, fill: (np.ascontiguousarray(a, dtype=np.float64) if a is not None else np.full(k, fill))
+        vecs = [f(data.c, n, 0.0), f(data.var_lb, n, -np.inf), f(data.var_ub, n, np.inf),
+                f(data.con_lb, m, -np.inf), f(data.con_ub, m, np.inf)]
+        self.keep += vecs
+        p = N.QpProblem()
+        p.num_variables, p.num_constraints, p.num_rank_lowrank_obj = n, m, nr
+        p.objective_vector = vecs[0].ctypes.data_as(_dp)
+        p.variable_lower_bound = vecs[1].ctypes.data_as(_dp)
+        p.variable_upper_bound = vecs[2].ctypes.data_as(_dp)
+        p.constraint_lower_bound = vecs[3].ctypes.data_as(_dp)
+        p.constraint_upper_bound = vecs[4].ctypes.data_as(_dp)
+        p.objective_constant = float(data.c0)
+        p.constraint_matrix = C.pointer(cA)
+        p.constraint_matrix_num_nonzeros = nA
+        p.objective_sparse_matrix = C.pointer(cQ)
+        p.objective_sparse_matrix_num_nonzeros = nQ
+        p.objective_lowrank_matrix = C.pointer(cR)
+        p.objective_lowrank_matrix_num_nonzeros = nR
+        for name, a in (("primal_start", data.primal_start), ("dual_start", data.dual_start)):
+            if a is not None:
+                s = np.ascontiguousarray(a, dtype=np.float64)
+                self.keep.append(s)
+                setattr(p, name, s.ctypes.data_as(_dp))
+        self.p, self.m, self.n = p, m, n
+
+
+def solve_qp(data: QPData, params: dict | None = None, trace: bool = False) -> QPResult:
+    """The oracle's FA_CP solve (serial FP64)."""
+    L = _qp_lib()
+    p = _qp_apply_params(qp_default_parameters(), params)
+    prob = _QpProblem(data)
+    L.oracle_facp_set_trace(1 if trace else 0)
+    rp = L.oracle_facp_solve(C.byref(prob.p), C.byref(p))
+    if not rp:
+        raise RuntimeError("oracle QP solve failed (invalid parameters)")
+    try:
+        return _qp_result(rp.contents, prob.m, prob.n)
+    finally:
+        L.oracle_facp_result_free(rp)

@@ -1,5 +1,6 @@
-"""ctypes mirror of the C interface in include/cp_al_types.h, include/cp_al.h
-and include/cp_al_gb300.h, plus the loader of the in-tree libraries.
+"""ctypes mirror of the C interfaces in include/ (cp_al_types.h, cp_al.h,
+cp_al_gb300.h for the LP library; fa_cp_types.h, fa_cp.h, fa_cp_gb300.h for
+the QP library), plus the loader of the in-tree libraries.
 
 The loader never falls back to anything: if the CUDA library is missing it
 raises, so a product path cannot silently run elsewhere.
@@ -254,6 +255,186 @@ LP_SYMBOLS = {
 _LIBS: dict[str, C.CDLL] = {}
 
 
+# ---------------------------------------------------------------- FA_CP (QP)
+
+SIGMA_RULES = {
+    "fixed": 0, "residual_balance": 1, "kkt_balance": 2, "displacement": 3,
+    "progress": 4, "greedy_score": 5, "guarded": 6, "balanced_guarded": 7,
+}
+Q_TYPES = {0: "SPARSE_Q", 1: "DIAG_Q", 2: "LOW_RANK_PLUS_SPARSE_Q", 3: "LOW_RANK_Q", 4: "NON_Q"}
+
+
+class CsrComponent(C.Structure):
+    _fields_ = [("row_ptr", _ip), ("col_ind", _ip), ("val", _dp)]
+
+
+class QpProblem(C.Structure):
+    """QP/FA_CP/include/fa_cp_types.h:56-83"""
+
+    _fields_ = [
+        ("num_variables", C.c_int),
+        ("num_constraints", C.c_int),
+        ("num_rank_lowrank_obj", C.c_int),
+        ("variable_lower_bound", _dp),
+        ("variable_upper_bound", _dp),
+        ("objective_vector", _dp),
+        ("objective_constant", C.c_double),
+        ("constraint_matrix", C.POINTER(CsrComponent)),
+        ("constraint_matrix_num_nonzeros", C.c_int),
+        ("objective_sparse_matrix", C.POINTER(CsrComponent)),
+        ("objective_sparse_matrix_num_nonzeros", C.c_int),
+        ("objective_lowrank_matrix", C.POINTER(CsrComponent)),
+        ("objective_lowrank_matrix_num_nonzeros", C.c_int),
+        ("constraint_lower_bound", _dp),
+        ("constraint_upper_bound", _dp),
+        ("primal_start", _dp),
+        ("dual_start", _dp),
+    ]
+
+
+class FacpTerminationCriteria(C.Structure):
+    _fields_ = [
+        ("eps_optimal_relative", C.c_double),
+        ("eps_feasible_relative", C.c_double),
+        ("eps_feas_polish_relative", C.c_double),
+        ("eps_infeasible", C.c_double),
+        ("time_sec_limit", C.c_double),
+        ("iteration_limit", C.c_int),
+    ]
+
+
+class FacpParameters(C.Structure):
+    """QP/FA_CP/include/fa_cp_types.h:111-139"""
+
+    _fields_ = [
+        ("l_inf_ruiz_iterations", C.c_int),
+        ("has_pock_chambolle_alpha", C.c_bool),
+        ("pock_chambolle_alpha", C.c_double),
+        ("bound_objective_rescaling", C.c_bool),
+        ("trajectory_csv", C.c_char_p),
+        ("use_al_qp", C.c_bool),
+        ("al_sigma", C.c_double),
+        ("sigma_update_rule", C.c_int),
+        ("sigma_update_gain", C.c_double),
+        ("sigma_clip_low", C.c_double),
+        ("sigma_clip_high", C.c_double),
+        ("sigma_min", C.c_double),
+        ("sigma_max", C.c_double),
+        ("sigma_rollback_tol", C.c_double),
+        ("sigma_zero_threshold", C.c_double),
+        ("sigma_activation_threshold", C.c_double),
+        ("sigma_normal_motion_threshold", C.c_double),
+        ("sigma_activation_value", C.c_double),
+        ("verbose", C.c_int),
+        ("termination_evaluation_frequency", C.c_int),
+        ("sv_max_iter", C.c_int),
+        ("sv_tol", C.c_double),
+        ("termination_criteria", FacpTerminationCriteria),
+        ("restart_params", RestartParams),
+        ("reflection_coefficient", C.c_double),
+        ("feasibility_polishing", C.c_bool),
+        ("optimality_norm", C.c_int),
+    ]
+
+
+class FacpResult(C.Structure):
+    """QP/FA_CP/include/fa_cp_types.h:141-176"""
+
+    _fields_ = [
+        ("num_variables", C.c_int),
+        ("num_constraints", C.c_int),
+        ("num_nonzeros", C.c_int),
+        ("num_reduced_variables", C.c_int),
+        ("num_reduced_constraints", C.c_int),
+        ("num_reduced_nonzeros", C.c_int),
+        ("primal_solution", _dp),
+        ("dual_solution", _dp),
+        ("reduced_cost", _dp),
+        ("total_count", C.c_int),
+        ("total_inner_count", C.c_int),
+        ("rescaling_time_sec", C.c_double),
+        ("cumulative_time_sec", C.c_double),
+        ("absolute_primal_residual", C.c_double),
+        ("relative_primal_residual", C.c_double),
+        ("absolute_dual_residual", C.c_double),
+        ("relative_dual_residual", C.c_double),
+        ("primal_objective_value", C.c_double),
+        ("dual_objective_value", C.c_double),
+        ("objective_gap", C.c_double),
+        ("relative_objective_gap", C.c_double),
+        ("max_primal_ray_infeasibility", C.c_double),
+        ("max_dual_ray_infeasibility", C.c_double),
+        ("primal_ray_linear_objective", C.c_double),
+        ("dual_ray_objective", C.c_double),
+        ("final_al_sigma", C.c_double),
+        ("sigma_update_count", C.c_int),
+        ("sigma_update_rule", C.c_int),
+        ("termination_reason", C.c_int),
+        ("feasibility_polishing_time", C.c_double),
+        ("feasibility_iteration", C.c_int),
+    ]
+
+
+class QpMatrixDesc(C.Structure):
+    """QP/FA_CP/include/fa_cp_types.h:178-222 (CP_AL's layout plus zero_tolerance)."""
+
+    _fields_ = [("m", C.c_int), ("n", C.c_int), ("fmt", C.c_int), ("zero_tolerance", C.c_double),
+                ("data", _MatrixData)]
+
+
+class FacpOptions(C.Structure):
+    _fields_ = [
+        ("device", C.c_int),
+        ("blocks_per_sm", C.c_int),
+        ("restart_select", C.c_int),
+        ("restart_select_margin", C.c_double),
+        ("restart_select_min_iters", C.c_int),
+        ("restart_select_min_time", C.c_double),
+    ]
+
+
+class FacpStats(C.Structure):
+    _fields_ = [
+        ("setup_sec", C.c_double),
+        ("loop_sec", C.c_double),
+        ("total_sec", C.c_double),
+        ("max_singular_value", C.c_double),
+        ("q_norm", C.c_double),
+        ("q_nonconvexity", C.c_double),
+        ("q_type", C.c_int),
+        ("grid_blocks", C.c_int),
+        ("restarts", C.c_int),
+        ("evaluations", C.c_int),
+        ("kernel_launches", C.c_int64),
+        ("inner_iterations", C.c_int64),
+        ("primal_weight", C.c_double),
+        ("step_size", C.c_double),
+        ("device_loop_ms", C.c_double),
+    ]
+
+
+QP_SYMBOLS = {
+    "create_qp_problem": (
+        C.POINTER(QpProblem),
+        [_dp, C.POINTER(QpMatrixDesc), C.POINTER(QpMatrixDesc), C.POINTER(QpMatrixDesc), _dp, _dp, _dp, _dp, _dp],
+    ),
+    "set_start_values": (None, [C.POINTER(QpProblem), _dp, _dp]),
+    "solve_qp_problem": (C.POINTER(FacpResult), [C.POINTER(QpProblem), C.POINTER(FacpParameters)]),
+    "set_default_parameters": (None, [C.POINTER(FacpParameters)]),
+    "fa_cp_result_free": (None, [C.POINTER(FacpResult)]),
+    "qp_problem_free": (None, [C.POINTER(QpProblem)]),
+    "fa_cp_gb300_default_options": (None, [C.POINTER(FacpOptions)]),
+    "fa_cp_gb300_options_from_env": (None, [C.POINTER(FacpOptions)]),
+    "fa_cp_gb300_solve": (
+        C.POINTER(FacpResult),
+        [C.POINTER(QpProblem), C.POINTER(FacpParameters), C.POINTER(FacpOptions)],
+    ),
+    "fa_cp_gb300_last_stats": (None, [C.POINTER(FacpStats)]),
+    "fa_cp_gb300_last_error": (C.c_char_p, []),
+    "fa_cp_gb300_rand_sequence": (None, [C.c_uint, C.c_int, _ip]),
+}
+
+
 def lib_path(name: str) -> Path:
     return LIBDIR / name
 
@@ -280,6 +461,11 @@ def load_lp() -> C.CDLL:
     return load("libcp_al_gb300.so", LP_SYMBOLS)
 
 
+def load_qp() -> C.CDLL:
+    return load("libfa_cp_gb300.so", QP_SYMBOLS)
+
+
 def last_error(lib: C.CDLL) -> str:
-    msg = lib.cp_al_gb300_last_error()
+    fn = getattr(lib, "fa_cp_gb300_last_error", None) or lib.cp_al_gb300_last_error
+    msg = fn()
     return msg.decode() if msg else ""

@@ -27,6 +27,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 # library name -> sources
 LIBRARIES = {
     "libcp_al_gb300.so": ["cpal_solver.cu", "common.cpp", "cp_al_api.cpp", "noalloc.cu"],
+    "libfa_cp_gb300.so": ["facp_solver.cu", "common.cpp", "fa_cp_api.cpp"],
 }
 
 
@@ -68,15 +69,18 @@ def build_product(jobs: int | None = None) -> list[Path]:
     out = []
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 2)) as ex:
         futs = {}
-        for lib, srcs in LIBRARIES.items():
+        for srcs in LIBRARIES.values():
             for s in srcs:
-                src = CSRC / s
-                obj = BUILD / (src.stem + ".o")
-                futs[(lib, s)] = ex.submit(_compile, src, obj)
-        objs = {k: f.result() for k, f in futs.items()}
+                if s not in futs:
+                    src = CSRC / s
+                    futs[s] = ex.submit(_compile, src, BUILD / (src.stem + ".o"))
+        objs = {s: f.result() for s, f in futs.items()}
     for lib, srcs in LIBRARIES.items():
         target = LIBDIR / lib
-        cmd = [_nvcc(), "-shared", "-o", str(target), *[str(objs[(lib, s)]) for s in srcs], "-Xcompiler", "-fPIC"]
+        # -Bsymbolic: calls inside a library bind to its own definitions (both
+        # libraries export set_start_values and set_default_parameters)
+        cmd = [_nvcc(), "-shared", "-o", str(target), *[str(objs[s]) for s in srcs], "-Xcompiler", "-fPIC",
+               "-Xlinker", "-Bsymbolic"]
         _run(cmd)
         out.append(target)
     return out

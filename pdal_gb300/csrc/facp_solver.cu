@@ -1,0 +1,987 @@
+/*
+ * facp_solver.cu -- host side of the FA_CP (convex QP) solver: equilibration,
+ * device layout, the evaluation / restart / sigma control of
+ * QP/FA_CP/src/solver.cu:74-165, and the C entry points solve_qp_problem and
+ * fa_cp_gb300_solve.
+ *
+ * The iterations themselves run in the persistent kernel of facp_kernels.cuh:
+ * the host launches one segment per evaluation point (every print-frequency
+ * iteration and every major iteration, the only places where the reference
+ * makes a data-dependent decision), reads a few scalars back, and decides
+ * termination and restarts exactly where the reference does.
+ */
+#include "../../include/fa_cp.h"
+#include "../../include/fa_cp_gb300.h"
+#include "common.h"
+#include "facp_kernels.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+namespace pdal {
+namespace {
+
+using namespace facp;
+
+thread_local fa_cp_gb300_stats_t g_stats;
+thread_local std::string g_error;
+
+double now_sec() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+/* The C library's rand() as a fresh process sees it (seed 1): the additive
+ * feedback generator r[i] = r[i-3] + r[i-31] (mod 2^32) over a table seeded
+ * with the Park-Miller sequence 16807^i mod (2^31 - 1), the first 310 outputs
+ * discarded, each output shifted right by one bit.  Kept per solve so the
+ * process-wide rand() state is never touched. */
+class CRandom {
+  public:
+    explicit CRandom(unsigned seed = 1) {
+        std::vector<int32_t> r(34);
+        r[0] = (int32_t)seed;
+        for (int i = 1; i < 31; ++i) {
+            const long long v = (16807LL * r[i - 1]) % 2147483647LL;
+            r[i] = (int32_t)(v < 0 ? v + 2147483647LL : v);
+        }
+        for (int i = 31; i < 34; ++i) r[i] = r[i - 31];
+        for (int i = 0; i < 34; ++i) s_[i] = (uint32_t)r[i];
+        k_ = 34;
+        for (int i = 34; i < 344; ++i) next_raw();
+    }
+    int next() { return (int)(next_raw() >> 1); }
+    static constexpr int kMax = 2147483647;
+
+  private:
+    uint32_t next_raw() {
+        const uint32_t v = s_[(k_ - 31) % 34] + s_[(k_ - 3) % 34];
+        s_[k_ % 34] = v;
+        ++k_;
+        return v;
+    }
+    uint32_t s_[34];
+    long long k_;
+};
+
+struct HostQP {
+    int n = 0, m = 0, nr = 0;
+    HostCsr A, Q, R;
+    std::vector<double> c, vlb, vub, clb, cub;
+    std::vector<double> dcum, rcum;
+    double cbr = 1.0, ovr = 1.0, c0 = 0.0;
+    double obj_norm = 0.0, bnd_norm = 0.0;
+};
+
+HostCsr from_component(const CsrComponent *cc, int rows, int cols, int nnz, const char *what) {
+    HostCsr M;
+    M.nr = rows;
+    M.nc = cols;
+    M.rp.assign((size_t)rows + 1, 0);
+    if (cc && cc->row_ptr && nnz > 0) {
+        csr_validate(rows, cols, cc->row_ptr, cc->col_ind, nnz, what);
+        M.rp.assign(cc->row_ptr, cc->row_ptr + rows + 1);
+        M.ci.assign(cc->col_ind, cc->col_ind + nnz);
+        M.v.assign(cc->val, cc->val + nnz);
+    } else if (cc && cc->row_ptr && rows > 0) {
+        csr_validate(rows, cols, cc->row_ptr, cc->col_ind, 0, what);
+    }
+    return M;
+}
+
+/* ---------------------------------------------------------------- equilibration
+ * QP/FA_CP/src/preconditioner.c:92-331 on the host: Ruiz passes (columns see
+ * A and Q), one Pock-Chambolle pass, then bound/objective scaling that also
+ * rescales Q by ovr/cbr and R by sqrt(ovr/cbr). */
+void scale_problem(HostQP &P, const std::vector<double> &r, const std::vector<double> &d) {
+    for (int i = 0; i < P.n; ++i) {
+        P.c[i] /= d[i];
+        P.vub[i] *= d[i];
+        P.vlb[i] *= d[i];
+    }
+    for (int i = 0; i < P.m; ++i) {
+        P.clb[i] /= r[i];
+        P.cub[i] /= r[i];
+    }
+    for (int row = 0; row < P.m; ++row)
+        for (int k = P.A.rp[row]; k < P.A.rp[row + 1]; ++k) P.A.v[k] /= (r[row] * d[P.A.ci[k]]);
+    for (int row = 0; row < P.n; ++row)
+        for (int k = P.Q.rp[row]; k < P.Q.rp[row + 1]; ++k) P.Q.v[k] /= (d[row] * d[P.Q.ci[k]]);
+    if (P.R.nnz() > 0)
+        for (int row = 0; row < P.nr; ++row)
+            for (int k = P.R.rp[row]; k < P.R.rp[row + 1]; ++k) P.R.v[k] /= d[P.R.ci[k]];
+}
+
+void equilibrate(HostQP &P, const fa_cp_parameters_t &prm) {
+    P.dcum.assign(P.n, 1.0);
+    P.rcum.assign(P.m, 1.0);
+    std::vector<double> cr(P.m), vr(P.n);
+    auto finish = [&]() {
+        for (int i = 0; i < P.n; ++i) vr[i] = (vr[i] < 1e-12) ? 1.0 : std::sqrt(vr[i]);
+        for (int i = 0; i < P.m; ++i) cr[i] = (cr[i] < 1e-12) ? 1.0 : std::sqrt(cr[i]);
+        scale_problem(P, cr, vr);
+        for (int i = 0; i < P.n; ++i) P.dcum[i] *= vr[i];
+        for (int i = 0; i < P.m; ++i) P.rcum[i] *= cr[i];
+    };
+    for (int it = 0; it < prm.l_inf_ruiz_iterations; ++it) {
+        std::fill(vr.begin(), vr.end(), 0.0);
+        std::fill(cr.begin(), cr.end(), 0.0);
+        for (int row = 0; row < P.m; ++row)
+            for (int k = P.A.rp[row]; k < P.A.rp[row + 1]; ++k) {
+                const double v = std::fabs(P.A.v[k]);
+                if (v > vr[P.A.ci[k]]) vr[P.A.ci[k]] = v;
+                if (v > cr[row]) cr[row] = v;
+            }
+        for (int row = 0; row < P.n; ++row)
+            for (int k = P.Q.rp[row]; k < P.Q.rp[row + 1]; ++k) {
+                const double v = std::fabs(P.Q.v[k]);
+                if (v > vr[P.Q.ci[k]]) vr[P.Q.ci[k]] = v;
+            }
+        finish();
+    }
+    if (prm.has_pock_chambolle_alpha) {
+        const double a = prm.pock_chambolle_alpha;
+        std::fill(vr.begin(), vr.end(), 0.0);
+        std::fill(cr.begin(), cr.end(), 0.0);
+        for (int row = 0; row < P.m; ++row)
+            for (int k = P.A.rp[row]; k < P.A.rp[row + 1]; ++k) {
+                const double v = std::fabs(P.A.v[k]);
+                vr[P.A.ci[k]] += std::pow(v, 2.0 - a);
+                cr[row] += std::pow(v, a);
+            }
+        for (int row = 0; row < P.n; ++row)
+            for (int k = P.Q.rp[row]; k < P.Q.rp[row + 1]; ++k) vr[P.Q.ci[k]] += std::pow(std::fabs(P.Q.v[k]), 2.0 - a);
+        finish();
+    }
+    if (prm.bound_objective_rescaling) {
+        double bsq = 0.0, csq = 0.0;
+        for (int i = 0; i < P.m; ++i) {
+            if (std::isfinite(P.clb[i]) && P.clb[i] != P.cub[i]) bsq += P.clb[i] * P.clb[i];
+            if (std::isfinite(P.cub[i])) bsq += P.cub[i] * P.cub[i];
+        }
+        for (int i = 0; i < P.n; ++i) csq += P.c[i] * P.c[i];
+        P.cbr = 1.0 / (std::sqrt(bsq) + 1.0);
+        P.ovr = 1.0 / (std::sqrt(csq) + 1.0);
+        for (int i = 0; i < P.m; ++i) {
+            P.clb[i] *= P.cbr;
+            P.cub[i] *= P.cbr;
+        }
+        for (int i = 0; i < P.n; ++i) {
+            P.vlb[i] *= P.cbr;
+            P.vub[i] *= P.cbr;
+            P.c[i] *= P.ovr;
+        }
+        for (double &v : P.Q.v) v *= P.ovr / P.cbr;
+        if (P.R.nnz() > 0) {
+            const double f = std::sqrt(P.ovr / P.cbr);
+            for (double &v : P.R.v) v *= f;
+        }
+    } else {
+        P.cbr = P.ovr = 1.0;
+    }
+}
+
+int detect_q_type(const HostCsr &Q, const HostCsr &R) { /* QP/FA_CP/src/utils.cu:1576-1616 */
+    if (Q.nnz() == 0 && R.nnz() == 0) return Q_NONE;
+    if (R.nnz() > 0) return Q.nnz() > 0 ? Q_LOWRANK_SPARSE : Q_LOWRANK;
+    for (int i = 0; i < Q.nr; ++i)
+        for (int k = Q.rp[i]; k < Q.rp[i + 1]; ++k)
+            if (Q.ci[k] != i) return Q_SPARSE;
+    return Q_DIAG;
+}
+
+double sane_positive(double v, double fb) { return (std::isfinite(v) && v > 0.0) ? v : fb; }
+double score_component(double v) { return std::isfinite(v) ? std::fmax(v, 1e-300) : INFINITY; }
+double clamp_d(double v, double lo, double hi) { return std::fmin(std::fmax(v, lo), hi); }
+
+int print_frequency_host(int iter) {
+    int step = 10;
+    long long threshold = 1000;
+    while (iter >= threshold) {
+        step *= 10;
+        threshold *= 10;
+    }
+    return step;
+}
+
+struct DevMat {
+    HostCsr h;
+    HostPlan plan;
+    DMat d{};
+};
+
+class FacpSolver {
+  public:
+    FacpSolver(const qp_problem_t *prob, const fa_cp_parameters_t &prm, const fa_cp_gb300_options_t &opt)
+        : prob_(prob), p_(prm), o_(opt) {}
+    ~FacpSolver() {
+        if (stream_) cudaStreamDestroy(stream_);
+        if (ev0_) cudaEventDestroy(ev0_);
+        if (ev1_) cudaEventDestroy(ev1_);
+    }
+    fa_cp_result_t *run();
+
+  private:
+    void prepare();
+    void upload();
+    void launch(Args a);
+    void read_ctl();
+    Args base_args(int mode) const;
+    void power_iterations();
+    void evaluate(bool infeas);
+    bool check_termination(double elapsed);
+    bool should_restart();
+    void choose_restart_candidate(double elapsed);
+    void perform_restart();
+    void update_sigma(double pd, double dd, double normal);
+    void set_sigma_active(double s, double zt);
+    double clipped(double cur, double ratio) const;
+    void print_eval() const;
+
+    const qp_problem_t *prob_;
+    fa_cp_parameters_t p_;
+    fa_cp_gb300_options_t o_;
+    HostQP H_;
+    int qtype_ = Q_NONE;
+    DevMat M_[NMAT];
+    Arena arena_;
+    Prob P_{};
+    Ctl ctl_{};
+    cudaStream_t stream_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    int grid_ = 0;
+    std::vector<double> diag_;
+    double qnorm_ = 0.0, nonconvexity_ = 0.0;
+    double sv_max_ = 0.0;
+    double setup_sec_ = 0.0, rescale_sec_ = 0.0;
+    long long launches_ = 0;
+    float dev_ms_ = 0.f;
+
+    /* solver state (solver_state.cu:494-877 of the reference) */
+    int total_ = 0, inner_ = 0;
+    double step_ = 0.0, pw_ = 1.0, best_pw_ = 1.0, pw_esum_ = 0.0, pw_last_ = 0.0, best_gap_ = INFINITY;
+    double fp_ = INFINITY, fp0_ = INFINITY, fp_last_ = INFINITY;
+    bool al_available_ = false, use_al_ = false, has_inner_ = false;
+    double al_sigma_ = 0.0, best_al_sigma_ = 0.0, best_sigma_score_ = INFINITY, last_sigma_score_ = INFINITY;
+    double last_rp_ = INFINITY, last_rd_ = INFINITY, last_rg_ = INFINITY;
+    int sigma_updates_ = 0, sigma_dir_ = 1;
+    int inner_limit_ = 1000;
+    termination_reason_t reason_ = TERMINATION_REASON_UNSPECIFIED;
+    int restart_target_ = 0;
+    int restarts_ = 0, evals_ = 0;
+};
+
+void FacpSolver::prepare() {
+    const qp_problem_t *q = prob_;
+    if (!q) throw Error("solve_qp_problem: invalid arguments");
+    if (p_.termination_evaluation_frequency < 1) throw Error("termination_evaluation_frequency must be >= 1");
+    HostQP &P = H_;
+    P.n = q->num_variables;
+    P.m = q->num_constraints;
+    P.nr = q->num_rank_lowrank_obj;
+    if (P.n < 1 || P.m < 0 || P.nr < 0) throw Error("solve_qp_problem: the problem needs n >= 1 variables");
+    if (!q->objective_vector || !q->variable_lower_bound || !q->variable_upper_bound ||
+        (P.m > 0 && (!q->constraint_lower_bound || !q->constraint_upper_bound)))
+        throw Error("solve_qp_problem: missing problem vectors");
+    P.A = from_component(q->constraint_matrix, P.m, P.n, q->constraint_matrix_num_nonzeros, "A");
+    P.Q = from_component(q->objective_sparse_matrix, P.n, P.n, q->objective_sparse_matrix_num_nonzeros, "Q");
+    P.R = from_component(q->objective_lowrank_matrix, P.nr, P.n, q->objective_lowrank_matrix_num_nonzeros, "R");
+    P.c.assign(q->objective_vector, q->objective_vector + P.n);
+    P.vlb.assign(q->variable_lower_bound, q->variable_lower_bound + P.n);
+    P.vub.assign(q->variable_upper_bound, q->variable_upper_bound + P.n);
+    if (P.m > 0) {
+        P.clb.assign(q->constraint_lower_bound, q->constraint_lower_bound + P.m);
+        P.cub.assign(q->constraint_upper_bound, q->constraint_upper_bound + P.m);
+    }
+    P.c0 = q->objective_constant;
+    /* norms of the unscaled problem (solver_state.cu:700-740) */
+    const bool linf = p_.optimality_norm == NORM_TYPE_L_INF;
+    {
+        double s = 0.0, mx = 0.0;
+        for (int i = 0; i < P.n; ++i) {
+            const double v = q->objective_vector[i];
+            if (linf)
+                mx = std::max(mx, std::fabs(v));
+            else
+                s += v * v;
+        }
+        P.obj_norm = linf ? mx : std::sqrt(s);
+        s = 0.0;
+        mx = 0.0;
+        for (int i = 0; i < P.m; ++i) {
+            const double lo = q->constraint_lower_bound[i], up = q->constraint_upper_bound[i];
+            if (linf) {
+                if (std::isfinite(lo) && lo != up) mx = std::max(mx, std::fabs(lo));
+                if (std::isfinite(up)) mx = std::max(mx, std::fabs(up));
+            } else {
+                if (std::isfinite(lo) && lo != up) s += lo * lo;
+                if (std::isfinite(up)) s += up * up;
+            }
+        }
+        P.bnd_norm = linf ? mx : std::sqrt(s);
+    }
+    const double t0 = now_sec();
+    equilibrate(P, p_);
+    rescale_sec_ = now_sec() - t0;
+    qtype_ = detect_q_type(P.Q, P.R);
+    if (qtype_ == Q_DIAG) { /* solver_state.cu:252-270, 478-492 */
+        diag_.assign(P.n, 0.0);
+        for (int i = 0; i < P.n; ++i)
+            for (int k = P.Q.rp[i]; k < P.Q.rp[i + 1]; ++k)
+                if (P.Q.ci[k] < P.n) diag_[P.Q.ci[k]] = P.Q.v[k] + 1e-12;
+        double mx = 0.0, mn = 0.0;
+        for (double d : diag_) {
+            mx = std::fmax(mx, std::fabs(d));
+            mn = std::fmin(mn, d);
+        }
+        qnorm_ = mx;
+        nonconvexity_ = mn;
+    }
+    M_[MAT_A].h = P.A;
+    M_[MAT_AT].h = csr_transpose(P.m, P.n, P.A.rp.data(), P.A.ci.data(), P.A.v.data());
+    M_[MAT_Q].h = P.Q;
+    M_[MAT_R].h = P.R;
+    M_[MAT_RT].h = csr_transpose(P.nr, P.n, P.R.rp.data(), P.R.ci.data(), P.R.v.data());
+    M_[MAT_A].h.nr = P.m;
+    M_[MAT_A].h.nc = P.n;
+    int lbase = 0;
+    for (int k = 0; k < NMAT; ++k) {
+        DevMat &dm = M_[k];
+        dm.plan = plan_rows(dm.h.nr, dm.h.rp.data(), kS);
+        dm.d.rows = dm.h.nr;
+        dm.d.lbase = lbase;
+        lbase += dm.plan.nlong;
+    }
+    P_.nlong_total = lbase;
+}
+
+void FacpSolver::upload() {
+    const HostQP &H = H_;
+    const size_t n = H.n, m = H.m, nr = H.nr;
+    int dev = 0;
+    if (o_.device >= 0) PDAL_CUDA(cudaSetDevice(o_.device));
+    PDAL_CUDA(cudaGetDevice(&dev));
+    PDAL_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    PDAL_CUDA(cudaEventCreate(&ev0_));
+    PDAL_CUDA(cudaEventCreate(&ev1_));
+    int coop = 0, sms = 0;
+    PDAL_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (!coop) throw Error("the device does not support cooperative launches");
+    int per_sm = 0;
+    PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_facp, kThreads, 0));
+    if (per_sm < 1) throw Error("the persistent kernel does not fit on one SM");
+    if (o_.blocks_per_sm > 0) per_sm = std::min(per_sm, o_.blocks_per_sm);
+    long long work = 0;
+    for (int k = 0; k < NMAT; ++k) work = std::max<long long>(work, M_[k].plan.nblocks);
+    work = std::max<long long>(work, ((long long)std::max(n, m) + kThreads - 1) / kThreads);
+    grid_ = (int)std::max<long long>(1, std::min<long long>((long long)per_sm * sms, work));
+
+    const size_t vec = std::max<size_t>(std::max(n, m), 1);
+    const int nl = std::max(P_.nlong_total, 1);
+    auto alloc_all = [&]() {
+        for (int k = 0; k < NMAT; ++k) {
+            DevMat &dm = M_[k];
+            const size_t nnz = dm.h.ci.size();
+            dm.d.rp = arena_.take<int>((size_t)dm.h.nr + 1);
+            dm.d.ci = arena_.take<int>(nnz + 8);
+            dm.d.v = arena_.take<double>(nnz + 8);
+            dm.d.plan.nblocks = dm.plan.nblocks;
+            dm.d.plan.nlong = dm.plan.nlong;
+            dm.d.plan.desc = arena_.take<int4>(std::max(dm.plan.nblocks, 1));
+            dm.d.plan.linfo = arena_.take<int4>(std::max(dm.plan.nlong, 1));
+            dm.d.plan.lpart = arena_.take<double>(kLongStride * (size_t)std::max(dm.plan.npieces, 1));
+            dm.d.plan.lcount = arena_.take<unsigned>(std::max(dm.plan.nlong, 1));
+        }
+        double **consts[] = {(double **)&P_.c,       (double **)&P_.vlb,     (double **)&P_.vub,
+                             (double **)&P_.vlb_fin, (double **)&P_.vub_fin, (double **)&P_.diag,
+                             (double **)&P_.dcum};
+        for (double **p : consts) *p = arena_.take<double>(n);
+        double **cons[] = {(double **)&P_.clb, (double **)&P_.cub, (double **)&P_.clb_fin, (double **)&P_.cub_fin,
+                           (double **)&P_.rcum};
+        for (double **p : cons) *p = arena_.take<double>(std::max<size_t>(m, 1));
+        for (double **p : {&P_.x0, &P_.x, &P_.xh, &P_.xbar, &P_.dprod, &P_.dslack, &P_.dx, &P_.qx, &P_.grad, &P_.dir,
+                           &P_.out_x, &P_.out_rc})
+            *p = arena_.take<double>(n);
+        for (double **p : {&P_.y0, &P_.y, &P_.yh, &P_.ybar, &P_.dy, &P_.aldual, &P_.out_y})
+            *p = arena_.take<double>(std::max<size_t>(m, 1));
+        P_.rx = arena_.take<double>(std::max<size_t>(nr, 1));
+        P_.pv = arena_.take<double>(vec);
+        P_.pv2 = arena_.take<double>(vec);
+        P_.pv3 = arena_.take<double>(vec);
+        P_.part = arena_.take<double>((size_t)3 * grid_ * kSlot);
+        P_.lpart = arena_.take<double>((size_t)3 * nl * kSlot);
+        P_.bar = arena_.take<GridBar>(1);
+        P_.ctl = arena_.take<Ctl>(1);
+    };
+    arena_.begin_measure();
+    alloc_all();
+    arena_.reserve_measured();
+    alloc_all();
+
+    auto h2d = [&](const void *dst, const void *src, size_t bytes) {
+        if (bytes) PDAL_CUDA(cudaMemcpyAsync((void *)dst, src, bytes, cudaMemcpyHostToDevice, stream_));
+    };
+    for (int k = 0; k < NMAT; ++k) {
+        DevMat &dm = M_[k];
+        h2d(dm.d.rp, dm.h.rp.data(), dm.h.rp.size() * sizeof(int));
+        h2d(dm.d.ci, dm.h.ci.data(), dm.h.ci.size() * sizeof(int));
+        h2d(dm.d.v, dm.h.v.data(), dm.h.v.size() * sizeof(double));
+        h2d(dm.d.plan.desc, dm.plan.desc.data(), dm.plan.desc.size() * sizeof(int));
+        h2d(dm.d.plan.linfo, dm.plan.linfo.data(), dm.plan.linfo.size() * sizeof(int));
+        PDAL_CUDA(cudaMemsetAsync(dm.d.plan.lcount, 0, sizeof(unsigned) * std::max(dm.plan.nlong, 1), stream_));
+        P_.M[k] = dm.d;
+    }
+    P_.n = H.n;
+    P_.m = H.m;
+    P_.nr = H.nr;
+    P_.qtype = qtype_;
+    std::vector<double> fin(n);
+    h2d(P_.c, H.c.data(), n * 8);
+    h2d(P_.vlb, H.vlb.data(), n * 8);
+    h2d(P_.vub, H.vub.data(), n * 8);
+    std::vector<double> vlf(n), vuf(n);
+    for (size_t i = 0; i < n; ++i) {
+        vlf[i] = std::isfinite(H.vlb[i]) ? H.vlb[i] : 0.0;
+        vuf[i] = std::isfinite(H.vub[i]) ? H.vub[i] : 0.0;
+    }
+    h2d(P_.vlb_fin, vlf.data(), n * 8);
+    h2d(P_.vub_fin, vuf.data(), n * 8);
+    if (qtype_ == Q_DIAG) h2d(P_.diag, diag_.data(), n * 8);
+    h2d(P_.dcum, H.dcum.data(), n * 8);
+    if (m > 0) {
+        std::vector<double> clf(m), cuf(m);
+        for (size_t i = 0; i < m; ++i) {
+            clf[i] = std::isfinite(H.clb[i]) ? H.clb[i] : 0.0;
+            cuf[i] = std::isfinite(H.cub[i]) ? H.cub[i] : 0.0;
+        }
+        h2d(P_.clb, H.clb.data(), m * 8);
+        h2d(P_.cub, H.cub.data(), m * 8);
+        h2d(P_.clb_fin, clf.data(), m * 8);
+        h2d(P_.cub_fin, cuf.data(), m * 8);
+        h2d(P_.rcum, H.rcum.data(), m * 8);
+    }
+    /* iterates: zero, or the scaled warm start (solver_state.cu:621-656) */
+    for (double *p : {P_.x0, P_.x, P_.xh, P_.xbar, P_.dprod, P_.dslack, P_.dx, P_.qx, P_.grad, P_.dir})
+        PDAL_CUDA(cudaMemsetAsync(p, 0, n * 8, stream_));
+    for (double *p : {P_.y0, P_.y, P_.yh, P_.ybar, P_.dy, P_.aldual})
+        PDAL_CUDA(cudaMemsetAsync(p, 0, std::max<size_t>(m, 1) * 8, stream_));
+    PDAL_CUDA(cudaMemsetAsync(P_.rx, 0, std::max<size_t>(nr, 1) * 8, stream_));
+    std::vector<double> ws;
+    if (prob_->primal_start) {
+        ws.resize(n);
+        for (size_t i = 0; i < n; ++i) ws[i] = prob_->primal_start[i] * H.dcum[i] * H.cbr;
+        for (double *p : {P_.x0, P_.x, P_.xh}) h2d(p, ws.data(), n * 8);
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
+    }
+    if (prob_->dual_start && m > 0) {
+        ws.resize(m);
+        for (size_t i = 0; i < m; ++i) ws[i] = prob_->dual_start[i] * H.rcum[i] * H.ovr;
+        for (double *p : {P_.y0, P_.y, P_.yh}) h2d(p, ws.data(), m * 8);
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
+    }
+    PDAL_CUDA(cudaMemsetAsync(P_.lpart, 0, (size_t)3 * nl * kSlot * 8, stream_));
+    PDAL_CUDA(cudaMemsetAsync(P_.ctl, 0, sizeof(Ctl), stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+}
+
+Args FacpSolver::base_args(int mode) const {
+    Args a{};
+    a.mode = mode;
+    a.F = p_.termination_evaluation_frequency;
+    a.linf = p_.optimality_norm == NORM_TYPE_L_INF;
+    a.cbr = H_.cbr;
+    a.ovr = H_.ovr;
+    a.c0 = H_.c0;
+    a.obj_norm = H_.obj_norm;
+    a.bnd_norm = H_.bnd_norm;
+    a.step = step_;
+    a.pw = pw_;
+    a.tau_eval = step_ > 0 ? step_ / pw_ : 1.0;
+    a.refl = p_.reflection_coefficient;
+    a.max_iter = p_.sv_max_iter;
+    a.tol = p_.sv_tol;
+    return a;
+}
+
+void FacpSolver::launch(Args a) {
+    PDAL_CUDA(cudaMemsetAsync(P_.bar, 0, sizeof(GridBar), stream_));
+    if (P_.nlong_total > 0)
+        PDAL_CUDA(cudaMemsetAsync(P_.lpart, 0, (size_t)3 * P_.nlong_total * kSlot * 8, stream_));
+    void *args[] = {(void *)&P_, (void *)&a};
+    PDAL_CUDA(cudaLaunchCooperativeKernel((const void *)k_facp, dim3(grid_), dim3(kThreads), args, 0, stream_));
+    ++launches_;
+}
+
+void FacpSolver::read_ctl() {
+    PDAL_CUDA(cudaMemcpyAsync(&ctl_, P_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    if (ctl_.status != 0) throw Error("the persistent kernel gave up waiting at a grid barrier");
+}
+
+void FacpSolver::power_iterations() {
+    const HostQP &H = H_;
+    if (qtype_ == Q_SPARSE) { /* solver_state.cu:462-476 */
+        CRandom rnd(1);
+        std::vector<double> v(H.n);
+        for (double &x : v) x = (double)rnd.next() / CRandom::kMax;
+        PDAL_CUDA(cudaMemcpyAsync(P_.pv, v.data(), H.n * 8, cudaMemcpyHostToDevice, stream_));
+        launch(base_args(MODE_POWER_QMAX));
+        read_ctl();
+        qnorm_ = ctl_.power_value;
+        for (double &x : v) x = (double)rnd.next() / CRandom::kMax;
+        PDAL_CUDA(cudaMemcpyAsync(P_.pv, v.data(), H.n * 8, cudaMemcpyHostToDevice, stream_));
+        Args a = base_args(MODE_POWER_QMIN);
+        a.lam_max = qnorm_;
+        launch(a);
+        read_ctl();
+        nonconvexity_ = ctl_.power_value;
+    }
+    if (M_[MAT_A].h.nnz() == 0) { /* fa_cp_core_op.cu:1022-1040 */
+        step_ = 1.0;
+    } else {
+        std::mt19937 gen(1);
+        std::normal_distribution<double> dist(0.0, 1.0);
+        std::vector<double> v(H.m);
+        for (double &x : v) x = dist(gen);
+        PDAL_CUDA(cudaMemcpyAsync(P_.pv, v.data(), H.m * 8, cudaMemcpyHostToDevice, stream_));
+        launch(base_args(MODE_POWER_A));
+        read_ctl();
+        sv_max_ = ctl_.power_value;
+        step_ = 0.998 / sv_max_;
+    }
+    pw_ = p_.bound_objective_rescaling ? 1.0 : (H.obj_norm + 1.0) / (H.bnd_norm + 1.0);
+    best_pw_ = pw_;
+}
+
+void FacpSolver::evaluate(bool infeas) {
+    Args a = base_args(MODE_EVAL);
+    a.infeas = infeas ? 1 : 0;
+    launch(a);
+    read_ctl();
+    ++evals_;
+}
+
+bool FacpSolver::check_termination(double elapsed) { /* QP/FA_CP/src/utils.cu:413-462 */
+    const auto &T = p_.termination_criteria;
+    if (ctl_.rel_d < T.eps_feasible_relative && ctl_.rel_p < T.eps_feasible_relative &&
+        ctl_.rel_gap < T.eps_optimal_relative)
+        reason_ = TERMINATION_REASON_OPTIMAL;
+    else if (ctl_.dray_obj > 0.0 && ctl_.max_dray / ctl_.dray_obj <= T.eps_infeasible)
+        reason_ = TERMINATION_REASON_PRIMAL_INFEASIBLE;
+    else if (ctl_.pray_lin < 0.0 && ctl_.max_pray / (-ctl_.pray_lin) <= T.eps_infeasible)
+        reason_ = TERMINATION_REASON_DUAL_INFEASIBLE;
+    else if (total_ >= T.iteration_limit)
+        reason_ = TERMINATION_REASON_ITERATION_LIMIT;
+    else if (elapsed >= T.time_sec_limit)
+        reason_ = TERMINATION_REASON_TIME_LIMIT;
+    return reason_ != TERMINATION_REASON_UNSPECIFIED;
+}
+
+bool FacpSolver::should_restart() { /* QP/FA_CP/src/utils.cu:464-492 */
+    const auto &R = p_.restart_params;
+    const int F = p_.termination_evaluation_frequency;
+    bool rs = false;
+    if (total_ == F) {
+        rs = true;
+    } else if (total_ > F) {
+        if (fp_ <= R.sufficient_reduction_for_restart * fp0_) rs = true;
+        if (fp_ <= R.necessary_reduction_for_restart * fp0_ && fp_ > fp_last_) rs = true;
+        if (inner_ >= R.artificial_restart_threshold * total_) rs = true;
+    }
+    fp_last_ = fp_;
+    return rs;
+}
+
+void FacpSolver::choose_restart_candidate(double elapsed) { /* fa_cp_core_op.cu:1130-1169 */
+    restart_target_ = 0;
+    const double cur = std::isfinite(fp_) ? fp_ : INFINITY;
+    if (o_.restart_select == 0 || total_ == 0 || !std::isfinite(cur)) return;
+    if (total_ < o_.restart_select_min_iters || elapsed < o_.restart_select_min_time) return;
+    launch(base_args(MODE_DELTA_SCORE));
+    read_ctl();
+    const double halpern = ctl_.score;
+    if (!(cur > 0.0)) return;
+    if (o_.restart_select == 2 || (std::isfinite(halpern) && halpern < o_.restart_select_margin * cur)) {
+        restart_target_ = 1;
+        fp_ = halpern;
+    }
+}
+
+void FacpSolver::set_sigma_active(double s, double zt) {
+    if (!std::isfinite(s) || s <= zt) {
+        al_sigma_ = 0.0;
+        use_al_ = false;
+    } else {
+        al_sigma_ = s;
+        use_al_ = al_available_;
+    }
+}
+
+double FacpSolver::clipped(double cur, double ratio) const {
+    const double gain = sane_positive(p_.sigma_update_gain, 0.5);
+    double lo = sane_positive(p_.sigma_clip_low, 0.6), hi = sane_positive(p_.sigma_clip_high, 1.7);
+    if (lo > hi) std::swap(lo, hi);
+    ratio = sane_positive(ratio, 1.0);
+    return cur * clamp_d(std::pow(ratio, gain), lo, hi);
+}
+
+/* The sigma rules of update_al_sigma_at_restart (fa_cp_core_op.cu:722-906). */
+void FacpSolver::update_sigma(double pd, double dd, double normal) {
+    const int rule = p_.sigma_update_rule;
+    const bool bal = rule == FA_CP_SIGMA_UPDATE_BALANCED_GUARDED;
+    const bool guarded = rule == FA_CP_SIGMA_UPDATE_GUARDED || bal;
+    if (!al_available_ || rule == FA_CP_SIGMA_UPDATE_FIXED) return;
+    if (!guarded && !use_al_) return;
+    const double ref = bal ? sane_positive(step_ * pw_, 1.0) : 1.0;
+    double smin = sane_positive(p_.sigma_min, 1e-8) * ref;
+    double smax = sane_positive(p_.sigma_max, 10.0) * ref;
+    const double zt = sane_positive(p_.sigma_zero_threshold, sane_positive(p_.sigma_min, 1e-8)) * ref;
+    if (smin > smax) std::swap(smin, smax);
+    if (zt > smin) smin = zt;
+    const double cur = use_al_ ? clamp_d(sane_positive(al_sigma_, smin), smin, smax) : 0.0;
+    set_sigma_active(cur, zt);
+    const double rp = sane_positive(ctl_.rel_p, 1e-300), rd = sane_positive(ctl_.rel_d, 1e-300),
+                 rg = sane_positive(ctl_.rel_gap, 1e-300);
+    const double score = std::fmax(score_component(ctl_.rel_p),
+                                   std::fmax(score_component(ctl_.rel_d), score_component(ctl_.rel_gap)));
+    if (!std::isfinite(score)) return;
+    if (!std::isfinite(best_sigma_score_) || score < best_sigma_score_) {
+        best_sigma_score_ = score;
+        best_al_sigma_ = cur;
+    }
+    auto record = [&]() {
+        last_sigma_score_ = score;
+        last_rp_ = rp;
+        last_rd_ = rd;
+        last_rg_ = rg;
+        sigma_updates_++;
+    };
+    if (p_.sigma_rollback_tol > 0.0 && (!guarded || cur > zt) && std::isfinite(best_sigma_score_) &&
+        best_sigma_score_ > 0.0 && score > p_.sigma_rollback_tol * best_sigma_score_ &&
+        std::isfinite(best_al_sigma_) && (guarded ? best_al_sigma_ >= 0.0 : best_al_sigma_ > 0.0)) {
+        set_sigma_active((guarded && best_al_sigma_ <= zt) ? 0.0 : clamp_d(best_al_sigma_, smin, smax), zt);
+        record();
+        return;
+    }
+    double prop = cur;
+    switch (rule) {
+    case FA_CP_SIGMA_UPDATE_RESIDUAL_BALANCE:
+        prop = clipped(cur, rp / rd);
+        break;
+    case FA_CP_SIGMA_UPDATE_KKT_BALANCE:
+        prop = clipped(cur, rp / std::fmax(rd, rg));
+        break;
+    case FA_CP_SIGMA_UPDATE_DISPLACEMENT:
+        if (std::isfinite(pd) && std::isfinite(dd) && pd > 1e-16 && dd > 1e-16)
+            prop = clipped(cur, clamp_d(dd / pd, smin, smax) / cur);
+        break;
+    case FA_CP_SIGMA_UPDATE_PROGRESS: {
+        const double last_other = std::fmax(last_rd_, last_rg_), other = std::fmax(rd, rg);
+        if (std::isfinite(last_rp_) && std::isfinite(last_other) && last_rp_ > 0.0 && last_other > 0.0)
+            prop = clipped(cur, (last_other / other) / (last_rp_ / rp));
+        else
+            prop = clipped(cur, rp / std::fmax(rd, rg));
+        break;
+    }
+    case FA_CP_SIGMA_UPDATE_GREEDY_SCORE:
+        if (sigma_updates_ == 0)
+            sigma_dir_ = (rp >= std::fmax(rd, rg)) ? 1 : -1;
+        else if (std::isfinite(last_sigma_score_) && score > last_sigma_score_)
+            sigma_dir_ = -sigma_dir_;
+        prop = clipped(cur, sigma_dir_ > 0 ? p_.sigma_clip_high : p_.sigma_clip_low);
+        break;
+    case FA_CP_SIGMA_UPDATE_GUARDED:
+    case FA_CP_SIGMA_UPDATE_BALANCED_GUARDED: {
+        const double nmt = sane_positive(p_.sigma_normal_motion_threshold, 1e-10);
+        const bool normal_ok = !std::isfinite(normal) || normal > nmt;
+        const bool zero_ok = !std::isfinite(normal) || normal > std::fmax(nmt, 2e-1);
+        const bool bottleneck =
+            rp >= sane_positive(p_.sigma_activation_threshold, 2.0) * sane_positive(std::fmax(rd, rg), 1e-300);
+        const bool zero_stalled = cur <= zt && std::isfinite(last_sigma_score_) && score > 0.9 * last_sigma_score_;
+        const bool primal_signal = rp >= 0.5 * sane_positive(rd, 1e-300);
+        const double act = sane_positive(p_.sigma_activation_value, 0.1) * ref;
+        const bool scale_ok = !bal || act >= 1e-6;
+        const bool activate = cur <= zt ? (zero_ok && zero_stalled && primal_signal && scale_ok) : (normal_ok && bottleneck);
+        if (cur <= zt)
+            prop = activate ? act : 0.0;
+        else if (!normal_ok || !activate)
+            prop = clipped(cur, p_.sigma_clip_low);
+        else
+            prop = clipped(cur, rp / std::fmax(rd, rg));
+        break;
+    }
+    default:
+        break;
+    }
+    prop = prop > zt ? clamp_d(prop, smin, smax) : 0.0;
+    set_sigma_active(prop, zt);
+    record();
+}
+
+void FacpSolver::perform_restart() { /* fa_cp_core_op.cu:908-1020 */
+    Args a = base_args(MODE_RESTART);
+    const bool to_halpern = o_.restart_select != 0 && restart_target_ == 1;
+    if (to_halpern) {
+        /* measure against the current (Halpern) iterate: swap the roles of
+         * xh/x and yh/y for the measurement launch */
+        std::swap(P_.xh, P_.x);
+        std::swap(P_.yh, P_.y);
+    }
+    launch(a);
+    read_ctl();
+    if (to_halpern) {
+        std::swap(P_.xh, P_.x);
+        std::swap(P_.yh, P_.y);
+    }
+    const double pd = ctl_.pd, dd = ctl_.dd;
+    double normal = INFINITY;
+    if (pd > 1e-16 && std::isfinite(pd)) normal = ctl_.normal_dist / pd;
+    const double ratio = ctl_.rel_d / ctl_.rel_p;
+    const auto &R = p_.restart_params;
+    if (pd > 1e-16 && dd > 1e-16 && pd < 1e12 && dd < 1e12 && ratio > 1e-8 && ratio < 1e8) {
+        const double err = std::log(dd) - std::log(pd) - std::log(pw_);
+        pw_esum_ *= R.i_smooth;
+        pw_esum_ += err;
+        const double de = err - pw_last_;
+        pw_ *= std::exp(R.k_p * err + R.k_i * pw_esum_ + R.k_d * de);
+        pw_last_ = err;
+    } else {
+        pw_ = best_pw_;
+        pw_esum_ = 0.0;
+        pw_last_ = 0.0;
+    }
+    const double g = std::fabs(std::log10(ctl_.rel_d / ctl_.rel_p));
+    if (g < best_gap_) {
+        best_gap_ = g;
+        best_pw_ = pw_;
+    }
+    update_sigma(pd, dd, normal);
+    const size_t nb = (size_t)H_.n * 8, mb = (size_t)H_.m * 8;
+    double *src_x = to_halpern ? P_.x : P_.xh, *src_y = to_halpern ? P_.y : P_.yh;
+    double *dst_x = to_halpern ? P_.xh : P_.x, *dst_y = to_halpern ? P_.yh : P_.y;
+    PDAL_CUDA(cudaMemcpyAsync(P_.x0, src_x, nb, cudaMemcpyDeviceToDevice, stream_));
+    PDAL_CUDA(cudaMemcpyAsync(dst_x, src_x, nb, cudaMemcpyDeviceToDevice, stream_));
+    if (mb) {
+        PDAL_CUDA(cudaMemcpyAsync(P_.y0, src_y, mb, cudaMemcpyDeviceToDevice, stream_));
+        PDAL_CUDA(cudaMemcpyAsync(dst_y, src_y, mb, cudaMemcpyDeviceToDevice, stream_));
+    }
+    inner_ = 0;
+    fp_last_ = INFINITY;
+    ++restarts_;
+}
+
+void FacpSolver::print_eval() const {
+    printf("%6d %.1e | %8.1e  %8.1e | %.1e %.1e %.1e | %.1e %.1e %.1e \n", total_, 0.0, ctl_.pobj, ctl_.dobj,
+           ctl_.abs_p, ctl_.abs_d, ctl_.gap, ctl_.rel_p, ctl_.rel_d, ctl_.rel_gap);
+}
+
+fa_cp_result_t *FacpSolver::run() {
+    const double t_begin = now_sec();
+    prepare();
+    upload();
+    /* solver state */
+    al_available_ = p_.use_al_qp;
+    use_al_ = p_.use_al_qp;
+    al_sigma_ = p_.al_sigma;
+    best_al_sigma_ = p_.al_sigma;
+    power_iterations();
+    if (al_available_ && p_.al_sigma <= p_.sigma_zero_threshold) {
+        use_al_ = false;
+        al_sigma_ = 0.0;
+    }
+    has_inner_ = use_al_ || al_available_ || !(qtype_ == Q_NONE || qtype_ == Q_DIAG);
+    inner_limit_ = nonconvexity_ < 0 ? 1 : 1000;
+    ctl_ = Ctl{};
+    ctl_.inner_tol = 1e-3;
+    ctl_.fp = INFINITY;
+    ctl_.fp_first = INFINITY;
+    PDAL_CUDA(cudaMemcpyAsync(P_.ctl, &ctl_, sizeof(Ctl), cudaMemcpyHostToDevice, stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    const double t_loop = now_sec();
+    setup_sec_ = t_loop - t_begin;
+
+    const int F = p_.termination_evaluation_frequency;
+    const int limit = p_.termination_criteria.iteration_limit;
+    bool major = false, do_restart = false;
+    double elapsed = 0.0;
+    while (total_ < limit) { /* QP/FA_CP/src/solver.cu:94-144 */
+        const bool consider = major || total_ == 0;
+        bool planned = false;
+        if (consider || (total_ % print_frequency_host(total_) == 0)) {
+            evaluate(major && total_ < 3 * F);
+            elapsed = now_sec() - t_loop;
+            check_termination(elapsed);
+            if (consider && reason_ == TERMINATION_REASON_UNSPECIFIED) {
+                choose_restart_candidate(elapsed);
+                planned = should_restart();
+            }
+            if (p_.verbose >= 2) print_eval();
+            if (reason_ != TERMINATION_REASON_UNSPECIFIED) break;
+        }
+        if (consider) {
+            do_restart = planned;
+            if (do_restart) perform_restart();
+        }
+        /* iterations up to the next evaluation point */
+        int t_end = total_ + 1;
+        while (t_end < limit && (t_end % F) != 0 && (t_end % print_frequency_host(t_end)) != 0) ++t_end;
+        double tau = step_ / pw_;
+        if (nonconvexity_ < 0) {
+            tau = std::fmax(tau, -1.01 * std::fmin(0.0, nonconvexity_));
+            tau /= 2;
+        }
+        Args a = base_args(MODE_SEGMENT);
+        a.t0 = total_;
+        a.t1 = t_end;
+        a.inner0 = inner_;
+        a.fp_first = do_restart ? 1 : 0;
+        a.has_inner = has_inner_ ? 1 : 0;
+        a.inner_limit = inner_limit_;
+        a.use_al = use_al_ ? 1 : 0;
+        a.tau = tau;
+        a.rho = step_ * pw_;
+        a.sigma = use_al_ ? al_sigma_ : 0.0;
+        PDAL_CUDA(cudaEventRecord(ev0_, stream_));
+        launch(a);
+        PDAL_CUDA(cudaEventRecord(ev1_, stream_));
+        read_ctl();
+        float ms = 0.f;
+        PDAL_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+        dev_ms_ += ms;
+        major = (t_end % F) == 0;
+        if (major || do_restart) fp_ = ctl_.fp;
+        if (do_restart) {
+            fp0_ = ctl_.fp_first;
+            do_restart = false;
+        }
+        inner_ += t_end - total_;
+        total_ = t_end;
+    }
+    if (reason_ == TERMINATION_REASON_UNSPECIFIED) {
+        reason_ = TERMINATION_REASON_ITERATION_LIMIT;
+        evaluate(false);
+        if (p_.verbose >= 2) print_eval();
+    }
+    elapsed = now_sec() - t_loop;
+
+    launch(base_args(MODE_RESULT));
+    fa_cp_result_t *r = (fa_cp_result_t *)calloc(1, sizeof(fa_cp_result_t));
+    if (!r) throw Error("out of host memory");
+    const int n = H_.n, m = H_.m;
+    r->primal_solution = (double *)malloc(sizeof(double) * (size_t)std::max(n, 1));
+    r->dual_solution = (double *)malloc(sizeof(double) * (size_t)std::max(m, 1));
+    r->reduced_cost = (double *)malloc(sizeof(double) * (size_t)std::max(n, 1));
+    if (!r->primal_solution || !r->dual_solution || !r->reduced_cost) {
+        fa_cp_result_free(r);
+        throw Error("out of host memory");
+    }
+    PDAL_CUDA(cudaMemcpyAsync(r->primal_solution, P_.out_x, (size_t)n * 8, cudaMemcpyDeviceToHost, stream_));
+    PDAL_CUDA(cudaMemcpyAsync(r->reduced_cost, P_.out_rc, (size_t)n * 8, cudaMemcpyDeviceToHost, stream_));
+    if (m > 0) PDAL_CUDA(cudaMemcpyAsync(r->dual_solution, P_.out_y, (size_t)m * 8, cudaMemcpyDeviceToHost, stream_));
+    read_ctl();
+    r->num_variables = n;
+    r->num_constraints = m;
+    r->num_nonzeros = prob_->constraint_matrix_num_nonzeros;
+    r->total_count = total_;
+    r->total_inner_count = (int)ctl_.inner_total;
+    r->rescaling_time_sec = rescale_sec_;
+    r->cumulative_time_sec = elapsed;
+    r->absolute_primal_residual = ctl_.abs_p;
+    r->relative_primal_residual = ctl_.rel_p;
+    r->absolute_dual_residual = ctl_.abs_d;
+    r->relative_dual_residual = ctl_.rel_d;
+    r->primal_objective_value = ctl_.pobj;
+    r->dual_objective_value = ctl_.dobj;
+    r->objective_gap = ctl_.gap;
+    r->relative_objective_gap = ctl_.rel_gap;
+    r->max_primal_ray_infeasibility = ctl_.max_pray;
+    r->max_dual_ray_infeasibility = ctl_.max_dray;
+    r->primal_ray_linear_objective = ctl_.pray_lin;
+    r->dual_ray_objective = ctl_.dray_obj;
+    r->final_al_sigma = al_sigma_;
+    r->sigma_update_count = sigma_updates_;
+    r->sigma_update_rule = al_available_ ? p_.sigma_update_rule : FA_CP_SIGMA_UPDATE_FIXED;
+    r->termination_reason = reason_;
+
+    fa_cp_gb300_stats_t &st = g_stats;
+    memset(&st, 0, sizeof(st));
+    st.setup_sec = setup_sec_;
+    st.loop_sec = elapsed;
+    st.total_sec = now_sec() - t_begin;
+    st.max_singular_value = sv_max_;
+    st.q_norm = qnorm_;
+    st.q_nonconvexity = nonconvexity_;
+    st.q_type = qtype_;
+    st.grid_blocks = grid_;
+    st.restarts = restarts_;
+    st.evaluations = evals_;
+    st.kernel_launches = launches_;
+    st.inner_iterations = ctl_.inner_total;
+    st.primal_weight = pw_;
+    st.step_size = step_;
+    st.device_loop_ms = dev_ms_;
+    if (p_.verbose >= 1)
+        printf("[fa_cp_gb300] %s after %d iterations (%lld inner), objective %.10e, rel. KKT %.2e, %.3f s\n",
+               reason_ == TERMINATION_REASON_OPTIMAL ? "optimal" : "stopped", total_, (long long)ctl_.inner_total,
+               ctl_.pobj, std::max(ctl_.rel_p, std::max(ctl_.rel_d, ctl_.rel_gap)), st.total_sec);
+    return r;
+}
+
+fa_cp_result_t *solve_guarded(const qp_problem_t *prob, const fa_cp_parameters_t *params,
+                              const fa_cp_gb300_options_t *opts) {
+    g_error.clear();
+    fa_cp_parameters_t p;
+    if (params)
+        p = *params;
+    else
+        set_default_parameters(&p);
+    fa_cp_gb300_options_t o;
+    if (opts)
+        o = *opts;
+    else
+        fa_cp_gb300_default_options(&o);
+    try {
+        FacpSolver s(prob, p, o);
+        return s.run();
+    } catch (const std::exception &e) {
+        g_error = e.what();
+        fprintf(stderr, "[fa_cp_gb300] %s\n", e.what());
+        return nullptr;
+    }
+}
+
+} // namespace
+} // namespace pdal
+
+extern "C" {
+
+fa_cp_result_t *solve_qp_problem(const qp_problem_t *prob, const fa_cp_parameters_t *params) {
+    fa_cp_gb300_options_t o;
+    fa_cp_gb300_options_from_env(&o);
+    return pdal::solve_guarded(prob, params, &o);
+}
+
+fa_cp_result_t *fa_cp_gb300_solve(const qp_problem_t *prob, const fa_cp_parameters_t *params,
+                                  const fa_cp_gb300_options_t *opts) {
+    return pdal::solve_guarded(prob, params, opts);
+}
+
+void fa_cp_gb300_last_stats(fa_cp_gb300_stats_t *stats) {
+    if (stats) *stats = pdal::g_stats;
+}
+
+const char *fa_cp_gb300_last_error(void) { return pdal::g_error.c_str(); }
+
+void fa_cp_gb300_rand_sequence(unsigned seed, int count, int *out) {
+    pdal::CRandom r(seed);
+    for (int i = 0; i < count; ++i) out[i] = r.next();
+}
+
+} // extern "C"

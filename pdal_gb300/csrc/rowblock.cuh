@@ -223,7 +223,7 @@ __device__ __forceinline__ void block_sum_t(T (&s)[NP], T *sbuf) {
 }
 
 /*
- * Runs the row block blockIdx.x of `plan`.
+ * Runs row block `blk` of `plan` (rowblock_run below: blk = blockIdx.x).
  *   gat(col, T out[NP])         the NP vector entries a nonzero in column col
  *                               multiplies (one per simultaneous product)
  *   epi(row, const T s[NP], R&) the fused row epilogue; may add to R
@@ -234,13 +234,13 @@ __device__ __forceinline__ void block_sum_t(T (&s)[NP], T *sbuf) {
  * on which block finished last).
  */
 template <int S, int NP, typename T, class R, class Gat, class Epi>
-__device__ __forceinline__ void rowblock_run(const RowPlanDev &plan, const int *__restrict__ rp,
-                                             const int *__restrict__ ci, const T *__restrict__ val, Gat &gat, Epi &epi,
-                                             R &red, RowBlockSmem<S, NP, T> &sm) {
+__device__ __forceinline__ void rowblock_run_at(int blk, const RowPlanDev &plan, const int *__restrict__ rp,
+                                                const int *__restrict__ ci, const T *__restrict__ val, Gat &gat,
+                                                Epi &epi, R &red, RowBlockSmem<S, NP, T> &sm) {
     constexpr int NT = kThreads;
     static_assert(S % NT == 0, "S must be a multiple of the block size");
     static_assert(NP <= kLongStride, "too many products per nonzero");
-    const int4 d = plan.desc[blockIdx.x];
+    const int4 d = plan.desc[blk];
     const int tid = threadIdx.x;
     if (d.y >= d.x) {
         const int r0 = d.x, nrows = d.y - d.x, k0 = d.z, k1 = d.w;
@@ -326,6 +326,13 @@ __device__ __forceinline__ void rowblock_run(const RowPlanDev &plan, const int *
             epi.long_red(lid, lr);
         }
     }
+}
+
+template <int S, int NP, typename T, class R, class Gat, class Epi>
+__device__ __forceinline__ void rowblock_run(const RowPlanDev &plan, const int *__restrict__ rp,
+                                             const int *__restrict__ ci, const T *__restrict__ val, Gat &gat, Epi &epi,
+                                             R &red, RowBlockSmem<S, NP, T> &sm) {
+    rowblock_run_at<S, NP, T>((int)blockIdx.x, plan, rp, ci, val, gat, epi, red, sm);
 }
 
 } // namespace pdal

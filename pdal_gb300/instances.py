@@ -192,3 +192,74 @@ def docs_example_lp() -> LPData:
     v = np.array([1.0, 2.0, 1.0, 3.0, 2.0])
     return LPData(np.array([1.0, 1.0]), (rp, ci, v, (3, 2)), np.array([5.0, -np.inf, -np.inf]),
                   np.array([5.0, 2.0, 8.0]), np.full(2, -np.inf), np.full(2, np.inf))
+
+
+def planted_qp(n: int = 200_000, m: int = 100_000, nnz_per_col: int = 10, b_rows: int = 50_000,
+               b_nnz_per_row: int = 5, seed: int = 2000, eq_fraction: float = 0.5, diag_lo: float = 1e-4,
+               q_form: str = "sparse"):
+    """Convex QP with a known optimum (the FA_CP workload at its default sizes):
+    A has nnz_per_col N(0,1) entries per column; Q = B'B + diag(U[diag_lo, 1])
+    with B b_rows x n at b_nnz_per_row N(0,1) entries per row; box
+    -U[0,10] <= x <= U[0,10].  x* lies strictly inside the box, y* ~ N(0,1)
+    on equality rows and -|N(0,1)| or 0 on the <= rows (active rows get
+    u = (Ax*)_i, the others a positive slack), and c = -Q x* + A'y*, so x*
+    satisfies the KKT conditions exactly and f* = 1/2 x*'Qx* + c'x*.
+
+    q_form "sparse" stores Q explicitly (SPARSE_Q path); "lowrank" passes
+    R = B and the diagonal as a separate Q (LOW_RANK_PLUS_SPARSE_Q path).
+    Returns (QPData, x_star, f_star)."""
+    from .qp import QPData
+
+    rng = np.random.default_rng(seed)
+    rows, cols = _distinct_rows_per_col(rng, m, n, nnz_per_col)
+    A = _csr_from_coo(rows, cols, rng.standard_normal(rows.shape[0]), m, n)
+    br = np.repeat(np.arange(b_rows), b_nnz_per_row)
+    bc = rng.integers(0, n, size=br.shape[0])
+    key = br.astype(np.int64) * n + bc
+    key = np.unique(key)
+    br, bc = (key // n).astype(np.int64), (key % n).astype(np.int64)
+    B = _csr_from_coo(br, bc, rng.standard_normal(br.shape[0]), b_rows, n)
+    dq = diag_lo + rng.random(n) * (1.0 - diag_lo)
+    lo = -10.0 * rng.random(n)
+    hi = 10.0 * rng.random(n)
+    x = lo + (0.1 + 0.8 * rng.random(n)) * (hi - lo)
+
+    def csr_mv(M, v, nr):
+        rp, ci, vals = M
+        out = np.zeros(nr)
+        np.add.at(out, np.repeat(np.arange(nr), np.diff(rp)), vals * v[ci])
+        return out
+
+    def csr_tmv(M, v, nr, nc):
+        rp, ci, vals = M
+        out = np.zeros(nc)
+        np.add.at(out, ci, vals * v[np.repeat(np.arange(nr), np.diff(rp))])
+        return out
+
+    Bx = csr_mv(B, x, b_rows)
+    Qx = csr_tmv(B, Bx, b_rows, n) + dq * x
+    Ax = csr_mv(A, x, m)
+    is_eq = rng.random(m) < eq_fraction
+    active = rng.random(m) < 0.5
+    y = rng.standard_normal(m)
+    y = np.where(is_eq, y, np.where(active, -np.abs(y), 0.0))
+    con_ub = Ax + np.where(is_eq | active, 0.0, rng.random(m))
+    con_lb = np.where(is_eq, Ax, -np.inf)
+    c = -Qx + csr_tmv(A, y, m, n)
+    f = 0.5 * float(x @ Qx) + float(c @ x)
+    Acsr = (A[0], A[1], A[2], (m, n))
+    if q_form == "sparse":
+        import scipy.sparse as sp
+
+        Bs = sp.csr_matrix((B[2], B[1], B[0]), shape=(b_rows, n))
+        Q = (Bs.T @ Bs + sp.diags(dq)).tocsr()
+        Q.sort_indices()
+        data = QPData(c=c, A=Acsr, con_lb=con_lb, con_ub=con_ub, var_lb=lo, var_ub=hi,
+                      Q=(Q.indptr, Q.indices, Q.data, Q.shape))
+    elif q_form == "lowrank":
+        diag = (np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32), dq, (n, n))
+        data = QPData(c=c, A=Acsr, con_lb=con_lb, con_ub=con_ub, var_lb=lo, var_ub=hi, Q=diag,
+                      R=(B[0], B[1], B[2], (b_rows, n)))
+    else:
+        raise ValueError(q_form)
+    return data, x, f

@@ -21,3 +21,13 @@ def lp_lib():
     if not N.lib_path("libcp_al_gb300.so").exists():
         build.build_product()
     return N.load_lp()
+
+
+@pytest.fixture(scope="session")
+def qp_lib():
+    from pdal_gb300 import _native as N
+    from pdal_gb300 import build
+
+    if not N.lib_path("libfa_cp_gb300.so").exists():
+        build.build_product()
+    return N.load_qp()

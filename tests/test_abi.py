@@ -13,7 +13,7 @@ from pdal_gb300 import _native as N
 from pdal_gb300 import lp
 
 ROOT = Path(__file__).resolve().parent.parent
-HEADERS = {"libcp_al_gb300.so": ["cp_al.h", "cp_al_gb300.h"]}
+HEADERS = {"libcp_al_gb300.so": ["cp_al.h", "cp_al_gb300.h"], "libfa_cp_gb300.so": ["fa_cp.h", "fa_cp_gb300.h"]}
 
 
 def declared_functions(header: Path):
@@ -23,7 +23,7 @@ def declared_functions(header: Path):
 
 
 @pytest.mark.parametrize("libname", list(HEADERS))
-def test_library_exports_every_declared_symbol(libname, lp_lib):
+def test_library_exports_every_declared_symbol(libname, lp_lib, qp_lib):
     lib = C.CDLL(str(N.lib_path(libname)))
     for h in HEADERS[libname]:
         for fn in declared_functions(ROOT / "include" / h):
@@ -77,6 +77,50 @@ def test_struct_layouts_match_c(tmp_path):
     }
     for k, v in offs.items():
         assert int(out[k]) == v, k
+
+
+QP_PROBE = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "fa_cp_types.h"
+#include "fa_cp_gb300.h"
+#define S(T) printf(#T " %zu\n", sizeof(T));
+#define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
+int main(void) {
+  S(qp_problem_t) S(fa_cp_parameters_t) S(fa_cp_result_t) S(matrix_desc_t) S(fa_cp_gb300_options_t)
+  S(fa_cp_gb300_stats_t) S(termination_criteria_t) S(restart_parameters_t) S(CsrComponent)
+  O(fa_cp_parameters_t, trajectory_csv) O(fa_cp_parameters_t, sigma_update_rule) O(fa_cp_parameters_t, verbose)
+  O(fa_cp_parameters_t, termination_criteria) O(fa_cp_parameters_t, restart_params)
+  O(fa_cp_parameters_t, feasibility_polishing) O(fa_cp_parameters_t, optimality_norm)
+  O(fa_cp_result_t, total_inner_count) O(fa_cp_result_t, final_al_sigma) O(fa_cp_result_t, termination_reason)
+  O(fa_cp_result_t, feasibility_iteration) O(qp_problem_t, objective_lowrank_matrix) O(qp_problem_t, dual_start)
+  O(matrix_desc_t, zero_tolerance) O(matrix_desc_t, data) O(termination_criteria_t, iteration_limit)
+  O(fa_cp_gb300_stats_t, device_loop_ms)
+  return 0;
+}
+"""
+
+
+def test_qp_struct_layouts_match_c(tmp_path):
+    src = tmp_path / "probe.c"
+    src.write_text(QP_PROBE)
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.rsplit(" ", 1) for line in subprocess.check_output([str(exe)], text=True).splitlines())
+    sizes = {
+        "qp_problem_t": N.QpProblem, "fa_cp_parameters_t": N.FacpParameters, "fa_cp_result_t": N.FacpResult,
+        "matrix_desc_t": N.QpMatrixDesc, "fa_cp_gb300_options_t": N.FacpOptions, "fa_cp_gb300_stats_t": N.FacpStats,
+        "termination_criteria_t": N.FacpTerminationCriteria, "restart_parameters_t": N.RestartParams,
+        "CsrComponent": N.CsrComponent,
+    }
+    for cname, ct in sizes.items():
+        assert int(out[cname]) == C.sizeof(ct), cname
+    for key, val in out.items():
+        if "." not in key:
+            continue
+        cname, field = key.split(".")
+        ct = {**sizes, "termination_criteria_t": N.FacpTerminationCriteria}[cname]
+        assert int(val) == getattr(ct, field).offset, key
 
 
 def _problem_from_desc(lib, desc, m, n):

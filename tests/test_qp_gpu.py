@@ -1,0 +1,169 @@
+"""FA_CP (convex QP) on the GPU through the C-ABI library, against the CPU
+oracle and the known answers.
+
+Tolerances: both sides compute in FP64 with different summation orders, so
+iterates agree to ~1e-12 relative per step; after hundreds of iterations and
+a few restart decisions the fixed-iteration iterates are compared at 1e-7
+(relative to the vector's scale), objective values at the requested
+tolerance, iteration counts exactly where both stop at the same evaluation.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import oracle as O
+from pdal_gb300 import qp
+from pdal_gb300.instances import planted_qp, random_lp
+from pdal_gb300.qp import QPData
+from test_oracle_qp import A3, INF, docs_diag_qp, docs_lowrank_qp
+
+pytestmark = pytest.mark.gpu
+
+
+def both(data, params):
+    g = qp.solve(data, {**params, "verbose": 0})
+    o = O.solve_qp(data, params)
+    return g, o
+
+
+@pytest.mark.parametrize("make,f", [(docs_diag_qp, -20.0 / 3.0), (docs_lowrank_qp, -8.0)])
+def test_docs_examples(make, f):
+    g, o = both(make(), {"eps": 1e-9})
+    assert g.status == o.status == "OPTIMAL"
+    assert abs(g.primal_objective - f) < 1e-7 * abs(f)
+    np.testing.assert_allclose(g.x, [2 / 3, 4 / 3], atol=1e-7)
+    assert g.iterations == o.iterations
+
+
+def test_model_interface_solves_readme_example():
+    from pdal_gb300.fa_cp import FA_CP, Model
+
+    m = Model(objective_matrix=sp.csc_matrix([[1.0, -1.0], [-1.0, 2.0]]),
+              objective_matrix_low_rank=sp.csc_matrix([[1.0, 0.0]]), objective_vector=np.array([-2.0, -6.0]),
+              constraint_matrix=sp.csc_matrix(A3), constraint_lower_bound=np.full(3, -INF),
+              constraint_upper_bound=np.array([2.0, 2.0, 3.0]), variable_lower_bound=np.zeros(2),
+              variable_upper_bound=np.full(2, INF))
+    m.setParams(LogLevel=0, OptimalityTol=1e-8, FeasibilityTol=1e-8)
+    m.optimize()
+    assert m.Status == "OPTIMAL" and m.StatusCode == FA_CP.OPTIMAL
+    assert abs(m.ObjVal + 8.0) < 1e-6
+    np.testing.assert_allclose(m.X, [2 / 3, 4 / 3], atol=1e-6)
+    # MAXIMIZE flips the sign of c and c0 only (QP/FA_CP/python/fa_cp/model.py:500-553)
+    m.ModelSense = FA_CP.MAXIMIZE
+    m.setObjectiveVector(np.array([2.0, 6.0]))
+    m.optimize()
+    assert m.Status == "OPTIMAL" and abs(m.ObjVal - 8.0) < 1e-6
+    np.testing.assert_allclose(m.X, [2 / 3, 4 / 3], atol=1e-6)
+
+
+@pytest.mark.parametrize("form", ["sparse", "lowrank"])
+def test_planted_qp_matches_oracle(form):
+    data, xs, fs = planted_qp(n=3000, m=1500, b_rows=750, seed=21, q_form=form)
+    g, o = both(data, {"eps": 1e-7})
+    assert g.status == o.status == "OPTIMAL"
+    assert abs(g.primal_objective - fs) <= 1e-5 * (1 + abs(fs))
+    assert abs(g.iterations - o.iterations) <= 0.05 * o.iterations + 10
+    assert g.inner_iterations > 0
+
+
+@pytest.mark.parametrize("form,al_sigma", [("sparse", 0.0), ("lowrank", 0.0), ("sparse", 0.3)])
+def test_fixed_iterations_track_oracle(form, al_sigma):
+    """Same seed, same iteration budget: the iterates agree."""
+    data, _, _ = planted_qp(n=800, m=400, b_rows=200, seed=3, q_form=form)
+    prm = {"eps": 1e-14, "iteration_limit": 600, "al_sigma": al_sigma,
+           "sigma_update_rule": "fixed" if al_sigma else "guarded"}
+    g, o = both(data, prm)
+    assert g.iterations == o.iterations == 600
+    sx = 1 + np.abs(o.x).max()
+    sy = 1 + np.abs(o.y).max()
+    assert np.abs(g.x - o.x).max() <= 1e-7 * sx
+    assert np.abs(g.y - o.y).max() <= 1e-7 * sy
+    assert abs(g.inner_iterations - o.inner_iterations) <= 0.02 * o.inner_iterations + 5
+
+
+def test_lp_through_fa_cp_matches_oracle():
+    d = random_lp(m=400, n=1000, nnz_per_col=5, seed=9)
+    q = QPData(c=d.c, A=d.csr(), con_lb=d.con_lb, con_ub=d.con_ub, var_lb=d.var_lb, var_ub=d.var_ub)
+    g, o = both(q, {"eps": 1e-8})
+    assert g.status == o.status == "OPTIMAL"
+    assert abs(g.primal_objective - o.primal_objective) <= 1e-7 * (1 + abs(o.primal_objective))
+    assert abs(g.iterations - o.iterations) <= 0.05 * o.iterations + 10
+    g2, o2 = both(q, {"eps": 1e-14, "iteration_limit": 500})
+    assert np.abs(g2.x - o2.x).max() <= 1e-8 * (1 + np.abs(o2.x).max())
+
+
+@pytest.mark.parametrize("rule", ["residual_balance", "kkt_balance", "displacement", "progress", "greedy_score",
+                                  "balanced_guarded"])
+def test_sigma_rules_match_oracle(rule):
+    data, _, fs = planted_qp(n=600, m=300, b_rows=150, seed=5, q_form="sparse")
+    prm = {"eps": 1e-7, "al_sigma": 0.1, "sigma_update_rule": rule}
+    g, o = both(data, prm)
+    assert g.status == o.status
+    assert abs(g.sigma_update_count - o.sigma_update_count) <= 2
+    if o.status == "OPTIMAL":
+        assert abs(g.primal_objective - fs) <= 1e-5 * (1 + abs(fs))
+
+
+def test_infeasibility_detection():
+    d = QPData(c=np.array([1.0, 1.0]), A=np.array([[1.0, 1.0]]), con_lb=np.array([-INF]), con_ub=np.array([-1.0]),
+               var_lb=np.zeros(2), var_ub=np.full(2, INF), Q=np.eye(2))
+    g, o = both(d, {"eps": 1e-8, "iteration_limit": 20000})
+    assert g.status == o.status == "PRIMAL_INFEASIBLE"
+    d = QPData(c=np.array([-1.0, -1.0]), A=np.array([[1.0, -1.0]]), con_lb=np.array([0.0]), con_ub=np.array([0.0]),
+               var_lb=np.zeros(2), var_ub=np.full(2, INF))
+    g, o = both(d, {"eps": 1e-8, "iteration_limit": 20000})
+    assert g.status == o.status == "DUAL_INFEASIBLE"
+
+
+def test_long_rows_and_columns():
+    """A dense row and a dense column longer than one row block (1,024), and
+    a dense row of Q."""
+    rng = np.random.default_rng(4)
+    n, m = 3000, 200
+    A = sp.random(m, n, density=0.003, random_state=5, format="lil")
+    A[0, :] = rng.standard_normal(n)
+    A = A.tocsr()
+    Acol = sp.random(2500, n, density=0.002, random_state=6, format="lil")
+    Acol[:, 7] = rng.standard_normal((2500, 1))
+    A = sp.vstack([A, Acol.tocsr()]).tocsr()
+    m = A.shape[0]
+    B = sp.random(400, n, density=0.002, random_state=7, format="lil")
+    B[3, :] = rng.standard_normal(n) * 0.1
+    Q = (B.T @ B + sp.diags(rng.random(n) + 0.1)).tocsr()
+    x = rng.uniform(-1, 1, n)
+    Ax = A @ x
+    data = QPData(c=rng.standard_normal(n), A=A, con_lb=Ax - 1.0, con_ub=Ax + 1.0, var_lb=-np.ones(n) * 3,
+                  var_ub=np.ones(n) * 3, Q=Q)
+    g, o = both(data, {"eps": 1e-14, "iteration_limit": 400})
+    assert np.abs(g.x - o.x).max() <= 1e-7 * (1 + np.abs(o.x).max())
+    assert np.abs(g.y - o.y).max() <= 1e-7 * (1 + np.abs(o.y).max())
+
+
+def test_box_only_and_warm_start():
+    rng = np.random.default_rng(8)
+    n = 500
+    Q = sp.diags(rng.random(n) + 0.5).tocsr() + sp.random(n, n, density=0.002, random_state=1) * 0.01
+    Q = ((Q + Q.T) * 0.5).tocsr()
+    data = QPData(c=rng.standard_normal(n), Q=Q, var_lb=-np.ones(n), var_ub=np.ones(n))
+    g, o = both(data, {"eps": 1e-9})
+    assert g.status == o.status == "OPTIMAL"
+    assert abs(g.primal_objective - o.primal_objective) <= 1e-7 * (1 + abs(o.primal_objective))
+    d2, _, _ = planted_qp(n=600, m=300, b_rows=150, seed=12, q_form="sparse")
+    cold, _ = both(d2, {"eps": 1e-8})
+    d2.primal_start, d2.dual_start = cold.x, cold.y
+    g, o = both(d2, {"eps": 1e-8})
+    assert g.status == o.status == "OPTIMAL" and g.iterations <= cold.iterations
+    assert g.iterations == o.iterations
+
+
+def test_restart_select_halpern_matches_oracle_objective():
+    data, _, fs = planted_qp(n=600, m=300, b_rows=150, seed=13, q_form="sparse")
+    g = qp.solve(data, {"eps": 1e-7, "verbose": 0}, {"restart_select": 1})
+    assert g.status == "OPTIMAL" and abs(g.primal_objective - fs) <= 1e-5 * (1 + abs(fs))
+
+
+def test_deterministic_repeat():
+    data, _, _ = planted_qp(n=2000, m=1000, b_rows=500, seed=17, q_form="sparse")
+    a = qp.solve(data, {"eps": 1e-6, "verbose": 0})
+    b = qp.solve(data, {"eps": 1e-6, "verbose": 0})
+    assert a.iterations == b.iterations and np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)

@@ -115,6 +115,37 @@ void cp_al_gb300_last_stats(cp_al_gb300_stats_t *out);
 const char *cp_al_gb300_last_error(void);
 
 /* --- device-resident solves (inputs already in HBM) ---------------------- */
+/* ------------------------------------------------------------------ batch
+ * Many independent LPs in one persistent launch: every resident CUDA block
+ * takes the next instance from a device queue (largest first), runs the whole
+ * solve -- equilibration, power iteration, iterations, restarts, termination
+ * -- with its own controller state, and takes the next.  There is no
+ * counterpart in the reference, whose benchmarks solve instances one at a
+ * time through solve_lp_problem.  Every instance uses the same parameters and
+ * options; the iteration is the FP64 form (precision is ignored). */
+typedef struct {
+    int instances;
+    int optimal;          /* instances that reached OPTIMAL */
+    int grid_blocks;      /* resident CUDA blocks of the launch */
+    double host_prep_sec; /* validation, transposes, row-block plans, packing */
+    double upload_sec;
+    double kernel_sec;    /* the persistent launch (CUDA events) */
+    double download_sec;
+    double total_sec;
+    double solves_per_sec; /* instances / total_sec */
+    int iterations_p50, iterations_p99, iterations_max;
+    long long total_iterations;
+    long long device_bytes;
+} cp_al_gb300_batch_stats_t;
+
+/* Solves problems[0..count) and stores one result per instance in
+ * results[0..count) (free each with cp_al_result_free).  params / opts may be
+ * NULL (defaults).  Returns 0, or -1 with nothing allocated (message in
+ * cp_al_gb300_last_error). */
+int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t *params,
+                            const cp_al_gb300_options_t *opts, cp_al_result_t **results,
+                            cp_al_gb300_batch_stats_t *stats);
+
 typedef struct cp_al_gb300_session cp_al_gb300_session_t;
 
 /* Uploads and prepares the problem (transpose, scaling, power iteration are

@@ -218,6 +218,25 @@ class CpalStats(C.Structure):
     ]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [
+        ("instances", C.c_int),
+        ("optimal", C.c_int),
+        ("grid_blocks", C.c_int),
+        ("host_prep_sec", C.c_double),
+        ("upload_sec", C.c_double),
+        ("kernel_sec", C.c_double),
+        ("download_sec", C.c_double),
+        ("total_sec", C.c_double),
+        ("solves_per_sec", C.c_double),
+        ("iterations_p50", C.c_int),
+        ("iterations_p99", C.c_int),
+        ("iterations_max", C.c_int),
+        ("total_iterations", C.c_longlong),
+        ("device_bytes", C.c_longlong),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/cp_al.h and
 # include/cp_al_gb300.h declare
 LP_SYMBOLS = {
@@ -245,6 +264,11 @@ LP_SYMBOLS = {
     "cp_al_gb300_session_scaling": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp]),
     "cp_al_gb300_session_start": (C.c_int, [C.c_void_p]),
     "cp_al_gb300_session_iterate": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(CpalResult)]),
+    "cp_al_gb300_batch_solve": (
+        C.c_int,
+        [C.c_int, C.POINTER(C.POINTER(LpProblem)), C.POINTER(CpalParameters), C.POINTER(CpalOptions),
+         C.POINTER(C.POINTER(CpalResult)), C.POINTER(BatchStats)],
+    ),
     "cp_al_gb300_primal_kkt_noalloc": (
         C.c_int,
         [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -26,7 +26,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 
 # library name -> sources
 LIBRARIES = {
-    "libcp_al_gb300.so": ["cpal_solver.cu", "common.cpp", "cp_al_api.cpp", "noalloc.cu"],
+    "libcp_al_gb300.so": ["cpal_solver.cu", "common.cpp", "cp_al_api.cpp", "noalloc.cu", "batch_solver.cu"],
     "libfa_cp_gb300.so": ["facp_solver.cu", "common.cpp", "fa_cp_api.cpp"],
 }
 
@@ -51,9 +51,8 @@ def _run(cmd: list[str]) -> None:
 
 def _compile(src: Path, obj: Path) -> Path:
     obj.parent.mkdir(parents=True, exist_ok=True)
-    if obj.exists() and obj.stat().st_mtime > max(
-        src.stat().st_mtime, *(p.stat().st_mtime for p in CSRC.glob("*.h*")), *(p.stat().st_mtime for p in (ROOT / "include").glob("*.h"))
-    ):
+    deps = [*CSRC.glob("*.h"), *CSRC.glob("*.cuh"), *(ROOT / "include").glob("*.h")]
+    if obj.exists() and obj.stat().st_mtime > max(src.stat().st_mtime, *(p.stat().st_mtime for p in deps)):
         return obj
     if src.suffix == ".cu":
         cmd = [_nvcc(), *NVCC_ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]

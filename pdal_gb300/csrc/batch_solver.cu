@@ -1,0 +1,419 @@
+/*
+ * batch_solver.cu -- host side of the batched CP_AL solver
+ * (cp_al_gb300_batch_solve): validation, transposes and row-block plans per
+ * instance (host threads), one packed image of every instance's arrays
+ * uploaded with a single copy, the persistent launch of batch_kernels.cuh,
+ * and the per-instance results.
+ */
+#include "../../include/cp_al.h"
+#include "../../include/cp_al_gb300.h"
+#include "batch_kernels.cuh"
+#include "common.h"
+#include "cpal_setup.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <exception>
+#include <functional>
+#include <mutex>
+#include <random>
+#include <thread>
+#include <vector>
+
+namespace pdal {
+namespace {
+
+using namespace batch;
+
+double now_sec() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+/* Offsets (bytes from the image base) of one instance's arrays. */
+struct Layout {
+    size_t Arp, Aci, Av, Atrp, Atci, Atv, Adesc, Alinfo, Alpart, Alcount, Atdesc, Atlinfo, Atlpart, Atlcount;
+    size_t c, vlb, vub, clb, cub, x0, y0, x, xbar, xh, lam, y, yh, ybar, ax, u, ax0, phat;
+    size_t dsc, rsc, clbf, cubf, tn, tm, tm2, pv0;
+    size_t out_x, out_y, out_rc;
+};
+
+struct Prepared {
+    HostCsr At;
+    HostPlan pa, pat;
+    CpalParams cp;
+};
+
+class Packer {
+  public:
+    size_t take(size_t bytes) {
+        const size_t o = off_;
+        off_ += (std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+        return o;
+    }
+    size_t size() const { return off_; }
+
+  private:
+    size_t off_ = 0;
+};
+
+void run_threads(int count, const std::function<void(int)> &fn) {
+    const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 32));
+    std::atomic<int> next{0};
+    std::vector<std::thread> th;
+    std::exception_ptr err = nullptr;
+    std::mutex mu;
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&]() {
+            for (;;) {
+                const int i = next.fetch_add(1);
+                if (i >= count) break;
+                try {
+                    fn(i);
+                } catch (...) {
+                    std::lock_guard<std::mutex> lk(mu);
+                    if (!err) err = std::current_exception();
+                }
+            }
+        });
+    for (auto &t : th) t.join();
+    if (err) std::rethrow_exception(err);
+}
+
+int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t &P, const cp_al_gb300_options_t &O,
+                cp_al_result_t **results, cp_al_gb300_batch_stats_t *stats) {
+    const double t_begin = now_sec();
+    if (count <= 0) throw Error("batch_solve: count must be positive");
+    if (!problems || !results) throw Error("batch_solve: missing problem or result array");
+    if (P.termination_evaluation_frequency < 3) throw Error("termination_evaluation_frequency must be >= 3");
+    std::vector<Prepared> prep(count);
+    run_threads(count, [&](int i) {
+        const lp_problem_t *q = problems[i];
+        if (!q) throw Error("batch_solve: NULL problem " + std::to_string(i));
+        const int n = q->num_variables, m = q->num_constraints, nnz = q->constraint_matrix_num_nonzeros;
+        if (n <= 0 || m < 0) throw Error("batch_solve: instance " + std::to_string(i) + " has no variables");
+        if (!q->objective_vector || !q->variable_lower_bound || !q->variable_upper_bound ||
+            (m > 0 && (!q->constraint_lower_bound || !q->constraint_upper_bound)))
+            throw Error("batch_solve: instance " + std::to_string(i) + " misses a vector");
+        csr_validate(m, n, q->constraint_matrix_row_pointers, q->constraint_matrix_col_indices, nnz,
+                     "constraint matrix");
+        Prepared &p = prep[i];
+        p.At = csr_transpose(m, n, q->constraint_matrix_row_pointers, q->constraint_matrix_col_indices,
+                             q->constraint_matrix_values);
+        p.pa = plan_rows(m, q->constraint_matrix_row_pointers, kBS);
+        p.pat = plan_rows(n, p.At.rp.data(), kBS);
+        p.cp = resolve_cpal_params(P, O, q);
+    });
+
+    /* image layout */
+    Packer pk;
+    std::vector<Layout> L(count);
+    for (int i = 0; i < count; ++i) {
+        const lp_problem_t *q = problems[i];
+        const size_t n = q->num_variables, m = q->num_constraints, nnz = q->constraint_matrix_num_nonzeros;
+        const Prepared &p = prep[i];
+        Layout &l = L[i];
+        l.Arp = pk.take((m + 1) * 4);
+        l.Aci = pk.take((nnz + 8) * 4);
+        l.Av = pk.take((nnz + 8) * 8);
+        l.Atrp = pk.take((n + 1) * 4);
+        l.Atci = pk.take((nnz + 8) * 4);
+        l.Atv = pk.take((nnz + 8) * 8);
+        l.Adesc = pk.take(p.pa.desc.size() * 4);
+        l.Alinfo = pk.take(p.pa.linfo.size() * 4);
+        l.Alpart = pk.take((size_t)kLongStride * std::max(p.pa.npieces, 1) * 8);
+        l.Alcount = pk.take((size_t)std::max(p.pa.nlong, 1) * 4);
+        l.Atdesc = pk.take(p.pat.desc.size() * 4);
+        l.Atlinfo = pk.take(p.pat.linfo.size() * 4);
+        l.Atlpart = pk.take((size_t)kLongStride * std::max(p.pat.npieces, 1) * 8);
+        l.Atlcount = pk.take((size_t)std::max(p.pat.nlong, 1) * 4);
+        for (size_t *f : {&l.c, &l.vlb, &l.vub, &l.x0, &l.x, &l.xbar, &l.xh, &l.lam, &l.dsc, &l.tn}) *f = pk.take(n * 8);
+        for (size_t *f : {&l.clb, &l.cub, &l.y0, &l.y, &l.yh, &l.ybar, &l.ax, &l.u, &l.ax0, &l.phat, &l.rsc, &l.clbf,
+                          &l.cubf, &l.tm, &l.tm2, &l.pv0})
+            *f = pk.take(m * 8);
+    }
+    /* outputs last, contiguous: one download */
+    const size_t out_begin = pk.size();
+    for (int i = 0; i < count; ++i) {
+        const lp_problem_t *q = problems[i];
+        L[i].out_x = pk.take((size_t)q->num_variables * 8);
+        L[i].out_rc = pk.take((size_t)q->num_variables * 8);
+        L[i].out_y = pk.take((size_t)q->num_constraints * 8);
+    }
+    const size_t outs_off = pk.take(sizeof(BOut) * count);
+    const size_t out_end = pk.size();
+    const size_t insts_off = pk.take(sizeof(BInst) * count);
+    const size_t order_off = pk.take(sizeof(int) * count);
+    const size_t queue_off = pk.take(sizeof(unsigned));
+    const size_t total = pk.size();
+
+    char *dev = nullptr, *host = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    struct Guard {
+        char *&d, *&h;
+        cudaStream_t &s;
+        cudaEvent_t &a, &b;
+        ~Guard() {
+            if (d) cudaFree(d);
+            if (h) cudaFreeHost(h);
+            if (s) cudaStreamDestroy(s);
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } guard{dev, host, stream, e0, e1};
+    if (O.device >= 0) PDAL_CUDA(cudaSetDevice(O.device));
+    PDAL_CUDA(cudaMalloc(&dev, total));
+    PDAL_CUDA(cudaMallocHost(&host, total));
+    PDAL_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    PDAL_CUDA(cudaEventCreate(&e0));
+    PDAL_CUDA(cudaEventCreate(&e1));
+
+    /* fill the image (host threads) */
+    std::vector<BInst> insts(count);
+    run_threads(count, [&](int i) {
+        const lp_problem_t *q = problems[i];
+        const int n = q->num_variables, m = q->num_constraints, nnz = q->constraint_matrix_num_nonzeros;
+        const Prepared &p = prep[i];
+        const Layout &l = L[i];
+        auto put = [&](size_t off, const void *src, size_t bytes) {
+            if (bytes) memcpy(host + off, src, bytes);
+        };
+        auto zero = [&](size_t off, size_t bytes) { memset(host + off, 0, bytes); };
+        put(l.Arp, q->constraint_matrix_row_pointers, (size_t)(m + 1) * 4);
+        zero(l.Aci, (size_t)(nnz + 8) * 4);
+        zero(l.Av, (size_t)(nnz + 8) * 8);
+        put(l.Aci, q->constraint_matrix_col_indices, (size_t)nnz * 4);
+        put(l.Av, q->constraint_matrix_values, (size_t)nnz * 8);
+        put(l.Atrp, p.At.rp.data(), (size_t)(n + 1) * 4);
+        zero(l.Atci, (size_t)(nnz + 8) * 4);
+        zero(l.Atv, (size_t)(nnz + 8) * 8);
+        put(l.Atci, p.At.ci.data(), (size_t)nnz * 4);
+        put(l.Atv, p.At.v.data(), (size_t)nnz * 8);
+        put(l.Adesc, p.pa.desc.data(), p.pa.desc.size() * 4);
+        put(l.Alinfo, p.pa.linfo.data(), p.pa.linfo.size() * 4);
+        zero(l.Alcount, (size_t)std::max(p.pa.nlong, 1) * 4);
+        put(l.Atdesc, p.pat.desc.data(), p.pat.desc.size() * 4);
+        put(l.Atlinfo, p.pat.linfo.data(), p.pat.linfo.size() * 4);
+        zero(l.Atlcount, (size_t)std::max(p.pat.nlong, 1) * 4);
+        put(l.c, q->objective_vector, (size_t)n * 8);
+        put(l.vlb, q->variable_lower_bound, (size_t)n * 8);
+        put(l.vub, q->variable_upper_bound, (size_t)n * 8);
+        if (q->primal_start)
+            put(l.x0, q->primal_start, (size_t)n * 8);
+        else
+            zero(l.x0, (size_t)n * 8);
+        put(l.clb, q->constraint_lower_bound, (size_t)m * 8);
+        put(l.cub, q->constraint_upper_bound, (size_t)m * 8);
+        if (q->dual_start)
+            put(l.y0, q->dual_start, (size_t)m * 8);
+        else
+            zero(l.y0, (size_t)m * 8);
+        /* power-iteration start: std::normal_distribution over
+         * std::mt19937(1), what a fresh reference process draws */
+        {
+            std::mt19937 gen(1);
+            std::normal_distribution<double> dist(0.0, 1.0);
+            double *v = reinterpret_cast<double *>(host + l.pv0);
+            for (int k = 0; k < m; ++k) v[k] = dist(gen);
+        }
+        BInst &I = insts[i];
+        I.m = m;
+        I.n = n;
+        I.nnz = nnz;
+        I.nbA = p.pa.nblocks;
+        I.nlA = p.pa.nlong;
+        I.nbAt = p.pat.nblocks;
+        I.nlAt = p.pat.nlong;
+        auto D = [&](size_t off) { return dev + off; };
+        I.Arp = (const int *)D(l.Arp);
+        I.Aci = (const int *)D(l.Aci);
+        I.Av = (double *)D(l.Av);
+        I.Atrp = (const int *)D(l.Atrp);
+        I.Atci = (const int *)D(l.Atci);
+        I.Atv = (double *)D(l.Atv);
+        I.Adesc = (const int4 *)D(l.Adesc);
+        I.Alinfo = (const int4 *)D(l.Alinfo);
+        I.Alpart = (double *)D(l.Alpart);
+        I.Alcount = (unsigned *)D(l.Alcount);
+        I.Atdesc = (const int4 *)D(l.Atdesc);
+        I.Atlinfo = (const int4 *)D(l.Atlinfo);
+        I.Atlpart = (double *)D(l.Atlpart);
+        I.Atlcount = (unsigned *)D(l.Atlcount);
+        I.c = (double *)D(l.c);
+        I.vlb = (double *)D(l.vlb);
+        I.vub = (double *)D(l.vub);
+        I.clb = (double *)D(l.clb);
+        I.cub = (double *)D(l.cub);
+        I.x0 = (double *)D(l.x0);
+        I.y0 = (double *)D(l.y0);
+        I.x = (double *)D(l.x);
+        I.xbar = (double *)D(l.xbar);
+        I.xh = (double *)D(l.xh);
+        I.lam = (double *)D(l.lam);
+        I.y = (double *)D(l.y);
+        I.yh = (double *)D(l.yh);
+        I.ybar = (double *)D(l.ybar);
+        I.ax = (double *)D(l.ax);
+        I.u = (double *)D(l.u);
+        I.ax0 = (double *)D(l.ax0);
+        I.phat = (double *)D(l.phat);
+        I.dsc = (double *)D(l.dsc);
+        I.rsc = (double *)D(l.rsc);
+        I.clbf = (double *)D(l.clbf);
+        I.cubf = (double *)D(l.cubf);
+        I.tn = (double *)D(l.tn);
+        I.tm = (double *)D(l.tm);
+        I.tm2 = (double *)D(l.tm2);
+        I.pv0 = (const double *)D(l.pv0);
+        I.out_x = (double *)D(l.out_x);
+        I.out_y = (double *)D(l.out_y);
+        I.out_rc = (double *)D(l.out_rc);
+        I.obj_norm = p.cp.obj_norm;
+        I.bnd_norm = p.cp.bnd_norm;
+        I.obj_const = p.cp.obj_const;
+    });
+    memcpy(host + insts_off, insts.data(), sizeof(BInst) * count);
+    std::vector<int> order(count);
+    for (int i = 0; i < count; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const long long wa = (long long)problems[a]->constraint_matrix_num_nonzeros + problems[a]->num_variables;
+        const long long wb = (long long)problems[b]->constraint_matrix_num_nonzeros + problems[b]->num_variables;
+        return wa > wb;
+    });
+    memcpy(host + order_off, order.data(), sizeof(int) * count);
+    memset(host + queue_off, 0, sizeof(unsigned));
+    const double t_prep = now_sec();
+
+    PDAL_CUDA(cudaMemcpyAsync(dev, host, total, cudaMemcpyHostToDevice, stream));
+    PDAL_CUDA(cudaStreamSynchronize(stream));
+    const double t_up = now_sec();
+
+    BOpts bo{};
+    bo.ruiz = P.l_inf_ruiz_iterations;
+    bo.pc = P.has_pock_chambolle_alpha ? 1 : 0;
+    bo.pc_alpha = P.pock_chambolle_alpha;
+    bo.boundobj = P.bound_objective_rescaling ? 1 : 0;
+    bo.sv_max_iter = P.sv_max_iter;
+    bo.sv_tol = P.sv_tol;
+    bo.al_lambda = O.al_lambda;
+    bo.sigma_mode = O.sigma_mode;
+    bo.sigma_set = O.sigma_set;
+    bo.sigma_adaptive = O.sigma_adaptive;
+    bo.lambda_param_set = O.lambda_param_set;
+    bo.sigma = O.sigma;
+    bo.sigma_init_factor = O.sigma_init_factor;
+    bo.sigma_min_factor = O.sigma_min_factor;
+    bo.sigma_max_factor = O.sigma_max_factor;
+    bo.lambda_param = O.lambda_param;
+    CpalParams cp = prep[0].cp; /* instance-specific norms are overridden per instance in the kernel */
+
+    int dev_id = 0, sms = 0, per_sm = 0;
+    PDAL_CUDA(cudaGetDevice(&dev_id));
+    PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
+    PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_lp, kThreads, 0));
+    if (per_sm < 1) throw Error("the batch kernel does not fit on one SM");
+    const int grid = std::max(1, std::min(count, per_sm * sms));
+    PDAL_CUDA(cudaEventRecord(e0, stream));
+    k_batch_lp<<<grid, kThreads, 0, stream>>>((const BInst *)(dev + insts_off), count, (const int *)(dev + order_off),
+                                               (unsigned *)(dev + queue_off), cp, bo, (BOut *)(dev + outs_off));
+    PDAL_CUDA(cudaGetLastError());
+    PDAL_CUDA(cudaEventRecord(e1, stream));
+    PDAL_CUDA(cudaMemcpyAsync(host + out_begin, dev + out_begin, out_end - out_begin, cudaMemcpyDeviceToHost, stream));
+    PDAL_CUDA(cudaStreamSynchronize(stream));
+    float kms = 0.f;
+    PDAL_CUDA(cudaEventElapsedTime(&kms, e0, e1));
+    const double t_kernel_end = now_sec();
+
+    const BOut *outs = reinterpret_cast<const BOut *>(host + outs_off);
+    std::vector<int> iters(count);
+    int optimal = 0;
+    long long total_iters = 0;
+    for (int i = 0; i < count; ++i) {
+        const lp_problem_t *q = problems[i];
+        const int n = q->num_variables, m = q->num_constraints;
+        const BOut &o = outs[i];
+        cp_al_result_t *r = (cp_al_result_t *)calloc(1, sizeof(cp_al_result_t));
+        r->primal_solution = (double *)malloc(sizeof(double) * std::max(n, 1));
+        r->dual_solution = (double *)malloc(sizeof(double) * std::max(m, 1));
+        r->reduced_cost = (double *)malloc(sizeof(double) * std::max(n, 1));
+        memcpy(r->primal_solution, host + L[i].out_x, sizeof(double) * n);
+        memcpy(r->reduced_cost, host + L[i].out_rc, sizeof(double) * n);
+        if (m) memcpy(r->dual_solution, host + L[i].out_y, sizeof(double) * m);
+        r->num_variables = n;
+        r->num_constraints = m;
+        r->num_nonzeros = q->constraint_matrix_num_nonzeros;
+        r->num_reduced_variables = n;
+        r->num_reduced_constraints = m;
+        r->num_reduced_nonzeros = q->constraint_matrix_num_nonzeros;
+        r->total_count = o.iterations;
+        r->rescaling_time_sec = o.setup_sec;
+        r->cumulative_time_sec = o.elapsed;
+        r->absolute_primal_residual = o.abs_p;
+        r->relative_primal_residual = o.rel_p;
+        r->absolute_dual_residual = o.abs_d;
+        r->relative_dual_residual = o.rel_d;
+        r->primal_objective_value = o.pobj;
+        r->dual_objective_value = o.dobj;
+        r->objective_gap = std::fabs(o.pobj - o.dobj);
+        r->relative_objective_gap = o.rel_gap;
+        r->termination_reason = (termination_reason_t)o.status;
+        results[i] = r;
+        iters[i] = o.iterations;
+        total_iters += o.iterations;
+        if (o.status == TERMINATION_REASON_OPTIMAL) ++optimal;
+    }
+    const double t_end = now_sec();
+    if (stats) {
+        std::vector<int> sorted = iters;
+        std::sort(sorted.begin(), sorted.end());
+        auto pct = [&](double f) {
+            const size_t k = (size_t)std::min<double>(sorted.size() - 1, std::ceil(f * sorted.size()) - 1);
+            return sorted[k];
+        };
+        memset(stats, 0, sizeof(*stats));
+        stats->instances = count;
+        stats->optimal = optimal;
+        stats->grid_blocks = grid;
+        stats->host_prep_sec = t_prep - t_begin;
+        stats->upload_sec = t_up - t_prep;
+        stats->kernel_sec = kms * 1e-3;
+        stats->download_sec = t_end - t_kernel_end;
+        stats->total_sec = t_end - t_begin;
+        stats->solves_per_sec = count / stats->total_sec;
+        stats->iterations_p50 = pct(0.5);
+        stats->iterations_p99 = pct(0.99);
+        stats->iterations_max = sorted.back();
+        stats->total_iterations = total_iters;
+        stats->device_bytes = (long long)total;
+    }
+    return 0;
+}
+
+} // namespace
+} // namespace pdal
+
+extern "C" int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t *params,
+                                       const cp_al_gb300_options_t *opts, cp_al_result_t **results,
+                                       cp_al_gb300_batch_stats_t *stats) {
+    pdal::clear_last_error();
+    cp_al_parameters_t p;
+    if (params)
+        p = *params;
+    else
+        set_default_parameters(&p);
+    cp_al_gb300_options_t o;
+    if (opts)
+        o = *opts;
+    else
+        cp_al_gb300_default_options(&o);
+    try {
+        return pdal::batch_solve(count, problems, p, o, results, stats);
+    } catch (const std::exception &e) {
+        pdal::set_last_error(e.what());
+        return -1;
+    }
+}

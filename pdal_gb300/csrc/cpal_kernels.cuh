@@ -222,13 +222,13 @@ __global__ void __launch_bounds__(kThreads) k_dual(RowPlanDev plan, const int *_
 }
 
 /* Halpern weights for the block starting at st->inner (one block). */
-__global__ void k_fill_weights(const CpalState *__restrict__ st, HalpernW *wt, HalpernWf *wtf, int F) {
+static __global__ void k_fill_weights(const CpalState *__restrict__ st, HalpernW *wt, HalpernWf *wtf, int F) {
     const int inner = st->inner;
     for (int i = threadIdx.x + 1; i <= F; i += blockDim.x) cpal_halpern_entry(inner, i, wt[i], wtf[i]);
 }
 
 /* FP64 vector -> (hi, lo) float pairs */
-__global__ void k_split(const double *__restrict__ src, float2 *dst, int len) {
+static __global__ void k_split(const double *__restrict__ src, float2 *dst, int len) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) dst[i] = split_anchor(src[i]);
 }
 
@@ -420,7 +420,7 @@ __device__ __forceinline__ void reduce_slots(const double *part, int nslots, Red
     block_reduce<kThreads, 6, 1>(r, sbuf);
 }
 
-__global__ void __launch_bounds__(kThreads) k_control(const double *__restrict__ prow, int nrow_slots,
+static __global__ void __launch_bounds__(kThreads) k_control(const double *__restrict__ prow, int nrow_slots,
                                                       const double *__restrict__ pcol, int ncol_slots,
                                                       CpalState *st, CpalParams p, HalpernW *wt, HalpernWf *wtf) {
     if (st->status) return;
@@ -492,7 +492,7 @@ __global__ void k_restart(const CpalState *__restrict__ st, int n, int m, const 
     }
 }
 
-__global__ void k_start_clock(CpalState *st) { st->t_start_ns = globaltimer_ns(); }
+static __global__ void k_start_clock(CpalState *st) { st->t_start_ns = globaltimer_ns(); }
 
 /* ------------------------------------------------------------------ */
 /* result (LP/CP_AL/src/solver.cu:1768-1793, 2481-2500)                 */
@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(kThreads) k_result_cols(RowPlanDev plan, const
     rowblock_run<S, 1, double>(plan, rp, ci, val, g, epi, red, sm);
 }
 
-__global__ void k_result_rows(int m, const double *__restrict__ yh, const double *__restrict__ rscale,
+static __global__ void k_result_rows(int m, const double *__restrict__ yh, const double *__restrict__ rscale,
                               const CpalState *__restrict__ st, double *y_out) {
     const double ovr = st->ovr;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
@@ -539,7 +539,7 @@ __global__ void k_convert(const A *__restrict__ src, B *dst, int len) {
 
 /* warp per row: s = clamp_sqrt(max |a| or sum |a|^deg), cum *= s
  * (preconditioner.cu:532-550, 634-667). mode 0 = abs max, 1 = power sum. */
-__global__ void k_row_scale(int nr, const int *__restrict__ rp, const double *__restrict__ val, int mode, double deg,
+static __global__ void k_row_scale(int nr, const int *__restrict__ rp, const double *__restrict__ val, int mode, double deg,
                             double *scale, double *cum) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -577,7 +577,7 @@ __global__ void k_row_scale(int nr, const int *__restrict__ rp, const double *__
 
 /* A values *= (1/d[j]) * (1/r[i]); rows of this matrix are scaled by
  * row_is_var ? d : r (preconditioner.cu:514-530). */
-__global__ void k_scale_matrix(int nr, const int *__restrict__ rp, const int *__restrict__ ci, double *val,
+static __global__ void k_scale_matrix(int nr, const int *__restrict__ rp, const int *__restrict__ ci, double *val,
                                const double *__restrict__ rowscale, const double *__restrict__ colscale,
                                int row_is_var) {
     const int lane = threadIdx.x & 31;
@@ -592,7 +592,7 @@ __global__ void k_scale_matrix(int nr, const int *__restrict__ rp, const int *__
 }
 
 /* preconditioner.cu:476-512 */
-__global__ void k_scale_vectors(int n, int m, const double *__restrict__ d, const double *__restrict__ r, double *c,
+static __global__ void k_scale_vectors(int n, int m, const double *__restrict__ d, const double *__restrict__ r, double *c,
                                 double *vlb, double *vub, double *x0, double *clb, double *cub, double *y0) {
     const int total = n > m ? n : m;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
@@ -614,7 +614,7 @@ __global__ void k_scale_vectors(int n, int m, const double *__restrict__ d, cons
 
 /* bound/objective norms (preconditioner.cu:329-377, 669-691): partial sums of
  * the bound contributions and of c^2 per block. */
-__global__ void __launch_bounds__(kThreads) k_boundobj_partials(int n, int m, const double *__restrict__ clb,
+static __global__ void __launch_bounds__(kThreads) k_boundobj_partials(int n, int m, const double *__restrict__ clb,
                                                                 const double *__restrict__ cub,
                                                                 const double *__restrict__ c, double *part) {
     __shared__ double sbuf[2 * (kThreads / 32)];
@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(kThreads) k_boundobj_partials(int n, int m, co
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_boundobj_finish(const double *__restrict__ part, int nparts,
+static __global__ void __launch_bounds__(kThreads) k_boundobj_finish(const double *__restrict__ part, int nparts,
                                                               CpalState *st, int enabled) {
     __shared__ double sbuf[2 * (kThreads / 32)];
     Red<2, 0> r;
@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(kThreads) k_boundobj_finish(const double *__re
     }
 }
 
-__global__ void k_scale_boundobj(int n, int m, const CpalState *__restrict__ st, double *c, double *vlb, double *vub,
+static __global__ void k_scale_boundobj(int n, int m, const CpalState *__restrict__ st, double *c, double *vlb, double *vub,
                                  double *x0, double *clb, double *cub, double *y0) {
     const double cs = st->cbr, os = st->ovr;
     const int total = n > m ? n : m;
@@ -680,7 +680,7 @@ __global__ void k_scale_boundobj(int n, int m, const CpalState *__restrict__ st,
 }
 
 /* finite-bound copies (LP/CP_AL/src/solver.cu:2323-2338) */
-__global__ void k_finite_bounds(int m, const double *__restrict__ lb, const double *__restrict__ ub, double *lbf,
+static __global__ void k_finite_bounds(int m, const double *__restrict__ lb, const double *__restrict__ ub, double *lbf,
                                 double *ubf) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
         lbf[i] = isfinite(lb[i]) ? lb[i] : 0.0;
@@ -758,7 +758,7 @@ __global__ void __launch_bounds__(kThreads) k_power_a(RowPlanDev plan, const int
 }
 
 /* s2 = sum(part) */
-__global__ void __launch_bounds__(kThreads) k_power_dot(const double *__restrict__ part, int nparts, PowerState *ps) {
+static __global__ void __launch_bounds__(kThreads) k_power_dot(const double *__restrict__ part, int nparts, PowerState *ps) {
     if (ps->done) return;
     __shared__ double sbuf[kThreads / 32];
     Red<1, 0> r;
@@ -769,7 +769,7 @@ __global__ void __launch_bounds__(kThreads) k_power_dot(const double *__restrict
 }
 
 /* residual vn - s2 * (inv v) and |vn|^2; then v <- vn */
-__global__ void __launch_bounds__(kThreads) k_power_resid(int m, double *v, const double *__restrict__ vn,
+static __global__ void __launch_bounds__(kThreads) k_power_resid(int m, double *v, const double *__restrict__ vn,
                                                           double *part, const PowerState *__restrict__ ps) {
     if (ps->done) return;
     __shared__ double sbuf[2 * (kThreads / 32)];
@@ -792,7 +792,7 @@ __global__ void __launch_bounds__(kThreads) k_power_resid(int m, double *v, cons
 }
 
 /* residual test and the normalisation of the next vector */
-__global__ void __launch_bounds__(kThreads) k_power_check(const double *__restrict__ part, int nparts,
+static __global__ void __launch_bounds__(kThreads) k_power_check(const double *__restrict__ part, int nparts,
                                                           PowerState *ps) {
     if (ps->done) return;
     __shared__ double sbuf[2 * (kThreads / 32)];
@@ -812,7 +812,7 @@ __global__ void __launch_bounds__(kThreads) k_power_check(const double *__restri
 }
 
 /* 1/|v| of the start vector */
-__global__ void __launch_bounds__(kThreads) k_power_start(int m, const double *__restrict__ v, PowerState *ps) {
+static __global__ void __launch_bounds__(kThreads) k_power_start(int m, const double *__restrict__ v, PowerState *ps) {
     __shared__ double sbuf[kThreads / 32];
     Red<1, 0> r;
     r.zero();

@@ -17,6 +17,7 @@
 #include "../../include/cp_al_gb300.h"
 #include "common.h"
 #include "cpal_kernels.cuh"
+#include "cpal_setup.h"
 
 #include <algorithm>
 #include <chrono>
@@ -223,6 +224,67 @@ void CpalSolver::release() {
     stream_ = nullptr;
 }
 
+/* Controller parameters of one solve: options resolved against the
+ * parameters (NaN options fall back to them), and the norms of the unscaled
+ * problem (LP/CP_AL/src/solver.cu:1999-2067). */
+CpalParams resolve_cpal_params(const cp_al_parameters_t &P, const cp_al_gb300_options_t &O, const lp_problem_t *prob) {
+    CpalParams cp{};
+    const auto &R = P.restart_params;
+    cp.F = P.termination_evaluation_frequency;
+    cp.iteration_limit = P.termination_criteria.iteration_limit;
+    cp.time_limit = P.termination_criteria.time_sec_limit;
+    cp.eps_opt = P.termination_criteria.eps_optimal_relative;
+    cp.eps_feas = P.termination_criteria.eps_feasible_relative;
+    cp.norm_linf = P.optimality_norm == NORM_TYPE_L_INF;
+    cp.refl = P.reflection_coefficient;
+    cp.suff = std::isnan(O.restart_sufficient) ? R.sufficient_reduction_for_restart : O.restart_sufficient;
+    cp.nec = std::isnan(O.restart_necessary) ? R.necessary_reduction_for_restart : O.restart_necessary;
+    cp.art = std::isnan(O.restart_artificial) ? R.artificial_restart_threshold : O.restart_artificial;
+    cp.kp = R.k_p;
+    cp.ki = R.k_i;
+    cp.kd = R.k_d;
+    cp.ismooth = R.i_smooth;
+    cp.sigma_mode = O.sigma_mode != 0;
+    cp.sigma_adaptive = O.sigma_adaptive != 0;
+    cp.s_kp = std::isnan(O.sigma_kp) ? R.k_p : O.sigma_kp;
+    cp.s_ki = std::isnan(O.sigma_ki) ? R.k_i : O.sigma_ki;
+    cp.s_kd = std::isnan(O.sigma_kd) ? R.k_d : O.sigma_kd;
+    cp.s_ismooth = std::isnan(O.sigma_i_smooth) ? R.i_smooth : O.sigma_i_smooth;
+    cp.s_gain = O.sigma_balance_gain;
+    cp.s_umin = O.sigma_update_min;
+    cp.s_umax = O.sigma_update_max;
+    cp.step_margin = O.step_margin;
+    cp.lambda_factor = O.lambda_factor;
+    cp.lambda_param_set = O.lambda_param_set;
+    cp.lambda_param_opt = O.lambda_param;
+    cp.obj_const = prob->objective_constant;
+    const int n = prob->num_variables, m = prob->num_constraints;
+    const bool linf = cp.norm_linf;
+    double s = 0, mx = 0;
+    for (int j = 0; j < n; ++j) {
+        const double v = prob->objective_vector[j];
+        if (linf)
+            mx = std::fmax(mx, std::fabs(v));
+        else
+            s += v * v;
+    }
+    cp.obj_norm = linf ? mx : std::sqrt(s);
+    s = 0;
+    mx = 0;
+    for (int i = 0; i < m; ++i) {
+        const double lo = prob->constraint_lower_bound[i], up = prob->constraint_upper_bound[i];
+        if (linf) {
+            if (std::isfinite(lo) && lo != up) mx = std::fmax(mx, std::fabs(lo));
+            if (std::isfinite(up)) mx = std::fmax(mx, std::fabs(up));
+        } else {
+            if (std::isfinite(lo) && lo != up) s += lo * lo;
+            if (std::isfinite(up)) s += up * up;
+        }
+    }
+    cp.bnd_norm = linf ? mx : std::sqrt(s);
+    return cp;
+}
+
 void CpalSolver::prepare() {
     n_ = prob_->num_variables;
     m_ = prob_->num_constraints;
@@ -245,62 +307,7 @@ void CpalSolver::prepare() {
         throw Error("spmv_nnz_per_block must be 256, 512, 1024 or 2048");
     S_ev_ = std::min(S_it_, 1024);
 
-    /* controller parameters, environment overrides resolved */
-    const auto &R = P_.restart_params;
-    cp_.F = P_.termination_evaluation_frequency;
-    cp_.iteration_limit = P_.termination_criteria.iteration_limit;
-    cp_.time_limit = P_.termination_criteria.time_sec_limit;
-    cp_.eps_opt = P_.termination_criteria.eps_optimal_relative;
-    cp_.eps_feas = P_.termination_criteria.eps_feasible_relative;
-    cp_.norm_linf = P_.optimality_norm == NORM_TYPE_L_INF;
-    cp_.refl = P_.reflection_coefficient;
-    cp_.suff = std::isnan(O_.restart_sufficient) ? R.sufficient_reduction_for_restart : O_.restart_sufficient;
-    cp_.nec = std::isnan(O_.restart_necessary) ? R.necessary_reduction_for_restart : O_.restart_necessary;
-    cp_.art = std::isnan(O_.restart_artificial) ? R.artificial_restart_threshold : O_.restart_artificial;
-    cp_.kp = R.k_p;
-    cp_.ki = R.k_i;
-    cp_.kd = R.k_d;
-    cp_.ismooth = R.i_smooth;
-    cp_.sigma_mode = O_.sigma_mode != 0;
-    cp_.sigma_adaptive = O_.sigma_adaptive != 0;
-    cp_.s_kp = std::isnan(O_.sigma_kp) ? R.k_p : O_.sigma_kp;
-    cp_.s_ki = std::isnan(O_.sigma_ki) ? R.k_i : O_.sigma_ki;
-    cp_.s_kd = std::isnan(O_.sigma_kd) ? R.k_d : O_.sigma_kd;
-    cp_.s_ismooth = std::isnan(O_.sigma_i_smooth) ? R.i_smooth : O_.sigma_i_smooth;
-    cp_.s_gain = O_.sigma_balance_gain;
-    cp_.s_umin = O_.sigma_update_min;
-    cp_.s_umax = O_.sigma_update_max;
-    cp_.step_margin = O_.step_margin;
-    cp_.lambda_factor = O_.lambda_factor;
-    cp_.lambda_param_set = O_.lambda_param_set;
-    cp_.lambda_param_opt = O_.lambda_param;
-    cp_.obj_const = prob_->objective_constant;
-    /* norms of the unscaled problem (LP/CP_AL/src/solver.cu:1999-2067) */
-    {
-        const bool linf = cp_.norm_linf;
-        double s = 0, mx = 0;
-        for (int j = 0; j < n_; ++j) {
-            const double v = prob_->objective_vector[j];
-            if (linf)
-                mx = std::fmax(mx, std::fabs(v));
-            else
-                s += v * v;
-        }
-        cp_.obj_norm = linf ? mx : std::sqrt(s);
-        s = 0;
-        mx = 0;
-        for (int i = 0; i < m_; ++i) {
-            const double lo = prob_->constraint_lower_bound[i], up = prob_->constraint_upper_bound[i];
-            if (linf) {
-                if (std::isfinite(lo) && lo != up) mx = std::fmax(mx, std::fabs(lo));
-                if (std::isfinite(up)) mx = std::fmax(mx, std::fabs(up));
-            } else {
-                if (std::isfinite(lo) && lo != up) s += lo * lo;
-                if (std::isfinite(up)) s += up * up;
-            }
-        }
-        cp_.bnd_norm = linf ? mx : std::sqrt(s);
-    }
+    cp_ = resolve_cpal_params(P_, O_, prob_);
     fp32_phase_ = O_.precision == CP_AL_GB300_FP32_REFINE;
 }
 
@@ -1011,6 +1018,11 @@ void set_error(const std::string &msg) {
     fprintf(stderr, "[cp_al_gb300] %s\n", msg.c_str());
 }
 } // namespace
+
+namespace pdal {
+void set_last_error(const std::string &msg) { set_error(msg); }
+void clear_last_error() { g_last_error.clear(); }
+} // namespace pdal
 
 struct cp_al_gb300_session {
     std::unique_ptr<pdal::CpalSolver> solver;

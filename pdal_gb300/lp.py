@@ -280,3 +280,29 @@ class LPSession:
 
     def __del__(self):
         self.close()
+
+
+def solve_batch(items: list[LPData], params: dict | N.CpalParameters | None = None,
+                options: dict | N.CpalOptions | None = None) -> tuple[list[LPResult], dict]:
+    """All instances in one persistent launch (cp_al_gb300_batch_solve);
+    returns the per-instance results and the batch statistics."""
+    lib = N.load_lp()
+    p = params if isinstance(params, N.CpalParameters) else apply_params(default_parameters(lib), params)
+    o = options if isinstance(options, N.CpalOptions) else apply_options(default_options(lib), options)
+    probs = [_CProblem(lib, d) for d in items]
+    try:
+        arr = (C.POINTER(N.LpProblem) * len(probs))(*[q.ptr for q in probs])
+        res = (C.POINTER(N.CpalResult) * len(probs))()
+        st = N.BatchStats()
+        if lib.cp_al_gb300_batch_solve(len(probs), arr, C.byref(p), C.byref(o), res, C.byref(st)) != 0:
+            raise RuntimeError("batch solve failed: " + N.last_error(lib))
+        out = []
+        for q, r in zip(probs, res):
+            try:
+                out.append(_result_from_c(lib, r.contents, q.m, q.n))
+            finally:
+                lib.cp_al_result_free(r)
+        return out, {f: getattr(st, f) for f, _ in N.BatchStats._fields_}
+    finally:
+        for q in probs:
+            q.close()

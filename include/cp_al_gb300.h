@@ -138,13 +138,24 @@ typedef struct {
     long long device_bytes;
 } cp_al_gb300_batch_stats_t;
 
+/* Controller state of one instance at the end of its solve. */
+typedef struct {
+    double sigma;        /* sigma mode: the final sigma (0 otherwise) */
+    double sigma_best;   /* sigma mode: the sigma of the best residual balance */
+    double primal_weight;
+    double step_size;
+    double lambda_est;   /* sigma_max(A)^2 estimate of the scaled matrix */
+    int restarts;
+    int power_iterations;
+} cp_al_gb300_instance_info_t;
+
 /* Solves problems[0..count) and stores one result per instance in
- * results[0..count) (free each with cp_al_result_free).  params / opts may be
- * NULL (defaults).  Returns 0, or -1 with nothing allocated (message in
- * cp_al_gb300_last_error). */
+ * results[0..count) (free each with cp_al_result_free); info (may be NULL)
+ * receives count entries.  params / opts may be NULL (defaults).  Returns 0,
+ * or -1 with nothing allocated (message in cp_al_gb300_last_error). */
 int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t *params,
                             const cp_al_gb300_options_t *opts, cp_al_result_t **results,
-                            cp_al_gb300_batch_stats_t *stats);
+                            cp_al_gb300_instance_info_t *info, cp_al_gb300_batch_stats_t *stats);
 
 typedef struct cp_al_gb300_session cp_al_gb300_session_t;
 

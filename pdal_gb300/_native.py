@@ -237,6 +237,18 @@ class BatchStats(C.Structure):
     ]
 
 
+class InstanceInfo(C.Structure):
+    _fields_ = [
+        ("sigma", C.c_double),
+        ("sigma_best", C.c_double),
+        ("primal_weight", C.c_double),
+        ("step_size", C.c_double),
+        ("lambda_est", C.c_double),
+        ("restarts", C.c_int),
+        ("power_iterations", C.c_int),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/cp_al.h and
 # include/cp_al_gb300.h declare
 LP_SYMBOLS = {
@@ -267,7 +279,7 @@ LP_SYMBOLS = {
     "cp_al_gb300_batch_solve": (
         C.c_int,
         [C.c_int, C.POINTER(C.POINTER(LpProblem)), C.POINTER(CpalParameters), C.POINTER(CpalOptions),
-         C.POINTER(C.POINTER(CpalResult)), C.POINTER(BatchStats)],
+         C.POINTER(C.POINTER(CpalResult)), C.POINTER(InstanceInfo), C.POINTER(BatchStats)],
     ),
     "cp_al_gb300_primal_kkt_noalloc": (
         C.c_int,

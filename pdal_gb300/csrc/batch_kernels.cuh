@@ -51,6 +51,7 @@ struct BOut {
     double pobj, dobj, rel_p, rel_d, rel_gap, abs_p, abs_d;
     double lambda_est, pw, step, elapsed;
     double setup_sec;
+    double sigma, sigma_best;
 };
 
 /* Batch-wide options resolved on the host. */
@@ -603,6 +604,8 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
         r.step = s.step;
         r.elapsed = (double)(globaltimer_ns() - s.t_start_ns) * 1e-9;
         r.setup_sec = sh[3];
+        r.sigma = s.sigma_on ? s.sigma : 0.0;
+        r.sigma_best = s.sigma_on ? s.sigma_best : 0.0;
         *out = r;
     }
     __syncthreads();

@@ -84,7 +84,7 @@ void run_threads(int count, const std::function<void(int)> &fn) {
 }
 
 int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t &P, const cp_al_gb300_options_t &O,
-                cp_al_result_t **results, cp_al_gb300_batch_stats_t *stats) {
+                cp_al_result_t **results, cp_al_gb300_instance_info_t *info, cp_al_gb300_batch_stats_t *stats) {
     const double t_begin = now_sec();
     if (count <= 0) throw Error("batch_solve: count must be positive");
     if (!problems || !results) throw Error("batch_solve: missing problem or result array");
@@ -362,6 +362,16 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
         r->relative_objective_gap = o.rel_gap;
         r->termination_reason = (termination_reason_t)o.status;
         results[i] = r;
+        if (info) {
+            cp_al_gb300_instance_info_t &f = info[i];
+            f.sigma = o.sigma;
+            f.sigma_best = o.sigma_best;
+            f.primal_weight = o.pw;
+            f.step_size = o.step;
+            f.lambda_est = o.lambda_est;
+            f.restarts = o.restarts;
+            f.power_iterations = o.power_iters;
+        }
         iters[i] = o.iterations;
         total_iters += o.iterations;
         if (o.status == TERMINATION_REASON_OPTIMAL) ++optimal;
@@ -398,7 +408,7 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
 
 extern "C" int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t *params,
                                        const cp_al_gb300_options_t *opts, cp_al_result_t **results,
-                                       cp_al_gb300_batch_stats_t *stats) {
+                                       cp_al_gb300_instance_info_t *info, cp_al_gb300_batch_stats_t *stats) {
     pdal::clear_last_error();
     cp_al_parameters_t p;
     if (params)
@@ -411,7 +421,7 @@ extern "C" int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems,
     else
         cp_al_gb300_default_options(&o);
     try {
-        return pdal::batch_solve(count, problems, p, o, results, stats);
+        return pdal::batch_solve(count, problems, p, o, results, info, stats);
     } catch (const std::exception &e) {
         pdal::set_last_error(e.what());
         return -1;

@@ -293,13 +293,16 @@ def solve_batch(items: list[LPData], params: dict | N.CpalParameters | None = No
     try:
         arr = (C.POINTER(N.LpProblem) * len(probs))(*[q.ptr for q in probs])
         res = (C.POINTER(N.CpalResult) * len(probs))()
+        info = (N.InstanceInfo * len(probs))()
         st = N.BatchStats()
-        if lib.cp_al_gb300_batch_solve(len(probs), arr, C.byref(p), C.byref(o), res, C.byref(st)) != 0:
+        if lib.cp_al_gb300_batch_solve(len(probs), arr, C.byref(p), C.byref(o), res, info, C.byref(st)) != 0:
             raise RuntimeError("batch solve failed: " + N.last_error(lib))
         out = []
-        for q, r in zip(probs, res):
+        for q, r, f in zip(probs, res, info):
             try:
-                out.append(_result_from_c(lib, r.contents, q.m, q.n))
+                lr = _result_from_c(lib, r.contents, q.m, q.n)
+                lr.stats = {k: getattr(f, k) for k, _ in N.InstanceInfo._fields_}
+                out.append(lr)
             finally:
                 lib.cp_al_result_free(r)
         return out, {f: getattr(st, f) for f, _ in N.BatchStats._fields_}

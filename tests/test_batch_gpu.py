@@ -41,7 +41,7 @@ def long_row_lp(seed=2):
 @pytest.mark.parametrize("options", [{}, SIGMA], ids=["default", "sigma_protocol"])
 def test_batch_matches_single_solver(options):
     items = batch_lps(count=20, seed=77, m_range=(50, 700)) + [long_row_lp()]
-    params = {"eps": 1e-8, "l_inf_ruiz_iterations": 4}
+    params = {"eps": 1e-8, "l_inf_ruiz_iterations": 4, "iteration_limit": 200000}
     res, st = lp.solve_batch(items, params, options)
     assert st["instances"] == len(items) and st["grid_blocks"] > 0
     for d, b in zip(items, res):
@@ -56,7 +56,7 @@ def test_batch_matches_single_solver(options):
 
 def test_batch_matches_oracle():
     items = batch_lps(count=6, seed=5, m_range=(60, 300))
-    params = {"eps": 1e-8, "l_inf_ruiz_iterations": 4}
+    params = {"eps": 1e-8, "l_inf_ruiz_iterations": 4, "iteration_limit": 200000}
     res, _ = lp.solve_batch(items, params)
     for d, b in zip(items, res):
         o = O.solve_lp(d, params)
@@ -69,8 +69,8 @@ def test_batch_handles_iteration_limit_and_warm_start():
     items = batch_lps(count=4, seed=8, m_range=(80, 200))
     res, st = lp.solve_batch(items, {"eps": 1e-12, "iteration_limit": 400})
     assert all(r.status == "ITERATION_LIMIT" and r.iterations == 400 for r in res)
-    cold, _ = lp.solve_batch(items, {"eps": 1e-8})
+    cold, _ = lp.solve_batch(items, {"eps": 1e-8, "iteration_limit": 200000})
     for d, r in zip(items, cold):
         d.primal_start, d.dual_start = r.x, r.y
-    warm, _ = lp.solve_batch(items, {"eps": 1e-8})
+    warm, _ = lp.solve_batch(items, {"eps": 1e-8, "iteration_limit": 200000})
     assert all(w.status == "OPTIMAL" and w.iterations <= c.iterations for w, c in zip(warm, cold))

@@ -151,10 +151,12 @@ typedef struct {
 
 /* Solves problems[0..count) and stores one result per instance in
  * results[0..count) (free each with cp_al_result_free); info (may be NULL)
- * receives count entries.  params / opts may be NULL (defaults).  Returns 0,
- * or -1 with nothing allocated (message in cp_al_gb300_last_error). */
+ * receives count entries.  sigma0 (may be NULL) gives a per-instance initial
+ * sigma for sigma mode (entries <= 0 keep the options' rule).  params / opts
+ * may be NULL (defaults).  Returns 0, or -1 with nothing allocated (message
+ * in cp_al_gb300_last_error). */
 int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t *params,
-                            const cp_al_gb300_options_t *opts, cp_al_result_t **results,
+                            const cp_al_gb300_options_t *opts, const double *sigma0, cp_al_result_t **results,
                             cp_al_gb300_instance_info_t *info, cp_al_gb300_batch_stats_t *stats);
 
 typedef struct cp_al_gb300_session cp_al_gb300_session_t;

@@ -278,7 +278,7 @@ LP_SYMBOLS = {
     "cp_al_gb300_session_iterate": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(CpalResult)]),
     "cp_al_gb300_batch_solve": (
         C.c_int,
-        [C.c_int, C.POINTER(C.POINTER(LpProblem)), C.POINTER(CpalParameters), C.POINTER(CpalOptions),
+        [C.c_int, C.POINTER(C.POINTER(LpProblem)), C.POINTER(CpalParameters), C.POINTER(CpalOptions), _dp,
          C.POINTER(C.POINTER(CpalResult)), C.POINTER(InstanceInfo), C.POINTER(BatchStats)],
     ),
     "cp_al_gb300_primal_kkt_noalloc": (
@@ -469,6 +469,27 @@ QP_SYMBOLS = {
     "fa_cp_gb300_last_error": (C.c_char_p, []),
     "fa_cp_gb300_rand_sequence": (None, [C.c_uint, C.c_int, _ip]),
 }
+
+
+# ---------------------------------------------------------------- learned warm start
+
+_fp = C.POINTER(C.c_float)
+LEARN_SYMBOLS = {
+    "pdal_mlp_create": (C.c_void_p, [C.c_int, C.c_int, C.c_int, C.c_uint, C.c_int]),
+    "pdal_mlp_free": (None, [C.c_void_p]),
+    "pdal_mlp_num_params": (C.c_longlong, [C.c_void_p]),
+    "pdal_mlp_get_params": (C.c_int, [C.c_void_p, _fp]),
+    "pdal_mlp_set_params": (C.c_int, [C.c_void_p, _fp]),
+    "pdal_mlp_set_data": (C.c_int, [C.c_void_p, C.c_int, _fp, _fp]),
+    "pdal_mlp_train": (C.c_double, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_uint]),
+    "pdal_mlp_loss_grad": (C.c_double, [C.c_void_p, C.c_int, _fp, _fp, _fp]),
+    "pdal_mlp_predict": (C.c_int, [C.c_void_p, C.c_int, _fp, _fp, C.c_int]),
+    "pdal_mlp_last_error": (C.c_char_p, []),
+}
+
+
+def load_learn() -> C.CDLL:
+    return load("libpdal_learn_gb300.so", LEARN_SYMBOLS)
 
 
 def lib_path(name: str) -> Path:

@@ -43,6 +43,7 @@ struct BInst {
     const double *pv0; /* power-iteration start vector (m) */
     double *out_x, *out_y, *out_rc;
     double obj_norm, bnd_norm, obj_const;
+    double sigma0; /* > 0: initial sigma of this instance (sigma mode) */
 };
 
 /* Per-instance outcome. */
@@ -348,7 +349,7 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
             s.sigma_base = 1.0 / sqrt(fmax(s.lambda_param, 1e-16));
             s.sigma_min = o.sigma_min_factor * s.sigma_base;
             s.sigma_max = o.sigma_max_factor * s.sigma_base;
-            s.sigma = o.sigma_set ? o.sigma : o.sigma_init_factor * s.sigma_base;
+            s.sigma = I.sigma0 > 0.0 ? I.sigma0 : (o.sigma_set ? o.sigma : o.sigma_init_factor * s.sigma_base);
             s.sigma = fmin(fmax(s.sigma, s.sigma_min), s.sigma_max);
             s.sigma_best = s.sigma;
             s.sigma_adapt = o.sigma_adaptive != 0;

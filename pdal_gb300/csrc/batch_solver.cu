@@ -84,7 +84,8 @@ void run_threads(int count, const std::function<void(int)> &fn) {
 }
 
 int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t &P, const cp_al_gb300_options_t &O,
-                cp_al_result_t **results, cp_al_gb300_instance_info_t *info, cp_al_gb300_batch_stats_t *stats) {
+                const double *sigma0, cp_al_result_t **results, cp_al_gb300_instance_info_t *info,
+                cp_al_gb300_batch_stats_t *stats) {
     const double t_begin = now_sec();
     if (count <= 0) throw Error("batch_solve: count must be positive");
     if (!problems || !results) throw Error("batch_solve: missing problem or result array");
@@ -275,6 +276,7 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
         I.obj_norm = p.cp.obj_norm;
         I.bnd_norm = p.cp.bnd_norm;
         I.obj_const = p.cp.obj_const;
+        I.sigma0 = (sigma0 && std::isfinite(sigma0[i])) ? sigma0[i] : 0.0;
     });
     memcpy(host + insts_off, insts.data(), sizeof(BInst) * count);
     std::vector<int> order(count);
@@ -407,8 +409,9 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
 } // namespace pdal
 
 extern "C" int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t *params,
-                                       const cp_al_gb300_options_t *opts, cp_al_result_t **results,
-                                       cp_al_gb300_instance_info_t *info, cp_al_gb300_batch_stats_t *stats) {
+                                       const cp_al_gb300_options_t *opts, const double *sigma0,
+                                       cp_al_result_t **results, cp_al_gb300_instance_info_t *info,
+                                       cp_al_gb300_batch_stats_t *stats) {
     pdal::clear_last_error();
     cp_al_parameters_t p;
     if (params)
@@ -421,7 +424,7 @@ extern "C" int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems,
     else
         cp_al_gb300_default_options(&o);
     try {
-        return pdal::batch_solve(count, problems, p, o, results, info, stats);
+        return pdal::batch_solve(count, problems, p, o, sigma0, results, info, stats);
     } catch (const std::exception &e) {
         pdal::set_last_error(e.what());
         return -1;

@@ -283,9 +283,12 @@ class LPSession:
 
 
 def solve_batch(items: list[LPData], params: dict | N.CpalParameters | None = None,
-                options: dict | N.CpalOptions | None = None) -> tuple[list[LPResult], dict]:
+                options: dict | N.CpalOptions | None = None,
+                sigma0: np.ndarray | None = None) -> tuple[list[LPResult], dict]:
     """All instances in one persistent launch (cp_al_gb300_batch_solve);
-    returns the per-instance results and the batch statistics."""
+    returns the per-instance results (their .stats hold the final controller
+    state) and the batch statistics.  sigma0: optional per-instance initial
+    sigma for sigma mode."""
     lib = N.load_lp()
     p = params if isinstance(params, N.CpalParameters) else apply_params(default_parameters(lib), params)
     o = options if isinstance(options, N.CpalOptions) else apply_options(default_options(lib), options)
@@ -295,7 +298,9 @@ def solve_batch(items: list[LPData], params: dict | N.CpalParameters | None = No
         res = (C.POINTER(N.CpalResult) * len(probs))()
         info = (N.InstanceInfo * len(probs))()
         st = N.BatchStats()
-        if lib.cp_al_gb300_batch_solve(len(probs), arr, C.byref(p), C.byref(o), res, info, C.byref(st)) != 0:
+        s0 = None if sigma0 is None else np.ascontiguousarray(sigma0, dtype=np.float64)
+        if lib.cp_al_gb300_batch_solve(len(probs), arr, C.byref(p), C.byref(o), _ptr(s0), res, info,
+                                       C.byref(st)) != 0:
             raise RuntimeError("batch solve failed: " + N.last_error(lib))
         out = []
         for q, r, f in zip(probs, res, info):

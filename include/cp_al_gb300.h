@@ -122,7 +122,9 @@ const char *cp_al_gb300_last_error(void);
  * -- with its own controller state, and takes the next.  There is no
  * counterpart in the reference, whose benchmarks solve instances one at a
  * time through solve_lp_problem.  Every instance uses the same parameters and
- * options; the iteration is the FP64 form (precision is ignored). */
+ * options; precision CP_AL_GB300_FP32_REFINE runs each instance's FP32 phase
+ * (FP64 anchors, evaluation and control) and then its FP64 refinement, as the
+ * single-instance solver does. */
 typedef struct {
     int instances;
     int optimal;          /* instances that reached OPTIMAL */
@@ -147,6 +149,7 @@ typedef struct {
     double lambda_est;   /* sigma_max(A)^2 estimate of the scaled matrix */
     int restarts;
     int power_iterations;
+    int fp32_iterations; /* iterations run in the FP32 phase */
 } cp_al_gb300_instance_info_t;
 
 /* Solves problems[0..count) and stores one result per instance in

@@ -246,6 +246,7 @@ class InstanceInfo(C.Structure):
         ("lambda_est", C.c_double),
         ("restarts", C.c_int),
         ("power_iterations", C.c_int),
+        ("fp32_iterations", C.c_int),
     ]
 
 

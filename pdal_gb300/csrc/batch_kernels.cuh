@@ -41,6 +41,11 @@ struct BInst {
     double *x, *xbar, *xh, *lam, *y, *yh, *ybar, *ax, *u, *ax0, *phat;
     double *dsc, *rsc, *clbf, *cubf, *tn, *tm, *tm2;
     const double *pv0; /* power-iteration start vector (m) */
+    /* the FP32 phase: matrix values, bounds and iterates rounded to FP32,
+     * the FP64 anchors as (hi, lo) float pairs */
+    float *Avf, *Atvf, *cf, *vlbf, *vubf, *clbF, *cubF;
+    float *xf, *xbarf, *xhf, *lamf, *yf, *yhf, *ybarf, *axf, *uf;
+    float2 *x0f, *y0f, *ax0f;
     double *out_x, *out_y, *out_rc;
     double obj_norm, bnd_norm, obj_const;
     double sigma0; /* > 0: initial sigma of this instance (sigma mode) */
@@ -53,6 +58,7 @@ struct BOut {
     double lambda_est, pw, step, elapsed;
     double setup_sec;
     double sigma, sigma_best;
+    int fp32_iterations, pad;
 };
 
 /* Batch-wide options resolved on the host. */
@@ -65,11 +71,15 @@ struct BOpts {
     double al_lambda;
     int sigma_mode, sigma_set, sigma_adaptive, lambda_param_set;
     double sigma, sigma_init_factor, sigma_min_factor, sigma_max_factor, lambda_param;
+    int fp32;              /* run the FP32 phase first */
+    int fp32_stall_evals;
+    double fp32_switch_tol;
 };
 
 /* Shared-memory staging reused by every phase (the evaluation of the rows
  * gathers three vectors, the largest user). */
 union BSmem {
+    RowBlockSmem<kBS, 1, float> onef;
     RowBlockSmem<kBS, 1, double> one;
     RowBlockSmem<kBS, 2, double> two;
     RowBlockSmem<kBS, 3, double> three;
@@ -88,10 +98,10 @@ __device__ __forceinline__ void blk_rows(int nr, F f) {
 }
 
 /* The instance's row blocks of one matrix, run by this block. */
-template <int NP, class Gat, class Epi, class R>
+template <int NP, typename T, class Gat, class Epi, class R>
 __device__ __forceinline__ void blk_spmv(int nblocks, const int4 *desc, const int4 *linfo, double *lpart,
-                                         unsigned *lcount, int nlong, const int *rp, const int *ci, const double *val,
-                                         Gat &gat, Epi &epi, R &red, RowBlockSmem<kBS, NP, double> &sm) {
+                                         unsigned *lcount, int nlong, const int *rp, const int *ci, const T *val,
+                                         Gat &gat, Epi &epi, R &red, RowBlockSmem<kBS, NP, T> &sm) {
     RowPlanDev plan;
     plan.desc = desc;
     plan.linfo = linfo;
@@ -100,7 +110,7 @@ __device__ __forceinline__ void blk_spmv(int nblocks, const int4 *desc, const in
     plan.nblocks = nblocks;
     plan.nlong = nlong;
     for (int b = 0; b < nblocks; ++b) {
-        rowblock_run_at<kBS, NP, double>(b, plan, rp, ci, val, gat, epi, red, sm);
+        rowblock_run_at<kBS, NP, T>(b, plan, rp, ci, val, gat, epi, red, sm);
         __syncthreads();
     }
 }
@@ -324,6 +334,258 @@ __device__ double blk_power(const BInst &I, const BOpts &o, BSmem &sm, double *s
 
 /* ------------------------------------------------------------------ one instance */
 
+/* The arrays one precision phase iterates on. */
+template <typename T>
+struct BVec {
+    T *x, *xbar, *xh, *lam, *y, *yh, *ybar, *ax, *u;
+    const T *c, *vlb, *vub, *clb, *cub, *Av, *Atv;
+    const typename AnchorT<T>::type *x0, *y0, *ax0;
+};
+__device__ __forceinline__ BVec<double> bvec64(const BInst &I) {
+    return BVec<double>{I.x,   I.xbar, I.xh,  I.lam, I.y,  I.yh, I.ybar, I.ax, I.u,  I.c,  I.vlb,
+                        I.vub, I.clb,  I.cub, I.Av,  I.Atv, I.x0, I.y0,   I.ax0};
+}
+__device__ __forceinline__ BVec<float> bvec32(const BInst &I) {
+    return BVec<float>{I.xf,   I.xbarf, I.xhf, I.lamf, I.yf,   I.yhf, I.ybarf, I.axf, I.uf,  I.cf,  I.vlbf,
+                       I.vubf, I.clbF,  I.cubF, I.Avf, I.Atvf, I.x0f, I.y0f,   I.ax0f};
+}
+
+template <typename T>
+__device__ __forceinline__ BVec<T> bvec(const BInst &I);
+template <>
+__device__ __forceinline__ BVec<double> bvec<double>(const BInst &I) {
+    return bvec64(I);
+}
+template <>
+__device__ __forceinline__ BVec<float> bvec<float>(const BInst &I) {
+    return bvec32(I);
+}
+
+template <typename T>
+__device__ __forceinline__ float2 *anchor_split(const BInst &I, int which);
+template <>
+__device__ __forceinline__ float2 *anchor_split<double>(const BInst &, int) {
+    return nullptr;
+}
+template <>
+__device__ __forceinline__ float2 *anchor_split<float>(const BInst &I, int which) {
+    return which == 0 ? I.x0f : (which == 1 ? I.y0f : I.ax0f);
+}
+
+/* A x0 (FP64 matrix) and the first predictor of a phase (k_init_ax). */
+template <typename T>
+__device__ void blk_init_ax(const BInst &I, const BVec<T> &v, const CpalState &s, bool beta_on, BSmem &sm) {
+    Coefs<T> k;
+    load_coefs(&s, k);
+    auto g = [&](int c, double *o2) { o2[0] = I.x0[c]; };
+    Red<0, 0> z;
+    if (beta_on) {
+        InitAxEpi<T, true> e;
+        e.ax = v.ax;
+        e.u = v.u;
+        e.ax0 = I.ax0;
+        e.ax0f = anchor_split<T>(I, 2);
+        e.y = v.y;
+        e.lb = v.clb;
+        e.ub = v.cub;
+        e.beta = k.beta;
+        e.inv_beta = k.inv_beta;
+        blk_spmv<1>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, (const double *)I.Av, g, e, z,
+                    sm.one);
+    } else {
+        InitAxEpi<T, false> e;
+        e.ax = v.ax;
+        e.u = v.u;
+        e.ax0 = I.ax0;
+        e.ax0f = anchor_split<T>(I, 2);
+        e.y = v.y;
+        e.lb = v.clb;
+        e.ub = v.cub;
+        e.beta = k.beta;
+        e.inv_beta = k.inv_beta;
+        blk_spmv<1>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, (const double *)I.Av, g, e, z,
+                    sm.one);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ RowBlockSmem<kBS, 1, T> &smem1(BSmem &sm);
+template <>
+__device__ __forceinline__ RowBlockSmem<kBS, 1, double> &smem1<double>(BSmem &sm) {
+    return sm.one;
+}
+template <>
+__device__ __forceinline__ RowBlockSmem<kBS, 1, float> &smem1<float>(BSmem &sm) {
+    return sm.onef;
+}
+
+/* One precision phase: evaluation blocks until the controller terminates the
+ * solve or (FP32) ends the phase.  The arithmetic of k_primal / k_dual /
+ * k_eval_rows / k_eval_cols / k_control / k_restart. */
+template <typename T>
+__device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem &sm, double *sbuf, CpalState &s,
+                          Red<6, 1> *lacc6, double *sh, bool beta_on) {
+    const BVec<T> v = bvec<T>(I);
+    const int F = p.F;
+    for (;;) {
+        Coefs<T> k;
+        load_coefs(&s, k);
+        const int inner = s.inner;
+        for (int i = 1; i <= F; ++i) {
+            HalpernW wd;
+            HalpernWf wf;
+            cpal_halpern_entry(inner, i, wd, wf);
+            const T w = sizeof(T) == 8 ? (T)wd.w : (T)wf.w;
+            const T omw = sizeof(T) == 8 ? (T)wd.omw : (T)wf.omw;
+            const T *gat = beta_on ? v.u : v.y;
+            auto gp = [&](int c, T *o2) { o2[0] = gat[c]; };
+            PrimalArgs<T> pa{v.x, v.xbar, v.xh, v.lam, v.x0, v.c, v.vlb, v.vub};
+            Red<0, 0> z;
+            if (i == F) {
+                PrimalEpi<T, true> e;
+                e.a = pa;
+                e.k = k;
+                e.w = w;
+                e.omw = omw;
+                blk_spmv<1>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci, v.Atv, gp, e,
+                            z, smem1<T>(sm));
+            } else {
+                PrimalEpi<T, false> e;
+                e.a = pa;
+                e.k = k;
+                e.w = w;
+                e.omw = omw;
+                blk_spmv<1>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci, v.Atv, gp, e,
+                            z, smem1<T>(sm));
+            }
+            if (I.m > 0) {
+                DualArgs<T> da{v.y, v.yh, v.ybar, v.ax, v.u, v.y0, v.ax0, v.clb, v.cub};
+                auto gd = [&](int c, T *o2) { o2[0] = v.xbar[c]; };
+#define PDAL_BATCH_DUAL(MAJ, BET)                                                                                      \
+    {                                                                                                                  \
+        DualEpi<T, MAJ, BET> e;                                                                                        \
+        e.a = da;                                                                                                      \
+        e.k = k;                                                                                                       \
+        e.w = w;                                                                                                       \
+        e.omw = omw;                                                                                                   \
+        blk_spmv<1>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, v.Av, gd, e, z, smem1<T>(sm)); \
+    }
+                if (i == F) {
+                    if (beta_on)
+                        PDAL_BATCH_DUAL(true, true)
+                    else
+                        PDAL_BATCH_DUAL(true, false)
+                } else {
+                    if (beta_on)
+                        PDAL_BATCH_DUAL(false, true)
+                    else
+                        PDAL_BATCH_DUAL(false, false)
+                }
+#undef PDAL_BATCH_DUAL
+            }
+        }
+        /* evaluation in FP64 over the FP64 matrices */
+        CpalEval e{};
+        if (threadIdx.x == 0) lacc6->zero();
+        __syncthreads();
+        {
+            EvalRowsB<EvalRowEpi<T>> ep;
+            ep.a = EvalRowArgs<T>{v.xh, v.xbar, v.yh, v.ybar, I.x0, I.y0, I.ax0, I.clb, I.cub, I.clbf, I.cubf,
+                                  I.rsc, I.phat, nullptr, 0};
+            ep.la.acc = lacc6;
+            auto g = [&](int c, double *o2) {
+                const double xhc = (double)v.xh[c];
+                o2[0] = xhc;
+                o2[1] = (double)v.xbar[c] - xhc;
+                o2[2] = xhc - I.x0[c];
+            };
+            Red<6, 1> r;
+            r.zero();
+            blk_spmv<3>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, (const double *)I.Av, g,
+                        ep, r, sm.three);
+            block_reduce<kThreads, 6, 1>(r, sbuf);
+            if (threadIdx.x == 0) {
+                for (int q = 0; q < 6; ++q) r.s[q] += lacc6->s[q];
+                r.mx[0] = fmax(r.mx[0], lacc6->mx[0]);
+                sh[4] = r.s[0];
+                sh[5] = r.s[1];
+                sh[6] = r.s[2];
+                sh[7] = r.s[3];
+                sh[8] = r.s[4];
+                sh[9] = r.s[5];
+                sh[10] = r.mx[0];
+                lacc6->zero();
+            }
+            __syncthreads();
+        }
+        {
+            EvalRowsB<EvalColEpi<T>> ec;
+            ec.a = EvalColArgs<T>{v.xh, v.xbar, v.yh, v.ybar, v.lam, I.x0, I.c, I.dsc, nullptr, 0};
+            ec.la.acc = lacc6;
+            auto g = [&](int c, double *o2) {
+                const double yhc = (double)v.yh[c];
+                o2[0] = yhc;
+                o2[1] = (double)v.ybar[c] - yhc;
+            };
+            Red<6, 1> r;
+            r.zero();
+            blk_spmv<2>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci,
+                        (const double *)I.Atv, g, ec, r, sm.two);
+            block_reduce<kThreads, 6, 1>(r, sbuf);
+            if (threadIdx.x == 0) {
+                for (int q = 0; q < 6; ++q) r.s[q] += lacc6->s[q];
+                r.mx[0] = fmax(r.mx[0], lacc6->mx[0]);
+                e.rp2 = sh[4];
+                e.contrib = sh[5];
+                e.adx2 = sh[6];
+                e.dy2 = sh[7];
+                e.ddy2 = sh[8];
+                e.axd2 = sh[9];
+                e.rpmax = sh[10];
+                e.rd2 = r.s[0];
+                e.dx2 = r.s[1];
+                e.cross = r.s[2];
+                e.cx = r.s[3];
+                e.lx = r.s[4];
+                e.ddx2 = r.s[5];
+                e.rdmax = r.mx[0];
+                s.elapsed = (double)(globaltimer_ns() - s.t_start_ns) * 1e-9;
+                cpal_end_of_block(s, p, e);
+            }
+            __syncthreads();
+        }
+        if (s.status) return;
+        if (s.restart) { /* k_restart */
+            Coefs<T> kr;
+            load_coefs(&s, kr);
+            float2 *x0s = anchor_split<T>(I, 0), *y0s = anchor_split<T>(I, 1), *ax0s = anchor_split<T>(I, 2);
+            blk_for(I.n, [&](int j) {
+                const T val = v.xh[j];
+                v.x[j] = val;
+                I.x0[j] = (double)val;
+                if (x0s) x0s[j] = split_anchor((double)val);
+            });
+            blk_for(I.m, [&](int i) {
+                const T val = v.yh[i];
+                v.y[i] = val;
+                I.y0[i] = (double)val;
+                if (y0s) y0s[i] = split_anchor((double)val);
+                const double ph = I.phat[i];
+                I.ax0[i] = ph;
+                if (ax0s) ax0s[i] = split_anchor(ph);
+                const T axv = (T)ph;
+                v.ax[i] = axv;
+                if (beta_on) {
+                    const T z2 = vmax(v.clb[i], vmin(axv - val * kr.inv_beta, v.cub[i]));
+                    v.u[i] = val - kr.beta * (axv - z2);
+                }
+            });
+            __syncthreads();
+        }
+        if (sizeof(T) == 4 && s.phase_switch) return;
+    }
+}
+
 __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *out, BSmem &sm, double *sbuf,
                           CpalState &s, Red<6, 1> *lacc6, Red<1, 0> *lacc1, double *sh) {
     const unsigned long long t0 = globaltimer_ns();
@@ -360,7 +622,9 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
         s.best_gap = INFINITY;
         s.fp_last = INFINITY;
         s.refl = p.refl;
-        s.fp32_switch_tol = -1.0;
+        s.fp32_switch_tol = o.fp32 ? o.fp32_switch_tol : -1.0;
+        s.fp32_stall_limit = o.fp32_stall_evals;
+        s.fp32_best_kkt = INFINITY;
         s.iter_limit = p.iteration_limit;
         cpal_set_coefficients(s);
         s.t_start_ns = globaltimer_ns();
@@ -381,193 +645,75 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
         I.ybar[i] = 0.0;
         I.u[i] = 0.0;
     });
-    __syncthreads();
-    auto init_ax = [&]() {
-        if (beta_on) {
-            InitAxEpi<double, true> e;
-            e.ax = I.ax;
-            e.u = I.u;
-            e.ax0 = I.ax0;
-            e.ax0f = nullptr;
-            e.y = I.y;
-            e.lb = I.clb;
-            e.ub = I.cub;
-            e.beta = s.beta;
-            e.inv_beta = s.inv_beta;
-            auto g = [&](int c, double *o2) { o2[0] = I.x0[c]; };
-            Red<0, 0> z;
-            blk_spmv<1>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, I.Av, g, e, z, sm.one);
-        } else {
-            InitAxEpi<double, false> e;
-            e.ax = I.ax;
-            e.u = I.u;
-            e.ax0 = I.ax0;
-            e.ax0f = nullptr;
-            e.y = I.y;
-            e.lb = I.clb;
-            e.ub = I.cub;
-            e.beta = 0.0;
-            e.inv_beta = 0.0;
-            auto g = [&](int c, double *o2) { o2[0] = I.x0[c]; };
-            Red<0, 0> z;
-            blk_spmv<1>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, I.Av, g, e, z, sm.one);
+    int fp32_iters = 0;
+    if (o.fp32) {
+        /* FP32 copies of the scaled problem and the starting point */
+        for (int k = threadIdx.x; k < I.nnz; k += kThreads) {
+            I.Avf[k] = (float)I.Av[k];
+            I.Atvf[k] = (float)I.Atv[k];
         }
-    };
-    init_ax();
-
-    const int F = p.F;
-    for (;;) {
-        Coefs<double> k;
-        k.tau = s.tau;
-        k.inv_tau = s.inv_tau;
-        k.rho = s.rho;
-        k.inv_prox = s.inv_prox;
-        k.beta = s.beta;
-        k.inv_beta = s.inv_beta;
-        k.r = s.refl;
-        const int inner = s.inner;
-        for (int i = 1; i <= F; ++i) {
-            const int kk = inner + i;
-            const double w = (double)kk / (double)(kk + 1);
-            const double omw = 1.0 - w;
-            const double *gat = beta_on ? I.u : I.y;
-            auto gp = [&](int c, double *o2) { o2[0] = gat[c]; };
-            PrimalArgs<double> pa{I.x, I.xbar, I.xh, I.lam, I.x0, I.c, I.vlb, I.vub};
-            Red<0, 0> z;
-            if (i == F) {
-                PrimalEpi<double, true> e;
-                e.a = pa;
-                e.k = k;
-                e.w = w;
-                e.omw = omw;
-                blk_spmv<1>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci, I.Atv, gp, e,
-                            z, sm.one);
-            } else {
-                PrimalEpi<double, false> e;
-                e.a = pa;
-                e.k = k;
-                e.w = w;
-                e.omw = omw;
-                blk_spmv<1>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci, I.Atv, gp, e,
-                            z, sm.one);
-            }
-            if (I.m > 0) {
-                DualArgs<double> da{I.y, I.yh, I.ybar, I.ax, I.u, I.y0, I.ax0, I.clb, I.cub};
-                auto gd = [&](int c, double *o2) { o2[0] = I.xbar[c]; };
-#define PDAL_BATCH_DUAL(MAJ, BET)                                                                                      \
-    {                                                                                                                  \
-        DualEpi<double, MAJ, BET> e;                                                                                   \
-        e.a = da;                                                                                                      \
-        e.k = k;                                                                                                       \
-        e.w = w;                                                                                                       \
-        e.omw = omw;                                                                                                   \
-        blk_spmv<1>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, I.Av, gd, e, z, sm.one);     \
-    }
-                if (i == F) {
-                    if (beta_on)
-                        PDAL_BATCH_DUAL(true, true)
-                    else
-                        PDAL_BATCH_DUAL(true, false)
-                } else {
-                    if (beta_on)
-                        PDAL_BATCH_DUAL(false, true)
-                    else
-                        PDAL_BATCH_DUAL(false, false)
-                }
-#undef PDAL_BATCH_DUAL
-            }
-        }
-        /* evaluation (k_eval_rows / k_eval_cols / k_control) */
-        CpalEval e{};
-        if (threadIdx.x == 0) lacc6->zero();
+        blk_for(I.n, [&](int j) {
+            I.cf[j] = (float)I.c[j];
+            I.vlbf[j] = (float)I.vlb[j];
+            I.vubf[j] = (float)I.vub[j];
+            const float xv = (float)I.x0[j];
+            I.xf[j] = xv;
+            I.xhf[j] = xv;
+            I.lamf[j] = 0.f;
+            I.xbarf[j] = 0.f;
+            I.x0f[j] = split_anchor(I.x0[j]);
+        });
+        blk_for(I.m, [&](int i) {
+            I.clbF[i] = (float)I.clb[i];
+            I.cubF[i] = (float)I.cub[i];
+            const float yv = (float)I.y0[i];
+            I.yf[i] = yv;
+            I.yhf[i] = yv;
+            I.ybarf[i] = 0.f;
+            I.uf[i] = 0.f;
+            I.y0f[i] = split_anchor(I.y0[i]);
+        });
         __syncthreads();
-        {
-            EvalRowsB<EvalRowEpi<double>> ep;
-            ep.a = EvalRowArgs<double>{I.xh, I.xbar, I.yh, I.ybar, I.x0, I.y0, I.ax0, I.clb, I.cub, I.clbf, I.cubf,
-                                       I.rsc, I.phat, nullptr, 0};
-            ep.la.acc = lacc6;
-            auto g = [&](int c, double *o2) {
-                const double xhc = I.xh[c];
-                o2[0] = xhc;
-                o2[1] = I.xbar[c] - xhc;
-                o2[2] = xhc - I.x0[c];
-            };
-            Red<6, 1> r;
-            r.zero();
-            blk_spmv<3>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, I.Av, g, ep, r, sm.three);
-            block_reduce<kThreads, 6, 1>(r, sbuf);
-            if (threadIdx.x == 0) {
-                for (int q = 0; q < 6; ++q) r.s[q] += lacc6->s[q];
-                r.mx[0] = fmax(r.mx[0], lacc6->mx[0]);
-                sh[4] = r.s[0];
-                sh[5] = r.s[1];
-                sh[6] = r.s[2];
-                sh[7] = r.s[3];
-                sh[8] = r.s[4];
-                sh[9] = r.s[5];
-                sh[10] = r.mx[0];
-                lacc6->zero();
-            }
-            __syncthreads();
-        }
-        {
-            EvalRowsB<EvalColEpi<double>> ec;
-            ec.a = EvalColArgs<double>{I.xh, I.xbar, I.yh, I.ybar, I.lam, I.x0, I.c, I.dsc, nullptr, 0};
-            ec.la.acc = lacc6;
-            auto g = [&](int c, double *o2) {
-                const double yhc = I.yh[c];
-                o2[0] = yhc;
-                o2[1] = I.ybar[c] - yhc;
-            };
-            Red<6, 1> r;
-            r.zero();
-            blk_spmv<2>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci, I.Atv, g, ec, r,
-                        sm.two);
-            block_reduce<kThreads, 6, 1>(r, sbuf);
-            if (threadIdx.x == 0) {
-                for (int q = 0; q < 6; ++q) r.s[q] += lacc6->s[q];
-                r.mx[0] = fmax(r.mx[0], lacc6->mx[0]);
-                e.rp2 = sh[4];
-                e.contrib = sh[5];
-                e.adx2 = sh[6];
-                e.dy2 = sh[7];
-                e.ddy2 = sh[8];
-                e.axd2 = sh[9];
-                e.rpmax = sh[10];
-                e.rd2 = r.s[0];
-                e.dx2 = r.s[1];
-                e.cross = r.s[2];
-                e.cx = r.s[3];
-                e.lx = r.s[4];
-                e.ddx2 = r.s[5];
-                e.rdmax = r.mx[0];
-                s.elapsed = (double)(globaltimer_ns() - s.t_start_ns) * 1e-9;
-                cpal_end_of_block(s, p, e);
-            }
-            __syncthreads();
-        }
-        if (s.status) break;
-        if (s.restart) { /* k_restart */
+        blk_init_ax<float>(I, bvec32(I), s, beta_on, sm);
+        blk_phase<float>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
+        fp32_iters = s.total;
+        if (!s.status) {
+            /* FP64 refinement from the FP32 iterate (switch_to_fp64) */
             blk_for(I.n, [&](int j) {
-                const double v = I.xh[j];
-                I.x[j] = v;
-                I.x0[j] = v;
+                const double xv = (double)I.xhf[j];
+                I.xh[j] = xv;
+                I.x[j] = xv;
+                I.x0[j] = xv;
+                I.xbar[j] = (double)I.xbarf[j];
+                I.lam[j] = (double)I.lamf[j];
             });
-            const double beta = s.beta, inv_beta = s.inv_beta;
             blk_for(I.m, [&](int i) {
-                const double v = I.yh[i];
-                I.y[i] = v;
-                I.y0[i] = v;
-                const double ph = I.phat[i];
-                I.ax0[i] = ph;
-                I.ax[i] = ph;
-                if (beta_on) {
-                    const double z2 = fmax(I.clb[i], fmin(ph - v * inv_beta, I.cub[i]));
-                    I.u[i] = v - beta * (ph - z2);
-                }
+                const double yv = (double)I.yhf[i];
+                I.yh[i] = yv;
+                I.y[i] = yv;
+                I.y0[i] = yv;
+                I.ybar[i] = (double)I.ybarf[i];
             });
+            if (threadIdx.x == 0) {
+                s.inner = 0;
+                s.fp_last = INFINITY;
+                if (!s.restart) s.fp0 = s.fp;
+                s.phase_switch = 0;
+                s.fp32_switch_tol = -1.0;
+                s.restart = 0;
+            }
+            __syncthreads();
+            blk_init_ax<double>(I, bvec64(I), s, beta_on, sm);
+            blk_phase<double>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
+        } else {
+            blk_for(I.n, [&](int j) { I.xh[j] = (double)I.xhf[j]; });
+            blk_for(I.m, [&](int i) { I.yh[i] = (double)I.yhf[i]; });
             __syncthreads();
         }
+    } else {
+        __syncthreads();
+        blk_init_ax<double>(I, bvec64(I), s, beta_on, sm);
+        blk_phase<double>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
     }
     /* result (k_result_cols / k_result_rows) */
     {
@@ -582,8 +728,8 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
         re.rc_out = I.out_rc;
         auto g = [&](int c, double *o2) { o2[0] = I.yh[c]; };
         Red<0, 0> z;
-        blk_spmv<1>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci, I.Atv, g, re, z,
-                    sm.one);
+        blk_spmv<1>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci,
+                    (const double *)I.Atv, g, re, z, sm.one);
         const double ovr = s.ovr;
         blk_for(I.m, [&](int i) { I.out_y[i] = I.yh[i] / I.rsc[i] / ovr; });
     }
@@ -607,14 +753,19 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
         r.setup_sec = sh[3];
         r.sigma = s.sigma_on ? s.sigma : 0.0;
         r.sigma_best = s.sigma_on ? s.sigma_best : 0.0;
+        r.fp32_iterations = fp32_iters;
+        r.pad = 0;
         *out = r;
     }
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads, 2) k_batch_lp(const BInst *__restrict__ insts, int count,
-                                                          const int *__restrict__ order, unsigned *queue, CpalParams p,
-                                                          BOpts o, BOut *outs) {
+/* MINB: resident blocks per SM the register allocation targets (more
+ * resident instances hide more of each block's load latency). */
+template <int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_batch_lp(const BInst *__restrict__ insts, int count,
+                                                             const int *__restrict__ order, unsigned *queue,
+                                                             CpalParams p, BOpts o, BOut *outs) {
     __shared__ BSmem sm;
     __shared__ CpalState s;
     __shared__ double sbuf[8 * (kThreads / 32)];

@@ -29,6 +29,9 @@ namespace {
 
 using namespace batch;
 
+/* resident blocks per SM of the persistent launch */
+constexpr int kBatchMinBlocks = 2;
+
 double now_sec() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -38,6 +41,7 @@ struct Layout {
     size_t Arp, Aci, Av, Atrp, Atci, Atv, Adesc, Alinfo, Alpart, Alcount, Atdesc, Atlinfo, Atlpart, Atlcount;
     size_t c, vlb, vub, clb, cub, x0, y0, x, xbar, xh, lam, y, yh, ybar, ax, u, ax0, phat;
     size_t dsc, rsc, clbf, cubf, tn, tm, tm2, pv0;
+    size_t Avf, Atvf, cf, vlbf, vubf, clbF, cubF, xf, xbarf, xhf, lamf, yf, yhf, ybarf, axf, uf, x0f, y0f, ax0f;
     size_t out_x, out_y, out_rc;
 };
 
@@ -135,6 +139,15 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
         for (size_t *f : {&l.clb, &l.cub, &l.y0, &l.y, &l.yh, &l.ybar, &l.ax, &l.u, &l.ax0, &l.phat, &l.rsc, &l.clbf,
                           &l.cubf, &l.tm, &l.tm2, &l.pv0})
             *f = pk.take(m * 8);
+        const bool f32 = O.precision == CP_AL_GB300_FP32_REFINE;
+        const size_t fn = f32 ? n : 0, fm = f32 ? m : 0, fz = f32 ? nnz + 8 : 0;
+        l.Avf = pk.take(fz * 4);
+        l.Atvf = pk.take(fz * 4);
+        for (size_t *f : {&l.cf, &l.vlbf, &l.vubf, &l.xf, &l.xbarf, &l.xhf, &l.lamf}) *f = pk.take(fn * 4);
+        for (size_t *f : {&l.clbF, &l.cubF, &l.yf, &l.yhf, &l.ybarf, &l.axf, &l.uf}) *f = pk.take(fm * 4);
+        l.x0f = pk.take(fn * 8);
+        l.y0f = pk.take(fm * 8);
+        l.ax0f = pk.take(fm * 8);
     }
     /* outputs last, contiguous: one download */
     const size_t out_begin = pk.size();
@@ -270,6 +283,25 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
         I.tm = (double *)D(l.tm);
         I.tm2 = (double *)D(l.tm2);
         I.pv0 = (const double *)D(l.pv0);
+        I.Avf = (float *)D(l.Avf);
+        I.Atvf = (float *)D(l.Atvf);
+        I.cf = (float *)D(l.cf);
+        I.vlbf = (float *)D(l.vlbf);
+        I.vubf = (float *)D(l.vubf);
+        I.clbF = (float *)D(l.clbF);
+        I.cubF = (float *)D(l.cubF);
+        I.xf = (float *)D(l.xf);
+        I.xbarf = (float *)D(l.xbarf);
+        I.xhf = (float *)D(l.xhf);
+        I.lamf = (float *)D(l.lamf);
+        I.yf = (float *)D(l.yf);
+        I.yhf = (float *)D(l.yhf);
+        I.ybarf = (float *)D(l.ybarf);
+        I.axf = (float *)D(l.axf);
+        I.uf = (float *)D(l.uf);
+        I.x0f = (float2 *)D(l.x0f);
+        I.y0f = (float2 *)D(l.y0f);
+        I.ax0f = (float2 *)D(l.ax0f);
         I.out_x = (double *)D(l.out_x);
         I.out_y = (double *)D(l.out_y);
         I.out_rc = (double *)D(l.out_rc);
@@ -311,17 +343,23 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
     bo.sigma_min_factor = O.sigma_min_factor;
     bo.sigma_max_factor = O.sigma_max_factor;
     bo.lambda_param = O.lambda_param;
+    bo.fp32 = O.precision == CP_AL_GB300_FP32_REFINE ? 1 : 0;
+    bo.fp32_stall_evals = O.fp32_stall_evals;
+    bo.fp32_switch_tol = O.fp32_switch_tol;
     CpalParams cp = prep[0].cp; /* instance-specific norms are overridden per instance in the kernel */
 
     int dev_id = 0, sms = 0, per_sm = 0;
     PDAL_CUDA(cudaGetDevice(&dev_id));
     PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
-    PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_lp, kThreads, 0));
+    int minb = kBatchMinBlocks;
+    if (const char *e = getenv("PDAL_BATCH_MINB")) minb = std::max(2, std::min(4, atoi(e)));
+    auto kern = minb == 4 ? k_batch_lp<4> : (minb == 3 ? k_batch_lp<3> : k_batch_lp<2>);
+    PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0));
     if (per_sm < 1) throw Error("the batch kernel does not fit on one SM");
     const int grid = std::max(1, std::min(count, per_sm * sms));
     PDAL_CUDA(cudaEventRecord(e0, stream));
-    k_batch_lp<<<grid, kThreads, 0, stream>>>((const BInst *)(dev + insts_off), count, (const int *)(dev + order_off),
-                                               (unsigned *)(dev + queue_off), cp, bo, (BOut *)(dev + outs_off));
+    kern<<<grid, kThreads, 0, stream>>>((const BInst *)(dev + insts_off), count, (const int *)(dev + order_off),
+                                        (unsigned *)(dev + queue_off), cp, bo, (BOut *)(dev + outs_off));
     PDAL_CUDA(cudaGetLastError());
     PDAL_CUDA(cudaEventRecord(e1, stream));
     PDAL_CUDA(cudaMemcpyAsync(host + out_begin, dev + out_begin, out_end - out_begin, cudaMemcpyDeviceToHost, stream));
@@ -373,6 +411,7 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
             f.lambda_est = o.lambda_est;
             f.restarts = o.restarts;
             f.power_iterations = o.power_iters;
+            f.fp32_iterations = o.fp32_iterations;
         }
         iters[i] = o.iterations;
         total_iters += o.iterations;

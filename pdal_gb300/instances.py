@@ -263,3 +263,27 @@ def planted_qp(n: int = 200_000, m: int = 100_000, nnz_per_col: int = 10, b_rows
     else:
         raise ValueError(q_form)
     return data, x, f
+
+
+def transport_family(supplies: int, demands: int, seeds, base_costs=None, perturb: float = 0.2) -> list[LPData]:
+    """transport_lp for many seeds, sharing one CSR of the (unit, complete
+    bipartite) constraint matrix: instance k equals
+    transport_lp(supplies, demands, seeds[k], base_costs, perturb)."""
+    S, D = supplies, demands
+    n = S * D
+    if base_costs is None:
+        base_costs = np.random.default_rng(4000).uniform(1, 100, size=n)
+    arc = np.arange(n)
+    A = _csr_from_coo(np.concatenate([arc // D, S + arc % D]), np.concatenate([arc, arc]), np.ones(2 * n), S + D, n)
+    Acsr = (A[0], A[1], A[2], (S + D, n))
+    out = []
+    for sd in seeds:
+        rng = np.random.default_rng(sd)
+        cost = base_costs * (1.0 + perturb * rng.standard_normal(n))
+        s = rng.uniform(10, 100, size=S)
+        d = rng.uniform(10, 100, size=D)
+        d *= s.sum() / d.sum()
+        cap = rng.uniform(20, 200, size=n)
+        b = np.concatenate([s, d])
+        out.append(LPData(cost, Acsr, b.copy(), b.copy(), np.zeros(n), cap))
+    return out

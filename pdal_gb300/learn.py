@@ -146,9 +146,16 @@ def point_kkt(d: LPData, x: np.ndarray, y: np.ndarray) -> float:
 
 @dataclass
 class WarmStart:
+    """MLP from instance features to (primal, dual, log sigma); inputs and
+    outputs are standardised with the training set's mean and deviation."""
+
     mlp: MLP
     S: int
     D: int
+    xm: np.ndarray
+    xs: np.ndarray
+    ym: np.ndarray
+    ys: np.ndarray
     train_loss: float
     train_sec: float
 
@@ -173,24 +180,33 @@ class WarmStart:
         X = np.stack([features(items[i], S, D) for i in keep])
         Y = np.stack([targets(items[i], res[i].x, res[i].y, res[i].stats.get("sigma_best", 0.0) or 1.0)
                       for i in keep])
+        xm, xs = X.mean(0), X.std(0) + 1e-6
+        ym, ys = Y.mean(0), Y.std(0) + 1e-6
         mlp = MLP(X.shape[1], hidden, Y.shape[1], seed=seed)
-        mlp.set_data(X, Y)
+        mlp.set_data((X - xm) / xs, (Y - ym) / ys)
         t0 = time.perf_counter()
         loss = mlp.train(epochs, batch, lr, seed)
-        return cls(mlp, S, D, loss, time.perf_counter() - t0)
+        return cls(mlp, S, D, xm, xs, ym, ys, loss, time.perf_counter() - t0)
+
+    def raw_predict(self, items: list[LPData], bf16: bool = True) -> np.ndarray:
+        X = np.stack([features(d, self.S, self.D) for d in items])
+        T = self.mlp.predict((X - self.xm) / self.xs, bf16=bf16).astype(np.float64)
+        return T * self.ys + self.ym
 
     def predict(self, items: list[LPData], bf16: bool = True):
-        """Warm starts, initial sigmas and whether each prediction was kept
-        (False: its residual was worse than the cold start's)."""
-        X = np.stack([features(d, self.S, self.D) for d in items])
-        T = self.mlp.predict(X, bf16=bf16)
-        xs, ys, sig, used = [], [], [], []
+        """Warm starts, initial sigmas, whether each prediction was kept
+        (False: its residual was worse than the cold start's) and the
+        predicted points' KKT errors."""
+        T = self.raw_predict(items, bf16)
+        xs, ys, sig, used, kkt = [], [], [], [], []
         for d, t in zip(items, T):
-            x, y, s = decode(d, t.astype(np.float64), self.S, self.D)
+            x, y, s = decode(d, t, self.S, self.D)
             m = len(d.con_ub)
-            ok = point_kkt(d, x, y) < point_kkt(d, np.zeros_like(x), np.zeros(m))
+            k = point_kkt(d, x, y)
+            ok = k < point_kkt(d, np.zeros_like(x), np.zeros(m))
             xs.append(x if ok else None)
             ys.append(y if ok else None)
             sig.append(s if ok else 0.0)
             used.append(ok)
-        return xs, ys, np.array(sig), np.array(used)
+            kkt.append(k)
+        return xs, ys, np.array(sig), np.array(used), np.array(kkt)

@@ -74,3 +74,21 @@ def test_batch_handles_iteration_limit_and_warm_start():
         d.primal_start, d.dual_start = r.x, r.y
     warm, _ = lp.solve_batch(items, {"eps": 1e-8, "iteration_limit": 200000})
     assert all(w.status == "OPTIMAL" and w.iterations <= c.iterations for w, c in zip(warm, cold))
+
+
+def test_batch_fp32_refine_matches_single_solver():
+    """Chosen form: FP32 phase with FP64 anchors/evaluation, then FP64
+    refinement; the result meets the FP64 tolerance and agrees with the
+    single-instance FP32_REFINE solve."""
+    items = batch_lps(count=12, seed=31, m_range=(80, 600)) + [long_row_lp(3)]
+    params = {"eps": 1e-8, "l_inf_ruiz_iterations": 4, "iteration_limit": 200000}
+    opts = {"precision": "fp32_refine"}
+    res, st = lp.solve_batch(items, params, opts)
+    for d, b in zip(items, res):
+        s = lp.solve(d, params, opts)
+        o = lp.solve(d, params)
+        assert b.status == s.status == "OPTIMAL"
+        assert b.kkt < 1e-8
+        assert abs(b.primal_objective - o.primal_objective) <= 1e-8 * (1 + abs(o.primal_objective))
+        assert abs(b.iterations - s.iterations) <= 0.05 * s.iterations + 200
+        assert b.stats["fp32_iterations"] > 0

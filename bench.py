@@ -22,6 +22,17 @@ resident session (every evaluation, restart and phase decision included).
             LP (2,000 x 5,000), which converges in seconds; the large LP needs
             minutes per solve
 
+Further sections of the same JSON line (skipped with --lp-only):
+  fa_cp_qp            the FA_CP convex QP at its benchmark size: time to
+                      relative KKT 1e-6 / 1e-8 through the C entry points,
+                      error against the planted optimum, CPU port per iteration
+  batch_4096          4,096 uneven LPs in one persistent launch (chosen form
+                      and FP64): solves/s, p50/p99 iterations, and the speed-up
+                      over the FP64 single-instance solver run one by one
+  learned_warm_start  the MLP warm start + initial sigma on the 200 x 200
+                      transportation family: iterations from the learned
+                      start vs the cold start on held-out instances
+
 --impl reference times the CPU restatement of the iteration (the reference
 has no CPU solver; the oracle port, every host thread) on a bounded sample:
 one evaluation block (200 iterations) per step, same metric.
@@ -37,6 +48,8 @@ import sys
 import tempfile
 import time
 from pathlib import Path
+
+import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
@@ -123,6 +136,22 @@ def peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def run_profile(args, local):
+    """Only the chosen-form iteration steps on the large LP (no other
+    sections): the command the ncu captures in profiles/ run."""
+    from pdal_gb300 import instances, lp
+
+    gen_kwargs, _ = WORKLOADS[args.workload]
+    data = instances.zipf_lp(**gen_kwargs)
+    chosen = {**SIGMA_PROTOCOL, "precision": "fp32_refine", "device": local, "fp32_stall_evals": 1_000_000_000}
+    sess = lp.LPSession(data, PARAMS, chosen)
+    sess.start()
+    for _ in range(args.warmup + args.steps):
+        r = sess.iterate(ITERS_PER_STEP)
+    sess.close()
+    print(json.dumps({"profile_run": args.workload, "iterations": r.iterations, "kkt": r.kkt}), flush=True)
 
 
 def run_ours(args, rank, world, local):
@@ -250,9 +279,112 @@ def run_ours(args, rank, world, local):
             "clocks": clk.summary(),
         }
         line["cpu_baseline"] = cpu_baseline(data, m, n, nnz)
+        if not args.lp_only:
+            line["fa_cp_qp"] = bench_qp(local)
+            line["batch_4096"] = bench_batch(local)
+            line["learned_warm_start"] = bench_learned(local)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def bench_qp(local):
+    """The FA_CP convex QP at its full benchmark size (n = 200,000, m = 100,000,
+    A 10 nnz/column, Q = B'B + diag with B 50,000 x 200,000 at 5 nnz/row, box
+    bounds, planted optimum): time to relative KKT 1e-6 and 1e-8 through the C
+    entry points (host buffers), against the planted objective; the CPU port's
+    time per iteration on a bounded sample (50 iterations, one thread)."""
+    from oracle import oracle as O
+    from pdal_gb300 import instances, qp
+
+    qd, _, f_star = instances.planted_qp()
+    out = {"workload": "QP n=200,000 m=100,000, A 2.0M nnz, Q=B'B+diag (sparse Q), planted optimum"}
+    for eps in (1e-6, 1e-8):
+        prm = {"eps": eps, "verbose": 0, "iteration_limit": 200_000, "time_limit": 300.0}
+        if eps == 1e-6:
+            qp.solve(qd, prm, {"device": local})
+        t0 = time.perf_counter()
+        r = qp.solve(qd, prm, {"device": local})
+        dt = time.perf_counter() - t0
+        out[f"eps_{eps:g}"] = {"s": dt, "status": r.status, "iterations": r.iterations,
+                               "inner_iterations": r.inner_iterations, "kkt": r.kkt,
+                               "rel_obj_err_vs_planted": abs(r.primal_objective - f_star) / (1 + abs(f_star)),
+                               "setup_s": r.stats["setup_sec"], "loop_s": r.stats["loop_sec"],
+                               "device_segments_ms": r.stats["device_loop_ms"],
+                               "kernel_launches": r.stats["kernel_launches"]}
+    t0 = time.perf_counter()
+    ro = O.solve_qp(qd, {"eps": 1e-14, "iteration_limit": 50, "sv_max_iter": 20})
+    out["cpu_port_s_per_iteration"] = ro.solve_sec / max(ro.iterations, 1)
+    out["cpu_port_sample"] = f"{ro.iterations} iterations ({ro.inner_iterations} BB steps), 1 thread, setup excluded"
+    out["gpu_s_per_iteration"] = out["eps_1e-06"]["loop_s"] / max(out["eps_1e-06"]["iterations"], 1)
+    return out
+
+
+def bench_batch(local, count=4096):
+    """4,096 uneven LPs (m log-uniform in [50, 5000], n = m*U[2,3], 3-20
+    nnz/column, planted) solved to relative KKT 1e-6 in one persistent launch,
+    chosen form (FP32 phase + FP64 refinement) and FP64, against the plain FP64
+    single-instance solver run instance by instance on the same GPU (timed on
+    48 evenly spaced instances, scaled to the batch)."""
+    from pdal_gb300 import instances, lp
+
+    items = instances.batch_lps(count=count)
+    nnz = sum(int(d.csr()[1].shape[0]) for d in items)
+    params = {"eps": 1e-6, "l_inf_ruiz_iterations": 4, "iteration_limit": 100_000}
+    out = {"workload": f"{count} LPs, m log-uniform [50, 5000], n = m*U[2,3], 3-20 nnz/column",
+           "sum_nnz": nnz}
+    for tag, opts in (("chosen_fp32_refine", {"precision": "fp32_refine", "device": local}),
+                      ("fp64", {"device": local})):
+        res, st = lp.solve_batch(items, params, opts)
+        out[tag] = {"total_s": st["total_sec"], "kernel_s": st["kernel_sec"], "solves_per_s": st["solves_per_sec"],
+                    "optimal": st["optimal"], "iterations_p50": st["iterations_p50"],
+                    "iterations_p99": st["iterations_p99"], "iterations_max": st["iterations_max"],
+                    "max_kkt": max(r.kkt for r in res), "grid_blocks": st["grid_blocks"]}
+    idx = [int(i) for i in np.linspace(0, count - 1, 48)]
+    lp.solve(items[idx[0]], params, {"device": local})
+    t0 = time.perf_counter()
+    seq_its = [lp.solve(items[i], params, {"device": local}).iterations for i in idx]
+    dt = time.perf_counter() - t0
+    out["sequential_fp64"] = {"sample": len(idx), "s_per_instance": dt / len(idx),
+                              "extrapolated_s": dt / len(idx) * count, "mean_iterations": float(np.mean(seq_its))}
+    out["speedup_vs_sequential"] = out["sequential_fp64"]["extrapolated_s"] / out["chosen_fp32_refine"]["total_s"]
+    return out
+
+
+def bench_learned(local, S=200, D=200, n_train=1024, n_test=128, epochs=60):
+    """Learned warm start + initial sigma on the 200 x 200 transportation
+    family: an MLP (3 layers, width 256, trained by the library's kernels on
+    solver-generated optima, BF16 inference) predicts the start; held-out
+    instances are solved to relative KKT 1e-6 from it and from the cold start
+    (both as one batch launch)."""
+    from pdal_gb300.instances import transport_family
+    from pdal_gb300.learn import WarmStart
+
+    base = np.random.default_rng(4000).uniform(1, 100, S * D)
+    train = transport_family(S, D, range(10_000, 10_000 + n_train), base)
+    test = transport_family(S, D, range(900_000, 900_000 + n_test), base)
+    params = {"eps": 1e-6, "l_inf_ruiz_iterations": 10, "iteration_limit": 100_000}
+    t0 = time.perf_counter()
+    solved, _ = WarmStart.solve_family(train, params)
+    t_label = time.perf_counter() - t0
+    ws = WarmStart.fit(train, S, D, params, hidden=256, epochs=epochs, batch=128, lr=1e-3, solved=solved)
+    cold, cst = WarmStart.solve_family(test, params)
+    t0 = time.perf_counter()
+    xs, ys, sig, used, kkt = ws.predict(test)
+    t_pred = time.perf_counter() - t0
+    for d, x, y in zip(test, xs, ys):
+        d.primal_start, d.dual_start = x, y
+    warm, wst = WarmStart.solve_family(test, params, sigma0=sig)
+    ic = float(np.mean([r.iterations for r in cold]))
+    iw = float(np.mean([r.iterations for r in warm]))
+    return {"workload": f"transportation LPs {S}x{D} ({S * D} arcs); {n_train} training optima, "
+                        f"{n_test} held-out instances",
+            "label_solve_s": t_label, "train_s": ws.train_sec, "train_loss": ws.train_loss,
+            "predict_s": t_pred, "predictions_used": float(np.mean(used)),
+            "predicted_point_kkt_median": float(np.median(kkt)),
+            "cold_mean_iterations": ic, "warm_mean_iterations": iw, "iteration_ratio": iw / ic,
+            "cold_batch_s": sum(s["total_sec"] for s in cst), "warm_batch_s": sum(s["total_sec"] for s in wst),
+            "all_optimal": all(r.status == "OPTIMAL" for r in cold + warm)}
 
 
 def cpu_baseline(data, m, n, nnz, blocks=1, warm=0):
@@ -314,9 +446,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_lp", choices=list(WORKLOADS))
+    ap.add_argument("--lp-only", action="store_true", help="skip the QP, batch and learned-start sections")
+    ap.add_argument("--profile", action="store_true", help="only the chosen-form iteration steps (for ncu)")
     args = ap.parse_args()
     rank, world, local = dist_env()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args, local)
+    elif args.impl == "reference":
         run_reference(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)

@@ -30,7 +30,7 @@ namespace {
 using namespace batch;
 
 /* resident blocks per SM of the persistent launch */
-constexpr int kBatchMinBlocks = 2;
+constexpr int kBatchMinBlocks = 3;
 
 double now_sec() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();

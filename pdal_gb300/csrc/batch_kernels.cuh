@@ -25,7 +25,6 @@
 namespace pdal {
 namespace batch {
 
-constexpr int kBS = 1024; /* nonzeros per row block */
 
 /* One instance: its arrays (device pointers into the batch arena). */
 struct BInst {
@@ -78,11 +77,12 @@ struct BOpts {
 
 /* Shared-memory staging reused by every phase (the evaluation of the rows
  * gathers three vectors, the largest user). */
+template <int BS>
 union BSmem {
-    RowBlockSmem<kBS, 1, float> onef;
-    RowBlockSmem<kBS, 1, double> one;
-    RowBlockSmem<kBS, 2, double> two;
-    RowBlockSmem<kBS, 3, double> three;
+    RowBlockSmem<BS, 1, float> onef;
+    RowBlockSmem<BS, 1, double> one;
+    RowBlockSmem<BS, 2, double> two;
+    RowBlockSmem<BS, 3, double> three;
 };
 
 template <class F>
@@ -98,10 +98,10 @@ __device__ __forceinline__ void blk_rows(int nr, F f) {
 }
 
 /* The instance's row blocks of one matrix, run by this block. */
-template <int NP, typename T, class Gat, class Epi, class R>
+template <int NP, int BS, typename T, class Gat, class Epi, class R>
 __device__ __forceinline__ void blk_spmv(int nblocks, const int4 *desc, const int4 *linfo, double *lpart,
                                          unsigned *lcount, int nlong, const int *rp, const int *ci, const T *val,
-                                         Gat &gat, Epi &epi, R &red, RowBlockSmem<kBS, NP, T> &sm) {
+                                         Gat &gat, Epi &epi, R &red, RowBlockSmem<BS, NP, T> &sm) {
     RowPlanDev plan;
     plan.desc = desc;
     plan.linfo = linfo;
@@ -110,7 +110,7 @@ __device__ __forceinline__ void blk_spmv(int nblocks, const int4 *desc, const in
     plan.nblocks = nblocks;
     plan.nlong = nlong;
     for (int b = 0; b < nblocks; ++b) {
-        rowblock_run_at<kBS, NP, T>(b, plan, rp, ci, val, gat, epi, red, sm);
+        rowblock_run_at<BS, NP, T>(b, plan, rp, ci, val, gat, epi, red, sm);
         __syncthreads();
     }
 }
@@ -267,7 +267,8 @@ struct PowRowEpiB {
 };
 
 /* sigma_max(A)^2 by the power iteration of k_power_* (start vector in tm). */
-__device__ double blk_power(const BInst &I, const BOpts &o, BSmem &sm, double *sbuf, Red<1, 0> *lacc,
+template <int BS>
+__device__ double blk_power(const BInst &I, const BOpts &o, BSmem<BS> &sm, double *sbuf, Red<1, 0> *lacc,
                             double *sh, int &iters) {
     double *v = I.tm, *vn = I.tm2, *dp = I.tn;
     blk_for(I.m, [&](int i) { v[i] = I.pv0[i]; });
@@ -373,8 +374,8 @@ __device__ __forceinline__ float2 *anchor_split<float>(const BInst &I, int which
 }
 
 /* A x0 (FP64 matrix) and the first predictor of a phase (k_init_ax). */
-template <typename T>
-__device__ void blk_init_ax(const BInst &I, const BVec<T> &v, const CpalState &s, bool beta_on, BSmem &sm) {
+template <typename T, int BS>
+__device__ void blk_init_ax(const BInst &I, const BVec<T> &v, const CpalState &s, bool beta_on, BSmem<BS> &sm) {
     Coefs<T> k;
     load_coefs(&s, k);
     auto g = [&](int c, double *o2) { o2[0] = I.x0[c]; };
@@ -408,22 +409,20 @@ __device__ void blk_init_ax(const BInst &I, const BVec<T> &v, const CpalState &s
     }
 }
 
-template <typename T>
-__device__ __forceinline__ RowBlockSmem<kBS, 1, T> &smem1(BSmem &sm);
-template <>
-__device__ __forceinline__ RowBlockSmem<kBS, 1, double> &smem1<double>(BSmem &sm) {
+template <int BS>
+__device__ __forceinline__ RowBlockSmem<BS, 1, double> &smem1(BSmem<BS> &sm, double) {
     return sm.one;
 }
-template <>
-__device__ __forceinline__ RowBlockSmem<kBS, 1, float> &smem1<float>(BSmem &sm) {
+template <int BS>
+__device__ __forceinline__ RowBlockSmem<BS, 1, float> &smem1(BSmem<BS> &sm, float) {
     return sm.onef;
 }
 
 /* One precision phase: evaluation blocks until the controller terminates the
  * solve or (FP32) ends the phase.  The arithmetic of k_primal / k_dual /
  * k_eval_rows / k_eval_cols / k_control / k_restart. */
-template <typename T>
-__device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem &sm, double *sbuf, CpalState &s,
+template <typename T, int BS>
+__device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem<BS> &sm, double *sbuf, CpalState &s,
                           Red<6, 1> *lacc6, double *sh, bool beta_on) {
     const BVec<T> v = bvec<T>(I);
     const int F = p.F;
@@ -448,7 +447,7 @@ __device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem &sm, double
                 e.w = w;
                 e.omw = omw;
                 blk_spmv<1>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci, v.Atv, gp, e,
-                            z, smem1<T>(sm));
+                            z, smem1(sm, T(0)));
             } else {
                 PrimalEpi<T, false> e;
                 e.a = pa;
@@ -456,7 +455,7 @@ __device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem &sm, double
                 e.w = w;
                 e.omw = omw;
                 blk_spmv<1>(I.nbAt, I.Atdesc, I.Atlinfo, I.Atlpart, I.Atlcount, I.nlAt, I.Atrp, I.Atci, v.Atv, gp, e,
-                            z, smem1<T>(sm));
+                            z, smem1(sm, T(0)));
             }
             if (I.m > 0) {
                 DualArgs<T> da{v.y, v.yh, v.ybar, v.ax, v.u, v.y0, v.ax0, v.clb, v.cub};
@@ -468,7 +467,7 @@ __device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem &sm, double
         e.k = k;                                                                                                       \
         e.w = w;                                                                                                       \
         e.omw = omw;                                                                                                   \
-        blk_spmv<1>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, v.Av, gd, e, z, smem1<T>(sm)); \
+        blk_spmv<1>(I.nbA, I.Adesc, I.Alinfo, I.Alpart, I.Alcount, I.nlA, I.Arp, I.Aci, v.Av, gd, e, z, smem1(sm, T(0))); \
     }
                 if (i == F) {
                     if (beta_on)
@@ -586,7 +585,8 @@ __device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem &sm, double
     }
 }
 
-__device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *out, BSmem &sm, double *sbuf,
+template <int BS>
+__device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *out, BSmem<BS> &sm, double *sbuf,
                           CpalState &s, Red<6, 1> *lacc6, Red<1, 0> *lacc1, double *sh) {
     const unsigned long long t0 = globaltimer_ns();
     p.obj_norm = I.obj_norm;
@@ -674,8 +674,8 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
             I.y0f[i] = split_anchor(I.y0[i]);
         });
         __syncthreads();
-        blk_init_ax<float>(I, bvec32(I), s, beta_on, sm);
-        blk_phase<float>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
+        blk_init_ax<float, BS>(I, bvec32(I), s, beta_on, sm);
+        blk_phase<float, BS>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
         fp32_iters = s.total;
         if (!s.status) {
             /* FP64 refinement from the FP32 iterate (switch_to_fp64) */
@@ -703,8 +703,8 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
                 s.restart = 0;
             }
             __syncthreads();
-            blk_init_ax<double>(I, bvec64(I), s, beta_on, sm);
-            blk_phase<double>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
+            blk_init_ax<double, BS>(I, bvec64(I), s, beta_on, sm);
+            blk_phase<double, BS>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
         } else {
             blk_for(I.n, [&](int j) { I.xh[j] = (double)I.xhf[j]; });
             blk_for(I.m, [&](int i) { I.yh[i] = (double)I.yhf[i]; });
@@ -712,8 +712,8 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
         }
     } else {
         __syncthreads();
-        blk_init_ax<double>(I, bvec64(I), s, beta_on, sm);
-        blk_phase<double>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
+        blk_init_ax<double, BS>(I, bvec64(I), s, beta_on, sm);
+        blk_phase<double, BS>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
     }
     /* result (k_result_cols / k_result_rows) */
     {
@@ -762,11 +762,12 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
 
 /* MINB: resident blocks per SM the register allocation targets (more
  * resident instances hide more of each block's load latency). */
-template <int MINB>
+template <int MINB, int BS>
 __global__ void __launch_bounds__(kThreads, MINB) k_batch_lp(const BInst *__restrict__ insts, int count,
                                                              const int *__restrict__ order, unsigned *queue,
                                                              CpalParams p, BOpts o, BOut *outs) {
-    __shared__ BSmem sm;
+    extern __shared__ __align__(16) unsigned char batch_dyn_smem[];
+    BSmem<BS> &sm = *reinterpret_cast<BSmem<BS> *>(batch_dyn_smem);
     __shared__ CpalState s;
     __shared__ double sbuf[8 * (kThreads / 32)];
     __shared__ Red<6, 1> lacc6;
@@ -781,7 +782,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_batch_lp(const BInst *__rest
         if (q >= count) return;
         const int idx = order[q];
         const BInst &I = insts[idx];
-        blk_solve(I, p, o, outs + idx, sm, sbuf, s, &lacc6, &lacc1, sh);
+        blk_solve<BS>(I, p, o, outs + idx, sm, sbuf, s, &lacc6, &lacc1, sh);
     }
 }
 

@@ -31,6 +31,8 @@ using namespace batch;
 
 /* resident blocks per SM of the persistent launch */
 constexpr int kBatchMinBlocks = 3;
+/* nonzeros per row block of the batch plans */
+constexpr int kBatchBlockNnz = 1024;
 
 double now_sec() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -94,6 +96,8 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
     if (count <= 0) throw Error("batch_solve: count must be positive");
     if (!problems || !results) throw Error("batch_solve: missing problem or result array");
     if (P.termination_evaluation_frequency < 3) throw Error("termination_evaluation_frequency must be >= 3");
+    int bs = kBatchBlockNnz;
+    if (const char *e = getenv("PDAL_BATCH_BLOCK_NNZ")) bs = atoi(e) == 2048 ? 2048 : 1024;
     std::vector<Prepared> prep(count);
     run_threads(count, [&](int i) {
         const lp_problem_t *q = problems[i];
@@ -108,8 +112,8 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
         Prepared &p = prep[i];
         p.At = csr_transpose(m, n, q->constraint_matrix_row_pointers, q->constraint_matrix_col_indices,
                              q->constraint_matrix_values);
-        p.pa = plan_rows(m, q->constraint_matrix_row_pointers, kBS);
-        p.pat = plan_rows(n, p.At.rp.data(), kBS);
+        p.pa = plan_rows(m, q->constraint_matrix_row_pointers, bs);
+        p.pat = plan_rows(n, p.At.rp.data(), bs);
         p.cp = resolve_cpal_params(P, O, q);
     });
 
@@ -353,13 +357,23 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
     PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
     int minb = kBatchMinBlocks;
     if (const char *e = getenv("PDAL_BATCH_MINB")) minb = std::max(2, std::min(4, atoi(e)));
-    auto kern = minb == 4 ? k_batch_lp<4> : (minb == 3 ? k_batch_lp<3> : k_batch_lp<2>);
-    PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0));
+    using KernT = void (*)(const BInst *, int, const int *, unsigned *, CpalParams, BOpts, BOut *);
+    KernT kern;
+    size_t dsm;
+    if (bs == 2048) {
+        kern = minb >= 3 ? k_batch_lp<3, 2048> : k_batch_lp<2, 2048>;
+        dsm = sizeof(BSmem<2048>);
+    } else {
+        kern = minb == 4 ? k_batch_lp<4, 1024> : (minb == 3 ? k_batch_lp<3, 1024> : k_batch_lp<2, 1024>);
+        dsm = sizeof(BSmem<1024>);
+    }
+    PDAL_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+    PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, dsm));
     if (per_sm < 1) throw Error("the batch kernel does not fit on one SM");
     const int grid = std::max(1, std::min(count, per_sm * sms));
     PDAL_CUDA(cudaEventRecord(e0, stream));
-    kern<<<grid, kThreads, 0, stream>>>((const BInst *)(dev + insts_off), count, (const int *)(dev + order_off),
-                                        (unsigned *)(dev + queue_off), cp, bo, (BOut *)(dev + outs_off));
+    kern<<<grid, kThreads, dsm, stream>>>((const BInst *)(dev + insts_off), count, (const int *)(dev + order_off),
+                                          (unsigned *)(dev + queue_off), cp, bo, (BOut *)(dev + outs_off));
     PDAL_CUDA(cudaGetLastError());
     PDAL_CUDA(cudaEventRecord(e1, stream));
     PDAL_CUDA(cudaMemcpyAsync(host + out_begin, dev + out_begin, out_end - out_begin, cudaMemcpyDeviceToHost, stream));

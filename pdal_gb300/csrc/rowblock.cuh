@@ -287,37 +287,16 @@ __device__ __forceinline__ void rowblock_run_at(int blk, const RowPlanDev &plan,
         const int lid = ~d.y;
         const int4 li = plan.linfo[lid];
         const int piece = (d.z - li.w) / S;
-        /* every nonzero of a piece belongs to the same row: each thread
-         * multiplies its 4-element windows straight from registers (no
-         * shared-memory staging, no barrier before the block sum) */
+        rowblock_stage<S, NP, T>(d.z, d.w, ci, val, gat, sm);
+        __syncthreads();
         T s[NP];
 #pragma unroll
         for (int p = 0; p < NP; ++p) s[p] = T(0);
-        {
-            constexpr int MAXIT = (S / 4 + 1 + NT - 1) / NT;
-            const int kb = d.z & ~3;
-            const int nch = (d.w - kb + 3) >> 2;
+        const int lo = d.z - (d.z & ~3), hi = d.w - (d.z & ~3);
+        for (int kk = lo + tid; kk < hi; kk += NT) {
+            const T v = sm.val[kk];
 #pragma unroll
-            for (int it = 0; it < MAXIT; ++it) {
-                const int c = it * NT + tid;
-                if (c < nch) {
-                    const int kc = kb + 4 * c;
-                    int cols[4];
-                    T vals[4];
-                    load4_stream(ci + kc, cols);
-                    load4_stream(val + kc, vals);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int e = kc + q;
-                        if (e >= d.z && e < d.w) {
-                            T t[NP];
-                            gat(cols[q], t);
-#pragma unroll
-                            for (int p = 0; p < NP; ++p) s[p] = vfma(vals[q], t[p], s[p]);
-                        }
-                    }
-                }
-            }
+            for (int p = 0; p < NP; ++p) s[p] = vfma(v, sm.g[p][kk], s[p]);
         }
         block_sum_t<NP, T>(s, reinterpret_cast<T *>(sm.red));
         if (tid == 0) {

@@ -69,6 +69,9 @@ SIGMA_PROTOCOL = {"sigma_mode": 1, "sigma_adaptive": 1, "sigma_init_factor": 0.5
                   "sigma_kd": 0.0, "sigma_update_min": 1e-6, "sigma_update_max": 1e6, "lambda_factor": 2.01,
                   "al_lambda": 0.0, "restart_sufficient": 0.2, "restart_necessary": 0.8, "restart_artificial": 0.36}
 PARAMS = {"eps": 1e-6, "l_inf_ruiz_iterations": 10}
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_dual<float> launch on this
+# workload, from the ncu capture summarised in profiles/k_dual_large_lp_fp32.md
+KDUAL_NCU_TRAFFIC = 200_110_336 + 4_137_984
 
 
 def dist_env():
@@ -273,7 +276,9 @@ def run_ours(args, rank, world, local):
                     "d2h_bytes_per_step": int(re.stats["d2h_bytes"]), "s_per_step": dte / len(rese)},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                         "frac": (achieved / hbm) if achieved else None,
+                         "traffic": KDUAL_NCU_TRAFFIC if name == "k_dual<float>" else None,
+                         "traffic_unit": "bytes per launch (dram read + write, ncu)",
                          "bytes_per_launch": b, "avg_launch_ms": t_ms, "peak_source": src},
             "time_to_kkt_1e-6_small_lp": kkt,
             "clocks": clk.summary(),

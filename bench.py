@@ -249,6 +249,13 @@ def run_ours(args, rank, world, local):
         kkt[tag] = {"s": time.perf_counter() - t0, "iterations": rr.iterations, "status": rr.status,
                     "objective": rr.primal_objective}
 
+    extras = {}
+    if not args.lp_only:
+        extras["batch_4096"] = bench_batch(local, rank=rank, world=world, barrier=barrier,
+                                           max_over_ranks=max_over_ranks)
+        if rank == 0:
+            extras["fa_cp_qp"] = bench_qp(local)
+            extras["learned_warm_start"] = bench_learned(local)
     if rank == 0:
         line = {
             "metric": METRIC,
@@ -284,10 +291,7 @@ def run_ours(args, rank, world, local):
             "clocks": clk.summary(),
         }
         line["cpu_baseline"] = cpu_baseline(data, m, n, nnz)
-        if not args.lp_only:
-            line["fa_cp_qp"] = bench_qp(local)
-            line["batch_4096"] = bench_batch(local)
-            line["learned_warm_start"] = bench_learned(local)
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -325,26 +329,39 @@ def bench_qp(local):
     return out
 
 
-def bench_batch(local, count=4096):
+def bench_batch(local, count=4096, rank=0, world=1, barrier=None, max_over_ranks=None):
     """4,096 uneven LPs (m log-uniform in [50, 5000], n = m*U[2,3], 3-20
     nnz/column, planted) solved to relative KKT 1e-6 in one persistent launch,
     chosen form (FP32 phase + FP64 refinement) and FP64, against the plain FP64
     single-instance solver run instance by instance on the same GPU (timed on
-    48 evenly spaced instances, scaled to the batch)."""
+    48 evenly spaced instances, scaled to the batch).  With N ranks the
+    instances are split by an LPT assignment (no collective on the data path)
+    and the time is the maximum over ranks."""
     from pdal_gb300 import instances, lp
+    from pdal_gb300.shard import instance_weight, lpt_partition
 
     items = instances.batch_lps(count=count)
     nnz = sum(int(d.csr()[1].shape[0]) for d in items)
+    mine = lpt_partition([instance_weight(d) for d in items], world)[rank]
+    shard = [items[i] for i in mine]
     params = {"eps": 1e-6, "l_inf_ruiz_iterations": 4, "iteration_limit": 100_000}
     out = {"workload": f"{count} LPs, m log-uniform [50, 5000], n = m*U[2,3], 3-20 nnz/column",
-           "sum_nnz": nnz}
+           "sum_nnz": nnz, "sharding": f"LPT over {world} GPU(s), no collective"}
     for tag, opts in (("chosen_fp32_refine", {"precision": "fp32_refine", "device": local}),
                       ("fp64", {"device": local})):
-        res, st = lp.solve_batch(items, params, opts)
-        out[tag] = {"total_s": st["total_sec"], "kernel_s": st["kernel_sec"], "solves_per_s": st["solves_per_sec"],
+        if barrier:
+            barrier()
+        t0 = time.perf_counter()
+        res, st = lp.solve_batch(shard, params, opts)
+        wall = time.perf_counter() - t0
+        if max_over_ranks:
+            wall = max_over_ranks(wall)
+        out[tag] = {"total_s": wall, "kernel_s": st["kernel_sec"], "solves_per_s": count / wall,
                     "optimal": st["optimal"], "iterations_p50": st["iterations_p50"],
                     "iterations_p99": st["iterations_p99"], "iterations_max": st["iterations_max"],
                     "max_kkt": max(r.kkt for r in res), "grid_blocks": st["grid_blocks"]}
+    if rank != 0:
+        return out
     idx = [int(i) for i in np.linspace(0, count - 1, 48)]
     lp.solve(items[idx[0]], params, {"device": local})
     t0 = time.perf_counter()

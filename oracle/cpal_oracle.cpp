@@ -423,10 +423,51 @@ struct Solver {
         fp_last = fp;
         return rs;
     }
-    void perform_restart() { /* solver.cu:2821-3101, restart target 0 */
+    /* solver.cu:2663-2747: fixed-point score of candidate (x^, y^) against
+     * the current iterate (x, y) */
+    double restart_delta_score() {
+        std::vector<double> ddx(n), ddy(m), dp(n), pp(m);
+        for (int j = 0; j < n; ++j) ddx[j] = xh[j] - x[j];
+        for (int i = 0; i < m; ++i) ddy[i] = yh[i] - y[i];
+        spmv(At, ddy.data(), dp.data());
+        spmv(A, ddx.data(), pp.data());
+        const double pn = nrm2(ddx), dn = nrm2(ddy), axn = nrm2(pp);
+        if (sigma_mode && sigma > 0.0 && lambda_param > 0.0) {
+            const double val = sigma * (lambda_param * pn * pn - axn * axn) + dn * dn / std::fmax(sigma, 1e-16);
+            return std::sqrt(std::fmax(val, 0.0));
+        }
+        const double movement = pn * pn * pw + dn * dn / pw;
+        const double interaction = 2 * step * dot(dp, ddx);
+        const double aug = step * beta * axn * axn;
+        return std::sqrt(std::fmax(movement + interaction - aug, 0.0));
+    }
+    /* solver.cu:2749-2819 (two-point modes): restart to the Halpern iterate
+     * when its score beats the averaged point's by the margin (mode 1) or
+     * always (mode 2) */
+    int restart_target = 0;
+    void choose_restart_candidate() {
+        restart_target = 0;
+        if (O.restart_select == 0) return;
+        if (total < O.restart_select_min_iters) return;
+        const double cur = fp;
+        const double avg = restart_delta_score();
+        if (O.restart_select == 2) {
+            restart_target = 1;
+            fp = avg;
+        } else if (std::isfinite(cur)) {
+            if (std::isfinite(avg) && avg < cur && avg <= O.restart_select_margin * cur) {
+                restart_target = 1;
+                fp = avg;
+            }
+        }
+    }
+    void perform_restart() { /* solver.cu:2821-3101 */
+        const bool to_current = O.restart_select != 0 && restart_target == 1;
+        const std::vector<double> &rx = to_current ? x : xh;
+        const std::vector<double> &ry = to_current ? y : yh;
         std::vector<double> ddx(n), ddy(m);
-        for (int j = 0; j < n; ++j) ddx[j] = xh[j] - x0[j];
-        for (int i = 0; i < m; ++i) ddy[i] = yh[i] - y0[i];
+        for (int j = 0; j < n; ++j) ddx[j] = rx[j] - x0[j];
+        for (int i = 0; i < m; ++i) ddy[i] = ry[i] - y0[i];
         const double pd = nrm2(ddx), dd = nrm2(ddy);
         const double ratio = rel_d / std::fmax(rel_p, 1e-300);
         const auto &R = P->restart_params;
@@ -491,10 +532,19 @@ struct Solver {
             }
         }
         refresh_step_schedule();
-        x0 = xh;
-        x = xh;
-        y0 = yh;
-        y = yh;
+        if (to_current) { /* solver.cu:3015-3040 */
+            xbar = xh;
+            ybar = yh;
+            x0 = x;
+            xh = x;
+            y0 = y;
+            yh = y;
+        } else {
+            x0 = xh;
+            x = xh;
+            y0 = yh;
+            y = yh;
+        }
         inner = 0;
         fp_last = INFINITY;
         restarts++;
@@ -705,6 +755,7 @@ bool oracle_block(Solver &S, bool &do_restart, int &charged, double elapsed, int
     S.check_termination(elapsed);
     if (S.reason == TERMINATION_REASON_UNSPECIFIED && charged >= limit) S.reason = TERMINATION_REASON_ITERATION_LIMIT;
     if (S.reason != TERMINATION_REASON_UNSPECIFIED) return true;
+    S.choose_restart_candidate();
     do_restart = S.should_restart(F);
     if (do_restart) S.perform_restart();
     return false;

@@ -43,6 +43,12 @@ struct CpalParams {
     int lambda_param_set;
     double lambda_param_opt;
     double obj_norm, bnd_norm, obj_const;
+    /* restart target selection (LP/CP_AL/src/solver.cu:2749-2819, two-point
+     * modes): 0 off, 1 restart to the Halpern iterate when its score beats
+     * the averaged point's within the margin, 2 always */
+    int restart_select;
+    int restart_select_min_iters;
+    double restart_select_margin;
 };
 
 /* Solver scalars, resident in device memory during the loop. */
@@ -73,7 +79,7 @@ struct CpalState {
     int iter_limit;        /* iteration limit (device copy, a session may extend it) */
     int fp32_stall_limit;  /* evaluations without a 2x KKT gain that end the FP32 phase */
     int fp32_stall;        /* evaluations since the FP32 phase last halved its best KKT */
-    int pad2_;
+    int restart_target; /* 1: the last restart went to the Halpern iterate */
     double fp32_best_kkt;
 };
 
@@ -83,6 +89,10 @@ struct CpalEval {
     double rp2, contrib, adx2, dy2, ddy2, axd2, rpmax;
     /* rows of A^T */
     double rd2, dx2, cross, cx, lx, ddx2, rdmax;
+    /* restart target selection only: |A(x^ - x)|^2, |y^ - y|^2, |x^ - x|^2,
+     * <A^T(y^ - y), x^ - x>, and the distances of the Halpern iterate from
+     * the anchors |x - x0|^2, |y - y0|^2, |A x - A x0|^2 */
+    double sel_ax2, sel_dy2, sel_dx2, sel_cross, cur_dx2, cur_dy2, cur_axd2;
 };
 
 PDAL_HD void cpal_set_coefficients(CpalState &s) {
@@ -298,13 +308,32 @@ PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval
         s.status = 5; /* TERMINATION_REASON_TIME_LIMIT */
         return true;
     }
+    /* LP/CP_AL/src/solver.cu:2749-2819: the averaged point's score against
+     * the Halpern iterate, the same formula as the fixed-point error */
+    s.restart_target = 0;
+    if (p.restart_select != 0 && s.total >= p.restart_select_min_iters) {
+        const double cur = s.fp;
+        const double avg = cpal_fixed_point_error(s, e.sel_dx2, e.sel_dy2, e.sel_ax2, e.sel_cross);
+        if (p.restart_select == 2) {
+            s.restart_target = 1;
+            s.fp = avg;
+        } else if (isfinite(cur) && isfinite(avg) && avg < cur && avg <= p.restart_select_margin * cur) {
+            s.restart_target = 1;
+            s.fp = avg;
+        }
+    }
     if (cpal_should_restart(s, p)) {
-        cpal_restart_scalars(s, p, e.ddx2, e.ddy2, e.axd2);
+        const bool to_current = s.restart_target == 1;
+        cpal_restart_scalars(s, p, to_current ? e.cur_dx2 : e.ddx2, to_current ? e.cur_dy2 : e.ddy2,
+                             to_current ? e.cur_axd2 : e.axd2);
         s.restart = 1;
         /* the reference recomputes the fixed-point error of the unchanged
          * iterates with the new coefficients at the start of the next block
-         * (solver.cu:1279-1284) */
-        s.fp0 = cpal_fixed_point_error(s, e.dx2, e.dy2, e.adx2, e.cross);
+         * (solver.cu:1279-1284); a restart to the Halpern iterate first sets
+         * x-bar = x^ and x^ = x (solver.cu:3015-3040), so the deltas are then
+         * x^ - x */
+        s.fp0 = to_current ? cpal_fixed_point_error(s, e.sel_dx2, e.sel_dy2, e.sel_ax2, e.sel_cross)
+                           : cpal_fixed_point_error(s, e.dx2, e.dy2, e.adx2, e.cross);
     }
     cpal_set_coefficients(s);
     return false;

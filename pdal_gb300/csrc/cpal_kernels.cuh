@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(kThreads) k_init_ax(RowPlanDev plan, const int
 /* ------------------------------------------------------------------ */
 /* evaluation                                                          */
 /* ------------------------------------------------------------------ */
-constexpr int kEvalStride = 8; /* doubles per partial slot */
+constexpr int kEvalStride = 12; /* doubles per partial slot: 6 sums, the maximum, up to 4 extra sums */
 
 /* rows of A: p^ = A x^, A dx, A (x^ - x0); primal residual, dual-objective
  * contribution, |A dx|^2, |dy|^2, |y^ - y0|^2, |A(x^ - x0)|^2. */
@@ -292,12 +292,15 @@ struct EvalRowArgs {
     double *phat;
     double *part; /* (nblocks + nlong) * kEvalStride */
     int nblocks;
+    const T *x, *y, *ax; /* restart target selection: the Halpern iterate and its tracked A x */
 };
 
-template <typename T>
+/* SEL (restart target selection on): also A(x^ - x), |y^ - y|^2, |y - y0|^2
+ * and |A x - A x0|^2 in extra sums 6..9 (slot indices 7..10). */
+template <typename T, bool SEL = false>
 struct EvalRowEpi {
     EvalRowArgs<T> a;
-    __device__ __forceinline__ void operator()(int i, const double *s, Red<6, 1> &r) const {
+    __device__ __forceinline__ void operator()(int i, const double *s, Red<SEL ? 10 : 6, 1> &r) const {
         const double ph = s[0];
         a.phat[i] = ph;
         const double cl = fmax(a.clb[i], fmin(ph, a.cub[i]));
@@ -312,39 +315,52 @@ struct EvalRowEpi {
         const double ddy = yhi - a.y0[i];
         r.s[4] += ddy * ddy;
         r.s[5] += s[2] * s[2];
+        if (SEL) {
+            r.s[SEL ? 6 : 0] += s[SEL ? 3 : 0] * s[SEL ? 3 : 0];
+            const double yc = (double)a.y[i];
+            const double d1 = yhi - yc, d2 = yc - a.y0[i], d3 = (double)a.ax[i] - a.ax0[i];
+            r.s[SEL ? 7 : 0] += d1 * d1;
+            r.s[SEL ? 8 : 0] += d2 * d2;
+            r.s[SEL ? 9 : 0] += d3 * d3;
+        }
     }
-    __device__ __forceinline__ void long_red(int lid, Red<6, 1> &r) const {
+    __device__ __forceinline__ void long_red(int lid, Red<SEL ? 10 : 6, 1> &r) const {
         double *d = a.part + (size_t)(a.nblocks + lid) * kEvalStride;
         for (int q = 0; q < 6; ++q) d[q] = r.s[q];
         d[6] = r.mx[0];
+        for (int q = 6; q < (SEL ? 10 : 6); ++q) d[q + 1] = r.s[q];
     }
 };
 
-template <typename T, int S>
+template <typename T, int S, bool SEL = false>
 __global__ void __launch_bounds__(kThreads) k_eval_rows(RowPlanDev plan, const int *__restrict__ rp,
                                                         const int *__restrict__ ci, const double *__restrict__ val,
                                                         EvalRowArgs<T> a, const CpalState *__restrict__ st) {
     if (st->status) return;
-    __shared__ RowBlockSmem<S, 3, double> sm;
-    EvalRowEpi<T> epi;
+    constexpr int NP = SEL ? 4 : 3, NS = SEL ? 10 : 6;
+    __shared__ RowBlockSmem<S, NP, double> sm;
+    EvalRowEpi<T, SEL> epi;
     epi.a = a;
     const T *xh = a.xh;
     const T *xb = a.xbar;
+    const T *xc = a.x;
     const double *x0 = a.x0;
     auto g = [&](int c, double *out) {
         const double xhc = (double)xh[c];
         out[0] = xhc;
         out[1] = (double)xb[c] - xhc;
         out[2] = xhc - x0[c];
+        if (SEL) out[SEL ? 3 : 0] = xhc - (double)xc[c];
     };
-    Red<6, 1> red;
+    Red<NS, 1> red;
     red.zero();
-    rowblock_run<S, 3, double>(plan, rp, ci, val, g, epi, red, sm);
-    block_reduce<kThreads, 6, 1>(red, sm.red);
+    rowblock_run<S, NP, double>(plan, rp, ci, val, g, epi, red, sm);
+    block_reduce<kThreads, NS, 1>(red, sm.red);
     if (threadIdx.x == 0) {
         double *d = a.part + (size_t)blockIdx.x * kEvalStride;
         for (int q = 0; q < 6; ++q) d[q] = red.s[q];
         d[6] = red.mx[0];
+        for (int q = 6; q < NS; ++q) d[q + 1] = red.s[q];
     }
 }
 
@@ -356,12 +372,15 @@ struct EvalColArgs {
     const double *x0, *c, *cscale;
     double *part;
     int nblocks;
+    const T *x, *y; /* restart target selection: the Halpern iterate */
 };
 
-template <typename T>
+/* SEL: also <A^T(y^ - y), x^ - x>, |x^ - x|^2 and |x - x0|^2 in extra sums
+ * 6..8 (slot indices 7..9). */
+template <typename T, bool SEL = false>
 struct EvalColEpi {
     EvalColArgs<T> a;
-    __device__ __forceinline__ void operator()(int j, const double *s, Red<6, 1> &r) const {
+    __device__ __forceinline__ void operator()(int j, const double *s, Red<SEL ? 9 : 6, 1> &r) const {
         const double xhj = (double)a.xh[j];
         const double lj = (double)a.lam[j];
         const double cj = a.c[j];
@@ -375,57 +394,70 @@ struct EvalColEpi {
         r.s[4] += lj * xhj;
         const double ddx = xhj - a.x0[j];
         r.s[5] += ddx * ddx;
+        if (SEL) {
+            const double xc = (double)a.x[j];
+            const double d1 = xhj - xc, d2 = xc - a.x0[j];
+            r.s[SEL ? 6 : 0] += s[SEL ? 2 : 0] * d1;
+            r.s[SEL ? 7 : 0] += d1 * d1;
+            r.s[SEL ? 8 : 0] += d2 * d2;
+        }
     }
-    __device__ __forceinline__ void long_red(int lid, Red<6, 1> &r) const {
+    __device__ __forceinline__ void long_red(int lid, Red<SEL ? 9 : 6, 1> &r) const {
         double *d = a.part + (size_t)(a.nblocks + lid) * kEvalStride;
         for (int q = 0; q < 6; ++q) d[q] = r.s[q];
         d[6] = r.mx[0];
+        for (int q = 6; q < (SEL ? 9 : 6); ++q) d[q + 1] = r.s[q];
     }
 };
 
-template <typename T, int S>
+template <typename T, int S, bool SEL = false>
 __global__ void __launch_bounds__(kThreads) k_eval_cols(RowPlanDev plan, const int *__restrict__ rp,
                                                         const int *__restrict__ ci, const double *__restrict__ val,
                                                         EvalColArgs<T> a, const CpalState *__restrict__ st) {
     if (st->status) return;
-    __shared__ RowBlockSmem<S, 2, double> sm;
-    EvalColEpi<T> epi;
+    constexpr int NP = SEL ? 3 : 2, NS = SEL ? 9 : 6;
+    __shared__ RowBlockSmem<S, NP, double> sm;
+    EvalColEpi<T, SEL> epi;
     epi.a = a;
     const T *yh = a.yh;
     const T *yb = a.ybar;
+    const T *yc = a.y;
     auto g = [&](int c, double *out) {
         const double yhc = (double)yh[c];
         out[0] = yhc;
         out[1] = (double)yb[c] - yhc;
+        if (SEL) out[SEL ? 2 : 0] = yhc - (double)yc[c];
     };
-    Red<6, 1> red;
+    Red<NS, 1> red;
     red.zero();
-    rowblock_run<S, 2, double>(plan, rp, ci, val, g, epi, red, sm);
-    block_reduce<kThreads, 6, 1>(red, sm.red);
+    rowblock_run<S, NP, double>(plan, rp, ci, val, g, epi, red, sm);
+    block_reduce<kThreads, NS, 1>(red, sm.red);
     if (threadIdx.x == 0) {
         double *d = a.part + (size_t)blockIdx.x * kEvalStride;
         for (int q = 0; q < 6; ++q) d[q] = red.s[q];
         d[6] = red.mx[0];
+        for (int q = 6; q < NS; ++q) d[q + 1] = red.s[q];
     }
 }
 
 /* Sums the partial slots of one evaluation kernel in a fixed order. */
-__device__ __forceinline__ void reduce_slots(const double *part, int nslots, Red<6, 1> &r, double *sbuf) {
+__device__ __forceinline__ void reduce_slots(const double *part, int nslots, Red<10, 1> &r, double *sbuf) {
     r.zero();
     for (int b = threadIdx.x; b < nslots; b += kThreads) {
         const double *d = part + (size_t)b * kEvalStride;
         for (int q = 0; q < 6; ++q) r.s[q] += d[q];
         r.mx[0] = fmax(r.mx[0], d[6]);
+        for (int q = 6; q < 10; ++q) r.s[q] += d[q + 1];
     }
-    block_reduce<kThreads, 6, 1>(r, sbuf);
+    block_reduce<kThreads, 10, 1>(r, sbuf);
 }
 
 static __global__ void __launch_bounds__(kThreads) k_control(const double *__restrict__ prow, int nrow_slots,
                                                       const double *__restrict__ pcol, int ncol_slots,
                                                       CpalState *st, CpalParams p, HalpernW *wt, HalpernWf *wtf) {
     if (st->status) return;
-    __shared__ double sbuf[8 * (kThreads / 32)];
-    Red<6, 1> r1, r2;
+    __shared__ double sbuf[11 * (kThreads / 32)];
+    Red<10, 1> r1, r2;
     reduce_slots(prow, nrow_slots, r1, sbuf);
     reduce_slots(pcol, ncol_slots, r2, sbuf);
     if (threadIdx.x == 0) {
@@ -444,6 +476,13 @@ static __global__ void __launch_bounds__(kThreads) k_control(const double *__res
         e.lx = r2.s[4];
         e.ddx2 = r2.s[5];
         e.rdmax = r2.mx[0];
+        e.sel_ax2 = r1.s[6];
+        e.sel_dy2 = r1.s[7];
+        e.cur_dy2 = r1.s[8];
+        e.cur_axd2 = r1.s[9];
+        e.sel_cross = r2.s[6];
+        e.sel_dx2 = r2.s[7];
+        e.cur_dx2 = r2.s[8];
         CpalState s = *st;
         s.elapsed = (double)(globaltimer_ns() - s.t_start_ns) * 1e-9;
         cpal_end_of_block(s, p, e);
@@ -459,14 +498,43 @@ static __global__ void __launch_bounds__(kThreads) k_control(const double *__res
  * and the next predictor from the new beta.  The FP64 anchors are written
  * together with the (hi, lo) copies the FP32 phase reads. */
 template <typename T, bool BETA>
-__global__ void k_restart(const CpalState *__restrict__ st, int n, int m, const T *__restrict__ xh, T *x,
-                          double *x0, float2 *x0f, const T *__restrict__ yh, T *y, double *y0, float2 *y0f,
-                          const double *__restrict__ phat, T *ax, double *ax0, float2 *ax0f, T *u,
-                          const T *__restrict__ lb, const T *__restrict__ ub) {
+__global__ void k_restart(const CpalState *__restrict__ st, int n, int m, const T *xh, T *x, double *x0,
+                          float2 *x0f, const T *yh, T *y, double *y0, float2 *y0f, const double *__restrict__ phat,
+                          T *ax, double *ax0, float2 *ax0f, T *u, const T *__restrict__ lb,
+                          const T *__restrict__ ub, T *xbar, T *ybar) {
     if (st->status || !st->restart) return;
     Coefs<T> k;
     load_coefs(st, k);
     const int total = n > m ? n : m;
+    if (st->restart_target == 1) {
+        /* restart to the Halpern iterate (LP/CP_AL/src/solver.cu:3015-3040):
+         * x-bar = x^, x^ = x, x0 = x; the same for y; A x0 = the tracked A x */
+        T *xh_w = const_cast<T *>(xh), *yh_w = const_cast<T *>(yh);
+        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+            if (t < n) {
+                const T v = x[t];
+                xbar[t] = xh_w[t];
+                xh_w[t] = v;
+                x0[t] = (double)v;
+                if (x0f) x0f[t] = split_anchor((double)v);
+            }
+            if (t < m) {
+                const T v = y[t];
+                ybar[t] = yh_w[t];
+                yh_w[t] = v;
+                y0[t] = (double)v;
+                if (y0f) y0f[t] = split_anchor((double)v);
+                const T axv = ax[t];
+                ax0[t] = (double)axv;
+                if (ax0f) ax0f[t] = split_anchor((double)axv);
+                if (BETA) {
+                    const T z = vmax(lb[t], vmin(axv - v * k.inv_beta, ub[t]));
+                    u[t] = v - k.beta * (axv - z);
+                }
+            }
+        }
+        return;
+    }
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         if (t < n) {
             const T v = xh[t];

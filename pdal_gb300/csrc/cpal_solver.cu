@@ -257,6 +257,11 @@ CpalParams resolve_cpal_params(const cp_al_parameters_t &P, const cp_al_gb300_op
     cp.lambda_factor = O.lambda_factor;
     cp.lambda_param_set = O.lambda_param_set;
     cp.lambda_param_opt = O.lambda_param;
+    cp.restart_select = O.restart_select;
+    cp.restart_select_min_iters = O.restart_select_min_iters;
+    cp.restart_select_margin = O.restart_select_margin;
+    if (O.restart_select < 0 || O.restart_select > 2 || O.restart_select_threepoint)
+        throw Error("restart_select supports the two-point modes 0, 1 and 2 (the three-point mode is not built)");
     cp.obj_const = prob->objective_constant;
     const int n = prob->num_variables, m = prob->num_constraints;
     const bool linf = cp.norm_linf;
@@ -774,13 +779,23 @@ template <typename T>
 void CpalSolver::launch_eval() {
     auto &v = vecs<T>();
     EvalRowArgs<T> ra{v.xh, v.xbar, v.yh, v.ybar, x0_, y0_, ax0_, clb_, cub_, clbf_, cubf_, rsc_, phat_, part_row_,
-                      A_.ev.d.nblocks};
-    EvalColArgs<T> ca{v.xh, v.xbar, v.yh, v.ybar, v.lam, x0_, c_, dsc_, part_col_, At_.ev.d.nblocks};
-    PDAL_WITH_SE(S_ev_, {
-        if (m_ > 0)
-            k_eval_rows<T, SE><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, ra, st_);
-        k_eval_cols<T, SE><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, ca, st_);
-    });
+                      A_.ev.d.nblocks, v.x, v.y, v.ax};
+    EvalColArgs<T> ca{v.xh, v.xbar, v.yh, v.ybar, v.lam, x0_, c_, dsc_, part_col_, At_.ev.d.nblocks, v.x, v.y};
+    if (cp_.restart_select) {
+        PDAL_WITH_SE(S_ev_, {
+            if (m_ > 0)
+                k_eval_rows<T, SE, true>
+                    <<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, ra, st_);
+            k_eval_cols<T, SE, true>
+                <<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, ca, st_);
+        });
+    } else {
+        PDAL_WITH_SE(S_ev_, {
+            if (m_ > 0)
+                k_eval_rows<T, SE><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, ra, st_);
+            k_eval_cols<T, SE><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, ca, st_);
+        });
+    }
     const int nrow_slots = m_ > 0 ? A_.ev.d.nblocks + A_.ev.d.nlong : 0;
     k_control<<<1, kThreads, 0, stream_>>>(part_row_, nrow_slots, part_col_, At_.ev.d.nblocks + At_.ev.d.nlong, st_,
                                            cp_, wt_, wtf_);
@@ -789,10 +804,10 @@ void CpalSolver::launch_eval() {
     float2 *x0f = f32 ? x0f_ : nullptr, *y0f = f32 ? y0f_ : nullptr, *ax0f = f32 ? ax0f_ : nullptr;
     if (beta_on_)
         k_restart<T, true><<<gr, kThreads, 0, stream_>>>(st_, n_, m_, v.xh, v.x, x0_, x0f, v.yh, v.y, y0_, y0f, phat_,
-                                                         v.ax, ax0_, ax0f, v.u, v.clb, v.cub);
+                                                         v.ax, ax0_, ax0f, v.u, v.clb, v.cub, v.xbar, v.ybar);
     else
         k_restart<T, false><<<gr, kThreads, 0, stream_>>>(st_, n_, m_, v.xh, v.x, x0_, x0f, v.yh, v.y, y0_, y0f,
-                                                          phat_, v.ax, ax0_, ax0f, v.u, v.clb, v.cub);
+                                                          phat_, v.ax, ax0_, ax0f, v.u, v.clb, v.cub, v.xbar, v.ybar);
 }
 
 template <typename T>

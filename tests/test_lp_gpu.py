@@ -200,3 +200,23 @@ def test_badly_scaled_zipf_iterates_match(lp_lib, iters):
     for a, b in ((g.x, o.x), (g.y, o.y)):
         err = np.abs(a - b).max() / (1 + np.abs(b).max())
         assert err < 1e-8, err
+
+
+@pytest.mark.parametrize("options", [
+    {"restart_select": 1},
+    {"restart_select": 2},
+    {"restart_select": 1, "sigma_mode": 1, "sigma_init_factor": 0.5, "al_lambda": 0.0, "sigma_kp": 0.5,
+     "sigma_ki": 0.0, "sigma_kd": 0.0, "sigma_balance_gain": 0.0, "restart_necessary": 0.8},
+], ids=["select1", "select2", "select1_sigma"])
+def test_restart_target_selection_parity(lp_lib, options):
+    """Restart to the Halpern iterate when its score wins (A13): iterates after
+    fixed blocks and the full solve match the oracle."""
+    d = I.random_lp(300, 700, 6, seed=21)
+    p = {"eps": 1e-14, "iteration_limit": 1600, "l_inf_ruiz_iterations": 4}
+    g, o = both(d, p, options)
+    assert g.iterations == o.iterations
+    assert np.abs(g.x - o.x).max() / (1 + np.abs(o.x).max()) < 1e-8
+    assert np.abs(g.y - o.y).max() / (1 + np.abs(o.y).max()) < 1e-8
+    g, o = both(d, {"eps": 1e-8, "l_inf_ruiz_iterations": 4}, options)
+    assert g.status == "OPTIMAL"
+    assert_parity(g, o)

@@ -46,6 +46,11 @@ typedef struct {
     double primal_weight;
     double step_size;
     double device_loop_ms;     /* device time of the iteration segments (CUDA events) */
+    double equilibration_sec;  /* host equilibration */
+    double upload_sec;         /* plans, transposes, device arena and copies */
+    double power_sec;          /* power iterations (sigma_max(A), eigenvalues of Q) */
+    int power_iterations_a;
+    int power_iterations_q;
 } fa_cp_gb300_stats_t;
 
 /* Defaults: current device, automatic grid and block budget, restart to the

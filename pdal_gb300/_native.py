@@ -447,6 +447,11 @@ class FacpStats(C.Structure):
         ("primal_weight", C.c_double),
         ("step_size", C.c_double),
         ("device_loop_ms", C.c_double),
+        ("equilibration_sec", C.c_double),
+        ("upload_sec", C.c_double),
+        ("power_sec", C.c_double),
+        ("power_iterations_a", C.c_int),
+        ("power_iterations_q", C.c_int),
     ]
 
 

@@ -259,7 +259,8 @@ class FacpSolver {
     std::vector<double> diag_;
     double qnorm_ = 0.0, nonconvexity_ = 0.0;
     double sv_max_ = 0.0;
-    double setup_sec_ = 0.0, rescale_sec_ = 0.0;
+    double setup_sec_ = 0.0, rescale_sec_ = 0.0, upload_sec_ = 0.0, power_sec_ = 0.0;
+    int power_iters_a_ = 0, power_iters_q_ = 0;
     long long launches_ = 0;
     float dev_ms_ = 0.f;
 
@@ -535,6 +536,7 @@ void FacpSolver::power_iterations() {
         launch(base_args(MODE_POWER_QMAX));
         read_ctl();
         qnorm_ = ctl_.power_value;
+        power_iters_q_ += ctl_.power_iters;
         for (double &x : v) x = (double)rnd.next() / CRandom::kMax;
         PDAL_CUDA(cudaMemcpyAsync(P_.pv, v.data(), H.n * 8, cudaMemcpyHostToDevice, stream_));
         Args a = base_args(MODE_POWER_QMIN);
@@ -542,6 +544,7 @@ void FacpSolver::power_iterations() {
         launch(a);
         read_ctl();
         nonconvexity_ = ctl_.power_value;
+        power_iters_q_ += ctl_.power_iters;
     }
     if (M_[MAT_A].h.nnz() == 0) { /* fa_cp_core_op.cu:1022-1040 */
         step_ = 1.0;
@@ -554,6 +557,7 @@ void FacpSolver::power_iterations() {
         launch(base_args(MODE_POWER_A));
         read_ctl();
         sv_max_ = ctl_.power_value;
+        power_iters_a_ = ctl_.power_iters;
         step_ = 0.998 / sv_max_;
     }
     pw_ = p_.bound_objective_rescaling ? 1.0 : (H.obj_norm + 1.0) / (H.bnd_norm + 1.0);
@@ -785,13 +789,17 @@ void FacpSolver::print_eval() const {
 fa_cp_result_t *FacpSolver::run() {
     const double t_begin = now_sec();
     prepare();
+    const double t_up = now_sec();
     upload();
+    upload_sec_ = now_sec() - t_up;
     /* solver state */
     al_available_ = p_.use_al_qp;
     use_al_ = p_.use_al_qp;
     al_sigma_ = p_.al_sigma;
     best_al_sigma_ = p_.al_sigma;
+    const double t_pow = now_sec();
     power_iterations();
+    power_sec_ = now_sec() - t_pow;
     if (al_available_ && p_.al_sigma <= p_.sigma_zero_threshold) {
         use_al_ = false;
         al_sigma_ = 0.0;
@@ -927,6 +935,11 @@ fa_cp_result_t *FacpSolver::run() {
     st.primal_weight = pw_;
     st.step_size = step_;
     st.device_loop_ms = dev_ms_;
+    st.equilibration_sec = rescale_sec_;
+    st.upload_sec = upload_sec_;
+    st.power_sec = power_sec_;
+    st.power_iterations_a = power_iters_a_;
+    st.power_iterations_q = power_iters_q_;
     if (p_.verbose >= 1)
         printf("[fa_cp_gb300] %s after %d iterations (%lld inner), objective %.10e, rel. KKT %.2e, %.3f s\n",
                reason_ == TERMINATION_REASON_OPTIMAL ? "optimal" : "stopped", total_, (long long)ctl_.inner_total,

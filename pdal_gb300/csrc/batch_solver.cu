@@ -30,9 +30,10 @@ namespace {
 using namespace batch;
 
 /* resident blocks per SM of the persistent launch */
-constexpr int kBatchMinBlocks = 3;
-/* nonzeros per row block of the batch plans */
-constexpr int kBatchBlockNnz = 1024;
+constexpr int kBatchMinBlocks = 2;
+/* nonzeros per row block of the batch plans (measured on the 4,096-LP batch:
+ * 2,048 nonzeros with 2 resident blocks per SM beat 1,024 with 2-4) */
+constexpr int kBatchBlockNnz = 2048;
 
 double now_sec() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -362,7 +363,7 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
     KernT kern;
     size_t dsm;
     if (bs == 2048) {
-        kern = minb >= 3 ? k_batch_lp<3, 2048> : k_batch_lp<2, 2048>;
+        kern = minb >= 3 ? k_batch_lp<3, 2048> : k_batch_lp<2, 2048>;  /* 3: ~70 KB of staging each */
         dsm = sizeof(BSmem<2048>);
     } else {
         kern = minb == 4 ? k_batch_lp<4, 1024> : (minb == 3 ? k_batch_lp<3, 1024> : k_batch_lp<2, 1024>);

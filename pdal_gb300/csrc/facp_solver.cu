@@ -23,6 +23,7 @@
 #include <cstring>
 #include <random>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace pdal {
@@ -96,10 +97,48 @@ HostCsr from_component(const CsrComponent *cc, int rows, int cols, int nnz, cons
 }
 
 /* ---------------------------------------------------------------- equilibration
- * QP/FA_CP/src/preconditioner.c:92-331 on the host: Ruiz passes (columns see
- * A and Q), one Pock-Chambolle pass, then bound/objective scaling that also
- * rescales Q by ovr/cbr and R by sqrt(ovr/cbr). */
-void scale_problem(HostQP &P, const std::vector<double> &r, const std::vector<double> &d) {
+ * QP/FA_CP/src/preconditioner.c:92-331: Ruiz passes (columns see A and Q),
+ * one Pock-Chambolle pass, then bound/objective scaling that also rescales Q
+ * by ovr/cbr and R by sqrt(ovr/cbr).
+ *
+ * Run on host threads over rows: column statistics come from the rows of the
+ * transposes A' and Q', which hold each column's entries in increasing row
+ * order -- the order the reference's row-major scatter visits them -- and
+ * every transpose value is scaled by the same expression as its original, so
+ * the results are bit-identical to the serial loops. */
+template <class F>
+void parallel_rows(int rows, F f) {
+    const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 32));
+    if (rows < 4096 || nt == 1) {
+        f(0, rows);
+        return;
+    }
+    std::vector<std::thread> th;
+    const int chunk = (rows + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t) {
+        const int r0 = t * chunk, r1 = std::min(rows, r0 + chunk);
+        if (r0 < r1) th.emplace_back([=]() { f(r0, r1); });
+    }
+    for (auto &x : th) x.join();
+}
+
+void scale_matrix(HostCsr &M, const std::vector<double> &row_s, const std::vector<double> &col_s) {
+    parallel_rows(M.nr, [&](int r0, int r1) {
+        for (int row = r0; row < r1; ++row)
+            for (int k = M.rp[row]; k < M.rp[row + 1]; ++k) M.v[k] /= (row_s[row] * col_s[M.ci[k]]);
+    });
+}
+
+/* the transpose's row `row` is column `row` of the original: scaled by
+ * (orig_row_scale * col_scale) in the original's operand order */
+void scale_transpose(HostCsr &T, const std::vector<double> &orig_row_s, const std::vector<double> &orig_col_s) {
+    parallel_rows(T.nr, [&](int r0, int r1) {
+        for (int row = r0; row < r1; ++row)
+            for (int k = T.rp[row]; k < T.rp[row + 1]; ++k) T.v[k] /= (orig_row_s[T.ci[k]] * orig_col_s[row]);
+    });
+}
+
+void scale_problem(HostQP &P, HostCsr &At, HostCsr &Qt, const std::vector<double> &r, const std::vector<double> &d) {
     for (int i = 0; i < P.n; ++i) {
         P.c[i] /= d[i];
         P.vub[i] *= d[i];
@@ -109,54 +148,55 @@ void scale_problem(HostQP &P, const std::vector<double> &r, const std::vector<do
         P.clb[i] /= r[i];
         P.cub[i] /= r[i];
     }
-    for (int row = 0; row < P.m; ++row)
-        for (int k = P.A.rp[row]; k < P.A.rp[row + 1]; ++k) P.A.v[k] /= (r[row] * d[P.A.ci[k]]);
-    for (int row = 0; row < P.n; ++row)
-        for (int k = P.Q.rp[row]; k < P.Q.rp[row + 1]; ++k) P.Q.v[k] /= (d[row] * d[P.Q.ci[k]]);
+    scale_matrix(P.A, r, d);
+    scale_transpose(At, r, d);
+    scale_matrix(P.Q, d, d);
+    scale_transpose(Qt, d, d);
     if (P.R.nnz() > 0)
         for (int row = 0; row < P.nr; ++row)
             for (int k = P.R.rp[row]; k < P.R.rp[row + 1]; ++k) P.R.v[k] /= d[P.R.ci[k]];
 }
 
-void equilibrate(HostQP &P, const fa_cp_parameters_t &prm) {
+/* per-row statistic of the rows of M (abs max, or sum of |a|^deg in order) */
+void row_stat(const HostCsr &M, int mode, double deg, std::vector<double> &out, bool accumulate) {
+    parallel_rows(M.nr, [&](int r0, int r1) {
+        for (int row = r0; row < r1; ++row) {
+            double acc = accumulate ? out[row] : 0.0;
+            for (int k = M.rp[row]; k < M.rp[row + 1]; ++k) {
+                const double v = std::fabs(M.v[k]);
+                if (mode == 0) {
+                    if (v > acc) acc = v;
+                } else {
+                    acc += std::pow(v, deg);
+                }
+            }
+            out[row] = acc;
+        }
+    });
+}
+
+void equilibrate(HostQP &P, HostCsr &At, HostCsr &Qt, const fa_cp_parameters_t &prm) {
     P.dcum.assign(P.n, 1.0);
     P.rcum.assign(P.m, 1.0);
     std::vector<double> cr(P.m), vr(P.n);
     auto finish = [&]() {
         for (int i = 0; i < P.n; ++i) vr[i] = (vr[i] < 1e-12) ? 1.0 : std::sqrt(vr[i]);
         for (int i = 0; i < P.m; ++i) cr[i] = (cr[i] < 1e-12) ? 1.0 : std::sqrt(cr[i]);
-        scale_problem(P, cr, vr);
+        scale_problem(P, At, Qt, cr, vr);
         for (int i = 0; i < P.n; ++i) P.dcum[i] *= vr[i];
         for (int i = 0; i < P.m; ++i) P.rcum[i] *= cr[i];
     };
     for (int it = 0; it < prm.l_inf_ruiz_iterations; ++it) {
-        std::fill(vr.begin(), vr.end(), 0.0);
-        std::fill(cr.begin(), cr.end(), 0.0);
-        for (int row = 0; row < P.m; ++row)
-            for (int k = P.A.rp[row]; k < P.A.rp[row + 1]; ++k) {
-                const double v = std::fabs(P.A.v[k]);
-                if (v > vr[P.A.ci[k]]) vr[P.A.ci[k]] = v;
-                if (v > cr[row]) cr[row] = v;
-            }
-        for (int row = 0; row < P.n; ++row)
-            for (int k = P.Q.rp[row]; k < P.Q.rp[row + 1]; ++k) {
-                const double v = std::fabs(P.Q.v[k]);
-                if (v > vr[P.Q.ci[k]]) vr[P.Q.ci[k]] = v;
-            }
+        row_stat(P.A, 0, 0.0, cr, false);
+        row_stat(At, 0, 0.0, vr, false);
+        row_stat(Qt, 0, 0.0, vr, true);
         finish();
     }
     if (prm.has_pock_chambolle_alpha) {
         const double a = prm.pock_chambolle_alpha;
-        std::fill(vr.begin(), vr.end(), 0.0);
-        std::fill(cr.begin(), cr.end(), 0.0);
-        for (int row = 0; row < P.m; ++row)
-            for (int k = P.A.rp[row]; k < P.A.rp[row + 1]; ++k) {
-                const double v = std::fabs(P.A.v[k]);
-                vr[P.A.ci[k]] += std::pow(v, 2.0 - a);
-                cr[row] += std::pow(v, a);
-            }
-        for (int row = 0; row < P.n; ++row)
-            for (int k = P.Q.rp[row]; k < P.Q.rp[row + 1]; ++k) vr[P.Q.ci[k]] += std::pow(std::fabs(P.Q.v[k]), 2.0 - a);
+        row_stat(P.A, 1, a, cr, false);
+        row_stat(At, 1, 2.0 - a, vr, false);
+        row_stat(Qt, 1, 2.0 - a, vr, true);
         finish();
     }
     if (prm.bound_objective_rescaling) {
@@ -328,7 +368,9 @@ void FacpSolver::prepare() {
         P.bnd_norm = linf ? mx : std::sqrt(s);
     }
     const double t0 = now_sec();
-    equilibrate(P, p_);
+    HostCsr At = csr_transpose(P.m, P.n, P.A.rp.data(), P.A.ci.data(), P.A.v.data());
+    HostCsr Qt = csr_transpose(P.n, P.n, P.Q.rp.data(), P.Q.ci.data(), P.Q.v.data());
+    equilibrate(P, At, Qt, p_);
     rescale_sec_ = now_sec() - t0;
     qtype_ = detect_q_type(P.Q, P.R);
     if (qtype_ == Q_DIAG) { /* solver_state.cu:252-270, 478-492 */
@@ -345,7 +387,7 @@ void FacpSolver::prepare() {
         nonconvexity_ = mn;
     }
     M_[MAT_A].h = P.A;
-    M_[MAT_AT].h = csr_transpose(P.m, P.n, P.A.rp.data(), P.A.ci.data(), P.A.v.data());
+    M_[MAT_AT].h = std::move(At);
     M_[MAT_Q].h = P.Q;
     M_[MAT_R].h = P.R;
     M_[MAT_RT].h = csr_transpose(P.nr, P.n, P.R.rp.data(), P.R.ci.data(), P.R.v.data());

@@ -143,9 +143,27 @@ def peaks():
 
 def run_profile(args, local):
     """Only the chosen-form iteration steps on the large LP (no other
-    sections): the command the ncu captures in profiles/ run."""
+    sections): the command the ncu captures in profiles/ run.  With
+    --profile-section qp: 300 iterations of the full-size QP (one persistent
+    k_facp launch per evaluation segment); batch: one k_batch_lp launch over
+    304 small LPs (m log-uniform in [50, 400]), chosen form."""
     from pdal_gb300 import instances, lp
 
+    if args.profile_section == "qp":
+        from pdal_gb300 import qp
+
+        qd, _, _ = instances.planted_qp()
+        r = qp.solve(qd, {"eps": 1e-12, "verbose": 0, "iteration_limit": 300}, {"device": local})
+        print(json.dumps({"profile_run": "qp", "iterations": r.iterations, "inner_iterations": r.inner_iterations,
+                          "kernel_launches": r.stats["kernel_launches"]}), flush=True)
+        return
+    if args.profile_section == "batch":
+        items = instances.batch_lps(count=304, seed=3100, m_range=(50, 400))
+        res, st = lp.solve_batch(items, {"eps": 1e-6, "l_inf_ruiz_iterations": 4, "iteration_limit": 100_000},
+                                 {"precision": "fp32_refine", "device": local})
+        print(json.dumps({"profile_run": "batch", "optimal": st["optimal"], "kernel_s": st["kernel_sec"],
+                          "iterations_max": st["iterations_max"], "grid_blocks": st["grid_blocks"]}), flush=True)
+        return
     gen_kwargs, _ = WORKLOADS[args.workload]
     data = instances.zipf_lp(**gen_kwargs)
     chosen = {**SIGMA_PROTOCOL, "precision": "fp32_refine", "device": local, "fp32_stall_evals": 1_000_000_000}
@@ -474,6 +492,8 @@ def main():
     ap.add_argument("--workload", default="large_lp", choices=list(WORKLOADS))
     ap.add_argument("--lp-only", action="store_true", help="skip the QP, batch and learned-start sections")
     ap.add_argument("--profile", action="store_true", help="only the chosen-form iteration steps (for ncu)")
+    ap.add_argument("--profile-section", default="lp", choices=["lp", "qp", "batch"],
+                    help="with --profile: which solver's kernels to run")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.profile:

@@ -6,6 +6,7 @@ than one thread).
 """
 from __future__ import annotations
 
+import shutil
 import subprocess
 from pathlib import Path
 
@@ -28,5 +29,51 @@ def build() -> Path:
     return TARGET
 
 
+REFERENCE = Path("/root/reference")
+REF_OUT = HERE / "_ref"
+SHIM = HERE / "ref_shim"
+# reference MPS readers, compiled from their own sources where they lie:
+# output name -> (project directory, shim macro)
+REF_READERS = {
+    "libref_mps_lp.so": ("LP/CP_AL", "REF_LP"),
+    "libref_mps_qp.so": ("QP/FA_CP", "REF_QP"),
+}
+
+
+def _cuda_include() -> str:
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return str(Path(nvcc).resolve().parent.parent / "include")
+
+
+def build_ref() -> list[Path]:
+    """Compiles the reference's own MPS readers (LP/CP_AL/src/mps_parser.c and
+    QP/FA_CP/src/mps_parser.c, unmodified, read in place) into oracle/_ref/
+    with gcc, zlib and ref_shim/ (allocation helpers, the problem free
+    functions and an empty PSLP_stats.h).  Their internal headers include the
+    CUDA headers for declarations only; nothing of CUDA is linked.  Returns
+    the built objects, or [] where the reference sources are absent."""
+    if not REFERENCE.exists():
+        return []
+    REF_OUT.mkdir(exist_ok=True)
+    out = []
+    for name, (proj, macro) in REF_READERS.items():
+        src = REFERENCE / proj / "src" / "mps_parser.c"
+        target = REF_OUT / name
+        deps = [src, *SHIM.iterdir()]
+        if target.exists() and target.stat().st_mtime > max(p.stat().st_mtime for p in deps):
+            out.append(target)
+            continue
+        cmd = ["gcc", "-O2", "-fPIC", "-shared", "-w", f"-D{macro}", "-I", str(SHIM),
+               "-I", str(REFERENCE / proj / "include"), "-I", str(REFERENCE / proj / "internal"),
+               "-I", _cuda_include(), str(src), str(SHIM / "ref_mps_shim.c"), "-lz", "-o", str(target)]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("reference reader build failed:\n" + " ".join(cmd) + "\n" + res.stderr)
+        out.append(target)
+    return out
+
+
 if __name__ == "__main__":
     print(build())
+    for p in build_ref():
+        print(p)

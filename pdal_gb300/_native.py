@@ -282,6 +282,7 @@ LP_SYMBOLS = {
         [C.c_int, C.POINTER(C.POINTER(LpProblem)), C.POINTER(CpalParameters), C.POINTER(CpalOptions), _dp,
          C.POINTER(C.POINTER(CpalResult)), C.POINTER(InstanceInfo), C.POINTER(BatchStats)],
     ),
+    "read_mps_file": (C.POINTER(LpProblem), [C.c_char_p]),
     "cp_al_gb300_primal_kkt_noalloc": (
         C.c_int,
         [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -474,6 +475,7 @@ QP_SYMBOLS = {
     "fa_cp_gb300_last_stats": (None, [C.POINTER(FacpStats)]),
     "fa_cp_gb300_last_error": (C.c_char_p, []),
     "fa_cp_gb300_rand_sequence": (None, [C.c_uint, C.c_int, _ip]),
+    "read_mps_file": (C.POINTER(QpProblem), [C.c_char_p]),
 }
 
 

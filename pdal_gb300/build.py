@@ -26,9 +26,15 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 
 # library name -> sources
 LIBRARIES = {
-    "libcp_al_gb300.so": ["cpal_solver.cu", "common.cpp", "cp_al_api.cpp", "noalloc.cu", "batch_solver.cu"],
-    "libfa_cp_gb300.so": ["facp_solver.cu", "common.cpp", "fa_cp_api.cpp"],
+    "libcp_al_gb300.so": ["cpal_solver.cu", "common.cpp", "cp_al_api.cpp", "noalloc.cu", "batch_solver.cu",
+                          "mps_reader.cpp"],
+    "libfa_cp_gb300.so": ["facp_solver.cu", "common.cpp", "fa_cp_api.cpp", "mps_reader.cpp"],
     "libpdal_learn_gb300.so": ["mlp.cu", "common.cpp"],
+}
+# the drop-in commands: executable name -> (source, library it links)
+EXECUTABLES = {
+    "cp_al": ("cli_cp_al.cpp", "libcp_al_gb300.so"),
+    "fa_cp": ("cli_fa_cp.cpp", "libfa_cp_gb300.so"),
 }
 
 
@@ -50,6 +56,21 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
 
 
+_ZLIB: bool | None = None
+
+
+def _have_zlib() -> bool:
+    """zlib header and library present (then .gz MPS files can be read)."""
+    global _ZLIB
+    if _ZLIB is None:
+        BUILD.mkdir(exist_ok=True)
+        probe = BUILD / "zlib_probe.cpp"
+        probe.write_text("#include <zlib.h>\nint main() { return zlibVersion() == nullptr; }\n")
+        res = subprocess.run(["g++", str(probe), "-lz", "-o", str(BUILD / "zlib_probe")], capture_output=True)
+        _ZLIB = res.returncode == 0
+    return _ZLIB
+
+
 def _compile(src: Path, obj: Path) -> Path:
     obj.parent.mkdir(parents=True, exist_ok=True)
     deps = [*CSRC.glob("*.h"), *CSRC.glob("*.cuh"), *(ROOT / "include").glob("*.h")]
@@ -58,7 +79,8 @@ def _compile(src: Path, obj: Path) -> Path:
     if src.suffix == ".cu":
         cmd = [_nvcc(), *NVCC_ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
     else:
-        cmd = ["g++", *CXX_FLAGS, "-I", _cuda_include(), "-c", str(src), "-o", str(obj)]
+        extra = ["-DPDAL_HAVE_ZLIB"] if src.name == "mps_reader.cpp" and _have_zlib() else []
+        cmd = ["g++", *CXX_FLAGS, *extra, "-I", _cuda_include(), "-c", str(src), "-o", str(obj)]
     _run(cmd)
     return obj
 
@@ -81,6 +103,14 @@ def build_product(jobs: int | None = None) -> list[Path]:
         # libraries export set_start_values and set_default_parameters)
         cmd = [_nvcc(), "-shared", "-o", str(target), *[str(objs[s]) for s in srcs], "-Xcompiler", "-fPIC",
                "-Xlinker", "-Bsymbolic"]
+        if "mps_reader.cpp" in srcs and _have_zlib():
+            cmd.append("-lz")
+        _run(cmd)
+        out.append(target)
+    for exe, (src, lib) in EXECUTABLES.items():
+        target = LIBDIR / exe
+        cmd = ["g++", *CXX_FLAGS, str(CSRC / src), "-o", str(target), "-L", str(LIBDIR), f"-l:{lib}",
+               "-Wl,-rpath,$ORIGIN"]
         _run(cmd)
         out.append(target)
     return out

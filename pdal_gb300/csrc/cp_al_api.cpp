@@ -383,3 +383,63 @@ void cp_al_gb300_options_from_env(cp_al_gb300_options_t *o) {
 }
 
 } // extern "C"
+
+/* ---------------------------------------------------------------------- */
+/* read_mps_file: LP/CP_AL/include/mps_parser.h:22                         */
+/* ---------------------------------------------------------------------- */
+#include "../../include/cp_al_mps_parser.h"
+#include "mps_reader.h"
+
+#include <string>
+#include <vector>
+
+namespace pdal {
+void set_last_error(const std::string &msg);
+void clear_last_error();
+} // namespace pdal
+
+namespace {
+
+template <class T>
+bool copy_out(const std::vector<T> &v, T **dst) {
+    *dst = nullptr;
+    if (v.empty()) return true;
+    *dst = (T *)malloc(v.size() * sizeof(T));
+    if (!*dst) return false;
+    memcpy(*dst, v.data(), v.size() * sizeof(T));
+    return true;
+}
+
+} // namespace
+
+extern "C" lp_problem_t *read_mps_file(const char *filename) {
+    pdal::clear_last_error();
+    pdal::mps::Model M;
+    std::string err;
+    if (!pdal::mps::read_file(filename, false, M, err)) {
+        pdal::set_last_error("read_mps_file: " + err);
+        return nullptr;
+    }
+    lp_problem_t *p = (lp_problem_t *)calloc(1, sizeof(lp_problem_t));
+    if (!p) {
+        pdal::set_last_error("read_mps_file: out of host memory");
+        return nullptr;
+    }
+    p->num_variables = M.num_cols;
+    p->num_constraints = M.num_rows;
+    p->constraint_matrix_num_nonzeros = (int)M.A.val.size();
+    p->objective_constant = M.objective_constant;
+    const bool ok = copy_out(M.c, &p->objective_vector) && copy_out(M.var_lb, &p->variable_lower_bound) &&
+                    copy_out(M.var_ub, &p->variable_upper_bound) &&
+                    copy_out(M.con_lb, &p->constraint_lower_bound) &&
+                    copy_out(M.con_ub, &p->constraint_upper_bound) &&
+                    copy_out(M.A.row_ptr, &p->constraint_matrix_row_pointers) &&
+                    copy_out(M.A.col_ind, &p->constraint_matrix_col_indices) &&
+                    copy_out(M.A.val, &p->constraint_matrix_values);
+    if (!ok) {
+        lp_problem_free(p);
+        pdal::set_last_error("read_mps_file: out of host memory");
+        return nullptr;
+    }
+    return p;
+}

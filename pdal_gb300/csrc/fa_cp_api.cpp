@@ -374,3 +374,85 @@ void fa_cp_gb300_options_from_env(fa_cp_gb300_options_t *o) { /* fa_cp_core_op.c
 }
 
 } // extern "C"
+
+/* ---------------------------------------------------------------------- */
+/* read_mps_file: QP/FA_CP/include/mps_parser.h:23                         */
+/* ---------------------------------------------------------------------- */
+#include "../../include/fa_cp_mps_parser.h"
+#include "mps_reader.h"
+
+#include <string>
+#include <vector>
+
+namespace pdal {
+void facp_set_last_error(const std::string &msg);
+} // namespace pdal
+
+namespace {
+
+template <class T>
+bool copy_out(const std::vector<T> &v, T **dst) {
+    *dst = nullptr;
+    if (v.empty()) return true;
+    *dst = (T *)malloc(v.size() * sizeof(T));
+    if (!*dst) return false;
+    memcpy(*dst, v.data(), v.size() * sizeof(T));
+    return true;
+}
+
+/* A component with the reader's rows + 1 row pointers; empty column and
+ * value arrays get one element so that no pointer of the problem is NULL. */
+CsrComponent *component(const pdal::mps::Csr &A) {
+    CsrComponent *c = (CsrComponent *)calloc(1, sizeof(CsrComponent));
+    if (!c) return nullptr;
+    const bool ok = copy_out(A.row_ptr, &c->row_ptr) && copy_out(A.col_ind, &c->col_ind) &&
+                    copy_out(A.val, &c->val);
+    if (ok && !c->col_ind) c->col_ind = (int *)calloc(1, sizeof(int));
+    if (ok && !c->val) c->val = (double *)calloc(1, sizeof(double));
+    if (!ok || !c->row_ptr || !c->col_ind || !c->val) {
+        free_component(c);
+        return nullptr;
+    }
+    return c;
+}
+
+} // namespace
+
+extern "C" qp_problem_t *read_mps_file(const char *filename) {
+    pdal::facp_set_last_error("");
+    pdal::mps::Model M;
+    std::string err;
+    if (!pdal::mps::read_file(filename, true, M, err)) {
+        fprintf(stderr, "[fa_cp_gb300] read_mps_file: %s\n", err.c_str());
+        pdal::facp_set_last_error("read_mps_file: " + err);
+        return nullptr;
+    }
+    qp_problem_t *p = (qp_problem_t *)calloc(1, sizeof(qp_problem_t));
+    if (!p) {
+        pdal::facp_set_last_error("read_mps_file: out of host memory");
+        return nullptr;
+    }
+    p->num_variables = M.num_cols;
+    p->num_constraints = M.num_rows;
+    p->num_rank_lowrank_obj = 0;
+    p->objective_constant = M.objective_constant;
+    p->constraint_matrix_num_nonzeros = (int)M.A.val.size();
+    p->objective_sparse_matrix_num_nonzeros = (int)M.Q.val.size();
+    p->objective_lowrank_matrix_num_nonzeros = 0;
+    pdal::mps::Csr lowrank;
+    lowrank.row_ptr.assign(1, 0);
+    p->constraint_matrix = component(M.A);
+    p->objective_sparse_matrix = component(M.Q);
+    p->objective_lowrank_matrix = component(lowrank);
+    const bool ok = p->constraint_matrix && p->objective_sparse_matrix && p->objective_lowrank_matrix &&
+                    copy_out(M.c, &p->objective_vector) && copy_out(M.var_lb, &p->variable_lower_bound) &&
+                    copy_out(M.var_ub, &p->variable_upper_bound) &&
+                    copy_out(M.con_lb, &p->constraint_lower_bound) &&
+                    copy_out(M.con_ub, &p->constraint_upper_bound);
+    if (!ok) {
+        qp_problem_free(p);
+        pdal::facp_set_last_error("read_mps_file: out of host memory");
+        return nullptr;
+    }
+    return p;
+}

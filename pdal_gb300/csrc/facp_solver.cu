@@ -283,6 +283,8 @@ class FacpSolver {
     void set_sigma_active(double s, double zt);
     double clipped(double cur, double ratio) const;
     void print_eval() const;
+    void trajectory_header() const;
+    void trajectory_row(double elapsed, bool restart) const;
 
     const qp_problem_t *prob_;
     fa_cp_parameters_t p_;
@@ -823,6 +825,30 @@ void FacpSolver::perform_restart() { /* fa_cp_core_op.cu:908-1020 */
     ++restarts_;
 }
 
+/* QP/FA_CP/src/solver.cu:35-70: one CSV row per evaluation point (the file
+ * is created with its header before the loop and reopened for each row). */
+void FacpSolver::trajectory_header() const {
+    const char *path = p_.trajectory_csv;
+    if (!path || !path[0]) return;
+    FILE *f = fopen(path, "w");
+    if (!f) throw Error(std::string("cannot open trajectory CSV ") + path);
+    fprintf(f, "iteration,time_sec,rel_primal,rel_dual,rel_gap,kkt_residual,fixed_point_residual,restart,al_sigma,"
+               "sigma_update_count\n");
+    fclose(f);
+}
+
+void FacpSolver::trajectory_row(double elapsed, bool restart) const {
+    const char *path = p_.trajectory_csv;
+    if (!path || !path[0]) return;
+    FILE *f = fopen(path, "a");
+    if (!f) throw Error(std::string("cannot append to trajectory CSV ") + path);
+    const double kkt = std::fmax(ctl_.rel_p, std::fmax(ctl_.rel_d, ctl_.rel_gap));
+    const double fp = total_ == 0 ? NAN : fp_;
+    fprintf(f, "%d,%.17e,%.17e,%.17e,%.17e,%.17e,%.17e,%d,%.17e,%d\n", total_, elapsed, ctl_.rel_p, ctl_.rel_d,
+            ctl_.rel_gap, kkt, fp, restart ? 1 : 0, al_sigma_, sigma_updates_);
+    fclose(f);
+}
+
 void FacpSolver::print_eval() const {
     printf("%6d %.1e | %8.1e  %8.1e | %.1e %.1e %.1e | %.1e %.1e %.1e \n", total_, 0.0, ctl_.pobj, ctl_.dobj,
            ctl_.abs_p, ctl_.abs_d, ctl_.gap, ctl_.rel_p, ctl_.rel_d, ctl_.rel_gap);
@@ -859,6 +885,7 @@ fa_cp_result_t *FacpSolver::run() {
 
     const int F = p_.termination_evaluation_frequency;
     const int limit = p_.termination_criteria.iteration_limit;
+    trajectory_header();
     bool major = false, do_restart = false;
     double elapsed = 0.0;
     while (total_ < limit) { /* QP/FA_CP/src/solver.cu:94-144 */
@@ -872,6 +899,7 @@ fa_cp_result_t *FacpSolver::run() {
                 choose_restart_candidate(elapsed);
                 planned = should_restart();
             }
+            trajectory_row(elapsed, planned);
             if (p_.verbose >= 2) print_eval();
             if (reason_ != TERMINATION_REASON_UNSPECIFIED) break;
         }
@@ -917,6 +945,7 @@ fa_cp_result_t *FacpSolver::run() {
     if (reason_ == TERMINATION_REASON_UNSPECIFIED) {
         reason_ = TERMINATION_REASON_ITERATION_LIMIT;
         evaluate(false);
+        trajectory_row(now_sec() - t_loop, false);
         if (p_.verbose >= 2) print_eval();
     }
     elapsed = now_sec() - t_loop;
@@ -1013,6 +1042,9 @@ fa_cp_result_t *solve_guarded(const qp_problem_t *prob, const fa_cp_parameters_t
 }
 
 } // namespace
+
+void facp_set_last_error(const std::string &msg) { g_error = msg; }
+
 } // namespace pdal
 
 extern "C" {

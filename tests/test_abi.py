@@ -13,7 +13,8 @@ from pdal_gb300 import _native as N
 from pdal_gb300 import lp
 
 ROOT = Path(__file__).resolve().parent.parent
-HEADERS = {"libcp_al_gb300.so": ["cp_al.h", "cp_al_gb300.h"], "libfa_cp_gb300.so": ["fa_cp.h", "fa_cp_gb300.h"],
+HEADERS = {"libcp_al_gb300.so": ["cp_al.h", "cp_al_gb300.h", "cp_al_mps_parser.h"],
+           "libfa_cp_gb300.so": ["fa_cp.h", "fa_cp_gb300.h", "fa_cp_mps_parser.h"],
            "libpdal_learn_gb300.so": ["pdal_learn.h"]}
 
 

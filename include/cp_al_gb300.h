@@ -72,7 +72,7 @@ typedef struct {
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */
 typedef struct {
-    double setup_sec;             /* upload, transpose, scaling, power iteration */
+    double setup_sec;             /* device setup: scaling, power iteration, initial iterate */
     double loop_sec;              /* iteration loop (wall) */
     double total_sec;             /* whole call, including result download */
     double lambda_est;            /* power-iteration estimate of sigma_max(A)^2 */
@@ -95,6 +95,13 @@ typedef struct {
     double avg_dual32_ms;
     double avg_block32_ms;
     int timed_blocks32;
+    /* setup phases of the last solve (wall seconds): validation, transpose
+     * and parameter checks on the host; row-block plans, allocation and
+     * host-to-device copies; equilibration; power iteration */
+    double prepare_sec;
+    double upload_sec;
+    double equilibration_sec;
+    double power_sec;
 } cp_al_gb300_stats_t;
 
 /* The reference defaults of every field, ignoring the environment. */

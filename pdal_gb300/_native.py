@@ -215,6 +215,10 @@ class CpalStats(C.Structure):
         ("avg_dual32_ms", C.c_double),
         ("avg_block32_ms", C.c_double),
         ("timed_blocks32", C.c_int),
+        ("prepare_sec", C.c_double),
+        ("upload_sec", C.c_double),
+        ("equilibration_sec", C.c_double),
+        ("power_sec", C.c_double),
     ]
 
 

@@ -5,9 +5,39 @@
 #include "rowblock_config.h"
 
 #include <algorithm>
+#include <functional>
+#include <thread>
 
 namespace pdal {
 
+/* Host threads for setup work over `work` items (1 below ~1M items). */
+int host_threads(long long work) {
+    if (work < (1ll << 20)) return 1;
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    return std::max(1, std::min(hw, 32));
+}
+
+void parallel_for(int nt, const std::function<void(int)> &f) {
+    if (nt <= 1) {
+        f(0);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(nt - 1);
+    for (int t = 1; t < nt; ++t) th.emplace_back(f, t);
+    f(0);
+    for (auto &x : th) x.join();
+}
+
+/*
+ * Counting-sort transpose.  The rows of A are cut into nt chunks of about
+ * equal nonzero count; chunk t counts its entries per column, the counts are
+ * turned into each chunk's first slot in every column (columns in order,
+ * chunks in order within a column), and each chunk then scatters its rows in
+ * order.  Every column of the result therefore lists its entries in
+ * increasing row order -- the output of the one-thread scatter, bit for bit,
+ * for any thread count.
+ */
 HostCsr csr_transpose(int nr, int nc, const int *rp, const int *ci, const double *v) {
     HostCsr T;
     T.nr = nc;
@@ -16,15 +46,64 @@ HostCsr csr_transpose(int nr, int nc, const int *rp, const int *ci, const double
     T.rp.assign((size_t)nc + 1, 0);
     T.ci.resize(nnz);
     T.v.resize(nnz);
-    for (int k = 0; k < nnz; ++k) T.rp[ci[k] + 1]++;
-    for (int j = 0; j < nc; ++j) T.rp[j + 1] += T.rp[j];
-    std::vector<int> next(T.rp.begin(), T.rp.end() - 1);
-    for (int i = 0; i < nr; ++i)
-        for (int k = rp[i]; k < rp[i + 1]; ++k) {
-            const int p = next[ci[k]]++;
-            T.ci[p] = i;
-            T.v[p] = v[k];
+    int nt = host_threads(nnz);
+    /* per-chunk column counts: nt x nc ints, kept under 512 MB */
+    while (nt > 1 && (size_t)nt * (size_t)nc * sizeof(int) > ((size_t)512 << 20)) --nt;
+    if (nt <= 1) {
+        for (int k = 0; k < nnz; ++k) T.rp[ci[k] + 1]++;
+        for (int j = 0; j < nc; ++j) T.rp[j + 1] += T.rp[j];
+        std::vector<int> next(T.rp.begin(), T.rp.end() - 1);
+        for (int i = 0; i < nr; ++i)
+            for (int k = rp[i]; k < rp[i + 1]; ++k) {
+                const int p = next[ci[k]]++;
+                T.ci[p] = i;
+                T.v[p] = v[k];
+            }
+        return T;
+    }
+    std::vector<int> rb(nt + 1, nr);
+    rb[0] = 0;
+    for (int t = 1; t < nt; ++t)
+        rb[t] = (int)(std::lower_bound(rp, rp + nr + 1, (int)((long long)nnz * t / nt)) - rp);
+    for (int t = 1; t <= nt; ++t) rb[t] = std::max(rb[t], rb[t - 1]);
+    std::vector<int> cnt((size_t)nt * nc);
+    parallel_for(nt, [&](int t) {
+        int *c = cnt.data() + (size_t)t * nc;
+        std::fill(c, c + nc, 0);
+        for (int k = rp[rb[t]]; k < rp[rb[t + 1]]; ++k) c[ci[k]]++;
+    });
+    /* column totals, then each chunk's first slot per column */
+    const int ntc = nt;
+    parallel_for(ntc, [&](int t) {
+        const int j0 = (int)((long long)nc * t / ntc), j1 = (int)((long long)nc * (t + 1) / ntc);
+        for (int j = j0; j < j1; ++j) {
+            int s = 0;
+            for (int q = 0; q < nt; ++q) s += cnt[(size_t)q * nc + j];
+            T.rp[j + 1] = s;
         }
+    });
+    for (int j = 0; j < nc; ++j) T.rp[j + 1] += T.rp[j];
+    parallel_for(ntc, [&](int t) {
+        const int j0 = (int)((long long)nc * t / ntc), j1 = (int)((long long)nc * (t + 1) / ntc);
+        for (int j = j0; j < j1; ++j) {
+            int at = T.rp[j];
+            for (int q = 0; q < nt; ++q) {
+                int &c = cnt[(size_t)q * nc + j];
+                const int n = c;
+                c = at;
+                at += n;
+            }
+        }
+    });
+    parallel_for(nt, [&](int t) {
+        int *next = cnt.data() + (size_t)t * nc;
+        for (int i = rb[t]; i < rb[t + 1]; ++i)
+            for (int k = rp[i]; k < rp[i + 1]; ++k) {
+                const int p = next[ci[k]]++;
+                T.ci[p] = i;
+                T.v[p] = v[k];
+            }
+    });
     return T;
 }
 
@@ -36,8 +115,18 @@ void csr_validate(int nr, int nc, const int *rp, const int *ci, int nnz, const c
     for (int i = 0; i < nr; ++i)
         if (rp[i + 1] < rp[i]) throw Error(std::string(what) + ": row pointers decrease");
     if (rp && rp[nr] != nnz) throw Error(std::string(what) + ": row_ptr[m] != nnz");
-    for (int k = 0; k < nnz; ++k)
-        if (ci[k] < 0 || ci[k] >= nc) throw Error(std::string(what) + ": column index out of range");
+    const int nt = host_threads(nnz);
+    std::vector<char> bad(nt, 0);
+    parallel_for(nt, [&](int t) {
+        const long long k0 = (long long)nnz * t / nt, k1 = (long long)nnz * (t + 1) / nt;
+        for (long long k = k0; k < k1; ++k)
+            if (ci[k] < 0 || ci[k] >= nc) {
+                bad[t] = 1;
+                break;
+            }
+    });
+    for (char b : bad)
+        if (b) throw Error(std::string(what) + ": column index out of range");
 }
 
 HostPlan plan_rows(int nr, const int *rp, int S) {

@@ -9,6 +9,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -87,7 +88,13 @@ struct HostCsr {
     int nnz() const { return (int)ci.size(); }
 };
 
-/* Transpose with rows of A^T in increasing row order of A. */
+/* Host threads worth using for setup work over `work` items, and a fork-join
+ * over thread ids 0..nt-1 (id 0 runs on the calling thread). */
+int host_threads(long long work);
+void parallel_for(int nt, const std::function<void(int)> &f);
+
+/* Transpose with rows of A^T in increasing row order of A (host threads;
+ * the result does not depend on their number). */
 HostCsr csr_transpose(int nr, int nc, const int *rp, const int *ci, const double *v);
 
 /* Checks row pointers (monotone, rp[0]=0, rp[nr]=nnz) and column range; the

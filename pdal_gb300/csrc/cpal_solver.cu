@@ -133,6 +133,7 @@ class CpalSolver {
 
     CpalState host_state{};
     double setup_sec = 0, loop_sec = 0;
+    double prepare_sec = 0, upload_sec = 0, equil_sec = 0, power_sec = 0;
     int64_t launches = 0;
     int64_t h2d = 0, d2h = 0;
     int power_iters = 0;
@@ -291,6 +292,7 @@ CpalParams resolve_cpal_params(const cp_al_parameters_t &P, const cp_al_gb300_op
 }
 
 void CpalSolver::prepare() {
+    const double t_prep = now_sec();
     n_ = prob_->num_variables;
     m_ = prob_->num_constraints;
     nnz_ = prob_->constraint_matrix_num_nonzeros;
@@ -314,6 +316,7 @@ void CpalSolver::prepare() {
 
     cp_ = resolve_cpal_params(P_, O_, prob_);
     fp32_phase_ = O_.precision == CP_AL_GB300_FP32_REFINE;
+    prepare_sec = now_sec() - t_prep;
 }
 
 void CpalSolver::alloc_plan(PlanDev &pd) {
@@ -433,6 +436,7 @@ void CpalSolver::alloc_all() {
 }
 
 void CpalSolver::upload() {
+    const double t_up = now_sec();
     if (O_.device >= 0) PDAL_CUDA(cudaSetDevice(O_.device));
     PDAL_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     PDAL_CUDA(cudaMallocHost(&h_st_, sizeof(CpalState)));
@@ -483,6 +487,7 @@ void CpalSolver::upload() {
         PDAL_CUDA(cudaMemsetAsync(y00_, 0, std::max<size_t>(m, 1) * sizeof(double), stream_));
     PDAL_CUDA(cudaStreamSynchronize(stream_));
     At_host_ = HostCsr(); /* host transpose no longer needed */
+    upload_sec = now_sec() - t_up;
 }
 
 void CpalSolver::power_iteration() {
@@ -594,6 +599,8 @@ void CpalSolver::setup_device() {
     CpalState s{};
     s.cbr = h_st_->cbr;
     s.ovr = h_st_->ovr;
+    equil_sec = now_sec() - t0;
+    const double t_pow = now_sec();
 
     /* step size and primal weight: LP/CP_AL/src/solver.cu:3538-3609 */
     if (nnz_ == 0) {
@@ -603,6 +610,7 @@ void CpalSolver::setup_device() {
         power_iteration();
     }
     s.lambda_est = host_state.lambda_est;
+    power_sec = now_sec() - t_pow;
     s.pw = P_.bound_objective_rescaling ? 1.0 : (cp_.obj_norm + 1.0) / (cp_.bnd_norm + 1.0);
     s.sigma_on = cp_.sigma_mode;
     s.sigma_adapt = 0;
@@ -1080,6 +1088,10 @@ static void fill_stats(const pdal::CpalSolver &s, double total) {
     }
     st.step_size = s.host_state.step;
     st.al_penalty = s.host_state.beta;
+    st.prepare_sec = s.prepare_sec;
+    st.upload_sec = s.upload_sec;
+    st.equilibration_sec = s.equil_sec;
+    st.power_sec = s.power_sec;
 }
 
 cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *params,

@@ -81,6 +81,13 @@ void fa_cp_gb300_rand_sequence(unsigned seed, int count, int *out);
 /* Message of the last failure on this thread ("" if none). */
 const char *fa_cp_gb300_last_error(void);
 
+/* The equilibration of a solve without the solve: column scales (n), row
+ * scales (m) and the bound/objective factors {cbr, ovr} the solver computes
+ * on the device before its first iteration (QP/FA_CP/src/preconditioner.c).
+ * For tests and diagnostics; 0 on success, -1 on failure. */
+int fa_cp_gb300_scaling(const qp_problem_t *prob, const fa_cp_parameters_t *params,
+                        const fa_cp_gb300_options_t *opts, double *dcum, double *rcum, double *cbr_ovr);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

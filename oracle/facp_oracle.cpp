@@ -973,6 +973,34 @@ fa_cp_result_t *oracle_facp_solve(const qp_problem_t *prob, const fa_cp_paramete
     return r;
 }
 
+/* Only the equilibration of oracle_facp_solve: column and row scales and
+ * {cbr, ovr}. */
+int oracle_facp_scaling(const qp_problem_t *prob, const fa_cp_parameters_t *params, double *dcum, double *rcum,
+                        double *cbr_ovr) {
+    if (!prob || !params) return -1;
+    std::unique_ptr<QP> SP(new QP());
+    QP &S = *SP;
+    S.P = params;
+    S.n = prob->num_variables;
+    S.m = prob->num_constraints;
+    S.nr = prob->num_rank_lowrank_obj;
+    const int n = S.n, m = S.m;
+    S.A = from_component(prob->constraint_matrix, m, n, prob->constraint_matrix_num_nonzeros);
+    S.Q = from_component(prob->objective_sparse_matrix, n, n, prob->objective_sparse_matrix_num_nonzeros);
+    S.R = from_component(prob->objective_lowrank_matrix, S.nr, n, prob->objective_lowrank_matrix_num_nonzeros);
+    S.c.assign(prob->objective_vector, prob->objective_vector + n);
+    S.vlb.assign(prob->variable_lower_bound, prob->variable_lower_bound + n);
+    S.vub.assign(prob->variable_upper_bound, prob->variable_upper_bound + n);
+    S.clb.assign(prob->constraint_lower_bound, prob->constraint_lower_bound + m);
+    S.cub.assign(prob->constraint_upper_bound, prob->constraint_upper_bound + m);
+    S.rescale();
+    std::copy(S.dcum.begin(), S.dcum.end(), dcum);
+    std::copy(S.rcum.begin(), S.rcum.end(), rcum);
+    cbr_ovr[0] = S.cbr;
+    cbr_ovr[1] = S.ovr;
+    return 0;
+}
+
 void oracle_facp_set_trace(int on) { g_trace = on; }
 
 void oracle_facp_result_free(fa_cp_result_t *r) {

@@ -260,6 +260,22 @@ class _QpProblem:
         self.p, self.m, self.n = p, m, n
 
 
+def qp_scaling(data: QPData, params: dict | None = None):
+    """The oracle's equilibration alone: (dcum, rcum, cbr, ovr)."""
+    L = _qp_lib()
+    if not getattr(L, "_facp_scaling_ready", False):
+        L.oracle_facp_scaling.restype = C.c_int
+        L.oracle_facp_scaling.argtypes = [C.POINTER(N.QpProblem), C.POINTER(N.FacpParameters), _dp, _dp, _dp]
+        L._facp_scaling_ready = True
+    p = _qp_apply_params(qp_default_parameters(), params)
+    prob = _QpProblem(data)
+    d, r, f = np.zeros(max(prob.n, 1)), np.zeros(max(prob.m, 1)), np.zeros(2)
+    if L.oracle_facp_scaling(C.byref(prob.p), C.byref(p), d.ctypes.data_as(_dp), r.ctypes.data_as(_dp),
+                             f.ctypes.data_as(_dp)) != 0:
+        raise RuntimeError("oracle QP scaling failed")
+    return d[:prob.n], r[:prob.m], float(f[0]), float(f[1])
+
+
 def solve_qp(data: QPData, params: dict | None = None, trace: bool = False) -> QPResult:
     """The oracle's FA_CP solve (serial FP64)."""
     L = _qp_lib()

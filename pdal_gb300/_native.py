@@ -480,6 +480,9 @@ QP_SYMBOLS = {
     "fa_cp_gb300_last_error": (C.c_char_p, []),
     "fa_cp_gb300_rand_sequence": (None, [C.c_uint, C.c_int, _ip]),
     "read_mps_file": (C.POINTER(QpProblem), [C.c_char_p]),
+    "fa_cp_gb300_scaling": (
+        C.c_int, [C.POINTER(QpProblem), C.POINTER(FacpParameters), C.POINTER(FacpOptions), _dp, _dp, _dp],
+    ),
 }
 
 

@@ -769,58 +769,64 @@ struct PowerState {
     double tol;
 };
 
+/* The power iteration runs in the arithmetic type T: FP64 in the plain form
+ * (the reference's arithmetic), FP32 in the chosen form, where its SpMVs
+ * stream half the bytes; the Rayleigh quotient, the residual and the norms
+ * are accumulated in FP64 either way. */
+template <typename T>
 struct PowerColEpi : NoLongRed {
-    double *dp;
-    __device__ __forceinline__ void operator()(int j, const double *s, Red<0, 0> &) const { dp[j] = s[0]; }
+    T *dp;
+    __device__ __forceinline__ void operator()(int j, const T *s, Red<0, 0> &) const { dp[j] = s[0]; }
 };
 
 /* dp = A^T (inv * v) */
-template <int S>
+template <int S, typename T>
 __global__ void __launch_bounds__(kThreads) k_power_at(RowPlanDev plan, const int *__restrict__ rp,
-                                                       const int *__restrict__ ci, const double *__restrict__ val,
-                                                       const double *__restrict__ v, double *dp,
+                                                       const int *__restrict__ ci, const T *__restrict__ val,
+                                                       const T *__restrict__ v, T *dp,
                                                        const PowerState *__restrict__ ps) {
     if (ps->done) return;
-    __shared__ RowBlockSmem<S, 1, double> sm;
-    const double inv = ps->inv;
-    PowerColEpi epi;
+    __shared__ RowBlockSmem<S, 1, T> sm;
+    const T inv = (T)ps->inv;
+    PowerColEpi<T> epi;
     epi.dp = dp;
-    auto g = [&](int c, double *out) { out[0] = inv * v[c]; };
+    auto g = [&](int c, T *out) { out[0] = inv * v[c]; };
     Red<0, 0> red;
-    rowblock_run<S, 1, double>(plan, rp, ci, val, g, epi, red, sm);
+    rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);
 }
 
 /* vn = A dp, partial sums of (inv * v) . vn */
+template <typename T>
 struct PowerRowEpi {
-    const double *v;
-    double *vn;
+    const T *v;
+    T *vn;
     double inv;
     double *part;
     int nblocks;
-    __device__ __forceinline__ void operator()(int i, const double *s, Red<1, 0> &r) const {
+    __device__ __forceinline__ void operator()(int i, const T *s, Red<1, 0> &r) const {
         vn[i] = s[0];
-        r.s[0] += (inv * v[i]) * s[0];
+        r.s[0] += (inv * (double)v[i]) * (double)s[0];
     }
     __device__ __forceinline__ void long_red(int lid, Red<1, 0> &r) const { part[nblocks + lid] = r.s[0]; }
 };
 
-template <int S>
+template <int S, typename T>
 __global__ void __launch_bounds__(kThreads) k_power_a(RowPlanDev plan, const int *__restrict__ rp,
-                                                      const int *__restrict__ ci, const double *__restrict__ val,
-                                                      const double *__restrict__ dp, const double *__restrict__ v,
-                                                      double *vn, double *part, const PowerState *__restrict__ ps) {
+                                                      const int *__restrict__ ci, const T *__restrict__ val,
+                                                      const T *__restrict__ dp, const T *__restrict__ v,
+                                                      T *vn, double *part, const PowerState *__restrict__ ps) {
     if (ps->done) return;
-    __shared__ RowBlockSmem<S, 1, double> sm;
-    PowerRowEpi epi;
+    __shared__ RowBlockSmem<S, 1, T> sm;
+    PowerRowEpi<T> epi;
     epi.v = v;
     epi.vn = vn;
     epi.inv = ps->inv;
     epi.part = part;
     epi.nblocks = plan.nblocks;
-    auto g = [&](int c, double *out) { out[0] = dp[c]; };
+    auto g = [&](int c, T *out) { out[0] = dp[c]; };
     Red<1, 0> red;
     red.zero();
-    rowblock_run<S, 1, double>(plan, rp, ci, val, g, epi, red, sm);
+    rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);
     block_reduce<kThreads, 1, 0>(red, sm.red);
     if (threadIdx.x == 0) part[blockIdx.x] = red.s[0];
 }
@@ -837,20 +843,21 @@ static __global__ void __launch_bounds__(kThreads) k_power_dot(const double *__r
 }
 
 /* residual vn - s2 * (inv v) and |vn|^2; then v <- vn */
-static __global__ void __launch_bounds__(kThreads) k_power_resid(int m, double *v, const double *__restrict__ vn,
-                                                          double *part, const PowerState *__restrict__ ps) {
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_power_resid(int m, T *v, const T *__restrict__ vn, double *part,
+                                                          const PowerState *__restrict__ ps) {
     if (ps->done) return;
     __shared__ double sbuf[2 * (kThreads / 32)];
     const double inv = ps->inv, s2 = ps->s2;
     Red<2, 0> r;
     r.zero();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-        const double nv = inv * v[i];
-        const double vni = vn[i];
+        const double nv = inv * (double)v[i];
+        const double vni = (double)vn[i];
         const double q = (-s2 * nv) + vni;
         r.s[0] += q * q;
         r.s[1] += vni * vni;
-        v[i] = vni;
+        v[i] = vn[i];
     }
     block_reduce<kThreads, 2, 0>(r, sbuf);
     if (threadIdx.x == 0) {
@@ -880,11 +887,12 @@ static __global__ void __launch_bounds__(kThreads) k_power_check(const double *_
 }
 
 /* 1/|v| of the start vector */
-static __global__ void __launch_bounds__(kThreads) k_power_start(int m, const double *__restrict__ v, PowerState *ps) {
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_power_start(int m, const T *__restrict__ v, PowerState *ps) {
     __shared__ double sbuf[kThreads / 32];
     Red<1, 0> r;
     r.zero();
-    for (int i = threadIdx.x; i < m; i += kThreads) r.s[0] += v[i] * v[i];
+    for (int i = threadIdx.x; i < m; i += kThreads) r.s[0] += (double)v[i] * (double)v[i];
     block_reduce<kThreads, 1, 0>(r, sbuf);
     if (threadIdx.x == 0) ps->inv = 1.0 / sqrt(r.s[0]);
 }

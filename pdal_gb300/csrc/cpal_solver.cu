@@ -429,7 +429,8 @@ void CpalSolver::alloc_all() {
     wtf_ = arena_.take<HalpernWf>((size_t)cp_.F + 1);
     part_row_ = arena_.take<double>((size_t)(A_.ev.hp.nblocks + A_.ev.hp.nlong + 1) * kEvalStride);
     part_col_ = arena_.take<double>((size_t)(At_.ev.hp.nblocks + At_.ev.hp.nlong + 1) * kEvalStride);
-    nmisc_ = std::max({A_.ev.hp.nblocks + A_.ev.hp.nlong, grid_for(std::max(n_, m_)), 1});
+    nmisc_ = std::max({A_.ev.hp.nblocks + A_.ev.hp.nlong, A_.it.hp.nblocks + A_.it.hp.nlong,
+                       grid_for(std::max(n_, m_)), 1});
     part_misc_ = arena_.take<double>(2 * (size_t)nmisc_ + 2);
     st_ = arena_.take<CpalState>(1);
     ps_ = arena_.take<PowerState>(1);
@@ -501,26 +502,54 @@ void CpalSolver::power_iteration() {
     std::mt19937 gen(1);
     std::normal_distribution<double> dist(0.0, 1.0);
     for (int i = 0; i < m_; ++i) v0[i] = dist(gen);
-    double *v = tmp_m_, *vn = tmp_m2_, *dp = tmp_n_;
-    PDAL_CUDA(cudaMemcpyAsync(v, v0.data(), sizeof(double) * m_, cudaMemcpyHostToDevice, stream_));
-    h2d += sizeof(double) * m_;
+    /* plain form: FP64 over the evaluation plans; chosen form: FP32 over the
+     * iteration plans and the FP32 matrix copies (made before this call) */
+    const bool f32 = fp32_phase_;
+    if (f32) {
+        std::vector<float> v0f(v0.begin(), v0.end());
+        PDAL_CUDA(cudaMemcpyAsync(tmp_m_, v0f.data(), sizeof(float) * m_, cudaMemcpyHostToDevice, stream_));
+        h2d += sizeof(float) * m_;
+    } else {
+        PDAL_CUDA(cudaMemcpyAsync(tmp_m_, v0.data(), sizeof(double) * m_, cudaMemcpyHostToDevice, stream_));
+        h2d += sizeof(double) * m_;
+    }
     *h_ps_ = h;
     PDAL_CUDA(cudaMemcpyAsync(ps_, h_ps_, sizeof(PowerState), cudaMemcpyHostToDevice, stream_));
-    k_power_start<<<1, kThreads, 0, stream_>>>(m_, v, ps_);
+    if (f32)
+        k_power_start<float><<<1, kThreads, 0, stream_>>>(m_, (const float *)tmp_m_, ps_);
+    else
+        k_power_start<double><<<1, kThreads, 0, stream_>>>(m_, tmp_m_, ps_);
     PDAL_LAUNCH_CHECK();
     launches += 1;
     const int gres = grid_for(m_);
     const int steps_per_graph = 16;
     cudaGraphExec_t exec = nullptr;
     PDAL_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-    for (int s = 0; s < steps_per_graph; ++s) {
-        PDAL_WITH_SE(S_ev_, {
-            k_power_at<SE><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, v, dp, ps_);
-            k_power_a<SE><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, dp, v, vn,
-                                                                     part_misc_, ps_);
-        });
-        k_power_dot<<<1, kThreads, 0, stream_>>>(part_misc_, A_.ev.d.nblocks + A_.ev.d.nlong, ps_);
-        k_power_resid<<<gres, kThreads, 0, stream_>>>(m_, v, vn, part_misc_, ps_);
+    for (int st = 0; st < steps_per_graph; ++st) {
+        int nparts = 0;
+        if (f32) {
+            float *v = (float *)tmp_m_, *vn = (float *)tmp_m2_, *dp = (float *)tmp_n_;
+            PDAL_WITH_S(S_it_, {
+                k_power_at<SB, float><<<At_.it.d.nblocks, kThreads, 0, stream_>>>(At_.it.d, At_.rp, At_.ci, At_.vf,
+                                                                                  v, dp, ps_);
+                k_power_a<SB, float><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, A_.vf, dp, v,
+                                                                                vn, part_misc_, ps_);
+            });
+            nparts = A_.it.d.nblocks + A_.it.d.nlong;
+            k_power_dot<<<1, kThreads, 0, stream_>>>(part_misc_, nparts, ps_);
+            k_power_resid<float><<<gres, kThreads, 0, stream_>>>(m_, v, vn, part_misc_, ps_);
+        } else {
+            double *v = tmp_m_, *vn = tmp_m2_, *dp = tmp_n_;
+            PDAL_WITH_SE(S_ev_, {
+                k_power_at<SE, double><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v,
+                                                                                   v, dp, ps_);
+                k_power_a<SE, double><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, dp, v,
+                                                                                 vn, part_misc_, ps_);
+            });
+            nparts = A_.ev.d.nblocks + A_.ev.d.nlong;
+            k_power_dot<<<1, kThreads, 0, stream_>>>(part_misc_, nparts, ps_);
+            k_power_resid<double><<<gres, kThreads, 0, stream_>>>(m_, v, vn, part_misc_, ps_);
+        }
         k_power_check<<<1, kThreads, 0, stream_>>>(part_misc_, gres, ps_);
     }
     cudaGraph_t graph;
@@ -602,6 +631,14 @@ void CpalSolver::setup_device() {
     equil_sec = now_sec() - t0;
     const double t_pow = now_sec();
 
+    /* FP32 matrix copies of the equilibrated values (chosen form), which the
+     * power iteration already uses */
+    if (fp32_phase_) {
+        if (nnz) k_convert<double, float><<<grid_for(nnz), kThreads, 0, stream_>>>(A_.v, A_.vf, (int)nnz);
+        if (nnz) k_convert<double, float><<<grid_for(nnz), kThreads, 0, stream_>>>(At_.v, At_.vf, (int)nnz);
+        PDAL_LAUNCH_CHECK();
+        launches += 2;
+    }
     /* step size and primal weight: LP/CP_AL/src/solver.cu:3538-3609 */
     if (nnz_ == 0) {
         host_state.lambda_est = 1.0;
@@ -658,8 +695,6 @@ void CpalSolver::setup_device() {
             if (len) k_convert<double, float><<<grid_for(len), kThreads, 0, stream_>>>(src, dst, (int)len);
             launches += 1;
         };
-        cv(A_.v, A_.vf, nnz);
-        cv(At_.v, At_.vf, nnz);
         cv(c_, v32_.c, n);
         cv(vlb_, v32_.vlb, n);
         cv(vub_, v32_.vub, n);

@@ -101,130 +101,111 @@ HostCsr from_component(const CsrComponent *cc, int rows, int cols, int nnz, cons
  * one Pock-Chambolle pass, then bound/objective scaling that also rescales Q
  * by ovr/cbr and R by sqrt(ovr/cbr).
  *
- * Run on host threads over rows: column statistics come from the rows of the
- * transposes A' and Q', which hold each column's entries in increasing row
- * order -- the order the reference's row-major scatter visits them -- and
- * every transpose value is scaled by the same expression as its original, so
- * the results are bit-identical to the serial loops. */
-template <class F>
-void parallel_rows(int rows, F f) {
-    const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 32));
-    if (rows < 4096 || nt == 1) {
-        f(0, rows);
-        return;
-    }
-    std::vector<std::thread> th;
-    const int chunk = (rows + nt - 1) / nt;
-    for (int t = 0; t < nt; ++t) {
-        const int r0 = t * chunk, r1 = std::min(rows, r0 + chunk);
-        if (r0 < r1) th.emplace_back([=]() { f(r0, r1); });
-    }
-    for (auto &x : th) x.join();
+ * Run on the device.  Column statistics come from the rows of the transposes
+ * A' and Q', which hold each column's entries in increasing row order -- the
+ * order the reference's row-major scatter visits them -- and each row's
+ * statistic is formed by one thread in storage order, so every sum has the
+ * reference's order.  Every matrix and transpose value is divided by the
+ * same product of scale factors as in the reference, with IEEE division and
+ * multiplication, and the bound/objective norms are summed on the host in
+ * the reference's loop order: the scaled problem is bit-identical to the
+ * reference's (|a|^deg uses pow() except for deg 1 and 2, where it is exact
+ * on both sides). */
+__device__ __forceinline__ double pow_deg(double a, double deg) {
+    if (deg == 1.0) return a;
+    if (deg == 2.0) return __dmul_rn(a, a);
+    return pow(a, deg);
 }
 
-void scale_matrix(HostCsr &M, const std::vector<double> &row_s, const std::vector<double> &col_s) {
-    parallel_rows(M.nr, [&](int r0, int r1) {
-        for (int row = r0; row < r1; ++row)
-            for (int k = M.rp[row]; k < M.rp[row + 1]; ++k) M.v[k] /= (row_s[row] * col_s[M.ci[k]]);
-    });
-}
-
-/* the transpose's row `row` is column `row` of the original: scaled by
- * (orig_row_scale * col_scale) in the original's operand order */
-void scale_transpose(HostCsr &T, const std::vector<double> &orig_row_s, const std::vector<double> &orig_col_s) {
-    parallel_rows(T.nr, [&](int r0, int r1) {
-        for (int row = r0; row < r1; ++row)
-            for (int k = T.rp[row]; k < T.rp[row + 1]; ++k) T.v[k] /= (orig_row_s[T.ci[k]] * orig_col_s[row]);
-    });
-}
-
-void scale_problem(HostQP &P, HostCsr &At, HostCsr &Qt, const std::vector<double> &r, const std::vector<double> &d) {
-    for (int i = 0; i < P.n; ++i) {
-        P.c[i] /= d[i];
-        P.vub[i] *= d[i];
-        P.vlb[i] *= d[i];
-    }
-    for (int i = 0; i < P.m; ++i) {
-        P.clb[i] /= r[i];
-        P.cub[i] /= r[i];
-    }
-    scale_matrix(P.A, r, d);
-    scale_transpose(At, r, d);
-    scale_matrix(P.Q, d, d);
-    scale_transpose(Qt, d, d);
-    if (P.R.nnz() > 0)
-        for (int row = 0; row < P.nr; ++row)
-            for (int k = P.R.rp[row]; k < P.R.rp[row + 1]; ++k) P.R.v[k] /= d[P.R.ci[k]];
-}
-
-/* per-row statistic of the rows of M (abs max, or sum of |a|^deg in order) */
-void row_stat(const HostCsr &M, int mode, double deg, std::vector<double> &out, bool accumulate) {
-    parallel_rows(M.nr, [&](int r0, int r1) {
-        for (int row = r0; row < r1; ++row) {
-            double acc = accumulate ? out[row] : 0.0;
-            for (int k = M.rp[row]; k < M.rp[row + 1]; ++k) {
-                const double v = std::fabs(M.v[k]);
-                if (mode == 0) {
-                    if (v > acc) acc = v;
-                } else {
-                    acc += std::pow(v, deg);
-                }
+/* abs max (mode 0) or sum of |a|^deg in storage order (mode 1) of each row */
+__global__ void k_row_stat(int rows, const int *__restrict__ rp, const double *__restrict__ v, int mode, double deg,
+                           double *out, int accumulate) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        double acc = accumulate ? out[r] : 0.0;
+        for (int k = rp[r]; k < rp[r + 1]; ++k) {
+            const double a = fabs(v[k]);
+            if (mode == 0) {
+                if (a > acc) acc = a;
+            } else {
+                acc = __dadd_rn(acc, pow_deg(a, deg));
             }
-            out[row] = acc;
         }
-    });
+        out[r] = acc;
+    }
 }
 
-void equilibrate(HostQP &P, HostCsr &At, HostCsr &Qt, const fa_cp_parameters_t &prm) {
-    P.dcum.assign(P.n, 1.0);
-    P.rcum.assign(P.m, 1.0);
-    std::vector<double> cr(P.m), vr(P.n);
-    auto finish = [&]() {
-        for (int i = 0; i < P.n; ++i) vr[i] = (vr[i] < 1e-12) ? 1.0 : std::sqrt(vr[i]);
-        for (int i = 0; i < P.m; ++i) cr[i] = (cr[i] < 1e-12) ? 1.0 : std::sqrt(cr[i]);
-        scale_problem(P, At, Qt, cr, vr);
-        for (int i = 0; i < P.n; ++i) P.dcum[i] *= vr[i];
-        for (int i = 0; i < P.m; ++i) P.rcum[i] *= cr[i];
-    };
-    for (int it = 0; it < prm.l_inf_ruiz_iterations; ++it) {
-        row_stat(P.A, 0, 0.0, cr, false);
-        row_stat(At, 0, 0.0, vr, false);
-        row_stat(Qt, 0, 0.0, vr, true);
-        finish();
+/* s = s < 1e-12 ? 1 : sqrt(s); cum *= s */
+__global__ void k_finish_scale(int len, double *s, double *cum) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+        const double v = s[i];
+        const double f = (v < 1e-12) ? 1.0 : sqrt(v);
+        s[i] = f;
+        cum[i] = __dmul_rn(cum[i], f);
     }
-    if (prm.has_pock_chambolle_alpha) {
-        const double a = prm.pock_chambolle_alpha;
-        row_stat(P.A, 1, a, cr, false);
-        row_stat(At, 1, 2.0 - a, vr, false);
-        row_stat(Qt, 1, 2.0 - a, vr, true);
-        finish();
+}
+
+/* a_rk /= rs[r] * cs[col] (a missing factor is left out) */
+__global__ void k_scale_csr(int rows, const int *__restrict__ rp, const int *__restrict__ ci, double *v,
+                            const double *__restrict__ rs, const double *__restrict__ cs) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        for (int k = rp[r]; k < rp[r + 1]; ++k) {
+            const double den = rs ? (cs ? __dmul_rn(rs[r], cs[ci[k]]) : rs[r]) : cs[ci[k]];
+            v[k] = __ddiv_rn(v[k], den);
+        }
     }
-    if (prm.bound_objective_rescaling) {
-        double bsq = 0.0, csq = 0.0;
-        for (int i = 0; i < P.m; ++i) {
-            if (std::isfinite(P.clb[i]) && P.clb[i] != P.cub[i]) bsq += P.clb[i] * P.clb[i];
-            if (std::isfinite(P.cub[i])) bsq += P.cub[i] * P.cub[i];
+}
+
+__global__ void k_scale_vectors(int n, int m, double *c, double *vlb, double *vub, double *clb, double *cub,
+                                const double *__restrict__ d, const double *__restrict__ r) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < max(n, m); i += gridDim.x * blockDim.x) {
+        if (i < n) {
+            c[i] = __ddiv_rn(c[i], d[i]);
+            vub[i] = __dmul_rn(vub[i], d[i]);
+            vlb[i] = __dmul_rn(vlb[i], d[i]);
         }
-        for (int i = 0; i < P.n; ++i) csq += P.c[i] * P.c[i];
-        P.cbr = 1.0 / (std::sqrt(bsq) + 1.0);
-        P.ovr = 1.0 / (std::sqrt(csq) + 1.0);
-        for (int i = 0; i < P.m; ++i) {
-            P.clb[i] *= P.cbr;
-            P.cub[i] *= P.cbr;
+        if (i < m) {
+            clb[i] = __ddiv_rn(clb[i], r[i]);
+            cub[i] = __ddiv_rn(cub[i], r[i]);
         }
-        for (int i = 0; i < P.n; ++i) {
-            P.vlb[i] *= P.cbr;
-            P.vub[i] *= P.cbr;
-            P.c[i] *= P.ovr;
-        }
-        for (double &v : P.Q.v) v *= P.ovr / P.cbr;
-        if (P.R.nnz() > 0) {
-            const double f = std::sqrt(P.ovr / P.cbr);
-            for (double &v : P.R.v) v *= f;
-        }
-    } else {
-        P.cbr = P.ovr = 1.0;
     }
+}
+
+__global__ void k_bound_objective(int n, int m, double cbr, double ovr, double *c, double *vlb, double *vub,
+                                  double *clb, double *cub) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < max(n, m); i += gridDim.x * blockDim.x) {
+        if (i < m) {
+            clb[i] = __dmul_rn(clb[i], cbr);
+            cub[i] = __dmul_rn(cub[i], cbr);
+        }
+        if (i < n) {
+            vlb[i] = __dmul_rn(vlb[i], cbr);
+            vub[i] = __dmul_rn(vub[i], cbr);
+            c[i] = __dmul_rn(c[i], ovr);
+        }
+    }
+}
+
+__global__ void k_mul(long long len, double *v, double f) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+        v[i] = __dmul_rn(v[i], f);
+}
+
+__global__ void k_fill(int len, double *v, double val) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) v[i] = val;
+}
+
+/* finite part of a bound vector (infinite entries become 0) */
+__global__ void k_finite(int len, const double *__restrict__ src, double *dst) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x)
+        dst[i] = isfinite(src[i]) ? src[i] : 0.0;
+}
+
+/* diagonal of a diagonal Q plus 1e-12 (solver_state.cu:252-270) */
+__global__ void k_diag(int rows, int n, const int *__restrict__ rp, const int *__restrict__ ci,
+                       const double *__restrict__ v, double *diag) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+        for (int k = rp[r]; k < rp[r + 1]; ++k)
+            if (ci[k] < n) diag[ci[k]] = __dadd_rn(v[k], 1e-12);
 }
 
 int detect_q_type(const HostCsr &Q, const HostCsr &R) { /* QP/FA_CP/src/utils.cu:1576-1616 */
@@ -266,6 +247,17 @@ class FacpSolver {
         if (ev1_) cudaEventDestroy(ev1_);
     }
     fa_cp_result_t *run();
+    /* prepare, upload and equilibrate only; the scale vectors and factors */
+    void scaling(double *dcum, double *rcum, double *cbr_ovr) {
+        prepare();
+        upload();
+        if (dcum) std::copy(H_.dcum.begin(), H_.dcum.end(), dcum);
+        if (rcum) std::copy(H_.rcum.begin(), H_.rcum.end(), rcum);
+        if (cbr_ovr) {
+            cbr_ovr[0] = H_.cbr;
+            cbr_ovr[1] = H_.ovr;
+        }
+    }
 
   private:
     void prepare();
@@ -274,6 +266,7 @@ class FacpSolver {
     void read_ctl();
     Args base_args(int mode) const;
     void power_iterations();
+    void equilibrate_device();
     void evaluate(bool infeas);
     bool check_termination(double elapsed);
     bool should_restart();
@@ -290,6 +283,10 @@ class FacpSolver {
     fa_cp_parameters_t p_;
     fa_cp_gb300_options_t o_;
     HostQP H_;
+    HostCsr Qt_; /* Q' for the column statistics of the equilibration */
+    int *qt_rp_ = nullptr, *qt_ci_ = nullptr;
+    double *qt_v_ = nullptr;
+    double transpose_sec_ = 0.0;
     int qtype_ = Q_NONE;
     DevMat M_[NMAT];
     Arena arena_;
@@ -371,26 +368,13 @@ void FacpSolver::prepare() {
     }
     const double t0 = now_sec();
     HostCsr At = csr_transpose(P.m, P.n, P.A.rp.data(), P.A.ci.data(), P.A.v.data());
-    HostCsr Qt = csr_transpose(P.n, P.n, P.Q.rp.data(), P.Q.ci.data(), P.Q.v.data());
-    equilibrate(P, At, Qt, p_);
-    rescale_sec_ = now_sec() - t0;
+    Qt_ = csr_transpose(P.n, P.n, P.Q.rp.data(), P.Q.ci.data(), P.Q.v.data());
+    transpose_sec_ = now_sec() - t0;
     qtype_ = detect_q_type(P.Q, P.R);
-    if (qtype_ == Q_DIAG) { /* solver_state.cu:252-270, 478-492 */
-        diag_.assign(P.n, 0.0);
-        for (int i = 0; i < P.n; ++i)
-            for (int k = P.Q.rp[i]; k < P.Q.rp[i + 1]; ++k)
-                if (P.Q.ci[k] < P.n) diag_[P.Q.ci[k]] = P.Q.v[k] + 1e-12;
-        double mx = 0.0, mn = 0.0;
-        for (double d : diag_) {
-            mx = std::fmax(mx, std::fabs(d));
-            mn = std::fmin(mn, d);
-        }
-        qnorm_ = mx;
-        nonconvexity_ = mn;
-    }
-    M_[MAT_A].h = P.A;
+    /* unscaled values: equilibration runs on the device after the upload */
+    M_[MAT_A].h = std::move(P.A);
     M_[MAT_AT].h = std::move(At);
-    M_[MAT_Q].h = P.Q;
+    M_[MAT_Q].h = std::move(P.Q);
     M_[MAT_R].h = P.R;
     M_[MAT_RT].h = csr_transpose(P.nr, P.n, P.R.rp.data(), P.R.ci.data(), P.R.v.data());
     M_[MAT_A].h.nr = P.m;
@@ -407,6 +391,7 @@ void FacpSolver::prepare() {
 }
 
 void FacpSolver::upload() {
+    const double t_up = now_sec();
     const HostQP &H = H_;
     const size_t n = H.n, m = H.m, nr = H.nr;
     int dev = 0;
@@ -456,6 +441,9 @@ void FacpSolver::upload() {
             *p = arena_.take<double>(n);
         for (double **p : {&P_.y0, &P_.y, &P_.yh, &P_.ybar, &P_.dy, &P_.aldual, &P_.out_y})
             *p = arena_.take<double>(std::max<size_t>(m, 1));
+        qt_rp_ = arena_.take<int>(Qt_.rp.size());
+        qt_ci_ = arena_.take<int>(std::max<size_t>(Qt_.ci.size(), 1));
+        qt_v_ = arena_.take<double>(std::max<size_t>(Qt_.v.size(), 1));
         P_.rx = arena_.take<double>(std::max<size_t>(nr, 1));
         P_.pv = arena_.take<double>(vec);
         P_.pv2 = arena_.take<double>(vec);
@@ -487,31 +475,19 @@ void FacpSolver::upload() {
     P_.m = H.m;
     P_.nr = H.nr;
     P_.qtype = qtype_;
-    std::vector<double> fin(n);
+    h2d(qt_rp_, Qt_.rp.data(), Qt_.rp.size() * sizeof(int));
+    h2d(qt_ci_, Qt_.ci.data(), Qt_.ci.size() * sizeof(int));
+    h2d(qt_v_, Qt_.v.data(), Qt_.v.size() * sizeof(double));
     h2d(P_.c, H.c.data(), n * 8);
     h2d(P_.vlb, H.vlb.data(), n * 8);
     h2d(P_.vub, H.vub.data(), n * 8);
-    std::vector<double> vlf(n), vuf(n);
-    for (size_t i = 0; i < n; ++i) {
-        vlf[i] = std::isfinite(H.vlb[i]) ? H.vlb[i] : 0.0;
-        vuf[i] = std::isfinite(H.vub[i]) ? H.vub[i] : 0.0;
-    }
-    h2d(P_.vlb_fin, vlf.data(), n * 8);
-    h2d(P_.vub_fin, vuf.data(), n * 8);
-    if (qtype_ == Q_DIAG) h2d(P_.diag, diag_.data(), n * 8);
-    h2d(P_.dcum, H.dcum.data(), n * 8);
     if (m > 0) {
-        std::vector<double> clf(m), cuf(m);
-        for (size_t i = 0; i < m; ++i) {
-            clf[i] = std::isfinite(H.clb[i]) ? H.clb[i] : 0.0;
-            cuf[i] = std::isfinite(H.cub[i]) ? H.cub[i] : 0.0;
-        }
         h2d(P_.clb, H.clb.data(), m * 8);
         h2d(P_.cub, H.cub.data(), m * 8);
-        h2d(P_.clb_fin, clf.data(), m * 8);
-        h2d(P_.cub_fin, cuf.data(), m * 8);
-        h2d(P_.rcum, H.rcum.data(), m * 8);
     }
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    upload_sec_ = now_sec() - t_up;
+    equilibrate_device();
     /* iterates: zero, or the scaled warm start (solver_state.cu:621-656) */
     for (double *p : {P_.x0, P_.x, P_.xh, P_.xbar, P_.dprod, P_.dslack, P_.dx, P_.qx, P_.grad, P_.dir})
         PDAL_CUDA(cudaMemsetAsync(p, 0, n * 8, stream_));
@@ -606,6 +582,108 @@ void FacpSolver::power_iterations() {
     }
     pw_ = p_.bound_objective_rescaling ? 1.0 : (H.obj_norm + 1.0) / (H.bnd_norm + 1.0);
     best_pw_ = pw_;
+}
+
+void FacpSolver::equilibrate_device() {
+    const double t0 = now_sec();
+    HostQP &H = H_;
+    const int n = H.n, m = H.m, nr = H.nr;
+    auto grid = [&](long long len) {
+        return (int)std::max<long long>(1, std::min<long long>(152 * 16, (len + 255) / 256));
+    };
+    const int gv = grid(std::max(n, m));
+    double *cr = P_.pv, *vr = P_.pv2;
+    k_fill<<<grid(n), 256, 0, stream_>>>(n, (double *)P_.dcum, 1.0);
+    if (m) k_fill<<<grid(m), 256, 0, stream_>>>(m, (double *)P_.rcum, 1.0);
+    const DMat &A = P_.M[MAT_A], &At = P_.M[MAT_AT], &Q = P_.M[MAT_Q], &R = P_.M[MAT_R], &Rt = P_.M[MAT_RT];
+    const bool has_q = !Qt_.ci.empty(), has_r = !M_[MAT_R].h.ci.empty();
+    auto pass = [&](int mode, double deg_rows, double deg_cols) {
+        if (m) k_row_stat<<<grid(m), 256, 0, stream_>>>(m, A.rp, A.v, mode, deg_rows, cr, 0);
+        k_row_stat<<<grid(n), 256, 0, stream_>>>(n, At.rp, At.v, mode, deg_cols, vr, 0);
+        if (has_q) k_row_stat<<<grid(n), 256, 0, stream_>>>(n, qt_rp_, qt_v_, mode, deg_cols, vr, 1);
+        k_finish_scale<<<grid(n), 256, 0, stream_>>>(n, vr, (double *)P_.dcum);
+        if (m) k_finish_scale<<<grid(m), 256, 0, stream_>>>(m, cr, (double *)P_.rcum);
+        k_scale_vectors<<<gv, 256, 0, stream_>>>(n, m, (double *)P_.c, (double *)P_.vlb, (double *)P_.vub,
+                                                 (double *)P_.clb, (double *)P_.cub, vr, cr);
+        if (m) k_scale_csr<<<grid(m), 256, 0, stream_>>>(m, A.rp, A.ci, (double *)A.v, cr, vr);
+        k_scale_csr<<<grid(n), 256, 0, stream_>>>(n, At.rp, At.ci, (double *)At.v, vr, cr);
+        if (has_q) {
+            k_scale_csr<<<grid(n), 256, 0, stream_>>>(n, Q.rp, Q.ci, (double *)Q.v, vr, vr);
+            k_scale_csr<<<grid(n), 256, 0, stream_>>>(n, qt_rp_, qt_ci_, qt_v_, vr, vr);
+        }
+        if (has_r) {
+            k_scale_csr<<<grid(nr), 256, 0, stream_>>>(nr, R.rp, R.ci, (double *)R.v, nullptr, vr);
+            k_scale_csr<<<grid(n), 256, 0, stream_>>>(n, Rt.rp, Rt.ci, (double *)Rt.v, vr, nullptr);
+        }
+        PDAL_CUDA(cudaGetLastError());
+        launches_ += 8;
+    };
+    for (int it = 0; it < p_.l_inf_ruiz_iterations; ++it) pass(0, 0.0, 0.0);
+    if (p_.has_pock_chambolle_alpha) pass(1, p_.pock_chambolle_alpha, 2.0 - p_.pock_chambolle_alpha);
+    /* bound/objective scaling: the two norms are summed on the host in the
+     * reference's loop order (preconditioner.c:245-289) */
+    H.dcum.resize(n);
+    H.rcum.resize(m);
+    std::vector<double> c(n), lo(m), up(m);
+    PDAL_CUDA(cudaMemcpyAsync(c.data(), P_.c, (size_t)n * 8, cudaMemcpyDeviceToHost, stream_));
+    PDAL_CUDA(cudaMemcpyAsync(H.dcum.data(), P_.dcum, (size_t)n * 8, cudaMemcpyDeviceToHost, stream_));
+    if (m) {
+        PDAL_CUDA(cudaMemcpyAsync(lo.data(), P_.clb, (size_t)m * 8, cudaMemcpyDeviceToHost, stream_));
+        PDAL_CUDA(cudaMemcpyAsync(up.data(), P_.cub, (size_t)m * 8, cudaMemcpyDeviceToHost, stream_));
+        PDAL_CUDA(cudaMemcpyAsync(H.rcum.data(), P_.rcum, (size_t)m * 8, cudaMemcpyDeviceToHost, stream_));
+    }
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    if (p_.bound_objective_rescaling) {
+        double bsq = 0.0, csq = 0.0;
+        for (int i = 0; i < m; ++i) {
+            if (std::isfinite(lo[i]) && lo[i] != up[i]) bsq += lo[i] * lo[i];
+            if (std::isfinite(up[i])) bsq += up[i] * up[i];
+        }
+        for (int i = 0; i < n; ++i) csq += c[i] * c[i];
+        H.cbr = 1.0 / (std::sqrt(bsq) + 1.0);
+        H.ovr = 1.0 / (std::sqrt(csq) + 1.0);
+        k_bound_objective<<<gv, 256, 0, stream_>>>(n, m, H.cbr, H.ovr, (double *)P_.c, (double *)P_.vlb,
+                                                   (double *)P_.vub, (double *)P_.clb, (double *)P_.cub);
+        if (has_q) k_mul<<<grid((long long)M_[MAT_Q].h.ci.size()), 256, 0, stream_>>>(
+            (long long)M_[MAT_Q].h.ci.size(), (double *)Q.v, H.ovr / H.cbr);
+        if (has_r) {
+            const double f = std::sqrt(H.ovr / H.cbr);
+            k_mul<<<grid((long long)M_[MAT_R].h.ci.size()), 256, 0, stream_>>>((long long)M_[MAT_R].h.ci.size(),
+                                                                               (double *)R.v, f);
+            k_mul<<<grid((long long)M_[MAT_RT].h.ci.size()), 256, 0, stream_>>>((long long)M_[MAT_RT].h.ci.size(),
+                                                                                (double *)Rt.v, f);
+        }
+        launches_ += 4;
+    } else {
+        H.cbr = H.ovr = 1.0;
+    }
+    /* finite parts of the bounds, and the diagonal of a diagonal Q */
+    k_finite<<<grid(n), 256, 0, stream_>>>(n, P_.vlb, (double *)P_.vlb_fin);
+    k_finite<<<grid(n), 256, 0, stream_>>>(n, P_.vub, (double *)P_.vub_fin);
+    if (m) {
+        k_finite<<<grid(m), 256, 0, stream_>>>(m, P_.clb, (double *)P_.clb_fin);
+        k_finite<<<grid(m), 256, 0, stream_>>>(m, P_.cub, (double *)P_.cub_fin);
+    }
+    launches_ += 4;
+    if (qtype_ == Q_DIAG) { /* solver_state.cu:252-270, 478-492 */
+        k_fill<<<grid(n), 256, 0, stream_>>>(n, (double *)P_.diag, 0.0);
+        k_diag<<<grid(n), 256, 0, stream_>>>(n, n, Q.rp, Q.ci, Q.v, (double *)P_.diag);
+        diag_.resize(n);
+        PDAL_CUDA(cudaMemcpyAsync(diag_.data(), P_.diag, (size_t)n * 8, cudaMemcpyDeviceToHost, stream_));
+        launches_ += 2;
+    }
+    PDAL_CUDA(cudaGetLastError());
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    if (qtype_ == Q_DIAG) {
+        double mx = 0.0, mn = 0.0;
+        for (double d : diag_) {
+            mx = std::fmax(mx, std::fabs(d));
+            mn = std::fmin(mn, d);
+        }
+        qnorm_ = mx;
+        nonconvexity_ = mn;
+    }
+    rescale_sec_ = transpose_sec_ + (now_sec() - t0);
 }
 
 void FacpSolver::evaluate(bool infeas) {
@@ -857,9 +935,7 @@ void FacpSolver::print_eval() const {
 fa_cp_result_t *FacpSolver::run() {
     const double t_begin = now_sec();
     prepare();
-    const double t_up = now_sec();
     upload();
-    upload_sec_ = now_sec() - t_up;
     /* solver state */
     al_available_ = p_.use_al_qp;
     use_al_ = p_.use_al_qp;
@@ -1058,6 +1134,30 @@ fa_cp_result_t *solve_qp_problem(const qp_problem_t *prob, const fa_cp_parameter
 fa_cp_result_t *fa_cp_gb300_solve(const qp_problem_t *prob, const fa_cp_parameters_t *params,
                                   const fa_cp_gb300_options_t *opts) {
     return pdal::solve_guarded(prob, params, opts);
+}
+
+int fa_cp_gb300_scaling(const qp_problem_t *prob, const fa_cp_parameters_t *params,
+                        const fa_cp_gb300_options_t *opts, double *dcum, double *rcum, double *cbr_ovr) {
+    pdal::g_error.clear();
+    fa_cp_parameters_t p;
+    if (params)
+        p = *params;
+    else
+        set_default_parameters(&p);
+    fa_cp_gb300_options_t o;
+    if (opts)
+        o = *opts;
+    else
+        fa_cp_gb300_default_options(&o);
+    try {
+        pdal::FacpSolver s(prob, p, o);
+        s.scaling(dcum, rcum, cbr_ovr);
+        return 0;
+    } catch (const std::exception &e) {
+        pdal::g_error = e.what();
+        fprintf(stderr, "[fa_cp_gb300] %s\n", e.what());
+        return -1;
+    }
 }
 
 void fa_cp_gb300_last_stats(fa_cp_gb300_stats_t *stats) {

@@ -274,3 +274,20 @@ def solve(data: QPData, params: dict | N.FacpParameters | None = None,
             lib.fa_cp_result_free(rp)
     finally:
         prob.close()
+
+
+def scaling(data: QPData, params: dict | N.FacpParameters | None = None,
+            options: dict | N.FacpOptions | None = None):
+    """The device equilibration alone (fa_cp_gb300_scaling): column scales,
+    row scales, cbr, ovr."""
+    lib = N.load_qp()
+    p = params if isinstance(params, N.FacpParameters) else apply_params(default_parameters(lib), params)
+    o = options if isinstance(options, N.FacpOptions) else apply_options(default_options(lib), options)
+    prob = _CProblem(lib, data)
+    try:
+        d, r, f = np.zeros(max(prob.n, 1)), np.zeros(max(prob.m, 1)), np.zeros(2)
+        if lib.fa_cp_gb300_scaling(prob.ptr, C.byref(p), C.byref(o), _ptr(d), _ptr(r), _ptr(f)) != 0:
+            raise RuntimeError("scaling failed: " + N.last_error(lib))
+        return d[:prob.n], r[:prob.m], float(f[0]), float(f[1])
+    finally:
+        prob.close()

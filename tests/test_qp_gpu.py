@@ -167,3 +167,38 @@ def test_deterministic_repeat():
     a = qp.solve(data, {"eps": 1e-6, "verbose": 0})
     b = qp.solve(data, {"eps": 1e-6, "verbose": 0})
     assert a.iterations == b.iterations and np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
+
+
+def _diag_qp(n=3000, m=1200, seed=5):
+    rng = np.random.default_rng(seed)
+    A = sp.random(m, n, density=8.0 / m, random_state=seed, format="csr") * 10.0 ** rng.uniform(-2, 2)
+    Q = sp.diags(rng.uniform(1e-3, 10.0, n)).tocsr()
+    b = A @ rng.uniform(-1, 1, n)
+    return QPData(rng.standard_normal(n) * 100, A, b - 1.0, b + np.where(rng.random(m) < 0.5, 0.0, np.inf),
+                  np.full(n, -5.0), np.where(rng.random(n) < 0.1, np.inf, 5.0), Q=Q)
+
+
+@pytest.mark.parametrize("case", ["sparse", "lowrank", "diag", "lp", "pc_half"])
+def test_device_equilibration_is_bit_identical_to_oracle(case):
+    """The device equilibration (Ruiz passes, Pock-Chambolle, bound/objective
+    scaling) gives the oracle's scale vectors bit for bit (the oracle follows
+    QP/FA_CP/src/preconditioner.c:92-331); with alpha = 0.5 the |a|^alpha
+    terms go through pow(), whose last bit may differ between the device and
+    the host library, so that case is compared at 1e-14."""
+    params = {"l_inf_ruiz_iterations": 10}
+    if case in ("sparse", "lowrank", "pc_half"):
+        data, _, _ = planted_qp(n=4000, m=2000, b_rows=1000, seed=31, q_form="lowrank" if case == "lowrank" else "sparse")
+    elif case == "diag":
+        data = _diag_qp()
+    else:
+        d = random_lp(800, 2000, 6, seed=4)
+        data = QPData(d.c, d.A, d.con_lb, d.con_ub, d.var_lb, d.var_ub)
+    if case == "pc_half":
+        params["pock_chambolle_alpha"] = 0.5
+    g = qp.scaling(data, params)
+    o = O.qp_scaling(data, params)
+    for a, b in zip(g, o):
+        if case == "pc_half":
+            np.testing.assert_allclose(a, b, rtol=1e-14, atol=0)
+        else:
+            assert np.array_equal(np.asarray(a), np.asarray(b)), case

@@ -380,7 +380,9 @@ def bench_batch(local, count=4096, rank=0, world=1, barrier=None, max_over_ranks
         out[tag] = {"total_s": wall, "kernel_s": st["kernel_sec"], "solves_per_s": count / wall,
                     "optimal": st["optimal"], "iterations_p50": st["iterations_p50"],
                     "iterations_p99": st["iterations_p99"], "iterations_max": st["iterations_max"],
-                    "max_kkt": max(r.kkt for r in res), "grid_blocks": st["grid_blocks"]}
+                    "max_kkt": max(r.kkt for r in res), "grid_blocks": st["grid_blocks"],
+                    "schedule": {"block_nnz": st["block_nnz"], "blocks_per_sm": st["blocks_per_sm"],
+                                 "tune_s": st["tune_sec"]}}
     if rank != 0:
         return out
     idx = [int(i) for i in np.linspace(0, count - 1, 48)]

@@ -61,13 +61,20 @@ typedef struct {
     int precision;                /* cp_al_gb300_precision_t */
     double fp32_switch_tol;       /* FP32 phase ends when rel KKT < this (default 1e-5) */
     int fp32_max_iterations;      /* FP32 phase iteration cap (default: none, -1) */
-    int spmv_nnz_per_block;       /* row-block nonzero budget; 0 = autotune */
+    int spmv_nnz_per_block;       /* row-block nonzero budget; 0 = automatic (single LP: by
+                                     size; batch: autotuned, see batch_blocks_per_sm) */
     int device;                   /* CUDA device ordinal, -1 = current */
     int graph_blocks;             /* evaluation blocks per host check (default 1) */
     int timing;                   /* 1: time one primal and one dual launch per
                                      block with CUDA events (stats avg_*_ms) */
     int fp32_stall_evals;         /* FP32 phase ends after this many evaluations
                                      without halving its best KKT error (default 25) */
+    int batch_blocks_per_sm;      /* batch: resident blocks per SM (2-4); 0 = autotune.
+                                     When this or spmv_nnz_per_block is 0, the batch
+                                     solver times each candidate schedule (row-block
+                                     budget 1,024 / 2,048 x 2-4 blocks per SM) on a probe
+                                     of the largest instances (200 iterations) and keeps
+                                     the fastest, remembered per batch shape */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */
@@ -145,6 +152,9 @@ typedef struct {
     int iterations_p50, iterations_p99, iterations_max;
     long long total_iterations;
     long long device_bytes;
+    int block_nnz;        /* schedule used: row-block nonzero budget */
+    int blocks_per_sm;    /* schedule used: resident blocks per SM */
+    double tune_sec;      /* time spent timing candidate schedules (0 when given or remembered) */
 } cp_al_gb300_batch_stats_t;
 
 /* Controller state of one instance at the end of its solve. */

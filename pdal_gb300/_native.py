@@ -189,6 +189,7 @@ class CpalOptions(C.Structure):
         ("graph_blocks", C.c_int),
         ("timing", C.c_int),
         ("fp32_stall_evals", C.c_int),
+        ("batch_blocks_per_sm", C.c_int),
     ]
 
 
@@ -238,6 +239,9 @@ class BatchStats(C.Structure):
         ("iterations_max", C.c_int),
         ("total_iterations", C.c_longlong),
         ("device_bytes", C.c_longlong),
+        ("block_nnz", C.c_int),
+        ("blocks_per_sm", C.c_int),
+        ("tune_sec", C.c_double),
     ]
 
 

@@ -23,17 +23,21 @@
 #include <random>
 #include <thread>
 #include <vector>
+#include <tuple>
+#include <map>
 
 namespace pdal {
 namespace {
 
 using namespace batch;
 
-/* resident blocks per SM of the persistent launch */
-constexpr int kBatchMinBlocks = 2;
-/* nonzeros per row block of the batch plans (measured on the 4,096-LP batch:
- * 2,048 nonzeros with 2 resident blocks per SM beat 1,024 with 2-4) */
-constexpr int kBatchBlockNnz = 2048;
+/* Candidate schedules of the persistent launch: row-block nonzero budget x
+ * resident blocks per SM (every pair has a kernel instantiation; 2,048 x 4
+ * does not fit the SM's shared memory). */
+struct Schedule {
+    int bs, minb;
+};
+constexpr Schedule kSchedules[] = {{2048, 2}, {2048, 3}, {1024, 2}, {1024, 3}, {1024, 4}};
 
 double now_sec() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -90,15 +94,13 @@ void run_threads(int count, const std::function<void(int)> &fn) {
     if (err) std::rethrow_exception(err);
 }
 
-int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t &P, const cp_al_gb300_options_t &O,
-                const double *sigma0, cp_al_result_t **results, cp_al_gb300_instance_info_t *info,
-                cp_al_gb300_batch_stats_t *stats) {
+int run_batch(int count, lp_problem_t *const *problems, const cp_al_parameters_t &P, const cp_al_gb300_options_t &O,
+              const double *sigma0, cp_al_result_t **results, cp_al_gb300_instance_info_t *info,
+              cp_al_gb300_batch_stats_t *stats, int bs, int minb) {
     const double t_begin = now_sec();
     if (count <= 0) throw Error("batch_solve: count must be positive");
     if (!problems || !results) throw Error("batch_solve: missing problem or result array");
     if (P.termination_evaluation_frequency < 3) throw Error("termination_evaluation_frequency must be >= 3");
-    int bs = kBatchBlockNnz;
-    if (const char *e = getenv("PDAL_BATCH_BLOCK_NNZ")) bs = atoi(e) == 2048 ? 2048 : 1024;
     std::vector<Prepared> prep(count);
     run_threads(count, [&](int i) {
         const lp_problem_t *q = problems[i];
@@ -357,13 +359,12 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
     int dev_id = 0, sms = 0, per_sm = 0;
     PDAL_CUDA(cudaGetDevice(&dev_id));
     PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
-    int minb = kBatchMinBlocks;
-    if (const char *e = getenv("PDAL_BATCH_MINB")) minb = std::max(2, std::min(4, atoi(e)));
     using KernT = void (*)(const BInst *, int, const int *, unsigned *, CpalParams, BOpts, BOut *);
     KernT kern;
     size_t dsm;
     if (bs == 2048) {
-        kern = minb >= 3 ? k_batch_lp<3, 2048> : k_batch_lp<2, 2048>;  /* 3: ~70 KB of staging each */
+        if (minb > 3) throw Error("batch_solve: 2,048-nonzero blocks fit at most 3 per SM");
+        kern = minb == 3 ? k_batch_lp<3, 2048> : k_batch_lp<2, 2048>; /* 3: ~70 KB of staging each */
         dsm = sizeof(BSmem<2048>);
     } else {
         kern = minb == 4 ? k_batch_lp<4, 1024> : (minb == 3 ? k_batch_lp<3, 1024> : k_batch_lp<2, 1024>);
@@ -456,8 +457,100 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
         stats->iterations_max = sorted.back();
         stats->total_iterations = total_iters;
         stats->device_bytes = (long long)total;
+        stats->block_nnz = bs;
+        stats->blocks_per_sm = minb;
     }
     return 0;
+}
+
+/* Schedules chosen for earlier batches of the same shape (instance count,
+ * nonzeros in total and in the largest instance, precision). */
+std::mutex g_sched_mu;
+std::map<std::tuple<int, long long, long long, int>, Schedule> g_sched;
+
+/*
+ * The autotuner: the largest instances bound the makespan (each runs on one
+ * block from start to end), so every candidate schedule solves the same probe
+ * -- the 2 x SMs largest instances, 200 iterations and at most 32 power
+ * iterations each -- and the fastest kernel time wins.  A schedule the caller
+ * fixes (spmv_nnz_per_block, batch_blocks_per_sm) restricts the candidates.
+ */
+Schedule tune_schedule(int count, lp_problem_t *const *problems, const cp_al_parameters_t &P,
+                       const cp_al_gb300_options_t &O, double &tune_sec) {
+    const int want_bs = O.spmv_nnz_per_block, want_mb = O.batch_blocks_per_sm;
+    if (want_bs != 0 && want_bs != 1024 && want_bs != 2048)
+        throw Error("batch_solve: spmv_nnz_per_block must be 0, 1024 or 2048");
+    if (want_mb != 0 && (want_mb < 2 || want_mb > 4)) throw Error("batch_solve: batch_blocks_per_sm must be 0 or 2-4");
+    std::vector<Schedule> cand;
+    for (const Schedule &c : kSchedules)
+        if ((want_bs == 0 || c.bs == want_bs) && (want_mb == 0 || c.minb == want_mb)) cand.push_back(c);
+    if (cand.empty()) throw Error("batch_solve: no schedule with 2,048-nonzero blocks at 4 blocks per SM");
+    tune_sec = 0.0;
+    if (cand.size() == 1) return cand[0];
+    long long tot = 0, mx = 0;
+    for (int i = 0; i < count; ++i) {
+        const long long w = problems[i] ? problems[i]->constraint_matrix_num_nonzeros : 0;
+        tot += w;
+        mx = std::max(mx, w);
+    }
+    const auto key = std::make_tuple(count, tot, mx, O.precision * 16 + want_bs / 1024 * 4 + want_mb);
+    {
+        std::lock_guard<std::mutex> lk(g_sched_mu);
+        auto it = g_sched.find(key);
+        if (it != g_sched.end()) return it->second;
+    }
+    const double t0 = now_sec();
+    int dev_id = 0, sms = 0;
+    if (O.device >= 0) PDAL_CUDA(cudaSetDevice(O.device));
+    PDAL_CUDA(cudaGetDevice(&dev_id));
+    PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
+    std::vector<int> idx(count);
+    for (int i = 0; i < count; ++i) idx[i] = i;
+    auto weight = [&](int i) {
+        return problems[i] ? (long long)problems[i]->constraint_matrix_num_nonzeros + problems[i]->num_variables : 0;
+    };
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return weight(a) > weight(b); });
+    const int k = std::min(count, 2 * sms);
+    std::vector<lp_problem_t *> probe(k);
+    for (int i = 0; i < k; ++i) probe[i] = problems[idx[i]];
+    cp_al_parameters_t pp = P;
+    pp.termination_criteria.iteration_limit = std::min(P.termination_criteria.iteration_limit, 200);
+    pp.sv_max_iter = std::min(P.sv_max_iter, 32);
+    std::vector<cp_al_result_t *> res(k, nullptr);
+    Schedule best = cand[0];
+    double best_t = INFINITY;
+    for (const Schedule &c : cand) {
+        cp_al_gb300_batch_stats_t st{};
+        run_batch(k, probe.data(), pp, O, nullptr, res.data(), nullptr, &st, c.bs, c.minb);
+        for (cp_al_result_t *&r : res) {
+            cp_al_result_free(r);
+            r = nullptr;
+        }
+        if (st.kernel_sec < best_t) {
+            best_t = st.kernel_sec;
+            best = c;
+        }
+    }
+    tune_sec = now_sec() - t0;
+    std::lock_guard<std::mutex> lk(g_sched_mu);
+    g_sched[key] = best;
+    return best;
+}
+
+int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t &P, const cp_al_gb300_options_t &O,
+                const double *sigma0, cp_al_result_t **results, cp_al_gb300_instance_info_t *info,
+                cp_al_gb300_batch_stats_t *stats) {
+    if (count <= 0) throw Error("batch_solve: count must be positive");
+    if (!problems || !results) throw Error("batch_solve: missing problem or result array");
+    double tune_sec = 0.0;
+    const Schedule sc = tune_schedule(count, problems, P, O, tune_sec);
+    const int rc = run_batch(count, problems, P, O, sigma0, results, info, stats, sc.bs, sc.minb);
+    if (stats) {
+        stats->tune_sec = tune_sec;
+        stats->total_sec += tune_sec;
+        stats->solves_per_sec = count / stats->total_sec;
+    }
+    return rc;
 }
 
 } // namespace

@@ -96,3 +96,27 @@ def test_batch_fp32_refine_matches_single_solver():
         # FP32 trajectories depend on the reduction order, so the iteration
         # counts of the two FP32 paths differ; both run an FP32 phase
         assert b.stats["fp32_iterations"] > 0
+
+
+def test_schedule_autotuner_and_fixed_schedules():
+    """Every schedule solves the batch to the same optimum; with no schedule
+    given the autotuner times the candidates once per batch shape and then
+    reuses its choice."""
+    items = batch_lps(count=40, seed=91, m_range=(100, 1500))
+    params = {"eps": 1e-7, "l_inf_ruiz_iterations": 4, "iteration_limit": 200000}
+    ref = None
+    for bs, mb in ((2048, 2), (2048, 3), (1024, 2), (1024, 3), (1024, 4)):
+        res, st = lp.solve_batch(items, params, {"spmv_nnz_per_block": bs, "batch_blocks_per_sm": mb})
+        assert (st["block_nnz"], st["blocks_per_sm"]) == (bs, mb) and st["tune_sec"] == 0.0
+        assert st["optimal"] == len(items)
+        obj = np.array([r.primal_objective for r in res])
+        if ref is None:
+            ref = obj
+        np.testing.assert_allclose(obj, ref, rtol=2e-7)
+    res, st = lp.solve_batch(items, params)
+    assert (st["block_nnz"], st["blocks_per_sm"]) in {(2048, 2), (2048, 3), (1024, 2), (1024, 3), (1024, 4)}
+    assert st["tune_sec"] > 0.0 and st["optimal"] == len(items)
+    res2, st2 = lp.solve_batch(items, params)
+    assert st2["tune_sec"] == 0.0 and (st2["block_nnz"], st2["blocks_per_sm"]) == (st["block_nnz"], st["blocks_per_sm"])
+    with pytest.raises(RuntimeError):
+        lp.solve_batch(items, params, {"spmv_nnz_per_block": 2048, "batch_blocks_per_sm": 4})

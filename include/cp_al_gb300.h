@@ -179,6 +179,14 @@ int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems, const cp_a
                             const cp_al_gb300_options_t *opts, const double *sigma0, cp_al_result_t **results,
                             cp_al_gb300_instance_info_t *info, cp_al_gb300_batch_stats_t *stats);
 
+/* Runs only the schedule autotuner of cp_al_gb300_batch_solve for this batch
+ * (a no-op when opts fix the schedule or the batch shape was tuned before)
+ * and reports the schedule in stats (block_nnz, blocks_per_sm, tune_sec); a
+ * later cp_al_gb300_batch_solve of a batch of the same shape reuses it.
+ * Returns 0, or -1 (message in cp_al_gb300_last_error). */
+int cp_al_gb300_batch_tune(int count, lp_problem_t *const *problems, const cp_al_parameters_t *params,
+                           const cp_al_gb300_options_t *opts, cp_al_gb300_batch_stats_t *stats);
+
 typedef struct cp_al_gb300_session cp_al_gb300_session_t;
 
 /* Uploads and prepares the problem (transpose, scaling, power iteration are

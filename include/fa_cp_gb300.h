@@ -28,6 +28,16 @@ typedef struct {
     double restart_select_margin;
     int restart_select_min_iters;
     double restart_select_min_time;
+    /* precision (options of this implementation): 0 = FP64 throughout (the
+     * reference's arithmetic); 1 = FP32 iteration segments -- products,
+     * projections, the BB inner solve and Halpern updates in FP32 with
+     * (hi, lo) anchors and FP64 reductions, evaluation, restarts and
+     * termination in FP64 -- until the relative KKT error is below
+     * fp32_switch_tol or has not halved over fp32_stall_evals evaluations,
+     * then FP64 from that iterate (the refinement phase) */
+    int precision;
+    double fp32_switch_tol;  /* default 1e-5 */
+    int fp32_stall_evals;    /* default 25 */
 } fa_cp_gb300_options_t;
 
 typedef struct {
@@ -46,11 +56,12 @@ typedef struct {
     double primal_weight;
     double step_size;
     double device_loop_ms;     /* device time of the iteration segments (CUDA events) */
-    double equilibration_sec;  /* host equilibration */
-    double upload_sec;         /* plans, transposes, device arena and copies */
+    double equilibration_sec;  /* transposes on the host and equilibration on the device */
+    double upload_sec;         /* plans, device arena and copies */
     double power_sec;          /* power iterations (sigma_max(A), eigenvalues of Q) */
     int power_iterations_a;
     int power_iterations_q;
+    int fp32_iterations;       /* iterations run in FP32 segments (precision 1) */
 } fa_cp_gb300_stats_t;
 
 /* Defaults: current device, automatic grid and block budget, restart to the
@@ -60,7 +71,8 @@ void fa_cp_gb300_default_options(fa_cp_gb300_options_t *opts);
 /* The options solve_qp_problem uses: the defaults, overridden by the
  * environment variables the reference reads (FA_CP_RESTART_SELECT, with
  * FA_CP_RESTART_SELECT_LEGACY as fallback, FA_CP_RESTART_SELECT_MARGIN,
- * FA_CP_RESTART_SELECT_MIN_ITERS, FA_CP_RESTART_SELECT_MIN_TIME). */
+ * FA_CP_RESTART_SELECT_MIN_ITERS, FA_CP_RESTART_SELECT_MIN_TIME) and by
+ * FA_CP_GB300_PRECISION ("fp64" or "fp32_refine", this implementation's). */
 void fa_cp_gb300_options_from_env(fa_cp_gb300_options_t *opts);
 
 /* solve_qp_problem with explicit options; params == NULL selects the

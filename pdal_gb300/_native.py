@@ -291,6 +291,11 @@ LP_SYMBOLS = {
          C.POINTER(C.POINTER(CpalResult)), C.POINTER(InstanceInfo), C.POINTER(BatchStats)],
     ),
     "read_mps_file": (C.POINTER(LpProblem), [C.c_char_p]),
+    "cp_al_gb300_batch_tune": (
+        C.c_int,
+        [C.c_int, C.POINTER(C.POINTER(LpProblem)), C.POINTER(CpalParameters), C.POINTER(CpalOptions),
+         C.POINTER(BatchStats)],
+    ),
     "cp_al_gb300_primal_kkt_noalloc": (
         C.c_int,
         [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -436,6 +441,9 @@ class FacpOptions(C.Structure):
         ("restart_select_margin", C.c_double),
         ("restart_select_min_iters", C.c_int),
         ("restart_select_min_time", C.c_double),
+        ("precision", C.c_int),
+        ("fp32_switch_tol", C.c_double),
+        ("fp32_stall_evals", C.c_int),
     ]
 
 
@@ -461,6 +469,7 @@ class FacpStats(C.Structure):
         ("power_sec", C.c_double),
         ("power_iterations_a", C.c_int),
         ("power_iterations_q", C.c_int),
+        ("fp32_iterations", C.c_int),
     ]
 
 

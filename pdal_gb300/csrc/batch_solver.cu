@@ -471,7 +471,7 @@ std::map<std::tuple<int, long long, long long, int>, Schedule> g_sched;
 /*
  * The autotuner: the largest instances bound the makespan (each runs on one
  * block from start to end), so every candidate schedule solves the same probe
- * -- the 2 x SMs largest instances, 200 iterations and at most 32 power
+ * -- the SM-count largest instances, 100 iterations and at most 8 power
  * iterations each -- and the fastest kernel time wins.  A schedule the caller
  * fixes (spmv_nnz_per_block, batch_blocks_per_sm) restricts the candidates.
  */
@@ -510,12 +510,12 @@ Schedule tune_schedule(int count, lp_problem_t *const *problems, const cp_al_par
         return problems[i] ? (long long)problems[i]->constraint_matrix_num_nonzeros + problems[i]->num_variables : 0;
     };
     std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return weight(a) > weight(b); });
-    const int k = std::min(count, 2 * sms);
+    const int k = std::min(count, sms);
     std::vector<lp_problem_t *> probe(k);
     for (int i = 0; i < k; ++i) probe[i] = problems[idx[i]];
     cp_al_parameters_t pp = P;
-    pp.termination_criteria.iteration_limit = std::min(P.termination_criteria.iteration_limit, 200);
-    pp.sv_max_iter = std::min(P.sv_max_iter, 32);
+    pp.termination_criteria.iteration_limit = std::min(P.termination_criteria.iteration_limit, 100);
+    pp.sv_max_iter = std::min(P.sv_max_iter, 8);
     std::vector<cp_al_result_t *> res(k, nullptr);
     Schedule best = cand[0];
     double best_t = INFINITY;
@@ -555,6 +555,37 @@ int batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters
 
 } // namespace
 } // namespace pdal
+
+extern "C" int cp_al_gb300_batch_tune(int count, lp_problem_t *const *problems, const cp_al_parameters_t *params,
+                                      const cp_al_gb300_options_t *opts, cp_al_gb300_batch_stats_t *stats) {
+    pdal::clear_last_error();
+    cp_al_parameters_t p;
+    if (params)
+        p = *params;
+    else
+        set_default_parameters(&p);
+    cp_al_gb300_options_t o;
+    if (opts)
+        o = *opts;
+    else
+        cp_al_gb300_default_options(&o);
+    try {
+        if (count <= 0 || !problems) throw pdal::Error("batch_tune: no problems");
+        double t = 0.0;
+        const pdal::Schedule sc = pdal::tune_schedule(count, problems, p, o, t);
+        if (stats) {
+            memset(stats, 0, sizeof(*stats));
+            stats->instances = count;
+            stats->block_nnz = sc.bs;
+            stats->blocks_per_sm = sc.minb;
+            stats->tune_sec = t;
+        }
+        return 0;
+    } catch (const std::exception &e) {
+        pdal::set_last_error(e.what());
+        return -1;
+    }
+}
 
 extern "C" int cp_al_gb300_batch_solve(int count, lp_problem_t *const *problems, const cp_al_parameters_t *params,
                                        const cp_al_gb300_options_t *opts, const double *sigma0,

@@ -344,6 +344,9 @@ void fa_cp_gb300_default_options(fa_cp_gb300_options_t *o) {
     o->restart_select_margin = 1.0;
     o->restart_select_min_iters = 0;
     o->restart_select_min_time = 0.0;
+    o->precision = 0;
+    o->fp32_switch_tol = 1e-5;
+    o->fp32_stall_evals = 25;
 }
 
 static const char *env_value(const char *primary, const char *fallback) {
@@ -371,6 +374,8 @@ void fa_cp_gb300_options_from_env(fa_cp_gb300_options_t *o) { /* fa_cp_core_op.c
         else
             o->restart_select_margin = d;
     }
+    v = env_value("FA_CP_GB300_PRECISION", nullptr);
+    if (v && strcmp(v, "fp32_refine") == 0) o->precision = 1;
 }
 
 } // extern "C"

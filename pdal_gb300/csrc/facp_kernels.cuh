@@ -91,6 +91,29 @@ struct Ctl {
     int pad2;
 };
 
+/* The segment (iteration) path runs in T: FP64, or FP32 in the first phase
+ * of the chosen form.  SegV<T> holds what that path reads and writes in T;
+ * in FP32 the Halpern anchors stay FP64-accurate as unevaluated (hi, lo)
+ * float pairs, and every reduction still accumulates in FP64.  The FP64
+ * vectors of Prob are the state between launches: an FP32 segment converts
+ * them in at its start and back at its end. */
+template <typename T>
+struct AnchorOf {
+    using type = double;
+};
+template <>
+struct AnchorOf<float> {
+    using type = float2;
+};
+
+template <typename T>
+struct SegV {
+    const T *c, *vlb, *vub, *clb, *cub, *diag;
+    T *x, *xh, *xbar, *y, *yh, *ybar, *dprod, *dslack, *dx, *dy, *qx, *rx, *grad, *dir, *aldual;
+    typename AnchorOf<T>::type *x0, *y0;
+    const T *mv[NMAT]; /* matrix values */
+};
+
 struct Prob {
     int n, m, nr, qtype;
     DMat M[NMAT];
@@ -105,6 +128,7 @@ struct Prob {
     GridBar *bar;
     Ctl *ctl;
     double *out_x, *out_y, *out_rc;
+    SegV<float> f; /* FP32 mirror (chosen form only; null pointers otherwise) */
 };
 
 struct Args {
@@ -113,6 +137,7 @@ struct Args {
     int fp_first, has_inner, inner_limit, use_al;
     int linf, infeas;
     int max_iter;
+    int fp32; /* MODE_SEGMENT: run the segment in FP32 */
     double tau, rho, step, pw, sigma, refl;
     double tau_eval;
     double cbr, ovr, c0, obj_norm, bnd_norm;
@@ -142,6 +167,7 @@ struct Cx {
     const Prob &P;
     const Args &a;
     RowBlockSmem<kS, 1, double> &sm;
+    RowBlockSmem<kS, 1, float> &smf; /* the same shared bytes, typed for FP32 */
     double *stot; /* shared: totals of the last reduction */
     int *sok;     /* shared: barrier status */
     unsigned nb;
@@ -260,7 +286,23 @@ __device__ bool greduce(Cx &cx, Red<NS, NM> &r, unsigned lmask, double (&tot)[NS
     return true;
 }
 
-/* Runs the row blocks of M owned by this block. */
+/* Runs the row blocks of matrix `mat` owned by this block, with values `val`
+ * in the arithmetic type T. */
+template <typename T, class Gat, class Epi, class R>
+__device__ __forceinline__ void spmv_t(Cx &cx, int mat, const T *val, Gat &gat, Epi &epi, R &red) {
+    const DMat &M = cx.P.M[mat];
+    RowBlockSmem<kS, 1, T> *sm;
+    if constexpr (sizeof(T) == sizeof(double))
+        sm = &cx.sm;
+    else
+        sm = &cx.smf;
+    for (int b = blockIdx.x; b < M.plan.nblocks; b += gridDim.x) {
+        rowblock_run_at<kS, 1, T>(b, M.plan, M.rp, M.ci, val, gat, epi, red, *sm);
+        __syncthreads();
+    }
+}
+
+/* FP64 products of the evaluation, restart and power paths. */
 template <class Gat, class Epi, class R>
 __device__ __forceinline__ void spmv(Cx &cx, const DMat &M, Gat &gat, Epi &epi, R &red) {
     for (int b = blockIdx.x; b < M.plan.nblocks; b += gridDim.x) {
@@ -269,10 +311,12 @@ __device__ __forceinline__ void spmv(Cx &cx, const DMat &M, Gat &gat, Epi &epi, 
     }
 }
 
-struct Gat {
-    const double *v;
-    __device__ __forceinline__ void operator()(int col, double (&o)[1]) const { o[0] = v[col]; }
+template <typename T>
+struct GatT {
+    const T *v;
+    __device__ __forceinline__ void operator()(int col, T (&o)[1]) const { o[0] = v[col]; }
 };
+using Gat = GatT<double>;
 
 template <class F>
 __device__ __forceinline__ void foreach_elem(const Cx &cx, int count, F f) {
@@ -280,11 +324,13 @@ __device__ __forceinline__ void foreach_elem(const Cx &cx, int count, F f) {
 }
 
 /* Epilogue that stores the row sum (no reduction terms). */
-struct EpiStore {
-    double *out;
-    __device__ __forceinline__ void operator()(int row, const double (&s)[1], Red<1, 0> &) const { out[row] = s[0]; }
+template <typename T>
+struct EpiStoreT {
+    T *out;
+    __device__ __forceinline__ void operator()(int row, const T (&s)[1], Red<1, 0> &) const { out[row] = s[0]; }
     __device__ __forceinline__ void long_red(int, Red<1, 0> &) const {}
 };
+using EpiStore = EpiStoreT<double>;
 
 /* Adds the long-row reduction terms of `lr` to the row's slot. */
 template <int NS, int NM>
@@ -296,25 +342,80 @@ __device__ __forceinline__ void add_long(const Cx &cx, int mat, int lid, const R
     for (int i = 0; i < NM; ++i) s[NS + i] = fmax(s[NS + i], lr.mx[i]);
 }
 
+__device__ __forceinline__ double tmax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ double tmin(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float tmax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ float tmin(float a, float b) { return fminf(a, b); }
+
+/* Halpern average w * r + (1 - w) * anchor; the FP32 form keeps the anchor
+ * as (hi, lo) and adds both parts (FP64-accurate anchor, FP32 arithmetic). */
+__device__ __forceinline__ double halpern_avg(double w, double rv, double a) { return w * rv + (1.0 - w) * a; }
+__device__ __forceinline__ float halpern_avg(float w, float rv, float2 a) {
+    const float omw = 1.0f - w;
+    return fmaf(w, rv, fmaf(omw, a.x, omw * a.y));
+}
+__device__ __forceinline__ float2 split_anchor(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+
+__device__ __forceinline__ SegV<double> seg64(const Prob &P) {
+    SegV<double> v;
+    v.c = P.c;
+    v.vlb = P.vlb;
+    v.vub = P.vub;
+    v.clb = P.clb;
+    v.cub = P.cub;
+    v.diag = P.diag;
+    v.x = P.x;
+    v.xh = P.xh;
+    v.xbar = P.xbar;
+    v.y = P.y;
+    v.yh = P.yh;
+    v.ybar = P.ybar;
+    v.dprod = P.dprod;
+    v.dslack = P.dslack;
+    v.dx = P.dx;
+    v.dy = P.dy;
+    v.qx = P.qx;
+    v.rx = P.rx;
+    v.grad = P.grad;
+    v.dir = P.dir;
+    v.aldual = P.aldual;
+    v.x0 = P.x0;
+    v.y0 = P.y0;
+    for (int k = 0; k < NMAT; ++k) v.mv[k] = P.M[k].v;
+    return v;
+}
+
 /* ------------------------------------------------------------------ objective product */
+
+/* In the LOW_RANK_SPARSE form the R'R v row sum is added to the stored Q v
+ * (cuSPARSE's beta = 1 accumulation in the reference); every other form
+ * passes the row sum through. */
+template <typename T>
+__device__ __forceinline__ T q_total_t(int qtype, const T *qx, int j, T s) {
+    return qtype == Q_LOWRANK_SPARSE ? s + qx[j] : s;
+}
+__device__ __forceinline__ double q_total(const Prob &P, int j, double s) { return q_total_t(P.qtype, P.qx, j, s); }
 
 /* y = Q v for the objective term (solver_state.cu:371-442 of the reference):
  * SPARSE Q v; DIAG d.*v; LOW_RANK R'(R v); LOW_RANK_SPARSE Q v + R'(R v).
  * The final product of each row goes through `epi` (which may fuse more work);
- * `qtmp` receives Q v first in the LOW_RANK_SPARSE form. */
-template <class Epi, class R>
-__device__ bool obj_product(Cx &cx, const double *v, Epi &epi, R &red, unsigned &lmask) {
+ * `qx` receives Q v first in the LOW_RANK_SPARSE form. */
+template <typename T, class Epi, class R>
+__device__ bool obj_product_t(Cx &cx, const SegV<T> &V, const T *v, Epi &epi, R &red, unsigned &lmask) {
     const Prob &P = cx.P;
     switch (P.qtype) {
     case Q_SPARSE: {
-        Gat g{v};
-        spmv(cx, P.M[MAT_Q], g, epi, red);
+        GatT<T> g{v};
+        spmv_t<T>(cx, MAT_Q, V.mv[MAT_Q], g, epi, red);
         lmask |= 1u << MAT_Q;
         return true;
     }
     case Q_DIAG: {
         foreach_elem(cx, P.n, [&](int j) {
-            const double s[1] = {P.diag[j] * v[j]};
+            const T s[1] = {V.diag[j] * v[j]};
             epi(j, s, red);
         });
         return true;
@@ -323,107 +424,113 @@ __device__ bool obj_product(Cx &cx, const double *v, Epi &epi, R &red, unsigned 
     case Q_LOWRANK_SPARSE: {
         Red<1, 0> dummy;
         if (P.qtype == Q_LOWRANK_SPARSE) {
-            Gat g{v};
-            EpiStore st{P.qx};
-            spmv(cx, P.M[MAT_Q], g, st, dummy);
+            GatT<T> g{v};
+            EpiStoreT<T> st{V.qx};
+            spmv_t<T>(cx, MAT_Q, V.mv[MAT_Q], g, st, dummy);
         }
         {
-            Gat g{v};
-            EpiStore st{P.rx};
-            spmv(cx, P.M[MAT_R], g, st, dummy);
+            GatT<T> g{v};
+            EpiStoreT<T> st{V.rx};
+            spmv_t<T>(cx, MAT_R, V.mv[MAT_R], g, st, dummy);
         }
         FACP_SYNC(cx);
-        Gat g{P.rx};
-        spmv(cx, P.M[MAT_RT], g, epi, red);
+        GatT<T> g{(const T *)V.rx};
+        spmv_t<T>(cx, MAT_RT, V.mv[MAT_RT], g, epi, red);
         lmask |= 1u << MAT_RT;
         return true;
     }
     default: /* Q_NONE: the product buffer keeps its contents (zeros) */
         foreach_elem(cx, P.n, [&](int j) {
-            const double s[1] = {P.qx[j]};
+            const T s[1] = {V.qx[j]};
             epi(j, s, red);
         });
         return true;
     }
 }
 
-/* In the LOW_RANK_SPARSE form the R'R v row sum is added to the stored Q v
- * (cuSPARSE's beta = 1 accumulation in the reference); every other form
- * passes the row sum through. */
-__device__ __forceinline__ double q_total(const Prob &P, int j, double s) {
-    return P.qtype == Q_LOWRANK_SPARSE ? s + P.qx[j] : s;
+template <class Epi, class R>
+__device__ bool obj_product(Cx &cx, const double *v, Epi &epi, R &red, unsigned &lmask) {
+    const SegV<double> V = seg64(cx.P);
+    return obj_product_t<double>(cx, V, v, epi, red, lmask);
 }
 
 /* ------------------------------------------------------------------ iteration pieces */
 
 /* u = y - sigma (p - P(p - y/sigma)), p = A v   (fa_cp_core_op.cu:181-192, 275-303) */
+template <typename T>
 struct EpiAlDual {
-    const Prob *P;
-    double sigma;
-    __device__ __forceinline__ void operator()(int i, const double (&s)[1], Red<1, 0> &) const {
-        const double p = s[0];
-        const double yi = P->y[i];
-        const double shifted = p - yi / sigma;
-        const double proj = fmax(P->clb[i], fmin(shifted, P->cub[i]));
-        P->aldual[i] = yi - sigma * (p - proj);
+    const SegV<T> *V;
+    T sigma;
+    __device__ __forceinline__ void operator()(int i, const T (&s)[1], Red<1, 0> &) const {
+        const T p = s[0];
+        const T yi = V->y[i];
+        const T shifted = p - yi / sigma;
+        const T proj = tmax(V->clb[i], tmin(shifted, V->cub[i]));
+        V->aldual[i] = yi - sigma * (p - proj);
     }
     __device__ __forceinline__ void long_red(int, Red<1, 0> &) const {}
 };
 
 /* dprod = A' u with u = y (plain) or the AL effective dual at v. */
-__device__ bool dual_product(Cx &cx, const double *v, bool al) {
-    const Prob &P = cx.P;
+template <typename T>
+__device__ bool dual_product(Cx &cx, const SegV<T> &V, const T *v, bool al) {
     Red<1, 0> dummy;
-    const double *u = P.y;
+    const T *u = V.y;
     if (al) {
-        Gat g{v};
-        EpiAlDual e{&P, cx.a.sigma};
-        spmv(cx, P.M[MAT_A], g, e, dummy);
+        GatT<T> g{v};
+        EpiAlDual<T> e{&V, (T)cx.a.sigma};
+        spmv_t<T>(cx, MAT_A, V.mv[MAT_A], g, e, dummy);
         FACP_SYNC(cx);
-        u = P.aldual;
+        u = V.aldual;
     }
-    Gat g{u};
-    EpiStore st{P.dprod};
-    spmv(cx, P.M[MAT_AT], g, st, dummy);
+    GatT<T> g{u};
+    EpiStoreT<T> st{V.dprod};
+    spmv_t<T>(cx, MAT_AT, V.mv[MAT_AT], g, st, dummy);
     FACP_SYNC(cx);
     return true;
 }
 
-/* BB init (fa_cp_core_op.cu:398-417): g = Qx + c - q; x' = P(x - alpha g). */
+/* BB init (fa_cp_core_op.cu:398-417): g = Qx + c - q; x' = P(x - alpha g).
+ * s1 accumulates |x|^2 (the FP32 form's floor of the inner tolerance). */
+template <typename T>
 struct EpiBBInit {
-    const Prob *P;
-    double alpha;
-    __device__ __forceinline__ void operator()(int j, const double (&s)[1], Red<1, 0> &r) const {
-        const double qxj = q_total(*P, j, s[0]);
-        P->qx[j] = qxj;
-        const double g = qxj + P->c[j] - P->dprod[j];
-        const double xj = P->x[j];
-        double nx = xj - alpha * g;
-        nx = fmax(P->vlb[j], fmin(nx, P->vub[j]));
-        P->xh[j] = nx;
-        P->grad[j] = g;
-        const double d = nx - xj;
-        P->dir[j] = d;
-        r.s[0] += d * d;
+    const SegV<T> *V;
+    int qtype;
+    T alpha;
+    __device__ __forceinline__ void operator()(int j, const T (&s)[1], Red<2, 0> &r) const {
+        const T qxj = q_total_t(qtype, (const T *)V->qx, j, s[0]);
+        V->qx[j] = qxj;
+        const T g = qxj + V->c[j] - V->dprod[j];
+        const T xj = V->x[j];
+        T nx = xj - alpha * g;
+        nx = tmax(V->vlb[j], tmin(nx, V->vub[j]));
+        V->xh[j] = nx;
+        V->grad[j] = g;
+        const T d = nx - xj;
+        V->dir[j] = d;
+        r.s[0] += (double)d * (double)d;
+        r.s[1] += (double)xj * (double)xj;
     }
     const Cx *cx;
     int mat;
-    __device__ __forceinline__ void long_red(int lid, Red<1, 0> &lr) const { add_long(*cx, mat, lid, lr); }
+    __device__ __forceinline__ void long_red(int lid, Red<2, 0> &lr) const { add_long(*cx, mat, lid, lr); }
 };
 
 /* BB gradient (fa_cp_core_op.cu:401-417): g' = Qx' + c - q + (x' - x)/tau;
  * dg = g' - g; dot(d, dg) accumulates. */
+template <typename T>
 struct EpiBBGrad {
-    const Prob *P;
-    double inv;
-    __device__ __forceinline__ void operator()(int j, const double (&s)[1], Red<1, 0> &r) const {
-        const double qxj = q_total(*P, j, s[0]);
-        P->qx[j] = qxj;
-        const double last = P->grad[j];
-        const double cur = qxj + P->c[j] - P->dprod[j] + inv * (P->xh[j] - P->x[j]);
-        const double dg = cur - last;
-        P->grad[j] = cur;
-        r.s[0] += P->dir[j] * dg;
+    const SegV<T> *V;
+    int qtype;
+    T inv;
+    __device__ __forceinline__ void operator()(int j, const T (&s)[1], Red<1, 0> &r) const {
+        const T qxj = q_total_t(qtype, (const T *)V->qx, j, s[0]);
+        V->qx[j] = qxj;
+        const T last = V->grad[j];
+        const T cur = qxj + V->c[j] - V->dprod[j] + inv * (V->xh[j] - V->x[j]);
+        const T dg = cur - last;
+        V->grad[j] = cur;
+        r.s[0] += (double)V->dir[j] * (double)dg;
     }
     const Cx *cx;
     int mat;
@@ -434,47 +541,57 @@ __device__ __forceinline__ int obj_long_mat(int qtype) {
     return (qtype == Q_LOWRANK || qtype == Q_LOWRANK_SPARSE) ? MAT_RT : MAT_Q;
 }
 
+/* FP32 form: the BB loop also stops once |d| is at the FP32 resolution of
+ * the iterate (kF32Floor |x|), below which the FP32 step cannot make progress. */
+constexpr double kF32Floor = 1e-6;
+
 /* Projected BB on the primal subproblem (fa_cp_core_op.cu:445-503).  Leaves
  * x' in xh; returns false on a barrier failure. */
-__device__ bool bb_solve(Cx &cx, double tau, bool al, double &inner_tol, long long &inner_total) {
+template <typename T>
+__device__ bool bb_solve(Cx &cx, const SegV<T> &V, double tau, bool al, double &inner_tol, long long &inner_total) {
     const Prob &P = cx.P;
     const double inv = 1.0 / tau;
     double alpha = 1.0 / inv;
     int it = 1;
-    if (!dual_product(cx, P.x, al)) return false;
-    double tot[1];
+    if (!dual_product<T>(cx, V, V.x, al)) return false;
+    double tol = inner_tol;
+    double ng;
     {
-        Red<1, 0> r;
+        Red<2, 0> r;
         r.zero();
         unsigned lmask = 0;
-        EpiBBInit e{&P, alpha, &cx, obj_long_mat(P.qtype)};
-        if (!obj_product(cx, P.x, e, r, lmask)) return false;
-        if (!greduce<1, 0>(cx, r, lmask, tot)) return false;
+        EpiBBInit<T> e{&V, P.qtype, (T)alpha, &cx, obj_long_mat(P.qtype)};
+        if (!obj_product_t<T>(cx, V, V.x, e, r, lmask)) return false;
+        double tot[2];
+        if (!greduce<2, 0>(cx, r, lmask, tot)) return false;
+        ng = sqrt(tot[0]);
+        if (sizeof(T) == sizeof(float)) tol = fmax(tol, kF32Floor * sqrt(tot[1]));
     }
-    double ng = sqrt(tot[0]);
+    double tot[1];
     while (it < cx.a.inner_limit) {
-        if (ng <= inner_tol) break;
-        if (al && !dual_product(cx, P.xh, true)) return false;
+        if (ng <= tol) break;
+        if (al && !dual_product<T>(cx, V, V.xh, true)) return false;
         {
             Red<1, 0> r;
             r.zero();
             unsigned lmask = 0;
-            EpiBBGrad e{&P, inv, &cx, obj_long_mat(P.qtype)};
-            if (!obj_product(cx, P.xh, e, r, lmask)) return false;
+            EpiBBGrad<T> e{&V, P.qtype, (T)inv, &cx, obj_long_mat(P.qtype)};
+            if (!obj_product_t<T>(cx, V, V.xh, e, r, lmask)) return false;
             if (!greduce<1, 0>(cx, r, lmask, tot)) return false;
         }
         alpha = ng * ng / tot[0];
         {
             Red<1, 0> r;
             r.zero();
+            const T al_t = (T)alpha;
             foreach_elem(cx, P.n, [&](int j) {
-                const double cur = P.xh[j];
-                double nx = cur - alpha * P.grad[j];
-                nx = fmax(P.vlb[j], fmin(nx, P.vub[j]));
-                const double d = nx - cur;
-                P.dir[j] = d;
-                P.xh[j] = nx;
-                r.s[0] += d * d;
+                const T cur = V.xh[j];
+                T nx = cur - al_t * V.grad[j];
+                nx = tmax(V.vlb[j], tmin(nx, V.vub[j]));
+                const T d = nx - cur;
+                V.dir[j] = d;
+                V.xh[j] = nx;
+                r.s[0] += (double)d * (double)d;
             });
             if (!greduce<1, 0>(cx, r, 0u, tot)) return false;
         }
@@ -488,28 +605,29 @@ __device__ bool bb_solve(Cx &cx, double tau, bool al, double &inner_tol, long lo
 /* Closed-form primal step (LP and diagonal Q without AL) fused into the A'y
  * SpMV (fa_cp_core_op.cu:93-154, 305-347), with the reflection, the fixed-point
  * delta and the Halpern average of x. */
+template <typename T>
 struct EpiPrimalClosed {
-    const Prob *P;
-    double tau, w, refl;
+    const SegV<T> *V;
+    T tau, w, refl;
     int wm, fp, diag;
-    __device__ __forceinline__ void operator()(int j, const double (&s)[1], Red<3, 0> &r) const {
-        const double xj = P->x[j];
-        double t = xj - tau * (P->c[j] - s[0]);
-        if (diag) t = t / (1.0 + tau * P->diag[j]);
-        const double pr = fmax(P->vlb[j], fmin(t, P->vub[j]));
-        const double xb = 2.0 * pr - xj;
-        P->xbar[j] = xb;
+    __device__ __forceinline__ void operator()(int j, const T (&s)[1], Red<3, 0> &r) const {
+        const T xj = V->x[j];
+        T t = xj - tau * (V->c[j] - s[0]);
+        if (diag) t = t / (T(1) + tau * V->diag[j]);
+        const T pr = tmax(V->vlb[j], tmin(t, V->vub[j]));
+        const T xb = T(2) * pr - xj;
+        V->xbar[j] = xb;
         if (wm) {
-            P->xh[j] = pr;
-            if (!diag) P->dslack[j] = (pr - t) / tau;
+            V->xh[j] = pr;
+            if (!diag) V->dslack[j] = (pr - t) / tau;
         }
         if (fp) {
-            const double d = xb - xj;
-            P->dx[j] = d;
-            r.s[0] += d * d;
+            const T d = xb - xj;
+            V->dx[j] = d;
+            r.s[0] += (double)d * (double)d;
         }
-        const double refl_v = refl * xb + (1.0 - refl) * xj;
-        P->x[j] = w * refl_v + (1.0 - w) * P->x0[j];
+        const T refl_v = refl * xb + (T(1) - refl) * xj;
+        V->x[j] = halpern_avg(w, refl_v, V->x0[j]);
     }
     const Cx *cx;
     __device__ __forceinline__ void long_red(int lid, Red<3, 0> &lr) const { add_long(*cx, MAT_AT, lid, lr); }
@@ -517,51 +635,53 @@ struct EpiPrimalClosed {
 
 /* Dual step (AL form fa_cp_core_op.cu:194-223 or the Moreau form 156-179)
  * fused into the A x-bar SpMV, with the fixed-point delta and Halpern on y. */
+template <typename T>
 struct EpiDual {
-    const Prob *P;
-    double rho, sigma, w, refl;
+    const SegV<T> *V;
+    T rho, sigma, w, refl;
     int wm, fp, al;
-    __device__ __forceinline__ void operator()(int i, const double (&s)[1], Red<3, 0> &r) const {
-        const double p = s[0];
-        const double yi = P->y[i];
-        double yb;
+    __device__ __forceinline__ void operator()(int i, const T (&s)[1], Red<3, 0> &r) const {
+        const T p = s[0];
+        const T yi = V->y[i];
+        T yb;
         if (al) {
-            const double denom = sigma + rho;
-            const double shifted = p - yi / denom;
-            const double proj = fmax(P->clb[i], fmin(shifted, P->cub[i]));
-            const double nd = yi + rho * (proj - p);
-            if (wm) P->yh[i] = nd;
-            yb = 2.0 * nd - yi;
+            const T denom = sigma + rho;
+            const T shifted = p - yi / denom;
+            const T proj = tmax(V->clb[i], tmin(shifted, V->cub[i]));
+            const T nd = yi + rho * (proj - p);
+            if (wm) V->yh[i] = nd;
+            yb = T(2) * nd - yi;
         } else {
-            const double t = yi / rho - p;
-            const double tp = fmax(-P->cub[i], fmin(t, -P->clb[i]));
+            const T t = yi / rho - p;
+            const T tp = tmax(-V->cub[i], tmin(t, -V->clb[i]));
             if (wm) {
-                const double yhi = (t - tp) * rho;
-                P->yh[i] = yhi;
-                yb = 2.0 * yhi - yi;
+                const T yhi = (t - tp) * rho;
+                V->yh[i] = yhi;
+                yb = T(2) * yhi - yi;
             } else {
-                yb = 2.0 * (t - tp) * rho - yi;
+                yb = T(2) * (t - tp) * rho - yi;
             }
         }
-        P->ybar[i] = yb;
+        V->ybar[i] = yb;
         if (fp) {
-            const double d = yb - yi;
-            P->dy[i] = d;
-            r.s[1] += d * d;
+            const T d = yb - yi;
+            V->dy[i] = d;
+            r.s[1] += (double)d * (double)d;
         }
-        const double refl_v = refl * yb + (1.0 - refl) * yi;
-        P->y[i] = w * refl_v + (1.0 - w) * P->y0[i];
+        const T refl_v = refl * yb + (T(1) - refl) * yi;
+        V->y[i] = halpern_avg(w, refl_v, V->y0[i]);
     }
     const Cx *cx;
     __device__ __forceinline__ void long_red(int lid, Red<3, 0> &lr) const { add_long(*cx, MAT_A, lid, lr); }
 };
 
 /* <A'dy, dx> of the fixed-point error (fa_cp_core_op.cu:1042-1089). */
-struct EpiCross {
-    const Prob *P;
-    __device__ __forceinline__ void operator()(int j, const double (&s)[1], Red<3, 0> &r) const {
-        P->dprod[j] = s[0];
-        r.s[2] += s[0] * P->dx[j];
+template <typename T>
+struct EpiCrossT {
+    const SegV<T> *V;
+    __device__ __forceinline__ void operator()(int j, const T (&s)[1], Red<3, 0> &r) const {
+        V->dprod[j] = s[0];
+        r.s[2] += (double)s[0] * (double)V->dx[j];
     }
     const Cx *cx;
     __device__ __forceinline__ void long_red(int lid, Red<3, 0> &lr) const { add_long(*cx, MAT_AT, lid, lr); }
@@ -570,8 +690,9 @@ struct EpiCross {
 /* One outer iteration at total count k.  The Halpern average of x and y is
  * applied as soon as the reflected point is known: the fixed-point error only
  * needs the deltas, which are taken from the pre-update values. */
-__device__ bool iteration(Cx &cx, int k, int inner, bool fp, double &inner_tol, long long &inner_total,
-                          double &fp_out) {
+template <typename T>
+__device__ bool iteration(Cx &cx, const SegV<T> &V, int k, int inner, bool fp, double &inner_tol,
+                          long long &inner_total, double &fp_out) {
     const Prob &P = cx.P;
     const Args &a = cx.a;
     const bool major = ((k + 1) % a.F) == 0;
@@ -583,38 +704,39 @@ __device__ bool iteration(Cx &cx, int k, int inner, bool fp, double &inner_tol, 
     fr.zero();
     unsigned fmask = 0;
     if (closed) {
-        Gat g{P.y};
-        EpiPrimalClosed e{&P, a.tau, w, a.refl, wm ? 1 : 0, fp ? 1 : 0, P.qtype == Q_DIAG ? 1 : 0, &cx};
-        spmv(cx, P.M[MAT_AT], g, e, fr);
+        GatT<T> g{(const T *)V.y};
+        EpiPrimalClosed<T> e{&V, (T)a.tau, (T)w, (T)a.refl, wm ? 1 : 0, fp ? 1 : 0, P.qtype == Q_DIAG ? 1 : 0, &cx};
+        spmv_t<T>(cx, MAT_AT, V.mv[MAT_AT], g, e, fr);
         if (fp) fmask |= 1u << MAT_AT;
         FACP_SYNC(cx);
     } else {
-        if (!bb_solve(cx, a.tau, al, inner_tol, inner_total)) return false;
+        if (!bb_solve<T>(cx, V, a.tau, al, inner_tol, inner_total)) return false;
+        const T w_t = (T)w, refl_t = (T)a.refl;
         foreach_elem(cx, P.n, [&](int j) {
-            const double xj = P.x[j];
-            const double xb = 2.0 * P.xh[j] - xj;
-            P.xbar[j] = xb;
+            const T xj = V.x[j];
+            const T xb = T(2) * V.xh[j] - xj;
+            V.xbar[j] = xb;
             if (fp) {
-                const double d = xb - xj;
-                P.dx[j] = d;
-                fr.s[0] += d * d;
+                const T d = xb - xj;
+                V.dx[j] = d;
+                fr.s[0] += (double)d * (double)d;
             }
-            const double refl_v = a.refl * xb + (1.0 - a.refl) * xj;
-            P.x[j] = w * refl_v + (1.0 - w) * P.x0[j];
+            const T refl_v = refl_t * xb + (T(1) - refl_t) * xj;
+            V.x[j] = halpern_avg(w_t, refl_v, V.x0[j]);
         });
         FACP_SYNC(cx);
     }
     {
-        Gat g{P.xbar};
-        EpiDual e{&P, a.rho, a.sigma, w, a.refl, wm ? 1 : 0, fp ? 1 : 0, al ? 1 : 0, &cx};
-        spmv(cx, P.M[MAT_A], g, e, fr);
+        GatT<T> g{(const T *)V.xbar};
+        EpiDual<T> e{&V, (T)a.rho, (T)a.sigma, (T)w, (T)a.refl, wm ? 1 : 0, fp ? 1 : 0, al ? 1 : 0, &cx};
+        spmv_t<T>(cx, MAT_A, V.mv[MAT_A], g, e, fr);
         if (fp) fmask |= 1u << MAT_A;
         FACP_SYNC(cx);
     }
     if (fp) {
-        Gat g{P.dy};
-        EpiCross e{&P, &cx};
-        spmv(cx, P.M[MAT_AT], g, e, fr);
+        GatT<T> g{(const T *)V.dy};
+        EpiCrossT<T> e{&V, &cx};
+        spmv_t<T>(cx, MAT_AT, V.mv[MAT_AT], g, e, fr);
         fmask |= 1u << MAT_AT;
         double tot[3];
         if (!greduce<3, 0>(cx, fr, fmask, tot)) return false;
@@ -627,7 +749,8 @@ __device__ bool iteration(Cx &cx, int k, int inner, bool fp, double &inner_tol, 
     return true;
 }
 
-__device__ bool run_segment(Cx &cx) {
+template <typename T>
+__device__ bool run_segment_t(Cx &cx, const SegV<T> &V) {
     const Args &a = cx.a;
     Ctl *ctl = cx.P.ctl;
     double inner_tol = ctl->inner_tol;
@@ -639,7 +762,7 @@ __device__ bool run_segment(Cx &cx) {
         const bool first = (k == a.t0) && a.fp_first;
         const bool need_fp = major || first;
         double f = fp;
-        if (!iteration(cx, k, inner, need_fp, inner_tol, inner_total, f)) return false;
+        if (!iteration<T>(cx, V, k, inner, need_fp, inner_tol, inner_total, f)) return false;
         if (need_fp) {
             fp = f;
             if (first) fp_first = f;
@@ -651,6 +774,46 @@ __device__ bool run_segment(Cx &cx) {
         ctl->fp = fp;
         ctl->fp_first = fp_first;
     }
+    return true;
+}
+
+/* The FP64 state between launches is converted into the FP32 mirror at the
+ * start of an FP32 segment (iterates, anchors as (hi, lo), the buffers the
+ * evaluation and restart read or modify) and back at its end. */
+__device__ bool run_segment(Cx &cx) {
+    const Prob &P = cx.P;
+    if (!cx.a.fp32) {
+        const SegV<double> V = seg64(P);
+        return run_segment_t<double>(cx, V);
+    }
+    const SegV<float> &F = P.f;
+    foreach_elem(cx, P.n, [&](int j) {
+        F.x[j] = (float)P.x[j];
+        F.xh[j] = (float)P.xh[j];
+        F.dslack[j] = (float)P.dslack[j];
+        F.dx[j] = (float)P.dx[j];
+        F.x0[j] = split_anchor(P.x0[j]);
+    });
+    foreach_elem(cx, P.m, [&](int i) {
+        F.y[i] = (float)P.y[i];
+        F.yh[i] = (float)P.yh[i];
+        F.dy[i] = (float)P.dy[i];
+        F.y0[i] = split_anchor(P.y0[i]);
+    });
+    FACP_SYNC(cx);
+    if (!run_segment_t<float>(cx, F)) return false;
+    FACP_SYNC(cx);
+    foreach_elem(cx, P.n, [&](int j) {
+        P.x[j] = (double)F.x[j];
+        P.xh[j] = (double)F.xh[j];
+        P.dslack[j] = (double)F.dslack[j];
+        P.dx[j] = (double)F.dx[j];
+    });
+    foreach_elem(cx, P.m, [&](int i) {
+        P.y[i] = (double)F.y[i];
+        P.yh[i] = (double)F.yh[i];
+        P.dy[i] = (double)F.dy[i];
+    });
     return true;
 }
 
@@ -958,7 +1121,8 @@ __device__ bool run_delta_score(Cx &cx) {
     });
     FACP_SYNC(cx);
     Gat g{P.dy};
-    EpiCross e{&P, &cx};
+    const SegV<double> V = seg64(P);
+    EpiCrossT<double> e{&V, &cx};
     spmv(cx, P.M[MAT_AT], g, e, r);
     double t[3];
     if (!greduce<3, 0>(cx, r, 1u << MAT_AT, t)) return false;
@@ -1116,10 +1280,12 @@ __device__ bool run_power_q(Cx &cx, bool shifted) {
 /* ------------------------------------------------------------------ the kernel */
 
 __global__ void __launch_bounds__(kThreads, 2) k_facp(Prob P, Args a) {
-    __shared__ RowBlockSmem<kS, 1, double> sm;
+    static_assert(sizeof(RowBlockSmem<kS, 1, float>) <= sizeof(RowBlockSmem<kS, 1, double>), "shared staging");
+    __shared__ __align__(16) unsigned char smraw[sizeof(RowBlockSmem<kS, 1, double>)];
     __shared__ double stot[kSlot];
     __shared__ int sok;
-    Cx cx{P, a, sm, stot, &sok, gridDim.x, 0};
+    Cx cx{P, a, *reinterpret_cast<RowBlockSmem<kS, 1, double> *>(smraw),
+          *reinterpret_cast<RowBlockSmem<kS, 1, float> *>(smraw), stot, &sok, gridDim.x, 0};
     bool ok = true;
     switch (a.mode) {
     case MODE_SEGMENT:

@@ -200,6 +200,11 @@ __global__ void k_finite(int len, const double *__restrict__ src, double *dst) {
         dst[i] = isfinite(src[i]) ? src[i] : 0.0;
 }
 
+__global__ void k_to_float(long long len, const double *__restrict__ src, float *dst) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+
 /* diagonal of a diagonal Q plus 1e-12 (solver_state.cu:252-270) */
 __global__ void k_diag(int rows, int n, const int *__restrict__ rp, const int *__restrict__ ci,
                        const double *__restrict__ v, double *diag) {
@@ -315,11 +320,16 @@ class FacpSolver {
     termination_reason_t reason_ = TERMINATION_REASON_UNSPECIFIED;
     int restart_target_ = 0;
     int restarts_ = 0, evals_ = 0;
+    bool fp32_ = false; /* FP32 segments (first phase of precision 1) */
+    double fp32_best_ = INFINITY;
+    int fp32_stall_ = 0, fp32_iters_ = 0;
 };
 
 void FacpSolver::prepare() {
     const qp_problem_t *q = prob_;
     if (!q) throw Error("solve_qp_problem: invalid arguments");
+    if (o_.precision != 0 && o_.precision != 1) throw Error("precision must be 0 (FP64) or 1 (FP32 + FP64 refinement)");
+    if (o_.precision == 1 && !(o_.fp32_switch_tol >= 0.0)) throw Error("fp32_switch_tol must be >= 0");
     if (p_.termination_evaluation_frequency < 1) throw Error("termination_evaluation_frequency must be >= 1");
     HostQP &P = H_;
     P.n = q->num_variables;
@@ -452,6 +462,20 @@ void FacpSolver::upload() {
         P_.lpart = arena_.take<double>((size_t)3 * nl * kSlot);
         P_.bar = arena_.take<GridBar>(1);
         P_.ctl = arena_.take<Ctl>(1);
+        P_.f = SegV<float>{};
+        if (o_.precision == 1) { /* FP32 mirror of the segment path */
+            SegV<float> &f = P_.f;
+            const size_t mm = std::max<size_t>(m, 1), rr = std::max<size_t>(nr, 1);
+            for (const float **q : {&f.c, &f.vlb, &f.vub, &f.diag}) *q = arena_.take<float>(n);
+            for (const float **q : {&f.clb, &f.cub}) *q = arena_.take<float>(mm);
+            for (float **q : {&f.x, &f.xh, &f.xbar, &f.dprod, &f.dslack, &f.dx, &f.qx, &f.grad, &f.dir})
+                *q = arena_.take<float>(n);
+            for (float **q : {&f.y, &f.yh, &f.ybar, &f.dy, &f.aldual}) *q = arena_.take<float>(mm);
+            f.rx = arena_.take<float>(rr);
+            f.x0 = arena_.take<float2>(n);
+            f.y0 = arena_.take<float2>(mm);
+            for (int k = 0; k < NMAT; ++k) f.mv[k] = arena_.take<float>(M_[k].h.ci.size() + 8);
+        }
     };
     arena_.begin_measure();
     alloc_all();
@@ -682,6 +706,24 @@ void FacpSolver::equilibrate_device() {
         }
         qnorm_ = mx;
         nonconvexity_ = mn;
+    }
+    if (o_.precision == 1) { /* FP32 copies of the scaled data; zero product buffers */
+        SegV<float> &f = P_.f;
+        auto cv = [&](const double *src, const float *dst, long long len) {
+            if (len > 0) k_to_float<<<grid(len), 256, 0, stream_>>>(len, src, (float *)dst);
+        };
+        cv(P_.c, f.c, n);
+        cv(P_.vlb, f.vlb, n);
+        cv(P_.vub, f.vub, n);
+        cv(P_.clb, f.clb, m);
+        cv(P_.cub, f.cub, m);
+        if (qtype_ == Q_DIAG) cv(P_.diag, f.diag, n);
+        for (int k = 0; k < NMAT; ++k) cv(P_.M[k].v, f.mv[k], (long long)M_[k].h.ci.size());
+        PDAL_CUDA(cudaMemsetAsync(f.qx, 0, (size_t)n * sizeof(float), stream_));
+        PDAL_CUDA(cudaMemsetAsync(f.rx, 0, (size_t)std::max(nr, 1) * sizeof(float), stream_));
+        PDAL_CUDA(cudaGetLastError());
+        launches_ += 6 + NMAT;
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
     }
     rescale_sec_ = transpose_sec_ + (now_sec() - t0);
 }
@@ -961,6 +1003,10 @@ fa_cp_result_t *FacpSolver::run() {
 
     const int F = p_.termination_evaluation_frequency;
     const int limit = p_.termination_criteria.iteration_limit;
+    fp32_ = o_.precision == 1;
+    fp32_best_ = INFINITY;
+    fp32_stall_ = 0;
+    fp32_iters_ = 0;
     trajectory_header();
     bool major = false, do_restart = false;
     double elapsed = 0.0;
@@ -978,6 +1024,17 @@ fa_cp_result_t *FacpSolver::run() {
             trajectory_row(elapsed, planned);
             if (p_.verbose >= 2) print_eval();
             if (reason_ != TERMINATION_REASON_UNSPECIFIED) break;
+            if (fp32_) { /* end of the FP32 phase: tolerance reached, or no halving for a while */
+                const double kkt = std::fmax(ctl_.rel_p, std::fmax(ctl_.rel_d, ctl_.rel_gap));
+                if (kkt < 0.5 * fp32_best_) {
+                    fp32_best_ = kkt;
+                    fp32_stall_ = 0;
+                } else {
+                    ++fp32_stall_;
+                }
+                if (kkt < o_.fp32_switch_tol || (o_.fp32_stall_evals > 0 && fp32_stall_ >= o_.fp32_stall_evals))
+                    fp32_ = false;
+            }
         }
         if (consider) {
             do_restart = planned;
@@ -1002,6 +1059,8 @@ fa_cp_result_t *FacpSolver::run() {
         a.tau = tau;
         a.rho = step_ * pw_;
         a.sigma = use_al_ ? al_sigma_ : 0.0;
+        a.fp32 = fp32_ ? 1 : 0;
+        if (fp32_) fp32_iters_ += t_end - total_;
         PDAL_CUDA(cudaEventRecord(ev0_, stream_));
         launch(a);
         PDAL_CUDA(cudaEventRecord(ev1_, stream_));
@@ -1087,6 +1146,7 @@ fa_cp_result_t *FacpSolver::run() {
     st.power_sec = power_sec_;
     st.power_iterations_a = power_iters_a_;
     st.power_iterations_q = power_iters_q_;
+    st.fp32_iterations = fp32_iters_;
     if (p_.verbose >= 1)
         printf("[fa_cp_gb300] %s after %d iterations (%lld inner), objective %.10e, rel. KKT %.2e, %.3f s\n",
                reason_ == TERMINATION_REASON_OPTIMAL ? "optimal" : "stopped", total_, (long long)ctl_.inner_total,

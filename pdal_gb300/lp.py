@@ -314,3 +314,23 @@ def solve_batch(items: list[LPData], params: dict | N.CpalParameters | None = No
     finally:
         for q in probs:
             q.close()
+
+
+def tune_batch(items: list[LPData], params: dict | N.CpalParameters | None = None,
+               options: dict | N.CpalOptions | None = None) -> dict:
+    """The batch schedule autotuner alone (cp_al_gb300_batch_tune): the
+    schedule a later solve_batch of the same batch shape will use, and the
+    tuning time."""
+    lib = N.load_lp()
+    p = params if isinstance(params, N.CpalParameters) else apply_params(default_parameters(lib), params)
+    o = options if isinstance(options, N.CpalOptions) else apply_options(default_options(lib), options)
+    probs = [_CProblem(lib, d) for d in items]
+    try:
+        arr = (C.POINTER(N.LpProblem) * len(probs))(*[q.ptr for q in probs])
+        st = N.BatchStats()
+        if lib.cp_al_gb300_batch_tune(len(probs), arr, C.byref(p), C.byref(o), C.byref(st)) != 0:
+            raise RuntimeError("batch tune failed: " + N.last_error(lib))
+        return {"block_nnz": st.block_nnz, "blocks_per_sm": st.blocks_per_sm, "tune_sec": st.tune_sec}
+    finally:
+        for q in probs:
+            q.close()

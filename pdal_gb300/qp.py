@@ -165,7 +165,11 @@ def apply_params(p: N.FacpParameters, d: dict | None) -> N.FacpParameters:
 
 
 def apply_options(o: N.FacpOptions, d: dict | None) -> N.FacpOptions:
+    """Keys: any field of fa_cp_gb300_options_t; 'precision' also takes
+    "fp64" / "fp32_refine"."""
     for k, v in (d or {}).items():
+        if k == "precision":
+            v = {"fp64": 0, "fp32_refine": 1}.get(v, v)
         if not hasattr(o, k):
             raise KeyError(f"unknown option {k!r}")
         setattr(o, k, v)

@@ -118,5 +118,10 @@ def test_schedule_autotuner_and_fixed_schedules():
     assert st["tune_sec"] > 0.0 and st["optimal"] == len(items)
     res2, st2 = lp.solve_batch(items, params)
     assert st2["tune_sec"] == 0.0 and (st2["block_nnz"], st2["blocks_per_sm"]) == (st["block_nnz"], st["blocks_per_sm"])
+    other = batch_lps(count=41, seed=92, m_range=(100, 1500))
+    t = lp.tune_batch(other, params)
+    assert t["tune_sec"] > 0.0
+    _, st3 = lp.solve_batch(other, params)
+    assert st3["tune_sec"] == 0.0 and (st3["block_nnz"], st3["blocks_per_sm"]) == (t["block_nnz"], t["blocks_per_sm"])
     with pytest.raises(RuntimeError):
         lp.solve_batch(items, params, {"spmv_nnz_per_block": 2048, "batch_blocks_per_sm": 4})

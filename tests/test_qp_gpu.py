@@ -202,3 +202,26 @@ def test_device_equilibration_is_bit_identical_to_oracle(case):
             np.testing.assert_allclose(a, b, rtol=1e-14, atol=0)
         else:
             assert np.array_equal(np.asarray(a), np.asarray(b)), case
+
+
+@pytest.mark.parametrize("form", ["sparse", "lowrank", "diag", "lp"])
+def test_fp32_refine_reaches_fp64_tolerance(form):
+    """Chosen form: FP32 iteration segments (FP64 reductions, evaluation and
+    control), then FP64 from the FP32 iterate.  It meets the same relative KKT
+    tolerance as the FP64 solve, and two solutions that each meet 1e-8 along
+    different trajectories agree in objective to that tolerance."""
+    if form in ("sparse", "lowrank"):
+        data, _, f_star = planted_qp(n=3000, m=1500, b_rows=750, seed=41, q_form=form)
+    elif form == "diag":
+        data, f_star = _diag_qp(n=3000, m=1200, seed=7), None
+    else:
+        d = random_lp(800, 2000, 6, seed=9)
+        data, f_star = QPData(d.c, d.A, d.con_lb, d.con_ub, d.var_lb, d.var_ub), None
+    params = {"eps": 1e-8, "verbose": 0, "iteration_limit": 200_000}
+    g64 = qp.solve(data, params)
+    g32 = qp.solve(data, params, {"precision": "fp32_refine"})
+    assert g64.status == g32.status == "OPTIMAL"
+    assert g32.kkt < 1e-8 and g32.stats["fp32_iterations"] > 0
+    assert abs(g32.primal_objective - g64.primal_objective) <= 5e-8 * (1 + abs(g64.primal_objective))
+    if f_star is not None:
+        assert abs(g32.primal_objective - f_star) <= 1e-7 * (1 + abs(f_star))

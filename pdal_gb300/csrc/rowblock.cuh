@@ -160,11 +160,7 @@ __device__ __forceinline__ void store4_shared(double *dst, const double (&v)[4])
  * with 128-bit streaming loads, the gathered entries through the read-only
  * path.  Arrays are padded so that the four-element window may extend three
  * elements past k1; elements outside [k0, k1) are staged as zeros and never
- * read.  The three phases -- every index/value load of the thread, then every
- * gather, then every shared-memory store -- keep all of a thread's loads in
- * flight at once: the kernel is bound by the latency of the random gathers,
- * and a thread that waited for each chunk's gathers before loading the next
- * chunk's indices would serialise two memory round trips per chunk. */
+ * read. */
 template <int S, int NP, typename T, class Gat>
 __device__ __forceinline__ void rowblock_stage(int k0, int k1, const int *__restrict__ ci, const T *__restrict__ val,
                                                Gat &gat, RowBlockSmem<S, NP, T> &sm) {
@@ -172,45 +168,33 @@ __device__ __forceinline__ void rowblock_stage(int k0, int k1, const int *__rest
     constexpr int MAXIT = (S / 4 + 1 + NT - 1) / NT;
     const int kb = k0 & ~3;
     const int nch = (k1 - kb + 3) >> 2;
-    int cols[MAXIT][4];
-    T vals[MAXIT][4];
-#pragma unroll
-    for (int it = 0; it < MAXIT; ++it) {
-        const int c = it * NT + (int)threadIdx.x;
-        if (c < nch) {
-            load4_stream(ci + kb + 4 * c, cols[it]);
-            load4_stream(val + kb + 4 * c, vals[it]);
-        }
-    }
-    T gv[MAXIT][NP][4];
 #pragma unroll
     for (int it = 0; it < MAXIT; ++it) {
         const int c = it * NT + (int)threadIdx.x;
         if (c < nch) {
             const int kc = kb + 4 * c;
+            int cols[4];
+            T vals[4];
+            load4_stream(ci + kc, cols);
+            load4_stream(val + kc, vals);
+            T gv[NP][4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int e = kc + q;
                 if (e >= k0 && e < k1) {
                     T t[NP];
-                    gat(cols[it][q], t);
+                    gat(cols[q], t);
 #pragma unroll
-                    for (int p = 0; p < NP; ++p) gv[it][p][q] = t[p];
+                    for (int p = 0; p < NP; ++p) gv[p][q] = t[p];
                 } else {
 #pragma unroll
-                    for (int p = 0; p < NP; ++p) gv[it][p][q] = T(0);
-                    vals[it][q] = T(0);
+                    for (int p = 0; p < NP; ++p) gv[p][q] = T(0);
+                    vals[q] = T(0);
                 }
             }
-        }
-    }
+            store4_shared(&sm.val[4 * c], vals);
 #pragma unroll
-    for (int it = 0; it < MAXIT; ++it) {
-        const int c = it * NT + (int)threadIdx.x;
-        if (c < nch) {
-            store4_shared(&sm.val[4 * c], vals[it]);
-#pragma unroll
-            for (int p = 0; p < NP; ++p) store4_shared(&sm.g[p][4 * c], gv[it][p]);
+            for (int p = 0; p < NP; ++p) store4_shared(&sm.g[p][4 * c], gv[p]);
         }
     }
 }

@@ -47,7 +47,8 @@ def _cuda_include() -> str:
 
 def build_ref() -> list[Path]:
     """Compiles the reference's own MPS readers (LP/CP_AL/src/mps_parser.c and
-    QP/FA_CP/src/mps_parser.c, unmodified, read in place) into oracle/_ref/
+    QP/FA_CP/src/mps_parser.c) and its FA_CP equilibration
+    (QP/FA_CP/src/preconditioner.c), unmodified and read in place, into oracle/_ref/
     with gcc, zlib and ref_shim/ (allocation helpers, the problem free
     functions and an empty PSLP_stats.h).  Their internal headers include the
     CUDA headers for declarations only; nothing of CUDA is linked.  Returns
@@ -70,6 +71,19 @@ def build_ref() -> list[Path]:
         if res.returncode != 0:
             raise RuntimeError("reference reader build failed:\n" + " ".join(cmd) + "\n" + res.stderr)
         out.append(target)
+    # the FA_CP equilibration (host code in the reference)
+    proj = "QP/FA_CP"
+    src = REFERENCE / proj / "src" / "preconditioner.c"
+    target = REF_OUT / "libref_facp_precond.so"
+    deps = [src, *SHIM.iterdir()]
+    if not (target.exists() and target.stat().st_mtime > max(p.stat().st_mtime for p in deps)):
+        cmd = ["gcc", "-O2", "-fPIC", "-shared", "-w", "-I", str(SHIM), "-I", str(REFERENCE / proj / "include"),
+               "-I", str(REFERENCE / proj / "internal"), "-I", _cuda_include(), str(src),
+               str(SHIM / "ref_precond_shim.c"), str(SHIM / "ref_mps_shim.c"), "-lm", "-o", str(target)]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("reference preconditioner build failed:\n" + " ".join(cmd) + "\n" + res.stderr)
+    out.append(target)
     return out
 
 

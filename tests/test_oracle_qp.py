@@ -185,3 +185,56 @@ def test_model_interface_host_side():
     with pytest.warns(RuntimeWarning):
         m.setWarmStart(primal=[1.0, 2.0, 3.0])
     assert m.X is None and FA_CP.MAXIMIZE == -1
+
+
+def _reference_precond():
+    """The reference's own FA_CP equilibration (QP/FA_CP/src/preconditioner.c),
+    compiled unmodified by oracle/build.py (build_ref); skipped where the
+    reference sources are absent."""
+    from oracle import build as ob
+
+    built = {p.name: p for p in ob.build_ref()}
+    if "libref_facp_precond.so" not in built:
+        pytest.skip("reference sources absent")
+    lib = C.CDLL(str(built["libref_facp_precond.so"]))
+    _dp = C.POINTER(C.c_double)
+    lib.ref_facp_rescale.restype = C.c_int
+    lib.ref_facp_rescale.argtypes = [C.POINTER(N.QpProblem), C.POINTER(N.FacpParameters), _dp, _dp, _dp]
+    return lib
+
+
+def _scaling_cases():
+    rng = np.random.default_rng(12)
+    data_s, _, _ = planted_qp(n=900, m=400, b_rows=200, seed=13, q_form="sparse")
+    data_r, _, _ = planted_qp(n=900, m=400, b_rows=200, seed=14, q_form="lowrank")
+    n, m = 700, 300
+    A = sp.random(m, n, density=0.02, random_state=15, format="csr")
+    A.data *= 10.0 ** rng.uniform(-3, 3, A.nnz)
+    Qd = sp.diags(rng.uniform(1e-4, 50.0, n)).tocsr()
+    b = A @ rng.uniform(-1, 1, n)
+    data_d = QPData(rng.standard_normal(n) * 30, A, b - rng.random(m), np.where(rng.random(m) < 0.5, b, np.inf),
+                    np.where(rng.random(n) < 0.1, -np.inf, -3.0), np.full(n, 4.0), Q=Qd)
+    d = random_lp(300, 700, 5, seed=16)
+    data_l = QPData(d.c, d.A, d.con_lb, d.con_ub, d.var_lb, d.var_ub)
+    return {"sparse": data_s, "lowrank": data_r, "diag": data_d, "lp": data_l}
+
+
+@pytest.mark.parametrize("case", ["sparse", "lowrank", "diag", "lp"])
+@pytest.mark.parametrize("prm", [{"l_inf_ruiz_iterations": 10}, {"l_inf_ruiz_iterations": 3, "pock_chambolle_alpha": 0.6},
+                                 {"l_inf_ruiz_iterations": 0, "has_pock_chambolle_alpha": False,
+                                  "bound_objective_rescaling": False}], ids=["default", "pc0.6", "off"])
+def test_oracle_equilibration_is_the_reference_preconditioner(case, prm):
+    """Pins the oracle's equilibration on the reference's own code: scale
+    vectors and bound/objective factors bit for bit (the device equilibration
+    is held to the oracle bit for bit by tests/test_qp_gpu.py)."""
+    lib = _reference_precond()
+    data = _scaling_cases()[case]
+    d_o, r_o, cbr_o, ovr_o = O.qp_scaling(data, prm)
+    prob = O._QpProblem(data)
+    p = O._qp_apply_params(O.qp_default_parameters(), prm)
+    n, m = prob.n, prob.m
+    d, r, f = np.zeros(max(n, 1)), np.zeros(max(m, 1)), np.zeros(2)
+    assert lib.ref_facp_rescale(C.byref(prob.p), C.byref(p), d.ctypes.data_as(C.POINTER(C.c_double)),
+                                r.ctypes.data_as(C.POINTER(C.c_double)), f.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    assert np.array_equal(d[:n], d_o) and np.array_equal(r[:m], r_o)
+    assert f[0] == cbr_o and f[1] == ovr_o

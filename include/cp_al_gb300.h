@@ -109,6 +109,10 @@ typedef struct {
     double upload_sec;
     double equilibration_sec;
     double power_sec;
+    /* feasibility polishing of the last solve: termination_reason_t of its
+     * primal and dual phases (-1: not run) */
+    int polish_primal_status;
+    int polish_dual_status;
 } cp_al_gb300_stats_t;
 
 /* The reference defaults of every field, ignoring the environment. */

@@ -43,6 +43,7 @@
 namespace {
 
 int g_threads = 1;
+int g_polish_status[2] = {-1, -1};
 
 struct Csr {
     int nr = 0, nc = 0;
@@ -761,6 +762,161 @@ bool oracle_block(Solver &S, bool &do_restart, int &charged, double elapsed, int
     return false;
 }
 
+/* ---------------- feasibility polishing (LP/CP_AL/src/solver.cu:3912-4456) ----------------
+ * Primal polishing solves the feasibility problem (c = 0) from the final
+ * primal iterates with the dual iterates at zero; dual polishing solves the
+ * problem with every finite bound set to zero from the final dual iterates
+ * with the primal iterates at zero.  Both keep the step size and the AL /
+ * sigma state of the solve, take the primal weight of the start of the
+ * solve, run the iteration in blocks of F with the restart rule on a
+ * one-sided fixed-point error (|x^ - x_bar|^2 w, or |y^ - y_bar|^2 / w), and
+ * stop when their relative residual is below eps_feas_polish_relative.  A
+ * successful phase replaces the solve's primal (dual) solution, residuals and
+ * objective; the primal objective is then taken without the objective
+ * constant (utils.cu:1388-1391 adds the polishing state's constant, which is
+ * zero). */
+struct PolishOut {
+    termination_reason_t reason = TERMINATION_REASON_UNSPECIFIED;
+    int total = 0;
+};
+
+static PolishOut polish_phase(const Solver &S, bool primal, Solver &W) {
+    const int F = S.P->termination_evaluation_frequency;
+    const int n = S.n, m = S.m;
+    W = S;
+    if (primal) { /* solver.cu:4147-4200 */
+        std::fill(W.c.begin(), W.c.end(), 0.0);
+        for (auto *v : {&W.y0, &W.y, &W.yh, &W.ybar}) std::fill(v->begin(), v->end(), 0.0);
+        std::fill(W.dprod.begin(), W.dprod.end(), 0.0);
+    } else { /* solver.cu:4245-4330 */
+        auto zero_finite = [](std::vector<double> &v) {
+            for (double &x : v)
+                if (std::isfinite(x)) x = 0.0;
+        };
+        zero_finite(W.clb);
+        zero_finite(W.cub);
+        zero_finite(W.vlb);
+        zero_finite(W.vub);
+        std::fill(W.clb_fin.begin(), W.clb_fin.end(), 0.0);
+        std::fill(W.cub_fin.begin(), W.cub_fin.end(), 0.0);
+        for (auto *v : {&W.x0, &W.x, &W.xh, &W.xbar}) std::fill(v->begin(), v->end(), 0.0);
+        std::fill(W.pprod.begin(), W.pprod.end(), 0.0);
+    }
+    if (primal) std::fill(W.lam.begin(), W.lam.end(), 0.0);
+    W.pw_esum = W.pw_last = 0.0;
+    W.fp = W.fp0 = W.fp_last = INFINITY;
+    W.total = W.inner = 0;
+    W.reason = TERMINATION_REASON_UNSPECIFIED;
+    W.best_gap = INFINITY;
+    const double pw0 = S.P->bound_objective_rescaling ? 1.0 : (S.obj_norm + 1.0) / (S.bnd_norm + 1.0);
+    W.pw = pw0;
+    W.best_pw = pw0;
+    auto fpe = [&]() {
+        double acc = 0.0;
+        if (primal) {
+            for (int j = 0; j < n; ++j) acc += (W.xh[j] - W.xbar[j]) * (W.xh[j] - W.xbar[j]);
+            return acc * W.pw;
+        }
+        for (int i = 0; i < m; ++i) acc += (W.yh[i] - W.ybar[i]) * (W.yh[i] - W.ybar[i]);
+        return acc / W.pw;
+    };
+    const double eps = S.P->termination_criteria.eps_feas_polish_relative;
+    const int limit = S.P->termination_criteria.iteration_limit;
+    bool do_restart = false;
+    PolishOut out;
+    while (W.reason == TERMINATION_REASON_UNSPECIFIED) { /* solver.cu:3988-4051, 4063-4126 */
+        W.primal(1, true);
+        W.dual(1, true);
+        if (do_restart) {
+            W.fp = fpe();
+            W.fp0 = W.fp;
+            do_restart = false;
+        }
+        for (int i = 2; i <= F - 1; ++i) {
+            W.primal(i, false);
+            W.dual(i, false);
+        }
+        W.primal(F, true);
+        W.dual(F, true);
+        W.fp = fpe();
+        if (primal) { /* utils.cu:1341-1392 */
+            spmv(W.A, W.xh.data(), W.pprod.data());
+            for (int i = 0; i < m; ++i)
+                W.rp[i] = (W.pprod[i] - std::fmax(W.clb[i], std::fmin(W.pprod[i], W.cub[i]))) * W.rcum[i];
+            W.abs_p = (S.P->optimality_norm == NORM_TYPE_L_INF ? amax(W.rp) : nrm2(W.rp)) / W.cbr;
+            W.rel_p = W.abs_p / (1.0 + W.bnd_norm);
+            W.pobj = dot(S.c, W.xh) / (W.cbr * W.ovr);
+        } else { /* utils.cu:1394-1453 */
+            spmv(W.At, W.yh.data(), W.dprod.data());
+            for (int j = 0; j < n; ++j) W.rd[j] = (W.c[j] - W.dprod[j] - W.lam[j]) * W.dcum[j];
+            double csum = 0.0;
+            for (int i = 0; i < m; ++i)
+                csum += std::fmax(W.yh[i], 0.0) * S.clb_fin[i] + std::fmin(W.yh[i], 0.0) * S.cub_fin[i];
+            W.abs_d = (S.P->optimality_norm == NORM_TYPE_L_INF ? amax(W.rd) : nrm2(W.rd)) / W.ovr;
+            W.rel_d = W.abs_d / (1.0 + W.obj_norm);
+            W.dobj = (dot(W.lam, S.xh) + csum) / (W.cbr * W.ovr) + W.obj_const;
+        }
+        W.inner += F;
+        W.total += F;
+        /* utils.cu:1194-1226 (the time limit of the solve is not applied here) */
+        if ((primal ? W.rel_p : W.rel_d) <= eps)
+            W.reason = TERMINATION_REASON_FEAS_POLISH_SUCCESS;
+        else if (W.total >= limit)
+            W.reason = TERMINATION_REASON_ITERATION_LIMIT;
+        if (W.reason != TERMINATION_REASON_UNSPECIFIED) break;
+        do_restart = W.should_restart(F);
+        if (do_restart) { /* solver.cu:4376-4404 */
+            if (primal) {
+                W.x0 = W.xh;
+                W.x = W.xh;
+            } else {
+                W.y0 = W.yh;
+                W.y = W.yh;
+            }
+            W.inner = 0;
+            W.fp_last = INFINITY;
+        }
+    }
+    out.reason = W.reason;
+    out.total = W.total;
+    return out;
+}
+
+/* returns the iterations the two phases add to feasibility_iteration */
+static int oracle_polish(Solver &S, int *primal_status, int *dual_status) {
+    *primal_status = *dual_status = -1;
+    const double eps = S.P->termination_criteria.eps_feas_polish_relative;
+    if (S.rel_p < eps && S.rel_d < eps) return 0; /* solver.cu:3915-3920 */
+    int iters = 0;
+    {
+        std::unique_ptr<Solver> W(new Solver());
+        PolishOut o = polish_phase(S, true, *W);
+        *primal_status = (int)o.reason;
+        if (o.reason == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+            S.xh = W->xh;
+            S.abs_p = W->abs_p;
+            S.rel_p = W->rel_p;
+            S.pobj = W->pobj;
+        }
+        iters += o.total - 1;
+    }
+    {
+        std::unique_ptr<Solver> W(new Solver());
+        PolishOut o = polish_phase(S, false, *W);
+        *dual_status = (int)o.reason;
+        if (o.reason == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+            S.yh = W->yh;
+            S.abs_d = W->abs_d;
+            S.rel_d = W->rel_d;
+            S.dobj = W->dobj;
+        }
+        iters += o.total - 1;
+    }
+    S.gap = std::fabs(S.pobj - S.dobj);
+    S.rel_gap = S.gap / (1.0 + std::fabs(S.pobj) + std::fabs(S.dobj));
+    return iters;
+}
+
 /* result: solver.cu:3828-3909 */
 cp_al_result_t *oracle_result(Solver &S, double rescale_sec, double elapsed) {
     const int n = S.n, m = S.m;
@@ -828,7 +984,27 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
         S->compute_residual();
     }
     if (power_iterations_out) *power_iterations_out = S->power_iters;
-    return oracle_result(*S, rescale_sec, elapsed);
+    int polish_iters = 0, pst = -1, dst = -1;
+    double polish_sec = 0.0;
+    if (params->feasibility_polishing) { /* solver.cu:1715-1719 */
+        auto tp = std::chrono::steady_clock::now();
+        polish_iters = oracle_polish(*S, &pst, &dst);
+        polish_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
+    }
+    cp_al_result_t *r = oracle_result(*S, rescale_sec, elapsed);
+    if (r && params->feasibility_polishing) {
+        r->feasibility_iteration = polish_iters;
+        r->feasibility_polishing_time = polish_sec;
+    }
+    g_polish_status[0] = pst;
+    g_polish_status[1] = dst;
+    return r;
+}
+
+/* statuses of the last solve's primal and dual polishing phases (-1: not run) */
+void oracle_cpal_polish_status(int *primal, int *dual) {
+    *primal = g_polish_status[0];
+    *dual = g_polish_status[1];
 }
 
 /* Session form for timing: setup once, then blocks of iterations. */

@@ -94,6 +94,14 @@ class _Problem:
         self.p, self.m, self.n = p, m, n
 
 
+def _polish_status(L):
+    """Statuses of the last oracle solve's primal and dual polishing phases
+    (names, or None for a phase that did not run)."""
+    a, b = C.c_int(-1), C.c_int(-1)
+    L.oracle_cpal_polish_status(C.byref(a), C.byref(b))
+    return tuple(N.TERMINATION_REASONS.get(v.value) if v.value >= 0 else None for v in (a, b))
+
+
 def solve_lp(data: LPData, params: dict | None = None, options: dict | None = None, threads: int = 1) -> LPResult:
     L = lib()
     p = apply_params(default_parameters(), params)
@@ -123,7 +131,8 @@ def solve_lp(data: LPData, params: dict | None = None, options: dict | None = No
             absolute_dual_residual=r.absolute_dual_residual,
             setup_sec=r.rescaling_time_sec,
             solve_sec=r.cumulative_time_sec,
-            stats={"power_iterations": piters.value},
+            stats={"power_iterations": piters.value, "feasibility_iteration": r.feasibility_iteration,
+                   "feasibility_polishing_time": r.feasibility_polishing_time, "polish_status": _polish_status(L)},
         )
     finally:
         L.oracle_cpal_result_free(rp)

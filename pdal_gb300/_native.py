@@ -220,6 +220,8 @@ class CpalStats(C.Structure):
         ("upload_sec", C.c_double),
         ("equilibration_sec", C.c_double),
         ("power_sec", C.c_double),
+        ("polish_primal_status", C.c_int),
+        ("polish_dual_status", C.c_int),
     ]
 
 

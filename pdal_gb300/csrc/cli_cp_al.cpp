@@ -12,8 +12,7 @@
  * policies the reference runs when CP_AL_UNIFIED_POLICY,
  * CP_AL_FEATURE_AUTO_POLICY, CP_AL_STRUCTURAL_TAIL_CUT or
  * CP_AL_FEATURE_AUDIT_ONLY is set (the command refuses to run with exit
- * code 2), presolve (PSLP is not part of this build) and feasibility
- * polishing (-f prints a warning and solves without it).
+ * code 2) and presolve (PSLP is not part of this build).
  */
 #include "../../include/cp_al.h"
 #include "../../include/cp_al_mps_parser.h"
@@ -124,8 +123,8 @@ void usage(const char *prog) {
     fprintf(stderr, "      --sv_max_iter <int>             Max iterations for singular value estimation "
                     "(default: 5000).\n");
     fprintf(stderr, "      --sv_tol <float>                Tolerance for singular value estimation (default: 1e-4).\n");
-    fprintf(stderr, "  -f  --feasibility_polishing         Feasibility polishing (not built: warns and solves "
-                    "without it).\n");
+    fprintf(stderr, "  -f  --feasibility_polishing         Enable feasibility use feasibility polishing "
+                    "(default: false).\n");
     fprintf(stderr, "      --eps_feas_polish <tolerance>   Relative feasibility polish tolerance (default: 1e-6).\n");
     fprintf(stderr, "      --opt_norm <norm_type>          Norm for optimality criteria: l2 or linf (default: l2).\n");
     fprintf(stderr, "      --no_presolve                   Disable presolve (presolve is not built; accepted).\n");
@@ -205,10 +204,6 @@ int main(int argc, char *argv[]) {
             fprintf(stderr, "Error: %s is set, but the benchmark policy layer is not part of this build.\n", flag);
             return 2;
         }
-    }
-    if (params.feasibility_polishing) {
-        fprintf(stderr, "Warning: feasibility polishing is not part of this build; solving without it.\n");
-        params.feasibility_polishing = false;
     }
     const std::string name = instance_name(filename);
     lp_problem_t *problem = read_mps_file(filename);

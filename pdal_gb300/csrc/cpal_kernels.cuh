@@ -494,6 +494,66 @@ static __global__ void __launch_bounds__(kThreads) k_control(const double *__res
     for (int i = threadIdx.x + 1; i <= p.F; i += kThreads) cpal_halpern_entry(inner, i, wt[i], wtf[i]);
 }
 
+/* ------------------------------------------------------------------ */
+/* feasibility polishing (LP/CP_AL/src/solver.cu:3912-4456)           */
+/* ------------------------------------------------------------------ */
+/* The terms a polishing phase reads from the evaluation partials. */
+struct PolishEval {
+    double rp2, rpmax, rd2, rdmax, dx2, dy2, contrib, lx, cx;
+};
+
+static __global__ void __launch_bounds__(kThreads) k_polish_reduce(const double *__restrict__ prow, int nrow_slots,
+                                                                  const double *__restrict__ pcol, int ncol_slots,
+                                                                  PolishEval *out) {
+    __shared__ double sbuf[11 * (kThreads / 32)];
+    Red<10, 1> r1, r2;
+    reduce_slots(prow, nrow_slots, r1, sbuf);
+    reduce_slots(pcol, ncol_slots, r2, sbuf);
+    if (threadIdx.x == 0) {
+        out->rp2 = r1.s[0];
+        out->contrib = r1.s[1];
+        out->dy2 = r1.s[3];
+        out->rpmax = r1.mx[0];
+        out->rd2 = r2.s[0];
+        out->dx2 = r2.s[1];
+        out->cx = r2.s[3];
+        out->lx = r2.s[4];
+        out->rdmax = r2.mx[0];
+    }
+}
+
+/* the AL predictor u = y - beta (A x - P(A x - y / beta)) from the stored
+ * A x, after the dual iterate changed alone */
+static __global__ void __launch_bounds__(kThreads) k_predictor(int m, const double *__restrict__ ax,
+                                                              const double *__restrict__ y,
+                                                              const double *__restrict__ lb,
+                                                              const double *__restrict__ ub, double *u,
+                                                              const CpalState *__restrict__ st) {
+    Coefs<double> k;
+    load_coefs(st, k);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const double z = fmax(lb[i], fmin(ax[i] - y[i] * k.inv_beta, ub[i]));
+        u[i] = y[i] - k.beta * (ax[i] - z);
+    }
+}
+
+/* every finite entry of v becomes 0 (solver.cu:4237-4245) */
+static __global__ void __launch_bounds__(kThreads) k_zero_finite(int len, double *v) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x)
+        if (isfinite(v[i])) v[i] = 0.0;
+}
+
+/* a . b over len entries by one block in a fixed order */
+static __global__ void __launch_bounds__(kThreads) k_dot_block(int len, const double *__restrict__ a,
+                                                              const double *__restrict__ b, double *out) {
+    __shared__ double sbuf[kThreads / 32];
+    Red<1, 0> r;
+    r.zero();
+    for (int i = threadIdx.x; i < len; i += kThreads) r.s[0] += a[i] * b[i];
+    block_reduce<kThreads, 1, 0>(r, sbuf);
+    if (threadIdx.x == 0) *out = r.s[0];
+}
+
 /* Anchor reset after a restart: x0 = x = x^, y0 = y = y^, A x0 = A x = p^,
  * and the next predictor from the new beta.  The FP64 anchors are written
  * together with the (hi, lo) copies the FP32 phase reads. */

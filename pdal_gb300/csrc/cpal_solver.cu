@@ -124,6 +124,12 @@ class CpalSolver {
      * iteration and initial schedule */
     void setup_device();
     void run_loop();
+    /* feasibility polishing after the loop (LP/CP_AL/src/solver.cu:3912-4456) */
+    void polish();
+    double polish_sec = 0.0;
+    double loop_t0_ = 0.0; /* wall clock at the start of the loop (time limit) */
+    int polish_iters = 0;
+    int polish_status[2] = {-1, -1};
     /* extends the iteration limit by n and continues (session iterate) */
     bool extend(int n);
     void download(cp_al_result_t *res, bool vectors);
@@ -154,6 +160,8 @@ class CpalSolver {
     void launch_dual(int koff, bool major);
     template <typename T>
     void launch_eval();
+    template <typename T>
+    void launch_eval_terms();
     template <typename T>
     void launch_init_ax();
     template <typename T>
@@ -819,6 +827,18 @@ void CpalSolver::launch_iteration(int koff, bool major) {
 }
 
 template <typename T>
+void CpalSolver::launch_eval_terms() {
+    auto &v = vecs<T>();
+    EvalRowArgs<T> ra{v.xh, v.xbar, v.yh, v.ybar, x0_, y0_, ax0_, clb_, cub_, clbf_, cubf_, rsc_, phat_, part_row_,
+                      A_.ev.d.nblocks, v.x, v.y, v.ax};
+    EvalColArgs<T> ca{v.xh, v.xbar, v.yh, v.ybar, v.lam, x0_, c_, dsc_, part_col_, At_.ev.d.nblocks, v.x, v.y};
+    PDAL_WITH_SE(S_ev_, {
+        if (m_ > 0) k_eval_rows<T, SE><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, ra, st_);
+        k_eval_cols<T, SE><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, ca, st_);
+    });
+}
+
+template <typename T>
 void CpalSolver::launch_eval() {
     auto &v = vecs<T>();
     EvalRowArgs<T> ra{v.xh, v.xbar, v.yh, v.ybar, x0_, y0_, ax0_, clb_, cub_, clbf_, cubf_, rsc_, phat_, part_row_,
@@ -918,8 +938,248 @@ void CpalSolver::switch_to_fp64() {
     launch_init_ax<double>();
 }
 
+/*
+ * Feasibility polishing.  Primal phase: c = 0, the dual iterates at zero,
+ * the primal ones as the solve left them; dual phase: every finite bound 0,
+ * the primal iterates at zero, the dual ones as the solve left them.  Each
+ * phase keeps the step size, the AL / sigma coefficients and the counters of
+ * the solve except the primal weight (that of the start of the solve) and the
+ * Halpern counter, and runs blocks of F iterations with the restart rule on a
+ * one-sided fixed-point error until its relative residual is below
+ * eps_feas_polish_relative.  The evaluation kernels of the loop supply the
+ * residual terms; restarts reset one side's anchor and refresh A x0 and the
+ * AL predictor.  A successful phase replaces that side's solution, residuals
+ * and objective (the primal objective without the objective constant, as
+ * utils.cu:1388-1391 computes it).  Runs in FP64: a solve still in its FP32
+ * phase switches to FP64 first.
+ */
+void CpalSolver::polish() {
+    const double t_start = now_sec();
+    const double eps = P_.termination_criteria.eps_feas_polish_relative;
+    const CpalState base = host_state;
+    if (base.rel_p < eps && base.rel_d < eps) return; /* solver.cu:3915-3920 */
+    if (fp32_phase_) {
+        switch_to_fp64();
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
+    }
+    const size_t n = n_, m = m_, mm = std::max<size_t>(m, 1);
+    const int F = cp_.F;
+    auto &v = v64_;
+    /* saved state of the solve: 8 n-vectors, 9 m-vectors, two scalars */
+    double *sv = nullptr;
+    const size_t total_doubles = 8 * n + 9 * mm + 2;
+    PDAL_CUDA(cudaMalloc(&sv, total_doubles * sizeof(double)));
+    PolishEval *pe_d = nullptr, *pe_h = nullptr;
+    PDAL_CUDA(cudaMalloc(&pe_d, sizeof(PolishEval)));
+    PDAL_CUDA(cudaMallocHost(&pe_h, sizeof(PolishEval)));
+    struct Free {
+        double *a;
+        PolishEval *b, *c;
+        ~Free() {
+            if (a) cudaFree(a);
+            if (b) cudaFree(b);
+            if (c) cudaFreeHost(c);
+        }
+    } guard{sv, pe_d, pe_h};
+    double *p = sv;
+    double *s_x = p, *s_x0 = (p += n), *s_xh = (p += n), *s_xbar = (p += n), *s_lam = (p += n), *s_c = (p += n),
+           *s_vlb = (p += n), *s_vub = (p += n);
+    double *s_y = (p += n), *s_y0 = (p += mm), *s_yh = (p += mm), *s_ybar = (p += mm), *s_ax = (p += mm),
+           *s_ax0 = (p += mm), *s_u = (p += mm), *s_clb = (p += mm), *s_cub = (p += mm);
+    double *dot_out = (p += mm);
+    auto cp = [&](double *dst, const double *src, size_t len) {
+        if (len) PDAL_CUDA(cudaMemcpyAsync(dst, src, len * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+    };
+    auto zero = [&](double *dst, size_t len) {
+        if (len) PDAL_CUDA(cudaMemsetAsync(dst, 0, len * sizeof(double), stream_));
+    };
+    auto save = [&]() {
+        cp(s_x, v.x, n), cp(s_x0, x0_, n), cp(s_xh, v.xh, n), cp(s_xbar, v.xbar, n), cp(s_lam, v.lam, n);
+        cp(s_c, c_, n), cp(s_vlb, vlb_, n), cp(s_vub, vub_, n);
+        cp(s_y, v.y, m), cp(s_y0, y0_, m), cp(s_yh, v.yh, m), cp(s_ybar, v.ybar, m), cp(s_ax, v.ax, m);
+        cp(s_ax0, ax0_, m), cp(s_u, v.u, m), cp(s_clb, clb_, m), cp(s_cub, cub_, m);
+    };
+    auto restore = [&]() {
+        cp(v.x, s_x, n), cp(x0_, s_x0, n), cp(v.xh, s_xh, n), cp(v.xbar, s_xbar, n), cp(v.lam, s_lam, n);
+        cp(c_, s_c, n), cp(vlb_, s_vlb, n), cp(vub_, s_vub, n);
+        cp(v.y, s_y, m), cp(y0_, s_y0, m), cp(v.yh, s_yh, m), cp(v.ybar, s_ybar, m), cp(v.ax, s_ax, m);
+        cp(ax0_, s_ax0, m), cp(v.u, s_u, m), cp(clb_, s_clb, m), cp(cub_, s_cub, m);
+    };
+    save();
+    const double pw0 = P_.bound_objective_rescaling ? 1.0 : (cp_.obj_norm + 1.0) / (cp_.bnd_norm + 1.0);
+    const int gm = grid_for(std::max<size_t>(m, 1)), gn = grid_for(std::max<size_t>(n, 1));
+    const int nrow_slots = m_ > 0 ? A_.ev.d.nblocks + A_.ev.d.nlong : 0;
+    const int ncol_slots = At_.ev.d.nblocks + At_.ev.d.nlong;
+    auto evaluate = [&]() {
+        launch_eval_terms<double>();
+        k_polish_reduce<<<1, kThreads, 0, stream_>>>(part_row_, nrow_slots, part_col_, ncol_slots, pe_d);
+        PDAL_LAUNCH_CHECK();
+        launches += 3;
+        PDAL_CUDA(cudaMemcpyAsync(pe_h, pe_d, sizeof(PolishEval), cudaMemcpyDeviceToHost, stream_));
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
+        return *pe_h;
+    };
+    auto refresh_predictor = [&]() {
+        if (beta_on_ && m) {
+            k_predictor<<<gm, kThreads, 0, stream_>>>(m_, v.ax, v.y, clb_, cub_, v.u, st_);
+            PDAL_LAUNCH_CHECK();
+            launches += 1;
+        }
+    };
+    auto dot = [&](const double *a, const double *b) {
+        k_dot_block<<<1, kThreads, 0, stream_>>>(n_, a, b, dot_out);
+        PDAL_LAUNCH_CHECK();
+        launches += 1;
+        double h = 0.0;
+        PDAL_CUDA(cudaMemcpyAsync(&h, dot_out, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
+        return h;
+    };
+    const bool linf = cp_.norm_linf;
+    /* one phase; returns its termination_reason_t code and fills the
+     * residuals of its side */
+    auto phase = [&](bool primal, double &abs_r, double &rel_r, int &total, PolishEval &last) {
+        CpalState s = base;
+        s.status = 0;
+        s.restart = 0;
+        s.pw = pw0;
+        s.best_pw = pw0;
+        s.pw_esum = s.pw_last = 0.0;
+        s.best_gap = INFINITY;
+        s.fp = s.fp0 = s.fp_last = INFINITY;
+        s.inner = 0;
+        s.total = 0;
+        s.fp32_switch_tol = -1.0;
+        cpal_set_coefficients(s);
+        auto push = [&]() {
+            *h_st_ = s;
+            PDAL_CUDA(cudaMemcpyAsync(st_, h_st_, sizeof(CpalState), cudaMemcpyHostToDevice, stream_));
+            k_fill_weights<<<1, kThreads, 0, stream_>>>(st_, wt_, wtf_, F);
+            PDAL_LAUNCH_CHECK();
+            launches += 1;
+        };
+        push();
+        refresh_predictor();
+        const int limit = cp_.iteration_limit;
+        bool do_restart = false;
+        int status = 0;
+        auto fpe = [&](const PolishEval &e) { return primal ? e.dx2 * s.pw : e.dy2 / s.pw; };
+        for (;;) { /* solver.cu:3988-4051 (primal), 4063-4126 (dual) */
+            launch_iteration<double>(1, true);
+            launches += 2;
+            if (do_restart) {
+                s.fp = fpe(evaluate());
+                s.fp0 = s.fp;
+                do_restart = false;
+            }
+            for (int k = 2; k <= F - 1; ++k) launch_iteration<double>(k, false);
+            launch_iteration<double>(F, true);
+            launches += 2 * (F - 1);
+            last = evaluate();
+            s.fp = fpe(last);
+            if (primal) { /* utils.cu:1341-1392 */
+                abs_r = (linf ? last.rpmax : std::sqrt(last.rp2)) / s.cbr;
+                rel_r = abs_r / (1.0 + cp_.bnd_norm);
+            } else { /* utils.cu:1394-1453 */
+                abs_r = (linf ? last.rdmax : std::sqrt(last.rd2)) / s.ovr;
+                rel_r = abs_r / (1.0 + cp_.obj_norm);
+            }
+            s.inner += F;
+            s.total += F;
+            /* utils.cu:1194-1226; the time limit is the solve's */
+            if (rel_r <= eps) {
+                status = TERMINATION_REASON_FEAS_POLISH_SUCCESS;
+                break;
+            }
+            if (s.total >= limit) {
+                status = TERMINATION_REASON_ITERATION_LIMIT;
+                break;
+            }
+            if (now_sec() - loop_t0_ >= cp_.time_limit) {
+                status = TERMINATION_REASON_TIME_LIMIT;
+                break;
+            }
+            do_restart = cpal_should_restart(s, cp_);
+            if (do_restart) { /* solver.cu:4376-4404 */
+                if (primal) {
+                    cp(v.x, v.xh, n);
+                    cp(x0_, v.xh, n);
+                    push();
+                    launch_init_ax<double>(); /* A x0 = A x and the predictor */
+                } else {
+                    cp(v.y, v.yh, m);
+                    cp(y0_, v.yh, m);
+                }
+                s.inner = 0;
+                s.fp_last = INFINITY;
+            }
+            push();
+            if (do_restart && !primal) refresh_predictor();
+        }
+        total = s.total;
+        return status;
+    };
+    CpalState out = base;
+    int iters = 0;
+    {   /* primal phase (solver.cu:4131-4200 state) */
+        zero(c_, n);
+        zero(v.y, m), zero(y0_, m), zero(v.yh, m), zero(v.ybar, m), zero(v.lam, n);
+        double abs_r = 0, rel_r = 0;
+        int total = 0;
+        PolishEval last{};
+        const int st = phase(true, abs_r, rel_r, total, last);
+        polish_status[0] = st;
+        if (st == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+            out.abs_p = abs_r;
+            out.rel_p = rel_r;
+            out.pobj = dot(s_c, v.xh) / (base.cbr * base.ovr);
+            cp(s_xh, v.xh, n);
+        }
+        iters += total - 1;
+        restore();
+    }
+    {   /* dual phase (solver.cu:4247-4330 state) */
+        for (double *b : {clb_, cub_})
+            if (m) k_zero_finite<<<gm, kThreads, 0, stream_>>>(m_, b);
+        for (double *b : {vlb_, vub_}) k_zero_finite<<<gn, kThreads, 0, stream_>>>(n_, b);
+        PDAL_LAUNCH_CHECK();
+        launches += 4;
+        zero(v.x, n), zero(x0_, n), zero(v.xh, n), zero(v.xbar, n), zero(v.ax, m), zero(ax0_, m);
+        double abs_r = 0, rel_r = 0;
+        int total = 0;
+        PolishEval last{};
+        const int st = phase(false, abs_r, rel_r, total, last);
+        polish_status[1] = st;
+        if (st == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+            out.abs_d = abs_r;
+            out.rel_d = rel_r;
+            out.dobj = (dot(v.lam, s_xh) + last.contrib) / (base.cbr * base.ovr) + cp_.obj_const;
+            cp(s_yh, v.yh, m);
+        }
+        iters += total - 1;
+        restore();
+    }
+    out.gap = std::fabs(out.pobj - out.dobj);
+    out.rel_gap = out.gap / (1.0 + std::fabs(out.pobj) + std::fabs(out.dobj));
+    host_state.abs_p = out.abs_p;
+    host_state.rel_p = out.rel_p;
+    host_state.pobj = out.pobj;
+    host_state.abs_d = out.abs_d;
+    host_state.rel_d = out.rel_d;
+    host_state.dobj = out.dobj;
+    host_state.gap = out.gap;
+    host_state.rel_gap = out.rel_gap;
+    /* the device state returns to the solve's, for the result kernels */
+    *h_st_ = host_state;
+    PDAL_CUDA(cudaMemcpyAsync(st_, h_st_, sizeof(CpalState), cudaMemcpyHostToDevice, stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    polish_iters = iters;
+    polish_sec = now_sec() - t_start;
+}
+
 void CpalSolver::run_loop() {
     const double t0 = now_sec();
+    loop_t0_ = t0;
     const int F = cp_.F;
     const int G = std::max(1, O_.graph_blocks);
     const int64_t per_block = 2LL * F - (m_ == 0 ? F : 0) + (m_ > 0 ? 4 : 3);
@@ -1127,6 +1387,8 @@ static void fill_stats(const pdal::CpalSolver &s, double total) {
     st.upload_sec = s.upload_sec;
     st.equilibration_sec = s.equil_sec;
     st.power_sec = s.power_sec;
+    st.polish_primal_status = s.polish_status[0];
+    st.polish_dual_status = s.polish_status[1];
 }
 
 cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *params,
@@ -1158,8 +1420,12 @@ cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *
         s.upload();
         s.setup_device();
         s.run_loop();
+        /* solver.cu:1715-1719 (the LP path has no infeasibility statuses) */
+        if (local.feasibility_polishing) s.polish();
         s.result_on_device();
         s.download(res, true);
+        res->feasibility_polishing_time = s.polish_sec;
+        res->feasibility_iteration = s.polish_iters;
         fill_stats(s, pdal::now_sec() - t0);
         if (local.verbose) {
             printf("Solution Summary\n  Status                 : %d\n  Iterations             : %d\n"

@@ -98,7 +98,7 @@ def default_options(lib=None, from_env: bool = False) -> N.CpalOptions:
 def apply_params(p: N.CpalParameters, d: dict | None) -> N.CpalParameters:
     """Keys: any field of cp_al_parameters_t, plus 'eps' (sets both relative
     tolerances), 'iteration_limit', 'time_limit', 'eps_optimal', 'eps_feasible',
-    'linf' (optimality norm)."""
+    'eps_feas_polish', 'linf' (optimality norm)."""
     for k, v in (d or {}).items():
         if k == "eps":
             p.termination_criteria.eps_optimal_relative = v
@@ -109,6 +109,8 @@ def apply_params(p: N.CpalParameters, d: dict | None) -> N.CpalParameters:
             p.termination_criteria.eps_feasible_relative = v
         elif k == "iteration_limit":
             p.termination_criteria.iteration_limit = int(v)
+        elif k == "eps_feas_polish":
+            p.termination_criteria.eps_feas_polish_relative = v
         elif k == "time_limit":
             p.termination_criteria.time_sec_limit = float(v)
         elif k == "linf":
@@ -180,6 +182,8 @@ def _result_from_c(lib, r: N.CpalResult, m: int, n: int, with_vectors: bool = Tr
     st = N.CpalStats()
     lib.cp_al_gb300_last_stats(C.byref(st))
     stats = {f: getattr(st, f) for f, _ in N.CpalStats._fields_}
+    stats["feasibility_iteration"] = r.feasibility_iteration
+    stats["feasibility_polishing_time"] = r.feasibility_polishing_time
     return LPResult(
         status=N.TERMINATION_REASONS.get(r.termination_reason, str(r.termination_reason)),
         status_code=r.termination_reason,

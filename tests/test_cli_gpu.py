@@ -94,3 +94,18 @@ def test_fa_cp_command_matches_library(tmp_path, qp_lib):
     assert its == sorted(its)
     kkt = [float(b[5]) for b in body]
     assert kkt[-1] <= 1e-8
+
+
+def test_cp_al_command_feasibility_polishing(tmp_path, lp_lib):
+    data = instances.random_lp(300, 800, 6, seed=17)
+    src = mps.write_lp(data, tmp_path / "loose.mps")
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(N.LIBDIR / "cp_al"), "-f", "--eps_opt", "1e-3", "--eps_feas", "1e-3", "--eps_feas_polish",
+                        "1e-8", "--l_inf_ruiz_iter", "4", str(src), str(out)], capture_output=True, text=True,
+                       env=clean_env(), timeout=300)
+    assert r.returncode == 0, r.stderr
+    s = summary(out / "loose_summary.txt")
+    assert list(s) == LP_KEYS + ["Feasibility Polishing Time (sec)", "Feasibility Polishing Iteration Count"]
+    assert float(s["Relative Primal Residual"]) <= 1e-8 and float(s["Relative Dual Residual"]) <= 1e-8
+    assert int(s["Feasibility Polishing Iteration Count"]) > 0

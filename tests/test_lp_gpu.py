@@ -220,3 +220,30 @@ def test_restart_target_selection_parity(lp_lib, options):
     g, o = both(d, {"eps": 1e-8, "l_inf_ruiz_iterations": 4}, options)
     assert g.status == "OPTIMAL"
     assert_parity(g, o)
+
+
+@pytest.mark.parametrize("kind", ["random", "transport"])
+def test_feasibility_polishing_matches_oracle(kind):
+    """Feasibility polishing (LP/CP_AL/src/solver.cu:3912-4456) after a loose
+    solve: both phases reach eps_feas_polish_relative on the GPU and in the
+    oracle, the polished solution has the oracle's residual scale and
+    objective, and the phases take the same number of iterations within one
+    evaluation block."""
+    data = I.random_lp(300, 800, 6, seed=17) if kind == "random" else I.transport_lp(15, 12, seed=5)
+    prm = {"eps": 1e-3, "l_inf_ruiz_iterations": 4, "feasibility_polishing": True, "eps_feas_polish": 1e-8}
+    g = lp.solve(data, prm)
+    o = O.solve_lp(data, prm)
+    assert g.status == o.status
+    assert (g.stats["polish_primal_status"], g.stats["polish_dual_status"]) == (7, 7)
+    assert o.stats["polish_status"] == ("FEAS_POLISH_SUCCESS", "FEAS_POLISH_SUCCESS")
+    assert g.relative_primal_residual <= 1e-8 and g.relative_dual_residual <= 1e-8
+    assert abs(g.primal_objective - o.primal_objective) <= 1e-6 * (1 + abs(o.primal_objective))
+    assert abs(g.stats["feasibility_iteration"] - o.stats["feasibility_iteration"]) <= 400
+    # the polished point is primal feasible for the original problem
+    rp, ci, v, (m, n) = data.csr()
+    import scipy.sparse as sp
+
+    A = sp.csr_matrix((v, ci, rp), shape=(m, n))
+    ax = A @ g.x
+    viol = np.maximum(np.asarray(data.con_lb) - ax, 0) + np.maximum(ax - np.asarray(data.con_ub), 0)
+    assert np.linalg.norm(viol) <= 1e-6 * (1 + np.linalg.norm(np.nan_to_num(data.con_ub, posinf=0)))

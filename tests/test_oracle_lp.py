@@ -109,3 +109,23 @@ def test_defaults_are_the_reference_defaults(lp_lib):
     for name, _ in type(o_or)._fields_:
         a, b = getattr(o_prod, name), getattr(o_or, name)
         assert (a == b) or (np.isnan(a) and np.isnan(b)), name
+
+
+def test_oracle_feasibility_polishing():
+    """The oracle's feasibility polishing (LP/CP_AL/src/solver.cu:3912-4456):
+    after a loose solve both phases reach the polishing tolerance, the
+    primal objective moves toward the optimum, and a solve that is already
+    feasible enough runs no polishing iterations."""
+    from pdal_gb300.instances import random_lp
+
+    d = random_lp(300, 800, 6, seed=17)
+    loose = O.solve_lp(d, {"eps": 1e-3, "l_inf_ruiz_iterations": 4})
+    pol = O.solve_lp(d, {"eps": 1e-3, "l_inf_ruiz_iterations": 4, "feasibility_polishing": True,
+                         "eps_feas_polish": 1e-8})
+    assert pol.stats["polish_status"] == ("FEAS_POLISH_SUCCESS", "FEAS_POLISH_SUCCESS")
+    assert pol.relative_primal_residual <= 1e-8 < loose.relative_primal_residual
+    assert pol.relative_dual_residual <= 1e-8
+    assert pol.iterations == loose.iterations and pol.stats["feasibility_iteration"] > 0
+    tight = O.solve_lp(d, {"eps": 1e-9, "l_inf_ruiz_iterations": 4, "feasibility_polishing": True,
+                           "eps_feas_polish": 1e-6})
+    assert tight.stats["polish_status"] == (None, None) and tight.stats["feasibility_iteration"] == 0

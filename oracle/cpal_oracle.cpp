@@ -780,7 +780,8 @@ struct PolishOut {
     int total = 0;
 };
 
-static PolishOut polish_phase(const Solver &S, bool primal, Solver &W) {
+static PolishOut polish_phase(const Solver &S, bool primal, Solver &W,
+                              std::chrono::steady_clock::time_point solve_start) {
     const int F = S.P->termination_evaluation_frequency;
     const int n = S.n, m = S.m;
     W = S;
@@ -858,11 +859,14 @@ static PolishOut polish_phase(const Solver &S, bool primal, Solver &W) {
         }
         W.inner += F;
         W.total += F;
-        /* utils.cu:1194-1226 (the time limit of the solve is not applied here) */
+        /* utils.cu:1194-1226; the time limit counts from the start of the solve */
+        const double since = std::chrono::duration<double>(std::chrono::steady_clock::now() - solve_start).count();
         if ((primal ? W.rel_p : W.rel_d) <= eps)
             W.reason = TERMINATION_REASON_FEAS_POLISH_SUCCESS;
         else if (W.total >= limit)
             W.reason = TERMINATION_REASON_ITERATION_LIMIT;
+        else if (since >= S.P->termination_criteria.time_sec_limit)
+            W.reason = TERMINATION_REASON_TIME_LIMIT;
         if (W.reason != TERMINATION_REASON_UNSPECIFIED) break;
         do_restart = W.should_restart(F);
         if (do_restart) { /* solver.cu:4376-4404 */
@@ -883,14 +887,15 @@ static PolishOut polish_phase(const Solver &S, bool primal, Solver &W) {
 }
 
 /* returns the iterations the two phases add to feasibility_iteration */
-static int oracle_polish(Solver &S, int *primal_status, int *dual_status) {
+static int oracle_polish(Solver &S, int *primal_status, int *dual_status,
+                         std::chrono::steady_clock::time_point solve_start) {
     *primal_status = *dual_status = -1;
     const double eps = S.P->termination_criteria.eps_feas_polish_relative;
     if (S.rel_p < eps && S.rel_d < eps) return 0; /* solver.cu:3915-3920 */
     int iters = 0;
     {
         std::unique_ptr<Solver> W(new Solver());
-        PolishOut o = polish_phase(S, true, *W);
+        PolishOut o = polish_phase(S, true, *W, solve_start);
         *primal_status = (int)o.reason;
         if (o.reason == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
             S.xh = W->xh;
@@ -902,7 +907,7 @@ static int oracle_polish(Solver &S, int *primal_status, int *dual_status) {
     }
     {
         std::unique_ptr<Solver> W(new Solver());
-        PolishOut o = polish_phase(S, false, *W);
+        PolishOut o = polish_phase(S, false, *W, solve_start);
         *dual_status = (int)o.reason;
         if (o.reason == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
             S.yh = W->yh;
@@ -988,7 +993,7 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
     double polish_sec = 0.0;
     if (params->feasibility_polishing) { /* solver.cu:1715-1719 */
         auto tp = std::chrono::steady_clock::now();
-        polish_iters = oracle_polish(*S, &pst, &dst);
+        polish_iters = oracle_polish(*S, &pst, &dst, t_start);
         polish_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
     }
     cp_al_result_t *r = oracle_result(*S, rescale_sec, elapsed);

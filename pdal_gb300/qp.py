@@ -142,6 +142,8 @@ def apply_params(p: N.FacpParameters, d: dict | None) -> N.FacpParameters:
             p.termination_criteria.eps_feasible_relative = v
         elif k == "time_limit":
             p.termination_criteria.time_sec_limit = float(v)
+        elif k == "eps_feas_polish":
+            p.termination_criteria.eps_feas_polish_relative = float(v)
         elif k == "linf":
             p.optimality_norm = N.NORM_LINF if v else N.NORM_L2
         elif k == "optimality_norm":

@@ -668,7 +668,7 @@ __global__ void k_convert(const A *__restrict__ src, B *dst, int len) {
 /* warp per row: s = clamp_sqrt(max |a| or sum |a|^deg), cum *= s
  * (preconditioner.cu:532-550, 634-667). mode 0 = abs max, 1 = power sum. */
 static __global__ void k_row_scale(int nr, const int *__restrict__ rp, const double *__restrict__ val, int mode, double deg,
-                            double *scale, double *cum) {
+                            double *scale, double *cum, double *inv) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nr; row += warps) {
@@ -699,21 +699,24 @@ static __global__ void k_row_scale(int nr, const int *__restrict__ rp, const dou
             const double s = (acc < 1e-12) ? 1.0 : sqrt(acc);
             cum[row] *= s;
             scale[row] = s;
+            inv[row] = 1.0 / s;
         }
     }
 }
 
 /* A values *= (1/d[j]) * (1/r[i]); rows of this matrix are scaled by
- * row_is_var ? d : r (preconditioner.cu:514-530). */
+ * row_is_var ? d : r (preconditioner.cu:514-530).  The reciprocals come from
+ * k_row_scale (the same 1/s, computed once per row instead of once per
+ * nonzero: the FP64 divisions dominated this kernel on GB300's FP64 pipe). */
 static __global__ void k_scale_matrix(int nr, const int *__restrict__ rp, const int *__restrict__ ci, double *val,
-                               const double *__restrict__ rowscale, const double *__restrict__ colscale,
+                               const double *__restrict__ inv_rowscale, const double *__restrict__ inv_colscale,
                                int row_is_var) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nr; row += warps) {
-        const double inv_row = 1.0 / rowscale[row];
+        const double inv_row = inv_rowscale[row];
         for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) {
-            const double inv_col = 1.0 / colscale[ci[k]];
+            const double inv_col = inv_colscale[ci[k]];
             val[k] *= row_is_var ? inv_row * inv_col : inv_col * inv_row;
         }
     }

@@ -608,11 +608,14 @@ void CpalSolver::setup_device() {
     PDAL_CUDA(cudaMemcpyAsync(dsc_, ones_n.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
     if (m) PDAL_CUDA(cudaMemcpyAsync(rsc_, ones_m.data(), m * sizeof(double), cudaMemcpyHostToDevice, stream_));
     double *rstep = tmp_m_, *dstep = tmp_n_;
+    /* reciprocal scales: an m- and an n-sized buffer the iteration has not
+     * started to use (x_bar is cleared before the first iteration) */
+    double *rinv = tmp_m2_, *dinv = v64_.xbar;
     auto scale_pass = [&](int mode, double deg_rows, double deg_cols) {
-        if (m) k_row_scale<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.v, mode, deg_rows, rstep, rsc_);
-        k_row_scale<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.v, mode, deg_cols, dstep, dsc_);
-        if (m) k_scale_matrix<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, A_.v, rstep, dstep, 0);
-        k_scale_matrix<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, At_.v, dstep, rstep, 1);
+        if (m) k_row_scale<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.v, mode, deg_rows, rstep, rsc_, rinv);
+        k_row_scale<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.v, mode, deg_cols, dstep, dsc_, dinv);
+        if (m) k_scale_matrix<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, A_.v, rinv, dinv, 0);
+        k_scale_matrix<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, At_.v, dinv, rinv, 1);
         k_scale_vectors<<<grid_for(std::max(n, m)), kThreads, 0, stream_>>>(n_, m_, dstep, rstep, c_, vlb_, vub_, x0_,
                                                                             clb_, cub_, y0_);
         PDAL_LAUNCH_CHECK();

@@ -241,3 +241,38 @@ def test_cli_sigma_rule_names_and_policy_refusal(tmp_path):
     env = {"PATH": "/usr/bin:/bin", "CP_AL_UNIFIED_POLICY": "1"}
     r = subprocess.run([str(_exe("cp_al")), "a.mps", str(tmp_path)], capture_output=True, text=True, env=env)
     assert r.returncode == 2 and "CP_AL_UNIFIED_POLICY" in r.stderr
+
+
+@pytest.mark.parametrize("quad", [False, True])
+def test_reader_matches_reference_on_mutated_texts(quad, lp_lib, qp_lib, tmp_path):
+    """Seeded mutations of valid texts (lines dropped or repeated, tokens
+    dropped, stray tokens such as 1e309, nan, -inf, hex floats, names,
+    'MARKER' appended): the two readers agree on every one, refusal included."""
+    import random
+
+    ref = reference_libs()[quad]
+    rng = random.Random(7 + quad)
+    extras = ["1e309", "nan", "-inf", "X1", "R0", "'MARKER'", "0x1p3", "+", "COST"]
+    for it in range(150):
+        lines = messy_mps(7000 + it, quad).split("\n")
+        for _ in range(rng.randint(1, 6)):
+            op, i = rng.randint(0, 3), rng.randrange(len(lines))
+            if op == 0 and len(lines) > 1:
+                del lines[i]
+            elif op == 1:
+                lines.insert(i, lines[rng.randrange(len(lines))])
+            elif op == 2:
+                toks = lines[i].split()
+                if toks:
+                    del toks[rng.randrange(len(toks))]
+                lines[i] = " ".join(toks)
+            else:
+                lines[i] = lines[i] + " " + rng.choice(extras)
+        src = tmp_path / f"m{it}.{'qps' if quad else 'mps'}"
+        src.write_text("\n".join(lines))
+        want = ours(ref, src, quad)
+        got = ours(qp_lib if quad else lp_lib, src, quad)
+        if want is None:
+            assert got is None, it
+        else:
+            assert_same(got, want, f"mutation {it}")

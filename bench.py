@@ -145,15 +145,21 @@ def run_profile(args, local):
     """Only the chosen-form iteration steps on the large LP (no other
     sections): the command the ncu captures in profiles/ run.  With
     --profile-section qp: 300 iterations of the full-size QP (one persistent
-    k_facp launch per evaluation segment); batch: one k_batch_lp launch over
-    304 small LPs (m log-uniform in [50, 400]), chosen form."""
+    k_facp launch per evaluation segment), qp_fp32 the same in FP32 segments;
+    batch: one k_batch_lp launch over 304 small LPs (m log-uniform in
+    [50, 400]), chosen form."""
     from pdal_gb300 import instances, lp
 
-    if args.profile_section == "qp":
+    if args.profile_section in ("qp", "qp_fp32"):
         from pdal_gb300 import qp
 
         qd, _, _ = instances.planted_qp()
-        r = qp.solve(qd, {"eps": 1e-12, "verbose": 0, "iteration_limit": 300}, {"device": local})
+        opts = {"device": local}
+        if args.profile_section == "qp_fp32":
+            opts["precision"] = "fp32_refine"
+            opts["fp32_switch_tol"] = 0.0  # the whole run in FP32 segments
+            opts["fp32_stall_evals"] = 0
+        r = qp.solve(qd, {"eps": 1e-12, "verbose": 0, "iteration_limit": 300}, opts)
         print(json.dumps({"profile_run": "qp", "iterations": r.iterations, "inner_iterations": r.inner_iterations,
                           "kernel_launches": r.stats["kernel_launches"]}), flush=True)
         return
@@ -504,7 +510,7 @@ def main():
     ap.add_argument("--workload", default="large_lp", choices=list(WORKLOADS))
     ap.add_argument("--lp-only", action="store_true", help="skip the QP, batch and learned-start sections")
     ap.add_argument("--profile", action="store_true", help="only the chosen-form iteration steps (for ncu)")
-    ap.add_argument("--profile-section", default="lp", choices=["lp", "qp", "batch"],
+    ap.add_argument("--profile-section", default="lp", choices=["lp", "qp", "qp_fp32", "batch"],
                     help="with --profile: which solver's kernels to run")
     args = ap.parse_args()
     rank, world, local = dist_env()

@@ -20,7 +20,7 @@ resident session (every evaluation, restart and phase decision included).
   plain_fp64  the same metric for the plain FP64 form
   time_to_kkt the time to relative KKT 1e-6 of both forms on the plain CP_AL
             LP (2,000 x 5,000), which converges in seconds; the large LP needs
-            minutes per solve
+            minutes per solve (FP64 reaches KKT 3e-5 after 100 s)
 
 Further sections of the same JSON line (skipped with --lp-only):
   fa_cp_qp            the FA_CP convex QP at its benchmark size: time to

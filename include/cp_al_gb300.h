@@ -52,10 +52,15 @@ typedef struct {
     double restart_sufficient;    /* CP_AL_RESTART_SUFFICIENT; NaN = params */
     double restart_necessary;     /* CP_AL_RESTART_NECESSARY; NaN = params */
     double restart_artificial;    /* CP_AL_RESTART_ARTIFICIAL; NaN = params */
-    int restart_select;           /* CP_AL_RESTART_SELECT, 0 = off (solver.cu:2749-2819) */
+    int restart_select;           /* CP_AL_RESTART_SELECT (solver.cu:2749-2819): 0 = off; 1 = restart
+                                     to the reflected Halpern iterate when its score wins; 2 = always
+                                     to it; 3 = best of the current point, the reflected and the
+                                     plain Halpern iterate */
     double restart_select_margin; /* CP_AL_RESTART_SELECT_MARGIN, 1.0 */
     int restart_select_min_iters; /* CP_AL_RESTART_SELECT_MIN_ITERS, 0 */
-    int restart_select_threepoint;/* CP_AL_RESTART_SELECT_THREEPOINT, 0 */
+    int restart_select_threepoint;/* CP_AL_RESTART_SELECT_THREEPOINT, 0 (nonzero: mode 1 also scores
+                                     the plain Halpern iterate) */
+    double restart_select_min_time;/* CP_AL_RESTART_SELECT_MIN_TIME, 0.0 seconds */
 
     /* --- options of this implementation --- */
     int precision;                /* cp_al_gb300_precision_t */

@@ -44,6 +44,7 @@ namespace {
 
 int g_threads = 1;
 int g_polish_status[2] = {-1, -1};
+int g_restart_targets[3] = {0, 0, 0};
 
 struct Csr {
     int nr = 0, nc = 0;
@@ -121,6 +122,7 @@ struct Solver {
     double abs_p = 0, abs_d = 0, rel_p = 0, rel_d = 0, pobj = 0, dobj = 0, gap = 0, rel_gap = 0;
     termination_reason_t reason = TERMINATION_REASON_UNSPECIFIED;
     int power_iters = 0, restarts = 0;
+    int restarts_to[3] = {0, 0, 0}; /* restarts by target: current point, reflected, plain Halpern */
 
     double kp() const { return std::isnan(O.sigma_kp) ? P->restart_params.k_p : O.sigma_kp; }
 
@@ -424,12 +426,12 @@ struct Solver {
         fp_last = fp;
         return rs;
     }
-    /* solver.cu:2663-2747: fixed-point score of candidate (x^, y^) against
-     * the current iterate (x, y) */
-    double restart_delta_score() {
+    /* solver.cu:2663-2747: fixed-point score of candidate (x^, y^) against a
+     * reference point (rx, ry) */
+    double restart_delta_score(const std::vector<double> &rx, const std::vector<double> &ry) {
         std::vector<double> ddx(n), ddy(m), dp(n), pp(m);
-        for (int j = 0; j < n; ++j) ddx[j] = xh[j] - x[j];
-        for (int i = 0; i < m; ++i) ddy[i] = yh[i] - y[i];
+        for (int j = 0; j < n; ++j) ddx[j] = xh[j] - rx[j];
+        for (int i = 0; i < m; ++i) ddy[i] = yh[i] - ry[i];
         spmv(At, ddy.data(), dp.data());
         spmv(A, ddx.data(), pp.data());
         const double pn = nrm2(ddx), dn = nrm2(ddy), axn = nrm2(pp);
@@ -442,30 +444,58 @@ struct Solver {
         const double aug = step * beta * axn * axn;
         return std::sqrt(std::fmax(movement + interaction - aug, 0.0));
     }
-    /* solver.cu:2749-2819 (two-point modes): restart to the Halpern iterate
-     * when its score beats the averaged point's by the margin (mode 1) or
-     * always (mode 2) */
+    /* the plain Halpern point of the last (major) iteration of the block,
+     * w x^ + (1 - w) x0 with that iteration's weight (solver.cu:2392) */
+    std::vector<double> xhal, yhal;
+    void halpern_point() {
+        const double w = (double)inner / (double)(inner + 1);
+        xhal.resize(n);
+        yhal.resize(m);
+        for (int j = 0; j < n; ++j) xhal[j] = w * xh[j] + (1.0 - w) * x0[j];
+        for (int i = 0; i < m; ++i) yhal[i] = w * yh[i] + (1.0 - w) * y0[i];
+    }
+    /* solver.cu:2749-2819: target 1 is the reflected Halpern iterate (x, y),
+     * target 2 the plain Halpern point (three-point mode); the best score
+     * wins when it is within the margin of the current point's (mode 1, 3),
+     * or target 1 is taken always (mode 2) */
     int restart_target = 0;
-    void choose_restart_candidate() {
+    void choose_restart_candidate(double elapsed) {
         restart_target = 0;
         if (O.restart_select == 0) return;
-        if (total < O.restart_select_min_iters) return;
+        if (total < O.restart_select_min_iters || elapsed < O.restart_select_min_time) return;
         const double cur = fp;
-        const double avg = restart_delta_score();
+        const double avg = restart_delta_score(x, y);
+        const bool three = O.restart_select == 3 || O.restart_select_threepoint != 0;
+        double hal = INFINITY;
+        if (three) {
+            halpern_point();
+            hal = restart_delta_score(xhal, yhal);
+        }
         if (O.restart_select == 2) {
             restart_target = 1;
             fp = avg;
         } else if (std::isfinite(cur)) {
-            if (std::isfinite(avg) && avg < cur && avg <= O.restart_select_margin * cur) {
-                restart_target = 1;
-                fp = avg;
+            int best = 0;
+            double best_score = cur;
+            if (std::isfinite(avg) && avg < best_score) {
+                best = 1;
+                best_score = avg;
+            }
+            if (three && std::isfinite(hal) && hal < best_score) {
+                best = 2;
+                best_score = hal;
+            }
+            if (best != 0 && best_score <= O.restart_select_margin * cur) {
+                restart_target = best;
+                fp = best_score;
             }
         }
     }
     void perform_restart() { /* solver.cu:2821-3101 */
         const bool to_current = O.restart_select != 0 && restart_target == 1;
-        const std::vector<double> &rx = to_current ? x : xh;
-        const std::vector<double> &ry = to_current ? y : yh;
+        const bool to_halpern = O.restart_select != 0 && restart_target == 2;
+        const std::vector<double> &rx = to_current ? x : to_halpern ? xhal : xh;
+        const std::vector<double> &ry = to_current ? y : to_halpern ? yhal : yh;
         std::vector<double> ddx(n), ddy(m);
         for (int j = 0; j < n; ++j) ddx[j] = rx[j] - x0[j];
         for (int i = 0; i < m; ++i) ddy[i] = ry[i] - y0[i];
@@ -540,6 +570,15 @@ struct Solver {
             xh = x;
             y0 = y;
             yh = y;
+        } else if (to_halpern) { /* solver.cu:3043-3068 */
+            xbar = xh;
+            ybar = yh;
+            x0 = xhal;
+            x = xhal;
+            xh = xhal;
+            y0 = yhal;
+            y = yhal;
+            yh = yhal;
         } else {
             x0 = xh;
             x = xh;
@@ -549,6 +588,7 @@ struct Solver {
         inner = 0;
         fp_last = INFINITY;
         restarts++;
+        restarts_to[to_current ? 1 : to_halpern ? 2 : 0]++;
     }
     void check_termination(double elapsed) { /* utils.cu:275-317 */
         const auto &T = P->termination_criteria;
@@ -613,6 +653,7 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->restart_select_margin = 1.0;
     o->restart_select_min_iters = 0;
     o->restart_select_threepoint = 0;
+    o->restart_select_min_time = 0.0;
     o->precision = CP_AL_GB300_FP64;
     o->fp32_switch_tol = 1e-5;
     o->fp32_max_iterations = -1;
@@ -756,7 +797,7 @@ bool oracle_block(Solver &S, bool &do_restart, int &charged, double elapsed, int
     S.check_termination(elapsed);
     if (S.reason == TERMINATION_REASON_UNSPECIFIED && charged >= limit) S.reason = TERMINATION_REASON_ITERATION_LIMIT;
     if (S.reason != TERMINATION_REASON_UNSPECIFIED) return true;
-    S.choose_restart_candidate();
+    S.choose_restart_candidate(elapsed);
     do_restart = S.should_restart(F);
     if (do_restart) S.perform_restart();
     return false;
@@ -989,6 +1030,7 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
         S->compute_residual();
     }
     if (power_iterations_out) *power_iterations_out = S->power_iters;
+    for (int t = 0; t < 3; ++t) g_restart_targets[t] = S->restarts_to[t];
     int polish_iters = 0, pst = -1, dst = -1;
     double polish_sec = 0.0;
     if (params->feasibility_polishing) { /* solver.cu:1715-1719 */
@@ -1010,6 +1052,12 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
 void oracle_cpal_polish_status(int *primal, int *dual) {
     *primal = g_polish_status[0];
     *dual = g_polish_status[1];
+}
+
+/* restarts of the last solve by target: the current point, the reflected
+ * Halpern iterate, the plain Halpern point */
+void oracle_cpal_restart_targets(int *counts) {
+    for (int t = 0; t < 3; ++t) counts[t] = g_restart_targets[t];
 }
 
 /* Session form for timing: setup once, then blocks of iterations. */

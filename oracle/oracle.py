@@ -102,6 +102,14 @@ def _polish_status(L):
     return tuple(N.TERMINATION_REASONS.get(v.value) if v.value >= 0 else None for v in (a, b))
 
 
+def _restart_targets(L):
+    """Restarts of the last oracle solve by target: (current point,
+    reflected Halpern iterate, plain Halpern point)."""
+    counts = (C.c_int * 3)()
+    L.oracle_cpal_restart_targets(counts)
+    return tuple(int(v) for v in counts)
+
+
 def solve_lp(data: LPData, params: dict | None = None, options: dict | None = None, threads: int = 1) -> LPResult:
     L = lib()
     p = apply_params(default_parameters(), params)
@@ -132,7 +140,8 @@ def solve_lp(data: LPData, params: dict | None = None, options: dict | None = No
             setup_sec=r.rescaling_time_sec,
             solve_sec=r.cumulative_time_sec,
             stats={"power_iterations": piters.value, "feasibility_iteration": r.feasibility_iteration,
-                   "feasibility_polishing_time": r.feasibility_polishing_time, "polish_status": _polish_status(L)},
+                   "feasibility_polishing_time": r.feasibility_polishing_time, "polish_status": _polish_status(L),
+                   "restart_targets": _restart_targets(L)},
         )
     finally:
         L.oracle_cpal_result_free(rp)

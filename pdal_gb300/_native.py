@@ -181,6 +181,7 @@ class CpalOptions(C.Structure):
         ("restart_select_margin", C.c_double),
         ("restart_select_min_iters", C.c_int),
         ("restart_select_threepoint", C.c_int),
+        ("restart_select_min_time", C.c_double),
         ("precision", C.c_int),
         ("fp32_switch_tol", C.c_double),
         ("fp32_max_iterations", C.c_int),

@@ -337,6 +337,7 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->restart_select_margin = 1.0;
     o->restart_select_min_iters = 0;
     o->restart_select_threepoint = 0;
+    o->restart_select_min_time = 0.0;
     o->precision = CP_AL_GB300_FP64;
     o->fp32_switch_tol = 1e-5;
     o->fp32_max_iterations = -1;
@@ -380,6 +381,7 @@ void cp_al_gb300_options_from_env(cp_al_gb300_options_t *o) {
     o->restart_select_margin = env_double("CP_AL_RESTART_SELECT_MARGIN", 1.0);
     o->restart_select_min_iters = env_int("CP_AL_RESTART_SELECT_MIN_ITERS", 0);
     o->restart_select_threepoint = env_int("CP_AL_RESTART_SELECT_THREEPOINT", 0);
+    o->restart_select_min_time = env_double("CP_AL_RESTART_SELECT_MIN_TIME", 0.0);
 }
 
 } // extern "C"

@@ -49,6 +49,8 @@ struct CpalParams {
     int restart_select;
     int restart_select_min_iters;
     double restart_select_margin;
+    double restart_select_min_time;
+    int restart_threepoint; /* also score the plain Halpern point (mode 3 or the three-point switch) */
 };
 
 /* Solver scalars, resident in device memory during the loop. */
@@ -79,8 +81,11 @@ struct CpalState {
     int iter_limit;        /* iteration limit (device copy, a session may extend it) */
     int fp32_stall_limit;  /* evaluations without a 2x KKT gain that end the FP32 phase */
     int fp32_stall;        /* evaluations since the FP32 phase last halved its best KKT */
-    int restart_target; /* 1: the last restart went to the Halpern iterate */
+    int restart_target; /* 1: the last restart went to the reflected Halpern iterate, 2: to the
+                           plain Halpern point */
     double fp32_best_kkt;
+    double restart_w; /* Halpern weight of the block's last iteration, for a restart to the plain
+                         Halpern point w x^ + (1 - w) x0 */
 };
 
 /* Reduction terms of one evaluation (finished sums / maxima). */
@@ -93,6 +98,8 @@ struct CpalEval {
      * <A^T(y^ - y), x^ - x>, and the distances of the Halpern iterate from
      * the anchors |x - x0|^2, |y - y0|^2, |A x - A x0|^2 */
     double sel_ax2, sel_dy2, sel_dx2, sel_cross, cur_dx2, cur_dy2, cur_axd2;
+    /* three-point selection only: <A^T(y^ - y0), x^ - x0> */
+    double h_cross;
 };
 
 PDAL_HD void cpal_set_coefficients(CpalState &s) {
@@ -308,32 +315,64 @@ PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval
         s.status = 5; /* TERMINATION_REASON_TIME_LIMIT */
         return true;
     }
-    /* LP/CP_AL/src/solver.cu:2749-2819: the averaged point's score against
-     * the Halpern iterate, the same formula as the fixed-point error */
+    /* LP/CP_AL/src/solver.cu:2749-2819: the scores of the reflected Halpern
+     * iterate (x, y) and, in the three-point mode, of the plain Halpern point
+     * h = w x^ + (1 - w) x0 against (x^, y^), by the fixed-point error's
+     * formula.  x^ - h = (1 - w)(x^ - x0) and the score is homogeneous of
+     * degree one in the difference, so h's score is (1 - w) times the score of
+     * x^ - x0, whose terms the evaluation already holds. */
     s.restart_target = 0;
-    if (p.restart_select != 0 && s.total >= p.restart_select_min_iters) {
+    const double w = (double)s.inner / (double)(s.inner + 1);
+    s.restart_w = w;
+    if (p.restart_select != 0 && s.total >= p.restart_select_min_iters && s.elapsed >= p.restart_select_min_time) {
         const double cur = s.fp;
         const double avg = cpal_fixed_point_error(s, e.sel_dx2, e.sel_dy2, e.sel_ax2, e.sel_cross);
+        const double hal =
+            p.restart_threepoint ? (1.0 - w) * cpal_fixed_point_error(s, e.ddx2, e.ddy2, e.axd2, e.h_cross) : INFINITY;
         if (p.restart_select == 2) {
             s.restart_target = 1;
             s.fp = avg;
-        } else if (isfinite(cur) && isfinite(avg) && avg < cur && avg <= p.restart_select_margin * cur) {
-            s.restart_target = 1;
-            s.fp = avg;
+        } else if (isfinite(cur)) {
+            int best = 0;
+            double best_score = cur;
+            if (isfinite(avg) && avg < best_score) {
+                best = 1;
+                best_score = avg;
+            }
+            if (p.restart_threepoint && isfinite(hal) && hal < best_score) {
+                best = 2;
+                best_score = hal;
+            }
+            if (best != 0 && best_score <= p.restart_select_margin * cur) {
+                s.restart_target = best;
+                s.fp = best_score;
+            }
         }
     }
     if (cpal_should_restart(s, p)) {
-        const bool to_current = s.restart_target == 1;
-        cpal_restart_scalars(s, p, to_current ? e.cur_dx2 : e.ddx2, to_current ? e.cur_dy2 : e.ddy2,
-                             to_current ? e.cur_axd2 : e.axd2);
+        /* the PID distances run from the anchors to the restart point:
+         * h - x0 = w (x^ - x0) for the plain Halpern point */
+        const int tg = s.restart_target;
+        const double w2 = w * w;
+        if (tg == 1)
+            cpal_restart_scalars(s, p, e.cur_dx2, e.cur_dy2, e.cur_axd2);
+        else if (tg == 2)
+            cpal_restart_scalars(s, p, w2 * e.ddx2, w2 * e.ddy2, w2 * e.axd2);
+        else
+            cpal_restart_scalars(s, p, e.ddx2, e.ddy2, e.axd2);
         s.restart = 1;
         /* the reference recomputes the fixed-point error of the unchanged
          * iterates with the new coefficients at the start of the next block
-         * (solver.cu:1279-1284); a restart to the Halpern iterate first sets
-         * x-bar = x^ and x^ = x (solver.cu:3015-3040), so the deltas are then
-         * x^ - x */
-        s.fp0 = to_current ? cpal_fixed_point_error(s, e.sel_dx2, e.sel_dy2, e.sel_ax2, e.sel_cross)
-                           : cpal_fixed_point_error(s, e.dx2, e.dy2, e.adx2, e.cross);
+         * (solver.cu:1279-1284).  A restart to the reflected Halpern iterate
+         * first sets x-bar = x^ and x^ = x (solver.cu:3016-3042), so the
+         * deltas are then x^ - x; one to the plain Halpern point sets x-bar =
+         * x^ and x^ = h (solver.cu:3043-3075), so they are (1 - w)(x^ - x0). */
+        if (tg == 1)
+            s.fp0 = cpal_fixed_point_error(s, e.sel_dx2, e.sel_dy2, e.sel_ax2, e.sel_cross);
+        else if (tg == 2)
+            s.fp0 = (1.0 - w) * cpal_fixed_point_error(s, e.ddx2, e.ddy2, e.axd2, e.h_cross);
+        else
+            s.fp0 = cpal_fixed_point_error(s, e.dx2, e.dy2, e.adx2, e.cross);
     }
     cpal_set_coefficients(s);
     return false;

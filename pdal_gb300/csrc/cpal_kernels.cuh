@@ -216,7 +216,10 @@ __global__ void __launch_bounds__(kThreads) k_dual(RowPlanDev plan, const int *_
     load_coefs(st, epi.k);
     epi.w = wt[koff].w;
     epi.omw = wt[koff].omw;
-    auto g = [&](int c, T *out) { out[0] = __ldg(xbar + c); };
+    /* x-bar gathers bypass L1: the random column gathers of a large LP hit
+     * L2, and caching them in L1 only adds L1TEX pressure (measured 3.5%
+     * faster for this kernel; the same load in k_primal is slower) */
+    auto g = [&](int c, T *out) { out[0] = __ldcg(xbar + c); };
     Red<0, 0> red;
     rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);
 }
@@ -373,14 +376,17 @@ struct EvalColArgs {
     double *part;
     int nblocks;
     const T *x, *y; /* restart target selection: the Halpern iterate */
+    const double *y0; /* three-point selection: the dual anchor */
 };
 
 /* SEL: also <A^T(y^ - y), x^ - x>, |x^ - x|^2 and |x - x0|^2 in extra sums
- * 6..8 (slot indices 7..9). */
-template <typename T, bool SEL = false>
+ * 6..8 (slot indices 7..9); H3 (three-point selection, with SEL): also
+ * <A^T(y^ - y0), x^ - x0> in extra sum 9 (slot index 10). */
+template <typename T, bool SEL = false, bool H3 = false>
 struct EvalColEpi {
+    static constexpr int NS = SEL ? (H3 ? 10 : 9) : 6;
     EvalColArgs<T> a;
-    __device__ __forceinline__ void operator()(int j, const double *s, Red<SEL ? 9 : 6, 1> &r) const {
+    __device__ __forceinline__ void operator()(int j, const double *s, Red<NS, 1> &r) const {
         const double xhj = (double)a.xh[j];
         const double lj = (double)a.lam[j];
         const double cj = a.c[j];
@@ -401,32 +407,36 @@ struct EvalColEpi {
             r.s[SEL ? 7 : 0] += d1 * d1;
             r.s[SEL ? 8 : 0] += d2 * d2;
         }
+        if (H3) r.s[H3 ? 9 : 0] += s[H3 ? 3 : 0] * ddx;
     }
-    __device__ __forceinline__ void long_red(int lid, Red<SEL ? 9 : 6, 1> &r) const {
+    __device__ __forceinline__ void long_red(int lid, Red<NS, 1> &r) const {
         double *d = a.part + (size_t)(a.nblocks + lid) * kEvalStride;
         for (int q = 0; q < 6; ++q) d[q] = r.s[q];
         d[6] = r.mx[0];
-        for (int q = 6; q < (SEL ? 9 : 6); ++q) d[q + 1] = r.s[q];
+        for (int q = 6; q < NS; ++q) d[q + 1] = r.s[q];
     }
 };
 
-template <typename T, int S, bool SEL = false>
+template <typename T, int S, bool SEL = false, bool H3 = false>
 __global__ void __launch_bounds__(kThreads) k_eval_cols(RowPlanDev plan, const int *__restrict__ rp,
                                                         const int *__restrict__ ci, const double *__restrict__ val,
                                                         EvalColArgs<T> a, const CpalState *__restrict__ st) {
+    static_assert(SEL || !H3, "three-point selection extends the two-point terms");
     if (st->status) return;
-    constexpr int NP = SEL ? 3 : 2, NS = SEL ? 9 : 6;
+    constexpr int NP = SEL ? (H3 ? 4 : 3) : 2, NS = EvalColEpi<T, SEL, H3>::NS;
     __shared__ RowBlockSmem<S, NP, double> sm;
-    EvalColEpi<T, SEL> epi;
+    EvalColEpi<T, SEL, H3> epi;
     epi.a = a;
     const T *yh = a.yh;
     const T *yb = a.ybar;
     const T *yc = a.y;
+    const double *y0 = a.y0;
     auto g = [&](int c, double *out) {
         const double yhc = (double)yh[c];
         out[0] = yhc;
         out[1] = (double)yb[c] - yhc;
         if (SEL) out[SEL ? 2 : 0] = yhc - (double)yc[c];
+        if (H3) out[H3 ? 3 : 0] = yhc - y0[c];
     };
     Red<NS, 1> red;
     red.zero();
@@ -483,6 +493,7 @@ static __global__ void __launch_bounds__(kThreads) k_control(const double *__res
         e.sel_cross = r2.s[6];
         e.sel_dx2 = r2.s[7];
         e.cur_dx2 = r2.s[8];
+        e.h_cross = r2.s[9];
         CpalState s = *st;
         s.elapsed = (double)(globaltimer_ns() - s.t_start_ns) * 1e-9;
         cpal_end_of_block(s, p, e);
@@ -566,6 +577,44 @@ __global__ void k_restart(const CpalState *__restrict__ st, int n, int m, const 
     Coefs<T> k;
     load_coefs(st, k);
     const int total = n > m ? n : m;
+    if (st->restart_target == 2) {
+        /* restart to the plain Halpern point h = w x^ + (1 - w) x0 of the
+         * block's last iteration (LP/CP_AL/src/solver.cu:2392, 2452,
+         * 3043-3075): x-bar = x^, then x^ = x = x0 = h; the same for y;
+         * A x0 = A x = w p^ + (1 - w) A x0 */
+        const double w = st->restart_w, omw = 1.0 - w;
+        T *xh_w = const_cast<T *>(xh), *yh_w = const_cast<T *>(yh);
+        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+            if (t < n) {
+                const T xo = xh_w[t];
+                const T v = (T)(w * (double)xo + omw * x0[t]);
+                xbar[t] = xo;
+                xh_w[t] = v;
+                x[t] = v;
+                x0[t] = (double)v;
+                if (x0f) x0f[t] = split_anchor((double)v);
+            }
+            if (t < m) {
+                const T yo = yh_w[t];
+                const T v = (T)(w * (double)yo + omw * y0[t]);
+                ybar[t] = yo;
+                yh_w[t] = v;
+                y[t] = v;
+                y0[t] = (double)v;
+                if (y0f) y0f[t] = split_anchor((double)v);
+                const double axh = w * phat[t] + omw * ax0[t];
+                ax0[t] = axh;
+                if (ax0f) ax0f[t] = split_anchor(axh);
+                const T axv = (T)axh;
+                ax[t] = axv;
+                if (BETA) {
+                    const T z = vmax(lb[t], vmin(axv - v * k.inv_beta, ub[t]));
+                    u[t] = v - k.beta * (axv - z);
+                }
+            }
+        }
+        return;
+    }
     if (st->restart_target == 1) {
         /* restart to the Halpern iterate (LP/CP_AL/src/solver.cu:3015-3040):
          * x-bar = x^, x^ = x, x0 = x; the same for y; A x0 = the tracked A x */

@@ -269,8 +269,10 @@ CpalParams resolve_cpal_params(const cp_al_parameters_t &P, const cp_al_gb300_op
     cp.restart_select = O.restart_select;
     cp.restart_select_min_iters = O.restart_select_min_iters;
     cp.restart_select_margin = O.restart_select_margin;
-    if (O.restart_select < 0 || O.restart_select > 2 || O.restart_select_threepoint)
-        throw Error("restart_select supports the two-point modes 0, 1 and 2 (the three-point mode is not built)");
+    cp.restart_select_min_time = O.restart_select_min_time;
+    /* LP/CP_AL/src/solver.cu:2774-2775: mode 3, or the three-point switch
+     * with any other nonzero mode */
+    cp.restart_threepoint = O.restart_select != 0 && (O.restart_select == 3 || O.restart_select_threepoint != 0);
     cp.obj_const = prob->objective_constant;
     const int n = prob->num_variables, m = prob->num_constraints;
     const bool linf = cp.norm_linf;
@@ -834,7 +836,7 @@ void CpalSolver::launch_eval_terms() {
     auto &v = vecs<T>();
     EvalRowArgs<T> ra{v.xh, v.xbar, v.yh, v.ybar, x0_, y0_, ax0_, clb_, cub_, clbf_, cubf_, rsc_, phat_, part_row_,
                       A_.ev.d.nblocks, v.x, v.y, v.ax};
-    EvalColArgs<T> ca{v.xh, v.xbar, v.yh, v.ybar, v.lam, x0_, c_, dsc_, part_col_, At_.ev.d.nblocks, v.x, v.y};
+    EvalColArgs<T> ca{v.xh, v.xbar, v.yh, v.ybar, v.lam, x0_, c_, dsc_, part_col_, At_.ev.d.nblocks, v.x, v.y, y0_};
     PDAL_WITH_SE(S_ev_, {
         if (m_ > 0) k_eval_rows<T, SE><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, ra, st_);
         k_eval_cols<T, SE><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, ca, st_);
@@ -846,8 +848,16 @@ void CpalSolver::launch_eval() {
     auto &v = vecs<T>();
     EvalRowArgs<T> ra{v.xh, v.xbar, v.yh, v.ybar, x0_, y0_, ax0_, clb_, cub_, clbf_, cubf_, rsc_, phat_, part_row_,
                       A_.ev.d.nblocks, v.x, v.y, v.ax};
-    EvalColArgs<T> ca{v.xh, v.xbar, v.yh, v.ybar, v.lam, x0_, c_, dsc_, part_col_, At_.ev.d.nblocks, v.x, v.y};
-    if (cp_.restart_select) {
+    EvalColArgs<T> ca{v.xh, v.xbar, v.yh, v.ybar, v.lam, x0_, c_, dsc_, part_col_, At_.ev.d.nblocks, v.x, v.y, y0_};
+    if (cp_.restart_select && cp_.restart_threepoint) {
+        PDAL_WITH_SE(S_ev_, {
+            if (m_ > 0)
+                k_eval_rows<T, SE, true>
+                    <<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, ra, st_);
+            k_eval_cols<T, SE, true, true>
+                <<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, ca, st_);
+        });
+    } else if (cp_.restart_select) {
         PDAL_WITH_SE(S_ev_, {
             if (m_ > 0)
                 k_eval_rows<T, SE, true>

@@ -222,6 +222,45 @@ def test_restart_target_selection_parity(lp_lib, options):
     assert_parity(g, o)
 
 
+SIGMA_OPTS = {"sigma_mode": 1, "sigma_init_factor": 0.5, "al_lambda": 0.0, "sigma_kp": 0.5, "sigma_ki": 0.0,
+              "sigma_kd": 0.0, "sigma_balance_gain": 0.0, "restart_necessary": 0.8}
+
+
+@pytest.mark.parametrize("refl,options,halpern_restarts", [
+    (0.5, {"restart_select": 3}, 1),
+    (0.3, {"restart_select": 1, "restart_select_threepoint": 1, "al_lambda": 0.0}, 4),
+    (0.3, {"restart_select": 3, **SIGMA_OPTS}, 4),
+], ids=["select3_beta", "select1_threepoint", "select3_sigma"])
+def test_restart_three_point_parity(lp_lib, refl, options, halpern_restarts):
+    """Three-point restart target selection (A13, LP/CP_AL/src/solver.cu:
+    2749-2819, 3043-3075): the plain Halpern point w x^ + (1 - w) x0 wins
+    the oracle's restarts as counted here within the first 1600 iterations;
+    the iterates after those blocks and the full solve match the oracle."""
+    d = I.random_lp(300, 700, 6, seed=3)
+    base = {"l_inf_ruiz_iterations": 4, "reflection_coefficient": refl}
+    g, o = both(d, {**base, "eps": 1e-14, "iteration_limit": 1600}, options)
+    assert o.stats["restart_targets"][2] == halpern_restarts, o.stats["restart_targets"]
+    assert g.iterations == o.iterations
+    assert g.stats["restarts"] == sum(o.stats["restart_targets"])
+    assert np.abs(g.x - o.x).max() / (1 + np.abs(o.x).max()) < 1e-8
+    assert np.abs(g.y - o.y).max() / (1 + np.abs(o.y).max()) < 1e-8
+    g, o = both(d, {**base, "eps": 1e-8}, options)
+    assert g.status == "OPTIMAL"
+    assert_parity(g, o)
+
+
+def test_restart_three_point_fp32_form(lp_lib):
+    """The three-point selection in the FP32 form (anchors rebuilt as (hi, lo)
+    pairs at a restart to the plain Halpern point) reaches the oracle's
+    optimum at 1e-8."""
+    d = I.random_lp(300, 700, 6, seed=3)
+    p = {"eps": 1e-8, "l_inf_ruiz_iterations": 4, "reflection_coefficient": 0.3}
+    g = lp.solve(d, p, {"restart_select": 3, "precision": "fp32_refine"})
+    o = O.solve_lp(d, p, {"restart_select": 3})
+    assert g.status == "OPTIMAL" and o.stats["restart_targets"][2] > 0
+    assert rel(g.primal_objective, o.primal_objective) <= 1e-6
+
+
 @pytest.mark.parametrize("kind", ["random", "transport"])
 def test_feasibility_polishing_matches_oracle(kind):
     """Feasibility polishing (LP/CP_AL/src/solver.cu:3912-4456) after a loose

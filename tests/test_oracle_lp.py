@@ -129,3 +129,26 @@ def test_oracle_feasibility_polishing():
     tight = O.solve_lp(d, {"eps": 1e-9, "l_inf_ruiz_iterations": 4, "feasibility_polishing": True,
                            "eps_feas_polish": 1e-6})
     assert tight.stats["polish_status"] == (None, None) and tight.stats["feasibility_iteration"] == 0
+
+
+def test_oracle_restart_three_point():
+    """Restart target selection with the plain Halpern point as a third
+    candidate (LP/CP_AL/src/solver.cu:2749-2819, 3043-3075): on this
+    instance the plain Halpern point wins one restart, the solve reaches
+    HiGHS's optimum, and the selection stays off before its minimum
+    iteration count or time."""
+    d = I.random_lp(300, 700, 6, seed=3)
+    prm = {"eps": 1e-8, "l_inf_ruiz_iterations": 4, "reflection_coefficient": 0.5}
+    r = O.solve_lp(d, prm, {"restart_select": 3})
+    assert r.status == "OPTIMAL"
+    assert r.stats["restart_targets"][2] >= 1
+    f = highs_objective(d)
+    assert abs(r.primal_objective - f) <= 1e-6 * (1 + abs(f))
+    # the three-point switch with mode 1 is mode 3
+    r1 = O.solve_lp(d, prm, {"restart_select": 1, "restart_select_threepoint": 1})
+    assert (r1.iterations, r1.stats["restart_targets"]) == (r.iterations, r.stats["restart_targets"])
+    plain = O.solve_lp(d, prm)
+    for gate in ({"restart_select_min_iters": 10**8}, {"restart_select_min_time": 1e9}):
+        g = O.solve_lp(d, prm, {"restart_select": 3, **gate})
+        assert g.stats["restart_targets"][1:] == (0, 0)
+        assert g.iterations == plain.iterations

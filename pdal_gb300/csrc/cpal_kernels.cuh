@@ -935,7 +935,7 @@ __global__ void __launch_bounds__(kThreads) k_power_a(RowPlanDev plan, const int
     epi.inv = ps->inv;
     epi.part = part;
     epi.nblocks = plan.nblocks;
-    auto g = [&](int c, T *out) { out[0] = dp[c]; };
+    auto g = [&](int c, T *out) { out[0] = __ldcg(dp + c); };
     Red<1, 0> red;
     red.zero();
     rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);

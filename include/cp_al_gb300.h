@@ -80,10 +80,6 @@ typedef struct {
                                      budget 1,024 / 2,048 x 2-4 blocks per SM) on a probe
                                      of the largest instances (200 iterations) and keeps
                                      the fastest, remembered per batch shape */
-    int batch_vector_cache;       /* batch: 1 = each block's dynamic shared memory is raised
-                                     to its share of the SM and the iterations gather from a
-                                     shared-memory copy of the gathered vector (instances
-                                     whose longer side fits); 0 = gathers from global memory */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */

@@ -662,7 +662,6 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->graph_blocks = 1;
     o->timing = 0;
     o->fp32_stall_evals = 25;
-    o->batch_vector_cache = 0;
 }
 
 /* LP/CP_AL/src/utils.cu:361-394 (reflection coefficient without the

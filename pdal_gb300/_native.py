@@ -191,7 +191,6 @@ class CpalOptions(C.Structure):
         ("timing", C.c_int),
         ("fp32_stall_evals", C.c_int),
         ("batch_blocks_per_sm", C.c_int),
-        ("batch_vector_cache", C.c_int),
     ]
 
 

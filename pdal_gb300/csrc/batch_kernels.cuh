@@ -73,9 +73,6 @@ struct BOpts {
     int fp32;              /* run the FP32 phase first */
     int fp32_stall_evals;
     double fp32_switch_tol;
-    int vcache_bytes;      /* dynamic shared memory of a block when the gathered-vector cache is
-                              on, else 0 */
-    int pad;
 };
 
 /* Shared-memory staging reused by every phase (the evaluation of the rows
@@ -423,28 +420,12 @@ __device__ __forceinline__ RowBlockSmem<BS, 1, float> &smem1(BSmem<BS> &sm, floa
 
 /* One precision phase: evaluation blocks until the controller terminates the
  * solve or (FP32) ends the phase.  The arithmetic of k_primal / k_dual /
- * k_eval_rows / k_eval_cols / k_control / k_restart.
- *
- * Gathered-vector cache (vc_bytes > 0): the iterations stage only the
- * one-product buffers, so the shared memory beyond them holds a copy of the
- * vector the next product gathers -- the dual iterate (or the AL predictor)
- * before A^T, x-bar before A -- when the instance's longer side fits.  The
- * random gathers of the row blocks then read shared memory instead of
- * L1 / L2; the values, and so the results, are the same. */
+ * k_eval_rows / k_eval_cols / k_control / k_restart. */
 template <typename T, int BS>
 __device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem<BS> &sm, double *sbuf, CpalState &s,
-                          Red<6, 1> *lacc6, double *sh, bool beta_on, int vc_bytes) {
+                          Red<6, 1> *lacc6, double *sh, bool beta_on) {
     const BVec<T> v = bvec<T>(I);
     const int F = p.F;
-    constexpr int kVcOff = (int)((sizeof(RowBlockSmem<BS, 1, T>) + 15) & ~(size_t)15);
-    T *vc = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(&sm) + kVcOff);
-    const long long longer = I.n > I.m ? I.n : I.m;
-    const bool cached = vc_bytes > kVcOff && longer * (long long)sizeof(T) <= (long long)(vc_bytes - kVcOff);
-    auto fill = [&](const T *src, int len) {
-        __syncthreads();
-        for (int t = threadIdx.x; t < len; t += kThreads) vc[t] = src[t];
-        __syncthreads();
-    };
     for (;;) {
         Coefs<T> k;
         load_coefs(&s, k);
@@ -456,10 +437,6 @@ __device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem<BS> &sm, do
             const T w = sizeof(T) == 8 ? (T)wd.w : (T)wf.w;
             const T omw = sizeof(T) == 8 ? (T)wd.omw : (T)wf.omw;
             const T *gat = beta_on ? v.u : v.y;
-            if (cached) {
-                fill(gat, I.m);
-                gat = vc; /* a generic pointer into shared memory */
-            }
             auto gp = [&](int c, T *o2) { o2[0] = gat[c]; };
             PrimalArgs<T> pa{v.x, v.xbar, v.xh, v.lam, v.x0, v.c, v.vlb, v.vub};
             Red<0, 0> z;
@@ -482,12 +459,7 @@ __device__ void blk_phase(const BInst &I, const CpalParams &p, BSmem<BS> &sm, do
             }
             if (I.m > 0) {
                 DualArgs<T> da{v.y, v.yh, v.ybar, v.ax, v.u, v.y0, v.ax0, v.clb, v.cub};
-                const T *xs = v.xbar;
-                if (cached) {
-                    fill(v.xbar, I.n);
-                    xs = vc;
-                }
-                auto gd = [&](int c, T *o2) { o2[0] = xs[c]; };
+                auto gd = [&](int c, T *o2) { o2[0] = v.xbar[c]; };
 #define PDAL_BATCH_DUAL(MAJ, BET)                                                                                      \
     {                                                                                                                  \
         DualEpi<T, MAJ, BET> e;                                                                                        \
@@ -703,7 +675,7 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
         });
         __syncthreads();
         blk_init_ax<float, BS>(I, bvec32(I), s, beta_on, sm);
-        blk_phase<float, BS>(I, p, sm, sbuf, s, lacc6, sh, beta_on, o.vcache_bytes);
+        blk_phase<float, BS>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
         fp32_iters = s.total;
         if (!s.status) {
             /* FP64 refinement from the FP32 iterate (switch_to_fp64) */
@@ -732,7 +704,7 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
             }
             __syncthreads();
             blk_init_ax<double, BS>(I, bvec64(I), s, beta_on, sm);
-            blk_phase<double, BS>(I, p, sm, sbuf, s, lacc6, sh, beta_on, o.vcache_bytes);
+            blk_phase<double, BS>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
         } else {
             blk_for(I.n, [&](int j) { I.xh[j] = (double)I.xhf[j]; });
             blk_for(I.m, [&](int i) { I.yh[i] = (double)I.yhf[i]; });
@@ -741,7 +713,7 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
     } else {
         __syncthreads();
         blk_init_ax<double, BS>(I, bvec64(I), s, beta_on, sm);
-        blk_phase<double, BS>(I, p, sm, sbuf, s, lacc6, sh, beta_on, o.vcache_bytes);
+        blk_phase<double, BS>(I, p, sm, sbuf, s, lacc6, sh, beta_on);
     }
     /* result (k_result_cols / k_result_rows) */
     {

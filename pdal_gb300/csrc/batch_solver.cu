@@ -370,31 +370,6 @@ int run_batch(int count, lp_problem_t *const *problems, const cp_al_parameters_t
         kern = minb == 4 ? k_batch_lp<4, 1024> : (minb == 3 ? k_batch_lp<3, 1024> : k_batch_lp<2, 1024>);
         dsm = sizeof(BSmem<1024>);
     }
-    bo.vcache_bytes = 0;
-    if (O.batch_vector_cache) {
-        /* the gathered-vector cache: each of the minb resident blocks takes its
-         * share of the SM's shared memory (less its static part and the
-         * per-block reservation), then steps down until minb still fit */
-        int smem_sm = 0, smem_optin = 0, reserved = 0;
-        PDAL_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev_id));
-        PDAL_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev_id));
-        PDAL_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev_id));
-        cudaFuncAttributes fa{};
-        PDAL_CUDA(cudaFuncGetAttributes(&fa, (const void *)kern));
-        long long want = (long long)smem_sm / minb - (long long)fa.sharedSizeBytes - reserved;
-        want = std::min<long long>(want, (long long)smem_optin - (long long)fa.sharedSizeBytes);
-        want &= ~15LL;
-        for (int step = 0; step < 64 && want > (long long)dsm; ++step, want -= 1024) {
-            PDAL_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
-            int fit = 0;
-            PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, kThreads, (size_t)want));
-            if (fit >= minb) {
-                dsm = (size_t)want;
-                bo.vcache_bytes = (int)want;
-                break;
-            }
-        }
-    }
     PDAL_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
     PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, dsm));
     if (per_sm < 1) throw Error("the batch kernel does not fit on one SM");
@@ -518,8 +493,7 @@ Schedule tune_schedule(int count, lp_problem_t *const *problems, const cp_al_par
         tot += w;
         mx = std::max(mx, w);
     }
-    const auto key =
-        std::make_tuple(count, tot, mx, O.precision * 16 + want_bs / 1024 * 4 + want_mb + (O.batch_vector_cache ? 64 : 0));
+    const auto key = std::make_tuple(count, tot, mx, O.precision * 16 + want_bs / 1024 * 4 + want_mb);
     {
         std::lock_guard<std::mutex> lk(g_sched_mu);
         auto it = g_sched.find(key);

@@ -125,23 +125,3 @@ def test_schedule_autotuner_and_fixed_schedules():
     assert st3["tune_sec"] == 0.0 and (st3["block_nnz"], st3["blocks_per_sm"]) == (t["block_nnz"], t["blocks_per_sm"])
     with pytest.raises(RuntimeError):
         lp.solve_batch(items, params, {"spmv_nnz_per_block": 2048, "batch_blocks_per_sm": 4})
-
-
-@pytest.mark.parametrize("precision", ["fp64", "fp32_refine"])
-def test_vector_cache_is_bit_identical(precision):
-    """The gathered-vector cache (batch_vector_cache) only moves where the
-    row blocks read the gathered values from: every instance, including the
-    long-row one, ends with the same iterations and bit-identical solutions
-    as the global-memory gathers, in both precision forms and with the AL
-    predictor on (default) and off (sigma mode)."""
-    items = batch_lps(count=24, seed=41, m_range=(50, 1500)) + [long_row_lp()]
-    for extra in ({}, SIGMA):
-        params = {"eps": 1e-7, "l_inf_ruiz_iterations": 4, "iteration_limit": 20000}
-        base = {"precision": precision, "spmv_nnz_per_block": 2048, "batch_blocks_per_sm": 2, **extra}
-        a, sa = lp.solve_batch(items, params, {**base, "batch_vector_cache": 0})
-        b, sb = lp.solve_batch(items, params, {**base, "batch_vector_cache": 1})
-        for ra, rb in zip(a, b):
-            assert (ra.status, ra.iterations) == (rb.status, rb.iterations)
-            assert np.array_equal(ra.x, rb.x) and np.array_equal(ra.y, rb.y)
-        # a few instances of this set need more than 20,000 iterations
-        assert sa["optimal"] == sb["optimal"] >= 20

@@ -879,6 +879,7 @@ struct PowerState {
     int iters;
     int max_iter;
     double tol;
+    double vsq;  /* |v|^2 of the current (unnormalised) vector */
 };
 
 /* The power iteration runs in the arithmetic type T: FP64 in the plain form
@@ -907,40 +908,83 @@ __global__ void __launch_bounds__(kThreads) k_power_at(RowPlanDev plan, const in
     rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);
 }
 
-/* vn = A dp, partial sums of (inv * v) . vn */
-template <typename T>
+/* vn = A dp, partial sums of (inv * v) . vn; with W2 also |vn|^2, slot
+ * pairs (the fused FP32 step: the residual and the next normalisation then
+ * follow from the two sums, see k_power_fin) */
+template <typename T, bool W2 = false>
 struct PowerRowEpi {
+    static constexpr int NS = W2 ? 2 : 1;
     const T *v;
     T *vn;
     double inv;
     double *part;
     int nblocks;
-    __device__ __forceinline__ void operator()(int i, const T *s, Red<1, 0> &r) const {
+    __device__ __forceinline__ void operator()(int i, const T *s, Red<NS, 0> &r) const {
         vn[i] = s[0];
-        r.s[0] += (inv * (double)v[i]) * (double)s[0];
+        const double w = (double)s[0];
+        r.s[0] += (inv * (double)v[i]) * w;
+        if (W2) r.s[W2 ? 1 : 0] += w * w;
     }
-    __device__ __forceinline__ void long_red(int lid, Red<1, 0> &r) const { part[nblocks + lid] = r.s[0]; }
+    __device__ __forceinline__ void long_red(int lid, Red<NS, 0> &r) const {
+#pragma unroll
+        for (int q = 0; q < NS; ++q) part[NS * (nblocks + lid) + q] = r.s[q];
+    }
 };
 
-template <int S, typename T>
+template <int S, typename T, bool W2 = false>
 __global__ void __launch_bounds__(kThreads) k_power_a(RowPlanDev plan, const int *__restrict__ rp,
                                                       const int *__restrict__ ci, const T *__restrict__ val,
                                                       const T *__restrict__ dp, const T *__restrict__ v,
                                                       T *vn, double *part, const PowerState *__restrict__ ps) {
     if (ps->done) return;
+    constexpr int NS = PowerRowEpi<T, W2>::NS;
     __shared__ RowBlockSmem<S, 1, T> sm;
-    PowerRowEpi<T> epi;
+    PowerRowEpi<T, W2> epi;
     epi.v = v;
     epi.vn = vn;
     epi.inv = ps->inv;
     epi.part = part;
     epi.nblocks = plan.nblocks;
+    /* dp gathers bypass L1: the random column gathers of a large LP hit L2
+     * (measured faster; the same load in k_power_at is slower) */
     auto g = [&](int c, T *out) { out[0] = __ldcg(dp + c); };
-    Red<1, 0> red;
+    Red<NS, 0> red;
     red.zero();
     rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);
-    block_reduce<kThreads, 1, 0>(red, sm.red);
-    if (threadIdx.x == 0) part[blockIdx.x] = red.s[0];
+    block_reduce<kThreads, NS, 0>(red, sm.red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NS; ++q) part[NS * blockIdx.x + q] = red.s[q];
+    }
+}
+
+/* Fused FP32 step, after k_power_a<..., true>: the Rayleigh quotient
+ * s2 = (inv v) . vn, the residual |vn - s2 (inv v)| from
+ * |vn|^2 - 2 s2 (inv v) . vn + s2^2 |inv v|^2 (no pass over the vectors;
+ * FP64 sums, absolute error ~1e-16 |vn|^2 against the 1e-4 tolerance), the
+ * next normalisation 1/|vn| and the stopping test.  The vectors alternate
+ * between two buffers instead of being copied. */
+static __global__ void __launch_bounds__(kThreads) k_power_fin(const double *__restrict__ part, int nparts,
+                                                               PowerState *ps) {
+    if (ps->done) return;
+    __shared__ double sbuf[2 * (kThreads / 32)];
+    Red<2, 0> r;
+    r.zero();
+    for (int b = threadIdx.x; b < nparts; b += kThreads) {
+        r.s[0] += part[2 * b];
+        r.s[1] += part[2 * b + 1];
+    }
+    block_reduce<kThreads, 2, 0>(r, sbuf);
+    if (threadIdx.x == 0) {
+        const double s2 = r.s[0], w2 = r.s[1];
+        const double nv2 = ps->inv * ps->inv * ps->vsq;
+        ps->s2 = s2;
+        ps->iters += 1;
+        ps->res = sqrt(fmax(w2 - 2.0 * s2 * s2 + s2 * s2 * nv2, 0.0));
+        ps->inv = 1.0 / sqrt(w2);
+        ps->vsq = w2;
+        if (ps->res < ps->tol || ps->iters >= ps->max_iter) ps->done = 1;
+    }
 }
 
 /* s2 = sum(part) */
@@ -1006,7 +1050,10 @@ __global__ void __launch_bounds__(kThreads) k_power_start(int m, const T *__rest
     r.zero();
     for (int i = threadIdx.x; i < m; i += kThreads) r.s[0] += (double)v[i] * (double)v[i];
     block_reduce<kThreads, 1, 0>(r, sbuf);
-    if (threadIdx.x == 0) ps->inv = 1.0 / sqrt(r.s[0]);
+    if (threadIdx.x == 0) {
+        ps->inv = 1.0 / sqrt(r.s[0]);
+        ps->vsq = r.s[0];
+    }
 }
 
 } // namespace pdal

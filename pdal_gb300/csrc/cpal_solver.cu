@@ -536,18 +536,19 @@ void CpalSolver::power_iteration() {
     cudaGraphExec_t exec = nullptr;
     PDAL_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int st = 0; st < steps_per_graph; ++st) {
-        int nparts = 0;
         if (f32) {
-            float *v = (float *)tmp_m_, *vn = (float *)tmp_m2_, *dp = (float *)tmp_n_;
+            /* fused step: two products and one finishing block; v and vn
+             * alternate between the two buffers (an even number of steps per
+             * graph, so every launch starts from the first) */
+            float *bufa = (float *)tmp_m_, *bufb = (float *)tmp_m2_, *dp = (float *)tmp_n_;
+            float *v = (st % 2 == 0) ? bufa : bufb, *vn = (st % 2 == 0) ? bufb : bufa;
             PDAL_WITH_S(S_it_, {
                 k_power_at<SB, float><<<At_.it.d.nblocks, kThreads, 0, stream_>>>(At_.it.d, At_.rp, At_.ci, At_.vf,
                                                                                   v, dp, ps_);
-                k_power_a<SB, float><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, A_.vf, dp, v,
-                                                                                vn, part_misc_, ps_);
+                k_power_a<SB, float, true><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(
+                    A_.it.d, A_.rp, A_.ci, A_.vf, dp, v, vn, part_misc_, ps_);
             });
-            nparts = A_.it.d.nblocks + A_.it.d.nlong;
-            k_power_dot<<<1, kThreads, 0, stream_>>>(part_misc_, nparts, ps_);
-            k_power_resid<float><<<gres, kThreads, 0, stream_>>>(m_, v, vn, part_misc_, ps_);
+            k_power_fin<<<1, kThreads, 0, stream_>>>(part_misc_, A_.it.d.nblocks + A_.it.d.nlong, ps_);
         } else {
             double *v = tmp_m_, *vn = tmp_m2_, *dp = tmp_n_;
             PDAL_WITH_SE(S_ev_, {
@@ -556,11 +557,11 @@ void CpalSolver::power_iteration() {
                 k_power_a<SE, double><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, dp, v,
                                                                                  vn, part_misc_, ps_);
             });
-            nparts = A_.ev.d.nblocks + A_.ev.d.nlong;
+            const int nparts = A_.ev.d.nblocks + A_.ev.d.nlong;
             k_power_dot<<<1, kThreads, 0, stream_>>>(part_misc_, nparts, ps_);
             k_power_resid<double><<<gres, kThreads, 0, stream_>>>(m_, v, vn, part_misc_, ps_);
+            k_power_check<<<1, kThreads, 0, stream_>>>(part_misc_, gres, ps_);
         }
-        k_power_check<<<1, kThreads, 0, stream_>>>(part_misc_, gres, ps_);
     }
     cudaGraph_t graph;
     PDAL_CUDA(cudaStreamEndCapture(stream_, &graph));
@@ -569,7 +570,7 @@ void CpalSolver::power_iteration() {
     const int max_launch = P_.sv_max_iter / steps_per_graph + 2;
     for (int it = 0; it < max_launch; ++it) {
         PDAL_CUDA(cudaGraphLaunch(exec, stream_));
-        launches += 5 * steps_per_graph;
+        launches += (f32 ? 3 : 5) * steps_per_graph;
         PDAL_CUDA(cudaMemcpyAsync(h_ps_, ps_, sizeof(PowerState), cudaMemcpyDeviceToHost, stream_));
         d2h += sizeof(PowerState);
         PDAL_CUDA(cudaStreamSynchronize(stream_));

@@ -249,6 +249,26 @@ def test_restart_three_point_parity(lp_lib, refl, options, halpern_restarts):
     assert_parity(g, o)
 
 
+@pytest.mark.parametrize("sv_max_iter", [5000, 60])
+def test_fp32_power_iteration_matches_fp64(lp_lib, sv_max_iter):
+    """The chosen form's fused FP32 power step (FP32 products, FP64 sums, the
+    residual from the Rayleigh sums, alternating vector buffers) against the
+    FP64 form's separate residual pass: the same number of power iterations
+    (converged within 5,000, or at the 60 cap) within one, and the same
+    sigma_max(A)^2 estimate within 1e-6 relative."""
+    d = I.random_lp(300, 700, 6, seed=21)
+    p = {"eps": 1e-4, "l_inf_ruiz_iterations": 4, "sv_max_iter": sv_max_iter, "iteration_limit": 400}
+    g64 = lp.solve(d, p)
+    g32 = lp.solve(d, p, {"precision": "fp32_refine"})
+    it64, it32 = g64.stats["power_iterations"], g32.stats["power_iterations"]
+    assert abs(it32 - it64) <= 1, (it32, it64)
+    if sv_max_iter == 60:
+        assert it32 == it64 == 60
+    else:
+        assert it64 < 5000
+    assert rel(g32.stats["lambda_est"], g64.stats["lambda_est"]) < 1e-6
+
+
 def test_restart_three_point_fp32_form(lp_lib):
     """The three-point selection in the FP32 form (anchors rebuilt as (hi, lo)
     pairs at a restart to the plain Halpern point) reaches the oracle's

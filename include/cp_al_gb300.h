@@ -127,6 +127,17 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *opts);
  * field exactly as the reference's getenv readers do. */
 void cp_al_gb300_options_from_env(cp_al_gb300_options_t *opts);
 
+/* Name of the first CP_AL_* environment switch that turns on a controller of
+ * the reference this library does not implement -- adaptive lambda
+ * (CP_AL_ADAPTIVE_LAMBDA, the race / auto CP_AL_LAMBDA_PROFILE values),
+ * dynamic evaluation frequency (CP_AL_DYNAMIC_EVAL), the sigma trigger
+ * (CP_AL_SIGMA_TRIGGER outside sigma mode), the alpha rollback trial
+ * (CP_AL_ALPHA_ROLLBACK_TRIAL), the alpha pulse (CP_AL_ALPHA_DIRECT_PULSE) or
+ * Curtis-Reid scaling (CP_AL_CR_SCALING) -- or NULL.  solve_lp_problem
+ * returns NULL with a message while one is set, instead of solving without
+ * it.  Diagnostic and trace switches are ignored. */
+const char *cp_al_gb300_unbuilt_switch(void);
+
 /* solve_lp_problem with explicit options (opts == NULL -> from environment). */
 cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *params,
                                   const cp_al_gb300_options_t *opts);

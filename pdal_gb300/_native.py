@@ -278,6 +278,7 @@ LP_SYMBOLS = {
     ),
     "cp_al_gb300_last_stats": (None, [C.POINTER(CpalStats)]),
     "cp_al_gb300_last_error": (C.c_char_p, []),
+    "cp_al_gb300_unbuilt_switch": (C.c_char_p, []),
     "cp_al_gb300_session_create": (
         C.c_void_p,
         [C.POINTER(LpProblem), C.POINTER(CpalParameters), C.POINTER(CpalOptions)],

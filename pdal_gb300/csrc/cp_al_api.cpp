@@ -351,6 +351,25 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
 /* Each variable is read the way the reference reads it
  * (LP/CP_AL/src/solver.cu:377-413: empty = unset, strtod/strtol, non-finite
  * ignored). */
+/* The enabling reads: LP/CP_AL/src/solver.cu:592 (rollback trial), 889
+ * (pulse), 1235 (dynamic evaluation), 1497 (sigma trigger, outside sigma
+ * mode), 3168-3180 (adaptive lambda and its profiles); preconditioner.cu:
+ * 403-404 (Curtis-Reid). */
+const char *cp_al_gb300_unbuilt_switch(void) {
+    static const char *const kSwitches[] = {"CP_AL_ADAPTIVE_LAMBDA", "CP_AL_DYNAMIC_EVAL", "CP_AL_ALPHA_ROLLBACK_TRIAL",
+                                            "CP_AL_ALPHA_DIRECT_PULSE", "CP_AL_CR_SCALING"};
+    for (const char *name : kSwitches)
+        if (env_int(name, 0) != 0) return name;
+    if (const char *prof = getenv("CP_AL_LAMBDA_PROFILE")) {
+        static const char *const kProfiles[] = {"grid4_race", "race4", "mp_race", "safe_race", "mp_auto", "safe_auto"};
+        for (const char *p : kProfiles)
+            if (strcmp(prof, p) == 0) return "CP_AL_LAMBDA_PROFILE";
+    }
+    if (env_int("CP_AL_SIGMA_TRIGGER", 0) != 0 && !(env_set("CP_AL_SIGMA") || env_int("CP_AL_SIGMA_MODE", 0) != 0))
+        return "CP_AL_SIGMA_TRIGGER";
+    return nullptr;
+}
+
 void cp_al_gb300_options_from_env(cp_al_gb300_options_t *o) {
     if (!o) return;
     cp_al_gb300_default_options(o);

@@ -1459,6 +1459,12 @@ cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *
 }
 
 cp_al_result_t *solve_lp_problem(lp_problem_t *prob, const cp_al_parameters_t *params) {
+    if (const char *sw = cp_al_gb300_unbuilt_switch()) {
+        g_last_error.clear();
+        set_error(std::string("solve_lp_problem: ") + sw +
+                  " is set, but the controller it enables is not part of this library");
+        return nullptr;
+    }
     return cp_al_gb300_solve(prob, params, nullptr);
 }
 

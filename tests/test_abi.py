@@ -214,3 +214,40 @@ def test_options_from_env_reads_reference_variables(lp_lib, monkeypatch):
     monkeypatch.setenv("CP_AL_SIGMA", "0.3")
     o = lp.default_options(lp_lib, from_env=True)
     assert o.sigma_set == 1 and o.sigma == 0.3 and o.sigma_adaptive == 0
+
+
+@pytest.mark.parametrize("name,value,extra", [
+    ("CP_AL_ADAPTIVE_LAMBDA", "1", {}),
+    ("CP_AL_LAMBDA_PROFILE", "mp_race", {}),
+    ("CP_AL_DYNAMIC_EVAL", "1", {}),
+    ("CP_AL_SIGMA_TRIGGER", "1", {}),
+    ("CP_AL_ALPHA_ROLLBACK_TRIAL", "1", {}),
+    ("CP_AL_ALPHA_DIRECT_PULSE", "1", {}),
+    ("CP_AL_CR_SCALING", "1", {}),
+])
+def test_unbuilt_controller_switch_is_refused(lp_lib, monkeypatch, name, value, extra):
+    """A CP_AL_* switch that turns on a controller this library does not
+    implement makes solve_lp_problem return NULL with a message naming it
+    (before any device work, so this runs without a GPU) instead of solving
+    without the controller; switched off, or the sigma trigger inside sigma
+    mode (where the reference ignores it), nothing is refused."""
+    for var in ("CP_AL_ADAPTIVE_LAMBDA", "CP_AL_LAMBDA_PROFILE", "CP_AL_DYNAMIC_EVAL", "CP_AL_SIGMA_TRIGGER",
+                "CP_AL_ALPHA_ROLLBACK_TRIAL", "CP_AL_ALPHA_DIRECT_PULSE", "CP_AL_CR_SCALING", "CP_AL_SIGMA_MODE",
+                "CP_AL_SIGMA"):
+        monkeypatch.delenv(var, raising=False)
+    assert lp_lib.cp_al_gb300_unbuilt_switch() is None
+    monkeypatch.setenv(name, "0" if value == "1" else "mp_fixed")
+    assert lp_lib.cp_al_gb300_unbuilt_switch() is None
+    monkeypatch.setenv(name, value)
+    assert lp_lib.cp_al_gb300_unbuilt_switch() == name.encode()
+    data = lp.LPData(np.ones(2), (np.array([0, 2], np.int32), np.array([0, 1], np.int32), np.ones(2), (1, 2)),
+                     np.array([0.0]), np.array([1.0]), np.zeros(2), np.ones(2))
+    prob = lp._CProblem(lp_lib, data)
+    try:
+        assert not lp_lib.solve_lp_problem(prob.ptr, None)
+        assert name in N.last_error(lp_lib)
+    finally:
+        prob.close()
+    if name == "CP_AL_SIGMA_TRIGGER":
+        monkeypatch.setenv("CP_AL_SIGMA_MODE", "1")
+        assert lp_lib.cp_al_gb300_unbuilt_switch() is None

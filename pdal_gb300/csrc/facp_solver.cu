@@ -331,6 +331,11 @@ void FacpSolver::prepare() {
     if (o_.precision != 0 && o_.precision != 1) throw Error("precision must be 0 (FP64) or 1 (FP32 + FP64 refinement)");
     if (o_.precision == 1 && !(o_.fp32_switch_tol >= 0.0)) throw Error("fp32_switch_tol must be >= 0");
     if (p_.termination_evaluation_frequency < 1) throw Error("termination_evaluation_frequency must be >= 1");
+    /* QP/FA_CP/src/solver.cu:156-160 polishes after the solve; not built here
+     * (its dual phase measures a stored dual slack that only the problems
+     * without Q refresh), so the solve says so and runs without it */
+    if (p_.feasibility_polishing)
+        fprintf(stderr, "[fa_cp_gb300] feasibility polishing is not part of this library; solving without it\n");
     HostQP &P = H_;
     P.n = q->num_variables;
     P.m = q->num_constraints;

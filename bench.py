@@ -334,8 +334,13 @@ def bench_qp(local):
     from pdal_gb300 import instances, qp
 
     qd, _, f_star = instances.planted_qp()
-    out = {"workload": "QP n=200,000 m=100,000, A 2.0M nnz, Q=B'B+diag (sparse Q), planted optimum"}
-    for form, opts in (("chosen_fp32_refine", {"device": local, "precision": "fp32_refine"}),
+    out = {"workload": "QP n=200,000 m=100,000, A 2.0M nnz, Q=B'B+diag (sparse Q), planted optimum",
+           "chosen_form": "FP32 segments to relative KKT 5e-6 (fp32_switch_tol), then FP64"}
+    # the FP32 phase ends at relative KKT 5e-6 (measured on this QP, to 1e-6:
+    # 1e-5 / 5e-6 / 3e-6 / 2e-6 / 1e-6 gave 0.233 / 0.212 / 0.266 / 0.267 /
+    # 0.267 s; below 5e-6 the FP32 iterate reaches its rounding floor and the
+    # stall rule ends the phase 250 iterations later)
+    for form, opts in (("chosen_fp32_refine", {"device": local, "precision": "fp32_refine", "fp32_switch_tol": 5e-6}),
                        ("plain_fp64", {"device": local})):
         out[form] = {}
         for eps in (1e-6, 1e-8):

@@ -59,6 +59,17 @@ struct NoLongRed {
     __device__ __forceinline__ void long_red(int, Red<0, 0> &) const {}
 };
 
+/* Programmatic dependent launch of the iteration and FP32 power kernels: the
+ * launch of a kernel is prepared while the one before it finishes, and each
+ * block waits here until every write of that kernel is visible before it
+ * reads anything.  The dependents launch as the blocks exit (no explicit
+ * early trigger: blocks dispatched early and parked in the wait made the
+ * short kernels of small LPs almost twice as slow).  Without the launch
+ * attribute the wait is a no-op. */
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 /* ------------------------------------------------------------------ */
 /* iteration                                                           */
 /* ------------------------------------------------------------------ */
@@ -154,6 +165,7 @@ __global__ void __launch_bounds__(kThreads) k_primal(RowPlanDev plan, const int 
                                                      const T *__restrict__ gat, PrimalArgs<T> a,
                                                      const CpalState *__restrict__ st,
                                                      const typename WeightT<T>::type *__restrict__ wt, int koff) {
+    pdl_enter();
     if (st->status) return;
     __shared__ RowBlockSmem<S, 1, T> sm;
     PrimalEpi<T, MAJOR> epi;
@@ -209,6 +221,7 @@ __global__ void __launch_bounds__(kThreads) k_dual(RowPlanDev plan, const int *_
                                                    const T *__restrict__ xbar, DualArgs<T> a,
                                                    const CpalState *__restrict__ st,
                                                    const typename WeightT<T>::type *__restrict__ wt, int koff) {
+    pdl_enter();
     if (st->status) return;
     __shared__ RowBlockSmem<S, 1, T> sm;
     DualEpi<T, MAJOR, BETA> epi;
@@ -898,6 +911,7 @@ __global__ void __launch_bounds__(kThreads) k_power_at(RowPlanDev plan, const in
                                                        const int *__restrict__ ci, const T *__restrict__ val,
                                                        const T *__restrict__ v, T *dp,
                                                        const PowerState *__restrict__ ps) {
+    pdl_enter();
     if (ps->done) return;
     __shared__ RowBlockSmem<S, 1, T> sm;
     const T inv = (T)ps->inv;
@@ -936,6 +950,7 @@ __global__ void __launch_bounds__(kThreads) k_power_a(RowPlanDev plan, const int
                                                       const int *__restrict__ ci, const T *__restrict__ val,
                                                       const T *__restrict__ dp, const T *__restrict__ v,
                                                       T *vn, double *part, const PowerState *__restrict__ ps) {
+    pdl_enter();
     if (ps->done) return;
     constexpr int NS = PowerRowEpi<T, W2>::NS;
     __shared__ RowBlockSmem<S, 1, T> sm;
@@ -966,6 +981,7 @@ __global__ void __launch_bounds__(kThreads) k_power_a(RowPlanDev plan, const int
  * between two buffers instead of being copied. */
 static __global__ void __launch_bounds__(kThreads) k_power_fin(const double *__restrict__ part, int nparts,
                                                                PowerState *ps) {
+    pdl_enter();
     if (ps->done) return;
     __shared__ double sbuf[2 * (kThreads / 32)];
     Red<2, 0> r;

@@ -501,6 +501,26 @@ void CpalSolver::upload() {
     upload_sec = now_sec() - t_up;
 }
 
+/* A kernel launched with programmatic stream serialization (the iteration
+ * and FP32 power kernels begin with pdl_enter): its launch is prepared while
+ * the previous kernel finishes, which hides part of the launch latency that
+ * bounds small problems (measured: 6,800 iterations of a 2,000 x 5,000 LP
+ * 67.4 -> 62.3 ms).  Stream capture records the same programmatic edges. */
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), int grid, cudaStream_t stream, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PDAL_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+}
+
 void CpalSolver::power_iteration() {
     PowerState h{};
     h.max_iter = P_.sv_max_iter;
@@ -542,13 +562,16 @@ void CpalSolver::power_iteration() {
              * graph, so every launch starts from the first) */
             float *bufa = (float *)tmp_m_, *bufb = (float *)tmp_m2_, *dp = (float *)tmp_n_;
             float *v = (st % 2 == 0) ? bufa : bufb, *vn = (st % 2 == 0) ? bufb : bufa;
+            const int *Arp = A_.rp, *Aci = A_.ci, *Atrp = At_.rp, *Atci = At_.ci;
+            const float *Av = A_.vf, *Atv = At_.vf;
+            const PowerState *psc = ps_;
             PDAL_WITH_S(S_it_, {
-                k_power_at<SB, float><<<At_.it.d.nblocks, kThreads, 0, stream_>>>(At_.it.d, At_.rp, At_.ci, At_.vf,
-                                                                                  v, dp, ps_);
-                k_power_a<SB, float, true><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(
-                    A_.it.d, A_.rp, A_.ci, A_.vf, dp, v, vn, part_misc_, ps_);
+                launch_pdl(k_power_at<SB, float>, At_.it.d.nblocks, stream_, At_.it.d, Atrp, Atci, Atv,
+                           (const float *)v, dp, psc);
+                launch_pdl(k_power_a<SB, float, true>, A_.it.d.nblocks, stream_, A_.it.d, Arp, Aci, Av,
+                           (const float *)dp, (const float *)v, vn, part_misc_, psc);
             });
-            k_power_fin<<<1, kThreads, 0, stream_>>>(part_misc_, A_.it.d.nblocks + A_.it.d.nlong, ps_);
+            launch_pdl(k_power_fin, 1, stream_, (const double *)part_misc_, A_.it.d.nblocks + A_.it.d.nlong, ps_);
         } else {
             double *v = tmp_m_, *vn = tmp_m2_, *dp = tmp_n_;
             PDAL_WITH_SE(S_ev_, {
@@ -792,11 +815,11 @@ void CpalSolver::launch_primal(int koff, bool major) {
     const auto *wt = weights<T>(wt_, wtf_);
     PDAL_WITH_S(S_it_, {
         if (major)
-            k_primal<T, SB, true><<<At_.it.d.nblocks, kThreads, 0, stream_>>>(At_.it.d, At_.rp, At_.ci, Atv, gat, pa,
-                                                                             st_, wt, koff);
+            launch_pdl(k_primal<T, SB, true>, At_.it.d.nblocks, stream_, At_.it.d, (const int *)At_.rp,
+                       (const int *)At_.ci, Atv, gat, pa, (const CpalState *)st_, wt, koff);
         else
-            k_primal<T, SB, false><<<At_.it.d.nblocks, kThreads, 0, stream_>>>(At_.it.d, At_.rp, At_.ci, Atv, gat,
-                                                                              pa, st_, wt, koff);
+            launch_pdl(k_primal<T, SB, false>, At_.it.d.nblocks, stream_, At_.it.d, (const int *)At_.rp,
+                       (const int *)At_.ci, Atv, gat, pa, (const CpalState *)st_, wt, koff);
     });
 }
 
@@ -807,21 +830,24 @@ void CpalSolver::launch_dual(int koff, bool major) {
     const T *Av = matvals<T>(A_.v, A_.vf);
     DualArgs<T> da{v.y, v.yh, v.ybar, v.ax, v.u, anchor<T>(y0_, y0f_), anchor<T>(ax0_, ax0f_), v.clb, v.cub};
     const auto *wt = weights<T>(wt_, wtf_);
+    const T *xbar = v.xbar;
+    const int *rp = A_.rp, *ci = A_.ci;
+    const CpalState *st = st_;
     PDAL_WITH_S(S_it_, {
         if (major) {
             if (beta_on_)
-                k_dual<T, SB, true, true><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av, v.xbar,
-                                                                                    da, st_, wt, koff);
+                launch_pdl(k_dual<T, SB, true, true>, A_.it.d.nblocks, stream_, A_.it.d, rp, ci, Av, xbar, da, st, wt,
+                           koff);
             else
-                k_dual<T, SB, true, false><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av,
-                                                                                     v.xbar, da, st_, wt, koff);
+                launch_pdl(k_dual<T, SB, true, false>, A_.it.d.nblocks, stream_, A_.it.d, rp, ci, Av, xbar, da, st, wt,
+                           koff);
         } else {
             if (beta_on_)
-                k_dual<T, SB, false, true><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av,
-                                                                                     v.xbar, da, st_, wt, koff);
+                launch_pdl(k_dual<T, SB, false, true>, A_.it.d.nblocks, stream_, A_.it.d, rp, ci, Av, xbar, da, st, wt,
+                           koff);
             else
-                k_dual<T, SB, false, false><<<A_.it.d.nblocks, kThreads, 0, stream_>>>(A_.it.d, A_.rp, A_.ci, Av,
-                                                                                      v.xbar, da, st_, wt, koff);
+                launch_pdl(k_dual<T, SB, false, false>, A_.it.d.nblocks, stream_, A_.it.d, rp, ci, Av, xbar, da, st,
+                           wt, koff);
         }
     });
 }

@@ -61,6 +61,12 @@ typedef struct {
     int restart_select_threepoint;/* CP_AL_RESTART_SELECT_THREEPOINT, 0 (nonzero: mode 1 also scores
                                      the plain Halpern iterate) */
     double restart_select_min_time;/* CP_AL_RESTART_SELECT_MIN_TIME, 0.0 seconds */
+    int cr_iterations;            /* Curtis-Reid passes before Ruiz (preconditioner.cu:162-270,
+                                     403-425): CP_AL_CR_SCALING nonzero -> 20, CP_AL_CR_ITERS
+                                     overrides; 0 = off */
+    int cr_early_stop;            /* CP_AL_CR_EARLY_STOP: with 20 passes, stop after 5 when the
+                                     largest change of a scaled entry's log is <= the threshold */
+    double cr_early_stop_threshold; /* CP_AL_CR_EARLY_STOP_THRESHOLD, 0.1 */
 
     /* --- options of this implementation --- */
     int precision;                /* cp_al_gb300_precision_t */
@@ -118,6 +124,7 @@ typedef struct {
      * primal and dual phases (-1: not run) */
     int polish_primal_status;
     int polish_dual_status;
+    int cr_passes; /* Curtis-Reid passes run in the equilibration */
 } cp_al_gb300_stats_t;
 
 /* The reference defaults of every field, ignoring the environment. */
@@ -132,8 +139,8 @@ void cp_al_gb300_options_from_env(cp_al_gb300_options_t *opts);
  * (CP_AL_ADAPTIVE_LAMBDA, the race / auto CP_AL_LAMBDA_PROFILE values),
  * dynamic evaluation frequency (CP_AL_DYNAMIC_EVAL), the sigma trigger
  * (CP_AL_SIGMA_TRIGGER outside sigma mode), the alpha rollback trial
- * (CP_AL_ALPHA_ROLLBACK_TRIAL), the alpha pulse (CP_AL_ALPHA_DIRECT_PULSE) or
- * Curtis-Reid scaling (CP_AL_CR_SCALING) -- or NULL.  solve_lp_problem
+ * (CP_AL_ALPHA_ROLLBACK_TRIAL) or the alpha pulse (CP_AL_ALPHA_DIRECT_PULSE)
+ * -- or NULL.  solve_lp_problem
  * returns NULL with a message while one is set, instead of solving without
  * it.  Diagnostic and trace switches are ignored. */
 const char *cp_al_gb300_unbuilt_switch(void);

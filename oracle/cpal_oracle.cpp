@@ -147,6 +147,81 @@ struct Solver {
         for (int j = 0; j < n; ++j)
             for (int k = At.rp[j]; k < At.rp[j + 1]; ++k) At.v[k] *= (1.0 / d[j]) * (1.0 / r[At.ci[k]]);
     }
+    /* preconditioner.cu:128-160 + kernels 476-530 with the inverses given
+     * (the Curtis-Reid pass hands over f, not 1/(1/f)) */
+    void scale_problem_inv(const std::vector<double> &r, const std::vector<double> &rinv, const std::vector<double> &d,
+                           const std::vector<double> &dinv) {
+        for (int j = 0; j < n; ++j) {
+            c[j] *= dinv[j];
+            vlb[j] *= d[j];
+            vub[j] *= d[j];
+            x0[j] *= d[j];
+        }
+        for (int i = 0; i < m; ++i) {
+            clb[i] *= rinv[i];
+            cub[i] *= rinv[i];
+            y0[i] *= r[i];
+        }
+        for (int i = 0; i < m; ++i)
+            for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) A.v[k] *= dinv[A.ci[k]] * rinv[i];
+        for (int j = 0; j < n; ++j)
+            for (int k = At.rp[j]; k < At.rp[j + 1]; ++k) At.v[k] *= dinv[j] * rinv[At.ci[k]];
+    }
+    /* Curtis-Reid (preconditioner.cu:162-270, 553-624): alternating passes
+     * set each row's log scale to the mean of -log|a| - (column log scale)
+     * over its nonzeros, then each column's from the rows; the scales are
+     * 1 / clamp(exp(log), 1e-30, 1e30).  With early stop (20 passes) the
+     * passes end after the fifth when the largest change of a scaled entry's
+     * log, |delta_row + delta_col|, is at most the threshold. */
+    int cr_passes = 0;
+    void curtis_reid() {
+        const int iters = O.cr_iterations;
+        const bool early = O.cr_early_stop != 0 && iters == 20;
+        std::vector<double> lr(m, 0.0), lc(n, 0.0), dr(m, 0.0), dc(n, 0.0);
+        auto update = [](const Csr &M, const std::vector<double> &other, std::vector<double> &ls,
+                         std::vector<double> &delta) {
+            for (int i = 0; i < M.nr; ++i) {
+                const int k0 = M.rp[i], k1 = M.rp[i + 1];
+                double acc = 0.0;
+                for (int k = k0; k < k1; ++k) {
+                    double v = std::fabs(M.v[k]);
+                    if (!std::isfinite(v) || v < 1e-300) v = 1e-300;
+                    acc += -std::log(v) - other[M.ci[k]];
+                }
+                const double u = k1 > k0 ? acc / (double)(k1 - k0) : 0.0;
+                delta[i] = u - ls[i];
+                ls[i] = u;
+            }
+        };
+        for (int it = 0; it < iters; ++it) {
+            update(A, lc, lr, dr);
+            update(At, lr, lc, dc);
+            cr_passes = it + 1;
+            if (early && it + 1 == 5 && m > 0) {
+                double mx = 0.0;
+                for (int i = 0; i < m; ++i)
+                    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) {
+                        const double e = std::fabs(dr[i] + dc[A.ci[k]]);
+                        if (std::isfinite(e) && e > mx) mx = e;
+                    }
+                if (mx <= O.cr_early_stop_threshold) break;
+            }
+        }
+        std::vector<double> rinv(m), dinv(n);
+        for (int i = 0; i < m; ++i) {
+            const double f = std::fmin(std::fmax(std::exp(lr[i]), 1e-30), 1e30);
+            lr[i] = 1.0 / f;
+            rinv[i] = f;
+            rcum[i] *= lr[i];
+        }
+        for (int j = 0; j < n; ++j) {
+            const double f = std::fmin(std::fmax(std::exp(lc[j]), 1e-30), 1e30);
+            lc[j] = 1.0 / f;
+            dinv[j] = f;
+            dcum[j] *= lc[j];
+        }
+        scale_problem_inv(lr, rinv, lc, dinv);
+    }
     static void clamp_sqrt_accum(std::vector<double> &s, std::vector<double> &cum) {
         /* preconditioner.cu:653-667 */
         for (size_t t = 0; t < s.size(); ++t) {
@@ -191,6 +266,7 @@ struct Solver {
         std::vector<double> r(m), d(n);
         dcum.assign(n, 1.0);
         rcum.assign(m, 1.0);
+        if (O.cr_iterations > 0) curtis_reid(); /* 403-425: before Ruiz */
         for (int it = 0; it < P->l_inf_ruiz_iterations; ++it) { /* 273-299 */
             row_absmax(A, r);
             clamp_sqrt_accum(r, rcum);
@@ -654,6 +730,9 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->restart_select_min_iters = 0;
     o->restart_select_threepoint = 0;
     o->restart_select_min_time = 0.0;
+    o->cr_iterations = 0;
+    o->cr_early_stop = 0;
+    o->cr_early_stop_threshold = 0.1;
     o->precision = CP_AL_GB300_FP64;
     o->fp32_switch_tol = 1e-5;
     o->fp32_max_iterations = -1;
@@ -1104,11 +1183,14 @@ void oracle_cpal_result_free(cp_al_result_t *r) {
 
 /* Equilibration alone, for tests: writes the cumulative row/column scales and
  * the bound/objective factors of the reference's rescale_problem. */
-int oracle_cpal_rescale(const lp_problem_t *prob, const cp_al_parameters_t *params, double *row_scale,
-                        double *col_scale, double *cbr_ovr, double *scaled_vals) {
+int oracle_cpal_rescale(const lp_problem_t *prob, const cp_al_parameters_t *params, const cp_al_gb300_options_t *opts,
+                        double *row_scale, double *col_scale, double *cbr_ovr, double *scaled_vals) {
     Solver S;
     S.P = params;
-    oracle_cpal_default_options(&S.O);
+    if (opts)
+        S.O = *opts;
+    else
+        oracle_cpal_default_options(&S.O);
     S.n = prob->num_variables;
     S.m = prob->num_constraints;
     const int nnz = prob->constraint_matrix_num_nonzeros;
@@ -1132,7 +1214,7 @@ int oracle_cpal_rescale(const lp_problem_t *prob, const cp_al_parameters_t *para
     cbr_ovr[1] = S.ovr;
     if (scaled_vals)
         for (int k = 0; k < nnz; ++k) scaled_vals[k] = S.A.v[k];
-    return 0;
+    return S.cr_passes; /* Curtis-Reid passes run (0 when off) */
 }
 
 /* Power iteration alone: sigma_max(A) of the (unscaled) CSR matrix given. */

@@ -38,7 +38,8 @@ def lib():
         L.oracle_cpal_default_parameters.argtypes = [C.POINTER(N.CpalParameters)]
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_max_threads.restype = C.c_int
-        L.oracle_cpal_rescale.argtypes = [C.POINTER(N.LpProblem), C.POINTER(N.CpalParameters), _dp, _dp, _dp, _dp]
+        L.oracle_cpal_rescale.argtypes = [C.POINTER(N.LpProblem), C.POINTER(N.CpalParameters),
+                                          C.POINTER(N.CpalOptions), _dp, _dp, _dp, _dp]
         L.oracle_cpal_session_create.restype = C.c_void_p
         L.oracle_cpal_session_create.argtypes = [C.POINTER(N.LpProblem), C.POINTER(N.CpalParameters),
                                                  C.POINTER(N.CpalOptions)]
@@ -147,19 +148,22 @@ def solve_lp(data: LPData, params: dict | None = None, options: dict | None = No
         L.oracle_cpal_result_free(rp)
 
 
-def rescale(data: LPData, params: dict | None = None):
+def rescale(data: LPData, params: dict | None = None, options: dict | None = None, with_passes: bool = False):
     """(row_scale, col_scale, cbr, ovr, scaled A values) of the reference's
-    rescale_problem, from the oracle."""
+    rescale_problem, from the oracle; with_passes adds the number of
+    Curtis-Reid passes run."""
     L = lib()
     p = apply_params(default_parameters(), params)
+    o = apply_options(default_options(), options)
     prob = _Problem(data)
     r = np.empty(prob.m)
     d = np.empty(prob.n)
     co = np.empty(2)
     sv = np.empty(int(prob.p.constraint_matrix_num_nonzeros))
-    L.oracle_cpal_rescale(C.byref(prob.p), C.byref(p), r.ctypes.data_as(_dp), d.ctypes.data_as(_dp),
-                          co.ctypes.data_as(_dp), sv.ctypes.data_as(_dp))
-    return r, d, co[0], co[1], sv
+    passes = L.oracle_cpal_rescale(C.byref(prob.p), C.byref(p), C.byref(o), r.ctypes.data_as(_dp),
+                                   d.ctypes.data_as(_dp), co.ctypes.data_as(_dp), sv.ctypes.data_as(_dp))
+    out = (r, d, co[0], co[1], sv)
+    return out + (passes,) if with_passes else out
 
 
 def power_iteration(data: LPData, max_iter: int = 5000, tol: float = 1e-4):

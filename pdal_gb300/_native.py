@@ -182,6 +182,9 @@ class CpalOptions(C.Structure):
         ("restart_select_min_iters", C.c_int),
         ("restart_select_threepoint", C.c_int),
         ("restart_select_min_time", C.c_double),
+        ("cr_iterations", C.c_int),
+        ("cr_early_stop", C.c_int),
+        ("cr_early_stop_threshold", C.c_double),
         ("precision", C.c_int),
         ("fp32_switch_tol", C.c_double),
         ("fp32_max_iterations", C.c_int),
@@ -223,6 +226,7 @@ class CpalStats(C.Structure):
         ("power_sec", C.c_double),
         ("polish_primal_status", C.c_int),
         ("polish_dual_status", C.c_int),
+        ("cr_passes", C.c_int),
     ]
 
 

@@ -355,6 +355,7 @@ int run_batch(int count, lp_problem_t *const *problems, const cp_al_parameters_t
     bo.fp32_switch_tol = O.fp32_switch_tol;
     CpalParams cp = prep[0].cp; /* instance-specific norms are overridden per instance in the kernel */
     if (cp.restart_select != 0) throw Error("batch_solve: restart_select is not supported by the batched solver");
+    if (O.cr_iterations > 0) throw Error("batch_solve: Curtis-Reid scaling is not supported by the batched solver");
 
     int dev_id = 0, sms = 0, per_sm = 0;
     PDAL_CUDA(cudaGetDevice(&dev_id));

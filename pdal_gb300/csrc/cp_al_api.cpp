@@ -338,6 +338,9 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->restart_select_min_iters = 0;
     o->restart_select_threepoint = 0;
     o->restart_select_min_time = 0.0;
+    o->cr_iterations = 0;
+    o->cr_early_stop = 0;
+    o->cr_early_stop_threshold = 0.1;
     o->precision = CP_AL_GB300_FP64;
     o->fp32_switch_tol = 1e-5;
     o->fp32_max_iterations = -1;
@@ -353,11 +356,10 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
  * ignored). */
 /* The enabling reads: LP/CP_AL/src/solver.cu:592 (rollback trial), 889
  * (pulse), 1235 (dynamic evaluation), 1497 (sigma trigger, outside sigma
- * mode), 3168-3180 (adaptive lambda and its profiles); preconditioner.cu:
- * 403-404 (Curtis-Reid). */
+ * mode), 3168-3180 (adaptive lambda and its profiles). */
 const char *cp_al_gb300_unbuilt_switch(void) {
     static const char *const kSwitches[] = {"CP_AL_ADAPTIVE_LAMBDA", "CP_AL_DYNAMIC_EVAL", "CP_AL_ALPHA_ROLLBACK_TRIAL",
-                                            "CP_AL_ALPHA_DIRECT_PULSE", "CP_AL_CR_SCALING"};
+                                            "CP_AL_ALPHA_DIRECT_PULSE"};
     for (const char *name : kSwitches)
         if (env_int(name, 0) != 0) return name;
     if (const char *prof = getenv("CP_AL_LAMBDA_PROFILE")) {
@@ -401,6 +403,16 @@ void cp_al_gb300_options_from_env(cp_al_gb300_options_t *o) {
     o->restart_select_min_iters = env_int("CP_AL_RESTART_SELECT_MIN_ITERS", 0);
     o->restart_select_threepoint = env_int("CP_AL_RESTART_SELECT_THREEPOINT", 0);
     o->restart_select_min_time = env_double("CP_AL_RESTART_SELECT_MIN_TIME", 0.0);
+    /* LP/CP_AL/src/preconditioner.cu:174-178, 403-411 (atoi / atof, as read there) */
+    const char *cr = getenv("CP_AL_CR_SCALING");
+    int cr_iters = (cr && cr[0] != '\0' && atoi(cr) != 0) ? 20 : 0;
+    const char *cr_it = getenv("CP_AL_CR_ITERS");
+    if (cr_iters > 0 && cr_it && cr_it[0] != '\0') cr_iters = atoi(cr_it);
+    o->cr_iterations = cr_iters < 0 ? 0 : cr_iters;
+    const char *cr_es = getenv("CP_AL_CR_EARLY_STOP");
+    o->cr_early_stop = (cr_es && atoi(cr_es) != 0) ? 1 : 0;
+    const char *cr_th = getenv("CP_AL_CR_EARLY_STOP_THRESHOLD");
+    o->cr_early_stop_threshold = cr_th ? atof(cr_th) : 0.1;
 }
 
 } // extern "C"

@@ -784,6 +784,91 @@ static __global__ void k_scale_matrix(int nr, const int *__restrict__ rp, const 
     }
 }
 
+/* Curtis-Reid log scales (LP/CP_AL/src/preconditioner.cu:553-588), warp per
+ * row: the mean over the row's nonzeros of -log|a| - other[col] (|a| below
+ * 1e-300 or not finite counts as 1e-300); an empty row gets 0.  delta, when
+ * given, receives the change of the row's log scale. */
+static __global__ void k_cr_log_update(int nr, const int *__restrict__ rp, const int *__restrict__ ci,
+                                       const double *__restrict__ val, const double *__restrict__ other, double *ls,
+                                       double *delta) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nr; row += warps) {
+        const int k0 = rp[row], k1 = rp[row + 1];
+        double acc = 0.0;
+        for (int k = k0 + lane; k < k1; k += 32) {
+            double v = fabs(val[k]);
+            if (!isfinite(v) || v < 1e-300) v = 1e-300;
+            acc += -log(v) - other[ci[k]];
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) {
+            const double u = k1 > k0 ? acc / (double)(k1 - k0) : 0.0;
+            if (delta) delta[row] = u - ls[row];
+            ls[row] = u;
+        }
+    }
+}
+
+/* per-block maximum over the nonzeros of |delta_row + delta_col|, the change
+ * of a scaled entry's log (preconditioner.cu:590-609) */
+static __global__ void __launch_bounds__(kThreads) k_cr_edge_change(int nr, const int *__restrict__ rp,
+                                                                    const int *__restrict__ ci,
+                                                                    const double *__restrict__ rd,
+                                                                    const double *__restrict__ cd, double *part) {
+    __shared__ double sbuf[kThreads / 32];
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    double mx = 0.0;
+    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nr; row += warps)
+        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+            const double e = fabs(rd[row] + cd[ci[k]]);
+            if (isfinite(e) && e > mx) mx = e;
+        }
+    mx = warp_max(mx);
+    if (lane == 0) sbuf[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) b = fmax(b, sbuf[w]);
+        part[blockIdx.x] = b;
+    }
+}
+
+/* log scale -> scaling 1/f and its inverse f = clamp(exp(log), 1e-30, 1e30);
+ * cum *= 1/f (preconditioner.cu:611-624) */
+static __global__ void k_cr_exp(int len, double *ls, double *inv, double *cum) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+        const double f = fmin(fmax(exp(ls[i]), 1e-30), 1e30);
+        const double s = 1.0 / f;
+        ls[i] = s;
+        inv[i] = f;
+        cum[i] *= s;
+    }
+}
+
+/* preconditioner.cu:476-512 with the inverses given (the Curtis-Reid pass
+ * hands over f itself, not 1/(1/f)) */
+static __global__ void k_scale_vectors_inv(int n, int m, const double *__restrict__ d, const double *__restrict__ dinv,
+                                           const double *__restrict__ r, const double *__restrict__ rinv, double *c,
+                                           double *vlb, double *vub, double *x0, double *clb, double *cub, double *y0) {
+    const int total = n > m ? n : m;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        if (t < n) {
+            const double dj = d[t];
+            c[t] *= dinv[t];
+            vlb[t] *= dj;
+            vub[t] *= dj;
+            x0[t] *= dj;
+        }
+        if (t < m) {
+            clb[t] *= rinv[t];
+            cub[t] *= rinv[t];
+            y0[t] *= r[t];
+        }
+    }
+}
+
 /* preconditioner.cu:476-512 */
 static __global__ void k_scale_vectors(int n, int m, const double *__restrict__ d, const double *__restrict__ r, double *c,
                                 double *vlb, double *vub, double *x0, double *clb, double *cub, double *y0) {

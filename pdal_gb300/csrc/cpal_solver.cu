@@ -143,6 +143,7 @@ class CpalSolver {
     int64_t launches = 0;
     int64_t h2d = 0, d2h = 0;
     int power_iters = 0;
+    int cr_passes = 0; /* Curtis-Reid passes run (early stop may end them at 5) */
     int fp32_iters = 0;
     bool started = false;
     double sum_ms[2][3] = {{0, 0, 0}, {0, 0, 0}}; /* [fp64, fp32][primal, dual, block] */
@@ -647,6 +648,46 @@ void CpalSolver::setup_device() {
         PDAL_LAUNCH_CHECK();
         launches += 5;
     };
+    /* Curtis-Reid before Ruiz (LP/CP_AL/src/preconditioner.cu:162-270,
+     * 403-425): alternating row / column log-mean passes, then the scales
+     * exp(log) clamped to [1e-30, 1e30] applied like a Ruiz pass; with early
+     * stop (20 passes) the passes end after the fifth when no scaled entry's
+     * log moved by more than the threshold */
+    cr_passes = 0;
+    if (O_.cr_iterations > 0) {
+        double *lr = rstep, *lc = dstep, *dr = v64_.ybar, *dc = v64_.lam;
+        if (m) PDAL_CUDA(cudaMemsetAsync(lr, 0, m * sizeof(double), stream_));
+        PDAL_CUDA(cudaMemsetAsync(lc, 0, n * sizeof(double), stream_));
+        const bool early = O_.cr_early_stop != 0 && O_.cr_iterations == 20;
+        for (int it = 0; it < O_.cr_iterations; ++it) {
+            if (m) k_cr_log_update<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, A_.v, lc, lr, early ? dr : nullptr);
+            k_cr_log_update<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, At_.v, lr, lc, early ? dc : nullptr);
+            PDAL_LAUNCH_CHECK();
+            launches += 2;
+            cr_passes = it + 1;
+            if (early && it + 1 == 5 && m) {
+                const int ge = std::max(1, std::min(gwr_m, nmisc_));
+                k_cr_edge_change<<<ge, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, dr, dc, part_misc_);
+                PDAL_LAUNCH_CHECK();
+                launches += 1;
+                std::vector<double> part(ge);
+                PDAL_CUDA(cudaMemcpyAsync(part.data(), part_misc_, ge * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+                PDAL_CUDA(cudaStreamSynchronize(stream_));
+                d2h += ge * sizeof(double);
+                double mx = 0.0;
+                for (double v : part) mx = std::max(mx, v);
+                if (mx <= O_.cr_early_stop_threshold) break;
+            }
+        }
+        if (m) k_cr_exp<<<gm, kThreads, 0, stream_>>>(m_, lr, rinv, rsc_);
+        k_cr_exp<<<gn, kThreads, 0, stream_>>>(n_, lc, dinv, dsc_);
+        if (m) k_scale_matrix<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, A_.v, rinv, dinv, 0);
+        k_scale_matrix<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, At_.v, dinv, rinv, 1);
+        k_scale_vectors_inv<<<grid_for(std::max(n, m)), kThreads, 0, stream_>>>(n_, m_, lc, dinv, lr, rinv, c_, vlb_,
+                                                                                vub_, x0_, clb_, cub_, y0_);
+        PDAL_LAUNCH_CHECK();
+        launches += 5;
+    }
     for (int it = 0; it < P_.l_inf_ruiz_iterations; ++it) scale_pass(0, 0.0, 0.0);
     if (P_.has_pock_chambolle_alpha) scale_pass(1, P_.pock_chambolle_alpha, 2.0 - P_.pock_chambolle_alpha);
     const int gb = grid_for(std::max(n, m));
@@ -1429,6 +1470,7 @@ static void fill_stats(const pdal::CpalSolver &s, double total) {
     st.power_sec = s.power_sec;
     st.polish_primal_status = s.polish_status[0];
     st.polish_dual_status = s.polish_status[1];
+    st.cr_passes = s.cr_passes;
 }
 
 cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *params,

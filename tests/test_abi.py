@@ -223,7 +223,6 @@ def test_options_from_env_reads_reference_variables(lp_lib, monkeypatch):
     ("CP_AL_SIGMA_TRIGGER", "1", {}),
     ("CP_AL_ALPHA_ROLLBACK_TRIAL", "1", {}),
     ("CP_AL_ALPHA_DIRECT_PULSE", "1", {}),
-    ("CP_AL_CR_SCALING", "1", {}),
 ])
 def test_unbuilt_controller_switch_is_refused(lp_lib, monkeypatch, name, value, extra):
     """A CP_AL_* switch that turns on a controller this library does not
@@ -232,7 +231,7 @@ def test_unbuilt_controller_switch_is_refused(lp_lib, monkeypatch, name, value, 
     without the controller; switched off, or the sigma trigger inside sigma
     mode (where the reference ignores it), nothing is refused."""
     for var in ("CP_AL_ADAPTIVE_LAMBDA", "CP_AL_LAMBDA_PROFILE", "CP_AL_DYNAMIC_EVAL", "CP_AL_SIGMA_TRIGGER",
-                "CP_AL_ALPHA_ROLLBACK_TRIAL", "CP_AL_ALPHA_DIRECT_PULSE", "CP_AL_CR_SCALING", "CP_AL_SIGMA_MODE",
+                "CP_AL_ALPHA_ROLLBACK_TRIAL", "CP_AL_ALPHA_DIRECT_PULSE", "CP_AL_SIGMA_MODE",
                 "CP_AL_SIGMA"):
         monkeypatch.delenv(var, raising=False)
     assert lp_lib.cp_al_gb300_unbuilt_switch() is None
@@ -251,3 +250,25 @@ def test_unbuilt_controller_switch_is_refused(lp_lib, monkeypatch, name, value, 
     if name == "CP_AL_SIGMA_TRIGGER":
         monkeypatch.setenv("CP_AL_SIGMA_MODE", "1")
         assert lp_lib.cp_al_gb300_unbuilt_switch() is None
+
+
+def test_curtis_reid_options_from_env(lp_lib, monkeypatch):
+    """CP_AL_CR_SCALING / CP_AL_CR_ITERS / CP_AL_CR_EARLY_STOP(_THRESHOLD) are
+    read with the reference's atoi / atof rules (LP/CP_AL/src/
+    preconditioner.cu:174-178, 403-411)."""
+    for var in ("CP_AL_CR_SCALING", "CP_AL_CR_ITERS", "CP_AL_CR_EARLY_STOP", "CP_AL_CR_EARLY_STOP_THRESHOLD"):
+        monkeypatch.delenv(var, raising=False)
+    o = lp.default_options(lp_lib, from_env=True)
+    assert (o.cr_iterations, o.cr_early_stop, o.cr_early_stop_threshold) == (0, 0, 0.1)
+    monkeypatch.setenv("CP_AL_CR_ITERS", "7")
+    assert lp.default_options(lp_lib, from_env=True).cr_iterations == 0
+    monkeypatch.setenv("CP_AL_CR_SCALING", "1")
+    assert lp.default_options(lp_lib, from_env=True).cr_iterations == 7
+    monkeypatch.setenv("CP_AL_CR_ITERS", "abc")
+    assert lp.default_options(lp_lib, from_env=True).cr_iterations == 0
+    monkeypatch.delenv("CP_AL_CR_ITERS")
+    monkeypatch.setenv("CP_AL_CR_EARLY_STOP", "1")
+    monkeypatch.setenv("CP_AL_CR_EARLY_STOP_THRESHOLD", "0.25")
+    o = lp.default_options(lp_lib, from_env=True)
+    assert (o.cr_iterations, o.cr_early_stop, o.cr_early_stop_threshold) == (20, 1, 0.25)
+    assert lp_lib.cp_al_gb300_unbuilt_switch() is None

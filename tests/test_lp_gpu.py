@@ -281,6 +281,41 @@ def test_restart_three_point_fp32_form(lp_lib):
     assert rel(g.primal_objective, o.primal_objective) <= 1e-6
 
 
+@pytest.mark.parametrize("opts,passes", [
+    ({"cr_iterations": 20}, 20),
+    ({"cr_iterations": 20, "cr_early_stop": 1, "cr_early_stop_threshold": 1e9}, 5),
+    ({"cr_iterations": 7}, 7),
+], ids=["cr20", "cr_early_stop", "cr7"])
+def test_curtis_reid_scaling_matches_oracle(lp_lib, opts, passes):
+    """The device Curtis-Reid passes before Ruiz (LP/CP_AL/src/
+    preconditioner.cu:162-270, 553-624) on a badly scaled LP: the same number
+    of passes as the oracle and the same cumulative scales, scaled matrix and
+    bound/objective factors to 1e-11 relative (log and exp of the device and
+    the host libraries may differ in the last bit)."""
+    d = I.zipf_lp(400, 900, nnz=6000, seed=3, max_row=300)
+    prm = {"l_inf_ruiz_iterations": 4}
+    s = lp.LPSession(d, prm, opts)
+    try:
+        s.start()
+        vals, r, c, cbr, ovr, _ = s.scaling()
+    finally:
+        s.close()
+    ro, co, cbro, ovro, svo, po = O.rescale(d, prm, opts, with_passes=True)
+    assert po == passes
+    for a, b in ((r, ro), (c, co), (vals, svo)):
+        assert np.max(np.abs(a - b) / np.abs(b)) < 1e-11
+    assert rel(cbr, cbro) < 1e-11 and rel(ovr, ovro) < 1e-11
+
+
+def test_curtis_reid_solve_parity(lp_lib):
+    """A solve with Curtis-Reid scaling on: the oracle's status, iterations
+    and objectives."""
+    d = I.random_lp(300, 700, 6, seed=21)
+    g, o = both(d, {"eps": 1e-8, "l_inf_ruiz_iterations": 4}, {"cr_iterations": 20})
+    assert g.status == "OPTIMAL" and g.stats["cr_passes"] == 20
+    assert_parity(g, o)
+
+
 @pytest.mark.parametrize("kind", ["random", "transport"])
 def test_feasibility_polishing_matches_oracle(kind):
     """Feasibility polishing (LP/CP_AL/src/solver.cu:3912-4456) after a loose

@@ -152,3 +152,28 @@ def test_oracle_restart_three_point():
         g = O.solve_lp(d, prm, {"restart_select": 3, **gate})
         assert g.stats["restart_targets"][1:] == (0, 0)
         assert g.iterations == plain.iterations
+
+
+def test_oracle_curtis_reid():
+    """Curtis-Reid scaling before Ruiz (LP/CP_AL/src/preconditioner.cu:162-270,
+    553-624): on a badly scaled LP its passes shrink the spread of log|a| of
+    the scaled matrix to a fraction, early stop ends them after the fifth pass
+    when the threshold allows it and never otherwise, and a solve with it
+    reaches HiGHS's optimum."""
+    d = I.zipf_lp(400, 900, nnz=6000, seed=3, max_row=300)
+    base = {"l_inf_ruiz_iterations": 0, "has_pock_chambolle_alpha": False, "bound_objective_rescaling": False}
+    raw = np.log10(np.abs(d.csr()[2]))
+    *_, sv, p20 = O.rescale(d, base, {"cr_iterations": 20}, with_passes=True)
+    assert p20 == 20
+    assert np.log10(np.abs(sv)).std() < 0.3 * raw.std()
+    *_, p5 = O.rescale(d, base, {"cr_iterations": 20, "cr_early_stop": 1, "cr_early_stop_threshold": 1e9},
+                       with_passes=True)
+    *_, pn = O.rescale(d, base, {"cr_iterations": 20, "cr_early_stop": 1, "cr_early_stop_threshold": -1.0},
+                       with_passes=True)
+    *_, p7 = O.rescale(d, base, {"cr_iterations": 7, "cr_early_stop": 1, "cr_early_stop_threshold": 1e9},
+                       with_passes=True)
+    assert (p5, pn, p7) == (5, 20, 7)
+    case = I.random_lp(300, 700, 6, seed=21)
+    res = O.solve_lp(case, {"eps": 1e-8, "l_inf_ruiz_iterations": 4}, {"cr_iterations": 20})
+    f = highs_objective(case)
+    assert res.status == "OPTIMAL" and abs(res.primal_objective - f) <= 1e-6 * (1 + abs(f))

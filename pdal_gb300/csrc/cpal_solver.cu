@@ -1473,6 +1473,17 @@ static void fill_stats(const pdal::CpalSolver &s, double total) {
     st.cr_passes = s.cr_passes;
 }
 
+/* Options from the environment, unless a switch of a controller this library
+ * lacks is set (then false, with the message). */
+static bool options_from_env_checked(cp_al_gb300_options_t &o, const char *who) {
+    if (const char *sw = cp_al_gb300_unbuilt_switch()) {
+        set_error(std::string(who) + ": " + sw + " is set, but the controller it enables is not part of this library");
+        return false;
+    }
+    cp_al_gb300_options_from_env(&o);
+    return true;
+}
+
 cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *params,
                                   const cp_al_gb300_options_t *opts) {
     g_last_error.clear();
@@ -1488,8 +1499,8 @@ cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *
     cp_al_gb300_options_t o;
     if (opts)
         o = *opts;
-    else
-        cp_al_gb300_options_from_env(&o);
+    else if (!options_from_env_checked(o, "solve_lp_problem"))
+        return nullptr;
     const double t0 = pdal::now_sec();
     cp_al_result_t *res = (cp_al_result_t *)calloc(1, sizeof(cp_al_result_t));
     if (!res) {
@@ -1527,12 +1538,6 @@ cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *
 }
 
 cp_al_result_t *solve_lp_problem(lp_problem_t *prob, const cp_al_parameters_t *params) {
-    if (const char *sw = cp_al_gb300_unbuilt_switch()) {
-        g_last_error.clear();
-        set_error(std::string("solve_lp_problem: ") + sw +
-                  " is set, but the controller it enables is not part of this library");
-        return nullptr;
-    }
     return cp_al_gb300_solve(prob, params, nullptr);
 }
 
@@ -1543,6 +1548,11 @@ cp_al_gb300_session_t *cp_al_gb300_session_create(const lp_problem_t *prob, cons
         set_error("session_create: invalid arguments.");
         return nullptr;
     }
+    cp_al_gb300_options_t o;
+    if (opts)
+        o = *opts;
+    else if (!options_from_env_checked(o, "session_create"))
+        return nullptr;
     try {
         auto *sess = new cp_al_gb300_session;
         cp_al_parameters_t local;
@@ -1550,11 +1560,6 @@ cp_al_gb300_session_t *cp_al_gb300_session_create(const lp_problem_t *prob, cons
             local = *params;
         else
             set_default_parameters(&local);
-        cp_al_gb300_options_t o;
-        if (opts)
-            o = *opts;
-        else
-            cp_al_gb300_options_from_env(&o);
         sess->prob_copy = *prob;
         sess->solver.reset(new pdal::CpalSolver(&sess->prob_copy, &local, &o));
         sess->solver->prepare();

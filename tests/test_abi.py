@@ -226,10 +226,12 @@ def test_options_from_env_reads_reference_variables(lp_lib, monkeypatch):
 ])
 def test_unbuilt_controller_switch_is_refused(lp_lib, monkeypatch, name, value, extra):
     """A CP_AL_* switch that turns on a controller this library does not
-    implement makes solve_lp_problem return NULL with a message naming it
-    (before any device work, so this runs without a GPU) instead of solving
-    without the controller; switched off, or the sigma trigger inside sigma
-    mode (where the reference ignores it), nothing is refused."""
+    implement makes solve_lp_problem (and cp_al_gb300_solve or
+    cp_al_gb300_session_create without explicit options) return NULL with a
+    message naming it (before any device work, so this runs without a GPU)
+    instead of solving without the controller; switched off, or the sigma
+    trigger inside sigma mode (where the reference ignores it), nothing is
+    refused."""
     for var in ("CP_AL_ADAPTIVE_LAMBDA", "CP_AL_LAMBDA_PROFILE", "CP_AL_DYNAMIC_EVAL", "CP_AL_SIGMA_TRIGGER",
                 "CP_AL_ALPHA_ROLLBACK_TRIAL", "CP_AL_ALPHA_DIRECT_PULSE", "CP_AL_SIGMA_MODE",
                 "CP_AL_SIGMA"):
@@ -244,6 +246,10 @@ def test_unbuilt_controller_switch_is_refused(lp_lib, monkeypatch, name, value, 
     prob = lp._CProblem(lp_lib, data)
     try:
         assert not lp_lib.solve_lp_problem(prob.ptr, None)
+        assert name in N.last_error(lp_lib)
+        # every entry point that takes its options from the environment
+        assert not lp_lib.cp_al_gb300_solve(prob.ptr, None, None)
+        assert not lp_lib.cp_al_gb300_session_create(prob.ptr, None, None)
         assert name in N.last_error(lp_lib)
     finally:
         prob.close()

@@ -317,7 +317,7 @@ def run_ours(args, rank, world, local):
             "time_to_kkt_1e-6_small_lp": kkt,
             "clocks": clk.summary(),
         }
-        line["cpu_baseline"] = cpu_baseline(data, m, n, nnz)
+        line["cpu_baseline"] = cpu_baseline(data, m, n, nnz, single=args.cpu_single)
         line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:
@@ -458,9 +458,10 @@ def bench_learned(local, S=40, D=40, n_train=4096, n_test=256, epochs=100):
             "all_optimal": all(r.status == "OPTIMAL" for r in cold + warm)}
 
 
-def cpu_baseline(data, m, n, nnz, blocks=1, warm=0):
+def cpu_baseline(data, m, n, nnz, blocks=1, warm=0, single=False):
     """The CPU restatement (oracle port) on every host core: one evaluation
-    block (200 iterations) after setup, in the metric's unit."""
+    block (200 iterations) after setup, in the metric's unit; with single,
+    also one more block of the same session on one thread."""
     from oracle import oracle as O
 
     threads = os.cpu_count() or 1
@@ -470,12 +471,20 @@ def cpu_baseline(data, m, n, nnz, blocks=1, warm=0):
     t0 = time.perf_counter()
     done = sum(s.iterate(200) for _ in range(blocks))
     dt = time.perf_counter() - t0
-    s.close()
     b_p, b_d = iteration_bytes(m, n, nnz, 8)
-    return {"value": (b_p + b_d) * done / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
-            "sample": f"{done} iterations of the same LP and settings (setup excluded) with {threads} threads, "
-                      f"{dt / done * 1e3:.1f} ms/iteration",
-            "ms_per_iteration": dt / done * 1e3}
+    out = {"value": (b_p + b_d) * done / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+           "sample": f"{done} iterations of the same LP and settings (setup excluded) with {threads} threads, "
+                     f"{dt / done * 1e3:.1f} ms/iteration",
+           "ms_per_iteration": dt / done * 1e3}
+    if single:
+        s.set_threads(1)
+        t0 = time.perf_counter()
+        d1 = s.iterate(200)
+        dt1 = time.perf_counter() - t0
+        out["single_thread"] = {"value": (b_p + b_d) * d1 / dt1 / 1e9, "unit": "GB/s", "cores": 1,
+                                "ms_per_iteration": dt1 / d1 * 1e3, "iterations": d1}
+    s.close()
+    return out
 
 
 def run_reference(args, rank, world, local):
@@ -518,6 +527,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_lp", choices=list(WORKLOADS))
     ap.add_argument("--lp-only", action="store_true", help="skip the QP, batch and learned-start sections")
+    ap.add_argument("--cpu-single", action="store_true",
+                    help="also time the CPU port on one thread (one more 200-iteration block, ~30 s)")
     ap.add_argument("--profile", action="store_true", help="only the chosen-form iteration steps (for ncu)")
     ap.add_argument("--profile-section", default="lp", choices=["lp", "qp", "qp_fp32", "batch"],
                     help="with --profile: which solver's kernels to run")

@@ -191,6 +191,10 @@ class Session:
     def iterate(self, iterations: int) -> int:
         return lib().oracle_cpal_session_iterate(self.h, int(iterations))
 
+    def set_threads(self, threads: int):
+        """Host threads of the following iterations."""
+        lib().oracle_set_threads(int(threads))
+
     def close(self):
         if self.h:
             lib().oracle_cpal_session_free(self.h)

@@ -278,3 +278,19 @@ def test_curtis_reid_options_from_env(lp_lib, monkeypatch):
     o = lp.default_options(lp_lib, from_env=True)
     assert (o.cr_iterations, o.cr_early_stop, o.cr_early_stop_threshold) == (20, 1, 0.25)
     assert lp_lib.cp_al_gb300_unbuilt_switch() is None
+
+
+@pytest.mark.parametrize("profile,refused", [
+    ("grid4_race", True), ("race4", True), ("mp_race", True), ("safe_race", True), ("mp_auto", True),
+    ("safe_auto", True), ("fixed", False), ("", False),
+])
+def test_lambda_profiles_that_enable_adaptive_lambda(lp_lib, monkeypatch, profile, refused):
+    """The CP_AL_LAMBDA_PROFILE values that switch the reference's adaptive
+    lambda on (LP/CP_AL/src/solver.cu:3168-3180) are refused; others are
+    not."""
+    for var in ("CP_AL_ADAPTIVE_LAMBDA", "CP_AL_DYNAMIC_EVAL", "CP_AL_SIGMA_TRIGGER", "CP_AL_ALPHA_ROLLBACK_TRIAL",
+                "CP_AL_ALPHA_DIRECT_PULSE"):
+        monkeypatch.delenv(var, raising=False)
+    monkeypatch.setenv("CP_AL_LAMBDA_PROFILE", profile)
+    got = lp_lib.cp_al_gb300_unbuilt_switch()
+    assert got == (b"CP_AL_LAMBDA_PROFILE" if refused else None)

@@ -177,3 +177,16 @@ def test_oracle_curtis_reid():
     res = O.solve_lp(case, {"eps": 1e-8, "l_inf_ruiz_iterations": 4}, {"cr_iterations": 20})
     f = highs_objective(case)
     assert res.status == "OPTIMAL" and abs(res.primal_objective - f) <= 1e-6 * (1 + abs(f))
+
+
+@pytest.mark.parametrize("options", [
+    {"restart_select": 1}, {"restart_select": 2}, {"restart_select": 3},
+    {"restart_select": 1, "restart_select_margin": 0.9}, {"restart_select": 3, "al_lambda": 0.0},
+], ids=["select1", "select2", "select3", "select1_margin", "select3_lambda0"])
+def test_oracle_restart_selection_reaches_optimum(options):
+    """Every restart target selection mode of the oracle
+    (LP/CP_AL/src/solver.cu:2749-2819) still solves to HiGHS's optimum."""
+    for d in (I.random_lp(300, 700, 6, seed=21), I.transport_lp(15, 12, seed=5)):
+        r = O.solve_lp(d, {"eps": 1e-8, "l_inf_ruiz_iterations": 4, "reflection_coefficient": 0.5}, options)
+        f = highs_objective(d)
+        assert r.status == "OPTIMAL" and abs(r.primal_objective - f) <= 1e-6 * (1 + abs(f))

@@ -197,7 +197,9 @@ struct Solver {
             update(A, lc, lr, dr);
             update(At, lr, lc, dc);
             cr_passes = it + 1;
-            if (early && it + 1 == 5 && m > 0) {
+            if (early && it + 1 == 5) {
+                /* a maximum over no rows is the lowest double: below any threshold */
+                if (m == 0) break;
                 double mx = 0.0;
                 for (int i = 0; i < m; ++i)
                     for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) {

@@ -665,7 +665,9 @@ void CpalSolver::setup_device() {
             PDAL_LAUNCH_CHECK();
             launches += 2;
             cr_passes = it + 1;
-            if (early && it + 1 == 5 && m) {
+            if (early && it + 1 == 5) {
+                /* a maximum over no rows is the lowest double: below any threshold */
+                if (!m) break;
                 const int ge = std::max(1, std::min(gwr_m, nmisc_));
                 k_cr_edge_change<<<ge, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, dr, dc, part_misc_);
                 PDAL_LAUNCH_CHECK();

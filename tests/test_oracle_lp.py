@@ -12,6 +12,7 @@ from scipy.optimize import linprog
 
 from oracle import oracle as O
 from pdal_gb300 import instances as I
+from pdal_gb300.lp import LPData
 
 
 def highs_objective(d):
@@ -190,3 +191,17 @@ def test_oracle_restart_selection_reaches_optimum(options):
         r = O.solve_lp(d, {"eps": 1e-8, "l_inf_ruiz_iterations": 4, "reflection_coefficient": 0.5}, options)
         f = highs_objective(d)
         assert r.status == "OPTIMAL" and abs(r.primal_objective - f) <= 1e-6 * (1 + abs(f))
+
+
+def test_oracle_curtis_reid_without_constraints():
+    """Curtis-Reid on an LP without constraints: every scale stays 1 and early
+    stop ends the passes after the fifth (the reference's maximum over no
+    rows is the lowest double)."""
+    n = 50
+    d = LPData(np.linspace(-1, 1, n), (np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0), (0, n)),
+               np.zeros(0), np.zeros(0), np.zeros(n), np.full(n, 3.0))
+    base = {"l_inf_ruiz_iterations": 0, "has_pock_chambolle_alpha": False, "bound_objective_rescaling": False}
+    _, c, _, _, _, p = O.rescale(d, base, {"cr_iterations": 20, "cr_early_stop": 1}, with_passes=True)
+    assert p == 5 and np.all(c == 1.0)
+    *_, p20 = O.rescale(d, base, {"cr_iterations": 20}, with_passes=True)
+    assert p20 == 20

@@ -275,8 +275,13 @@ def run_ours(args, rank, world, local):
 
     extras = {}
     if not args.lp_only:
+        def gather(obj):
+            out = [None] * world
+            dist.all_gather_object(out, obj)
+            return out
+
         extras["batch_4096"] = bench_batch(local, rank=rank, world=world, barrier=barrier,
-                                           max_over_ranks=max_over_ranks)
+                                           max_over_ranks=max_over_ranks, gather=gather if dist else None)
         if rank == 0:
             extras["fa_cp_qp"] = bench_qp(local)
             extras["learned_warm_start"] = bench_learned(local)
@@ -365,7 +370,7 @@ def bench_qp(local):
     return out
 
 
-def bench_batch(local, count=4096, rank=0, world=1, barrier=None, max_over_ranks=None):
+def bench_batch(local, count=4096, rank=0, world=1, barrier=None, max_over_ranks=None, gather=None):
     """4,096 uneven LPs (m log-uniform in [50, 5000], n = m*U[2,3], 3-20
     nnz/column, planted) solved to relative KKT 1e-6 in one persistent launch,
     chosen form (FP32 phase + FP64 refinement) and FP64, against the plain FP64
@@ -374,11 +379,12 @@ def bench_batch(local, count=4096, rank=0, world=1, barrier=None, max_over_ranks
     instances are split by an LPT assignment (no collective on the data path)
     and the time is the maximum over ranks."""
     from pdal_gb300 import instances, lp
-    from pdal_gb300.shard import instance_weight, lpt_partition
+    from pdal_gb300.shard import assemble, instance_weight, lpt_partition
 
     items = instances.batch_lps(count=count)
     nnz = sum(int(d.csr()[1].shape[0]) for d in items)
-    mine = lpt_partition([instance_weight(d) for d in items], world)[rank]
+    parts = lpt_partition([instance_weight(d) for d in items], world)
+    mine = parts[rank]
     shard = [items[i] for i in mine]
     params = {"eps": 1e-6, "l_inf_ruiz_iterations": 4, "iteration_limit": 100_000}
     out = {"workload": f"{count} LPs, m log-uniform [50, 5000], n = m*U[2,3], 3-20 nnz/column",
@@ -399,10 +405,15 @@ def bench_batch(local, count=4096, rank=0, world=1, barrier=None, max_over_ranks
         wall = time.perf_counter() - t0
         if max_over_ranks:
             wall = max_over_ranks(wall)
+        rows = [(r.status == "OPTIMAL", r.iterations, r.kkt) for r in res]
+        if gather is not None and world > 1:
+            # every rank's per-instance results, back in the batch's order
+            rows = assemble(parts, gather(rows))
+        its = np.array([q[1] for q in rows])
         out[tag] = {"total_s": wall, "kernel_s": st["kernel_sec"], "solves_per_s": count / wall,
-                    "optimal": st["optimal"], "iterations_p50": st["iterations_p50"],
-                    "iterations_p99": st["iterations_p99"], "iterations_max": st["iterations_max"],
-                    "max_kkt": max(r.kkt for r in res), "grid_blocks": st["grid_blocks"],
+                    "optimal": int(sum(q[0] for q in rows)), "iterations_p50": float(np.percentile(its, 50)),
+                    "iterations_p99": float(np.percentile(its, 99)), "iterations_max": int(its.max()),
+                    "max_kkt": max(q[2] for q in rows), "grid_blocks": st["grid_blocks"],
                     "schedule": {"block_nnz": st["block_nnz"], "blocks_per_sm": st["blocks_per_sm"],
                                  "tune_s": sched["tune_sec"], "tuned_before_solve": st["tune_sec"] == 0.0}}
     if rank != 0:
@@ -519,6 +530,24 @@ def run_reference(args, rank, world, local):
     }), flush=True)
 
 
+def spawn_ranks(n: int) -> int:
+    """--gpus N without a launcher: start N local ranks of this same command
+    (RANK = LOCAL_RANK = i, WORLD_SIZE = N, rendezvous on 127.0.0.1), one per
+    GPU, as torchrun would; rank 0 prints the line.  Returns the worst exit
+    code."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    procs = []
+    for i in range(n):
+        env = {**os.environ, "RANK": str(i), "LOCAL_RANK": str(i), "WORLD_SIZE": str(n),
+               "LOCAL_WORLD_SIZE": str(n), "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)}
+        procs.append(subprocess.Popen([sys.executable, str(Path(__file__).resolve()), *sys.argv[1:]], env=env))
+    return max(abs(p.wait()) for p in procs)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -533,6 +562,8 @@ def main():
     ap.add_argument("--profile-section", default="lp", choices=["lp", "qp", "qp_fp32", "batch"],
                     help="with --profile: which solver's kernels to run")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(spawn_ranks(args.gpus))
     rank, world, local = dist_env()
     if args.profile:
         run_profile(args, local)

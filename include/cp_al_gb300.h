@@ -86,6 +86,12 @@ typedef struct {
                                      budget 1,024 / 2,048 x 2-4 blocks per SM) on a probe
                                      of the largest instances (200 iterations) and keeps
                                      the fastest, remembered per batch shape */
+    int dual_panels;              /* rows with more nonzeros than the row-block budget in the
+                                     iteration's A x product: 1 = by column panels (x staged in
+                                     shared memory, one partial per row and panel), 0 = as
+                                     row pieces, -1 (default) = panels when those rows hold at
+                                     least 2^20 nonzeros */
+    int panel_width;              /* columns per panel, a multiple of 4 up to 65536; 0 = 16384 */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */
@@ -125,6 +131,8 @@ typedef struct {
     int polish_primal_status;
     int polish_dual_status;
     int cr_passes; /* Curtis-Reid passes run in the equilibration */
+    int panel_rows; /* long rows the iteration's A x product runs by column panels (0: none) */
+    int panels;     /* column panels of that product */
 } cp_al_gb300_stats_t;
 
 /* The reference defaults of every field, ignoring the environment. */
@@ -255,10 +263,15 @@ int cp_al_gb300_session_scaling(cp_al_gb300_session_t *s, double *scaled_values,
  * inside the library, which every device that loads the library holds until
  * the process exits, so at most 524,288 rows are accepted (larger m returns
  * -1 with a message).  The first call on a device looks up that array's
- * device address (cudaGetSymbolAddress); make it before any stream capture.
+ * device address (cudaGetSymbolAddress) and keeps it with the id of the
+ * current context; a call under another context of that device (after
+ * cudaDeviceReset, say) looks it up again.  Make the first call on each
+ * device, and the first after a reset, before any stream capture.
  * All calls share the array, so calls that overlap on the GPU (different
- * streams, or several host threads) race; serialise them.  The launch is
- * asynchronous on `stream`; returns 0, or -1 on a bad argument or CUDA error. */
+ * streams, or several host threads) race; serialise them.  A NaN in the
+ * inputs shows as NaN in out[0] and out[1].  The launch is asynchronous on
+ * `stream`; returns 0, or -1 on a bad argument or CUDA error, with the
+ * message in cp_al_gb300_last_error(). */
 int cp_al_gb300_primal_kkt_noalloc(int m, int n, const int *row_ptr, const int *col_ind, const double *vals,
                                    const double *con_lb, const double *con_ub, const double *c, const double *x,
                                    double *out, void *stream);

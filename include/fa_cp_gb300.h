@@ -38,6 +38,14 @@ typedef struct {
     int precision;
     double fp32_switch_tol;  /* default 1e-5 */
     int fp32_stall_evals;    /* default 25 */
+    /* The persistent kernel's grid barriers give up after barrier_spin_limit
+     * polls (0 = the default, about two seconds) and the solve then fails
+     * with a message instead of hanging.  barrier_extra_arrivals makes every
+     * barrier wait for that many blocks more than the launch has, so that
+     * the bounded wait runs out: it exists to test that failure path, never
+     * set it in a real solve. */
+    long long barrier_spin_limit;
+    int barrier_extra_arrivals;
 } fa_cp_gb300_options_t;
 
 typedef struct {

@@ -6,6 +6,8 @@ than one thread).
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -29,7 +31,8 @@ def build() -> Path:
     return TARGET
 
 
-REFERENCE = Path("/root/reference")
+# where the reference sources lie (read in place, never copied into the repository)
+REFERENCE = Path(os.environ.get("PDAL_REFERENCE_DIR", "/root/reference"))
 REF_OUT = HERE / "_ref"
 SHIM = HERE / "ref_shim"
 # reference MPS readers, compiled from their own sources where they lie:
@@ -87,7 +90,76 @@ def build_ref() -> list[Path]:
     return out
 
 
+# the reference solvers: executable -> (project, C sources, CUDA sources, driver macro)
+REF_SOLVERS = {
+    "ref_cp_al": ("LP/CP_AL", ["cp_al.c"], ["solver.cu", "utils.cu", "preconditioner.cu"], "REF_LP"),
+    "ref_fa_cp": ("QP/FA_CP", ["fa_cp.c", "preconditioner.c"],
+                  ["solver.cu", "utils.cu", "solver_state.cu", "fa_cp_core_op.cu"], "REF_QP"),
+}
+DRIVER = HERE / "ref_driver" / "ref_solve.c"
+
+
+def build_ref_solvers(reference: Path | None = None, jobs: int | None = None) -> list[Path]:
+    """Compiles the reference's own CP_AL and FA_CP solvers (their src/*.c and
+    src/*.cu, unmodified, read where they lie) for sm_103a as the reference's
+    CMake does (-O3, separable device compilation, cuSPARSE and cuBLAS), and
+    links each with the driver ref_driver/ref_solve.c into oracle/_ref/.
+    CP_AL's presolve library (PSLP) is absent: ref_shim/ gives its header and
+    entry points, never reached with presolve off.  The MPS readers and the
+    command-line programs are not part of these builds.  `reference` (default:
+    PDAL_REFERENCE_DIR, else the reference's usual location) must hold
+    LP/CP_AL and QP/FA_CP.  Returns the executables, or [] where the sources
+    are absent.  Test infrastructure: only the fixture script
+    tests/golden/make_ref_solver_golden.py runs them."""
+    ref = Path(reference) if reference else REFERENCE
+    if not (ref / "LP" / "CP_AL" / "src" / "solver.cu").exists():
+        return []
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cuda_inc = _cuda_include()
+    REF_OUT.mkdir(exist_ok=True)
+    objdir = REF_OUT / "obj"
+    objdir.mkdir(exist_ok=True)
+    jobs_list = []  # (exe, object, command)
+    for exe, (proj, csrcs, cusrcs, macro) in REF_SOLVERS.items():
+        inc = ["-I", str(SHIM), "-I", str(ref / proj / "include"), "-I", str(ref / proj / "internal")]
+        for s in cusrcs:
+            obj = objdir / f"{exe}_{Path(s).stem}.o"
+            jobs_list.append((exe, obj, [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-rdc=true",
+                                         "-std=c++17", "-w", *inc, "-c", str(ref / proj / "src" / s), "-o",
+                                         str(obj)]))
+        for s in csrcs:
+            obj = objdir / f"{exe}_{Path(s).stem}.o"
+            jobs_list.append((exe, obj, ["gcc", "-O3", "-std=gnu99", "-w", *inc, "-I", cuda_inc, "-c",
+                                         str(ref / proj / "src" / s), "-o", str(obj)]))
+        extra = [SHIM / "ref_presolve_stub.c"] if macro == "REF_LP" else []
+        for s in [DRIVER, *extra]:
+            obj = objdir / f"{exe}_{s.stem}.o"
+            jobs_list.append((exe, obj, ["gcc", "-O2", "-std=gnu99", "-w", f"-D{macro}", *inc, "-I", cuda_inc,
+                                         "-c", str(s), "-o", str(obj)]))
+
+    def run(cmd):
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("reference solver build failed:\n" + " ".join(cmd) + "\n" + res.stderr[-4000:])
+
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 2)) as ex:
+        list(ex.map(run, [j[2] for j in jobs_list]))
+    out = []
+    for exe in REF_SOLVERS:
+        objs = [str(o) for e, o, _ in jobs_list if e == exe]
+        target = REF_OUT / exe
+        run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-rdc=true", *objs, "-lcusparse", "-lcublas",
+             "-lm", "-o", str(target)])
+        out.append(target)
+    return out
+
+
 if __name__ == "__main__":
+    import sys
+
     print(build())
     for p in build_ref():
         print(p)
+    if "--solvers" in sys.argv:
+        for p in build_ref_solvers():
+            print(p)

@@ -194,6 +194,8 @@ class CpalOptions(C.Structure):
         ("timing", C.c_int),
         ("fp32_stall_evals", C.c_int),
         ("batch_blocks_per_sm", C.c_int),
+        ("dual_panels", C.c_int),
+        ("panel_width", C.c_int),
     ]
 
 
@@ -227,6 +229,8 @@ class CpalStats(C.Structure):
         ("polish_primal_status", C.c_int),
         ("polish_dual_status", C.c_int),
         ("cr_passes", C.c_int),
+        ("panel_rows", C.c_int),
+        ("panels", C.c_int),
     ]
 
 
@@ -452,6 +456,8 @@ class FacpOptions(C.Structure):
         ("precision", C.c_int),
         ("fp32_switch_tol", C.c_double),
         ("fp32_stall_evals", C.c_int),
+        ("barrier_spin_limit", C.c_longlong),
+        ("barrier_extra_arrivals", C.c_int),
     ]
 
 

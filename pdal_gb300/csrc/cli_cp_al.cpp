@@ -100,35 +100,91 @@ void save_summary(const cp_al_result_t *r, const char *dir, const std::string &n
     fclose(f);
 }
 
+/* One command-line option: its long name, its short letter (0 if none),
+ * whether it takes a value, what it sets, and its help line.  The names,
+ * meanings and defaults are the reference command's (LP/CP_AL/src/cli.c:
+ * 908-1005), which scripts call by name; the table, its order and the help
+ * wording are this command's own. */
+struct Option {
+    const char *name;
+    char letter;
+    const char *value; /* name of the value in the help, nullptr for a switch */
+    const char *help;
+    /* returns false on a bad value (message already printed) */
+    bool (*apply)(cp_al_parameters_t &, const char *);
+};
+
+bool set_norm(cp_al_parameters_t &p, const char *v) {
+    if (strcmp(v, "l2") == 0) {
+        p.optimality_norm = NORM_TYPE_L2;
+    } else if (strcmp(v, "linf") == 0) {
+        p.optimality_norm = NORM_TYPE_L_INF;
+    } else {
+        fprintf(stderr, "Error: opt_norm must be 'l2' or 'linf'\n");
+        return false;
+    }
+    return true;
+}
+
+const Option kOptions[] = {
+    {"eps_opt", 0, "TOL", "stop when the relative duality gap is below TOL (1e-4)",
+     [](cp_al_parameters_t &p, const char *v) { return p.termination_criteria.eps_optimal_relative = atof(v), true; }},
+    {"eps_feas", 0, "TOL", "and both relative residuals are below TOL (1e-4)",
+     [](cp_al_parameters_t &p, const char *v) { return p.termination_criteria.eps_feasible_relative = atof(v), true; }},
+    {"opt_norm", 0, "l2|linf", "norm of the residuals in that test (l2)", set_norm},
+    {"iter_limit", 0, "N", "give up after N iterations (no limit)",
+     [](cp_al_parameters_t &p, const char *v) { return p.termination_criteria.iteration_limit = atoi(v), true; }},
+    {"time_limit", 0, "SEC", "give up after SEC seconds of wall time (3600)",
+     [](cp_al_parameters_t &p, const char *v) { return p.termination_criteria.time_sec_limit = atof(v), true; }},
+    {"eval_freq", 0, "N", "iterations between two evaluations of the stopping test (200, at least 3)",
+     [](cp_al_parameters_t &p, const char *v) { return p.termination_evaluation_frequency = atoi(v), true; }},
+    {"l_inf_ruiz_iter", 0, "N", "passes of Ruiz max-norm equilibration (10)",
+     [](cp_al_parameters_t &p, const char *v) { return p.l_inf_ruiz_iterations = atoi(v), true; }},
+    {"pock_chambolle_alpha", 0, "A", "exponent of the Pock-Chambolle scaling pass (1.0)",
+     [](cp_al_parameters_t &p, const char *v) { return p.pock_chambolle_alpha = atof(v), true; }},
+    {"no_pock_chambolle", 0, nullptr, "skip the Pock-Chambolle scaling pass",
+     [](cp_al_parameters_t &p, const char *) { return p.has_pock_chambolle_alpha = false, true; }},
+    {"no_bound_obj_rescaling", 0, nullptr, "skip the scaling of bounds and objective",
+     [](cp_al_parameters_t &p, const char *) { return p.bound_objective_rescaling = false, true; }},
+    {"sv_max_iter", 0, "N", "cap on power-iteration steps for the largest singular value (5000)",
+     [](cp_al_parameters_t &p, const char *v) { return p.sv_max_iter = atoi(v), true; }},
+    {"sv_tol", 0, "TOL", "power-iteration stopping tolerance (1e-4)",
+     [](cp_al_parameters_t &p, const char *v) { return p.sv_tol = atof(v), true; }},
+    {"feasibility_polishing", 'f', nullptr, "run the primal and dual polishing phases after the solve",
+     [](cp_al_parameters_t &p, const char *) { return p.feasibility_polishing = true, true; }},
+    {"eps_feas_polish", 0, "TOL", "residual target of the polishing phases (1e-6)",
+     [](cp_al_parameters_t &p, const char *v) {
+         return p.termination_criteria.eps_feas_polish_relative = atof(v), true;
+     }},
+    {"matrix_zero_tol", 0, "TOL", "treat constraint entries below TOL in magnitude as zero",
+     [](cp_al_parameters_t &p, const char *v) { return p.matrix_zero_tol = atof(v), true; }},
+    {"no_presolve", 0, nullptr, "accepted for compatibility; this build never presolves",
+     [](cp_al_parameters_t &p, const char *) { return p.presolve = false, true; }},
+    {"verbose", 'v', nullptr, "print progress while solving",
+     [](cp_al_parameters_t &p, const char *) { return p.verbose = true, true; }},
+};
+constexpr int kNumOptions = sizeof(kOptions) / sizeof(kOptions[0]);
+constexpr int kHelpCode = 'h';
+constexpr int kFirstCode = 0x200; /* getopt return value of option i: kFirstCode + i */
+
 void usage(const char *prog) {
     fprintf(stderr, "Usage: %s [OPTIONS] <mps_file> <output_dir>\n\n", prog);
-    fprintf(stderr, "Arguments:\n");
-    fprintf(stderr, "  <mps_file>               Path to the input problem in MPS format (.mps or .mps.gz).\n");
-    fprintf(stderr, "  <output_dir>             Directory where output files will be saved. It will contain:\n");
-    fprintf(stderr, "                             - <basename>_summary.txt\n");
-    fprintf(stderr, "                             - <basename>_primal_solution.txt\n");
-    fprintf(stderr, "                             - <basename>_dual_solution.txt\n\n");
-    fprintf(stderr, "Options:\n");
-    fprintf(stderr, "  -h, --help                          Display this help message.\n");
-    fprintf(stderr, "  -v, --verbose                       Enable verbose logging (default: false).\n");
-    fprintf(stderr, "      --time_limit <seconds>          Time limit in seconds (default: 3600.0).\n");
-    fprintf(stderr, "      --iter_limit <iterations>       Iteration limit (default: %d).\n", INT32_MAX);
-    fprintf(stderr, "      --eps_opt <tolerance>           Relative optimality tolerance (default: 1e-4).\n");
-    fprintf(stderr, "      --eps_feas <tolerance>          Relative feasibility tolerance (default: 1e-4).\n");
-    fprintf(stderr, "      --l_inf_ruiz_iter <int>         Iterations for L-inf Ruiz rescaling (default: 10).\n");
-    fprintf(stderr, "      --no_pock_chambolle             Disable Pock-Chambolle rescaling (default: enabled).\n");
-    fprintf(stderr, "      --pock_chambolle_alpha <float>  Value for Pock-Chambolle alpha (default: 1.0).\n");
-    fprintf(stderr, "      --no_bound_obj_rescaling        Disable bound objective rescaling (default: enabled).\n");
-    fprintf(stderr, "      --eval_freq <int>               Termination evaluation frequency (default: 200).\n");
-    fprintf(stderr, "      --sv_max_iter <int>             Max iterations for singular value estimation "
-                    "(default: 5000).\n");
-    fprintf(stderr, "      --sv_tol <float>                Tolerance for singular value estimation (default: 1e-4).\n");
-    fprintf(stderr, "  -f  --feasibility_polishing         Enable feasibility use feasibility polishing "
-                    "(default: false).\n");
-    fprintf(stderr, "      --eps_feas_polish <tolerance>   Relative feasibility polish tolerance (default: 1e-6).\n");
-    fprintf(stderr, "      --opt_norm <norm_type>          Norm for optimality criteria: l2 or linf (default: l2).\n");
-    fprintf(stderr, "      --no_presolve                   Disable presolve (presolve is not built; accepted).\n");
-    fprintf(stderr, "      --matrix_zero_tol <tolerance>.  Zero tolerance in constraint matrix.\n");
+    fprintf(stderr, "Solves the linear program in <mps_file> (MPS text, optionally gzip-compressed) on the GPU\n");
+    fprintf(stderr, "and writes into <output_dir>, for an input named NAME.mps:\n");
+    fprintf(stderr, "  NAME_summary.txt          status, iterations, objectives, residuals, times\n");
+    fprintf(stderr, "  NAME_primal_solution.txt  one value of x per line\n");
+    fprintf(stderr, "  NAME_dual_solution.txt    one value of y per line\n\n");
+    fprintf(stderr, "Options (defaults in parentheses):\n");
+    fprintf(stderr, "  -h, --help  show this text\n");
+    for (const Option &o : kOptions) {
+        char head[64];
+        snprintf(head, sizeof head, "--%s%s%s", o.name, o.value ? " " : "", o.value ? o.value : "");
+        if (o.letter)
+            fprintf(stderr, "  -%c, %-34s %s\n", o.letter, head, o.help);
+        else
+            fprintf(stderr, "      %-34s %s\n", head, o.help);
+    }
+    fprintf(stderr, "\nCP_AL_* environment variables are read as the solver library reads them.\n");
 }
 
 } // namespace
@@ -137,58 +193,31 @@ int main(int argc, char *argv[]) {
     cp_al_parameters_t params;
     set_default_parameters(&params);
 
-    static struct option long_options[] = {{"help", no_argument, 0, 'h'},
-                                           {"verbose", no_argument, 0, 'v'},
-                                           {"time_limit", required_argument, 0, 1001},
-                                           {"iter_limit", required_argument, 0, 1002},
-                                           {"eps_opt", required_argument, 0, 1003},
-                                           {"eps_feas", required_argument, 0, 1004},
-                                           {"eps_feas_polish", required_argument, 0, 1006},
-                                           {"feasibility_polishing", no_argument, 0, 'f'},
-                                           {"l_inf_ruiz_iter", required_argument, 0, 1007},
-                                           {"pock_chambolle_alpha", required_argument, 0, 1008},
-                                           {"no_pock_chambolle", no_argument, 0, 1009},
-                                           {"no_bound_obj_rescaling", no_argument, 0, 1010},
-                                           {"sv_max_iter", required_argument, 0, 1011},
-                                           {"sv_tol", required_argument, 0, 1012},
-                                           {"eval_freq", required_argument, 0, 1013},
-                                           {"opt_norm", required_argument, 0, 1014},
-                                           {"no_presolve", no_argument, 0, 1015},
-                                           {"matrix_zero_tol", required_argument, 0, 1016},
-                                           {0, 0, 0, 0}};
+    struct option long_options[kNumOptions + 2];
+    std::string shorts = "h";
+    long_options[0] = {"help", no_argument, nullptr, kHelpCode};
+    for (int i = 0; i < kNumOptions; ++i) {
+        const Option &o = kOptions[i];
+        long_options[i + 1] = {o.name, o.value ? required_argument : no_argument, nullptr, kFirstCode + i};
+        if (o.letter) shorts += o.letter;
+    }
+    long_options[kNumOptions + 1] = {nullptr, 0, nullptr, 0};
+    shorts += "p"; /* accepted and ignored, as by the reference command */
     int opt;
-    while ((opt = getopt_long(argc, argv, "hvfp", long_options, nullptr)) != -1) {
-        switch (opt) {
-        case 'h': usage(argv[0]); return 0;
-        case 'v': params.verbose = true; break;
-        case 1001: params.termination_criteria.time_sec_limit = atof(optarg); break;
-        case 1002: params.termination_criteria.iteration_limit = atoi(optarg); break;
-        case 1003: params.termination_criteria.eps_optimal_relative = atof(optarg); break;
-        case 1004: params.termination_criteria.eps_feasible_relative = atof(optarg); break;
-        case 1006: params.termination_criteria.eps_feas_polish_relative = atof(optarg); break;
-        case 'f': params.feasibility_polishing = true; break;
-        case 1007: params.l_inf_ruiz_iterations = atoi(optarg); break;
-        case 1008: params.pock_chambolle_alpha = atof(optarg); break;
-        case 1009: params.has_pock_chambolle_alpha = false; break;
-        case 1010: params.bound_objective_rescaling = false; break;
-        case 1011: params.sv_max_iter = atoi(optarg); break;
-        case 1012: params.sv_tol = atof(optarg); break;
-        case 1013: params.termination_evaluation_frequency = atoi(optarg); break;
-        case 1014:
-            if (strcmp(optarg, "l2") == 0) {
-                params.optimality_norm = NORM_TYPE_L2;
-            } else if (strcmp(optarg, "linf") == 0) {
-                params.optimality_norm = NORM_TYPE_L_INF;
-            } else {
-                fprintf(stderr, "Error: opt_norm must be 'l2' or 'linf'\n");
-                return 1;
-            }
-            break;
-        case 1015: params.presolve = false; break;
-        case 1016: params.matrix_zero_tol = atof(optarg); break;
-        case '?': return 1;
-        default: break;
+    while ((opt = getopt_long(argc, argv, shorts.c_str(), long_options, nullptr)) != -1) {
+        if (opt == kHelpCode) {
+            usage(argv[0]);
+            return 0;
         }
+        if (opt == '?') return 1;
+        int idx = -1;
+        if (opt >= kFirstCode && opt < kFirstCode + kNumOptions) {
+            idx = opt - kFirstCode;
+        } else {
+            for (int i = 0; i < kNumOptions; ++i)
+                if (kOptions[i].letter && kOptions[i].letter == opt) idx = i;
+        }
+        if (idx >= 0 && !kOptions[idx].apply(params, optarg)) return 1;
     }
     if (argc - optind != 2) {
         fprintf(stderr, "Error: You must specify an input file and an output directory.\n\n");

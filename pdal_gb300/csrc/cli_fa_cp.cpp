@@ -137,57 +137,124 @@ void save_summary(const fa_cp_result_t *r, const char *dir, const std::string &n
     fclose(f);
 }
 
+/* One command-line option: long name, short letter (0 if none), value name
+ * in the help (nullptr for a switch), help line, and what it sets.  Names,
+ * meanings and defaults are the reference command's (QP/FA_CP/src/cli.c:
+ * 265-400), which scripts call by name; the table and the help wording are
+ * this command's own. */
+struct Option {
+    const char *name;
+    char letter;
+    const char *value;
+    const char *help;
+    bool (*apply)(fa_cp_parameters_t &, const char *); /* false: bad value, message printed */
+};
+
+using P = fa_cp_parameters_t;
+
+bool set_norm(P &p, const char *v) {
+    if (strcmp(v, "l2") == 0) {
+        p.optimality_norm = NORM_TYPE_L2;
+    } else if (strcmp(v, "linf") == 0) {
+        p.optimality_norm = NORM_TYPE_L_INF;
+    } else {
+        fprintf(stderr, "Error: opt_norm must be 'l2' or 'linf'\n");
+        return false;
+    }
+    return true;
+}
+
+bool set_rule(P &p, const char *v) {
+    if (parse_rule(v, &p.sigma_update_rule)) return true;
+    fprintf(stderr, "Error: sigma_update must be fixed, residual, kkt, displacement, progress, greedy, "
+                    "guarded, or balanced_guarded\n");
+    return false;
+}
+
+#define PDAL_DBL(field) [](P &p, const char *v) { return p.field = atof(v), true; }
+#define PDAL_INT(field) [](P &p, const char *v) { return p.field = atoi(v), true; }
+
+const Option kOptions[] = {
+    {"eps_opt", 0, "TOL", "stop when the relative duality gap is below TOL (1e-4)",
+     PDAL_DBL(termination_criteria.eps_optimal_relative)},
+    {"eps_feas", 0, "TOL", "and both relative residuals are below TOL (1e-4)",
+     PDAL_DBL(termination_criteria.eps_feasible_relative)},
+    {"opt_norm", 0, "l2|linf", "norm of the residuals in that test (linf)", set_norm},
+    {"eps_infeas_detect", 0, "TOL", "tolerance of the infeasibility certificates (1e-10)",
+     PDAL_DBL(termination_criteria.eps_infeasible)},
+    {"iter_limit", 0, "N", "give up after N iterations (no limit)", PDAL_INT(termination_criteria.iteration_limit)},
+    {"time_limit", 0, "SEC", "give up after SEC seconds of wall time (3600)",
+     PDAL_DBL(termination_criteria.time_sec_limit)},
+    {"eval_freq", 0, "N", "iterations between two evaluations of the stopping test (200)",
+     PDAL_INT(termination_evaluation_frequency)},
+    {"l_inf_ruiz_iter", 0, "N", "passes of Ruiz max-norm equilibration (10)", PDAL_INT(l_inf_ruiz_iterations)},
+    {"pock_chambolle_alpha", 0, "A", "exponent of the Pock-Chambolle scaling pass (1.0)",
+     PDAL_DBL(pock_chambolle_alpha)},
+    {"no_pock_chambolle", 0, nullptr, "skip the Pock-Chambolle scaling pass",
+     [](P &p, const char *) { return p.has_pock_chambolle_alpha = false, true; }},
+    {"no_bound_obj_rescaling", 0, nullptr, "skip the scaling of bounds and objective",
+     [](P &p, const char *) { return p.bound_objective_rescaling = false, true; }},
+    {"sv_max_iter", 0, "N", "cap on power-iteration steps for the largest singular value (5000)",
+     PDAL_INT(sv_max_iter)},
+    {"sv_tol", 0, "TOL", "power-iteration stopping tolerance (1e-4)", PDAL_DBL(sv_tol)},
+    {"no_al_qp", 0, nullptr, "use the plain (non-augmented) primal-dual update",
+     [](P &p, const char *) { return p.use_al_qp = false, true; }},
+    {"al_sigma", 0, "S", "initial augmentation weight sigma of the primal subproblem (0)", PDAL_DBL(al_sigma)},
+    {"sigma_update", 0, "RULE",
+     "how sigma changes at restarts: fixed, residual, kkt, displacement, progress, greedy, guarded or "
+     "balanced_guarded (guarded)",
+     set_rule},
+    {"sigma_update_gain", 0, "G", "damping of each sigma change, in the log domain (0.5)",
+     PDAL_DBL(sigma_update_gain)},
+    {"sigma_clip_low", 0, "F", "smallest factor one restart may apply to sigma (0.6)", PDAL_DBL(sigma_clip_low)},
+    {"sigma_clip_high", 0, "F", "largest factor one restart may apply to sigma (1.7)", PDAL_DBL(sigma_clip_high)},
+    {"sigma_min", 0, "S", "floor of a positive adaptive sigma (1e-8)", PDAL_DBL(sigma_min)},
+    {"sigma_max", 0, "S", "ceiling of an adaptive sigma (10)", PDAL_DBL(sigma_max)},
+    {"sigma_rollback_tol", 0, "F",
+     "return to the best sigma seen when the restart score grows by more than F (1.25; <= 0: never)",
+     PDAL_DBL(sigma_rollback_tol)},
+    {"sigma_zero_threshold", 0, "S", "a guarded sigma below S becomes exactly 0 (1e-8)",
+     PDAL_DBL(sigma_zero_threshold)},
+    {"sigma_activation_threshold", 0, "R",
+     "primal residual over the larger of dual residual and gap that switches guarded sigma on (2)",
+     PDAL_DBL(sigma_activation_threshold)},
+    {"sigma_normal_motion_threshold", 0, "R", "smallest |A dx| / |dx| that lets guarded sigma switch on (1e-10)",
+     PDAL_DBL(sigma_normal_motion_threshold)},
+    {"sigma_activation_value", 0, "S",
+     "sigma a guarded rule starts from when it switches on; theta of sigma = theta * dual step for "
+     "balanced_guarded (0.1)",
+     PDAL_DBL(sigma_activation_value)},
+    {"feasibility_polishing", 'f', nullptr, "polishing phases after the solve (not built: a warning)",
+     [](P &p, const char *) { return p.feasibility_polishing = true, true; }},
+    {"eps_feas_polish", 0, "TOL", "residual target of the polishing phases (1e-6)",
+     PDAL_DBL(termination_criteria.eps_feas_polish_relative)},
+    {"trajectory_csv", 0, "PATH", "append one CSV line per evaluation to PATH",
+     [](P &p, const char *v) { return p.trajectory_csv = v, true; }},
+    {"verbose", 'v', "LEVEL", "0 silent, 1 summary, 2 every evaluation (1)", PDAL_INT(verbose)},
+};
+#undef PDAL_DBL
+#undef PDAL_INT
+constexpr int kNumOptions = sizeof(kOptions) / sizeof(kOptions[0]);
+constexpr int kHelpCode = 'h';
+constexpr int kFirstCode = 0x200; /* getopt return value of option i: kFirstCode + i */
+
 void usage(const char *prog) {
     fprintf(stderr, "Usage: %s [OPTIONS] <mps_file> <output_dir>\n\n", prog);
-    fprintf(stderr, "Arguments:\n");
-    fprintf(stderr, "  <mps_file>               Path to the input problem in MPS format (.mps .QPS or .mps.gz).\n");
-    fprintf(stderr, "  <output_dir>             Directory where output files will be saved. It will contain:\n");
-    fprintf(stderr, "                             - <basename>_summary.txt\n");
-    fprintf(stderr, "                             - <basename>_primal_solution.txt\n");
-    fprintf(stderr, "                             - <basename>_dual_solution.txt\n\n");
-    fprintf(stderr, "Options:\n");
-    fprintf(stderr, "  -h, --help                          Display this help message.\n");
-    fprintf(stderr, "  -v, --verbose <int>                 Verbosity level: 0=silent, 1=summary, 2=detailed "
-                    "(default: 1).\n");
-    fprintf(stderr, "      --time_limit <seconds>          Time limit in seconds (default: 3600.0).\n");
-    fprintf(stderr, "      --iter_limit <iterations>       Iteration limit (default: %d).\n", INT32_MAX);
-    fprintf(stderr, "      --eps_opt <tolerance>           Relative optimality tolerance (default: 1e-4).\n");
-    fprintf(stderr, "      --eps_feas <tolerance>          Relative feasibility tolerance (default: 1e-4).\n");
-    fprintf(stderr, "      --eps_infeas_detect <tolerance> Infeasibility detection tolerance (default: 1e-10).\n");
-    fprintf(stderr, "      --l_inf_ruiz_iter <int>         Iterations for L-inf Ruiz rescaling (default: 10).\n");
-    fprintf(stderr, "      --no_pock_chambolle             Disable Pock-Chambolle rescaling (default: enabled).\n");
-    fprintf(stderr, "      --pock_chambolle_alpha <float>  Value for Pock-Chambolle alpha (default: 1.0).\n");
-    fprintf(stderr, "      --no_bound_obj_rescaling        Disable bound objective rescaling (default: enabled).\n");
-    fprintf(stderr, "      --no_al_qp                      Disable the AL primal-dual update and use the "
-                    "non-augmented baseline branch.\n");
-    fprintf(stderr, "      --al_sigma <float>              AL penalty parameter used in the full AL primal "
-                    "subproblem (default: 0).\n");
-    fprintf(stderr, "      --sigma_update <rule>           Restart-only sigma rule: fixed, residual, kkt, "
-                    "displacement, progress, greedy, guarded, or balanced_guarded (default: guarded).\n");
-    fprintf(stderr, "      --sigma_update_gain <float>     Log-domain damping gain for sigma updates "
-                    "(default: 0.5).\n");
-    fprintf(stderr, "      --sigma_clip_low <float>        Lower per-restart multiplicative clip (default: 0.6).\n");
-    fprintf(stderr, "      --sigma_clip_high <float>       Upper per-restart multiplicative clip (default: 1.7).\n");
-    fprintf(stderr, "      --sigma_min <float>             Minimum positive sigma for adaptive rules "
-                    "(default: 1e-8).\n");
-    fprintf(stderr, "      --sigma_max <float>             Maximum sigma for adaptive rules (default: 10).\n");
-    fprintf(stderr, "      --sigma_rollback_tol <float>    Rollback to the best sigma if restart score worsens by "
-                    "this factor (default: 1.25; nonpositive disables rollback).\n");
-    fprintf(stderr, "      --sigma_zero_threshold <float>  Set guarded sigma to exactly zero below this value "
-                    "(default: 1e-8).\n");
-    fprintf(stderr, "      --sigma_activation_threshold <float> Primal bottleneck ratio needed to activate guarded "
-                    "sigma (default: 2).\n");
-    fprintf(stderr, "      --sigma_normal_motion_threshold <float> Minimum ||A dx||/||dx|| for guarded activation "
-                    "(default: 1e-10).\n");
-    fprintf(stderr, "      --sigma_activation_value <float> Positive sigma used when guarded mode activates from "
-                    "zero; for balanced_guarded this is theta in sigma = theta * dual_step (default: 0.1).\n");
-    fprintf(stderr, "      --eval_freq <int>               Termination evaluation frequency (default: 200).\n");
-    fprintf(stderr, "      --trajectory_csv <path>         Write iteration trajectory CSV for plotting.\n");
-    fprintf(stderr, "      --sv_max_iter <int>             Max iterations for singular value estimation "
-                    "(default: 5000).\n");
-    fprintf(stderr, "      --sv_tol <float>                Tolerance for singular value estimation (default: 1e-4).\n");
-    fprintf(stderr, "      --opt_norm <norm_type>          Norm for optimality criteria: l2 or linf "
-                    "(default: linf).\n");
+    fprintf(stderr, "Solves the convex quadratic program in <mps_file> (MPS or QPS text, optionally\n");
+    fprintf(stderr, "gzip-compressed) on the GPU and writes into <output_dir>, for an input NAME.qps:\n");
+    fprintf(stderr, "  NAME_summary.txt          status, iterations, objectives, residuals, sigma, times\n");
+    fprintf(stderr, "  NAME_primal_solution.txt  one value of x per line\n");
+    fprintf(stderr, "  NAME_dual_solution.txt    one value of y per line\n\n");
+    fprintf(stderr, "Options (defaults in parentheses):\n");
+    fprintf(stderr, "  -h, --help  show this text\n");
+    for (const Option &o : kOptions) {
+        char head[64];
+        snprintf(head, sizeof head, "--%s%s%s", o.name, o.value ? " " : "", o.value ? o.value : "");
+        if (o.letter)
+            fprintf(stderr, "  -%c, %-38s %s\n", o.letter, head, o.help);
+        else
+            fprintf(stderr, "      %-38s %s\n", head, o.help);
+    }
 }
 
 } // namespace
@@ -196,90 +263,34 @@ int main(int argc, char *argv[]) {
     fa_cp_parameters_t params;
     set_default_parameters(&params);
 
-    static struct option long_options[] = {{"help", no_argument, 0, 'h'},
-                                           {"verbose", required_argument, 0, 'v'},
-                                           {"time_limit", required_argument, 0, 1001},
-                                           {"iter_limit", required_argument, 0, 1002},
-                                           {"eps_opt", required_argument, 0, 1003},
-                                           {"eps_feas", required_argument, 0, 1004},
-                                           {"eps_infeas_detect", required_argument, 0, 1005},
-                                           {"eps_feas_polish", required_argument, 0, 1006},
-                                           {"feasibility_polishing", no_argument, 0, 'f'},
-                                           {"l_inf_ruiz_iter", required_argument, 0, 1007},
-                                           {"pock_chambolle_alpha", required_argument, 0, 1008},
-                                           {"no_pock_chambolle", no_argument, 0, 1009},
-                                           {"no_bound_obj_rescaling", no_argument, 0, 1010},
-                                           {"sv_max_iter", required_argument, 0, 1011},
-                                           {"sv_tol", required_argument, 0, 1012},
-                                           {"eval_freq", required_argument, 0, 1013},
-                                           {"opt_norm", required_argument, 0, 1014},
-                                           {"no_al_qp", no_argument, 0, 1015},
-                                           {"al_sigma", required_argument, 0, 1016},
-                                           {"trajectory_csv", required_argument, 0, 1017},
-                                           {"sigma_update", required_argument, 0, 1018},
-                                           {"sigma_update_gain", required_argument, 0, 1019},
-                                           {"sigma_clip_low", required_argument, 0, 1020},
-                                           {"sigma_clip_high", required_argument, 0, 1021},
-                                           {"sigma_min", required_argument, 0, 1022},
-                                           {"sigma_max", required_argument, 0, 1023},
-                                           {"sigma_rollback_tol", required_argument, 0, 1024},
-                                           {"sigma_zero_threshold", required_argument, 0, 1025},
-                                           {"sigma_activation_threshold", required_argument, 0, 1026},
-                                           {"sigma_normal_motion_threshold", required_argument, 0, 1027},
-                                           {"sigma_activation_value", required_argument, 0, 1028},
-                                           {0, 0, 0, 0}};
-    int opt;
-    while ((opt = getopt_long(argc, argv, "hv:fp", long_options, nullptr)) != -1) {
-        switch (opt) {
-        case 'h': usage(argv[0]); return 0;
-        case 'v': params.verbose = atoi(optarg); break;
-        case 1001: params.termination_criteria.time_sec_limit = atof(optarg); break;
-        case 1002: params.termination_criteria.iteration_limit = atoi(optarg); break;
-        case 1003: params.termination_criteria.eps_optimal_relative = atof(optarg); break;
-        case 1004: params.termination_criteria.eps_feasible_relative = atof(optarg); break;
-        case 1005: params.termination_criteria.eps_infeasible = atof(optarg); break;
-        case 1006: params.termination_criteria.eps_feas_polish_relative = atof(optarg); break;
-        case 'f': params.feasibility_polishing = true; break;
-        case 1007: params.l_inf_ruiz_iterations = atoi(optarg); break;
-        case 1008: params.pock_chambolle_alpha = atof(optarg); break;
-        case 1009: params.has_pock_chambolle_alpha = false; break;
-        case 1010: params.bound_objective_rescaling = false; break;
-        case 1011: params.sv_max_iter = atoi(optarg); break;
-        case 1012: params.sv_tol = atof(optarg); break;
-        case 1013: params.termination_evaluation_frequency = atoi(optarg); break;
-        case 1014:
-            if (strcmp(optarg, "l2") == 0) {
-                params.optimality_norm = NORM_TYPE_L2;
-            } else if (strcmp(optarg, "linf") == 0) {
-                params.optimality_norm = NORM_TYPE_L_INF;
-            } else {
-                fprintf(stderr, "Error: opt_norm must be 'l2' or 'linf'\n");
-                return 1;
-            }
-            break;
-        case 1015: params.use_al_qp = false; break;
-        case 1016: params.al_sigma = atof(optarg); break;
-        case 1017: params.trajectory_csv = optarg; break;
-        case 1018:
-            if (!parse_rule(optarg, &params.sigma_update_rule)) {
-                fprintf(stderr, "Error: sigma_update must be fixed, residual, kkt, displacement, progress, greedy, "
-                                "guarded, or balanced_guarded\n");
-                return 1;
-            }
-            break;
-        case 1019: params.sigma_update_gain = atof(optarg); break;
-        case 1020: params.sigma_clip_low = atof(optarg); break;
-        case 1021: params.sigma_clip_high = atof(optarg); break;
-        case 1022: params.sigma_min = atof(optarg); break;
-        case 1023: params.sigma_max = atof(optarg); break;
-        case 1024: params.sigma_rollback_tol = atof(optarg); break;
-        case 1025: params.sigma_zero_threshold = atof(optarg); break;
-        case 1026: params.sigma_activation_threshold = atof(optarg); break;
-        case 1027: params.sigma_normal_motion_threshold = atof(optarg); break;
-        case 1028: params.sigma_activation_value = atof(optarg); break;
-        case '?': return 1;
-        default: break;
+    struct option long_options[kNumOptions + 2];
+    std::string shorts = "h";
+    long_options[0] = {"help", no_argument, nullptr, kHelpCode};
+    for (int i = 0; i < kNumOptions; ++i) {
+        const Option &o = kOptions[i];
+        long_options[i + 1] = {o.name, o.value ? required_argument : no_argument, nullptr, kFirstCode + i};
+        if (o.letter) {
+            shorts += o.letter;
+            if (o.value) shorts += ':';
         }
+    }
+    long_options[kNumOptions + 1] = {nullptr, 0, nullptr, 0};
+    shorts += "p"; /* accepted and ignored, as by the reference command */
+    int opt;
+    while ((opt = getopt_long(argc, argv, shorts.c_str(), long_options, nullptr)) != -1) {
+        if (opt == kHelpCode) {
+            usage(argv[0]);
+            return 0;
+        }
+        if (opt == '?') return 1;
+        int idx = -1;
+        if (opt >= kFirstCode && opt < kFirstCode + kNumOptions) {
+            idx = opt - kFirstCode;
+        } else {
+            for (int i = 0; i < kNumOptions; ++i)
+                if (kOptions[i].letter && kOptions[i].letter == opt) idx = i;
+        }
+        if (idx >= 0 && !kOptions[idx].apply(params, optarg)) return 1;
     }
     if (argc - optind != 2) {
         fprintf(stderr, "Error: You must specify an input file and an output directory.\n\n");

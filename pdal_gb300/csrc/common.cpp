@@ -162,6 +162,98 @@ HostPlan plan_rows(int nr, const int *rp, int S) {
     return P;
 }
 
+HostPlan plan_short_rows(int nr, const int *rp, int S) {
+    HostPlan P;
+    P.S = S;
+    int r = 0;
+    while (r < nr) {
+        if (rp[r + 1] - rp[r] > S) {
+            ++r;
+            continue;
+        }
+        const int r0 = r;
+        int k = 0;
+        while (r < nr && (r - r0) < kMaxRowsPerBlock) {
+            const int l = rp[r + 1] - rp[r];
+            if (l > S || k + l > S) break;
+            k += l;
+            ++r;
+        }
+        P.desc.insert(P.desc.end(), {r0, r, rp[r0], rp[r]});
+    }
+    P.nblocks = (int)(P.desc.size() / 4);
+    return P;
+}
+
+HostPanels plan_panels(int nr, int nc, const int *rp, const int *ci, int S, int W, int target_blocks) {
+    HostPanels Q;
+    Q.W = W;
+    Q.P = nc > 0 ? (nc + W - 1) / W : 0;
+    for (int r = 0; r < nr; ++r)
+        if (rp[r + 1] - rp[r] > S) {
+            Q.rows.push_back(r);
+            Q.long_nnz += rp[r + 1] - rp[r];
+        }
+    Q.H = (int)Q.rows.size();
+    const int H = Q.H, P = Q.P;
+    if (H == 0 || P == 0) return Q;
+    /* entries of long row h in panel p, then padded segment starts: panel
+     * major, rows in order within a panel */
+    std::vector<int> cnt((size_t)H * P, 0);
+    const int nt = host_threads(Q.long_nnz);
+    parallel_for(nt, [&](int t) {
+        for (int h = t; h < H; h += nt) {
+            const int r = Q.rows[h];
+            int *c = cnt.data() + (size_t)h * P;
+            for (int k = rp[r]; k < rp[r + 1]; ++k) c[ci[k] / W]++;
+        }
+    });
+    std::vector<long long> start((size_t)H * P, 0);
+    long long pos = 0;
+    for (int p = 0; p < P; ++p)
+        for (int h = 0; h < H; ++h) {
+            const int c = cnt[(size_t)h * P + p];
+            start[(size_t)h * P + p] = pos;
+            if (c > 0) {
+                Q.seg.insert(Q.seg.end(), {h, (int)pos, (int)(pos + ((c + 3) & ~3)), p});
+                pos += (c + 3) & ~3;
+            }
+        }
+    if (pos > (long long)INT32_MAX - 16) throw Error("long rows too large for the panel plan");
+    Q.len = pos;
+    Q.pmap.assign((size_t)pos, -1);
+    Q.off.assign((size_t)pos, 0);
+    parallel_for(nt, [&](int t) {
+        std::vector<long long> at((size_t)P);
+        for (int h = t; h < H; h += nt) {
+            const int r = Q.rows[h];
+            for (int p = 0; p < P; ++p) at[p] = start[(size_t)h * P + p];
+            for (int k = rp[r]; k < rp[r + 1]; ++k) {
+                const int p = ci[k] / W;
+                const long long q = at[p]++;
+                Q.pmap[(size_t)q] = k;
+                Q.off[(size_t)q] = (uint16_t)(ci[k] - p * W);
+            }
+        }
+    });
+    /* blocks: each panel's segments cut into chunks of about target
+     * nonzeros, chunk borders on segment borders */
+    const long long target = std::max<long long>(1024, Q.long_nnz / std::max(1, target_blocks));
+    const int nseg = (int)(Q.seg.size() / 4);
+    int s = 0;
+    while (s < nseg) {
+        const int p = Q.seg[4 * s + 3];
+        const int s0 = s;
+        long long acc = 0;
+        while (s < nseg && Q.seg[4 * s + 3] == p && (s == s0 || acc + (Q.seg[4 * s + 2] - Q.seg[4 * s + 1]) <= target)) {
+            acc += Q.seg[4 * s + 2] - Q.seg[4 * s + 1];
+            ++s;
+        }
+        Q.cta.insert(Q.cta.end(), {p, s0, s, 0});
+    }
+    return Q;
+}
+
 int auto_block_nnz(long long nnz, int nr) {
     (void)nr;
     const long long target_blocks = 2 * 152;

@@ -111,6 +111,36 @@ struct HostPlan {
 };
 HostPlan plan_rows(int nr, const int *rp, int S);
 
+/* Row-block plan of the rows of at most S nonzeros only: rows longer than S
+ * are left out (the column-panel plan below takes them). */
+HostPlan plan_short_rows(int nr, const int *rp, int S);
+
+/*
+ * Column-panel plan of the long rows (more than S nonzeros) of a CSR matrix,
+ * for the dual product A x of a matrix whose long rows hold much of its
+ * nonzeros (the power-law rows of the large LP).  The columns are cut into
+ * panels of W; a CUDA block stages one panel of x in shared memory, so the
+ * long rows' random gathers become shared-memory reads, and reduces the
+ * segments (one long row restricted to the panel) of a contiguous chunk.
+ * The long rows' nonzeros are stored again in panel order, each segment
+ * padded with zeros to a multiple of 4 entries (128-bit loads), with the
+ * column as a 16-bit offset in its panel (W <= 65536).  Segment (h, p) --
+ * long row h, panel p -- writes partial sum h * P + p; a row's total is the
+ * sum of its P partials in panel order (zeros where the row has no entry in
+ * a panel), so the result is deterministic.
+ */
+struct HostPanels {
+    int W = 0, P = 0, H = 0;
+    std::vector<int> rows;      /* H long rows (ascending) */
+    std::vector<int> pmap;      /* panel-array position -> CSR position, -1 for padding */
+    std::vector<uint16_t> off;  /* column - p * W */
+    std::vector<int> seg;       /* 4 ints per segment: {h, k0, k1, p} (k0, k1 multiples of 4) */
+    std::vector<int> cta;       /* 4 ints per block: {p, first segment, end segment, 0} */
+    long long long_nnz = 0;
+    long long len = 0;          /* panel-array length, padding included */
+};
+HostPanels plan_panels(int nr, int nc, const int *rp, const int *ci, int S, int W, int target_blocks);
+
 /* Nonzero budget per block for a matrix of `nnz` nonzeros when none is
  * requested: enough blocks to cover the 152 SMs twice, at most 2048. */
 int auto_block_nnz(long long nnz, int nr);

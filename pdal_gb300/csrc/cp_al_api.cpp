@@ -349,6 +349,8 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->graph_blocks = 1;
     o->timing = 0;
     o->fp32_stall_evals = 25;
+    o->dual_panels = 0;
+    o->panel_width = 0;
 }
 
 /* Each variable is read the way the reference reads it

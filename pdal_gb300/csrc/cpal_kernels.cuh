@@ -30,6 +30,8 @@
 #include "cpal_control.h"
 #include "rowblock.cuh"
 
+#include <type_traits>
+
 namespace pdal {
 
 template <typename T>
@@ -235,6 +237,113 @@ __global__ void __launch_bounds__(kThreads) k_dual(RowPlanDev plan, const int *_
     auto g = [&](int c, T *out) { out[0] = __ldcg(xbar + c); };
     Red<0, 0> red;
     rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);
+}
+
+/* ------------------------------------------------------------------ */
+/* the long rows of the dual product, by column panels                 */
+/* ------------------------------------------------------------------ */
+/* Device side of HostPanels (common.h): the long rows' nonzeros in panel
+ * order (values in the iteration's type, 16-bit column offsets), the
+ * segments {h, k0, k1, p}, the blocks {p, first segment, end segment} and
+ * one partial sum per (long row, panel). */
+template <typename T>
+struct PanelDev {
+    const int *__restrict__ rows;
+    const int4 *__restrict__ seg;
+    const int4 *__restrict__ cta;
+    const T *__restrict__ val;
+    const uint16_t *__restrict__ off;
+    T *part;
+    int H, P, W, nblocks;
+};
+
+constexpr int kPanelThreads = 512;
+
+/* panel values from the CSR values (after equilibration, in each precision) */
+template <typename T>
+__global__ void k_panel_gather(const int *__restrict__ pmap, const double *__restrict__ src, T *dst, long long len) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+        const int k = pmap[i];
+        dst[i] = k >= 0 ? (T)src[k] : T(0);
+    }
+}
+
+__device__ __forceinline__ void load4_stream(const uint16_t *p, int (&c)[4]) {
+    const uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
+    c[0] = (int)(t.x & 0xffffu);
+    c[1] = (int)(t.x >> 16);
+    c[2] = (int)(t.y & 0xffffu);
+    c[3] = (int)(t.y >> 16);
+}
+
+/* One block per chunk of one panel: stage x-bar[pW, pW + W) in shared
+ * memory, then one warp per segment -- four nonzeros per lane per step with
+ * 128-bit streaming loads, the gathers from shared memory -- and a warp sum
+ * into the segment's partial slot. */
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads) k_dual_panels(PanelDev<T> pd, const T *__restrict__ xbar, int n,
+                                                               const CpalState *__restrict__ st) {
+    pdl_enter();
+    if (st->status) return;
+    extern __shared__ __align__(16) unsigned char panel_smem[];
+    T *sx = reinterpret_cast<T *>(panel_smem);
+    const int4 c = pd.cta[blockIdx.x];
+    const int col0 = c.x * pd.W;
+    const int wlen = min(pd.W, n - col0);
+    /* x-bar starts 256-byte aligned and W is a multiple of 4, so the panel
+     * starts on a 16-byte boundary */
+    constexpr int V = 16 / sizeof(T);
+    const int nvec = wlen / V;
+    using Vec = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    const Vec *src = reinterpret_cast<const Vec *>(xbar + col0);
+    Vec *dst = reinterpret_cast<Vec *>(sx);
+    for (int i = threadIdx.x; i < nvec; i += kPanelThreads) dst[i] = __ldcg(src + i);
+    for (int i = nvec * V + threadIdx.x; i < wlen; i += kPanelThreads) sx[i] = __ldcg(xbar + col0 + i);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NW = kPanelThreads / 32;
+    for (int s = c.y + warp; s < c.z; s += NW) {
+        const int4 sg = pd.seg[s];
+        T acc = T(0);
+        for (int k = sg.y + 4 * lane; k < sg.z; k += 128) {
+            T v[4];
+            int o[4];
+            load4_stream(pd.val + k, v);
+            load4_stream(pd.off + k, o);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc = vfma(v[q], sx[o[q]], acc);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) pd.part[(size_t)sg.x * pd.P + sg.w] = acc;
+    }
+}
+
+/* One warp per long row: the row's panel partials summed in FP64 in a fixed
+ * order, then the dual epilogue of k_dual. */
+template <typename T, bool MAJOR, bool BETA>
+__global__ void __launch_bounds__(kThreads) k_dual_long_finish(PanelDev<T> pd, DualArgs<T> a,
+                                                                const CpalState *__restrict__ st,
+                                                                const typename WeightT<T>::type *__restrict__ wt,
+                                                                int koff) {
+    pdl_enter();
+    if (st->status) return;
+    const int h = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (h >= pd.H) return;
+    double s = 0.0;
+    for (int p = lane; p < pd.P; p += 32) s += (double)pd.part[(size_t)h * pd.P + p];
+    s = warp_sum(s);
+    if (lane == 0) {
+        DualEpi<T, MAJOR, BETA> epi;
+        epi.a = a;
+        load_coefs(st, epi.k);
+        epi.w = wt[koff].w;
+        epi.omw = wt[koff].omw;
+        const T sum[1] = {(T)s};
+        Red<0, 0> red;
+        epi(pd.rows[h], sum, red);
+    }
 }
 
 /* Halpern weights for the block starting at st->inner (one block). */

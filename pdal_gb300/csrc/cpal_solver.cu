@@ -186,6 +186,26 @@ class CpalSolver {
     Arena arena_;
     cudaStream_t stream_ = nullptr;
     DevMatrix A_, At_;
+    /* the long rows of the iteration's A x by column panels (HostPanels in
+     * common.h); the iteration's row blocks then cover the other rows */
+    bool use_panels_ = false;
+    HostPanels pan_host_;
+    PlanDev a_short_;
+    int *pan_rows_ = nullptr, *pan_pmap_ = nullptr;
+    int4 *pan_seg_ = nullptr, *pan_cta_ = nullptr;
+    uint16_t *pan_off_ = nullptr;
+    double *pan_v64_ = nullptr, *pan_part64_ = nullptr;
+    float *pan_v32_ = nullptr, *pan_part32_ = nullptr;
+    template <typename T>
+    PanelDev<T> panel_dev() const;
+    /* kernels one iteration launches */
+    int iter_launches() const { return 1 + (m_ == 0 ? 0 : use_panels_ ? (a_short_.hp.nblocks > 0 ? 3 : 2) : 1); }
+
+  public:
+    int panel_rows() const { return use_panels_ ? pan_host_.H : 0; }
+    int panels() const { return use_panels_ ? pan_host_.P : 0; }
+
+  private:
     /* pristine copies (session solves start from these) */
     double *Av0_ = nullptr, *Atv0_ = nullptr, *c0_ = nullptr, *vlb0_ = nullptr, *vub0_ = nullptr, *clb0_ = nullptr,
            *cub0_ = nullptr, *x00_ = nullptr, *y00_ = nullptr;
@@ -217,6 +237,17 @@ IterVecs<double> &CpalSolver::vecs<double>() {
 template <>
 IterVecs<float> &CpalSolver::vecs<float>() {
     return v32_;
+}
+
+template <>
+PanelDev<double> CpalSolver::panel_dev<double>() const {
+    return PanelDev<double>{pan_rows_, pan_seg_, pan_cta_, pan_v64_, pan_off_, pan_part64_,
+                            pan_host_.H, pan_host_.P, pan_host_.W, (int)(pan_host_.cta.size() / 4)};
+}
+template <>
+PanelDev<float> CpalSolver::panel_dev<float>() const {
+    return PanelDev<float>{pan_rows_, pan_seg_, pan_cta_, pan_v32_, pan_off_, pan_part32_,
+                           pan_host_.H, pan_host_.P, pan_host_.W, (int)(pan_host_.cta.size() / 4)};
 }
 
 void CpalSolver::release() {
@@ -371,6 +402,21 @@ void CpalSolver::alloc_all() {
     alloc_plan(At_.it);
     alloc_plan(A_.ev);
     alloc_plan(At_.ev);
+    if (use_panels_) {
+        const size_t len = (size_t)pan_host_.len, hp = (size_t)pan_host_.H * pan_host_.P;
+        alloc_plan(a_short_);
+        pan_rows_ = arena_.take<int>(pan_host_.rows.size());
+        pan_pmap_ = arena_.take<int>(len);
+        pan_seg_ = arena_.take<int4>(pan_host_.seg.size() / 4);
+        pan_cta_ = arena_.take<int4>(pan_host_.cta.size() / 4);
+        pan_off_ = arena_.take<uint16_t>(len);
+        pan_v64_ = arena_.take<double>(len);
+        pan_part64_ = arena_.take<double>(hp);
+        if (fp32_phase_) {
+            pan_v32_ = arena_.take<float>(len);
+            pan_part32_ = arena_.take<float>(hp);
+        }
+    }
     c0_ = arena_.take<double>(n);
     vlb0_ = arena_.take<double>(n);
     vub0_ = arena_.take<double>(n);
@@ -463,6 +509,23 @@ void CpalSolver::upload() {
     At_.it.hp = plan_rows(n_, At_host_.rp.data(), S_it_);
     A_.ev.hp = plan_rows(m_, prob_->constraint_matrix_row_pointers, S_ev_);
     At_.ev.hp = plan_rows(n_, At_host_.rp.data(), S_ev_);
+    use_panels_ = false;
+    if (m_ > 0 && O_.dual_panels != 0 && A_.it.hp.nlong > 0) {
+        const int *rp = prob_->constraint_matrix_row_pointers;
+        long long long_nnz = 0;
+        for (int q = 0; q < A_.it.hp.nlong; ++q) {
+            const int r = A_.it.hp.linfo[4 * q];
+            long_nnz += rp[r + 1] - rp[r];
+        }
+        if (O_.dual_panels == 1 || long_nnz >= (1ll << 20)) {
+            const int W = O_.panel_width > 0 ? O_.panel_width : 16384;
+            if (W % 4 != 0 || W > 65536) throw Error("panel_width must be a multiple of 4 up to 65536");
+            /* about three panel blocks per SM (64 KB of FP32 x-bar each) */
+            pan_host_ = plan_panels(m_, n_, rp, prob_->constraint_matrix_col_indices, S_it_, W, 3 * 152);
+            a_short_.hp = plan_short_rows(m_, rp, S_it_);
+            use_panels_ = pan_host_.H > 0;
+        }
+    }
     arena_.begin_measure();
     alloc_all();
     arena_.reserve_measured();
@@ -484,6 +547,18 @@ void CpalSolver::upload() {
     upload_plan(At_.it);
     upload_plan(A_.ev);
     upload_plan(At_.ev);
+    if (use_panels_) {
+        const size_t len = (size_t)pan_host_.len, hp = (size_t)pan_host_.H * pan_host_.P;
+        upload_plan(a_short_);
+        up(pan_rows_, pan_host_.rows.data(), pan_host_.rows.size() * sizeof(int));
+        up(pan_pmap_, pan_host_.pmap.data(), len * sizeof(int));
+        up(pan_seg_, pan_host_.seg.data(), pan_host_.seg.size() * sizeof(int));
+        up(pan_cta_, pan_host_.cta.data(), pan_host_.cta.size() * sizeof(int));
+        up(pan_off_, pan_host_.off.data(), len * sizeof(uint16_t));
+        /* (row, panel) pairs without a segment keep a zero partial */
+        PDAL_CUDA(cudaMemsetAsync(pan_part64_, 0, hp * sizeof(double), stream_));
+        if (pan_part32_) PDAL_CUDA(cudaMemsetAsync(pan_part32_, 0, hp * sizeof(float), stream_));
+    }
     up(c0_, prob_->objective_vector, n * sizeof(double));
     up(vlb0_, prob_->variable_lower_bound, n * sizeof(double));
     up(vub0_, prob_->variable_upper_bound, n * sizeof(double));
@@ -499,6 +574,8 @@ void CpalSolver::upload() {
         PDAL_CUDA(cudaMemsetAsync(y00_, 0, std::max<size_t>(m, 1) * sizeof(double), stream_));
     PDAL_CUDA(cudaStreamSynchronize(stream_));
     At_host_ = HostCsr(); /* host transpose no longer needed */
+    pan_host_.pmap = std::vector<int>();
+    pan_host_.off = std::vector<uint16_t>();
     upload_sec = now_sec() - t_up;
 }
 
@@ -507,6 +584,22 @@ void CpalSolver::upload() {
  * the previous kernel finishes, which hides part of the launch latency that
  * bounds small problems (measured: 6,800 iterations of a 2,000 x 5,000 LP
  * 67.4 -> 62.3 ms).  Stream capture records the same programmatic edges. */
+template <typename... KArgs, typename... Args>
+static void launch_pdl_cfg(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t stream,
+                           Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PDAL_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+}
+
 template <typename... KArgs, typename... Args>
 static void launch_pdl(void (*kern)(KArgs...), int grid, cudaStream_t stream, Args... args) {
     cudaLaunchConfig_t cfg = {};
@@ -719,6 +812,19 @@ void CpalSolver::setup_device() {
         PDAL_LAUNCH_CHECK();
         launches += 2;
     }
+    /* the long rows' values in panel order, in each precision the
+     * iteration runs in */
+    if (use_panels_) {
+        const long long len = pan_host_.len;
+        k_panel_gather<double><<<grid_for(len), kThreads, 0, stream_>>>(pan_pmap_, A_.v, pan_v64_, len);
+        if (fp32_phase_) k_panel_gather<float><<<grid_for(len), kThreads, 0, stream_>>>(pan_pmap_, A_.v, pan_v32_, len);
+        PDAL_CUDA(cudaFuncSetAttribute(k_dual_panels<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       pan_host_.W * (int)sizeof(double)));
+        PDAL_CUDA(cudaFuncSetAttribute(k_dual_panels<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       pan_host_.W * (int)sizeof(float)));
+        PDAL_LAUNCH_CHECK();
+        launches += fp32_phase_ ? 2 : 1;
+    }
     /* step size and primal weight: LP/CP_AL/src/solver.cu:3538-3609 */
     if (nnz_ == 0) {
         host_state.lambda_est = 1.0;
@@ -876,23 +982,43 @@ void CpalSolver::launch_dual(int koff, bool major) {
     const T *xbar = v.xbar;
     const int *rp = A_.rp, *ci = A_.ci;
     const CpalState *st = st_;
-    PDAL_WITH_S(S_it_, {
-        if (major) {
-            if (beta_on_)
-                launch_pdl(k_dual<T, SB, true, true>, A_.it.d.nblocks, stream_, A_.it.d, rp, ci, Av, xbar, da, st, wt,
-                           koff);
-            else
-                launch_pdl(k_dual<T, SB, true, false>, A_.it.d.nblocks, stream_, A_.it.d, rp, ci, Av, xbar, da, st, wt,
-                           koff);
-        } else {
-            if (beta_on_)
-                launch_pdl(k_dual<T, SB, false, true>, A_.it.d.nblocks, stream_, A_.it.d, rp, ci, Av, xbar, da, st, wt,
-                           koff);
-            else
-                launch_pdl(k_dual<T, SB, false, false>, A_.it.d.nblocks, stream_, A_.it.d, rp, ci, Av, xbar, da, st,
-                           wt, koff);
-        }
-    });
+    /* rows within the row-block budget (all rows without panels) */
+    const PlanDev &pl = use_panels_ ? a_short_ : A_.it;
+    if (pl.d.nblocks > 0) {
+        PDAL_WITH_S(S_it_, {
+            if (major) {
+                if (beta_on_)
+                    launch_pdl(k_dual<T, SB, true, true>, pl.d.nblocks, stream_, pl.d, rp, ci, Av, xbar, da, st, wt, koff);
+                else
+                    launch_pdl(k_dual<T, SB, true, false>, pl.d.nblocks, stream_, pl.d, rp, ci, Av, xbar, da, st, wt,
+                               koff);
+            } else {
+                if (beta_on_)
+                    launch_pdl(k_dual<T, SB, false, true>, pl.d.nblocks, stream_, pl.d, rp, ci, Av, xbar, da, st, wt,
+                               koff);
+                else
+                    launch_pdl(k_dual<T, SB, false, false>, pl.d.nblocks, stream_, pl.d, rp, ci, Av, xbar, da, st, wt,
+                               koff);
+            }
+        });
+    }
+    if (!use_panels_) return;
+    /* the long rows: panel partials, then one warp per row for the sum and
+     * the dual epilogue */
+    const PanelDev<T> pd = panel_dev<T>();
+    launch_pdl_cfg(k_dual_panels<T>, pd.nblocks, kPanelThreads, (size_t)pd.W * sizeof(T), stream_, pd, xbar, n_, st);
+    const int gf = (pd.H * 32 + kThreads - 1) / kThreads;
+    if (major) {
+        if (beta_on_)
+            launch_pdl(k_dual_long_finish<T, true, true>, gf, stream_, pd, da, st, wt, koff);
+        else
+            launch_pdl(k_dual_long_finish<T, true, false>, gf, stream_, pd, da, st, wt, koff);
+    } else {
+        if (beta_on_)
+            launch_pdl(k_dual_long_finish<T, false, true>, gf, stream_, pd, da, st, wt, koff);
+        else
+            launch_pdl(k_dual_long_finish<T, false, false>, gf, stream_, pd, da, st, wt, koff);
+    }
 }
 
 template <typename T>
@@ -1149,7 +1275,7 @@ void CpalSolver::polish() {
         auto fpe = [&](const PolishEval &e) { return primal ? e.dx2 * s.pw : e.dy2 / s.pw; };
         for (;;) { /* solver.cu:3988-4051 (primal), 4063-4126 (dual) */
             launch_iteration<double>(1, true);
-            launches += 2;
+            launches += iter_launches();
             if (do_restart) {
                 s.fp = fpe(evaluate());
                 s.fp0 = s.fp;
@@ -1157,7 +1283,7 @@ void CpalSolver::polish() {
             }
             for (int k = 2; k <= F - 1; ++k) launch_iteration<double>(k, false);
             launch_iteration<double>(F, true);
-            launches += 2 * (F - 1);
+            launches += (int64_t)iter_launches() * (F - 1);
             last = evaluate();
             s.fp = fpe(last);
             if (primal) { /* utils.cu:1341-1392 */
@@ -1265,7 +1391,7 @@ void CpalSolver::run_loop() {
     loop_t0_ = t0;
     const int F = cp_.F;
     const int G = std::max(1, O_.graph_blocks);
-    const int64_t per_block = 2LL * F - (m_ == 0 ? F : 0) + (m_ > 0 ? 4 : 3);
+    const int64_t per_block = (int64_t)iter_launches() * F + (m_ > 0 ? 4 : 3);
     k_start_clock<<<1, 1, 0, stream_>>>(st_);
     PDAL_LAUNCH_CHECK();
     launches += 1;
@@ -1473,6 +1599,8 @@ static void fill_stats(const pdal::CpalSolver &s, double total) {
     st.polish_primal_status = s.polish_status[0];
     st.polish_dual_status = s.polish_status[1];
     st.cr_passes = s.cr_passes;
+    st.panel_rows = s.panel_rows();
+    st.panels = s.panels();
 }
 
 /* Options from the environment, unless a switch of a controller this library

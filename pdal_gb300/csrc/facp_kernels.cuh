@@ -124,7 +124,8 @@ struct Prob {
     double *part;           /* 3 windows x grid x kSlot */
     double *lpart;          /* 3 windows x nlong_total x kSlot (zero at launch) */
     int nlong_total;
-    int pad;
+    int bar_extra;          /* blocks a barrier waits for beyond the launch (failure-path test only) */
+    long long spin_limit;   /* polls before a barrier wait gives up */
     GridBar *bar;
     Ctl *ctl;
     double *out_x, *out_y, *out_rc;
@@ -182,7 +183,7 @@ __device__ bool gsync(Cx &cx) {
         const unsigned g = ld_acquire(&b->gen);
         __threadfence();
         const unsigned prev = atomicAdd(&b->count, 1u);
-        if (prev == cx.nb - 1) {
+        if (prev == cx.nb + (unsigned)cx.P.bar_extra - 1) {
             atomicExch(&b->count, 0u);
             __threadfence();
             atomicAdd(&b->gen, 1u);
@@ -193,7 +194,7 @@ __device__ bool gsync(Cx &cx) {
                     ok = 0;
                     break;
                 }
-                if (++spins > kSpinLimit) {
+                if (++spins > cx.P.spin_limit) {
                     atomicExch(&b->err, 1);
                     ok = 0;
                     break;

@@ -403,6 +403,8 @@ void FacpSolver::prepare() {
         lbase += dm.plan.nlong;
     }
     P_.nlong_total = lbase;
+    P_.bar_extra = std::max(0, o_.barrier_extra_arrivals);
+    P_.spin_limit = o_.barrier_spin_limit > 0 ? o_.barrier_spin_limit : kSpinLimit;
 }
 
 void FacpSolver::upload() {

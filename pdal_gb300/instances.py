@@ -249,13 +249,7 @@ def planted_qp(n: int = 200_000, m: int = 100_000, nnz_per_col: int = 10, b_rows
     f = 0.5 * float(x @ Qx) + float(c @ x)
     Acsr = (A[0], A[1], A[2], (m, n))
     if q_form == "sparse":
-        import scipy.sparse as sp
-
-        Bs = sp.csr_matrix((B[2], B[1], B[0]), shape=(b_rows, n))
-        Q = (Bs.T @ Bs + sp.diags(dq)).tocsr()
-        Q.sort_indices()
-        data = QPData(c=c, A=Acsr, con_lb=con_lb, con_ub=con_ub, var_lb=lo, var_ub=hi,
-                      Q=(Q.indptr, Q.indices, Q.data, Q.shape))
+        data = QPData(c=c, A=Acsr, con_lb=con_lb, con_ub=con_ub, var_lb=lo, var_ub=hi, Q=_gram_plus_diag(B, dq, n))
     elif q_form == "lowrank":
         diag = (np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32), dq, (n, n))
         data = QPData(c=c, A=Acsr, con_lb=con_lb, con_ub=con_ub, var_lb=lo, var_ub=hi, Q=diag,
@@ -263,6 +257,42 @@ def planted_qp(n: int = 200_000, m: int = 100_000, nnz_per_col: int = 10, b_rows
     else:
         raise ValueError(q_form)
     return data, x, f
+
+
+def _gram_plus_diag(B, dq, n):
+    """CSR of B'B + diag(dq), summed in a fixed order with plain IEEE products
+    and additions (rows of B in order, pairs of a row in order, then the
+    diagonal), so that every platform builds the same bits: a library sparse
+    product may fuse or reorder them."""
+    rp, ci, v = B
+    lens = np.diff(rp)
+    keys, prods = [], []
+    rows_all = np.arange(lens.shape[0])
+    for L in np.unique(lens):
+        if L == 0:
+            continue
+        rows = rows_all[lens == L]
+        idx = rp[rows][:, None] + np.arange(L)[None, :]          # (R, L) positions
+        cols, vals = ci[idx].astype(np.int64), v[idx]
+        k = (cols[:, :, None] * n + cols[:, None, :]).reshape(rows.shape[0], -1)
+        pv = (vals[:, :, None] * vals[:, None, :]).reshape(rows.shape[0], -1)
+        keys.append((rows, k))
+        prods.append(pv)
+    # the pairs in row order of B, then the diagonal
+    flat_k = np.concatenate([k.reshape(-1) for _, k in keys]) if keys else np.zeros(0, np.int64)
+    flat_v = np.concatenate([p.reshape(-1) for p in prods]) if prods else np.zeros(0)
+    owner = np.concatenate([np.repeat(r, k.shape[1]) for r, k in keys]) if keys else np.zeros(0, np.int64)
+    seq = np.argsort(owner, kind="stable")
+    flat_k, flat_v = flat_k[seq], flat_v[seq]
+    dk = np.arange(n, dtype=np.int64) * n + np.arange(n, dtype=np.int64)
+    all_k = np.concatenate([flat_k, dk])
+    all_v = np.concatenate([flat_v, np.asarray(dq, dtype=np.float64)])
+    uk, inv = np.unique(all_k, return_inverse=True)
+    qv = np.bincount(inv, weights=all_v, minlength=uk.shape[0])
+    qr, qc = uk // n, uk % n
+    qrp = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(qrp, qr + 1, 1)
+    return (np.cumsum(qrp).astype(np.int32), qc.astype(np.int32), qv, (n, n))
 
 
 def transport_family(supplies: int, demands: int, seeds, base_costs=None, perturb: float = 0.2) -> list[LPData]:

@@ -31,6 +31,19 @@ def lpt_partition(weights, parts: int) -> list[list[int]]:
     return out
 
 
+def assemble(parts: list[list[int]], shard_results: list[list]) -> list:
+    """Per-rank results (rank r's list in the order of parts[r]) back in the
+    batch's instance order."""
+    n = sum(len(p) for p in parts)
+    out: list = [None] * n
+    for idx, res in zip(parts, shard_results):
+        if len(idx) != len(res):
+            raise ValueError("a rank returned a different number of results than it was assigned")
+        for i, r in zip(idx, res):
+            out[i] = r
+    return out
+
+
 def instance_weight(d) -> float:
     rp, ci, v, (m, n) = d.csr()
     return float(ci.shape[0] + n)

@@ -122,6 +122,72 @@ def test_long_rows_and_block_budgets(lp_lib, S):
     assert np.abs(g.y - o.y).max() / (1 + np.abs(o.y).max()) < 1e-9
 
 
+def _lp_with_dense_rows(rows_dense=(3, 77, 150), m=200, n=3000, seed=5):
+    """random_lp with a few rows made dense (every first, second or third
+    column), bounds kept feasible around the planted point."""
+    d = I.random_lp(m, n, 3, seed=seed)
+    rp, ci, v, _ = d.csr()
+    rng = np.random.default_rng(0)
+    rows = [list(zip(ci[rp[i]:rp[i + 1]], v[rp[i]:rp[i + 1]])) for i in range(m)]
+    for i in rows_dense:
+        rows[i] = [(j, rng.standard_normal()) for j in range(0, n, 1 + i % 3)]
+    rp2 = np.zeros(m + 1, np.int32)
+    rp2[1:] = np.cumsum([len(r) for r in rows])
+    ci2 = np.array([j for r in rows for j, _ in r], np.int32)
+    v2 = np.array([x for r in rows for _, x in r])
+    for i in rows_dense:
+        s_i = v2[rp2[i]:rp2[i + 1]].sum()
+        d.con_lb[i] = s_i
+        d.con_ub[i] = s_i + 1.0
+    d.A = (rp2, ci2, v2, (m, n))
+    return d
+
+
+@pytest.mark.parametrize("width", [1024, 2048, 4096])
+def test_long_rows_by_column_panels(lp_lib, width):
+    """The long rows of the iteration's A x by column panels (x staged in
+    shared memory, one partial per row and panel, then a warp per row): the
+    iterates still follow the oracle, with one panel (4096), two and three."""
+    d = _lp_with_dense_rows()
+    n = d.A[3][1]
+    p = {"eps": 1e-14, "iteration_limit": 600, "l_inf_ruiz_iterations": 4}
+    g = lp.solve(d, p, {"spmv_nnz_per_block": 256, "dual_panels": 1, "panel_width": width})
+    assert g.stats["panel_rows"] == 3 and g.stats["panels"] == (n + width - 1) // width
+    o = O.solve_lp(d, p)
+    assert np.abs(g.x - o.x).max() / (1 + np.abs(o.x).max()) < 1e-9
+    assert np.abs(g.y - o.y).max() / (1 + np.abs(o.y).max()) < 1e-9
+
+
+@pytest.mark.parametrize("opts", [{"al_lambda": 0.0}, {"al_lambda": 0.0, "sigma_mode": 1, "sigma_init_factor": 0.5}],
+                         ids=["lambda0", "sigma"])
+def test_badly_scaled_zipf_panels_iterates_match(lp_lib, opts):
+    """The large-LP structure at 1/50 scale with its long rows by column
+    panels (ten panels): iterates against the oracle after 1,000 iterations."""
+    d = I.zipf_lp(20_000, 40_000, 400_000, seed=1002)
+    p = {"eps": 1e-14, "iteration_limit": 1000, "sv_max_iter": 200, "time_limit": 120}
+    g = lp.solve(d, p, {**opts, "dual_panels": 1, "panel_width": 4096})
+    assert g.stats["panel_rows"] > 0 and g.stats["panels"] == 10
+    o = O.solve_lp(d, p, opts)
+    assert g.iterations == o.iterations
+    for a, b in ((g.x, o.x), (g.y, o.y)):
+        err = np.abs(a - b).max() / (1 + np.abs(b).max())
+        assert err < 1e-8, err
+
+
+def test_panels_fp32_form_reaches_tolerance(lp_lib):
+    """Chosen form (FP32 phase, then FP64) with the panel path: same status and
+    objective as the oracle at relative KKT 1e-7."""
+    d = _lp_with_dense_rows()
+    p = {"eps": 1e-7, "iteration_limit": 200_000, "time_limit": 120, "l_inf_ruiz_iterations": 4}
+    g = lp.solve(d, p, {"precision": "fp32_refine", "spmv_nnz_per_block": 256, "dual_panels": 1,
+                        "panel_width": 1024})
+    assert g.stats["panel_rows"] == 3 and g.stats["fp32_iterations"] > 0
+    o = O.solve_lp(d, p)
+    assert g.status == o.status == "OPTIMAL"
+    assert g.kkt < 1e-7
+    assert rel(g.primal_objective, o.primal_objective) <= 1e-6
+
+
 def test_edge_rows_and_columns(lp_lib):
     """Empty rows, empty columns, free rows, free and fixed variables."""
     d = I.random_lp(120, 300, 4, seed=8)

@@ -225,3 +225,18 @@ def test_fp32_refine_reaches_fp64_tolerance(form):
     assert abs(g32.primal_objective - g64.primal_objective) <= 5e-8 * (1 + abs(g64.primal_objective))
     if f_star is not None:
         assert abs(g32.primal_objective - f_star) <= 1e-7 * (1 + abs(f_star))
+
+
+def test_grid_barrier_wait_runs_out_and_recovers(qp_lib):
+    """Failure detection without a GPU fault: every grid barrier of the
+    persistent kernel is told to wait for one block more than the launch has,
+    with a short poll limit, so each wait runs out; the kernel records the
+    error and returns, the solve fails with a message instead of hanging, and
+    the next solve on the same context succeeds."""
+    qd, _, f_star = planted_qp(n=400, m=200, b_rows=100, seed=23, q_form="sparse")
+    bad = {"device": 0, "barrier_extra_arrivals": 1, "barrier_spin_limit": 1 << 12}
+    with pytest.raises(RuntimeError, match="grid barrier"):
+        qp.solve(qd, {"eps": 1e-8, "verbose": 0}, bad)
+    g = qp.solve(qd, {"eps": 1e-8, "verbose": 0}, {"device": 0})
+    assert g.status == "OPTIMAL"
+    assert abs(g.primal_objective - f_star) <= 1e-6 * (1 + abs(f_star))

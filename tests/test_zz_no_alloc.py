@@ -65,3 +65,56 @@ def test_noalloc_refuses_too_many_rows(lp_lib):
     rc = lp_lib.cp_al_gb300_primal_kkt_noalloc(524_289, 10, dummy, dummy, dummy, dummy, dummy, dummy, dummy,
                                                dummy, None)
     assert rc == -1
+    # the refusal is reported through the library's error message, and checked
+    # before any device pointer is touched
+    assert "524288 rows" in N.last_error(lp_lib)
+
+
+def test_noalloc_refuses_missing_matrix_pointers(lp_lib):
+    dummy = C.c_void_p(1)
+    for k in (1, 2):  # col_ind, vals
+        args = [dummy] * 8
+        args[k] = None
+        rc = lp_lib.cp_al_gb300_primal_kkt_noalloc(10, 10, *args, dummy, None)
+        assert rc == -1
+        assert "missing device pointer" in N.last_error(lp_lib)
+
+
+def _call(lib, torch, m, n, rp, ci, v, lb, ub, c, x):
+    out = torch.full((3,), -1.0, dtype=torch.float64, device="cuda")
+    rc = lib.cp_al_gb300_primal_kkt_noalloc(m, n, rp.data_ptr(), ci.data_ptr(), v.data_ptr(), lb.data_ptr(),
+                                            ub.data_ptr(), c.data_ptr(), x.data_ptr(), out.data_ptr(), None)
+    assert rc == 0, N.last_error(lib)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def test_noalloc_edge_sizes_and_nan(lp_lib):
+    """m = 0 (no constraints: both norms 0, out[2] = c'x), exactly the largest
+    accepted row count (524,288 empty rows), and a NaN in x, which must show
+    in both norms instead of being dropped by a maximum."""
+    torch = pytest.importorskip("torch")
+    n = 1000
+    rng = np.random.default_rng(3)
+    c = _device(torch, rng.standard_normal(n), torch.float64)
+    x = _device(torch, rng.standard_normal(n), torch.float64)
+    one_i = torch.zeros(1, dtype=torch.int32, device="cuda")
+    one_d = torch.zeros(1, dtype=torch.float64, device="cuda")
+    cx = float((c * x).sum().item())
+    r = _call(lp_lib, torch, 0, n, one_i, one_i, one_d, one_d, one_d, c, x)
+    assert r[0] == 0.0 and r[1] == 0.0 and abs(r[2] - cx) <= 1e-12 * (1 + abs(cx))
+    m = 524_288
+    rp = torch.zeros(m + 1, dtype=torch.int32, device="cuda")
+    lb = torch.full((m,), -1.0, dtype=torch.float64, device="cuda")
+    ub = torch.ones(m, dtype=torch.float64, device="cuda")
+    r = _call(lp_lib, torch, m, n, rp, one_i, one_d, lb, ub, c, x)
+    assert r[0] == 0.0 and r[1] == 0.0 and abs(r[2] - cx) <= 1e-12 * (1 + abs(cx))
+    d = I.random_lp(200, 500, 5, seed=1)
+    drp, dci, dv, (dm, dn) = d.csr()
+    xn = np.linspace(0.0, 1.0, dn)
+    xn[7] = np.nan
+    r = _call(lp_lib, torch, dm, dn, _device(torch, drp, torch.int32), _device(torch, dci, torch.int32),
+              _device(torch, dv, torch.float64), _device(torch, d.con_lb, torch.float64),
+              _device(torch, d.con_ub, torch.float64), _device(torch, d.c, torch.float64),
+              _device(torch, xn, torch.float64))
+    assert np.isnan(r[0]) and np.isnan(r[1]) and np.isnan(r[2])

@@ -92,6 +92,13 @@ typedef struct {
                                      row pieces, -1 (default) = panels when those rows hold at
                                      least 2^20 nonzeros */
     int panel_width;              /* columns per panel, a multiple of 4 up to 65536; 0 = 16384 */
+    int power_method;             /* sigma_max(A)^2 before the iteration: 0 = the reference's power
+                                     iteration (LP/CP_AL/src/utils.cu:87-228, sv_max_iter, sv_tol);
+                                     otherwise (default -1) the FP32_REFINE form uses Lanczos on
+                                     A A^T with FP32 products -- at most min(512, sv_max_iter)
+                                     steps, stopping when the largest Ritz value moves by less than
+                                     1e-8 relative over 16 steps -- and the FP64 form the power
+                                     iteration */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */

@@ -351,6 +351,7 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->fp32_stall_evals = 25;
     o->dual_panels = 0;
     o->panel_width = 0;
+    o->power_method = -1;
 }
 
 /* Each variable is read the way the reference reads it

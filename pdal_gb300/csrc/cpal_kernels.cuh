@@ -1252,6 +1252,106 @@ static __global__ void __launch_bounds__(kThreads) k_power_check(const double *_
     }
 }
 
+/* ------------------------------------------------------------------ */
+/* Lanczos estimate of sigma_max(A)^2 (chosen form)                    */
+/* ------------------------------------------------------------------ */
+/* Lanczos on A A^T: q_1 = v0/|v0|, then for j = 1, 2, ...
+ *   w = A (A^T q_j)                      (FP32 products: k_power_at and
+ *                                         k_power_a with inv = 1, which also
+ *                                         give the partials of q_j . w)
+ *   alpha_j = q_j . w
+ *   r = w - alpha_j q_j - beta_{j-1} q_{j-1},  beta_j = |r|,  q_{j+1} = r / beta_j
+ * (vectors and reductions in FP64).  The largest eigenvalue of the
+ * tridiagonal (alpha, beta) matrix -- computed on the host -- is a lower
+ * bound of sigma_max^2 that converges much faster than the power iteration's
+ * Rayleigh quotient (Golub and Van Loan, Matrix Computations, ch. 10).  The
+ * step counter and the coefficients live in LanczosDev. */
+struct LanczosDev {
+    double *alpha, *beta; /* per step */
+    int *j;               /* steps done */
+};
+
+/* alpha_j = sum of the partials of q_j . w */
+static __global__ void __launch_bounds__(kThreads) k_lz_alpha(const double *__restrict__ part, int nparts,
+                                                              LanczosDev lz) {
+    pdl_enter();
+    __shared__ double sbuf[kThreads / 32];
+    Red<1, 0> r;
+    r.zero();
+    for (int b = threadIdx.x; b < nparts; b += kThreads) r.s[0] += part[b];
+    block_reduce<kThreads, 1, 0>(r, sbuf);
+    if (threadIdx.x == 0) lz.alpha[*lz.j] = r.s[0];
+}
+
+/* p <- w - alpha_j q - beta_{j-1} p (p holds q_{j-1}), partials of |p|^2 */
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_lz_update(int m, const T *__restrict__ w, const double *__restrict__ q,
+                                                        double *p, LanczosDev lz, double *part) {
+    pdl_enter();
+    __shared__ double sbuf[kThreads / 32];
+    const int j = *lz.j;
+    const double a = lz.alpha[j], b = j > 0 ? lz.beta[j - 1] : 0.0;
+    Red<1, 0> r;
+    r.zero();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const double v = (double)w[i] - a * q[i] - b * p[i];
+        p[i] = v;
+        r.s[0] += v * v;
+    }
+    block_reduce<kThreads, 1, 0>(r, sbuf);
+    if (threadIdx.x == 0) part[blockIdx.x] = r.s[0];
+}
+
+/* beta_j = |r|, then j <- j + 1 */
+static __global__ void __launch_bounds__(kThreads) k_lz_beta(const double *__restrict__ part, int nparts,
+                                                             LanczosDev lz) {
+    pdl_enter();
+    __shared__ double sbuf[kThreads / 32];
+    Red<1, 0> r;
+    r.zero();
+    for (int b = threadIdx.x; b < nparts; b += kThreads) r.s[0] += part[b];
+    block_reduce<kThreads, 1, 0>(r, sbuf);
+    if (threadIdx.x == 0) {
+        const int j = *lz.j;
+        lz.beta[j] = sqrt(r.s[0]);
+        *lz.j = j + 1;
+    }
+}
+
+/* q_{j+1} = r / beta_j into p (a zero beta -- an invariant subspace -- leaves
+ * a zero vector, so the later coefficients are zero) and its FP32 copy for
+ * the next products */
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_lz_next(int m, double *p, T *qf, LanczosDev lz) {
+    pdl_enter();
+    const double b = lz.beta[*lz.j - 1];
+    const double inv = b > 0.0 ? 1.0 / b : 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const double v = p[i] * inv;
+        p[i] = v;
+        qf[i] = (T)v;
+    }
+}
+
+/* q_1 = v0 / |v0| (one block; v0 in q), q_0 = 0 in p */
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_lz_start(int m, double *q, T *qf, double *p) {
+    __shared__ double sbuf[kThreads / 32];
+    __shared__ double inv;
+    Red<1, 0> r;
+    r.zero();
+    for (int i = threadIdx.x; i < m; i += kThreads) r.s[0] += q[i] * q[i];
+    block_reduce<kThreads, 1, 0>(r, sbuf);
+    if (threadIdx.x == 0) inv = r.s[0] > 0.0 ? 1.0 / sqrt(r.s[0]) : 0.0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += kThreads) {
+        const double v = q[i] * inv;
+        q[i] = v;
+        qf[i] = (T)v;
+        p[i] = 0.0;
+    }
+}
+
 /* 1/|v| of the start vector */
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_power_start(int m, const T *__restrict__ v, PowerState *ps) {

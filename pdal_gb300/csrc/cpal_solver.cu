@@ -46,6 +46,40 @@ int grid_for(long long len, int per_block = kThreads) {
 
 #define PDAL_LAUNCH_CHECK() PDAL_CUDA(cudaGetLastError())
 
+/* Lanczos steps at most, and the steps between two convergence checks */
+constexpr int kLanczosMax = 512;
+constexpr int kLanczosChunk = 16;
+
+/* Largest eigenvalue of the symmetric tridiagonal matrix with diagonal a[0..k)
+ * and off-diagonal b[0..k-1), by bisection on the Sturm count (the number of
+ * negative pivots of T - x I). */
+double tridiag_max_eig(const std::vector<double> &a, const std::vector<double> &b, int k) {
+    double lo = 0.0, hi = 0.0;
+    for (int i = 0; i < k; ++i) {
+        const double r = (i > 0 ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < k ? std::fabs(b[i]) : 0.0);
+        hi = std::max(hi, a[i] + r);
+        lo = std::min(lo, a[i] - r);
+    }
+    auto below = [&](double x) { /* eigenvalues < x */
+        int cnt = 0;
+        double d = 1.0;
+        for (int i = 0; i < k; ++i) {
+            d = a[i] - x - (i > 0 ? b[i - 1] * b[i - 1] / d : 0.0);
+            if (d == 0.0) d = -1e-300;
+            if (d < 0.0) ++cnt;
+        }
+        return cnt;
+    };
+    for (int it = 0; it < 200 && hi - lo > 1e-15 * std::max(1.0, std::fabs(hi)); ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (below(mid) >= k) /* every eigenvalue is below mid */
+            hi = mid;
+        else
+            lo = mid;
+    }
+    return hi;
+}
+
 /* Dispatch on the row-block nonzero budget. */
 #define PDAL_WITH_S(Sval, ...)                     \
     switch (Sval) {                                 \
@@ -168,6 +202,9 @@ class CpalSolver {
     template <typename T>
     IterVecs<T> &vecs();
     void power_iteration();
+    void lanczos();
+    /* the chosen form estimates sigma_max^2 by Lanczos unless told otherwise */
+    bool use_lanczos() const { return m_ > 0 && fp32_phase_ && O_.power_method != 0; }
     void switch_to_fp64();
     void alloc_plan(PlanDev &pd);
     void upload_plan(PlanDev &pd);
@@ -223,6 +260,9 @@ class CpalSolver {
     IterVecs<float> v32_;
     CpalState *st_ = nullptr;
     PowerState *ps_ = nullptr;
+    /* Lanczos coefficients and step counter (chosen form's sigma_max^2) */
+    double *lz_alpha_ = nullptr, *lz_beta_ = nullptr;
+    int *lz_j_ = nullptr;
     CpalState *h_st_ = nullptr; /* pinned */
     PowerState *h_ps_ = nullptr;
     cudaGraphExec_t exec64_ = nullptr, exec32_ = nullptr;
@@ -491,6 +531,9 @@ void CpalSolver::alloc_all() {
     part_misc_ = arena_.take<double>(2 * (size_t)nmisc_ + 2);
     st_ = arena_.take<CpalState>(1);
     ps_ = arena_.take<PowerState>(1);
+    lz_alpha_ = arena_.take<double>(kLanczosMax);
+    lz_beta_ = arena_.take<double>(kLanczosMax);
+    lz_j_ = arena_.take<int>(1);
 }
 
 void CpalSolver::upload() {
@@ -699,6 +742,86 @@ void CpalSolver::power_iteration() {
     host_state.lambda_est = smax * smax;
 }
 
+/* sigma_max(A)^2 by Lanczos on A A^T with FP32 products (the chosen form;
+ * k_lz_* in cpal_kernels.cuh): the power iteration's start vector, steps in
+ * CUDA graphs of kLanczosChunk, and after each graph the largest Ritz value;
+ * it stops when that value moves by less than 1e-8 relative over a chunk, at
+ * an invariant subspace, or after min(kLanczosMax, sv_max_iter) steps. */
+void CpalSolver::lanczos() {
+    std::vector<double> v0(m_);
+    std::mt19937 gen(1);
+    std::normal_distribution<double> dist(0.0, 1.0);
+    for (int i = 0; i < m_; ++i) v0[i] = dist(gen);
+    PDAL_CUDA(cudaMemcpyAsync(tmp_m_, v0.data(), sizeof(double) * m_, cudaMemcpyHostToDevice, stream_));
+    h2d += sizeof(double) * m_;
+    PowerState h{};
+    h.inv = 1.0; /* the product kernels scale their input by inv */
+    h.max_iter = 1 << 30;
+    *h_ps_ = h;
+    PDAL_CUDA(cudaMemcpyAsync(ps_, h_ps_, sizeof(PowerState), cudaMemcpyHostToDevice, stream_));
+    PDAL_CUDA(cudaMemsetAsync(lz_j_, 0, sizeof(int), stream_));
+    /* FP32 buffers the iteration has not started to use */
+    float *qf = v32_.ybar, *w = v32_.u, *dp = reinterpret_cast<float *>(tmp_n_);
+    const LanczosDev lz{lz_alpha_, lz_beta_, lz_j_};
+    k_lz_start<float><<<1, kThreads, 0, stream_>>>(m_, tmp_m_, qf, tmp_m2_);
+    PDAL_LAUNCH_CHECK();
+    launches += 1;
+    const int gm = grid_for(m_);
+    const int nparts = A_.it.d.nblocks + A_.it.d.nlong;
+    cudaGraphExec_t exec = nullptr;
+    PDAL_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    for (int st = 0; st < kLanczosChunk; ++st) {
+        /* q_j and q_{j-1} alternate between the two FP64 buffers */
+        double *q = (st % 2 == 0) ? tmp_m_ : tmp_m2_, *p = (st % 2 == 0) ? tmp_m2_ : tmp_m_;
+        const int *Arp = A_.rp, *Aci = A_.ci, *Atrp = At_.rp, *Atci = At_.ci;
+        const float *Av = A_.vf, *Atv = At_.vf;
+        const PowerState *psc = ps_;
+        PDAL_WITH_S(S_it_, {
+            launch_pdl(k_power_at<SB, float>, At_.it.d.nblocks, stream_, At_.it.d, Atrp, Atci, Atv, (const float *)qf,
+                       dp, psc);
+            launch_pdl(k_power_a<SB, float, false>, A_.it.d.nblocks, stream_, A_.it.d, Arp, Aci, Av,
+                       (const float *)dp, (const float *)qf, w, part_misc_, psc);
+        });
+        launch_pdl(k_lz_alpha, 1, stream_, (const double *)part_misc_, nparts, lz);
+        launch_pdl(k_lz_update<float>, gm, stream_, m_, (const float *)w, (const double *)q, p, lz, part_misc_);
+        launch_pdl(k_lz_beta, 1, stream_, (const double *)part_misc_, gm, lz);
+        launch_pdl(k_lz_next<float>, gm, stream_, m_, p, qf, lz);
+    }
+    cudaGraph_t graph;
+    PDAL_CUDA(cudaStreamEndCapture(stream_, &graph));
+    PDAL_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    PDAL_CUDA(cudaGraphDestroy(graph));
+    /* a multiple of the chunk, at most kLanczosMax: every step's slot exists */
+    const int jmax = std::max(kLanczosChunk, std::min(kLanczosMax, std::max(P_.sv_max_iter, 1)));
+    std::vector<double> a(kLanczosMax), b(kLanczosMax);
+    double theta = 0.0, prev = -1.0;
+    int steps = 0;
+    for (;;) {
+        PDAL_CUDA(cudaGraphLaunch(exec, stream_));
+        launches += 6 * kLanczosChunk;
+        steps += kLanczosChunk;
+        PDAL_CUDA(cudaMemcpyAsync(a.data(), lz_alpha_, sizeof(double) * steps, cudaMemcpyDeviceToHost, stream_));
+        PDAL_CUDA(cudaMemcpyAsync(b.data(), lz_beta_, sizeof(double) * steps, cudaMemcpyDeviceToHost, stream_));
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
+        d2h += 2 * sizeof(double) * steps;
+        /* an invariant subspace (zero beta): T up to that step holds the answer */
+        int k = steps;
+        for (int i = 0; i < steps; ++i)
+            if (!(b[i] > 0.0)) {
+                k = i + 1;
+                break;
+            }
+        theta = tridiag_max_eig(a, b, k);
+        const bool invariant = k < steps || b[k - 1] <= 1e-12 * std::max(theta, 1e-300);
+        if (invariant || steps >= jmax || steps >= m_ || (prev > 0.0 && std::fabs(theta - prev) <= 1e-8 * theta))
+            break;
+        prev = theta;
+    }
+    cudaGraphExecDestroy(exec);
+    power_iters = steps;
+    host_state.lambda_est = theta;
+}
+
 void CpalSolver::setup_device() {
     const double t0 = now_sec();
     for (auto &r : sum_ms)
@@ -829,6 +952,8 @@ void CpalSolver::setup_device() {
     if (nnz_ == 0) {
         host_state.lambda_est = 1.0;
         power_iters = 0;
+    } else if (use_lanczos()) {
+        lanczos();
     } else {
         power_iteration();
     }

@@ -140,6 +140,13 @@ typedef struct {
     int cr_passes; /* Curtis-Reid passes run in the equilibration */
     int panel_rows; /* long rows the iteration's A x product runs by column panels (0: none) */
     int panels;     /* column panels of that product */
+    /* timing == 1 with panels: the dual step's launch for the other rows and
+     * its panel launch (the rest of avg_dual*_ms is the long rows' finishing
+     * launch) */
+    double avg_dual_rows_ms;
+    double avg_dual_panels_ms;
+    double avg_dual_rows32_ms;
+    double avg_dual_panels32_ms;
 } cp_al_gb300_stats_t;
 
 /* The reference defaults of every field, ignoring the environment. */

@@ -743,6 +743,10 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->graph_blocks = 1;
     o->timing = 0;
     o->fp32_stall_evals = 25;
+    /* device-only choices of the library (the oracle has one arithmetic) */
+    o->dual_panels = 0;
+    o->panel_width = 0;
+    o->power_method = -1;
 }
 
 /* LP/CP_AL/src/utils.cu:361-394 (reflection coefficient without the

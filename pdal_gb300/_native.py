@@ -232,6 +232,10 @@ class CpalStats(C.Structure):
         ("cr_passes", C.c_int),
         ("panel_rows", C.c_int),
         ("panels", C.c_int),
+        ("avg_dual_rows_ms", C.c_double),
+        ("avg_dual_panels_ms", C.c_double),
+        ("avg_dual_rows32_ms", C.c_double),
+        ("avg_dual_panels32_ms", C.c_double),
     ]
 
 

@@ -162,29 +162,6 @@ HostPlan plan_rows(int nr, const int *rp, int S) {
     return P;
 }
 
-HostPlan plan_short_rows(int nr, const int *rp, int S) {
-    HostPlan P;
-    P.S = S;
-    int r = 0;
-    while (r < nr) {
-        if (rp[r + 1] - rp[r] > S) {
-            ++r;
-            continue;
-        }
-        const int r0 = r;
-        int k = 0;
-        while (r < nr && (r - r0) < kMaxRowsPerBlock) {
-            const int l = rp[r + 1] - rp[r];
-            if (l > S || k + l > S) break;
-            k += l;
-            ++r;
-        }
-        P.desc.insert(P.desc.end(), {r0, r, rp[r0], rp[r]});
-    }
-    P.nblocks = (int)(P.desc.size() / 4);
-    return P;
-}
-
 HostPanels plan_panels(int nr, int nc, const int *rp, const int *ci, int S, int W, int target_blocks) {
     HostPanels Q;
     Q.W = W;
@@ -236,20 +213,21 @@ HostPanels plan_panels(int nr, int nc, const int *rp, const int *ci, int S, int 
             }
         }
     });
-    /* blocks: each panel's segments cut into chunks of about target
-     * nonzeros, chunk borders on segment borders */
-    const long long target = std::max<long long>(1024, Q.long_nnz / std::max(1, target_blocks));
+    /* blocks: target_blocks ranges of consecutive segments of about equal
+     * nonzero counts (one wave of equal work); a range may cross panel
+     * borders -- the block then stages each panel in turn */
     const int nseg = (int)(Q.seg.size() / 4);
-    int s = 0;
-    while (s < nseg) {
-        const int p = Q.seg[4 * s + 3];
-        const int s0 = s;
-        long long acc = 0;
-        while (s < nseg && Q.seg[4 * s + 3] == p && (s == s0 || acc + (Q.seg[4 * s + 2] - Q.seg[4 * s + 1]) <= target)) {
-            acc += Q.seg[4 * s + 2] - Q.seg[4 * s + 1];
-            ++s;
-        }
-        Q.cta.insert(Q.cta.end(), {p, s0, s, 0});
+    std::vector<long long> cum((size_t)nseg + 1, 0);
+    for (int s = 0; s < nseg; ++s) cum[s + 1] = cum[s] + (Q.seg[4 * s + 2] - Q.seg[4 * s + 1]);
+    const int nb = std::max(1, std::min(target_blocks, nseg));
+    int s0 = 0;
+    for (int b = 0; b < nb && s0 < nseg; ++b) {
+        const long long goal = cum[nseg] * (b + 1) / nb;
+        int s1 = (int)(std::lower_bound(cum.begin() + s0 + 1, cum.end(), goal) - cum.begin());
+        s1 = std::max(s0 + 1, std::min(s1, nseg));
+        if (b == nb - 1) s1 = nseg;
+        Q.cta.insert(Q.cta.end(), {s0, s1, 0, 0});
+        s0 = s1;
     }
     return Q;
 }

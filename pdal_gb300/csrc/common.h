@@ -111,17 +111,14 @@ struct HostPlan {
 };
 HostPlan plan_rows(int nr, const int *rp, int S);
 
-/* Row-block plan of the rows of at most S nonzeros only: rows longer than S
- * are left out (the column-panel plan below takes them). */
-HostPlan plan_short_rows(int nr, const int *rp, int S);
-
 /*
  * Column-panel plan of the long rows (more than S nonzeros) of a CSR matrix,
  * for the dual product A x of a matrix whose long rows hold much of its
  * nonzeros (the power-law rows of the large LP).  The columns are cut into
- * panels of W; a CUDA block stages one panel of x in shared memory, so the
- * long rows' random gathers become shared-memory reads, and reduces the
- * segments (one long row restricted to the panel) of a contiguous chunk.
+ * panels of W; a CUDA block takes a contiguous range of segments (one long
+ * row restricted to one panel; panel-major order) of about equal nonzero
+ * count and stages each panel its range touches in shared memory in turn, so
+ * the long rows' random gathers become shared-memory reads.
  * The long rows' nonzeros are stored again in panel order, each segment
  * padded with zeros to a multiple of 4 entries (128-bit loads), with the
  * column as a 16-bit offset in its panel (W <= 65536).  Segment (h, p) --
@@ -135,7 +132,7 @@ struct HostPanels {
     std::vector<int> pmap;      /* panel-array position -> CSR position, -1 for padding */
     std::vector<uint16_t> off;  /* column - p * W */
     std::vector<int> seg;       /* 4 ints per segment: {h, k0, k1, p} (k0, k1 multiples of 4) */
-    std::vector<int> cta;       /* 4 ints per block: {p, first segment, end segment, 0} */
+    std::vector<int> cta;       /* 4 ints per block: {first segment, end segment, 0, 0} */
     long long long_nnz = 0;
     long long len = 0;          /* panel-array length, padding included */
 };

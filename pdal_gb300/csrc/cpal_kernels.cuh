@@ -187,16 +187,34 @@ struct DualArgs {
     const T *lb, *ub;
 };
 
+/* Per-row inputs of the dual epilogue, loaded apart from the product so that
+ * a kernel can issue them for several rows before any product is ready. */
+template <typename T>
+struct DualIn {
+    T y, lo, hi, ax;
+    typename AnchorT<T>::type y0, ax0;
+};
+
 template <typename T, bool MAJOR, bool BETA>
 struct DualEpi : NoLongRed {
     DualArgs<T> a;
     Coefs<T> k;
     T w, omw;
-    __device__ __forceinline__ void operator()(int i, const T *s, Red<0, 0> &) const {
-        const T yi = a.y[i];
-        const T p = s[0];
-        const T lo = a.lb[i], hi = a.ub[i];
-        const T zb = vmax(lo, vmin(p - yi * k.inv_prox, hi));
+    __device__ __forceinline__ DualIn<T> fetch(int i) const {
+        DualIn<T> d;
+        d.y = a.y[i];
+        d.lo = a.lb[i];
+        d.hi = a.ub[i];
+        d.y0 = a.y0[i];
+        if (BETA) {
+            d.ax = (k.r != T(1)) ? a.ax[i] : T(0);
+            d.ax0 = a.ax0[i];
+        }
+        return d;
+    }
+    __device__ __forceinline__ void finish(int i, T p, const DualIn<T> &d) const {
+        const T yi = d.y;
+        const T zb = vmax(d.lo, vmin(p - yi * k.inv_prox, d.hi));
         const T yn = yi - k.rho * (p - zb);
         const T yb = T(2) * yn - yi;
         if (MAJOR) {
@@ -204,17 +222,18 @@ struct DualEpi : NoLongRed {
             a.ybar[i] = yb;
         }
         const T refl = k.r * yb + (T(1) - k.r) * yi;
-        const T ynew = halpern(w, omw, refl, a.y0[i]);
+        const T ynew = halpern(w, omw, refl, d.y0);
         a.y[i] = ynew;
         if (BETA) {
             T mix = p;
-            if (k.r != T(1)) mix = k.r * p + (T(1) - k.r) * a.ax[i];
-            const T axn = halpern(w, omw, mix, a.ax0[i]);
+            if (k.r != T(1)) mix = k.r * p + (T(1) - k.r) * d.ax;
+            const T axn = halpern(w, omw, mix, d.ax0);
             a.ax[i] = axn;
-            const T z2 = vmax(lo, vmin(axn - ynew * k.inv_beta, hi));
+            const T z2 = vmax(d.lo, vmin(axn - ynew * k.inv_beta, d.hi));
             a.u[i] = ynew - k.beta * (axn - z2);
         }
     }
+    __device__ __forceinline__ void operator()(int i, const T *s, Red<0, 0> &) const { finish(i, s[0], fetch(i)); }
 };
 
 template <typename T, int S, bool MAJOR, bool BETA>
@@ -240,6 +259,121 @@ __global__ void __launch_bounds__(kThreads) k_dual(RowPlanDev plan, const int *_
 }
 
 /* ------------------------------------------------------------------ */
+/* the other rows of the dual product, split by length                 */
+/* ------------------------------------------------------------------ */
+/* With the long rows on panels, the rows of A with at most one nonzero (most
+ * rows of a power-law LP) run one thread per row from a compact copy -- row,
+ * column and value of the single entry (an empty row has value 0) -- so a row
+ * costs three coalesced loads, one gather and its epilogue; a thread takes
+ * kShortUnroll rows and issues every load of them before using any.  Rows of
+ * 2..kShortMidLen nonzeros run 8 lanes per row, longer rows (up to S) a warp
+ * per row, over the CSR arrays.  One launch, each part a fixed number of
+ * blocks looping over its rows (one wave, no tail of short-lived blocks). */
+constexpr int kShortUnroll = 4;
+constexpr int kShortMidLen = 64; /* rows up to this length: 8 lanes each; longer rows: a warp */
+
+template <typename T>
+struct ShortDev {
+    const int *__restrict__ r1; /* rows with at most one entry, ascending */
+    const int *__restrict__ c1; /* its column (0 for an empty row) */
+    const T *__restrict__ v1;   /* its value (0 for an empty row) */
+    const int *__restrict__ r2; /* rows of 2..kShortMidLen entries, ascending */
+    const int *__restrict__ r3; /* rows of kShortMidLen+1..S entries, ascending */
+    int n1, n2, n3;             /* row counts */
+    int b1, b2, b3;             /* blocks of each part (in that order) */
+};
+
+template <typename T, bool MAJOR, bool BETA>
+__global__ void __launch_bounds__(kThreads) k_dual_short(ShortDev<T> sd, const int *__restrict__ rp,
+                                                         const int *__restrict__ ci, const T *__restrict__ val,
+                                                         const T *__restrict__ xbar, DualArgs<T> a,
+                                                         const CpalState *__restrict__ st,
+                                                         const typename WeightT<T>::type *__restrict__ wt,
+                                                         int koff) {
+    pdl_enter();
+    if (st->status) return;
+    DualEpi<T, MAJOR, BETA> epi;
+    epi.a = a;
+    load_coefs(st, epi.k);
+    epi.w = wt[koff].w;
+    epi.omw = wt[koff].omw;
+    const int b = blockIdx.x;
+    const int lane = threadIdx.x & 31;
+    if (b < sd.b1) {
+        /* one thread per row, kShortUnroll rows per thread at a time */
+        const int stride = sd.b1 * kThreads * kShortUnroll;
+        for (int base = b * kThreads * kShortUnroll + threadIdx.x; base < sd.n1; base += stride) {
+            int row[kShortUnroll], col[kShortUnroll];
+            T v[kShortUnroll], g[kShortUnroll];
+            DualIn<T> in[kShortUnroll];
+#pragma unroll
+            for (int u = 0; u < kShortUnroll; ++u) {
+                const int t = base + u * kThreads;
+                if (t < sd.n1) {
+                    row[u] = __ldcs(sd.r1 + t);
+                    col[u] = __ldcs(sd.c1 + t);
+                    v[u] = __ldcs(sd.v1 + t);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kShortUnroll; ++u) {
+                if (base + u * kThreads < sd.n1) {
+                    g[u] = __ldcg(xbar + col[u]);
+                    in[u] = epi.fetch(row[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kShortUnroll; ++u)
+                if (base + u * kThreads < sd.n1) epi.finish(row[u], v[u] * g[u], in[u]);
+        }
+        return;
+    }
+    if (b < sd.b1 + sd.b2) {
+        /* 8 lanes per row, four rows per warp at a time */
+        const int sub = lane >> 3, li = lane & 7;
+        const int w0 = (b - sd.b1) * (kThreads / 32) + ((int)threadIdx.x >> 5);
+        const int nw = sd.b2 * (kThreads / 32);
+        const unsigned mask = 0xffu << (8 * sub);
+        for (int g0 = w0 * 4; g0 < sd.n2; g0 += nw * 4) {
+            const int t = g0 + sub;
+            if (t >= sd.n2) continue; /* whole 8-lane groups skip together */
+            const int i = __ldcs(sd.r2 + t);
+            const int k0 = rp[i], k1 = rp[i + 1];
+            DualIn<T> in;
+            if (li == 0) in = epi.fetch(i);
+            T acc = T(0);
+            for (int k = k0 + li; k < k1; k += 8) acc = vfma(__ldcs(val + k), __ldcg(xbar + __ldcs(ci + k)), acc);
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1) acc += __shfl_xor_sync(mask, acc, o, 8);
+            if (li == 0) epi.finish(i, acc, in);
+        }
+        return;
+    }
+    /* a warp per row */
+    const int w0 = (b - sd.b1 - sd.b2) * (kThreads / 32) + ((int)threadIdx.x >> 5);
+    const int nw = sd.b3 * (kThreads / 32);
+    for (int w = w0; w < sd.n3; w += nw) {
+        const int i = __ldcs(sd.r3 + w);
+        const int k0 = rp[i], k1 = rp[i + 1];
+        DualIn<T> in;
+        if (lane == 0) in = epi.fetch(i);
+        T acc = T(0);
+        for (int k = k0 + lane; k < k1; k += 64) {
+            const bool two = k + 32 < k1;
+            const T va = __ldcs(val + k);
+            const int ca = __ldcs(ci + k);
+            const T vb = two ? __ldcs(val + k + 32) : T(0);
+            const int cb = two ? __ldcs(ci + k + 32) : 0;
+            acc = vfma(va, __ldcg(xbar + ca), acc);
+            if (two) acc = vfma(vb, __ldcg(xbar + cb), acc);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) epi.finish(i, acc, in);
+    }
+}
+
+/* ------------------------------------------------------------------ */
 /* the long rows of the dual product, by column panels                 */
 /* ------------------------------------------------------------------ */
 /* Device side of HostPanels (common.h): the long rows' nonzeros in panel
@@ -258,6 +392,14 @@ struct PanelDev {
 };
 
 constexpr int kPanelThreads = 512;
+constexpr int kPanelLanes = 8;  /* lanes per segment */
+constexpr int kPanelUnroll = 2; /* groups of four nonzeros per segment a lane loads before using them */
+
+/* dynamic shared memory of a panel block: the x-bar panel */
+template <typename T>
+__host__ __device__ constexpr size_t panel_smem_bytes(int W) {
+    return (size_t)W * sizeof(T);
+}
 
 /* panel values from the CSR values (after equilibration, in each precision) */
 template <typename T>
@@ -276,46 +418,107 @@ __device__ __forceinline__ void load4_stream(const uint16_t *p, int (&c)[4]) {
     c[3] = (int)(t.y >> 16);
 }
 
-/* One block per chunk of one panel: stage x-bar[pW, pW + W) in shared
- * memory, then one warp per segment -- four nonzeros per lane per step with
- * 128-bit streaming loads, the gathers from shared memory -- and a warp sum
- * into the segment's partial slot. */
+/* One block per range of segments (about equal nonzero counts, one wave).
+ * For each panel its range touches, the block stages x-bar[pW, pW + W) in
+ * shared memory; then each group of kPanelLanes lanes takes two of the
+ * panel's segments at a time.  A lane loads up to kPanelUnroll groups of four
+ * nonzeros of each (values with 128-bit streaming loads, 16-bit offsets with
+ * 64-bit loads) before using any, gathers from shared memory, and the
+ * group's lanes add their sums in a fixed tree into the segments' partial
+ * slots.  The sum order is fixed, so results are deterministic. */
 template <typename T>
-__global__ void __launch_bounds__(kPanelThreads) k_dual_panels(PanelDev<T> pd, const T *__restrict__ xbar, int n,
-                                                               const CpalState *__restrict__ st) {
-    pdl_enter();
-    if (st->status) return;
-    extern __shared__ __align__(16) unsigned char panel_smem[];
-    T *sx = reinterpret_cast<T *>(panel_smem);
-    const int4 c = pd.cta[blockIdx.x];
-    const int col0 = c.x * pd.W;
-    const int wlen = min(pd.W, n - col0);
-    /* x-bar starts 256-byte aligned and W is a multiple of 4, so the panel
+__device__ __forceinline__ void panel_stage(T *sx, const T *__restrict__ xbar, int col0, int wlen) {
+    /* x-bar starts 256-byte aligned and W is a multiple of 4, so a panel
      * starts on a 16-byte boundary */
     constexpr int V = 16 / sizeof(T);
     const int nvec = wlen / V;
     using Vec = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
     const Vec *src = reinterpret_cast<const Vec *>(xbar + col0);
     Vec *dst = reinterpret_cast<Vec *>(sx);
-    for (int i = threadIdx.x; i < nvec; i += kPanelThreads) dst[i] = __ldcg(src + i);
+    for (int i = threadIdx.x; i < nvec; i += 4 * kPanelThreads) {
+        Vec t[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * kPanelThreads < nvec) t[u] = __ldcg(src + i + u * kPanelThreads);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * kPanelThreads < nvec) dst[i + u * kPanelThreads] = t[u];
+    }
     for (int i = nvec * V + threadIdx.x; i < wlen; i += kPanelThreads) sx[i] = __ldcg(xbar + col0 + i);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int NW = kPanelThreads / 32;
-    for (int s = c.y + warp; s < c.z; s += NW) {
-        const int4 sg = pd.seg[s];
-        T acc = T(0);
-        for (int k = sg.y + 4 * lane; k < sg.z; k += 128) {
-            T v[4];
-            int o[4];
-            load4_stream(pd.val + k, v);
-            load4_stream(pd.off + k, o);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads, sizeof(T) == 4 ? 2 : 1) k_dual_panels(PanelDev<T> pd,
+                                                                                      const T *__restrict__ xbar,
+                                                                                      int n,
+                                                                                      const CpalState *__restrict__ st) {
+    pdl_enter();
+    if (st->status) return;
+    extern __shared__ __align__(16) unsigned char panel_smem[];
+    T *sx = reinterpret_cast<T *>(panel_smem);
+    const int4 c = pd.cta[blockIdx.x];
+    constexpr int NG = kPanelThreads / kPanelLanes;
+    const int grp = threadIdx.x / kPanelLanes, li = threadIdx.x % kPanelLanes;
+    constexpr int STEP = 4 * kPanelLanes; /* nonzeros a group covers per group of loads */
+    /* the groups of a warp may run different numbers of segments: each
+     * shuffles among its own lanes only */
+    const unsigned mask = ((1u << kPanelLanes) - 1u) << ((threadIdx.x & 31) & ~(kPanelLanes - 1));
+    int sbeg = c.x;
+    while (sbeg < c.y) {
+        /* the segments of this range in panel p: [sbeg, send) */
+        const int p = pd.seg[sbeg].w;
+        int send = sbeg + 1;
+        while (send < c.y && pd.seg[send].w == p) ++send;
+        const int col0 = p * pd.W;
+        __syncthreads(); /* the previous panel's gathers are done */
+        panel_stage(sx, xbar, col0, min(pd.W, n - col0));
+        __syncthreads();
+        for (int s = sbeg + grp; s < send; s += 2 * NG) {
+            const bool two = s + NG < send;
+            const int4 sa = pd.seg[s];
+            const int4 sb = two ? pd.seg[s + NG] : make_int4(0, 0, 0, 0);
+            T acc_a = T(0), acc_b = T(0);
+            const int la = sa.z - sa.y, lb = two ? sb.z - sb.y : 0;
+            const int len = max(la, lb);
+            for (int d = 4 * li; d < len; d += kPanelUnroll * STEP) {
+                T va[kPanelUnroll][4], vb[kPanelUnroll][4];
+                int oa[kPanelUnroll][4], ob[kPanelUnroll][4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc = vfma(v[q], sx[o[q]], acc);
+                for (int u = 0; u < kPanelUnroll; ++u) {
+                    const int e = d + u * STEP;
+                    if (e < la) {
+                        load4_stream(pd.val + sa.y + e, va[u]);
+                        load4_stream(pd.off + sa.y + e, oa[u]);
+                    }
+                    if (e < lb) {
+                        load4_stream(pd.val + sb.y + e, vb[u]);
+                        load4_stream(pd.off + sb.y + e, ob[u]);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kPanelUnroll; ++u) {
+                    const int e = d + u * STEP;
+                    if (e < la) {
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc_a = vfma(va[u][q], sx[oa[u][q]], acc_a);
+                    }
+                    if (e < lb) {
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc_b = vfma(vb[u][q], sx[ob[u][q]], acc_b);
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = kPanelLanes / 2; o > 0; o >>= 1) {
+                acc_a += __shfl_xor_sync(mask, acc_a, o, kPanelLanes);
+                acc_b += __shfl_xor_sync(mask, acc_b, o, kPanelLanes);
+            }
+            if (li == 0) {
+                pd.part[(size_t)sa.x * pd.P + sa.w] = acc_a;
+                if (two) pd.part[(size_t)sb.x * pd.P + sb.w] = acc_b;
+            }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) pd.part[(size_t)sg.x * pd.P + sg.w] = acc;
+        sbeg = send;
     }
 }
 

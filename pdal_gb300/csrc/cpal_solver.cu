@@ -181,6 +181,7 @@ class CpalSolver {
     int fp32_iters = 0;
     bool started = false;
     double sum_ms[2][3] = {{0, 0, 0}, {0, 0, 0}}; /* [fp64, fp32][primal, dual, block] */
+    double sub_ms[2][2] = {{0, 0}, {0, 0}};       /* [fp64, fp32][dual short rows, dual panels] */
     int timed[2] = {0, 0};
 
   private:
@@ -192,7 +193,7 @@ class CpalSolver {
     template <typename T>
     void launch_primal(int koff, bool major);
     template <typename T>
-    void launch_dual(int koff, bool major);
+    void launch_dual(int koff, bool major, bool timed = false);
     template <typename T>
     void launch_eval();
     template <typename T>
@@ -227,7 +228,15 @@ class CpalSolver {
      * common.h); the iteration's row blocks then cover the other rows */
     bool use_panels_ = false;
     HostPanels pan_host_;
-    PlanDev a_short_;
+    /* the other rows of A: at most one entry (one thread each, compact copy)
+     * and 2..S entries (one warp each) -- k_dual_short */
+    std::vector<int> sh_r1_h, sh_p1_h, sh_c1_h, sh_r2_h, sh_r3_h;
+    int *sh_r1_ = nullptr, *sh_p1_ = nullptr, *sh_c1_ = nullptr, *sh_r2_ = nullptr, *sh_r3_ = nullptr;
+    double *sh_v64_ = nullptr;
+    float *sh_v32_ = nullptr;
+    int sh_b1_ = 0, sh_b2_ = 0, sh_b3_ = 0;
+    template <typename T>
+    ShortDev<T> short_dev() const;
     int *pan_rows_ = nullptr, *pan_pmap_ = nullptr;
     int4 *pan_seg_ = nullptr, *pan_cta_ = nullptr;
     uint16_t *pan_off_ = nullptr;
@@ -236,7 +245,7 @@ class CpalSolver {
     template <typename T>
     PanelDev<T> panel_dev() const;
     /* kernels one iteration launches */
-    int iter_launches() const { return 1 + (m_ == 0 ? 0 : use_panels_ ? (a_short_.hp.nblocks > 0 ? 3 : 2) : 1); }
+    int iter_launches() const { return 1 + (m_ == 0 ? 0 : use_panels_ ? (sh_b1_ + sh_b2_ + sh_b3_ > 0 ? 3 : 2) : 1); }
 
   public:
     int panel_rows() const { return use_panels_ ? pan_host_.H : 0; }
@@ -267,7 +276,7 @@ class CpalSolver {
     PowerState *h_ps_ = nullptr;
     cudaGraphExec_t exec64_ = nullptr, exec32_ = nullptr;
     int nmisc_ = 0;
-    cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 template <>
@@ -277,6 +286,17 @@ IterVecs<double> &CpalSolver::vecs<double>() {
 template <>
 IterVecs<float> &CpalSolver::vecs<float>() {
     return v32_;
+}
+
+template <>
+ShortDev<double> CpalSolver::short_dev<double>() const {
+    return ShortDev<double>{sh_r1_, sh_c1_, sh_v64_, sh_r2_, sh_r3_, (int)sh_r1_h.size(), (int)sh_r2_h.size(),
+                            (int)sh_r3_h.size(), sh_b1_, sh_b2_, sh_b3_};
+}
+template <>
+ShortDev<float> CpalSolver::short_dev<float>() const {
+    return ShortDev<float>{sh_r1_, sh_c1_, sh_v32_, sh_r2_, sh_r3_, (int)sh_r1_h.size(), (int)sh_r2_h.size(),
+                           (int)sh_r3_h.size(), sh_b1_, sh_b2_, sh_b3_};
 }
 
 template <>
@@ -444,7 +464,15 @@ void CpalSolver::alloc_all() {
     alloc_plan(At_.ev);
     if (use_panels_) {
         const size_t len = (size_t)pan_host_.len, hp = (size_t)pan_host_.H * pan_host_.P;
-        alloc_plan(a_short_);
+        const size_t n1 = std::max<size_t>(sh_r1_h.size(), 1), n2 = std::max<size_t>(sh_r2_h.size(), 1),
+                     n3 = std::max<size_t>(sh_r3_h.size(), 1);
+        sh_r1_ = arena_.take<int>(n1);
+        sh_p1_ = arena_.take<int>(n1);
+        sh_c1_ = arena_.take<int>(n1);
+        sh_r2_ = arena_.take<int>(n2);
+        sh_r3_ = arena_.take<int>(n3);
+        sh_v64_ = arena_.take<double>(n1);
+        if (fp32_phase_) sh_v32_ = arena_.take<float>(n1);
         pan_rows_ = arena_.take<int>(pan_host_.rows.size());
         pan_pmap_ = arena_.take<int>(len);
         pan_seg_ = arena_.take<int4>(pan_host_.seg.size() / 4);
@@ -562,10 +590,37 @@ void CpalSolver::upload() {
         }
         if (O_.dual_panels == 1 || long_nnz >= (1ll << 20)) {
             const int W = O_.panel_width > 0 ? O_.panel_width : 16384;
-            if (W % 4 != 0 || W > 65536) throw Error("panel_width must be a multiple of 4 up to 65536");
-            /* about three panel blocks per SM (64 KB of FP32 x-bar each) */
-            pan_host_ = plan_panels(m_, n_, rp, prob_->constraint_matrix_col_indices, S_it_, W, 3 * 152);
-            a_short_.hp = plan_short_rows(m_, rp, S_it_);
+            /* the FP64 phase stages W doubles per block */
+            if (W % 4 != 0 || W > 65536 || panel_smem_bytes<double>(W) > 227 * 1024)
+                throw Error("panel_width must be a multiple of 4 whose FP64 panel fits in shared memory "
+                            "(at most 29,056)");
+            /* one wave of two panel blocks per SM (64 KB of FP32 x-bar each) */
+            pan_host_ = plan_panels(m_, n_, rp, prob_->constraint_matrix_col_indices, S_it_, W, 2 * 152);
+            sh_r1_h.clear();
+            sh_p1_h.clear();
+            sh_c1_h.clear();
+            sh_r2_h.clear();
+            sh_r3_h.clear();
+            const int *cip = prob_->constraint_matrix_col_indices;
+            for (int r = 0; r < m_; ++r) {
+                const int len = rp[r + 1] - rp[r];
+                if (len <= 1) {
+                    sh_r1_h.push_back(r);
+                    sh_p1_h.push_back(len ? rp[r] : -1);
+                    sh_c1_h.push_back(len ? cip[rp[r]] : 0);
+                } else if (len <= kShortMidLen) {
+                    sh_r2_h.push_back(r);
+                } else if (len <= S_it_) {
+                    sh_r3_h.push_back(r);
+                }
+            }
+            /* a fixed number of blocks per part, each looping over its rows */
+            auto blocks = [](long long rows, long long per_block, long long cap) {
+                return (int)std::min<long long>((rows + per_block - 1) / per_block, cap);
+            };
+            sh_b1_ = blocks((long long)sh_r1_h.size(), kThreads * kShortUnroll, 152 * 4);
+            sh_b2_ = blocks((long long)sh_r2_h.size(), kThreads / 8, 152 * 4);
+            sh_b3_ = blocks((long long)sh_r3_h.size(), kThreads / 32, 152 * 2);
             use_panels_ = pan_host_.H > 0;
         }
     }
@@ -592,7 +647,11 @@ void CpalSolver::upload() {
     upload_plan(At_.ev);
     if (use_panels_) {
         const size_t len = (size_t)pan_host_.len, hp = (size_t)pan_host_.H * pan_host_.P;
-        upload_plan(a_short_);
+        up(sh_r1_, sh_r1_h.data(), sh_r1_h.size() * sizeof(int));
+        up(sh_p1_, sh_p1_h.data(), sh_p1_h.size() * sizeof(int));
+        up(sh_c1_, sh_c1_h.data(), sh_c1_h.size() * sizeof(int));
+        up(sh_r2_, sh_r2_h.data(), sh_r2_h.size() * sizeof(int));
+        up(sh_r3_, sh_r3_h.data(), sh_r3_h.size() * sizeof(int));
         up(pan_rows_, pan_host_.rows.data(), pan_host_.rows.size() * sizeof(int));
         up(pan_pmap_, pan_host_.pmap.data(), len * sizeof(int));
         up(pan_seg_, pan_host_.seg.data(), pan_host_.seg.size() * sizeof(int));
@@ -826,6 +885,8 @@ void CpalSolver::setup_device() {
     const double t0 = now_sec();
     for (auto &r : sum_ms)
         for (auto &x : r) x = 0;
+    for (auto &r : sub_ms)
+        for (auto &x : r) x = 0;
     timed[0] = timed[1] = 0;
     launches = 0;
     fp32_iters = 0;
@@ -941,10 +1002,15 @@ void CpalSolver::setup_device() {
         const long long len = pan_host_.len;
         k_panel_gather<double><<<grid_for(len), kThreads, 0, stream_>>>(pan_pmap_, A_.v, pan_v64_, len);
         if (fp32_phase_) k_panel_gather<float><<<grid_for(len), kThreads, 0, stream_>>>(pan_pmap_, A_.v, pan_v32_, len);
+        const long long n1 = (long long)sh_r1_h.size();
+        if (n1) {
+            k_panel_gather<double><<<grid_for(n1), kThreads, 0, stream_>>>(sh_p1_, A_.v, sh_v64_, n1);
+            if (fp32_phase_) k_panel_gather<float><<<grid_for(n1), kThreads, 0, stream_>>>(sh_p1_, A_.v, sh_v32_, n1);
+        }
         PDAL_CUDA(cudaFuncSetAttribute(k_dual_panels<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       pan_host_.W * (int)sizeof(double)));
+                                       (int)panel_smem_bytes<double>(pan_host_.W)));
         PDAL_CUDA(cudaFuncSetAttribute(k_dual_panels<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       pan_host_.W * (int)sizeof(float)));
+                                       (int)panel_smem_bytes<float>(pan_host_.W)));
         PDAL_LAUNCH_CHECK();
         launches += fp32_phase_ ? 2 : 1;
     }
@@ -1098,7 +1164,7 @@ void CpalSolver::launch_primal(int koff, bool major) {
 }
 
 template <typename T>
-void CpalSolver::launch_dual(int koff, bool major) {
+void CpalSolver::launch_dual(int koff, bool major, bool timed) {
     if (m_ == 0) return;
     auto &v = vecs<T>();
     const T *Av = matvals<T>(A_.v, A_.vf);
@@ -1107,9 +1173,8 @@ void CpalSolver::launch_dual(int koff, bool major) {
     const T *xbar = v.xbar;
     const int *rp = A_.rp, *ci = A_.ci;
     const CpalState *st = st_;
-    /* rows within the row-block budget (all rows without panels) */
-    const PlanDev &pl = use_panels_ ? a_short_ : A_.it;
-    if (pl.d.nblocks > 0) {
+    if (!use_panels_) {
+        const PlanDev &pl = A_.it;
         PDAL_WITH_S(S_it_, {
             if (major) {
                 if (beta_on_)
@@ -1126,12 +1191,30 @@ void CpalSolver::launch_dual(int koff, bool major) {
                                koff);
             }
         });
+        return;
     }
-    if (!use_panels_) return;
+    /* rows within the row-block budget, split by length */
+    if (sh_b1_ + sh_b2_ + sh_b3_ > 0) {
+        const ShortDev<T> sd = short_dev<T>();
+        const int g = sh_b1_ + sh_b2_ + sh_b3_;
+        if (major) {
+            if (beta_on_)
+                launch_pdl(k_dual_short<T, true, true>, g, stream_, sd, rp, ci, Av, xbar, da, st, wt, koff);
+            else
+                launch_pdl(k_dual_short<T, true, false>, g, stream_, sd, rp, ci, Av, xbar, da, st, wt, koff);
+        } else {
+            if (beta_on_)
+                launch_pdl(k_dual_short<T, false, true>, g, stream_, sd, rp, ci, Av, xbar, da, st, wt, koff);
+            else
+                launch_pdl(k_dual_short<T, false, false>, g, stream_, sd, rp, ci, Av, xbar, da, st, wt, koff);
+        }
+    }
     /* the long rows: panel partials, then one warp per row for the sum and
      * the dual epilogue */
+    if (timed) PDAL_CUDA(cudaEventRecordWithFlags(ev_[4], stream_, cudaEventRecordExternal));
     const PanelDev<T> pd = panel_dev<T>();
-    launch_pdl_cfg(k_dual_panels<T>, pd.nblocks, kPanelThreads, (size_t)pd.W * sizeof(T), stream_, pd, xbar, n_, st);
+    launch_pdl_cfg(k_dual_panels<T>, pd.nblocks, kPanelThreads, panel_smem_bytes<T>(pd.W), stream_, pd, xbar, n_, st);
+    if (timed) PDAL_CUDA(cudaEventRecordWithFlags(ev_[5], stream_, cudaEventRecordExternal));
     const int gf = (pd.H * 32 + kThreads - 1) / kThreads;
     if (major) {
         if (beta_on_)
@@ -1223,7 +1306,7 @@ void CpalSolver::capture_block(cudaGraphExec_t &exec) {
                 PDAL_CUDA(cudaEventRecordWithFlags(ev_[0], stream_, cudaEventRecordExternal));
                 launch_primal<T>(i, false);
                 PDAL_CUDA(cudaEventRecordWithFlags(ev_[1], stream_, cudaEventRecordExternal));
-                launch_dual<T>(i, false);
+                launch_dual<T>(i, false, use_panels_);
                 PDAL_CUDA(cudaEventRecordWithFlags(ev_[2], stream_, cudaEventRecordExternal));
             } else {
                 launch_iteration<T>(i, i == F);
@@ -1544,6 +1627,13 @@ void CpalSolver::run_loop() {
             sum_ms[ph][0] += a;
             sum_ms[ph][1] += b;
             sum_ms[ph][2] += c;
+            if (use_panels_) {
+                float d = 0, e = 0;
+                PDAL_CUDA(cudaEventElapsedTime(&d, ev_[1], ev_[4]));
+                PDAL_CUDA(cudaEventElapsedTime(&e, ev_[4], ev_[5]));
+                sub_ms[ph][0] += d;
+                sub_ms[ph][1] += e;
+            }
             timed[ph] += 1;
         }
         if (fp32_phase_) fp32_iters = h_st_->total;
@@ -1724,6 +1814,14 @@ static void fill_stats(const pdal::CpalSolver &s, double total) {
     st.polish_primal_status = s.polish_status[0];
     st.polish_dual_status = s.polish_status[1];
     st.cr_passes = s.cr_passes;
+    if (s.timed[0]) {
+        st.avg_dual_rows_ms = s.sub_ms[0][0] / s.timed[0];
+        st.avg_dual_panels_ms = s.sub_ms[0][1] / s.timed[0];
+    }
+    if (s.timed[1]) {
+        st.avg_dual_rows32_ms = s.sub_ms[1][0] / s.timed[1];
+        st.avg_dual_panels32_ms = s.sub_ms[1][1] / s.timed[1];
+    }
     st.panel_rows = s.panel_rows();
     st.panels = s.panels();
 }

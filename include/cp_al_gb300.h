@@ -92,6 +92,11 @@ typedef struct {
                                      row pieces, -1 (default) = panels when those rows hold at
                                      least 2^20 nonzeros */
     int panel_width;              /* columns per panel, a multiple of 4 up to 65536; 0 = 16384 */
+    int primal_hot_rows;          /* with the panel path: the primal product A^T u takes the long
+                                     rows' entries of u from a compact copy in shared memory (at
+                                     most 1,536 long rows).  1 = in both phases, 0 = never (global
+                                     memory like the rest), -1 (default) = in the FP64 phase only
+                                     (measured faster there, slower in FP32) */
     int power_method;             /* sigma_max(A)^2 before the iteration: 0 = the reference's power
                                      iteration (LP/CP_AL/src/utils.cu:87-228, sv_max_iter, sv_tol);
                                      otherwise (default -1) the FP32_REFINE form uses Lanczos on

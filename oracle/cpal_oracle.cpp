@@ -744,8 +744,9 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->timing = 0;
     o->fp32_stall_evals = 25;
     /* device-only choices of the library (the oracle has one arithmetic) */
-    o->dual_panels = 0;
+    o->dual_panels = -1;
     o->panel_width = 0;
+    o->primal_hot_rows = -1;
     o->power_method = -1;
 }
 

@@ -196,6 +196,7 @@ class CpalOptions(C.Structure):
         ("batch_blocks_per_sm", C.c_int),
         ("dual_panels", C.c_int),
         ("panel_width", C.c_int),
+        ("primal_hot_rows", C.c_int),
         ("power_method", C.c_int),
     ]
 

@@ -226,7 +226,16 @@ HostPanels plan_panels(int nr, int nc, const int *rp, const int *ci, int S, int 
         int s1 = (int)(std::lower_bound(cum.begin() + s0 + 1, cum.end(), goal) - cum.begin());
         s1 = std::max(s0 + 1, std::min(s1, nseg));
         if (b == nb - 1) s1 = nseg;
-        Q.cta.insert(Q.cta.end(), {s0, s1, 0, 0});
+        /* the block's range cut at panel borders into pieces of one panel */
+        const int first_piece = (int)(Q.piece.size() / 4);
+        for (int a = s0; a < s1;) {
+            const int p = Q.seg[4 * a + 3];
+            int e = a + 1;
+            while (e < s1 && Q.seg[4 * e + 3] == p) ++e;
+            Q.piece.insert(Q.piece.end(), {p, a, e, 0});
+            a = e;
+        }
+        Q.cta.insert(Q.cta.end(), {first_piece, (int)(Q.piece.size() / 4), 0, 0});
         s0 = s1;
     }
     return Q;

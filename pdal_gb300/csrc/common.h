@@ -132,7 +132,8 @@ struct HostPanels {
     std::vector<int> pmap;      /* panel-array position -> CSR position, -1 for padding */
     std::vector<uint16_t> off;  /* column - p * W */
     std::vector<int> seg;       /* 4 ints per segment: {h, k0, k1, p} (k0, k1 multiples of 4) */
-    std::vector<int> cta;       /* 4 ints per block: {first segment, end segment, 0, 0} */
+    std::vector<int> piece;     /* 4 ints per piece: {panel, first segment, end segment, 0} */
+    std::vector<int> cta;       /* 4 ints per block: {first piece, end piece, 0, 0} */
     long long long_nnz = 0;
     long long len = 0;          /* panel-array length, padding included */
 };

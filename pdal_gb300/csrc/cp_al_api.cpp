@@ -349,8 +349,9 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->graph_blocks = 1;
     o->timing = 0;
     o->fp32_stall_evals = 25;
-    o->dual_panels = 0;
+    o->dual_panels = -1;
     o->panel_width = 0;
+    o->primal_hot_rows = -1;
     o->power_method = -1;
 }
 

@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kThreads) k_dual(RowPlanDev plan, const int *_
  * 2..kShortMidLen nonzeros run 8 lanes per row, longer rows (up to S) a warp
  * per row, over the CSR arrays.  One launch, each part a fixed number of
  * blocks looping over its rows (one wave, no tail of short-lived blocks). */
-constexpr int kShortUnroll = 4;
+constexpr int kShortUnroll = 2;
 constexpr int kShortMidLen = 64; /* rows up to this length: 8 lanes each; longer rows: a warp */
 
 template <typename T>
@@ -278,13 +278,13 @@ struct ShortDev {
     const int *__restrict__ c1; /* its column (0 for an empty row) */
     const T *__restrict__ v1;   /* its value (0 for an empty row) */
     const int *__restrict__ r2; /* rows of 2..kShortMidLen entries, ascending */
-    const int *__restrict__ r3; /* rows of kShortMidLen+1..S entries, ascending */
+    const int *__restrict__ r3; /* rows of kShortMidLen+1..S entries, longest first */
     int n1, n2, n3;             /* row counts */
     int b1, b2, b3;             /* blocks of each part (in that order) */
 };
 
 template <typename T, bool MAJOR, bool BETA>
-__global__ void __launch_bounds__(kThreads) k_dual_short(ShortDev<T> sd, const int *__restrict__ rp,
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 6 : 4) k_dual_short(ShortDev<T> sd, const int *__restrict__ rp,
                                                          const int *__restrict__ ci, const T *__restrict__ val,
                                                          const T *__restrict__ xbar, DualArgs<T> a,
                                                          const CpalState *__restrict__ st,
@@ -358,14 +358,21 @@ __global__ void __launch_bounds__(kThreads) k_dual_short(ShortDev<T> sd, const i
         DualIn<T> in;
         if (lane == 0) in = epi.fetch(i);
         T acc = T(0);
-        for (int k = k0 + lane; k < k1; k += 64) {
-            const bool two = k + 32 < k1;
-            const T va = __ldcs(val + k);
-            const int ca = __ldcs(ci + k);
-            const T vb = two ? __ldcs(val + k + 32) : T(0);
-            const int cb = two ? __ldcs(ci + k + 32) : 0;
-            acc = vfma(va, __ldcg(xbar + ca), acc);
-            if (two) acc = vfma(vb, __ldcg(xbar + cb), acc);
+        constexpr int U3 = 8;
+        for (int k = k0 + lane; k < k1; k += 32 * U3) {
+            T vv[U3];
+            int cc[U3];
+#pragma unroll
+            for (int u = 0; u < U3; ++u) {
+                const bool in_row = k + 32 * u < k1;
+                vv[u] = in_row ? __ldcs(val + k + 32 * u) : T(0);
+                cc[u] = in_row ? __ldcs(ci + k + 32 * u) : 0;
+            }
+            T g[U3];
+#pragma unroll
+            for (int u = 0; u < U3; ++u) g[u] = (k + 32 * u < k1) ? __ldcg(xbar + cc[u]) : T(0);
+#pragma unroll
+            for (int u = 0; u < U3; ++u) acc = vfma(vv[u], g[u], acc);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -384,10 +391,12 @@ template <typename T>
 struct PanelDev {
     const int *__restrict__ rows;
     const int4 *__restrict__ seg;
-    const int4 *__restrict__ cta;
+    const int4 *__restrict__ piece; /* {panel, first segment, end segment} */
+    const int4 *__restrict__ cta;   /* {first piece, end piece} per block */
     const T *__restrict__ val;
     const uint16_t *__restrict__ off;
     T *part;
+    T *hot; /* the long rows' entries of the primal product's gathered vector (or null) */
     int H, P, W, nblocks;
 };
 
@@ -463,12 +472,10 @@ __global__ void __launch_bounds__(kPanelThreads, sizeof(T) == 4 ? 2 : 1) k_dual_
     /* the groups of a warp may run different numbers of segments: each
      * shuffles among its own lanes only */
     const unsigned mask = ((1u << kPanelLanes) - 1u) << ((threadIdx.x & 31) & ~(kPanelLanes - 1));
-    int sbeg = c.x;
-    while (sbeg < c.y) {
-        /* the segments of this range in panel p: [sbeg, send) */
-        const int p = pd.seg[sbeg].w;
-        int send = sbeg + 1;
-        while (send < c.y && pd.seg[send].w == p) ++send;
+    for (int pc = c.x; pc < c.y; ++pc) {
+        /* the segments of this block in panel p: [sbeg, send) */
+        const int4 pie = pd.piece[pc];
+        const int p = pie.x, sbeg = pie.y, send = pie.z;
         const int col0 = p * pd.W;
         __syncthreads(); /* the previous panel's gathers are done */
         panel_stage(sx, xbar, col0, min(pd.W, n - col0));
@@ -518,7 +525,6 @@ __global__ void __launch_bounds__(kPanelThreads, sizeof(T) == 4 ? 2 : 1) k_dual_
                 if (two) pd.part[(size_t)sb.x * pd.P + sb.w] = acc_b;
             }
         }
-        sbeg = send;
     }
 }
 
@@ -543,10 +549,52 @@ __global__ void __launch_bounds__(kThreads) k_dual_long_finish(PanelDev<T> pd, D
         load_coefs(st, epi.k);
         epi.w = wt[koff].w;
         epi.omw = wt[koff].omw;
-        const T sum[1] = {(T)s};
-        Red<0, 0> red;
-        epi(pd.rows[h], sum, red);
+        const int i = pd.rows[h];
+        epi.finish(i, (T)s, epi.fetch(i));
+        /* the value the next primal product gathers for this row */
+        if (pd.hot) pd.hot[h] = BETA ? a.u[i] : a.y[i];
     }
+}
+
+/* hot[h] = gat[rows[h]]: the compact copy of the long rows' gathered values,
+ * rebuilt at the start of every evaluation block (restarts, phase switches
+ * and polishing rewrite the vector between blocks; within a block only the
+ * dual step writes it, and k_dual_long_finish keeps the copy current) */
+template <typename T>
+__global__ void k_hot_refresh(int H, const int *__restrict__ rows, const T *__restrict__ gat, T *hot,
+                              const CpalState *__restrict__ st) {
+    pdl_enter();
+    if (st->status) return;
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < H; h += gridDim.x * blockDim.x) hot[h] = gat[rows[h]];
+}
+
+/* The primal product with the long rows' gathered values in shared memory:
+ * every column of a power-law LP meets the long rows, so most of A^T's
+ * gathers land on those few entries; each block stages their compact copy
+ * (one coalesced read) and takes them from shared memory.  A^T's column
+ * indices come in a copy where an entry of long row h is stored as -1 - h. */
+constexpr int kHotBytes = 12288; /* at most 1,536 hot rows in FP64, 3,072 in FP32 */
+
+template <typename T, int S, bool MAJOR>
+__global__ void __launch_bounds__(kThreads) k_primal_hot(RowPlanDev plan, const int *__restrict__ rp,
+                                                         const int *__restrict__ ci_hot, const T *__restrict__ val,
+                                                         const T *__restrict__ gat, const T *__restrict__ hot,
+                                                         int nhot, PrimalArgs<T> a, const CpalState *__restrict__ st,
+                                                         const typename WeightT<T>::type *__restrict__ wt, int koff) {
+    pdl_enter();
+    if (st->status) return;
+    __shared__ RowBlockSmem<S, 1, T> sm;
+    __shared__ T shot[kHotBytes / sizeof(T)];
+    for (int h = threadIdx.x; h < nhot; h += kThreads) shot[h] = __ldcg(hot + h);
+    __syncthreads();
+    PrimalEpi<T, MAJOR> epi;
+    epi.a = a;
+    load_coefs(st, epi.k);
+    epi.w = wt[koff].w;
+    epi.omw = wt[koff].omw;
+    auto g = [&](int c, T *out) { out[0] = c >= 0 ? __ldg(gat + c) : shot[-1 - c]; };
+    Red<0, 0> red;
+    rowblock_run<S, 1, T>(plan, rp, ci_hot, val, g, epi, red, sm);
 }
 
 /* Halpern weights for the block starting at st->inner (one block). */

@@ -237,11 +237,27 @@ class CpalSolver {
     int sh_b1_ = 0, sh_b2_ = 0, sh_b3_ = 0;
     template <typename T>
     ShortDev<T> short_dev() const;
+    template <typename T>
+    T *hot_ptr() const;
+    /* shared-memory hot values in the primal product of the phase in T:
+     * measured faster for FP64 and slower for FP32 on the large LP, so by
+     * default only the FP64 phase uses them */
+    template <typename T>
+    bool hot_in() const {
+        return use_hot_ && (std::is_same<T, double>::value || O_.primal_hot_rows == 1);
+    }
     int *pan_rows_ = nullptr, *pan_pmap_ = nullptr;
-    int4 *pan_seg_ = nullptr, *pan_cta_ = nullptr;
+    int4 *pan_seg_ = nullptr, *pan_piece_ = nullptr, *pan_cta_ = nullptr;
     uint16_t *pan_off_ = nullptr;
     double *pan_v64_ = nullptr, *pan_part64_ = nullptr;
     float *pan_v32_ = nullptr, *pan_part32_ = nullptr;
+    /* the same long rows' gathered values in shared memory in the primal
+     * product (k_primal_hot): A^T's column indices with entry -1 - h for long
+     * row h, and the compact copy of those values */
+    bool use_hot_ = false;
+    int *At_ci_hot_ = nullptr;
+    double *hot64_ = nullptr;
+    float *hot32_ = nullptr;
     template <typename T>
     PanelDev<T> panel_dev() const;
     /* kernels one iteration launches */
@@ -289,6 +305,15 @@ IterVecs<float> &CpalSolver::vecs<float>() {
 }
 
 template <>
+double *CpalSolver::hot_ptr<double>() const {
+    return hot64_;
+}
+template <>
+float *CpalSolver::hot_ptr<float>() const {
+    return hot32_;
+}
+
+template <>
 ShortDev<double> CpalSolver::short_dev<double>() const {
     return ShortDev<double>{sh_r1_, sh_c1_, sh_v64_, sh_r2_, sh_r3_, (int)sh_r1_h.size(), (int)sh_r2_h.size(),
                             (int)sh_r3_h.size(), sh_b1_, sh_b2_, sh_b3_};
@@ -301,12 +326,14 @@ ShortDev<float> CpalSolver::short_dev<float>() const {
 
 template <>
 PanelDev<double> CpalSolver::panel_dev<double>() const {
-    return PanelDev<double>{pan_rows_, pan_seg_, pan_cta_, pan_v64_, pan_off_, pan_part64_,
+    return PanelDev<double>{pan_rows_, pan_seg_, pan_piece_, pan_cta_, pan_v64_, pan_off_, pan_part64_,
+                            hot_in<double>() ? hot64_ : nullptr,
                             pan_host_.H, pan_host_.P, pan_host_.W, (int)(pan_host_.cta.size() / 4)};
 }
 template <>
 PanelDev<float> CpalSolver::panel_dev<float>() const {
-    return PanelDev<float>{pan_rows_, pan_seg_, pan_cta_, pan_v32_, pan_off_, pan_part32_,
+    return PanelDev<float>{pan_rows_, pan_seg_, pan_piece_, pan_cta_, pan_v32_, pan_off_, pan_part32_,
+                           hot_in<float>() ? hot32_ : nullptr,
                            pan_host_.H, pan_host_.P, pan_host_.W, (int)(pan_host_.cta.size() / 4)};
 }
 
@@ -476,8 +503,14 @@ void CpalSolver::alloc_all() {
         pan_rows_ = arena_.take<int>(pan_host_.rows.size());
         pan_pmap_ = arena_.take<int>(len);
         pan_seg_ = arena_.take<int4>(pan_host_.seg.size() / 4);
+        pan_piece_ = arena_.take<int4>(pan_host_.piece.size() / 4);
         pan_cta_ = arena_.take<int4>(pan_host_.cta.size() / 4);
         pan_off_ = arena_.take<uint16_t>(len);
+        if (use_hot_) {
+            At_ci_hot_ = arena_.take<int>(nnz + kPad);
+            hot64_ = arena_.take<double>(pan_host_.H);
+            if (fp32_phase_ && O_.primal_hot_rows == 1) hot32_ = arena_.take<float>(pan_host_.H);
+        }
         pan_v64_ = arena_.take<double>(len);
         pan_part64_ = arena_.take<double>(hp);
         if (fp32_phase_) {
@@ -581,6 +614,7 @@ void CpalSolver::upload() {
     A_.ev.hp = plan_rows(m_, prob_->constraint_matrix_row_pointers, S_ev_);
     At_.ev.hp = plan_rows(n_, At_host_.rp.data(), S_ev_);
     use_panels_ = false;
+    use_hot_ = false;
     if (m_ > 0 && O_.dual_panels != 0 && A_.it.hp.nlong > 0) {
         const int *rp = prob_->constraint_matrix_row_pointers;
         long long long_nnz = 0;
@@ -614,12 +648,18 @@ void CpalSolver::upload() {
                     sh_r3_h.push_back(r);
                 }
             }
+            use_hot_ = O_.primal_hot_rows != 0 && pan_host_.H > 0 &&
+                       pan_host_.H <= (int)(kHotBytes / sizeof(double));
+            /* the warp rows longest first, so that the longest start in the
+             * first round of the grid-stride loop */
+            std::stable_sort(sh_r3_h.begin(), sh_r3_h.end(),
+                             [&](int a, int b) { return rp[a + 1] - rp[a] > rp[b + 1] - rp[b]; });
             /* a fixed number of blocks per part, each looping over its rows */
             auto blocks = [](long long rows, long long per_block, long long cap) {
                 return (int)std::min<long long>((rows + per_block - 1) / per_block, cap);
             };
-            sh_b1_ = blocks((long long)sh_r1_h.size(), kThreads * kShortUnroll, 152 * 4);
-            sh_b2_ = blocks((long long)sh_r2_h.size(), kThreads / 8, 152 * 4);
+            sh_b1_ = blocks((long long)sh_r1_h.size(), kThreads * kShortUnroll, 152 * 3);
+            sh_b2_ = blocks((long long)sh_r2_h.size(), kThreads / 8, 152 * 1);
             sh_b3_ = blocks((long long)sh_r3_h.size(), kThreads / 32, 152 * 2);
             use_panels_ = pan_host_.H > 0;
         }
@@ -652,9 +692,25 @@ void CpalSolver::upload() {
         up(sh_c1_, sh_c1_h.data(), sh_c1_h.size() * sizeof(int));
         up(sh_r2_, sh_r2_h.data(), sh_r2_h.size() * sizeof(int));
         up(sh_r3_, sh_r3_h.data(), sh_r3_h.size() * sizeof(int));
+        if (use_hot_) {
+            std::vector<int> hot_id(m, -1);
+            for (int h = 0; h < pan_host_.H; ++h) hot_id[pan_host_.rows[h]] = h;
+            std::vector<int> cih(At_host_.ci.size());
+            const int nt = host_threads((long long)cih.size());
+            parallel_for(nt, [&](int t) {
+                const size_t k0 = cih.size() * t / nt, k1 = cih.size() * (t + 1) / nt;
+                for (size_t k = k0; k < k1; ++k) {
+                    const int r = At_host_.ci[k];
+                    cih[k] = hot_id[r] >= 0 ? -1 - hot_id[r] : r;
+                }
+            });
+            up(At_ci_hot_, cih.data(), cih.size() * sizeof(int));
+            PDAL_CUDA(cudaStreamSynchronize(stream_)); /* cih leaves scope */
+        }
         up(pan_rows_, pan_host_.rows.data(), pan_host_.rows.size() * sizeof(int));
         up(pan_pmap_, pan_host_.pmap.data(), len * sizeof(int));
         up(pan_seg_, pan_host_.seg.data(), pan_host_.seg.size() * sizeof(int));
+        up(pan_piece_, pan_host_.piece.data(), pan_host_.piece.size() * sizeof(int));
         up(pan_cta_, pan_host_.cta.data(), pan_host_.cta.size() * sizeof(int));
         up(pan_off_, pan_host_.off.data(), len * sizeof(uint16_t));
         /* (row, panel) pairs without a segment keep a zero partial */
@@ -1153,6 +1209,24 @@ void CpalSolver::launch_primal(int koff, bool major) {
     const T *gat = beta_on_ ? v.u : v.y;
     const T *Atv = matvals<T>(At_.v, At_.vf);
     const auto *wt = weights<T>(wt_, wtf_);
+    if (hot_in<T>()) {
+        T *hot = hot_ptr<T>();
+        const int nh = pan_host_.H;
+        /* the compact copy is rebuilt at the start of every block */
+        if (koff == 1) launch_pdl(k_hot_refresh<T>, grid_for(nh), stream_, nh, (const int *)pan_rows_, gat, hot,
+                                  (const CpalState *)st_);
+        PDAL_WITH_S(S_it_, {
+            if (major)
+                launch_pdl(k_primal_hot<T, SB, true>, At_.it.d.nblocks, stream_, At_.it.d, (const int *)At_.rp,
+                           (const int *)At_ci_hot_, Atv, gat, (const T *)hot, nh, pa, (const CpalState *)st_, wt,
+                           koff);
+            else
+                launch_pdl(k_primal_hot<T, SB, false>, At_.it.d.nblocks, stream_, At_.it.d, (const int *)At_.rp,
+                           (const int *)At_ci_hot_, Atv, gat, (const T *)hot, nh, pa, (const CpalState *)st_, wt,
+                           koff);
+        });
+        return;
+    }
     PDAL_WITH_S(S_it_, {
         if (major)
             launch_pdl(k_primal<T, SB, true>, At_.it.d.nblocks, stream_, At_.it.d, (const int *)At_.rp,
@@ -1483,7 +1557,7 @@ void CpalSolver::polish() {
         auto fpe = [&](const PolishEval &e) { return primal ? e.dx2 * s.pw : e.dy2 / s.pw; };
         for (;;) { /* solver.cu:3988-4051 (primal), 4063-4126 (dual) */
             launch_iteration<double>(1, true);
-            launches += iter_launches();
+            launches += iter_launches() + (hot_in<double>() ? 1 : 0);
             if (do_restart) {
                 s.fp = fpe(evaluate());
                 s.fp0 = s.fp;
@@ -1614,7 +1688,7 @@ void CpalSolver::run_loop() {
             exec = &exec64_;
         }
         PDAL_CUDA(cudaGraphLaunch(*exec, stream_));
-        launches += per_block * G;
+        launches += (per_block + ((fp32_phase_ ? hot_in<float>() : hot_in<double>()) ? 1 : 0)) * G;
         PDAL_CUDA(cudaMemcpyAsync(h_st_, st_, sizeof(CpalState), cudaMemcpyDeviceToHost, stream_));
         d2h += sizeof(CpalState);
         PDAL_CUDA(cudaStreamSynchronize(stream_));

@@ -60,6 +60,9 @@ WORKLOADS = {
                  "per row and column, 5% free variables"),
     "medium_lp": (dict(m=100_000, n=200_000, nnz=2_000_000, seed=1001),
                   "LP 100,000 x 200,000, ~2M nnz, same structure at 1/10 scale"),
+    # the size the full ncu captures run on: larger than L2, ~0.5 GB on the device
+    "half_lp": (dict(m=500_000, n=1_000_000, nnz=10_000_000, seed=1000),
+                "LP 500,000 x 1,000,000, ~10M nnz, same structure at 1/2 scale"),
 }
 ITERS_PER_STEP = 1000
 METRIC = "iteration HBM GB/s of the CP_AL iteration on the large LP (chosen form: FP32 + FP64 refinement)"

@@ -104,6 +104,12 @@ typedef struct {
                                      steps, stopping when the largest Ritz value moves by less than
                                      1e-8 relative over 16 steps -- and the FP64 form the power
                                      iteration */
+    int primal_staged;            /* the iteration's A^T u as a grid of one wave whose blocks walk
+                                     the row blocks and copy the next one into shared memory with
+                                     TMA bulk copies while they work on the current one: 1 = its
+                                     matrix slice, 2 = also its rows' epilogue inputs, 0 = off
+                                     (a block per row block, loads issued by the threads);
+                                     -1 (default) = off.  Results are bit-identical in every mode */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */

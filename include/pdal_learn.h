@@ -48,6 +48,24 @@ double pdal_mlp_loss_grad(pdal_mlp_t *mlp, int n, const float *X, const float *Y
  * BF16, products accumulated in FP32; bf16 == 0: FP32 throughout. */
 int pdal_mlp_predict(pdal_mlp_t *mlp, int n, const float *X, float *Y, int bf16);
 
+/* The transportation family on the device.  `count` instances of an S x D
+ * complete bipartite transportation LP (arc a = i*D + j, supply rows i, demand
+ * rows S + j, 0 <= x_a <= cap_a): costs and caps are count x (S*D), rhs is
+ * count x (S+D) (supplies, then demands), row-major host arrays.  For each
+ * instance the GPU forms the MLP's input (costs / 100, caps / 200, rhs / 100,
+ * standardised with xm, xs: in = 2 S D + S + D entries), runs the network
+ * (bf16 as in pdal_mlp_predict), decodes its output t = T * ys + ym
+ * (out = S D + S + D + 1 entries) into x = clip(t[:SD], 0, 1) * cap,
+ * y = 100 t[SD : SD+S+D], sigma = exp(t[last]), and evaluates the relative KKT
+ * error max(|A x - b| / (1 + |b|), |c'x - d(y)| / (1 + |c'x| + |d(y)|)),
+ * d(y) = b'y + sum min(c - A'y, 0) cap, of that point (kkt_pred) and of the
+ * cold start x = 0, y = 0 (kkt_cold).  Outputs are host arrays of count x
+ * (S*D), count x (S+D) and count entries. */
+int pdal_transport_warm_start(pdal_mlp_t *mlp, int S, int D, int count, const double *costs, const double *caps,
+                              const double *rhs, const double *xm, const double *xs, const double *ym,
+                              const double *ys, int bf16, double *x, double *y, double *sigma, double *kkt_pred,
+                              double *kkt_cold);
+
 const char *pdal_mlp_last_error(void);
 
 #ifdef __cplusplus

@@ -748,6 +748,7 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->panel_width = 0;
     o->primal_hot_rows = -1;
     o->power_method = -1;
+    o->primal_staged = -1;
 }
 
 /* LP/CP_AL/src/utils.cu:361-394 (reflection coefficient without the

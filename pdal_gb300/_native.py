@@ -198,6 +198,7 @@ class CpalOptions(C.Structure):
         ("panel_width", C.c_int),
         ("primal_hot_rows", C.c_int),
         ("power_method", C.c_int),
+        ("primal_staged", C.c_int),
     ]
 
 
@@ -533,6 +534,8 @@ LEARN_SYMBOLS = {
     "pdal_mlp_loss_grad": (C.c_double, [C.c_void_p, C.c_int, _fp, _fp, _fp]),
     "pdal_mlp_predict": (C.c_int, [C.c_void_p, C.c_int, _fp, _fp, C.c_int]),
     "pdal_mlp_last_error": (C.c_char_p, []),
+    "pdal_transport_warm_start": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [_dp] * 7 + [C.c_int]
+                                  + [_dp] * 5),
 }
 
 

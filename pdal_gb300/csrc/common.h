@@ -55,7 +55,10 @@ class Arena {
     }
     template <typename T>
     T *take(size_t count) {
-        size_t bytes = ((count * sizeof(T)) + 255) & ~size_t(255);
+        /* 256-byte aligned, with at least 64 bytes of slack after the last
+         * element: kernels that copy 16-byte-aligned windows (bulk copies,
+         * 128-bit loads) may read up to 15 bytes past an array's end */
+        size_t bytes = ((count * sizeof(T)) + 64 + 255) & ~size_t(255);
         if (bytes == 0) bytes = 256;
         if (measuring_) {
             off_ += bytes;

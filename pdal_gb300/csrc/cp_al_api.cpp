@@ -353,6 +353,7 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->panel_width = 0;
     o->primal_hot_rows = -1;
     o->power_method = -1;
+    o->primal_staged = -1;
 }
 
 /* Each variable is read the way the reference reads it

@@ -28,6 +28,7 @@
 #pragma once
 
 #include "cpal_control.h"
+#include "bulk_copy.cuh"
 #include "rowblock.cuh"
 
 #include <type_traits>
@@ -146,10 +147,12 @@ struct PrimalEpi : NoLongRed {
     PrimalArgs<T> a;
     Coefs<T> k;
     T w, omw;
-    __device__ __forceinline__ void operator()(int j, const T *s, Red<0, 0> &) const {
-        const T xj = a.x[j];
-        const T t = xj - k.tau * (a.c[j] - s[0]);
-        const T proj = vmax(a.lb[j], vmin(t, a.ub[j]));
+    /* row j with product entry s and its inputs x, c, lb, ub, x0 already read
+     * (from global memory, or from a staged copy in shared memory) */
+    __device__ __forceinline__ void apply(int j, T s, T xj, T cj, T lbj, T ubj,
+                                          typename AnchorT<T>::type x0j) const {
+        const T t = xj - k.tau * (cj - s);
+        const T proj = vmax(lbj, vmin(t, ubj));
         const T xb = T(2) * proj - xj;
         a.xbar[j] = xb;
         if (MAJOR) {
@@ -157,7 +160,10 @@ struct PrimalEpi : NoLongRed {
             a.lam[j] = (proj - t) * k.inv_tau;
         }
         const T refl = k.r * xb + (T(1) - k.r) * xj;
-        a.x[j] = halpern(w, omw, refl, a.x0[j]);
+        a.x[j] = halpern(w, omw, refl, x0j);
+    }
+    __device__ __forceinline__ void operator()(int j, const T *s, Red<0, 0> &) const {
+        apply(j, s[0], a.x[j], a.c[j], a.lb[j], a.ub[j], a.x0[j]);
     }
 };
 
@@ -178,6 +184,219 @@ __global__ void __launch_bounds__(kThreads) k_primal(RowPlanDev plan, const int 
     auto g = [&](int c, T *out) { out[0] = __ldg(gat + c); };
     Red<0, 0> red;
     rowblock_run<S, 1, T>(plan, rp, ci, val, g, epi, red, sm);
+}
+
+/* ------------------------------------------------------------------ */
+/* the primal product with TMA-staged row blocks                       */
+/* ------------------------------------------------------------------ */
+
+/* Row-vector entries staged per row block: rows [r0, r1) are copied from
+ * r0 rounded down to a multiple of 4, so at most kMaxRowsPerBlock + 7. */
+constexpr int kStageRows = kMaxRowsPerBlock + 8;
+
+/* the epilogue's inputs of a staged row block (ROWS), or nothing */
+template <typename T, bool ROWS>
+struct StageRows {
+    T x[kStageRows], c[kStageRows], lb[kStageRows], ub[kStageRows];
+    typename AnchorT<T>::type x0[kStageRows];
+};
+template <typename T>
+struct StageRows<T, false> {};
+
+/* One staged row block: the slice of A^T (column indices, values, row
+ * pointers) and, with ROWS, the epilogue's inputs for its rows, each copied
+ * by one bulk copy from a 16-byte-aligned start (nonzero k sits at
+ * k - (k0 & ~3), row j at j - (r0 & ~3)). */
+template <int S, typename T, bool ROWS>
+struct __align__(16) PrimalStage {
+    int ci[S + 8];
+    T val[S + 8];
+    int rp[kStageRows];
+    StageRows<T, ROWS> rows;
+};
+
+template <int S, typename T, bool ROWS>
+struct __align__(16) PrimalTmaSmem {
+    PrimalStage<S, T, ROWS> st[2];
+    /* the gathered entries; in FP32 they overwrite the stage's column
+     * indices in place (each thread rewrites only the entries it read) */
+    T g[sizeof(T) == 4 ? 4 : S + 8];
+    double red[kThreads / 32];
+    uint64_t bar[2];
+    int last;
+    int stop;
+};
+
+/* Thread 0 arms `bar` and issues the bulk copies of row block `blk`. */
+template <int S, typename T, bool ROWS>
+__device__ __forceinline__ void primal_stage_issue(const RowPlanDev &plan, const int *__restrict__ rp,
+                                                   const int *__restrict__ ci, const T *__restrict__ val,
+                                                   const PrimalArgs<T> &a, int blk, PrimalStage<S, T, ROWS> &s,
+                                                   uint64_t *bar) {
+    using A = typename AnchorT<T>::type;
+    const int4 d = plan.desc[blk];
+    const int kb = d.z & ~3, ke = (d.w + 3) & ~3;
+    const bool rows = d.y >= d.x;
+    const int rb = rows ? (d.x & ~3) : 0, re = rows ? ((d.y + 3) & ~3) : 0, rpe = rows ? ((d.y + 4) & ~3) : 0;
+    const unsigned nk = (unsigned)(ke - kb), nr = ROWS ? (unsigned)(re - rb) : 0u, np = (unsigned)(rpe - rb);
+    mbar_arrive_expect_tx(bar, nk * (unsigned)(sizeof(int) + sizeof(T)) + np * (unsigned)sizeof(int) +
+                                   nr * (unsigned)(4 * sizeof(T) + sizeof(A)));
+    if (nk) {
+        bulk_g2s(s.ci, ci + kb, nk * sizeof(int), bar);
+        bulk_g2s(s.val, val + kb, nk * sizeof(T), bar);
+    }
+    if (np) bulk_g2s(s.rp, rp + rb, np * sizeof(int), bar);
+    if constexpr (ROWS) {
+        if (nr) {
+            bulk_g2s(s.rows.x, a.x + rb, nr * sizeof(T), bar);
+            bulk_g2s(s.rows.c, a.c + rb, nr * sizeof(T), bar);
+            bulk_g2s(s.rows.lb, a.lb + rb, nr * sizeof(T), bar);
+            bulk_g2s(s.rows.ub, a.ub + rb, nr * sizeof(T), bar);
+            bulk_g2s(s.rows.x0, a.x0 + rb, nr * sizeof(A), bar);
+        }
+    }
+}
+
+/* The iteration's A^T u + primal epilogue as a grid of one wave: each block
+ * walks row blocks blockIdx.x, blockIdx.x + gridDim.x, ... and, while it
+ * gathers, reduces and finishes one, the TMA engine copies the next one's
+ * matrix slice (and, with ROWS, its rows' epilogue inputs) into the other
+ * stage buffer.  Same lane grouping, fused multiply-add chains and epilogue
+ * as k_primal, so the results are bit-identical to it.  A staging wait that
+ * runs out sets st->status = kStatusDeviceError and *err, and the block
+ * returns. */
+constexpr int kStatusDeviceError = 100;
+
+template <typename T, int S, bool MAJOR, bool ROWS>
+__global__ void __launch_bounds__(kThreads) k_primal_tma(RowPlanDev plan, const int *__restrict__ rp,
+                                                         const int *__restrict__ ci, const T *__restrict__ val,
+                                                         const T *__restrict__ gat, PrimalArgs<T> a, CpalState *st,
+                                                         const typename WeightT<T>::type *__restrict__ wt, int koff,
+                                                         int *err) {
+    constexpr int NT = kThreads;
+    constexpr int GIT = (S + 8 + NT - 1) / NT;
+    extern __shared__ __align__(16) unsigned char tma_smem[];
+    auto &sm = *reinterpret_cast<PrimalTmaSmem<S, T, ROWS> *>(tma_smem);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&sm.bar[0], 1);
+        mbar_init(&sm.bar[1], 1);
+        fence_mbar_init();
+    }
+    pdl_enter();
+    /* one read of the status for the whole block: another block may set it
+     * while this one starts */
+    if (tid == 0) sm.stop = st->status;
+    __syncthreads();
+    if (sm.stop) return;
+    PrimalEpi<T, MAJOR> epi;
+    epi.a = a;
+    load_coefs(st, epi.k);
+    epi.w = wt[koff].w;
+    epi.omw = wt[koff].omw;
+    int blk = blockIdx.x;
+    if (tid == 0 && blk < plan.nblocks)
+        primal_stage_issue<S, T, ROWS>(plan, rp, ci, val, a, blk, sm.st[0], &sm.bar[0]);
+    uint32_t parity = 0; /* bit b: the phase of bar[b] to wait for next */
+    for (int i = 0; blk < plan.nblocks; ++i, blk += gridDim.x) {
+        const int b = i & 1;
+        const int nxt = blk + gridDim.x;
+        if (tid == 0 && nxt < plan.nblocks) {
+            fence_proxy_async_smem();
+            primal_stage_issue<S, T, ROWS>(plan, rp, ci, val, a, nxt, sm.st[b ^ 1], &sm.bar[b ^ 1]);
+        }
+        const uint32_t pb = (parity >> b) & 1u;
+        const bool ok = mbar_wait(&sm.bar[b], pb, kStageWaitNs);
+        parity ^= 1u << b;
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+                atomicExch(&st->status, kStatusDeviceError);
+                /* let the copies still in flight land before the block exits */
+                mbar_wait(&sm.bar[b], pb, kStageWaitNs);
+                if (nxt < plan.nblocks) mbar_wait(&sm.bar[b ^ 1], (parity >> (b ^ 1)) & 1u, kStageWaitNs);
+            }
+            return;
+        }
+        PrimalStage<S, T, ROWS> &s = sm.st[b];
+        T *gbuf = sizeof(T) == 4 ? reinterpret_cast<T *>(s.ci) : sm.g;
+        const int4 d = plan.desc[blk];
+        const int k0 = d.z, k1 = d.w, kb = k0 & ~3;
+        {
+            /* every column index first, then every gather, so that a thread
+             * has all its loads of u in flight at once */
+            int cols[GIT];
+            T gv[GIT];
+#pragma unroll
+            for (int it = 0; it < GIT; ++it) {
+                const int e = kb + it * NT + tid;
+                cols[it] = (e >= k0 && e < k1) ? s.ci[it * NT + tid] : -1;
+            }
+#pragma unroll
+            for (int it = 0; it < GIT; ++it) gv[it] = cols[it] >= 0 ? __ldg(gat + cols[it]) : T(0);
+#pragma unroll
+            for (int it = 0; it < GIT; ++it)
+                if (it * NT + tid < S + 8) gbuf[it * NT + tid] = gv[it];
+        }
+        __syncthreads();
+        if (d.y >= d.x) {
+            const int r0 = d.x, nrows = d.y - d.x, ro = r0 - (r0 & ~3);
+            auto finish = [&](int row, T acc) {
+                if constexpr (ROWS) {
+                    const int q = ro + row;
+                    epi.apply(r0 + row, acc, s.rows.x[q], s.rows.c[q], s.rows.lb[q], s.rows.ub[q], s.rows.x0[q]);
+                } else {
+                    const T sv[1] = {acc};
+                    Red<0, 0> lr;
+                    epi(r0 + row, sv, lr);
+                }
+            };
+            if (nrows <= NT) {
+                int g = 32;
+                while (g > 1 && g * nrows > NT) g >>= 1;
+                const int row = tid / g, lane = tid & (g - 1);
+                T acc = T(0);
+                if (row < nrows) {
+                    const int e = s.rp[ro + row + 1] - kb;
+                    for (int kk = s.rp[ro + row] - kb + lane; kk < e; kk += g) acc = vfma(s.val[kk], gbuf[kk], acc);
+                }
+                for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, g);
+                if (row < nrows && lane == 0) finish(row, acc);
+            } else {
+                for (int row = tid; row < nrows; row += NT) {
+                    T acc = T(0);
+                    const int e = s.rp[ro + row + 1] - kb;
+                    for (int kk = s.rp[ro + row] - kb; kk < e; ++kk) acc = vfma(s.val[kk], gbuf[kk], acc);
+                    finish(row, acc);
+                }
+            }
+        } else {
+            /* one S-slice of a long row: as rowblock_run_at's LONG piece */
+            const int lid = ~d.y;
+            const int4 li = plan.linfo[lid];
+            const int piece = (k0 - li.w) / S;
+            T acc[1] = {T(0)};
+            for (int kk = k0 - kb + tid; kk < k1 - kb; kk += NT) acc[0] = vfma(s.val[kk], gbuf[kk], acc[0]);
+            block_sum_t<1, T>(acc, reinterpret_cast<T *>(sm.red));
+            if (tid == 0) {
+                plan.lpart[(size_t)(li.z + piece) * kLongStride] = (double)acc[0];
+                __threadfence();
+                const unsigned prev = atomicAdd(&plan.lcount[lid], 1u);
+                sm.last = (prev == (unsigned)(li.y - 1));
+            }
+            __syncthreads();
+            if (sm.last && tid == 0) {
+                __threadfence();
+                double tot = 0.0;
+                for (int q = 0; q < li.y; ++q) tot += __ldcg(&plan.lpart[(size_t)(li.z + q) * kLongStride]);
+                plan.lcount[lid] = 0u;
+                const T sv[1] = {(T)tot};
+                Red<0, 0> lr;
+                epi(li.x, sv, lr);
+            }
+        }
+        __syncthreads(); /* stage b and the gathered entries are free for the next refill */
+    }
 }
 
 template <typename T>
@@ -570,10 +789,13 @@ __global__ void k_hot_refresh(int H, const int *__restrict__ rows, const T *__re
 
 /* The primal product with the long rows' gathered values in shared memory:
  * every column of a power-law LP meets the long rows, so most of A^T's
- * gathers land on those few entries; each block stages their compact copy
- * (one coalesced read) and takes them from shared memory.  A^T's column
- * indices come in a copy where an entry of long row h is stored as -1 - h. */
-constexpr int kHotBytes = 12288; /* at most 1,536 hot rows in FP64, 3,072 in FP32 */
+ * gathers land on those few entries.  Each block stages their compact copy
+ * once (one coalesced read) and then walks row blocks blockIdx.x,
+ * blockIdx.x + gridDim.x, ... (a grid of one wave), taking those entries from
+ * shared memory: a warp's 32 gathers into the copy cost a few bank cycles
+ * instead of up to 32 L1 tag lookups.  A^T's column indices come in a copy
+ * where an entry of long row h is stored as -1 - h. */
+constexpr int kHotRows = 1536;
 
 template <typename T, int S, bool MAJOR>
 __global__ void __launch_bounds__(kThreads) k_primal_hot(RowPlanDev plan, const int *__restrict__ rp,
@@ -584,7 +806,7 @@ __global__ void __launch_bounds__(kThreads) k_primal_hot(RowPlanDev plan, const 
     pdl_enter();
     if (st->status) return;
     __shared__ RowBlockSmem<S, 1, T> sm;
-    __shared__ T shot[kHotBytes / sizeof(T)];
+    __shared__ T shot[kHotRows];
     for (int h = threadIdx.x; h < nhot; h += kThreads) shot[h] = __ldcg(hot + h);
     __syncthreads();
     PrimalEpi<T, MAJOR> epi;
@@ -594,7 +816,10 @@ __global__ void __launch_bounds__(kThreads) k_primal_hot(RowPlanDev plan, const 
     epi.omw = wt[koff].omw;
     auto g = [&](int c, T *out) { out[0] = c >= 0 ? __ldg(gat + c) : shot[-1 - c]; };
     Red<0, 0> red;
-    rowblock_run<S, 1, T>(plan, rp, ci_hot, val, g, epi, red, sm);
+    for (int blk = blockIdx.x; blk < plan.nblocks; blk += gridDim.x) {
+        rowblock_run_at<S, 1, T>(blk, plan, rp, ci_hot, val, g, epi, red, sm);
+        __syncthreads(); /* the next row block restages sm */
+    }
 }
 
 /* Halpern weights for the block starting at st->inner (one block). */

@@ -255,6 +255,15 @@ class CpalSolver {
      * product (k_primal_hot): A^T's column indices with entry -1 - h for long
      * row h, and the compact copy of those values */
     bool use_hot_ = false;
+    int hot_grid_[2][2] = {{0, 0}, {0, 0}}; /* [FP64?][major?]: one wave of k_primal_hot */
+    /* the staged primal product (k_primal_tma): one wave per variant, and
+     * the flag a staging wait that ran out sets */
+    bool use_staged_ = false;
+    int staged_grid_[2][2] = {{0, 0}, {0, 0}};
+    int *dev_err_ = nullptr;
+    void setup_staged();
+    bool staged_rows() const { return O_.primal_staged == 2; }
+    void check_device_error();
     int *At_ci_hot_ = nullptr;
     double *hot64_ = nullptr;
     float *hot32_ = nullptr;
@@ -489,6 +498,7 @@ void CpalSolver::alloc_all() {
     alloc_plan(At_.it);
     alloc_plan(A_.ev);
     alloc_plan(At_.ev);
+    dev_err_ = arena_.take<int>(1);
     if (use_panels_) {
         const size_t len = (size_t)pan_host_.len, hp = (size_t)pan_host_.H * pan_host_.P;
         const size_t n1 = std::max<size_t>(sh_r1_h.size(), 1), n2 = std::max<size_t>(sh_r2_h.size(), 1),
@@ -597,6 +607,50 @@ void CpalSolver::alloc_all() {
     lz_j_ = arena_.take<int>(1);
 }
 
+/* The staged primal product needs more than 48 KB of dynamic shared memory
+ * per block; its grid is one wave at the occupancy that leaves. */
+void CpalSolver::setup_staged() {
+    use_staged_ = O_.primal_staged > 0 && n_ > 0;
+    if (!use_staged_) return;
+    int dev = 0, sms = 0;
+    PDAL_CUDA(cudaGetDevice(&dev));
+    PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    auto wave = [&](auto kernel, size_t smem) {
+        PDAL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int occ = 0;
+        PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kThreads, smem));
+        if (occ < 1) throw Error("staged primal product does not fit on this device");
+        return std::max(1, std::min(At_.it.hp.nblocks, occ * sms));
+    };
+    PDAL_WITH_S(S_it_, {
+        if (staged_rows()) {
+            constexpr size_t s32 = sizeof(PrimalTmaSmem<SB, float, true>),
+                             s64 = sizeof(PrimalTmaSmem<SB, double, true>);
+            staged_grid_[0][0] = wave(k_primal_tma<float, SB, false, true>, s32);
+            staged_grid_[0][1] = wave(k_primal_tma<float, SB, true, true>, s32);
+            staged_grid_[1][0] = wave(k_primal_tma<double, SB, false, true>, s64);
+            staged_grid_[1][1] = wave(k_primal_tma<double, SB, true, true>, s64);
+        } else {
+            constexpr size_t s32 = sizeof(PrimalTmaSmem<SB, float, false>),
+                             s64 = sizeof(PrimalTmaSmem<SB, double, false>);
+            staged_grid_[0][0] = wave(k_primal_tma<float, SB, false, false>, s32);
+            staged_grid_[0][1] = wave(k_primal_tma<float, SB, true, false>, s32);
+            staged_grid_[1][0] = wave(k_primal_tma<double, SB, false, false>, s64);
+            staged_grid_[1][1] = wave(k_primal_tma<double, SB, true, false>, s64);
+        }
+    });
+}
+
+/* A staging wait of k_primal_tma that ran out stops the solve
+ * (status kStatusDeviceError) and is reported here as an error. */
+void CpalSolver::check_device_error() {
+    if (!dev_err_) return;
+    int e = 0;
+    PDAL_CUDA(cudaMemcpyAsync(&e, dev_err_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    if (e) throw Error("a staged copy of the primal product did not complete in time; the solve was stopped");
+}
+
 void CpalSolver::upload() {
     const double t_up = now_sec();
     if (O_.device >= 0) PDAL_CUDA(cudaSetDevice(O_.device));
@@ -649,7 +703,7 @@ void CpalSolver::upload() {
                 }
             }
             use_hot_ = O_.primal_hot_rows != 0 && pan_host_.H > 0 &&
-                       pan_host_.H <= (int)(kHotBytes / sizeof(double));
+                       pan_host_.H <= kHotRows;
             /* the warp rows longest first, so that the longest start in the
              * first round of the grid-stride loop */
             std::stable_sort(sh_r3_h.begin(), sh_r3_h.end(),
@@ -668,6 +722,8 @@ void CpalSolver::upload() {
     alloc_all();
     arena_.reserve_measured();
     alloc_all();
+    PDAL_CUDA(cudaMemsetAsync(dev_err_, 0, sizeof(int), stream_));
+    setup_staged();
 
     const size_t n = n_, m = m_, nnz = nnz_;
     auto up = [&](void *dst, const void *src, size_t b) {
@@ -706,6 +762,20 @@ void CpalSolver::upload() {
             });
             up(At_ci_hot_, cih.data(), cih.size() * sizeof(int));
             PDAL_CUDA(cudaStreamSynchronize(stream_)); /* cih leaves scope */
+            int dev = 0, sms = 0;
+            PDAL_CUDA(cudaGetDevice(&dev));
+            PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            auto wave = [&](auto kernel) {
+                int occ = 0;
+                PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kThreads, 0));
+                return std::max(1, std::min(At_.it.hp.nblocks, std::max(1, occ) * sms));
+            };
+            PDAL_WITH_S(S_it_, {
+                hot_grid_[0][0] = wave(k_primal_hot<float, SB, false>);
+                hot_grid_[0][1] = wave(k_primal_hot<float, SB, true>);
+                hot_grid_[1][0] = wave(k_primal_hot<double, SB, false>);
+                hot_grid_[1][1] = wave(k_primal_hot<double, SB, true>);
+            });
         }
         up(pan_rows_, pan_host_.rows.data(), pan_host_.rows.size() * sizeof(int));
         up(pan_pmap_, pan_host_.pmap.data(), len * sizeof(int));
@@ -1216,14 +1286,38 @@ void CpalSolver::launch_primal(int koff, bool major) {
         if (koff == 1) launch_pdl(k_hot_refresh<T>, grid_for(nh), stream_, nh, (const int *)pan_rows_, gat, hot,
                                   (const CpalState *)st_);
         PDAL_WITH_S(S_it_, {
+            const int *grid = hot_grid_[std::is_same<T, double>::value ? 1 : 0];
             if (major)
-                launch_pdl(k_primal_hot<T, SB, true>, At_.it.d.nblocks, stream_, At_.it.d, (const int *)At_.rp,
+                launch_pdl(k_primal_hot<T, SB, true>, grid[1], stream_, At_.it.d, (const int *)At_.rp,
                            (const int *)At_ci_hot_, Atv, gat, (const T *)hot, nh, pa, (const CpalState *)st_, wt,
                            koff);
             else
-                launch_pdl(k_primal_hot<T, SB, false>, At_.it.d.nblocks, stream_, At_.it.d, (const int *)At_.rp,
+                launch_pdl(k_primal_hot<T, SB, false>, grid[0], stream_, At_.it.d, (const int *)At_.rp,
                            (const int *)At_ci_hot_, Atv, gat, (const T *)hot, nh, pa, (const CpalState *)st_, wt,
                            koff);
+        });
+        return;
+    }
+    if (use_staged_) {
+        PDAL_WITH_S(S_it_, {
+            const int *grid = staged_grid_[std::is_same<T, double>::value ? 1 : 0];
+            auto go = [&](auto kernel, size_t smem, int g) {
+                launch_pdl_cfg(kernel, g, kThreads, smem, stream_, At_.it.d, (const int *)At_.rp,
+                               (const int *)At_.ci, Atv, gat, pa, st_, wt, koff, dev_err_);
+            };
+            if (staged_rows()) {
+                const size_t smem = sizeof(PrimalTmaSmem<SB, T, true>);
+                if (major)
+                    go(k_primal_tma<T, SB, true, true>, smem, grid[1]);
+                else
+                    go(k_primal_tma<T, SB, false, true>, smem, grid[0]);
+            } else {
+                const size_t smem = sizeof(PrimalTmaSmem<SB, T, false>);
+                if (major)
+                    go(k_primal_tma<T, SB, true, false>, smem, grid[1]);
+                else
+                    go(k_primal_tma<T, SB, false, false>, smem, grid[0]);
+            }
         });
         return;
     }
@@ -1720,6 +1814,7 @@ void CpalSolver::run_loop() {
                    q.restarts, fp32_phase_ ? "fp32" : "fp64");
             fflush(stdout);
         }
+        if (h_st_->status == kStatusDeviceError) check_device_error();
         if (h_st_->status) break;
         /* the device enforces the time limit; this host guard only covers a
          * device clock that does not advance */
@@ -1794,6 +1889,7 @@ void CpalSolver::fetch_scaling(double *vals, double *rsc, double *csc, double *b
 }
 
 void CpalSolver::download(cp_al_result_t *res, bool vectors) {
+    check_device_error();
     const CpalState &s = host_state;
     res->num_variables = n_;
     res->num_constraints = m_;

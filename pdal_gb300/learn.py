@@ -193,20 +193,36 @@ class WarmStart:
         T = self.mlp.predict((X - self.xm) / self.xs, bf16=bf16).astype(np.float64)
         return T * self.ys + self.ym
 
+    def predict_device(self, items: list[LPData], bf16: bool = True):
+        """The whole prediction on the GPU (pdal_transport_warm_start):
+        features, network, decoding and the KKT error of the predicted point
+        and of the cold start.  Returns (x, y, sigma, kkt_pred, kkt_cold) as
+        arrays over the instances."""
+        S, D = self.S, self.D
+        n, m = S * D, S + D
+        k = len(items)
+        c = np.ascontiguousarray(np.stack([np.asarray(d.c, dtype=np.float64) for d in items]))
+        u = np.ascontiguousarray(np.stack([np.asarray(d.var_ub, dtype=np.float64) for d in items]))
+        b = np.ascontiguousarray(np.stack([np.asarray(d.con_ub, dtype=np.float64) for d in items]))
+        x = np.empty((k, n))
+        y = np.empty((k, m))
+        sig, kp, kc = np.empty(k), np.empty(k), np.empty(k)
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        xm, xs, ym, ys = f64(self.xm), f64(self.xs), f64(self.ym), f64(self.ys)
+        P = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        lib = self.mlp.lib
+        rc = lib.pdal_transport_warm_start(self.mlp.h, S, D, k, P(c), P(u), P(b), P(xm), P(xs), P(ym), P(ys),
+                                           1 if bf16 else 0, P(x), P(y), P(sig), P(kp), P(kc))
+        if rc != 0:
+            raise RuntimeError(lib.pdal_mlp_last_error().decode())
+        return x, y, sig, kp, kc
+
     def predict(self, items: list[LPData], bf16: bool = True):
         """Warm starts, initial sigmas, whether each prediction was kept
         (False: its residual was worse than the cold start's) and the
-        predicted points' KKT errors."""
-        T = self.raw_predict(items, bf16)
-        xs, ys, sig, used, kkt = [], [], [], [], []
-        for d, t in zip(items, T):
-            x, y, s = decode(d, t, self.S, self.D)
-            m = len(d.con_ub)
-            k = point_kkt(d, x, y)
-            ok = k < point_kkt(d, np.zeros_like(x), np.zeros(m))
-            xs.append(x if ok else None)
-            ys.append(y if ok else None)
-            sig.append(s if ok else 0.0)
-            used.append(ok)
-            kkt.append(k)
-        return xs, ys, np.array(sig), np.array(used), np.array(kkt)
+        predicted points' KKT errors, all computed on the GPU."""
+        x, y, sig, kp, kc = self.predict_device(items, bf16)
+        used = kp < kc
+        xs = [x[i] if used[i] else None for i in range(len(items))]
+        ys = [y[i] if used[i] else None for i in range(len(items))]
+        return xs, ys, np.where(used, sig, 0.0), used, kp

@@ -174,6 +174,53 @@ def test_badly_scaled_zipf_panels_iterates_match(lp_lib, opts):
         assert err < 1e-8, err
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refine"])
+def test_primal_hot_rows_change_nothing(lp_lib, precision):
+    """Taking the long rows' entries of the gathered dual vector from shared
+    memory in A^T u changes where a value is read, not the value or the order
+    of the sums: bit-identical iterates with and without it, in both forms."""
+    d = I.zipf_lp(20_000, 40_000, 400_000, seed=1002)
+    p = {"eps": 1e-14, "iteration_limit": 1200, "sv_max_iter": 200, "time_limit": 120}
+    base = {"al_lambda": 0.0, "precision": precision, "dual_panels": 1, "panel_width": 4096,
+            "fp32_switch_tol": 1e-4, "fp32_stall_evals": 2}
+    a = lp.solve(d, p, {**base, "primal_hot_rows": 0})
+    b = lp.solve(d, p, {**base, "primal_hot_rows": 1})
+    assert a.stats["panel_rows"] > 0
+    assert a.iterations == b.iterations and a.stats["fp32_iterations"] == b.stats["fp32_iterations"]
+    assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refine"])
+@pytest.mark.parametrize("budget", [256, 2048])
+def test_staged_primal_product_changes_nothing(lp_lib, precision, budget):
+    """The staged primal product (one wave of blocks, each row block's slice
+    and row inputs copied ahead by TMA) keeps k_primal's lane groups and
+    summation order: bit-identical iterates with and without it, on an LP
+    with empty, one-entry and long columns (pieces of the row-block budget)."""
+    d = I.zipf_lp(20_000, 40_000, 400_000, seed=1002)
+    rp, ci, v, (m, n) = d.csr()
+    # two dense columns: rows of A^T long enough to be split into pieces
+    extra = np.arange(0, m, 3)
+    rows = np.repeat(np.arange(m), np.diff(rp))
+    keep = ~np.isin(ci, [5, 13])
+    rows = np.concatenate([rows[keep], extra, extra])
+    cols = np.concatenate([ci[keep], np.full(extra.size, 5), np.full(extra.size, 13)])
+    vals = np.concatenate([v[keep], np.ones(extra.size), -np.ones(extra.size)])
+    import scipy.sparse as sp
+
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(m, n))
+    A.sort_indices()
+    d.A = (A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data, (m, n))
+    p = {"eps": 1e-14, "iteration_limit": 1000, "sv_max_iter": 200, "time_limit": 120}
+    base = {"al_lambda": 0.0, "precision": precision, "spmv_nnz_per_block": budget, "fp32_switch_tol": 1e-4,
+            "fp32_stall_evals": 2}
+    a = lp.solve(d, p, {**base, "primal_staged": 0})
+    for mode in (1, 2):
+        b = lp.solve(d, p, {**base, "primal_staged": mode})
+        assert a.iterations == b.iterations and a.stats["fp32_iterations"] == b.stats["fp32_iterations"]
+        assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
+
+
 def test_panels_fp32_form_reaches_tolerance(lp_lib):
     """Chosen form (FP32 phase, then FP64) with the panel path: same status and
     objective as the oracle at relative KKT 1e-7."""

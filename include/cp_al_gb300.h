@@ -110,6 +110,13 @@ typedef struct {
                                      matrix slice, 2 = also its rows' epilogue inputs, 0 = off
                                      (a block per row block, loads issued by the threads);
                                      -1 (default) = off.  Results are bit-identical in every mode */
+    int infeasibility_detection;  /* nonzero: at every evaluation, test the iterates' displacement from
+                                     the restart anchor as infeasibility certificates and stop with
+                                     TERMINATION_REASON_PRIMAL_INFEASIBLE or _DUAL_INFEASIBLE (the ray
+                                     fields of the result filled).  The reference has the formulas
+                                     (LP/CP_AL/src/utils.cu:919-1029, 281-297) but never calls them:
+                                     default 0, as there.  Single-LP solver only */
+    double eps_infeasible;        /* tolerance of those tests (default 1e-8) */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */

@@ -668,11 +668,78 @@ struct Solver {
         restarts++;
         restarts_to[to_current ? 1 : to_halpern ? 2 : 0]++;
     }
+    /* Infeasibility certificates: an opt-in extension of this library.  The
+     * reference computes these quantities (compute_infeasibility_information,
+     * LP/CP_AL/src/utils.cu:919-1029) but never calls that function, and its
+     * termination test (utils.cu:298-317) checks only optimality and the
+     * limits.  The ray estimates are the iterates' displacement from the
+     * restart anchor, dx = x^ - x0 and dy = y^ - y0, projected onto the
+     * recession cones as utils.cu:684-720 does; the certificate tests are
+     * utils.cu:281-297 with tolerance eps_infeasible.  Both ratios are
+     * invariant to the rays' scale, so the raw displacements are used, and
+     * the reported values are normalised as utils.cu:929-1028 normalises
+     * them (primal ray by its max norm, dual ray by the larger of its max
+     * norm and its largest dual-slack violation). */
+    double ray_pinf = 0, ray_dinf = 0, ray_pobj = 0, ray_dobj = 0;
+    void infeasibility_information() {
+        std::vector<double> dxr(n), dyr(m), adx(m), aty(n);
+        for (int j = 0; j < n; ++j) {
+            double d = xh[j] - x0[j];
+            if (std::isfinite(vlb[j])) d = std::fmax(d, 0.0);
+            if (std::isfinite(vub[j])) d = std::fmin(d, 0.0);
+            dxr[j] = d;
+        }
+        for (int i = 0; i < m; ++i) {
+            double d = yh[i] - y0[i];
+            if (!std::isfinite(clb[i])) d = std::fmin(d, 0.0);
+            if (!std::isfinite(cub[i])) d = std::fmax(d, 0.0);
+            dyr[i] = d;
+        }
+        spmv(A, dxr.data(), adx.data());
+        spmv(At, dyr.data(), aty.data());
+        double pviol = 0.0, rowsum = 0.0, dy_inf = 0.0;
+        for (int i = 0; i < m; ++i) {
+            const double a = adx[i];
+            pviol = std::fmax(pviol, (std::fmax(0.0, -a) * (std::isfinite(clb[i]) ? 1.0 : 0.0) +
+                                      std::fmax(0.0, a) * (std::isfinite(cub[i]) ? 1.0 : 0.0)) *
+                                         rcum[i]);
+            rowsum += std::fmax(dyr[i], 0.0) * clb_fin[i] + std::fmin(dyr[i], 0.0) * cub_fin[i];
+            dy_inf = std::fmax(dy_inf, std::fabs(dyr[i]));
+        }
+        double dviol = 0.0, colsum = 0.0, dx_inf = 0.0, cdx = 0.0;
+        for (int j = 0; j < n; ++j) {
+            const double q = -aty[j];
+            const bool lf = std::isfinite(vlb[j]), uf = std::isfinite(vub[j]);
+            dviol = std::fmax(dviol, (std::fmax(0.0, q) * (lf ? 0.0 : 1.0) - std::fmin(0.0, q) * (uf ? 0.0 : 1.0)) *
+                                         dcum[j]);
+            colsum += std::fmax(q, 0.0) * (lf ? vlb[j] : 0.0) + std::fmin(q, 0.0) * (uf ? vub[j] : 0.0);
+            dx_inf = std::fmax(dx_inf, std::fabs(dxr[j]));
+            cdx += c[j] * dxr[j];
+        }
+        ray_pinf = dx_inf > 0.0 ? pviol / dx_inf : pviol;
+        ray_pobj = (dx_inf > 0.0 ? cdx / dx_inf : cdx) / (cbr * ovr);
+        const double sc = std::fmax(dy_inf, dviol);
+        ray_dinf = sc > 0.0 ? dviol / sc : 0.0;
+        ray_dobj = sc > 0.0 ? (rowsum + colsum) / (cbr * ovr) / sc : 0.0;
+    }
     void check_termination(double elapsed) { /* utils.cu:275-317 */
         const auto &T = P->termination_criteria;
         if (rel_d < T.eps_feasible_relative && rel_p < T.eps_feasible_relative && rel_gap < T.eps_optimal_relative) {
             reason = TERMINATION_REASON_OPTIMAL;
             return;
+        }
+        if (O.infeasibility_detection) {
+            infeasibility_information();
+            /* utils.cu:281-288: a dual ray certifies primal infeasibility */
+            if (ray_dobj > 0.0 && ray_dinf / ray_dobj <= O.eps_infeasible) {
+                reason = TERMINATION_REASON_PRIMAL_INFEASIBLE;
+                return;
+            }
+            /* utils.cu:290-297: a primal ray certifies dual infeasibility */
+            if (ray_pobj < 0.0 && ray_pinf / (-ray_pobj) <= O.eps_infeasible) {
+                reason = TERMINATION_REASON_DUAL_INFEASIBLE;
+                return;
+            }
         }
         if (total >= T.iteration_limit) {
             reason = TERMINATION_REASON_ITERATION_LIMIT;
@@ -749,6 +816,8 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->primal_hot_rows = -1;
     o->power_method = -1;
     o->primal_staged = -1;
+    o->infeasibility_detection = 0;
+    o->eps_infeasible = 1e-8;
 }
 
 /* LP/CP_AL/src/utils.cu:361-394 (reflection coefficient without the
@@ -1081,6 +1150,10 @@ cp_al_result_t *oracle_result(Solver &S, double rescale_sec, double elapsed) {
     res->objective_gap = S.gap;
     res->relative_objective_gap = S.rel_gap;
     res->termination_reason = S.reason;
+    res->max_primal_ray_infeasibility = S.ray_pinf;
+    res->max_dual_ray_infeasibility = S.ray_dinf;
+    res->primal_ray_linear_objective = S.ray_pobj;
+    res->dual_ray_objective = S.ray_dobj;
     return res;
 }
 
@@ -1120,7 +1193,8 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
     for (int t = 0; t < 3; ++t) g_restart_targets[t] = S->restarts_to[t];
     int polish_iters = 0, pst = -1, dst = -1;
     double polish_sec = 0.0;
-    if (params->feasibility_polishing) { /* solver.cu:1715-1719 */
+    if (params->feasibility_polishing && S->reason != TERMINATION_REASON_PRIMAL_INFEASIBLE &&
+        S->reason != TERMINATION_REASON_DUAL_INFEASIBLE) { /* solver.cu:1715-1719 */
         auto tp = std::chrono::steady_clock::now();
         polish_iters = oracle_polish(*S, &pst, &dst, t_start);
         polish_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();

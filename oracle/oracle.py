@@ -140,7 +140,11 @@ def solve_lp(data: LPData, params: dict | None = None, options: dict | None = No
             absolute_dual_residual=r.absolute_dual_residual,
             setup_sec=r.rescaling_time_sec,
             solve_sec=r.cumulative_time_sec,
-            stats={"power_iterations": piters.value, "feasibility_iteration": r.feasibility_iteration,
+            stats={"max_primal_ray_infeasibility": r.max_primal_ray_infeasibility,
+                   "max_dual_ray_infeasibility": r.max_dual_ray_infeasibility,
+                   "primal_ray_linear_objective": r.primal_ray_linear_objective,
+                   "dual_ray_objective": r.dual_ray_objective,
+                   "power_iterations": piters.value, "feasibility_iteration": r.feasibility_iteration,
                    "feasibility_polishing_time": r.feasibility_polishing_time, "polish_status": _polish_status(L),
                    "restart_targets": _restart_targets(L)},
         )

@@ -199,6 +199,8 @@ class CpalOptions(C.Structure):
         ("primal_hot_rows", C.c_int),
         ("power_method", C.c_int),
         ("primal_staged", C.c_int),
+        ("infeasibility_detection", C.c_int),
+        ("eps_infeasible", C.c_double),
     ]
 
 

@@ -118,6 +118,7 @@ int run_batch(int count, lp_problem_t *const *problems, const cp_al_parameters_t
         p.pa = plan_rows(m, q->constraint_matrix_row_pointers, bs);
         p.pat = plan_rows(n, p.At.rp.data(), bs);
         p.cp = resolve_cpal_params(P, O, q);
+        p.cp.infeas = 0; /* the batch controller evaluates no rays */
     });
 
     /* image layout */

@@ -354,6 +354,8 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->primal_hot_rows = -1;
     o->power_method = -1;
     o->primal_staged = -1;
+    o->infeasibility_detection = 0;
+    o->eps_infeasible = 1e-8;
 }
 
 /* Each variable is read the way the reference reads it

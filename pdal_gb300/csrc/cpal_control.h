@@ -51,6 +51,10 @@ struct CpalParams {
     double restart_select_margin;
     double restart_select_min_time;
     int restart_threepoint; /* also score the plain Halpern point (mode 3 or the three-point switch) */
+    /* infeasibility certificates (an opt-in extension: the reference never
+     * evaluates them) */
+    int infeas;
+    double eps_infeas;
 };
 
 /* Solver scalars, resident in device memory during the loop. */
@@ -86,6 +90,9 @@ struct CpalState {
     double fp32_best_kkt;
     double restart_w; /* Halpern weight of the block's last iteration, for a restart to the plain
                          Halpern point w x^ + (1 - w) x0 */
+    /* the last evaluation's ray quantities, normalised as the reference
+     * reports them (infeasibility detection only) */
+    double ray_pinf, ray_dinf, ray_pobj, ray_dobj;
 };
 
 /* Reduction terms of one evaluation (finished sums / maxima). */
@@ -100,6 +107,11 @@ struct CpalEval {
     double sel_ax2, sel_dy2, sel_dx2, sel_cross, cur_dx2, cur_dy2, cur_axd2;
     /* three-point selection only: <A^T(y^ - y0), x^ - x0> */
     double h_cross;
+    /* infeasibility detection only, for the projected displacements
+     * dx = P(x^ - x0), dy = P(y^ - y0): the largest unscaled violation of
+     * A dx, max|dx|, c'dx; the largest unscaled dual-slack violation of
+     * A^T dy, max|dy|, and the two dual-objective sums */
+    double ray_pviol, ray_dxinf, ray_cdx, ray_dviol, ray_dyinf, ray_rowsum, ray_colsum;
 };
 
 PDAL_HD void cpal_set_coefficients(CpalState &s) {
@@ -293,6 +305,23 @@ PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval
     if (s.rel_d < p.eps_feas && s.rel_p < p.eps_feas && s.rel_gap < p.eps_opt) {
         s.status = 1; /* TERMINATION_REASON_OPTIMAL */
         return true;
+    }
+    if (p.infeas) {
+        /* LP/CP_AL/src/utils.cu:919-1029 normalisation and 281-297 tests */
+        const double cs = s.cbr * s.ovr;
+        s.ray_pinf = e.ray_dxinf > 0.0 ? e.ray_pviol / e.ray_dxinf : e.ray_pviol;
+        s.ray_pobj = (e.ray_dxinf > 0.0 ? e.ray_cdx / e.ray_dxinf : e.ray_cdx) / cs;
+        const double sc = fmax(e.ray_dyinf, e.ray_dviol);
+        s.ray_dinf = sc > 0.0 ? e.ray_dviol / sc : 0.0;
+        s.ray_dobj = sc > 0.0 ? (e.ray_rowsum + e.ray_colsum) / cs / sc : 0.0;
+        if (s.ray_dobj > 0.0 && s.ray_dinf / s.ray_dobj <= p.eps_infeas) {
+            s.status = 2; /* TERMINATION_REASON_PRIMAL_INFEASIBLE */
+            return true;
+        }
+        if (s.ray_pobj < 0.0 && s.ray_pinf / (-s.ray_pobj) <= p.eps_infeas) {
+            s.status = 3; /* TERMINATION_REASON_DUAL_INFEASIBLE */
+            return true;
+        }
     }
     if (s.total >= s.iter_limit) {
         s.status = 6; /* TERMINATION_REASON_ITERATION_LIMIT */

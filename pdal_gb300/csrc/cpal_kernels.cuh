@@ -1048,6 +1048,137 @@ __global__ void __launch_bounds__(kThreads) k_eval_cols(RowPlanDev plan, const i
     }
 }
 
+/* ---- infeasibility certificates (opt-in) ------------------------------- */
+/* The projected displacements from the restart anchor (the ray estimates of
+ * LP/CP_AL/src/utils.cu:684-720): dx_j = x^_j - x0_j clipped to >= 0 where
+ * the lower bound is finite and to <= 0 where the upper bound is finite;
+ * dy_i = y^_i - y0_i clipped to <= 0 where the row's lower bound is
+ * infinite and to >= 0 where its upper bound is infinite. */
+__device__ __forceinline__ double ray_dx(double xh, double x0, double lb, double ub) {
+    double d = xh - x0;
+    if (isfinite(lb)) d = fmax(d, 0.0);
+    if (isfinite(ub)) d = fmin(d, 0.0);
+    return d;
+}
+__device__ __forceinline__ double ray_dy(double yh, double y0, double lb, double ub) {
+    double d = yh - y0;
+    if (!isfinite(lb)) d = fmin(d, 0.0);
+    if (!isfinite(ub)) d = fmax(d, 0.0);
+    return d;
+}
+
+template <typename T>
+struct RayArgs {
+    const T *xh, *yh;
+    const double *x0, *y0, *vlb, *vub, *clb, *cub, *clb_fin, *cub_fin, *rscale, *cscale, *c;
+    double *part; /* (nblocks + nlong) * kEvalStride */
+    int nblocks;
+};
+
+/* rows of A: s = (A dx)_i; sum 0: the dual-objective row term of dy, max 0:
+ * the unscaled violation of A dx (utils.cu:722-737), max 1: |dy_i| */
+template <typename T>
+struct RayRowEpi {
+    RayArgs<T> a;
+    __device__ __forceinline__ void operator()(int i, const double *s, Red<1, 2> &r) const {
+        const double lb = a.clb[i], ub = a.cub[i], v = s[0];
+        r.mx[0] = fmax(r.mx[0], (fmax(0.0, -v) * (isfinite(lb) ? 1.0 : 0.0) + fmax(0.0, v) * (isfinite(ub) ? 1.0 : 0.0)) *
+                                    a.rscale[i]);
+        const double dy = ray_dy((double)a.yh[i], a.y0[i], lb, ub);
+        r.s[0] += fmax(dy, 0.0) * a.clb_fin[i] + fmin(dy, 0.0) * a.cub_fin[i];
+        r.mx[1] = fmax(r.mx[1], fabs(dy));
+    }
+    __device__ __forceinline__ void long_red(int lid, Red<1, 2> &r) const {
+        double *d = a.part + (size_t)(a.nblocks + lid) * kEvalStride;
+        d[0] = r.s[0];
+        d[1] = 0.0;
+        d[2] = r.mx[0];
+        d[3] = r.mx[1];
+    }
+};
+
+/* rows of A^T: q = (A^T dy)_j; sum 0: the dual-objective slack term, sum 1:
+ * c_j dx_j, max 0: the unscaled dual-slack violation (utils.cu:739-754),
+ * max 1: |dx_j| */
+template <typename T>
+struct RayColEpi {
+    RayArgs<T> a;
+    __device__ __forceinline__ void operator()(int j, const double *s, Red<2, 2> &r) const {
+        const double lb = a.vlb[j], ub = a.vub[j], q = -s[0];
+        const bool lf = isfinite(lb), uf = isfinite(ub);
+        r.mx[0] = fmax(r.mx[0], (fmax(0.0, q) * (lf ? 0.0 : 1.0) - fmin(0.0, q) * (uf ? 0.0 : 1.0)) * a.cscale[j]);
+        r.s[0] += fmax(q, 0.0) * (lf ? lb : 0.0) + fmin(q, 0.0) * (uf ? ub : 0.0);
+        const double dx = ray_dx((double)a.xh[j], a.x0[j], lb, ub);
+        r.s[1] += a.c[j] * dx;
+        r.mx[1] = fmax(r.mx[1], fabs(dx));
+    }
+    __device__ __forceinline__ void long_red(int lid, Red<2, 2> &r) const {
+        double *d = a.part + (size_t)(a.nblocks + lid) * kEvalStride;
+        d[0] = r.s[0];
+        d[1] = r.s[1];
+        d[2] = r.mx[0];
+        d[3] = r.mx[1];
+    }
+};
+
+template <typename T, int S>
+__global__ void __launch_bounds__(kThreads) k_ray_rows(RowPlanDev plan, const int *__restrict__ rp,
+                                                       const int *__restrict__ ci, const double *__restrict__ val,
+                                                       RayArgs<T> a, const CpalState *__restrict__ st) {
+    if (st->status) return;
+    __shared__ RowBlockSmem<S, 1, double> sm;
+    RayRowEpi<T> epi;
+    epi.a = a;
+    auto g = [&](int c, double *out) { out[0] = ray_dx((double)a.xh[c], a.x0[c], a.vlb[c], a.vub[c]); };
+    Red<1, 2> red;
+    red.zero();
+    rowblock_run<S, 1, double>(plan, rp, ci, val, g, epi, red, sm);
+    block_reduce<kThreads, 1, 2>(red, sm.red);
+    if (threadIdx.x == 0) {
+        double *d = a.part + (size_t)blockIdx.x * kEvalStride;
+        d[0] = red.s[0];
+        d[1] = 0.0;
+        d[2] = red.mx[0];
+        d[3] = red.mx[1];
+    }
+}
+
+template <typename T, int S>
+__global__ void __launch_bounds__(kThreads) k_ray_cols(RowPlanDev plan, const int *__restrict__ rp,
+                                                       const int *__restrict__ ci, const double *__restrict__ val,
+                                                       RayArgs<T> a, const CpalState *__restrict__ st) {
+    if (st->status) return;
+    __shared__ RowBlockSmem<S, 1, double> sm;
+    RayColEpi<T> epi;
+    epi.a = a;
+    auto g = [&](int c, double *out) { out[0] = ray_dy((double)a.yh[c], a.y0[c], a.clb[c], a.cub[c]); };
+    Red<2, 2> red;
+    red.zero();
+    rowblock_run<S, 1, double>(plan, rp, ci, val, g, epi, red, sm);
+    block_reduce<kThreads, 2, 2>(red, sm.red);
+    if (threadIdx.x == 0) {
+        double *d = a.part + (size_t)blockIdx.x * kEvalStride;
+        d[0] = red.s[0];
+        d[1] = red.s[1];
+        d[2] = red.mx[0];
+        d[3] = red.mx[1];
+    }
+}
+
+/* Sums (slots 0, 1) and maxima (slots 2, 3) of the ray partials, in a fixed
+ * order. */
+__device__ __forceinline__ void reduce_ray_slots(const double *part, int nslots, Red<2, 2> &r, double *sbuf) {
+    r.zero();
+    for (int b = threadIdx.x; b < nslots; b += kThreads) {
+        const double *d = part + (size_t)b * kEvalStride;
+        r.s[0] += d[0];
+        r.s[1] += d[1];
+        r.mx[0] = fmax(r.mx[0], d[2]);
+        r.mx[1] = fmax(r.mx[1], d[3]);
+    }
+    block_reduce<kThreads, 2, 2>(r, sbuf);
+}
+
 /* Sums the partial slots of one evaluation kernel in a fixed order. */
 __device__ __forceinline__ void reduce_slots(const double *part, int nslots, Red<10, 1> &r, double *sbuf) {
     r.zero();
@@ -1062,12 +1193,21 @@ __device__ __forceinline__ void reduce_slots(const double *part, int nslots, Red
 
 static __global__ void __launch_bounds__(kThreads) k_control(const double *__restrict__ prow, int nrow_slots,
                                                       const double *__restrict__ pcol, int ncol_slots,
+                                                      const double *__restrict__ pray_row, int nray_row,
+                                                      const double *__restrict__ pray_col, int nray_col,
                                                       CpalState *st, CpalParams p, HalpernW *wt, HalpernWf *wtf) {
     if (st->status) return;
     __shared__ double sbuf[11 * (kThreads / 32)];
     Red<10, 1> r1, r2;
     reduce_slots(prow, nrow_slots, r1, sbuf);
     reduce_slots(pcol, ncol_slots, r2, sbuf);
+    Red<2, 2> q1, q2;
+    q1.zero();
+    q2.zero();
+    if (p.infeas) {
+        reduce_ray_slots(pray_row, nray_row, q1, sbuf);
+        reduce_ray_slots(pray_col, nray_col, q2, sbuf);
+    }
     if (threadIdx.x == 0) {
         CpalEval e;
         e.rp2 = r1.s[0];
@@ -1092,6 +1232,13 @@ static __global__ void __launch_bounds__(kThreads) k_control(const double *__res
         e.sel_dx2 = r2.s[7];
         e.cur_dx2 = r2.s[8];
         e.h_cross = r2.s[9];
+        e.ray_rowsum = q1.s[0];
+        e.ray_pviol = q1.mx[0];
+        e.ray_dyinf = q1.mx[1];
+        e.ray_colsum = q2.s[0];
+        e.ray_cdx = q2.s[1];
+        e.ray_dviol = q2.mx[0];
+        e.ray_dxinf = q2.mx[1];
         CpalState s = *st;
         s.elapsed = (double)(globaltimer_ns() - s.t_start_ns) * 1e-9;
         cpal_end_of_block(s, p, e);

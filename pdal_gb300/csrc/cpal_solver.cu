@@ -286,6 +286,7 @@ class CpalSolver {
     double *x0_ = nullptr, *y0_ = nullptr, *ax0_ = nullptr, *phat_ = nullptr, *dsc_ = nullptr, *rsc_ = nullptr;
     double *tmp_n_ = nullptr, *tmp_m_ = nullptr, *tmp_m2_ = nullptr;
     double *part_row_ = nullptr, *part_col_ = nullptr, *part_misc_ = nullptr;
+    double *part_ray_row_ = nullptr, *part_ray_col_ = nullptr; /* infeasibility detection */
     double *xout_ = nullptr, *yout_ = nullptr, *rcout_ = nullptr;
     float2 *x0f_ = nullptr, *y0f_ = nullptr, *ax0f_ = nullptr; /* FP32-phase anchors (hi, lo) */
     HalpernW *wt_ = nullptr;
@@ -401,6 +402,8 @@ CpalParams resolve_cpal_params(const cp_al_parameters_t &P, const cp_al_gb300_op
     /* LP/CP_AL/src/solver.cu:2774-2775: mode 3, or the three-point switch
      * with any other nonzero mode */
     cp.restart_threepoint = O.restart_select != 0 && (O.restart_select == 3 || O.restart_select_threepoint != 0);
+    cp.infeas = O.infeasibility_detection != 0;
+    cp.eps_infeas = O.eps_infeasible;
     cp.obj_const = prob->objective_constant;
     const int n = prob->num_variables, m = prob->num_constraints;
     const bool linf = cp.norm_linf;
@@ -597,6 +600,10 @@ void CpalSolver::alloc_all() {
     wtf_ = arena_.take<HalpernWf>((size_t)cp_.F + 1);
     part_row_ = arena_.take<double>((size_t)(A_.ev.hp.nblocks + A_.ev.hp.nlong + 1) * kEvalStride);
     part_col_ = arena_.take<double>((size_t)(At_.ev.hp.nblocks + At_.ev.hp.nlong + 1) * kEvalStride);
+    if (cp_.infeas) {
+        part_ray_row_ = arena_.take<double>((size_t)(A_.ev.hp.nblocks + A_.ev.hp.nlong + 1) * kEvalStride);
+        part_ray_col_ = arena_.take<double>((size_t)(At_.ev.hp.nblocks + At_.ev.hp.nlong + 1) * kEvalStride);
+    }
     nmisc_ = std::max({A_.ev.hp.nblocks + A_.ev.hp.nlong, A_.it.hp.nblocks + A_.it.hp.nlong,
                        grid_for(std::max(n_, m_)), 1});
     part_misc_ = arena_.take<double>(2 * (size_t)nmisc_ + 2);
@@ -1445,8 +1452,21 @@ void CpalSolver::launch_eval() {
         });
     }
     const int nrow_slots = m_ > 0 ? A_.ev.d.nblocks + A_.ev.d.nlong : 0;
-    k_control<<<1, kThreads, 0, stream_>>>(part_row_, nrow_slots, part_col_, At_.ev.d.nblocks + At_.ev.d.nlong, st_,
-                                           cp_, wt_, wtf_);
+    const int ncol_slots = At_.ev.d.nblocks + At_.ev.d.nlong;
+    if (cp_.infeas) {
+        RayArgs<T> rr{v.xh, v.yh, x0_, y0_, vlb_, vub_, clb_, cub_, clbf_, cubf_, rsc_, dsc_, c_, part_ray_row_,
+                      A_.ev.d.nblocks};
+        RayArgs<T> rc = rr;
+        rc.part = part_ray_col_;
+        rc.nblocks = At_.ev.d.nblocks;
+        PDAL_WITH_SE(S_ev_, {
+            if (m_ > 0) k_ray_rows<T, SE><<<A_.ev.d.nblocks, kThreads, 0, stream_>>>(A_.ev.d, A_.rp, A_.ci, A_.v, rr, st_);
+            k_ray_cols<T, SE><<<At_.ev.d.nblocks, kThreads, 0, stream_>>>(At_.ev.d, At_.rp, At_.ci, At_.v, rc, st_);
+        });
+    }
+    k_control<<<1, kThreads, 0, stream_>>>(part_row_, nrow_slots, part_col_, ncol_slots, part_ray_row_,
+                                           cp_.infeas ? nrow_slots : 0, part_ray_col_, cp_.infeas ? ncol_slots : 0,
+                                           st_, cp_, wt_, wtf_);
     const int gr = grid_for(std::max(n_, m_));
     const bool f32 = std::is_same<T, float>::value;
     float2 *x0f = f32 ? x0f_ : nullptr, *y0f = f32 ? y0f_ : nullptr, *ax0f = f32 ? ax0f_ : nullptr;
@@ -1767,7 +1787,7 @@ void CpalSolver::run_loop() {
     loop_t0_ = t0;
     const int F = cp_.F;
     const int G = std::max(1, O_.graph_blocks);
-    const int64_t per_block = (int64_t)iter_launches() * F + (m_ > 0 ? 4 : 3);
+    const int64_t per_block = (int64_t)iter_launches() * F + (m_ > 0 ? 4 : 3) + (cp_.infeas ? (m_ > 0 ? 2 : 1) : 0);
     k_start_clock<<<1, 1, 0, stream_>>>(st_);
     PDAL_LAUNCH_CHECK();
     launches += 1;
@@ -1908,6 +1928,10 @@ void CpalSolver::download(cp_al_result_t *res, bool vectors) {
     res->objective_gap = s.gap;
     res->relative_objective_gap = s.rel_gap;
     res->termination_reason = (termination_reason_t)s.status;
+    res->max_primal_ray_infeasibility = s.ray_pinf;
+    res->max_dual_ray_infeasibility = s.ray_dinf;
+    res->primal_ray_linear_objective = s.ray_pobj;
+    res->dual_ray_objective = s.ray_dobj;
     if (vectors) {
         res->primal_solution = (double *)malloc(sizeof(double) * std::max(n_, 1));
         res->dual_solution = (double *)malloc(sizeof(double) * std::max(m_, 1));
@@ -2036,8 +2060,11 @@ cp_al_result_t *cp_al_gb300_solve(lp_problem_t *prob, const cp_al_parameters_t *
         s.upload();
         s.setup_device();
         s.run_loop();
-        /* solver.cu:1715-1719 (the LP path has no infeasibility statuses) */
-        if (local.feasibility_polishing) s.polish();
+        /* solver.cu:1715-1719: no polishing after an infeasibility status
+         * (only infeasibility detection, off by default, produces one) */
+        if (local.feasibility_polishing && s.host_state.status != TERMINATION_REASON_PRIMAL_INFEASIBLE &&
+            s.host_state.status != TERMINATION_REASON_DUAL_INFEASIBLE)
+            s.polish();
         s.result_on_device();
         s.download(res, true);
         res->feasibility_polishing_time = s.polish_sec;

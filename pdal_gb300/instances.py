@@ -92,6 +92,35 @@ def random_lp(m: int = 2000, n: int = 5000, nnz_per_col=8, seed: int = 0, eq_fra
     return LPData(c, (A[0], A[1], A[2], (m, n)), cl, cu, lb, ubv)
 
 
+def infeasible_lp(kind: str, m: int = 300, n: int = 800, nnz_per_col: int = 6, seed: int = 0) -> LPData:
+    """random_lp made infeasible.  kind "primal": row 0 (an equality) is
+    asked to exceed its largest value over the variable box (10 * the sum of
+    its positive entries) by 1, so no x satisfies it.  kind "dual": one more
+    variable, 0 <= x_new unbounded above, with cost -1 and negative entries in
+    three <= rows only, so x_new -> infinity stays feasible and the objective
+    is unbounded below."""
+    d = random_lp(m, n, nnz_per_col, seed=seed)
+    rp, ci, v, _ = d.csr()
+    if kind == "primal":
+        row0 = v[rp[0]:rp[1]]
+        top = 10.0 * np.maximum(row0, 0.0).sum() + 1.0
+        d.con_lb = d.con_lb.copy()
+        d.con_ub = d.con_ub.copy()
+        d.con_lb[0], d.con_ub[0] = top, np.inf
+        return d
+    if kind != "dual":
+        raise ValueError(kind)
+    rng = np.random.default_rng(seed + 1)
+    le_rows = np.flatnonzero(np.isinf(d.con_lb))
+    pick = np.sort(rng.choice(le_rows, 3, replace=False))
+    rows = np.concatenate([np.repeat(np.arange(m), np.diff(rp)), pick])
+    cols = np.concatenate([ci, np.full(3, n)])
+    vals = np.concatenate([v, -rng.uniform(0.5, 1.5, 3)])
+    A = _csr_from_coo(rows, cols, vals, m, n + 1)
+    return LPData(np.append(d.c, -1.0), (A[0], A[1], A[2], (m, n + 1)), d.con_lb, d.con_ub, np.append(d.var_lb, 0.0),
+                  np.append(d.var_ub, np.inf))
+
+
 def zipf_lp(m: int = 1_000_000, n: int = 2_000_000, nnz: int = 20_000_000, seed: int = 1000,
             zipf_a: float = 1.5, max_row: int = 20_000, free_fraction: float = 0.05) -> LPData:
     """Large badly scaled LP: row lengths Zipf(zipf_a) capped at max_row and

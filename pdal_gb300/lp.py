@@ -183,6 +183,9 @@ def _result_from_c(lib, r: N.CpalResult, m: int, n: int, with_vectors: bool = Tr
     lib.cp_al_gb300_last_stats(C.byref(st))
     stats = {f: getattr(st, f) for f, _ in N.CpalStats._fields_}
     stats["feasibility_iteration"] = r.feasibility_iteration
+    for f in ("max_primal_ray_infeasibility", "max_dual_ray_infeasibility", "primal_ray_linear_objective",
+              "dual_ray_objective"):
+        stats[f] = getattr(r, f)
     stats["feasibility_polishing_time"] = r.feasibility_polishing_time
     return LPResult(
         status=N.TERMINATION_REASONS.get(r.termination_reason, str(r.termination_reason)),

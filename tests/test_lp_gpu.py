@@ -478,3 +478,30 @@ def test_feasibility_polishing_matches_oracle(kind):
     ax = A @ g.x
     viol = np.maximum(np.asarray(data.con_lb) - ax, 0) + np.maximum(ax - np.asarray(data.con_ub), 0)
     assert np.linalg.norm(viol) <= 1e-6 * (1 + np.linalg.norm(np.nan_to_num(data.con_ub, posinf=0)))
+
+
+@pytest.mark.parametrize("kind,status", [("primal", "PRIMAL_INFEASIBLE"), ("dual", "DUAL_INFEASIBLE")])
+@pytest.mark.parametrize("seed", [3, 8])
+def test_infeasibility_detection_matches_oracle(lp_lib, kind, status, seed):
+    """Opt-in infeasibility certificates, evaluated on the device at every
+    evaluation: same status, same evaluation and certificate values as the
+    oracle in FP64; the chosen form reaches the same status."""
+    d = I.infeasible_lp(kind, seed=seed)
+    p = {"eps": 1e-8, "iteration_limit": 20_000, "time_limit": 120}
+    g = lp.solve(d, p, {"infeasibility_detection": 1})
+    o = O.solve_lp(d, p, {"infeasibility_detection": 1})
+    assert g.status == o.status == status
+    assert g.iterations == o.iterations
+    for f in ("max_primal_ray_infeasibility", "max_dual_ray_infeasibility", "primal_ray_linear_objective",
+              "dual_ray_objective"):
+        assert abs(g.stats[f] - o.stats[f]) <= 1e-7 * (1 + abs(o.stats[f])), f
+    g32 = lp.solve(d, p, {"infeasibility_detection": 1, "precision": "fp32_refine"})
+    assert g32.status == status
+
+
+def test_infeasibility_detection_leaves_feasible_solves_alone(lp_lib):
+    d = I.random_lp(300, 800, 6, seed=21)
+    a = lp.solve(d, {"eps": 1e-8}, {"infeasibility_detection": 0})
+    b = lp.solve(d, {"eps": 1e-8}, {"infeasibility_detection": 1})
+    assert a.status == b.status == "OPTIMAL" and a.iterations == b.iterations
+    assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)

@@ -205,3 +205,48 @@ def test_oracle_curtis_reid_without_constraints():
     assert p == 5 and np.all(c == 1.0)
     *_, p20 = O.rescale(d, base, {"cr_iterations": 20}, with_passes=True)
     assert p20 == 20
+
+
+def _highs_status(d):
+    """HiGHS on the same LP: 0 optimal, 2 infeasible, 3 unbounded."""
+    rp, ci, v, (m, n) = d.csr()
+    A = sp.csr_matrix((v, ci, rp), shape=(m, n))
+    lo, hi = np.asarray(d.con_lb), np.asarray(d.con_ub)
+    eq = lo == hi
+    ub_rows, lb_rows = np.isfinite(hi) & ~eq, np.isfinite(lo) & ~eq
+    r = linprog(d.c, A_ub=sp.vstack([A[ub_rows], -A[lb_rows]]), b_ub=np.concatenate([hi[ub_rows], -lo[lb_rows]]),
+                A_eq=A[eq], b_eq=lo[eq],
+                bounds=[(l, u if np.isfinite(u) else None) for l, u in zip(d.var_lb, d.var_ub)], method="highs")
+    return r.status
+
+
+@pytest.mark.parametrize("kind,status,highs", [("primal", "PRIMAL_INFEASIBLE", 2), ("dual", "DUAL_INFEASIBLE", 3)])
+@pytest.mark.parametrize("seed", [3, 8])
+def test_oracle_infeasibility_detection(kind, status, highs, seed):
+    """Opt-in certificates (the reference's utils.cu:281-297 tests on the
+    displacement from the restart anchor): an infeasible LP stops with the
+    status HiGHS confirms, with a certificate that passes the tolerance;
+    without the option it runs to its iteration limit, as the reference's
+    solver does."""
+    d = I.infeasible_lp(kind, seed=seed)
+    assert _highs_status(d) == highs
+    p = {"eps": 1e-8, "iteration_limit": 20_000}
+    on = O.solve_lp(d, p, {"infeasibility_detection": 1})
+    off = O.solve_lp(d, p, {"infeasibility_detection": 0})
+    assert on.status == status and on.iterations < 20_000
+    assert off.status == "ITERATION_LIMIT"
+    s = on.stats
+    if kind == "primal":
+        assert s["dual_ray_objective"] > 0
+        assert s["max_dual_ray_infeasibility"] / s["dual_ray_objective"] <= 1e-8
+    else:
+        assert s["primal_ray_linear_objective"] < 0
+        assert s["max_primal_ray_infeasibility"] / -s["primal_ray_linear_objective"] <= 1e-8
+
+
+def test_oracle_infeasibility_detection_leaves_feasible_solves_alone():
+    d = I.random_lp(300, 800, 6, seed=21)
+    a = O.solve_lp(d, {"eps": 1e-8}, {"infeasibility_detection": 0})
+    b = O.solve_lp(d, {"eps": 1e-8}, {"infeasibility_detection": 1})
+    assert a.status == b.status == "OPTIMAL" and a.iterations == b.iterations
+    assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)

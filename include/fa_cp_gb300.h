@@ -70,6 +70,8 @@ typedef struct {
     int power_iterations_a;
     int power_iterations_q;
     int fp32_iterations;       /* iterations run in FP32 segments (precision 1) */
+    int polish_primal_status;  /* feasibility polishing: termination_reason_t of the primal and the */
+    int polish_dual_status;    /* dual phase (7 = FEAS_POLISH_SUCCESS), -1 when not run */
 } fa_cp_gb300_stats_t;
 
 /* Defaults: current device, automatic grid and block budget, restart to the

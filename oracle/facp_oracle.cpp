@@ -84,6 +84,7 @@ double vsum(const std::vector<double> &a) {
 }
 
 int g_trace = 0;
+int g_polish_status[2] = {-1, -1};
 
 int print_frequency(int iter) { /* utils.cu:636-647 */
     int step = 10;
@@ -730,6 +731,135 @@ struct QP {
     }
 };
 
+/* ---------- feasibility polishing (fa_cp_core_op.cu:1241-1735) ----------
+ * Two phases after the solve, each the same iteration and loop as the solve
+ * on a feasibility problem: the primal phase drops the objective (c = 0,
+ * constant 0) and starts from the solve's primal iterates with the dual
+ * iterates at zero; the dual phase sets every finite bound to zero and starts
+ * from the solve's dual iterates (and dual slack) with the primal iterates
+ * at zero.  Both take the primal weight of the start of the solve, restart by
+ * the solve's rule on a one-sided fixed-point error (|x_bar - x|^2 w, or
+ * |y_bar - y|^2 / w, no square root) by moving the anchor to the current
+ * point (no weight or sigma update), and stop when their relative residual is
+ * at most eps_feas_polish_relative (utils.cu:1360-1384).  Like the
+ * reference's loop, a phase runs one more iteration after its stopping test
+ * and reports total - 1 iterations. */
+struct PolishOut {
+    termination_reason_t reason;
+    int total;
+    double abs_r, rel_r, obj;
+    std::vector<double> sol; /* the phase's primal (dual) solution */
+};
+
+void polish_residual(QP &S, const QP &ori, bool primal) { /* utils.cu:1491-1574 */
+    const bool linf = S.P->optimality_norm == NORM_TYPE_L_INF;
+    if (primal) {
+        spmv(S.A, S.xh.data(), S.pprod.data());
+        for (int i = 0; i < S.m; ++i) {
+            const double cl = std::fmax(S.clb[i], std::fmin(S.pprod[i], S.cub[i]));
+            S.rres[i] = (S.pprod[i] - cl) * S.rcum[i];
+        }
+        S.abs_p = (linf ? amax(S.rres) : nrm2(S.rres)) / S.cbr;
+        S.rel_p = S.abs_p / (1.0 + S.bnd_norm);
+        S.pobj = dot(ori.c, S.xh) / (S.cbr * S.ovr) + S.c0;
+    } else {
+        spmv(S.At, S.yh.data(), S.dprod.data());
+        for (int j = 0; j < S.n; ++j) S.dres[j] = (S.c[j] - S.dprod[j] - S.dslack[j]) * S.dcum[j];
+        for (int i = 0; i < S.m; ++i)
+            S.pslack[i] = std::fmax(S.yh[i], 0.0) * ori.clb_fin[i] + std::fmin(S.yh[i], 0.0) * ori.cub_fin[i];
+        S.abs_d = (linf ? amax(S.dres) : nrm2(S.dres)) / S.ovr;
+        S.rel_d = S.abs_d / (1.0 + S.obj_norm);
+        S.dobj = (dot(S.dslack, ori.xh) + vsum(S.pslack)) / (S.cbr * S.ovr) + S.c0;
+    }
+}
+
+PolishOut polish_phase(const QP &ori, bool primal, double pw0, std::chrono::steady_clock::time_point t0) {
+    QP S = ori; /* *state copy (fa_cp_core_op.cu:1410-1478, 1525-1607) */
+    const int n = S.n, m = S.m;
+    auto zero = [](std::vector<double> &v) { std::fill(v.begin(), v.end(), 0.0); };
+    if (primal) {
+        zero(S.c);
+        S.c0 = 0.0;
+        zero(S.y0), zero(S.y), zero(S.yh), zero(S.ybar), zero(S.dprod);
+        zero(S.dslack);
+    } else {
+        auto zf = [](std::vector<double> &v) {
+            for (double &e : v)
+                if (std::isfinite(e)) e = 0.0;
+        };
+        zf(S.clb), zf(S.cub), zf(S.vlb), zf(S.vub);
+        zero(S.clb_fin), zero(S.cub_fin), zero(S.vlb_fin), zero(S.vub_fin);
+        zero(S.x0), zero(S.x), zero(S.xh), zero(S.xbar), zero(S.pprod);
+    }
+    zero(S.aldual), zero(S.pslack), zero(S.dres), zero(S.rres), zero(S.dx), zero(S.dy);
+    (void)n, (void)m;
+    S.pw_esum = 0.0;
+    S.pw_last = 0.0;
+    S.fp = S.fp0 = S.fp_last = INFINITY;
+    S.major = false;
+    S.total = S.inner = 0;
+    S.reason = TERMINATION_REASON_UNSPECIFIED;
+    S.best_gap = INFINITY;
+    if (primal) {
+        S.rel_d = S.abs_d = S.rel_gap = S.gap = 0.0;
+    } else {
+        S.rel_p = S.abs_p = S.rel_gap = S.gap = 0.0;
+    }
+    S.pw = S.best_pw = pw0;
+    const auto &T = S.P->termination_criteria;
+    const int F = S.P->termination_evaluation_frequency;
+    const auto tp = std::chrono::steady_clock::now();
+    (void)t0;
+    bool do_restart = false;
+    while (S.reason == TERMINATION_REASON_UNSPECIFIED) { /* fa_cp_core_op.cu:1313-1355, 1362-1404 */
+        if (S.major || S.total == 0 || S.total % print_frequency(S.total) == 0) {
+            polish_residual(S, ori, primal);
+            const double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
+            if ((primal ? S.rel_p : S.rel_d) <= T.eps_feas_polish_relative)
+                S.reason = TERMINATION_REASON_FEAS_POLISH_SUCCESS;
+            else if (S.total >= T.iteration_limit)
+                S.reason = TERMINATION_REASON_ITERATION_LIMIT;
+            else if (elapsed >= T.time_sec_limit)
+                S.reason = TERMINATION_REASON_TIME_LIMIT;
+        }
+        if (S.major || S.total == 0) {
+            do_restart = S.should_restart();
+            if (do_restart) { /* fa_cp_core_op.cu:1649-1668 */
+                if (primal) {
+                    S.x0 = S.xh;
+                    S.x = S.xh;
+                } else {
+                    S.y0 = S.yh;
+                    S.y = S.yh;
+                }
+                S.inner = 0;
+                S.fp_last = INFINITY;
+            }
+        }
+        S.major = ((S.total + 1) % F) == 0;
+        S.update();
+        if (S.major || do_restart) { /* fa_cp_core_op.cu:1705-1735 */
+            double s = 0.0;
+            if (primal) {
+                for (int j = 0; j < S.n; ++j) s += (S.xbar[j] - S.x[j]) * (S.xbar[j] - S.x[j]);
+                S.fp = s * S.pw;
+            } else {
+                for (int i = 0; i < S.m; ++i) s += (S.ybar[i] - S.y[i]) * (S.ybar[i] - S.y[i]);
+                S.fp = s / S.pw;
+            }
+            if (do_restart) {
+                S.fp0 = S.fp;
+                do_restart = false;
+            }
+        }
+        S.halpern();
+        S.inner++;
+        S.total++;
+    }
+    return PolishOut{S.reason, S.total, primal ? S.abs_p : S.abs_d, primal ? S.rel_p : S.rel_d,
+                     primal ? S.pobj : S.dobj, primal ? S.xh : S.yh};
+}
+
 quad_obj_type_t detect_q_type(const Csr &Q, const Csr &R) { /* utils.cu:1576-1616 */
     if (Q.nnz() == 0 && R.nnz() == 0) return FA_CP_NON_Q;
     if (R.nnz() > 0) return Q.nnz() > 0 ? FA_CP_LOW_RANK_PLUS_SPARSE_Q : FA_CP_LOW_RANK_Q;
@@ -797,6 +927,7 @@ void oracle_facp_default_parameters(fa_cp_parameters_t *p) { /* QP/FA_CP/src/uti
 }
 
 fa_cp_result_t *oracle_facp_solve(const qp_problem_t *prob, const fa_cp_parameters_t *params) {
+    g_polish_status[0] = g_polish_status[1] = -1;
     if (!prob || !params || params->termination_evaluation_frequency < 1) return nullptr;
     auto t0 = std::chrono::steady_clock::now();
     std::unique_ptr<QP> SP(new QP());
@@ -936,6 +1067,42 @@ fa_cp_result_t *oracle_facp_solve(const qp_problem_t *prob, const fa_cp_paramete
     }
     elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
 
+    /* solver.cu:156-160: polishing after the solve, except after an
+     * infeasibility status; built for problems without Q (for a QP the
+     * reference's dual phase keeps a stale dual slack and does not converge) */
+    int polish_iters = 0;
+    double polish_sec = 0.0;
+    if (params->feasibility_polishing && S.reason != TERMINATION_REASON_DUAL_INFEASIBLE &&
+        S.reason != TERMINATION_REASON_PRIMAL_INFEASIBLE && S.qtype == FA_CP_NON_Q) {
+        const auto &T = params->termination_criteria;
+        const auto tp = std::chrono::steady_clock::now();
+        /* fa_cp_core_op.cu:1244-1252: nothing to do when already feasible */
+        if (!(S.rel_p < T.eps_feas_polish_relative && S.rel_d < T.eps_feas_polish_relative)) {
+            const double pw0 = params->bound_objective_rescaling ? 1.0 : (S.obj_norm + 1.0) / (S.bnd_norm + 1.0);
+            PolishOut po = polish_phase(S, true, pw0, tp);
+            if (po.reason == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+                S.xh = po.sol;
+                S.abs_p = po.abs_r;
+                S.rel_p = po.rel_r;
+                S.pobj = po.obj;
+            }
+            polish_iters += po.total - 1;
+            PolishOut pd = polish_phase(S, false, pw0, tp);
+            if (pd.reason == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+                S.yh = pd.sol;
+                S.abs_d = pd.abs_r;
+                S.rel_d = pd.rel_r;
+                S.dobj = pd.obj;
+            }
+            polish_iters += pd.total - 1;
+            S.gap = std::fabs(S.pobj - S.dobj);
+            S.rel_gap = S.gap / (1.0 + std::fabs(S.pobj) + std::fabs(S.dobj));
+            g_polish_status[0] = po.reason;
+            g_polish_status[1] = pd.reason;
+        }
+        polish_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
+    }
+
     /* result (fa_cp_core_op.cu:1171-1239) */
     fa_cp_result_t *r = (fa_cp_result_t *)calloc(1, sizeof(fa_cp_result_t));
     r->primal_solution = (double *)malloc(sizeof(double) * (n > 0 ? n : 1));
@@ -970,6 +1137,8 @@ fa_cp_result_t *oracle_facp_solve(const qp_problem_t *prob, const fa_cp_paramete
     r->sigma_update_count = S.sigma_updates;
     r->sigma_update_rule = S.al_available ? params->sigma_update_rule : FA_CP_SIGMA_UPDATE_FIXED;
     r->termination_reason = S.reason;
+    r->feasibility_iteration = polish_iters;
+    r->feasibility_polishing_time = polish_sec;
     return r;
 }
 
@@ -1002,6 +1171,12 @@ int oracle_facp_scaling(const qp_problem_t *prob, const fa_cp_parameters_t *para
 }
 
 void oracle_facp_set_trace(int on) { g_trace = on; }
+
+/* statuses of the last solve's primal and dual polishing phases (-1: not run) */
+void oracle_facp_polish_status(int *primal, int *dual) {
+    *primal = g_polish_status[0];
+    *dual = g_polish_status[1];
+}
 
 void oracle_facp_result_free(fa_cp_result_t *r) {
     if (!r) return;

@@ -227,6 +227,7 @@ def _qp_lib():
         L.oracle_facp_result_free.argtypes = [C.POINTER(N.FacpResult)]
         L.oracle_facp_default_parameters.argtypes = [C.POINTER(N.FacpParameters)]
         L.oracle_facp_set_trace.argtypes = [C.c_int]
+        L.oracle_facp_polish_status.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L._facp_ready = True
     return L
 
@@ -316,6 +317,8 @@ def solve_qp(data: QPData, params: dict | None = None, trace: bool = False) -> Q
     if not rp:
         raise RuntimeError("oracle QP solve failed (invalid parameters)")
     try:
-        return _qp_result(rp.contents, prob.m, prob.n)
+        ps, ds = C.c_int(-1), C.c_int(-1)
+        L.oracle_facp_polish_status(C.byref(ps), C.byref(ds))
+        return _qp_result(rp.contents, prob.m, prob.n, {"polish_status": (ps.value, ds.value)})
     finally:
         L.oracle_facp_result_free(rp)

@@ -493,6 +493,8 @@ class FacpStats(C.Structure):
         ("power_iterations_a", C.c_int),
         ("power_iterations_q", C.c_int),
         ("fp32_iterations", C.c_int),
+        ("polish_primal_status", C.c_int),
+        ("polish_dual_status", C.c_int),
     ]
 
 

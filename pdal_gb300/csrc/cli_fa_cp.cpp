@@ -7,8 +7,9 @@
  * Same options, defaults and exit codes; writes <name>_summary.txt,
  * <name>_primal_solution.txt and <name>_dual_solution.txt into output_dir in
  * the reference's formats (cli.c:112-170), <name> being the file name up to
- * its first dot, and the per-evaluation CSV of --trajectory_csv.  Not built:
- * feasibility polishing (-f prints a warning and solves without it).
+ * its first dot, and the per-evaluation CSV of --trajectory_csv.  -f runs
+ * the feasibility polishing phases for problems without Q; for a QP the
+ * library warns and solves without them.
  */
 #include "../../include/fa_cp.h"
 #include "../../include/fa_cp_mps_parser.h"
@@ -224,7 +225,7 @@ const Option kOptions[] = {
      "sigma a guarded rule starts from when it switches on; theta of sigma = theta * dual step for "
      "balanced_guarded (0.1)",
      PDAL_DBL(sigma_activation_value)},
-    {"feasibility_polishing", 'f', nullptr, "polishing phases after the solve (not built: a warning)",
+    {"feasibility_polishing", 'f', nullptr, "polishing phases after the solve (problems without Q)",
      [](P &p, const char *) { return p.feasibility_polishing = true, true; }},
     {"eps_feas_polish", 0, "TOL", "residual target of the polishing phases (1e-6)",
      PDAL_DBL(termination_criteria.eps_feas_polish_relative)},
@@ -299,10 +300,6 @@ int main(int argc, char *argv[]) {
     }
     const char *filename = argv[optind];
     const char *output_dir = argv[optind + 1];
-    if (params.feasibility_polishing) {
-        fprintf(stderr, "Warning: feasibility polishing is not part of this build; solving without it.\n");
-        params.feasibility_polishing = false;
-    }
     const std::string name = instance_name(filename);
     qp_problem_t *problem = read_mps_file(filename);
     if (!problem) {

@@ -57,6 +57,8 @@ enum : int {
     MODE_POWER_A = 5,
     MODE_POWER_QMAX = 6,
     MODE_POWER_QMIN = 7,
+    MODE_POLISH_EVAL_P = 8, /* feasibility polishing: primal-phase residual */
+    MODE_POLISH_EVAL_D = 9, /* feasibility polishing: dual-phase residual */
 };
 
 struct DMat {
@@ -130,6 +132,9 @@ struct Prob {
     Ctl *ctl;
     double *out_x, *out_y, *out_rc;
     SegV<float> f; /* FP32 mirror (chosen form only; null pointers otherwise) */
+    /* feasibility polishing phases: the solve's objective, finite bounds and
+     * primal solution, which the phase residuals read (null otherwise) */
+    const double *ref_c, *ref_clb_fin, *ref_cub_fin, *ref_xh;
 };
 
 struct Args {
@@ -139,6 +144,8 @@ struct Args {
     int linf, infeas;
     int max_iter;
     int fp32; /* MODE_SEGMENT: run the segment in FP32 */
+    int polish; /* MODE_SEGMENT: 0 the solve; 1 (2) a primal (dual) polishing phase, whose
+                   fixed-point error is |x_bar - x|^2 w (|y_bar - y|^2 / w) */
     double tau, rho, step, pw, sigma, refl;
     double tau_eval;
     double cbr, ovr, c0, obj_norm, bnd_norm;
@@ -744,7 +751,8 @@ __device__ bool iteration(Cx &cx, const SegV<T> &V, int k, int inner, bool fp, d
         const double pn = sqrt(tot[0]), dn = sqrt(tot[1]);
         const double movement = pn * pn * a.pw + dn * dn / a.pw;
         const double interaction = 2 * a.step * tot[2];
-        fp_out = sqrt(fmax(movement + interaction, 0.0));
+        /* fa_cp_core_op.cu:1705-1735 in a polishing phase (no square root) */
+        fp_out = a.polish == 1 ? tot[0] * a.pw : a.polish == 2 ? tot[1] / a.pw : sqrt(fmax(movement + interaction, 0.0));
         if (a.has_inner) inner_tol = fmin(inner_tol, fmax(0.0005 * pn / a.step * a.pw, 1e-9));
     }
     return true;
@@ -1054,6 +1062,86 @@ __device__ bool run_eval(Cx &cx) {
     return true;
 }
 
+/* ------------------------------------------------------------------ feasibility polishing */
+
+/* primal phase (utils.cu:1456-1470, 1491-1529): |A x^ clamped-residual .* r|
+ * and the solve's objective at x^ */
+struct EpiPolishRows {
+    const Prob *P;
+    __device__ __forceinline__ void operator()(int i, const double (&s)[1], Red<2, 1> &r) const {
+        const double p = s[0];
+        const double cl = fmax(P->clb[i], fmin(p, P->cub[i]));
+        const double res = (p - cl) * P->rcum[i];
+        r.s[0] += res * res;
+        r.mx[0] = fmax(r.mx[0], fabs(res));
+    }
+    const Cx *cx;
+    __device__ __forceinline__ void long_red(int lid, Red<2, 1> &lr) const { add_long(*cx, MAT_A, lid, lr); }
+};
+
+/* dual phase (utils.cu:1472-1489, 1531-1574): |(c - A'y^ - slack) .* d| and
+ * the slack's product with the solve's primal solution */
+struct EpiPolishCols {
+    const Prob *P;
+    __device__ __forceinline__ void operator()(int j, const double (&s)[1], Red<2, 1> &r) const {
+        const double res = (P->c[j] - s[0] - P->dslack[j]) * P->dcum[j];
+        r.s[0] += res * res;
+        r.mx[0] = fmax(r.mx[0], fabs(res));
+        r.s[1] += P->dslack[j] * P->ref_xh[j];
+    }
+    const Cx *cx;
+    __device__ __forceinline__ void long_red(int lid, Red<2, 1> &lr) const { add_long(*cx, MAT_AT, lid, lr); }
+};
+
+__device__ bool run_polish_eval(Cx &cx, bool primal) {
+    const Prob &P = cx.P;
+    const Args &a = cx.a;
+    double t[3], o[2];
+    {
+        Red<2, 1> r;
+        r.zero();
+        if (primal) {
+            Gat g{P.xh};
+            EpiPolishRows e{&P, &cx};
+            spmv(cx, P.M[MAT_A], g, e, r);
+            if (!greduce<2, 1>(cx, r, 1u << MAT_A, t)) return false;
+        } else {
+            Gat g{P.yh};
+            EpiPolishCols e{&P, &cx};
+            spmv(cx, P.M[MAT_AT], g, e, r);
+            if (!greduce<2, 1>(cx, r, 1u << MAT_AT, t)) return false;
+        }
+    }
+    {
+        Red<2, 0> r;
+        r.zero();
+        if (primal) {
+            foreach_elem(cx, P.n, [&](int j) { r.s[0] += P.ref_c[j] * P.xh[j]; });
+        } else {
+            foreach_elem(cx, P.m, [&](int i) {
+                const double yi = P.yh[i];
+                r.s[1] += fmax(yi, 0.0) * P.ref_clb_fin[i] + fmin(yi, 0.0) * P.ref_cub_fin[i];
+            });
+        }
+        if (!greduce<2, 0>(cx, r, 0u, o)) return false;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Ctl *c = P.ctl;
+        if (primal) {
+            const double ap = P.m > 0 ? (a.linf ? t[2] : sqrt(t[0])) : 0.0;
+            c->abs_p = ap / a.cbr;
+            c->rel_p = c->abs_p / (1.0 + a.bnd_norm);
+            c->pobj = o[0] / (a.cbr * a.ovr) + a.c0;
+        } else {
+            const double ad = a.linf ? t[2] : sqrt(t[0]);
+            c->abs_d = ad / a.ovr;
+            c->rel_d = c->abs_d / (1.0 + a.obj_norm);
+            c->dobj = (t[1] + o[1]) / (a.cbr * a.ovr) + a.c0;
+        }
+    }
+    return true;
+}
+
 /* ------------------------------------------------------------------ restart support */
 
 struct EpiSumSq {
@@ -1312,6 +1400,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_facp(Prob P, Args a) {
         break;
     case MODE_POWER_QMIN:
         ok = run_power_q(cx, true);
+        break;
+    case MODE_POLISH_EVAL_P:
+        ok = run_polish_eval(cx, true);
+        break;
+    case MODE_POLISH_EVAL_D:
+        ok = run_polish_eval(cx, false);
         break;
     default:
         ok = false;

@@ -16,6 +16,7 @@
 #include "facp_kernels.cuh"
 
 #include <algorithm>
+#include <memory>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -268,6 +269,7 @@ class FacpSolver {
     void prepare();
     void upload();
     void launch(Args a);
+    void launch(Args a, const Prob &P);
     void read_ctl();
     Args base_args(int mode) const;
     void power_iterations();
@@ -281,6 +283,8 @@ class FacpSolver {
     void set_sigma_active(double s, double zt);
     double clipped(double cur, double ratio) const;
     void print_eval() const;
+    void polish(double t_loop);
+    int polish_phase(bool primal, double pw0, double &abs_r, double &rel_r, double &obj);
     void trajectory_header() const;
     void trajectory_row(double elapsed, bool restart) const;
 
@@ -321,6 +325,9 @@ class FacpSolver {
     int restart_target_ = 0;
     int restarts_ = 0, evals_ = 0;
     bool fp32_ = false; /* FP32 segments (first phase of precision 1) */
+    /* feasibility polishing (problems without Q) */
+    int polish_iters_ = 0, polish_status_[2] = {-1, -1};
+    double polish_sec_ = 0.0;
     double fp32_best_ = INFINITY;
     int fp32_stall_ = 0, fp32_iters_ = 0;
 };
@@ -331,11 +338,6 @@ void FacpSolver::prepare() {
     if (o_.precision != 0 && o_.precision != 1) throw Error("precision must be 0 (FP64) or 1 (FP32 + FP64 refinement)");
     if (o_.precision == 1 && !(o_.fp32_switch_tol >= 0.0)) throw Error("fp32_switch_tol must be >= 0");
     if (p_.termination_evaluation_frequency < 1) throw Error("termination_evaluation_frequency must be >= 1");
-    /* QP/FA_CP/src/solver.cu:156-160 polishes after the solve; not built here
-     * (its dual phase measures a stored dual slack that only the problems
-     * without Q refresh), so the solve says so and runs without it */
-    if (p_.feasibility_polishing)
-        fprintf(stderr, "[fa_cp_gb300] feasibility polishing is not part of this library; solving without it\n");
     HostQP &P = H_;
     P.n = q->num_variables;
     P.m = q->num_constraints;
@@ -562,11 +564,14 @@ Args FacpSolver::base_args(int mode) const {
     return a;
 }
 
-void FacpSolver::launch(Args a) {
-    PDAL_CUDA(cudaMemsetAsync(P_.bar, 0, sizeof(GridBar), stream_));
-    if (P_.nlong_total > 0)
-        PDAL_CUDA(cudaMemsetAsync(P_.lpart, 0, (size_t)3 * P_.nlong_total * kSlot * 8, stream_));
-    void *args[] = {(void *)&P_, (void *)&a};
+void FacpSolver::launch(Args a) { launch(a, P_); }
+
+void FacpSolver::launch(Args a, const Prob &P) {
+    PDAL_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), stream_));
+    if (P.nlong_total > 0)
+        PDAL_CUDA(cudaMemsetAsync(P.lpart, 0, (size_t)3 * P.nlong_total * kSlot * 8, stream_));
+    Prob Pc = P;
+    void *args[] = {(void *)&Pc, (void *)&a};
     PDAL_CUDA(cudaLaunchCooperativeKernel((const void *)k_facp, dim3(grid_), dim3(kThreads), args, 0, stream_));
     ++launches_;
 }
@@ -954,6 +959,240 @@ void FacpSolver::perform_restart() { /* fa_cp_core_op.cu:908-1020 */
 
 /* QP/FA_CP/src/solver.cu:35-70: one CSV row per evaluation point (the file
  * is created with its header before the loop and reopened for each row). */
+/* ---------------- feasibility polishing (fa_cp_core_op.cu:1241-1735) ----------------
+ * Built for problems without Q (for a QP the reference's dual phase measures
+ * a dual slack that nothing refreshes, and it runs to its limits).  Each phase
+ * runs the solve's iteration (the same persistent kernel and evaluation
+ * cadence) on a copy of the state whose problem is the feasibility problem:
+ * primal phase, c = 0 and objective constant 0, from the solve's primal
+ * iterates with the dual ones at zero; dual phase, every finite bound zero,
+ * from the solve's dual iterates and dual slack with the primal ones at zero.
+ * Both use the primal weight of the start of the solve, restart by the
+ * solve's rule on a one-sided fixed-point error by moving the anchor to the
+ * current point, and stop when their relative residual is at most
+ * eps_feas_polish_relative (utils.cu:1360-1384).  As in the reference's loop,
+ * a phase runs one more iteration after its stopping test and counts
+ * total - 1 iterations. */
+namespace {
+struct DevBuf {
+    void *p = nullptr;
+    explicit DevBuf(size_t bytes) { PDAL_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 16))); }
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+};
+
+__global__ void k_zero_finite_copy(const double *__restrict__ src, double *dst, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        dst[i] = isfinite(src[i]) ? 0.0 : src[i];
+}
+} // namespace
+
+int FacpSolver::polish_phase(bool primal, double pw0, double &abs_r, double &rel_r, double &obj) {
+    const size_t n = H_.n, m = H_.m, mm = std::max<size_t>(m, 1), nr = std::max<size_t>(H_.nr, 1);
+    std::vector<std::unique_ptr<DevBuf>> keep;
+    auto buf = [&](size_t len) {
+        keep.emplace_back(new DevBuf(len * sizeof(double)));
+        return (double *)keep.back()->p;
+    };
+    auto zeros = [&](size_t len) {
+        double *p = buf(len);
+        PDAL_CUDA(cudaMemsetAsync(p, 0, std::max<size_t>(len, 1) * sizeof(double), stream_));
+        return p;
+    };
+    auto copy = [&](const double *src, size_t len) {
+        double *p = buf(len);
+        if (len) PDAL_CUDA(cudaMemcpyAsync(p, src, len * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+        return p;
+    };
+    auto zero_finite = [&](const double *src, size_t len) {
+        double *p = buf(len);
+        if (len) k_zero_finite_copy<<<(int)std::min<size_t>((len + kThreads - 1) / kThreads, 1024), kThreads, 0,
+                                      stream_>>>(src, p, (int)len);
+        return p;
+    };
+    Prob Q = P_;
+    Q.ref_c = P_.c;
+    Q.ref_clb_fin = P_.clb_fin;
+    Q.ref_cub_fin = P_.cub_fin;
+    Q.ref_xh = P_.xh;
+    if (primal) { /* fa_cp_core_op.cu:1410-1478 */
+        Q.c = zeros(n);
+        Q.x0 = copy(P_.x0, n);
+        Q.x = copy(P_.x, n);
+        Q.xh = copy(P_.xh, n);
+        Q.xbar = copy(P_.xbar, n);
+        Q.y0 = zeros(mm);
+        Q.y = zeros(mm);
+        Q.yh = zeros(mm);
+        Q.ybar = zeros(mm);
+        Q.dprod = zeros(n);
+        Q.dslack = zeros(n);
+    } else { /* fa_cp_core_op.cu:1525-1607 */
+        Q.clb = zero_finite(P_.clb, m);
+        Q.cub = zero_finite(P_.cub, m);
+        Q.vlb = zero_finite(P_.vlb, n);
+        Q.vub = zero_finite(P_.vub, n);
+        Q.clb_fin = zeros(mm);
+        Q.cub_fin = zeros(mm);
+        Q.vlb_fin = zeros(n);
+        Q.vub_fin = zeros(n);
+        Q.y0 = copy(P_.y0, m);
+        Q.y = copy(P_.y, m);
+        Q.yh = copy(P_.yh, m);
+        Q.ybar = copy(P_.ybar, m);
+        Q.dprod = copy(P_.dprod, n);
+        Q.dslack = copy(P_.dslack, n);
+        Q.x0 = zeros(n);
+        Q.x = zeros(n);
+        Q.xh = zeros(n);
+        Q.xbar = zeros(n);
+    }
+    Q.aldual = zeros(mm);
+    Q.dx = zeros(n);
+    Q.dy = zeros(mm);
+    Q.qx = zeros(n);
+    Q.grad = zeros(n);
+    Q.dir = zeros(n);
+    Q.rx = zeros(nr);
+    keep.emplace_back(new DevBuf(sizeof(Ctl)));
+    Q.ctl = (Ctl *)keep.back()->p;
+    Ctl cl = ctl_; /* the state copy keeps the inner solver's tolerance */
+    cl.fp = INFINITY;
+    cl.fp_first = INFINITY;
+    cl.status = 0;
+    PDAL_CUDA(cudaMemcpyAsync(Q.ctl, &cl, sizeof(Ctl), cudaMemcpyHostToDevice, stream_));
+    auto read = [&]() {
+        PDAL_CUDA(cudaMemcpyAsync(&cl, Q.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_));
+        PDAL_CUDA(cudaStreamSynchronize(stream_));
+        if (cl.status != 0) throw Error("the persistent kernel gave up waiting at a grid barrier");
+    };
+    const auto &T = p_.termination_criteria;
+    const auto &R = p_.restart_params;
+    const int F = p_.termination_evaluation_frequency;
+    int total = 0, inner = 0, status = TERMINATION_REASON_UNSPECIFIED;
+    double fp = INFINITY, fp0 = INFINITY, fp_last = INFINITY;
+    bool major = false, do_restart = false;
+    const double t0 = now_sec();
+    while (status == TERMINATION_REASON_UNSPECIFIED) { /* fa_cp_core_op.cu:1313-1355, 1362-1404 */
+        if (major || total == 0 || total % print_frequency_host(total) == 0) {
+            Args a = base_args(primal ? MODE_POLISH_EVAL_P : MODE_POLISH_EVAL_D);
+            a.pw = pw0;
+            a.c0 = primal ? 0.0 : H_.c0;
+            launch(a, Q);
+            read();
+            abs_r = primal ? cl.abs_p : cl.abs_d;
+            rel_r = primal ? cl.rel_p : cl.rel_d;
+            obj = primal ? cl.pobj : cl.dobj;
+            if (rel_r <= T.eps_feas_polish_relative)
+                status = TERMINATION_REASON_FEAS_POLISH_SUCCESS;
+            else if (total >= T.iteration_limit)
+                status = TERMINATION_REASON_ITERATION_LIMIT;
+            else if (now_sec() - t0 >= T.time_sec_limit)
+                status = TERMINATION_REASON_TIME_LIMIT;
+        }
+        if (major || total == 0) { /* utils.cu:464-492, then fa_cp_core_op.cu:1649-1668 */
+            bool rs = false;
+            if (total == F) {
+                rs = true;
+            } else if (total > F) {
+                if (fp <= R.sufficient_reduction_for_restart * fp0) rs = true;
+                if (fp <= R.necessary_reduction_for_restart * fp0 && fp > fp_last) rs = true;
+                if (inner >= R.artificial_restart_threshold * total) rs = true;
+            }
+            fp_last = fp;
+            do_restart = rs;
+            if (rs) {
+                const size_t len = primal ? n : m;
+                double *anchor = primal ? Q.x0 : Q.y0, *cur = primal ? Q.x : Q.y;
+                const double *sol = primal ? Q.xh : Q.yh;
+                if (len) {
+                    PDAL_CUDA(cudaMemcpyAsync(anchor, sol, len * 8, cudaMemcpyDeviceToDevice, stream_));
+                    PDAL_CUDA(cudaMemcpyAsync(cur, sol, len * 8, cudaMemcpyDeviceToDevice, stream_));
+                }
+                inner = 0;
+                fp_last = INFINITY;
+            }
+        }
+        /* up to the next evaluation point, or the one iteration the
+         * reference's loop runs after its stopping test */
+        int t_end = total + 1;
+        if (status == TERMINATION_REASON_UNSPECIFIED)
+            while ((t_end % F) != 0 && (t_end % print_frequency_host(t_end)) != 0) ++t_end;
+        Args a = base_args(MODE_SEGMENT);
+        a.pw = pw0;
+        a.t0 = total;
+        a.t1 = t_end;
+        a.inner0 = inner;
+        a.fp_first = do_restart ? 1 : 0;
+        a.has_inner = has_inner_ ? 1 : 0;
+        a.inner_limit = inner_limit_;
+        a.use_al = use_al_ ? 1 : 0;
+        a.tau = step_ / pw0;
+        a.rho = step_ * pw0;
+        a.sigma = use_al_ ? al_sigma_ : 0.0;
+        a.fp32 = 0;
+        a.polish = primal ? 1 : 2;
+        launch(a, Q);
+        read();
+        major = (t_end % F) == 0;
+        if (major || do_restart) fp = cl.fp;
+        if (do_restart) {
+            fp0 = cl.fp_first;
+            do_restart = false;
+        }
+        inner += t_end - total;
+        total = t_end;
+    }
+    if (status == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+        const size_t len = primal ? n : m;
+        if (len)
+            PDAL_CUDA(cudaMemcpyAsync(primal ? P_.xh : P_.yh, primal ? Q.xh : Q.yh, len * 8, cudaMemcpyDeviceToDevice,
+                                      stream_));
+    }
+    PDAL_CUDA(cudaStreamSynchronize(stream_)); /* the phase's buffers are released next */
+    polish_iters_ += total - 1;
+    return status;
+}
+
+void FacpSolver::polish(double) { /* QP/FA_CP/src/solver.cu:156-160, fa_cp_core_op.cu:1242-1309 */
+    polish_status_[0] = polish_status_[1] = -1;
+    polish_iters_ = 0;
+    polish_sec_ = 0.0;
+    if (!p_.feasibility_polishing || reason_ == TERMINATION_REASON_PRIMAL_INFEASIBLE ||
+        reason_ == TERMINATION_REASON_DUAL_INFEASIBLE)
+        return;
+    if (qtype_ != Q_NONE) {
+        fprintf(stderr, "[fa_cp_gb300] feasibility polishing is built for problems without Q; solved without it\n");
+        return;
+    }
+    const double t0 = now_sec();
+    const auto &T = p_.termination_criteria;
+    if (ctl_.rel_p < T.eps_feas_polish_relative && ctl_.rel_d < T.eps_feas_polish_relative) return;
+    const double pw0 = p_.bound_objective_rescaling ? 1.0 : (H_.obj_norm + 1.0) / (H_.bnd_norm + 1.0);
+    double a = 0, r = 0, o = 0;
+    polish_status_[0] = polish_phase(true, pw0, a, r, o);
+    if (polish_status_[0] == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+        ctl_.abs_p = a;
+        ctl_.rel_p = r;
+        ctl_.pobj = o;
+    }
+    polish_status_[1] = polish_phase(false, pw0, a, r, o);
+    if (polish_status_[1] == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+        ctl_.abs_d = a;
+        ctl_.rel_d = r;
+        ctl_.dobj = o;
+    }
+    ctl_.gap = std::fabs(ctl_.pobj - ctl_.dobj);
+    ctl_.rel_gap = ctl_.gap / (1.0 + std::fabs(ctl_.pobj) + std::fabs(ctl_.dobj));
+    /* the result launch reads the controller block back */
+    PDAL_CUDA(cudaMemcpyAsync(P_.ctl, &ctl_, sizeof(Ctl), cudaMemcpyHostToDevice, stream_));
+    PDAL_CUDA(cudaStreamSynchronize(stream_));
+    polish_sec_ = now_sec() - t0;
+}
+
 void FacpSolver::trajectory_header() const {
     const char *path = p_.trajectory_csv;
     if (!path || !path[0]) return;
@@ -1091,6 +1330,7 @@ fa_cp_result_t *FacpSolver::run() {
         if (p_.verbose >= 2) print_eval();
     }
     elapsed = now_sec() - t_loop;
+    polish(t_loop);
 
     launch(base_args(MODE_RESULT));
     fa_cp_result_t *r = (fa_cp_result_t *)calloc(1, sizeof(fa_cp_result_t));
@@ -1130,6 +1370,8 @@ fa_cp_result_t *FacpSolver::run() {
     r->sigma_update_count = sigma_updates_;
     r->sigma_update_rule = al_available_ ? p_.sigma_update_rule : FA_CP_SIGMA_UPDATE_FIXED;
     r->termination_reason = reason_;
+    r->feasibility_iteration = polish_iters_;
+    r->feasibility_polishing_time = polish_sec_;
 
     fa_cp_gb300_stats_t &st = g_stats;
     memset(&st, 0, sizeof(st));
@@ -1154,6 +1396,8 @@ fa_cp_result_t *FacpSolver::run() {
     st.power_iterations_a = power_iters_a_;
     st.power_iterations_q = power_iters_q_;
     st.fp32_iterations = fp32_iters_;
+    st.polish_primal_status = polish_status_[0];
+    st.polish_dual_status = polish_status_[1];
     if (p_.verbose >= 1)
         printf("[fa_cp_gb300] %s after %d iterations (%lld inner), objective %.10e, rel. KKT %.2e, %.3f s\n",
                reason_ == TERMINATION_REASON_OPTIMAL ? "optimal" : "stopped", total_, (long long)ctl_.inner_total,

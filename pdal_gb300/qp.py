@@ -252,7 +252,8 @@ def result_from_c(r: N.FacpResult, m: int, n: int, stats: dict | None = None) ->
         sigma_update_count=r.sigma_update_count,
         setup_sec=r.rescaling_time_sec,
         solve_sec=r.cumulative_time_sec,
-        stats=stats or {},
+        stats={"feasibility_iteration": r.feasibility_iteration,
+               "feasibility_polishing_time": r.feasibility_polishing_time, **(stats or {})},
     )
 
 

@@ -85,6 +85,14 @@ CASES = [
          env={}, params={"eps": 1e-8, "sigma_update_rule": "fixed"}, parity=True, vectors=True, oracle=True),
     dict(name="qp_lp_through_facp", kind="qp", gen=("random_lp", {"m": 300, "n": 800, "nnz_per_col": 6, "seed": 17}),
          env={}, params={"eps": 1e-8}, parity=True, vectors=True, oracle=True),
+    # FA_CP feasibility polishing on LPs solved through FA_CP (fa_cp_core_op.cu:1241-1735)
+    dict(name="qp_lp_polish", kind="qp", gen=("random_lp", {"m": 300, "n": 800, "nnz_per_col": 6, "seed": 17}),
+         env={}, params={"eps": 1e-4, "feasibility_polishing": True, "eps_feas_polish": 1e-8}, parity=True,
+         vectors=True, oracle=True),
+    dict(name="qp_transport_polish", kind="qp",
+         gen=("transport_lp", {"supplies": 20, "demands": 20, "seed": 4001}),
+         env={}, params={"eps": 1e-4, "feasibility_polishing": True, "eps_feas_polish": 1e-8}, parity=True,
+         vectors=True, oracle=True),
     dict(name="qp_c2_20k", kind="qp",
          gen=("planted_qp", {"n": 20000, "m": 10000, "b_rows": 5000, "seed": 2000, "q_form": "sparse"}),
          env={}, params={"eps": 1e-8}, parity=True),

@@ -240,3 +240,36 @@ def test_grid_barrier_wait_runs_out_and_recovers(qp_lib):
     g = qp.solve(qd, {"eps": 1e-8, "verbose": 0}, {"device": 0})
     assert g.status == "OPTIMAL"
     assert abs(g.primal_objective - f_star) <= 1e-6 * (1 + abs(f_star))
+
+
+@pytest.mark.parametrize("gen", [("random_lp", {"m": 300, "n": 800, "nnz_per_col": 6, "seed": 17}),
+                                 ("transport_lp", {"supplies": 20, "demands": 20, "seed": 4001})],
+                         ids=["random_lp", "transport"])
+def test_feasibility_polishing_matches_oracle(qp_lib, gen):
+    """FA_CP feasibility polishing of an LP solved through FA_CP
+    (fa_cp_core_op.cu:1241-1735): both phases on the device against the
+    oracle's restatement -- same phase statuses and iteration count, the
+    polished residuals, objectives and solutions."""
+    import ref_cases as RC
+
+    d = RC.make_instance(gen, "qp")
+    p = {"eps": 1e-4, "feasibility_polishing": True, "eps_feas_polish": 1e-8, "verbose": 0}
+    g = qp.solve(d, p, {"device": 0})
+    o = O.solve_qp(d, p)
+    assert g.status == o.status == "OPTIMAL" and g.iterations == o.iterations
+    assert (g.stats["polish_primal_status"], g.stats["polish_dual_status"]) == o.stats["polish_status"] == (7, 7)
+    assert g.stats["feasibility_iteration"] == o.stats["feasibility_iteration"] > 0
+    assert g.relative_primal_residual <= 1e-8 and g.relative_dual_residual <= 1e-8
+    for a, b in ((g.primal_objective, o.primal_objective), (g.dual_objective, o.dual_objective)):
+        assert abs(a - b) <= 1e-9 * (1 + abs(b))
+    assert np.abs(g.x - o.x).max() <= 1e-9 * (1 + np.abs(o.x).max())
+    assert np.abs(g.y - o.y).max() <= 1e-9 * (1 + np.abs(o.y).max())
+
+
+def test_feasibility_polishing_skips_qps(qp_lib, capfd):
+    """A QP is solved without the polishing phases, with a warning."""
+    d, _, _ = planted_qp(n=400, m=200, b_rows=100, seed=23, q_form="sparse")
+    g = qp.solve(d, {"eps": 1e-6, "feasibility_polishing": True, "verbose": 0}, {"device": 0})
+    assert g.status == "OPTIMAL" and g.stats["feasibility_iteration"] == 0
+    assert g.stats["polish_primal_status"] == g.stats["polish_dual_status"] == -1
+    assert "built for problems without Q" in capfd.readouterr().err

@@ -90,3 +90,19 @@ def test_oracle_qp_matches_reference_solver(name):
     assert abs(o.iterations - ref["iterations"]) <= 0.02 * ref["iterations"], (o.iterations, ref["iterations"])
     if xr is not None:
         assert np.max(np.abs(o.x - xr)) / (1.0 + np.max(np.abs(xr))) <= 1e-6
+
+
+@pytest.mark.parametrize("name", [c["name"] for c in RC.CASES if c.get("oracle") and c["params"].get("feasibility_polishing")])
+def test_oracle_polishing_iterations_match_reference(lp_lib, name):
+    """The polishing phases' iteration count (result feasibility_iteration)
+    equals the reference's."""
+    from oracle import oracle as O
+
+    fx, _, _ = RC.load_fixture(name)
+    case = RC.BY_NAME[name]
+    data = RC.make_instance(case["gen"], case["kind"])
+    if case["kind"] == "qp":
+        o = O.solve_qp(data, case["params"])
+    else:
+        o = O.solve_lp(data, case["params"])
+    assert o.stats["feasibility_iteration"] == fx["ref"]["feasibility_iteration"]

@@ -117,6 +117,13 @@ typedef struct {
                                      (LP/CP_AL/src/utils.cu:919-1029, 281-297) but never calls them:
                                      default 0, as there.  Single-LP solver only */
     double eps_infeasible;        /* tolerance of those tests (default 1e-8) */
+    int persistent_loop;          /* small LPs: run the iteration, evaluation and restart loop inside one
+                                     cooperative launch (grid barriers between the products) instead of a
+                                     CUDA graph of per-iteration launches.  1 = when the problem allows it
+                                     (row blocks of at most 1,024 nonzeros, no column panels, staged or
+                                     hot-row product, restart target selection, infeasibility detection or
+                                     timing), 0 = never, -1 (default) = when it allows it and has at most
+                                     2^20 nonzeros */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */

@@ -201,6 +201,7 @@ class CpalOptions(C.Structure):
         ("primal_staged", C.c_int),
         ("infeasibility_detection", C.c_int),
         ("eps_infeasible", C.c_double),
+        ("persistent_loop", C.c_int),
     ]
 
 

@@ -356,6 +356,7 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->primal_staged = -1;
     o->infeasibility_detection = 0;
     o->eps_infeasible = 1e-8;
+    o->persistent_loop = -1;
 }
 
 /* Each variable is read the way the reference reads it

@@ -934,12 +934,10 @@ struct EvalRowEpi {
 };
 
 template <typename T, int S, bool SEL = false>
-__global__ void __launch_bounds__(kThreads) k_eval_rows(RowPlanDev plan, const int *__restrict__ rp,
-                                                        const int *__restrict__ ci, const double *__restrict__ val,
-                                                        EvalRowArgs<T> a, const CpalState *__restrict__ st) {
-    if (st->status) return;
+__device__ __forceinline__ void eval_rows_at(int blk, const RowPlanDev &plan, const int *__restrict__ rp,
+                                             const int *__restrict__ ci, const double *__restrict__ val,
+                                             const EvalRowArgs<T> &a, RowBlockSmem<S, SEL ? 4 : 3, double> &sm) {
     constexpr int NP = SEL ? 4 : 3, NS = SEL ? 10 : 6;
-    __shared__ RowBlockSmem<S, NP, double> sm;
     EvalRowEpi<T, SEL> epi;
     epi.a = a;
     const T *xh = a.xh;
@@ -955,14 +953,23 @@ __global__ void __launch_bounds__(kThreads) k_eval_rows(RowPlanDev plan, const i
     };
     Red<NS, 1> red;
     red.zero();
-    rowblock_run<S, NP, double>(plan, rp, ci, val, g, epi, red, sm);
+    rowblock_run_at<S, NP, double>(blk, plan, rp, ci, val, g, epi, red, sm);
     block_reduce<kThreads, NS, 1>(red, sm.red);
     if (threadIdx.x == 0) {
-        double *d = a.part + (size_t)blockIdx.x * kEvalStride;
+        double *d = a.part + (size_t)blk * kEvalStride;
         for (int q = 0; q < 6; ++q) d[q] = red.s[q];
         d[6] = red.mx[0];
         for (int q = 6; q < NS; ++q) d[q + 1] = red.s[q];
     }
+}
+
+template <typename T, int S, bool SEL = false>
+__global__ void __launch_bounds__(kThreads) k_eval_rows(RowPlanDev plan, const int *__restrict__ rp,
+                                                        const int *__restrict__ ci, const double *__restrict__ val,
+                                                        EvalRowArgs<T> a, const CpalState *__restrict__ st) {
+    if (st->status) return;
+    __shared__ RowBlockSmem<S, SEL ? 4 : 3, double> sm;
+    eval_rows_at<T, S, SEL>((int)blockIdx.x, plan, rp, ci, val, a, sm);
 }
 
 /* rows of A^T: q^ = A^T y^, A^T dy; dual residual, |dx|^2, <A^T dy, dx>,
@@ -1016,13 +1023,12 @@ struct EvalColEpi {
 };
 
 template <typename T, int S, bool SEL = false, bool H3 = false>
-__global__ void __launch_bounds__(kThreads) k_eval_cols(RowPlanDev plan, const int *__restrict__ rp,
-                                                        const int *__restrict__ ci, const double *__restrict__ val,
-                                                        EvalColArgs<T> a, const CpalState *__restrict__ st) {
+__device__ __forceinline__ void eval_cols_at(int blk, const RowPlanDev &plan, const int *__restrict__ rp,
+                                             const int *__restrict__ ci, const double *__restrict__ val,
+                                             const EvalColArgs<T> &a,
+                                             RowBlockSmem<S, SEL ? (H3 ? 4 : 3) : 2, double> &sm) {
     static_assert(SEL || !H3, "three-point selection extends the two-point terms");
-    if (st->status) return;
     constexpr int NP = SEL ? (H3 ? 4 : 3) : 2, NS = EvalColEpi<T, SEL, H3>::NS;
-    __shared__ RowBlockSmem<S, NP, double> sm;
     EvalColEpi<T, SEL, H3> epi;
     epi.a = a;
     const T *yh = a.yh;
@@ -1038,14 +1044,23 @@ __global__ void __launch_bounds__(kThreads) k_eval_cols(RowPlanDev plan, const i
     };
     Red<NS, 1> red;
     red.zero();
-    rowblock_run<S, NP, double>(plan, rp, ci, val, g, epi, red, sm);
+    rowblock_run_at<S, NP, double>(blk, plan, rp, ci, val, g, epi, red, sm);
     block_reduce<kThreads, NS, 1>(red, sm.red);
     if (threadIdx.x == 0) {
-        double *d = a.part + (size_t)blockIdx.x * kEvalStride;
+        double *d = a.part + (size_t)blk * kEvalStride;
         for (int q = 0; q < 6; ++q) d[q] = red.s[q];
         d[6] = red.mx[0];
         for (int q = 6; q < NS; ++q) d[q + 1] = red.s[q];
     }
+}
+
+template <typename T, int S, bool SEL = false, bool H3 = false>
+__global__ void __launch_bounds__(kThreads) k_eval_cols(RowPlanDev plan, const int *__restrict__ rp,
+                                                        const int *__restrict__ ci, const double *__restrict__ val,
+                                                        EvalColArgs<T> a, const CpalState *__restrict__ st) {
+    if (st->status) return;
+    __shared__ RowBlockSmem<S, SEL ? (H3 ? 4 : 3) : 2, double> sm;
+    eval_cols_at<T, S, SEL, H3>((int)blockIdx.x, plan, rp, ci, val, a, sm);
 }
 
 /* ---- infeasibility certificates (opt-in) ------------------------------- */
@@ -1191,13 +1206,13 @@ __device__ __forceinline__ void reduce_slots(const double *part, int nslots, Red
     block_reduce<kThreads, 10, 1>(r, sbuf);
 }
 
-static __global__ void __launch_bounds__(kThreads) k_control(const double *__restrict__ prow, int nrow_slots,
-                                                      const double *__restrict__ pcol, int ncol_slots,
-                                                      const double *__restrict__ pray_row, int nray_row,
-                                                      const double *__restrict__ pray_col, int nray_col,
-                                                      CpalState *st, CpalParams p, HalpernW *wt, HalpernWf *wtf) {
-    if (st->status) return;
-    __shared__ double sbuf[11 * (kThreads / 32)];
+/* The controller of one evaluation, run by one block: the partial sums in a
+ * fixed order, the end-of-block decisions, the next block's Halpern weights. */
+__device__ __forceinline__ void control_block(const double *__restrict__ prow, int nrow_slots,
+                                              const double *__restrict__ pcol, int ncol_slots,
+                                              const double *__restrict__ pray_row, int nray_row,
+                                              const double *__restrict__ pray_col, int nray_col, CpalState *st,
+                                              const CpalParams &p, HalpernW *wt, HalpernWf *wtf, double *sbuf) {
     Red<10, 1> r1, r2;
     reduce_slots(prow, nrow_slots, r1, sbuf);
     reduce_slots(pcol, ncol_slots, r2, sbuf);
@@ -1248,6 +1263,16 @@ static __global__ void __launch_bounds__(kThreads) k_control(const double *__res
     /* Halpern weights of the next block (the counter may have been reset) */
     const int inner = st->inner;
     for (int i = threadIdx.x + 1; i <= p.F; i += kThreads) cpal_halpern_entry(inner, i, wt[i], wtf[i]);
+}
+
+static __global__ void __launch_bounds__(kThreads) k_control(const double *__restrict__ prow, int nrow_slots,
+                                                      const double *__restrict__ pcol, int ncol_slots,
+                                                      const double *__restrict__ pray_row, int nray_row,
+                                                      const double *__restrict__ pray_col, int nray_col,
+                                                      CpalState *st, CpalParams p, HalpernW *wt, HalpernWf *wtf) {
+    if (st->status) return;
+    __shared__ double sbuf[11 * (kThreads / 32)];
+    control_block(prow, nrow_slots, pcol, ncol_slots, pray_row, nray_row, pray_col, nray_col, st, p, wt, wtf, sbuf);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1314,10 +1339,10 @@ static __global__ void __launch_bounds__(kThreads) k_dot_block(int len, const do
  * and the next predictor from the new beta.  The FP64 anchors are written
  * together with the (hi, lo) copies the FP32 phase reads. */
 template <typename T, bool BETA>
-__global__ void k_restart(const CpalState *__restrict__ st, int n, int m, const T *xh, T *x, double *x0,
-                          float2 *x0f, const T *yh, T *y, double *y0, float2 *y0f, const double *__restrict__ phat,
-                          T *ax, double *ax0, float2 *ax0f, T *u, const T *__restrict__ lb,
-                          const T *__restrict__ ub, T *xbar, T *ybar) {
+__device__ __forceinline__ void restart_all(const CpalState *__restrict__ st, int n, int m, const T *xh, T *x,
+                                            double *x0, float2 *x0f, const T *yh, T *y, double *y0, float2 *y0f,
+                                            const double *__restrict__ phat, T *ax, double *ax0, float2 *ax0f, T *u,
+                                            const T *__restrict__ lb, const T *__restrict__ ub, T *xbar, T *ybar) {
     if (st->status || !st->restart) return;
     Coefs<T> k;
     load_coefs(st, k);
@@ -1414,7 +1439,216 @@ __global__ void k_restart(const CpalState *__restrict__ st, int n, int m, const 
     }
 }
 
+/* the restart as a launch of its own (the evaluation blocks of the graph) */
+template <typename T, bool BETA>
+__global__ void k_restart(const CpalState *__restrict__ st, int n, int m, const T *xh, T *x, double *x0,
+                          float2 *x0f, const T *yh, T *y, double *y0, float2 *y0f, const double *__restrict__ phat,
+                          T *ax, double *ax0, float2 *ax0f, T *u, const T *__restrict__ lb,
+                          const T *__restrict__ ub, T *xbar, T *ybar) {
+    restart_all<T, BETA>(st, n, m, xh, x, x0, x0f, yh, y, y0, y0f, phat, ax, ax0, ax0f, u, lb, ub, xbar, ybar);
+}
+
+
 static __global__ void k_start_clock(CpalState *st) { st->t_start_ns = globaltimer_ns(); }
+
+/* ------------------------------------------------------------------ */
+/* small LPs: the whole loop in one cooperative launch                 */
+/* ------------------------------------------------------------------ */
+/* A small LP's iteration is a few microseconds of work spread over a few
+ * hundred blocks, so two kernel launches per iteration (even inside a CUDA
+ * graph) cost as much as the work.  k_cpal_loop runs evaluation blocks
+ * entirely on the device: every block of the grid (all co-resident, launched
+ * cooperatively) walks the row blocks of each product, and a grid barrier
+ * separates the primal product, the dual product, the evaluation, the
+ * controller (block 0) and the restart.  The row-block bodies, epilogues,
+ * controller and restart are the graph path's, with one difference: vectors
+ * written inside the launch are gathered through L2 (__ldcg), never through
+ * the read-only path. */
+struct LoopBar {
+    unsigned int count, gen;
+    int err, pad;
+};
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+/* Grid barrier; false (and the barrier marked failed for every block) when a
+ * wait exceeds `limit` polls. */
+__device__ __forceinline__ bool loop_sync(LoopBar *b, long long limit, int *sok) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned g = ld_acquire_gpu(&b->gen);
+        __threadfence();
+        const unsigned prev = atomicAdd(&b->count, 1u);
+        if (prev == gridDim.x - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (ld_acquire_gpu(&b->gen) == g) {
+                if (*(volatile int *)&b->err) {
+                    ok = 0;
+                    break;
+                }
+                if (++spins > limit) {
+                    atomicExch(&b->err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        if (*(volatile int *)&b->err) ok = 0;
+        *sok = ok;
+    }
+    __syncthreads();
+    return *sok != 0;
+}
+
+template <typename T>
+struct LoopArgs {
+    RowPlanDev at_it, a_it, at_ev, a_ev;
+    const int *at_rp, *at_ci, *a_rp, *a_ci;
+    const T *at_val, *a_val;      /* iteration values (the form's precision) */
+    const double *at_v64, *a_v64; /* evaluation values */
+    PrimalArgs<T> pa;
+    DualArgs<T> da;
+    const T *gat; /* gathered by the primal product: u (beta > 0) or y */
+    EvalRowArgs<T> ra;
+    EvalColArgs<T> ca;
+    CpalState *st;
+    CpalParams p;
+    HalpernW *wt;
+    HalpernWf *wtf;
+    int nrow_slots, ncol_slots;
+    int n, m;
+    double *x0, *y0, *ax0;
+    float2 *x0f, *y0f, *ax0f;
+    const double *phat;
+    LoopBar *bar;
+    long long spin_limit;
+    int max_blocks; /* evaluation blocks before the launch returns to the host */
+    int *err;
+};
+
+template <typename T>
+__device__ __forceinline__ const typename WeightT<T>::type &loop_weight(const LoopArgs<T> &L, int i);
+template <>
+__device__ __forceinline__ const HalpernW &loop_weight<double>(const LoopArgs<double> &L, int i) {
+    return L.wt[i];
+}
+template <>
+__device__ __forceinline__ const HalpernWf &loop_weight<float>(const LoopArgs<float> &L, int i) {
+    return L.wtf[i];
+}
+
+template <typename T, int S, bool MAJOR>
+__device__ __forceinline__ void loop_primal(const LoopArgs<T> &L, const Coefs<T> &k, int i,
+                                            RowBlockSmem<S, 1, T> &sm) {
+    PrimalEpi<T, MAJOR> epi;
+    epi.a = L.pa;
+    epi.k = k;
+    epi.w = loop_weight<T>(L, i).w;
+    epi.omw = loop_weight<T>(L, i).omw;
+    const T *gat = L.gat;
+    auto g = [&](int c, T *out) { out[0] = __ldcg(gat + c); };
+    Red<0, 0> red;
+    for (int blk = blockIdx.x; blk < L.at_it.nblocks; blk += gridDim.x) {
+        rowblock_run_at<S, 1, T>(blk, L.at_it, L.at_rp, L.at_ci, L.at_val, g, epi, red, sm);
+        __syncthreads();
+    }
+}
+
+template <typename T, int S, bool MAJOR, bool BETA>
+__device__ __forceinline__ void loop_dual(const LoopArgs<T> &L, const Coefs<T> &k, int i,
+                                          RowBlockSmem<S, 1, T> &sm) {
+    DualEpi<T, MAJOR, BETA> epi;
+    epi.a = L.da;
+    epi.k = k;
+    epi.w = loop_weight<T>(L, i).w;
+    epi.omw = loop_weight<T>(L, i).omw;
+    const T *xbar = L.pa.xbar;
+    auto g = [&](int c, T *out) { out[0] = __ldcg(xbar + c); };
+    Red<0, 0> red;
+    for (int blk = blockIdx.x; blk < L.a_it.nblocks; blk += gridDim.x) {
+        rowblock_run_at<S, 1, T>(blk, L.a_it, L.a_rp, L.a_ci, L.a_val, g, epi, red, sm);
+        __syncthreads();
+    }
+}
+
+template <typename T, int S, int SE, bool BETA>
+__global__ void __launch_bounds__(kThreads) k_cpal_loop(LoopArgs<T> L) {
+    constexpr size_t B1 = sizeof(RowBlockSmem<S, 1, T>), B2 = sizeof(RowBlockSmem<SE, 3, double>),
+                     B3 = sizeof(RowBlockSmem<SE, 2, double>);
+    constexpr size_t BM = B1 > B2 ? (B1 > B3 ? B1 : B3) : (B2 > B3 ? B2 : B3);
+    __shared__ __align__(16) unsigned char raw[BM];
+    __shared__ double sbuf[11 * (kThreads / 32)];
+    __shared__ int sok, sflag;
+    auto &smi = *reinterpret_cast<RowBlockSmem<S, 1, T> *>(raw);
+    auto &smr = *reinterpret_cast<RowBlockSmem<SE, 3, double> *>(raw);
+    auto &smc = *reinterpret_cast<RowBlockSmem<SE, 2, double> *>(raw);
+    const int F = L.p.F;
+    auto give_up = [&]() {
+        if (threadIdx.x == 0) {
+            atomicExch(L.err, 2);
+            atomicExch(&L.st->status, kStatusDeviceError);
+        }
+    };
+#define PDAL_LOOP_SYNC()                                                                                               \
+    do {                                                                                                               \
+        if (!loop_sync(L.bar, L.spin_limit, &sok)) {                                                                   \
+            give_up();                                                                                                 \
+            return;                                                                                                    \
+        }                                                                                                              \
+    } while (0)
+    for (int blocks = 0; blocks < L.max_blocks; ++blocks) {
+        /* every block reads the state after the same barrier */
+        if (threadIdx.x == 0) sflag = L.st->status;
+        __syncthreads();
+        if (sflag) return;
+        Coefs<T> k;
+        load_coefs(L.st, k);
+        for (int i = 1; i <= F; ++i) {
+            if (i == F)
+                loop_primal<T, S, true>(L, k, i, smi);
+            else
+                loop_primal<T, S, false>(L, k, i, smi);
+            PDAL_LOOP_SYNC();
+            if (i == F)
+                loop_dual<T, S, true, BETA>(L, k, i, smi);
+            else
+                loop_dual<T, S, false, BETA>(L, k, i, smi);
+            PDAL_LOOP_SYNC();
+        }
+        for (int blk = blockIdx.x; blk < L.a_ev.nblocks; blk += gridDim.x) {
+            eval_rows_at<T, SE, false>(blk, L.a_ev, L.a_rp, L.a_ci, L.a_v64, L.ra, smr);
+            __syncthreads();
+        }
+        for (int blk = blockIdx.x; blk < L.at_ev.nblocks; blk += gridDim.x) {
+            eval_cols_at<T, SE, false, false>(blk, L.at_ev, L.at_rp, L.at_ci, L.at_v64, L.ca, smc);
+            __syncthreads();
+        }
+        PDAL_LOOP_SYNC();
+        if (blockIdx.x == 0)
+            control_block(L.ra.part, L.nrow_slots, L.ca.part, L.ncol_slots, nullptr, 0, nullptr, 0, L.st, L.p, L.wt,
+                          L.wtf, sbuf);
+        PDAL_LOOP_SYNC();
+        restart_all<T, BETA>(L.st, L.n, L.m, L.pa.xh, L.pa.x, L.x0, L.x0f, L.da.yh, L.da.y, L.y0, L.y0f, L.phat,
+                             L.da.ax, L.ax0, L.ax0f, L.da.u, L.da.lb, L.da.ub, L.pa.xbar, L.da.ybar);
+        PDAL_LOOP_SYNC();
+        /* the end of the FP32 phase is the host's to carry out */
+        if (threadIdx.x == 0) sflag = L.st->phase_switch;
+        __syncthreads();
+        if (sflag) return;
+    }
+#undef PDAL_LOOP_SYNC
+}
 
 /* ------------------------------------------------------------------ */
 /* result (LP/CP_AL/src/solver.cu:1768-1793, 2481-2500)                 */

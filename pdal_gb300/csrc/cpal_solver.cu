@@ -262,6 +262,13 @@ class CpalSolver {
     int staged_grid_[2][2] = {{0, 0}, {0, 0}};
     int *dev_err_ = nullptr;
     void setup_staged();
+    /* the persistent cooperative loop (k_cpal_loop) for small LPs */
+    bool use_loop_ = false;
+    int loop_grid_[2] = {0, 0}; /* [FP64?] */
+    LoopBar *loop_bar_ = nullptr;
+    void setup_loop();
+    template <typename T>
+    void launch_loop(int max_blocks);
     bool staged_rows() const { return O_.primal_staged == 2; }
     void check_device_error();
     int *At_ci_hot_ = nullptr;
@@ -502,6 +509,7 @@ void CpalSolver::alloc_all() {
     alloc_plan(A_.ev);
     alloc_plan(At_.ev);
     dev_err_ = arena_.take<int>(1);
+    loop_bar_ = arena_.take<LoopBar>(1);
     if (use_panels_) {
         const size_t len = (size_t)pan_host_.len, hp = (size_t)pan_host_.H * pan_host_.P;
         const size_t n1 = std::max<size_t>(sh_r1_h.size(), 1), n2 = std::max<size_t>(sh_r2_h.size(), 1),
@@ -648,14 +656,74 @@ void CpalSolver::setup_staged() {
     });
 }
 
-/* A staging wait of k_primal_tma that ran out stops the solve
- * (status kStatusDeviceError) and is reported here as an error. */
+/* The persistent loop runs small LPs (row blocks of at most 1,024 nonzeros)
+ * on the default iteration path: no column panels, staged or hot-row primal
+ * product, restart target selection, infeasibility rays or per-launch
+ * timing, all of which the graph path carries.  Its grid is what the device
+ * holds at once (a cooperative launch), capped by the work. */
+#define PDAL_WITH_S_LOOP(Sval, ...)                   \
+    switch (Sval) {                                   \
+    case 256: {                                       \
+        constexpr int SL = 256;                       \
+        __VA_ARGS__;                                  \
+    } break;                                          \
+    case 512: {                                       \
+        constexpr int SL = 512;                       \
+        __VA_ARGS__;                                  \
+    } break;                                          \
+    case 1024: {                                      \
+        constexpr int SL = 1024;                      \
+        __VA_ARGS__;                                  \
+    } break;                                          \
+    default:                                          \
+        throw Error("persistent loop: unsupported row-block budget"); \
+    }
+
+void CpalSolver::setup_loop() {
+    const bool eligible = S_it_ <= 1024 && S_ev_ == S_it_ && !use_panels_ && !use_hot_ && !use_staged_ &&
+                          cp_.restart_select == 0 && !cp_.infeas && O_.timing == 0;
+    const bool want = O_.persistent_loop == 1 || (O_.persistent_loop < 0 && nnz_ <= (1 << 20));
+    use_loop_ = eligible && want;
+    if (!use_loop_) return;
+    int dev = 0, sms = 0, coop = 0;
+    PDAL_CUDA(cudaGetDevice(&dev));
+    PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PDAL_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) {
+        use_loop_ = false;
+        return;
+    }
+    const long long work = std::max({(long long)At_.it.hp.nblocks, (long long)A_.it.hp.nblocks,
+                                     (long long)At_.ev.hp.nblocks, (long long)A_.ev.hp.nblocks,
+                                     ((long long)std::max(n_, m_) + kThreads - 1) / kThreads, 1LL});
+    auto wave = [&](auto kernel) {
+        int occ = 0;
+        PDAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kThreads, 0));
+        if (occ < 1) throw Error("persistent loop does not fit on one SM");
+        return (int)std::min<long long>((long long)occ * sms, work);
+    };
+    PDAL_WITH_S_LOOP(S_it_, {
+        if (beta_on_) {
+            loop_grid_[0] = wave(k_cpal_loop<float, SL, SL, true>);
+            loop_grid_[1] = wave(k_cpal_loop<double, SL, SL, true>);
+        } else {
+            loop_grid_[0] = wave(k_cpal_loop<float, SL, SL, false>);
+            loop_grid_[1] = wave(k_cpal_loop<double, SL, SL, false>);
+        }
+    });
+    PDAL_CUDA(cudaMemsetAsync(loop_bar_, 0, sizeof(LoopBar), stream_));
+}
+
+/* A device wait that ran out (a staging wait of k_primal_tma, a grid
+ * barrier of k_cpal_loop) stops the solve (status kStatusDeviceError) and is
+ * reported here as an error. */
 void CpalSolver::check_device_error() {
     if (!dev_err_) return;
     int e = 0;
     PDAL_CUDA(cudaMemcpyAsync(&e, dev_err_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
     PDAL_CUDA(cudaStreamSynchronize(stream_));
-    if (e) throw Error("a staged copy of the primal product did not complete in time; the solve was stopped");
+    if (e == 1) throw Error("a staged copy of the primal product did not complete in time; the solve was stopped");
+    if (e) throw Error("a grid barrier of the persistent loop did not complete in time; the solve was stopped");
 }
 
 void CpalSolver::upload() {
@@ -1280,6 +1348,61 @@ const HalpernWf *weights<float>(const HalpernW *, const HalpernWf *w32) {
 }
 
 template <typename T>
+void CpalSolver::launch_loop(int max_blocks) {
+    auto &v = vecs<T>();
+    LoopArgs<T> L{};
+    L.at_it = At_.it.d;
+    L.a_it = A_.it.d;
+    L.at_ev = At_.ev.d;
+    L.a_ev = A_.ev.d;
+    if (m_ == 0) {
+        L.a_it.nblocks = 0;
+        L.a_ev.nblocks = 0;
+    }
+    L.at_rp = At_.rp;
+    L.at_ci = At_.ci;
+    L.a_rp = A_.rp;
+    L.a_ci = A_.ci;
+    L.at_val = matvals<T>(At_.v, At_.vf);
+    L.a_val = matvals<T>(A_.v, A_.vf);
+    L.at_v64 = At_.v;
+    L.a_v64 = A_.v;
+    L.pa = PrimalArgs<T>{v.x, v.xbar, v.xh, v.lam, anchor<T>(x0_, x0f_), v.c, v.vlb, v.vub};
+    L.da = DualArgs<T>{v.y, v.yh, v.ybar, v.ax, v.u, anchor<T>(y0_, y0f_), anchor<T>(ax0_, ax0f_), v.clb, v.cub};
+    L.gat = beta_on_ ? v.u : v.y;
+    L.ra = EvalRowArgs<T>{v.xh, v.xbar, v.yh, v.ybar, x0_, y0_, ax0_, clb_, cub_, clbf_, cubf_, rsc_, phat_, part_row_,
+                          A_.ev.d.nblocks, v.x, v.y, v.ax};
+    L.ca = EvalColArgs<T>{v.xh, v.xbar, v.yh, v.ybar, v.lam, x0_, c_, dsc_, part_col_, At_.ev.d.nblocks, v.x, v.y, y0_};
+    L.st = st_;
+    L.p = cp_;
+    L.wt = wt_;
+    L.wtf = wtf_;
+    L.nrow_slots = m_ > 0 ? A_.ev.d.nblocks + A_.ev.d.nlong : 0;
+    L.ncol_slots = At_.ev.d.nblocks + At_.ev.d.nlong;
+    L.n = n_;
+    L.m = m_;
+    const bool f32 = std::is_same<T, float>::value;
+    L.x0 = x0_;
+    L.y0 = y0_;
+    L.ax0 = ax0_;
+    L.x0f = f32 ? x0f_ : nullptr;
+    L.y0f = f32 ? y0f_ : nullptr;
+    L.ax0f = f32 ? ax0f_ : nullptr;
+    L.phat = phat_;
+    L.bar = loop_bar_;
+    L.spin_limit = 1LL << 25; /* polls of 32 ns and more: a barrier wait gives up after a second or two */
+    L.max_blocks = max_blocks;
+    L.err = dev_err_;
+    void *args[] = {(void *)&L};
+    const int grid = loop_grid_[f32 ? 0 : 1];
+    PDAL_WITH_S_LOOP(S_it_, {
+        const void *kern = beta_on_ ? (const void *)k_cpal_loop<T, SL, SL, true> : (const void *)k_cpal_loop<T, SL, SL, false>;
+        PDAL_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kThreads), args, 0, stream_));
+    });
+    launches += 1;
+}
+
+template <typename T>
 void CpalSolver::launch_primal(int koff, bool major) {
     auto &v = vecs<T>();
     PrimalArgs<T> pa{v.x, v.xbar, v.xh, v.lam, anchor<T>(x0_, x0f_), v.c, v.vlb, v.vub};
@@ -1792,21 +1915,33 @@ void CpalSolver::run_loop() {
     PDAL_LAUNCH_CHECK();
     launches += 1;
     const int fp32_cap = O_.fp32_max_iterations;
+    setup_loop();
     for (;;) {
-        cudaGraphExec_t *exec;
-        if (fp32_phase_) {
-            if (!exec32_) capture_block<float>(exec32_);
-            exec = &exec32_;
+        if (use_loop_) {
+            /* evaluation blocks on the device until a termination, the end
+             * of the FP32 phase or this many blocks (the host then checks
+             * its wall-clock guard and prints the verbose line) */
+            const int chunk = (P_.verbose || (fp32_phase_ && fp32_cap >= 0)) ? 1 : 50;
+            if (fp32_phase_)
+                launch_loop<float>(chunk);
+            else
+                launch_loop<double>(chunk);
         } else {
-            if (!exec64_) capture_block<double>(exec64_);
-            exec = &exec64_;
+            cudaGraphExec_t *exec;
+            if (fp32_phase_) {
+                if (!exec32_) capture_block<float>(exec32_);
+                exec = &exec32_;
+            } else {
+                if (!exec64_) capture_block<double>(exec64_);
+                exec = &exec64_;
+            }
+            PDAL_CUDA(cudaGraphLaunch(*exec, stream_));
+            launches += (per_block + ((fp32_phase_ ? hot_in<float>() : hot_in<double>()) ? 1 : 0)) * G;
         }
-        PDAL_CUDA(cudaGraphLaunch(*exec, stream_));
-        launches += (per_block + ((fp32_phase_ ? hot_in<float>() : hot_in<double>()) ? 1 : 0)) * G;
         PDAL_CUDA(cudaMemcpyAsync(h_st_, st_, sizeof(CpalState), cudaMemcpyDeviceToHost, stream_));
         d2h += sizeof(CpalState);
         PDAL_CUDA(cudaStreamSynchronize(stream_));
-        if (O_.timing && F >= 3 && ev_[0]) {
+        if (!use_loop_ && O_.timing && F >= 3 && ev_[0]) {
             float a = 0, b = 0, c = 0;
             PDAL_CUDA(cudaEventElapsedTime(&a, ev_[0], ev_[1]));
             PDAL_CUDA(cudaEventElapsedTime(&b, ev_[1], ev_[2]));

@@ -505,3 +505,21 @@ def test_infeasibility_detection_leaves_feasible_solves_alone(lp_lib):
     b = lp.solve(d, {"eps": 1e-8}, {"infeasibility_detection": 1})
     assert a.status == b.status == "OPTIMAL" and a.iterations == b.iterations
     assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refine"])
+@pytest.mark.parametrize("opts", [{}, {"al_lambda": 0.0}, {"al_lambda": 0.0, "sigma_mode": 1, "sigma_init_factor": 0.5}],
+                         ids=["default", "lambda0", "sigma"])
+def test_persistent_loop_matches_graph_path(lp_lib, precision, opts):
+    """The small-LP persistent loop (one cooperative launch, grid barriers)
+    runs the graph path's row blocks, epilogues, controller and restart:
+    bit-identical iterates, iteration counts and phase switch."""
+    d = I.random_lp(2000, 5000, 8, seed=0)
+    p = {"eps": 1e-7, "l_inf_ruiz_iterations": 4, "iteration_limit": 30_000}
+    base = {**opts, "precision": precision}
+    a = lp.solve(d, p, {**base, "persistent_loop": 0})
+    b = lp.solve(d, p, {**base, "persistent_loop": 1})
+    assert a.status == b.status and a.iterations == b.iterations
+    assert a.stats["fp32_iterations"] == b.stats["fp32_iterations"]
+    assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
+    assert b.stats["kernel_launches"] < a.stats["kernel_launches"]

@@ -77,8 +77,13 @@ SIGMA_PROTOCOL = {"sigma_mode": 1, "sigma_adaptive": 1, "sigma_init_factor": 0.5
                   "al_lambda": 0.0, "restart_sufficient": 0.2, "restart_necessary": 0.8, "restart_artificial": 0.36}
 PARAMS = {"eps": 1e-6, "l_inf_ruiz_iterations": 10}
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant
-# kernel on this workload, from the ncu captures summarised in profiles/
-NCU_TRAFFIC = {"k_dual<float>": 200_110_336 + 4_137_984}
+# kernel on this workload, from the ncu captures summarised in profiles/: the
+# single dual kernel measured at full size; the split dual step measured at
+# half size (102.2 MB for its three kernels) and doubled with the nonzeros
+# and rows it processes
+NCU_TRAFFIC = {"k_dual<float>": 200_110_336 + 4_137_984,
+               "dual step: k_dual_short<float> + k_dual_panels<float> + k_dual_long_finish<float>":
+                   2 * (40_567_296 + 54_784 + 60_497_920 + 348_672 + 688_640)}
 
 
 def dist_env():

@@ -277,15 +277,15 @@ def run_ours(args, rank, world, local):
     e2e_value = (b_primal + b_dual) * re.iterations * len(rese) * world / dte / 1e9
 
     # time to relative KKT 1e-6 on the plain CP_AL LP (2,000 x 5,000): the
-    # median of three solves of each form after one untimed, with the loop on
-    # the device (one cooperative launch per 50 evaluation blocks, the
-    # default for small LPs) and with one CUDA graph per evaluation block
+    # median of three solves of each form after one untimed, with one CUDA
+    # graph per evaluation block (the default) and with the loop on the device
+    # (one cooperative launch per 50 evaluation blocks)
     small = instances.random_lp(2000, 5000, 8, seed=0)
     sp = {"eps": 1e-6, "l_inf_ruiz_iterations": 4}
     kkt = {}
     for tag, opts in (("chosen", {"precision": "fp32_refine", "device": local}), ("plain_fp64", {"device": local}),
-                      ("chosen_graphs", {"precision": "fp32_refine", "device": local, "persistent_loop": 0}),
-                      ("plain_fp64_graphs", {"device": local, "persistent_loop": 0})):
+                      ("chosen_device_loop", {"precision": "fp32_refine", "device": local, "persistent_loop": 1}),
+                      ("plain_fp64_device_loop", {"device": local, "persistent_loop": 1})):
         lp.solve(small, sp, opts)
         runs = []
         for _ in range(3):

@@ -122,8 +122,8 @@ typedef struct {
                                      CUDA graph of per-iteration launches.  1 = when the problem allows it
                                      (row blocks of at most 1,024 nonzeros, no column panels, staged or
                                      hot-row product, restart target selection, infeasibility detection or
-                                     timing), 0 = never, -1 (default) = when it allows it and has at most
-                                     2^20 nonzeros */
+                                     timing); 0 or -1 (default) = never (measured no faster than the
+                                     graph path with programmatic launches, which hides the launches) */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */

@@ -1475,36 +1475,29 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
     return v;
 }
 
-/* Grid barrier; false (and the barrier marked failed for every block) when a
- * wait exceeds `limit` polls. */
-__device__ __forceinline__ bool loop_sync(LoopBar *b, long long limit, int *sok) {
+/* Grid barrier number `k` (1, 2, ... within the launch; the counter is zero
+ * at launch): one release-add per block on a monotonic counter, then an
+ * acquire spin until all blocks of the k-th barrier have arrived.  False,
+ * with the barrier marked failed for every block, when a wait exceeds
+ * `limit` polls. */
+__device__ __forceinline__ bool loop_sync(LoopBar *b, unsigned k, long long limit, int *sok) {
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        const unsigned g = ld_acquire_gpu(&b->gen);
-        __threadfence();
-        const unsigned prev = atomicAdd(&b->count, 1u);
-        if (prev == gridDim.x - 1) {
-            atomicExch(&b->count, 0u);
-            __threadfence();
-            atomicAdd(&b->gen, 1u);
-        } else {
-            long long spins = 0;
-            while (ld_acquire_gpu(&b->gen) == g) {
-                if (*(volatile int *)&b->err) {
-                    ok = 0;
-                    break;
-                }
-                if (++spins > limit) {
-                    atomicExch(&b->err, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(32);
+        const unsigned target = k * gridDim.x;
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&b->count) : "memory");
+        long long spins = 0;
+        while (ld_acquire_gpu(&b->count) < target) {
+            if (++spins > limit) {
+                atomicExch(&b->err, 1);
+                ok = 0;
+                break;
+            }
+            if ((spins & 1023) == 0 && *(volatile int *)&b->err) {
+                ok = 0;
+                break;
             }
         }
-        __threadfence();
-        if (*(volatile int *)&b->err) ok = 0;
         *sok = ok;
     }
     __syncthreads();
@@ -1600,9 +1593,10 @@ __global__ void __launch_bounds__(kThreads) k_cpal_loop(LoopArgs<T> L) {
             atomicExch(&L.st->status, kStatusDeviceError);
         }
     };
+    unsigned nsync = 0;
 #define PDAL_LOOP_SYNC()                                                                                               \
     do {                                                                                                               \
-        if (!loop_sync(L.bar, L.spin_limit, &sok)) {                                                                   \
+        if (!loop_sync(L.bar, ++nsync, L.spin_limit, &sok)) {                                                          \
             give_up();                                                                                                 \
             return;                                                                                                    \
         }                                                                                                              \

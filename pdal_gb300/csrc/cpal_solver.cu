@@ -682,7 +682,7 @@ void CpalSolver::setup_staged() {
 void CpalSolver::setup_loop() {
     const bool eligible = S_it_ <= 1024 && S_ev_ == S_it_ && !use_panels_ && !use_hot_ && !use_staged_ &&
                           cp_.restart_select == 0 && !cp_.infeas && O_.timing == 0;
-    const bool want = O_.persistent_loop == 1 || (O_.persistent_loop < 0 && nnz_ <= (1 << 20));
+    const bool want = O_.persistent_loop == 1;
     use_loop_ = eligible && want;
     if (!use_loop_) return;
     int dev = 0, sms = 0, coop = 0;
@@ -1390,11 +1390,13 @@ void CpalSolver::launch_loop(int max_blocks) {
     L.ax0f = f32 ? ax0f_ : nullptr;
     L.phat = phat_;
     L.bar = loop_bar_;
-    L.spin_limit = 1LL << 25; /* polls of 32 ns and more: a barrier wait gives up after a second or two */
+    L.spin_limit = 1LL << 22; /* polls of an L2 round trip each: a barrier wait gives up after about 2 s */
     L.max_blocks = max_blocks;
     L.err = dev_err_;
     void *args[] = {(void *)&L};
     const int grid = loop_grid_[f32 ? 0 : 1];
+    /* the barrier counter counts up from zero within a launch */
+    PDAL_CUDA(cudaMemsetAsync(loop_bar_, 0, sizeof(LoopBar), stream_));
     PDAL_WITH_S_LOOP(S_it_, {
         const void *kern = beta_on_ ? (const void *)k_cpal_loop<T, SL, SL, true> : (const void *)k_cpal_loop<T, SL, SL, false>;
         PDAL_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kThreads), args, 0, stream_));
@@ -1921,7 +1923,10 @@ void CpalSolver::run_loop() {
             /* evaluation blocks on the device until a termination, the end
              * of the FP32 phase or this many blocks (the host then checks
              * its wall-clock guard and prints the verbose line) */
-            const int chunk = (P_.verbose || (fp32_phase_ && fp32_cap >= 0)) ? 1 : 50;
+            int chunk = (P_.verbose || (fp32_phase_ && fp32_cap >= 0)) ? 1 : 50;
+            /* the launch's barrier counter (blocks x barriers) stays below 2^31 */
+            const long long per = (2LL * F + 3) * std::max(loop_grid_[0], loop_grid_[1]);
+            chunk = (int)std::max(1LL, std::min<long long>(chunk, (1LL << 31) / std::max(per, 1LL)));
             if (fp32_phase_)
                 launch_loop<float>(chunk);
             else

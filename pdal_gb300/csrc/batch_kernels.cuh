@@ -137,10 +137,25 @@ struct EvalRowsB : Base {
 /* ------------------------------------------------------------------ setup */
 
 /* Ruiz (mode 0) or Pock-Chambolle (mode 1) pass, the block-level form of
- * k_row_scale / k_scale_matrix / k_scale_vectors (same operation order). */
+ * k_row_scale / k_scale_matrix / k_scale_vectors (same operation order: the
+ * Pock-Chambolle sums in row order in one lane, as the reference adds them). */
 __device__ void blk_scale_pass(const BInst &I, int mode, double deg_rows, double deg_cols) {
     auto row_scale = [&](int nr, const int *rp, const double *val, double deg, double *scale, double *cum) {
         blk_rows(nr, [&](int row, int lane) {
+            if (mode != 0) {
+                if (lane == 0) {
+                    double acc = 0.0;
+                    for (int k = rp[row]; k < rp[row + 1]; ++k) {
+                        double v = fabs(val[k]);
+                        if (!isfinite(v)) v = 0.0;
+                        acc += deg == 2.0 ? v * v : deg == 1.0 ? v : deg == 0.5 ? sqrt(v) : pow(v, deg);
+                    }
+                    const double s = (acc < 1e-12) ? 1.0 : sqrt(acc);
+                    cum[row] *= s;
+                    scale[row] = s;
+                }
+                return;
+            }
             double acc = 0.0;
             for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) {
                 double v = fabs(val[k]);

@@ -1689,40 +1689,63 @@ __global__ void k_convert(const A *__restrict__ src, B *dst, int len) {
 
 /* warp per row: s = clamp_sqrt(max |a| or sum |a|^deg), cum *= s
  * (preconditioner.cu:532-550, 634-667). mode 0 = abs max, 1 = power sum. */
+/* Equilibration passes over the rows of a CSR matrix.  Rows of at most
+ * kEqShort nonzeros (nearly all rows of a sparse LP) run one thread per row;
+ * the longer rows, listed once at upload (`lrows`), run one warp per row in
+ * the same launch.  (A warp per row for every row left 31 lanes idle on the
+ * one-entry rows of a power-law LP and made each pass latency-bound.) */
+constexpr int kEqShort = 32;
+
+__device__ __forceinline__ double row_scale_term(double v, int mode, double deg) {
+    v = fabs(v);
+    if (!isfinite(v)) v = 0.0;
+    if (mode == 0) return v;
+    if (deg == 2.0) return v * v;
+    if (deg == 1.0) return v;
+    if (deg == 0.5) return sqrt(v);
+    return pow(v, deg);
+}
+
+__device__ __forceinline__ void row_scale_store(int row, double acc, double *scale, double *cum, double *inv) {
+    const double s = (acc < 1e-12) ? 1.0 : sqrt(acc);
+    cum[row] *= s;
+    scale[row] = s;
+    inv[row] = 1.0 / s;
+}
+
+/* Ruiz (mode 0: max |a|) or Pock-Chambolle (mode 1: sum |a|^deg) row scale
+ * (LP/CP_AL/src/preconditioner.cu:273-378, 600-657).  The sums run in row
+ * order in one thread, as the reference's kernel adds them (a long row too);
+ * the maxima of the long rows take a warp (the order does not matter). */
 static __global__ void k_row_scale(int nr, const int *__restrict__ rp, const double *__restrict__ val, int mode, double deg,
-                            double *scale, double *cum, double *inv) {
-    const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nr; row += warps) {
+                            double *scale, double *cum, double *inv, const int *__restrict__ lrows, int nlong) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    for (int row = t; row < nr; row += nt) {
+        const int k0 = rp[row], k1 = rp[row + 1];
+        if (k1 - k0 > kEqShort) continue;
         double acc = 0.0;
-        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) {
-            double v = fabs(val[k]);
-            if (!isfinite(v)) v = 0.0;
-            if (mode == 0) {
-                acc = fmax(acc, v);
-            } else {
-                double pv;
-                if (deg == 2.0)
-                    pv = v * v;
-                else if (deg == 1.0)
-                    pv = v;
-                else if (deg == 0.5)
-                    pv = sqrt(v);
-                else
-                    pv = pow(v, deg);
-                acc += pv;
-            }
+        for (int k = k0; k < k1; ++k) {
+            const double pv = row_scale_term(val[k], mode, deg);
+            acc = mode == 0 ? fmax(acc, pv) : acc + pv;
         }
-        if (mode == 0)
-            acc = warp_max(acc);
-        else
-            acc = warp_sum(acc);
-        if (lane == 0) {
-            const double s = (acc < 1e-12) ? 1.0 : sqrt(acc);
-            cum[row] *= s;
-            scale[row] = s;
-            inv[row] = 1.0 / s;
+        row_scale_store(row, acc, scale, cum, inv);
+    }
+    if (mode != 0) {
+        for (int q = t; q < nlong; q += nt) {
+            const int row = lrows[q];
+            double acc = 0.0;
+            for (int k = rp[row]; k < rp[row + 1]; ++k) acc += row_scale_term(val[k], mode, deg);
+            row_scale_store(row, acc, scale, cum, inv);
         }
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    for (int q = t >> 5; q < nlong; q += nt >> 5) {
+        const int row = lrows[q];
+        double acc = 0.0;
+        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) acc = fmax(acc, row_scale_term(val[k], 0, deg));
+        acc = warp_max(acc);
+        if (lane == 0) row_scale_store(row, acc, scale, cum, inv);
     }
 }
 
@@ -1732,10 +1755,20 @@ static __global__ void k_row_scale(int nr, const int *__restrict__ rp, const dou
  * nonzero: the FP64 divisions dominated this kernel on GB300's FP64 pipe). */
 static __global__ void k_scale_matrix(int nr, const int *__restrict__ rp, const int *__restrict__ ci, double *val,
                                const double *__restrict__ inv_rowscale, const double *__restrict__ inv_colscale,
-                               int row_is_var) {
+                               int row_is_var, const int *__restrict__ lrows, int nlong) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    for (int row = t; row < nr; row += nt) {
+        const int k0 = rp[row], k1 = rp[row + 1];
+        if (k1 - k0 > kEqShort) continue;
+        const double inv_row = inv_rowscale[row];
+        for (int k = k0; k < k1; ++k) {
+            const double inv_col = inv_colscale[ci[k]];
+            val[k] *= row_is_var ? inv_row * inv_col : inv_col * inv_row;
+        }
+    }
     const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nr; row += warps) {
+    for (int q = t >> 5; q < nlong; q += nt >> 5) {
+        const int row = lrows[q];
         const double inv_row = inv_rowscale[row];
         for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) {
             const double inv_col = inv_colscale[ci[k]];

@@ -261,6 +261,9 @@ class CpalSolver {
     bool use_staged_ = false;
     int staged_grid_[2][2] = {{0, 0}, {0, 0}};
     int *dev_err_ = nullptr;
+    /* rows longer than kEqShort nonzeros (equilibration: a warp each) */
+    std::vector<int> eq_long_h_[2];
+    int *eq_long_[2] = {nullptr, nullptr}; /* [A, A^T] */
     void setup_staged();
     /* the persistent cooperative loop (k_cpal_loop) for small LPs */
     bool use_loop_ = false;
@@ -509,6 +512,7 @@ void CpalSolver::alloc_all() {
     alloc_plan(A_.ev);
     alloc_plan(At_.ev);
     dev_err_ = arena_.take<int>(1);
+    for (int q = 0; q < 2; ++q) eq_long_[q] = arena_.take<int>(std::max<size_t>(eq_long_h_[q].size(), 1));
     loop_bar_ = arena_.take<LoopBar>(1);
     if (use_panels_) {
         const size_t len = (size_t)pan_host_.len, hp = (size_t)pan_host_.H * pan_host_.P;
@@ -793,11 +797,24 @@ void CpalSolver::upload() {
             use_panels_ = pan_host_.H > 0;
         }
     }
+    {
+        auto longs = [](int nr, const int *rp, std::vector<int> &out) {
+            out.clear();
+            for (int r = 0; r < nr; ++r)
+                if (rp[r + 1] - rp[r] > kEqShort) out.push_back(r);
+        };
+        longs(m_, prob_->constraint_matrix_row_pointers, eq_long_h_[0]);
+        longs(n_, At_host_.rp.data(), eq_long_h_[1]);
+    }
     arena_.begin_measure();
     alloc_all();
     arena_.reserve_measured();
     alloc_all();
     PDAL_CUDA(cudaMemsetAsync(dev_err_, 0, sizeof(int), stream_));
+    for (int q = 0; q < 2; ++q)
+        if (!eq_long_h_[q].empty())
+            PDAL_CUDA(cudaMemcpyAsync(eq_long_[q], eq_long_h_[q].data(), eq_long_h_[q].size() * sizeof(int),
+                                      cudaMemcpyHostToDevice, stream_));
     setup_staged();
 
     const size_t n = n_, m = m_, nnz = nnz_;
@@ -1116,11 +1133,16 @@ void CpalSolver::setup_device() {
     /* reciprocal scales: an m- and an n-sized buffer the iteration has not
      * started to use (x_bar is cleared before the first iteration) */
     double *rinv = tmp_m2_, *dinv = v64_.xbar;
+    const int nla = (int)eq_long_h_[0].size(), nlt = (int)eq_long_h_[1].size();
+    const int geq_m = grid_for(std::max<long long>(m, 32LL * nla)), geq_n = grid_for(std::max<long long>(n, 32LL * nlt));
     auto scale_pass = [&](int mode, double deg_rows, double deg_cols) {
-        if (m) k_row_scale<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.v, mode, deg_rows, rstep, rsc_, rinv);
-        k_row_scale<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.v, mode, deg_cols, dstep, dsc_, dinv);
-        if (m) k_scale_matrix<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, A_.v, rinv, dinv, 0);
-        k_scale_matrix<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, At_.v, dinv, rinv, 1);
+        if (m)
+            k_row_scale<<<geq_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.v, mode, deg_rows, rstep, rsc_, rinv, eq_long_[0],
+                                                         nla);
+        k_row_scale<<<geq_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.v, mode, deg_cols, dstep, dsc_, dinv, eq_long_[1],
+                                                     nlt);
+        if (m) k_scale_matrix<<<geq_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, A_.v, rinv, dinv, 0, eq_long_[0], nla);
+        k_scale_matrix<<<geq_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, At_.v, dinv, rinv, 1, eq_long_[1], nlt);
         k_scale_vectors<<<grid_for(std::max(n, m)), kThreads, 0, stream_>>>(n_, m_, dstep, rstep, c_, vlb_, vub_, x0_,
                                                                             clb_, cub_, y0_);
         PDAL_LAUNCH_CHECK();
@@ -1161,8 +1183,9 @@ void CpalSolver::setup_device() {
         }
         if (m) k_cr_exp<<<gm, kThreads, 0, stream_>>>(m_, lr, rinv, rsc_);
         k_cr_exp<<<gn, kThreads, 0, stream_>>>(n_, lc, dinv, dsc_);
-        if (m) k_scale_matrix<<<gwr_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, A_.v, rinv, dinv, 0);
-        k_scale_matrix<<<gwr_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, At_.v, dinv, rinv, 1);
+        if (m)
+            k_scale_matrix<<<geq_m, kThreads, 0, stream_>>>(m_, A_.rp, A_.ci, A_.v, rinv, dinv, 0, eq_long_[0], nla);
+        k_scale_matrix<<<geq_n, kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, At_.v, dinv, rinv, 1, eq_long_[1], nlt);
         k_scale_vectors_inv<<<grid_for(std::max(n, m)), kThreads, 0, stream_>>>(n_, m_, lc, dinv, lr, rinv, c_, vlb_,
                                                                                 vub_, x0_, clb_, cub_, y0_);
         PDAL_LAUNCH_CHECK();

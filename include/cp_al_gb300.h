@@ -100,7 +100,7 @@ typedef struct {
     int power_method;             /* sigma_max(A)^2 before the iteration: 0 = the reference's power
                                      iteration (LP/CP_AL/src/utils.cu:87-228, sv_max_iter, sv_tol);
                                      otherwise (default -1) the FP32_REFINE form uses Lanczos on
-                                     A A^T with FP32 products -- at most min(512, sv_max_iter)
+                                     A A^T with FP32 products -- at most min(128, sv_max_iter)
                                      steps, stopping when the largest Ritz value moves by less than
                                      1e-8 relative over 16 steps -- and the FP64 form the power
                                      iteration */

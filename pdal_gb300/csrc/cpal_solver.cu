@@ -47,7 +47,10 @@ int grid_for(long long len, int per_block = kThreads) {
 #define PDAL_LAUNCH_CHECK() PDAL_CUDA(cudaGetLastError())
 
 /* Lanczos steps at most, and the steps between two convergence checks */
-constexpr int kLanczosMax = 512;
+/* On the large LP the largest Ritz value after 128 steps (0.99989) is already
+ * above the reference's power-iteration estimate after 5,000 steps (0.99987);
+ * it is a lower bound, and the step's 0.998 margin covers the rest. */
+constexpr int kLanczosMax = 128;
 constexpr int kLanczosChunk = 16;
 
 /* Largest eigenvalue of the symmetric tridiagonal matrix with diagonal a[0..k)

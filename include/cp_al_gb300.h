@@ -124,6 +124,9 @@ typedef struct {
                                      hot-row product, restart target selection, infeasibility detection or
                                      timing); 0 or -1 (default) = never (measured no faster than the
                                      graph path with programmatic launches, which hides the launches) */
+    int device_transpose;         /* A^T built on the device (scatter, then a sort by row per column;
+                                     exactly the host transpose) when no column has more than 2,048
+                                     nonzeros: -1 (default) or 1 = so, 0 = on the host threads */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */

@@ -146,4 +146,9 @@ HostPanels plan_panels(int nr, int nc, const int *rp, const int *ci, int S, int 
  * requested: enough blocks to cover the 152 SMs twice, at most 2048. */
 int auto_block_nnz(long long nnz, int nr);
 
+/* Row pointers of the transpose of an nr x nc CSR matrix (its column counts,
+ * summed), on the host threads; the transpose itself can then be built on
+ * the device. */
+std::vector<int> csr_transpose_rp(int nr, int nc, const int *rp, const int *ci);
+
 } // namespace pdal

@@ -1689,13 +1689,124 @@ __global__ void k_convert(const A *__restrict__ src, B *dst, int len) {
 
 /* warp per row: s = clamp_sqrt(max |a| or sum |a|^deg), cum *= s
  * (preconditioner.cu:532-550, 634-667). mode 0 = abs max, 1 = power sum. */
+/* ------------------------------------------------------------------ */
+/* the transpose A^T built on the device                               */
+/* ------------------------------------------------------------------ */
+/* With the transpose's row pointers from the host (column counts), each
+ * nonzero of A is placed in its column's segment by an atomic cursor -- rows
+ * of at most kEqShort nonzeros one thread each, the listed longer rows a warp
+ * each -- and every segment is then sorted by row index, moving the values
+ * along.  Row indices within a column are distinct, so the result is exactly
+ * the host transpose (rows in increasing order in every column), whatever
+ * order the atomics took.  Columns of up to 32 entries are sorted by one
+ * thread (insertion sort), the listed longer ones (up to kTransposeSort) by a
+ * block (bitonic sort in shared memory). */
+constexpr int kTransposeSort = 2048;
+/* rows (columns) longer than this take a warp (a block) in the passes below */
+constexpr int kEqShort = 32;
+
+static __global__ void k_transpose_scatter(int nr, const int *__restrict__ rp, const int *__restrict__ ci,
+                                           const double *__restrict__ v, int *cursor, int *tci, double *tv,
+                                           const int *__restrict__ lrows, int nlong) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    for (int row = t; row < nr; row += nt) {
+        const int k0 = rp[row], k1 = rp[row + 1];
+        if (k1 - k0 > kEqShort) continue;
+        for (int k = k0; k < k1; ++k) {
+            const int p = atomicAdd(&cursor[ci[k]], 1);
+            tci[p] = row;
+            tv[p] = v[k];
+        }
+    }
+    const int lane = threadIdx.x & 31;
+    for (int q = t >> 5; q < nlong; q += nt >> 5) {
+        const int row = lrows[q];
+        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+            const int p = atomicAdd(&cursor[ci[k]], 1);
+            tci[p] = row;
+            tv[p] = v[k];
+        }
+    }
+}
+
+/* columns of at most kEqShort entries: insertion sort by row, one thread each */
+static __global__ void k_transpose_sort_short(int nc, const int *__restrict__ trp, int *tci, double *tv) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nc; j += gridDim.x * blockDim.x) {
+        const int k0 = trp[j], k1 = trp[j + 1];
+        if (k1 - k0 > kEqShort) continue;
+        for (int k = k0 + 1; k < k1; ++k) {
+            const int key = tci[k];
+            const double val = tv[k];
+            int q = k - 1;
+            while (q >= k0 && tci[q] > key) {
+                tci[q + 1] = tci[q];
+                tv[q + 1] = tv[q];
+                --q;
+            }
+            tci[q + 1] = key;
+            tv[q + 1] = val;
+        }
+    }
+}
+
+/* the listed longer columns: a block each, bitonic sort of the segment
+ * (padded to a power of two with keys above every row) in shared memory */
+static __global__ void __launch_bounds__(kThreads) k_transpose_sort_long(const int *__restrict__ trp, int *tci,
+                                                                          double *tv, const int *__restrict__ lcols,
+                                                                          int nlong) {
+    __shared__ int key[kTransposeSort];
+    __shared__ double val[kTransposeSort];
+    for (int q = blockIdx.x; q < nlong; q += gridDim.x) {
+        const int j = lcols[q], k0 = trp[j], len = trp[j + 1] - k0;
+        int n2 = 1;
+        while (n2 < len) n2 <<= 1;
+        for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+            key[i] = i < len ? tci[k0 + i] : 0x7fffffff;
+            val[i] = i < len ? tv[k0 + i] : 0.0;
+        }
+        __syncthreads();
+        for (int size = 2; size <= n2; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+                    const int p = i ^ stride;
+                    if (p > i) {
+                        const bool up = (i & size) == 0;
+                        if ((key[i] > key[p]) == up) {
+                            const int tk = key[i];
+                            key[i] = key[p];
+                            key[p] = tk;
+                            const double tvv = val[i];
+                            val[i] = val[p];
+                            val[p] = tvv;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = threadIdx.x; i < len; i += blockDim.x) {
+            tci[k0 + i] = key[i];
+            tv[k0 + i] = val[i];
+        }
+        __syncthreads();
+    }
+}
+
+/* A^T's column indices with the long rows of A (hot_id >= 0) as -1 - h */
+static __global__ void k_hot_indices(long long nnz, const int *__restrict__ ci, const int *__restrict__ hot_id,
+                                     int *ci_hot) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nnz;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int r = ci[k], h = hot_id[r];
+        ci_hot[k] = h >= 0 ? -1 - h : r;
+    }
+}
+
 /* Equilibration passes over the rows of a CSR matrix.  Rows of at most
  * kEqShort nonzeros (nearly all rows of a sparse LP) run one thread per row;
  * the longer rows, listed once at upload (`lrows`), run one warp per row in
  * the same launch.  (A warp per row for every row left 31 lanes idle on the
  * one-entry rows of a power-law LP and made each pass latency-bound.) */
-constexpr int kEqShort = 32;
-
 __device__ __forceinline__ double row_scale_term(double v, int mode, double deg) {
     v = fabs(v);
     if (!isfinite(v)) v = 0.0;

@@ -220,6 +220,10 @@ class CpalSolver {
     CpalParams cp_{};
     int n_ = 0, m_ = 0, nnz_ = 0;
     HostCsr At_host_;
+    /* A^T built on the device from its host row pointers (k_transpose_*),
+     * or on the host threads when a column is too long for the device sort */
+    bool device_transpose_ = false;
+    int *at_cursor_ = nullptr, *hot_id_d_ = nullptr;
     int S_it_ = 2048, S_ev_ = 1024;
     bool beta_on_ = false;
     bool fp32_phase_ = false;
@@ -461,8 +465,15 @@ void CpalSolver::prepare() {
         throw Error("constraint bounds missing");
     csr_validate(m_, n_, prob_->constraint_matrix_row_pointers, prob_->constraint_matrix_col_indices, nnz_,
                  "constraint matrix");
-    At_host_ = csr_transpose(m_, n_, prob_->constraint_matrix_row_pointers, prob_->constraint_matrix_col_indices,
-                             prob_->constraint_matrix_values);
+    At_host_.rp = csr_transpose_rp(m_, n_, prob_->constraint_matrix_row_pointers, prob_->constraint_matrix_col_indices);
+    int longest = 0;
+    for (int j = 0; j < n_; ++j) longest = std::max(longest, At_host_.rp[j + 1] - At_host_.rp[j]);
+    device_transpose_ = O_.device_transpose != 0 && longest <= kTransposeSort;
+    At_host_.nr = n_;
+    At_host_.nc = m_;
+    if (!device_transpose_)
+        At_host_ = csr_transpose(m_, n_, prob_->constraint_matrix_row_pointers, prob_->constraint_matrix_col_indices,
+                                 prob_->constraint_matrix_values);
     S_it_ = O_.spmv_nnz_per_block > 0 ? O_.spmv_nnz_per_block : auto_block_nnz(nnz_, std::max(m_, n_));
     if (S_it_ != 256 && S_it_ != 512 && S_it_ != 1024 && S_it_ != 2048)
         throw Error("spmv_nnz_per_block must be 256, 512, 1024 or 2048");
@@ -516,6 +527,8 @@ void CpalSolver::alloc_all() {
     alloc_plan(At_.ev);
     dev_err_ = arena_.take<int>(1);
     for (int q = 0; q < 2; ++q) eq_long_[q] = arena_.take<int>(std::max<size_t>(eq_long_h_[q].size(), 1));
+    if (device_transpose_) at_cursor_ = arena_.take<int>(n + 1);
+    if (device_transpose_ && use_hot_) hot_id_d_ = arena_.take<int>(std::max<size_t>(m, 1));
     loop_bar_ = arena_.take<LoopBar>(1);
     if (use_panels_) {
         const size_t len = (size_t)pan_host_.len, hp = (size_t)pan_host_.H * pan_host_.P;
@@ -830,8 +843,21 @@ void CpalSolver::upload() {
     up(A_.ci, prob_->constraint_matrix_col_indices, nnz * sizeof(int));
     up(Av0_, prob_->constraint_matrix_values, nnz * sizeof(double));
     up(At_.rp, At_host_.rp.data(), (n + 1) * sizeof(int));
-    up(At_.ci, At_host_.ci.data(), nnz * sizeof(int));
-    up(Atv0_, At_host_.v.data(), nnz * sizeof(double));
+    if (device_transpose_) {
+        PDAL_CUDA(cudaMemcpyAsync(at_cursor_, At_.rp, (n + 1) * sizeof(int), cudaMemcpyDeviceToDevice, stream_));
+        const int nla = (int)eq_long_h_[0].size(), nlt = (int)eq_long_h_[1].size();
+        if (m > 0)
+            k_transpose_scatter<<<grid_for(std::max<long long>(m, 32LL * nla)), kThreads, 0, stream_>>>(
+                m_, A_.rp, A_.ci, Av0_, at_cursor_, At_.ci, Atv0_, eq_long_[0], nla);
+        k_transpose_sort_short<<<grid_for(n), kThreads, 0, stream_>>>(n_, At_.rp, At_.ci, Atv0_);
+        if (nlt > 0)
+            k_transpose_sort_long<<<std::min(nlt, 152 * 4), kThreads, 0, stream_>>>(At_.rp, At_.ci, Atv0_, eq_long_[1],
+                                                                                 nlt);
+        PDAL_LAUNCH_CHECK();
+    } else {
+        up(At_.ci, At_host_.ci.data(), nnz * sizeof(int));
+        up(Atv0_, At_host_.v.data(), nnz * sizeof(double));
+    }
     upload_plan(A_.it);
     upload_plan(At_.it);
     upload_plan(A_.ev);
@@ -846,17 +872,24 @@ void CpalSolver::upload() {
         if (use_hot_) {
             std::vector<int> hot_id(m, -1);
             for (int h = 0; h < pan_host_.H; ++h) hot_id[pan_host_.rows[h]] = h;
-            std::vector<int> cih(At_host_.ci.size());
-            const int nt = host_threads((long long)cih.size());
-            parallel_for(nt, [&](int t) {
-                const size_t k0 = cih.size() * t / nt, k1 = cih.size() * (t + 1) / nt;
-                for (size_t k = k0; k < k1; ++k) {
-                    const int r = At_host_.ci[k];
-                    cih[k] = hot_id[r] >= 0 ? -1 - hot_id[r] : r;
-                }
-            });
-            up(At_ci_hot_, cih.data(), cih.size() * sizeof(int));
-            PDAL_CUDA(cudaStreamSynchronize(stream_)); /* cih leaves scope */
+            if (device_transpose_) {
+                up(hot_id_d_, hot_id.data(), m * sizeof(int));
+                k_hot_indices<<<grid_for((long long)nnz), kThreads, 0, stream_>>>((long long)nnz, At_.ci, hot_id_d_,
+                                                                                 At_ci_hot_);
+                PDAL_LAUNCH_CHECK();
+            } else {
+                std::vector<int> cih(At_host_.ci.size());
+                const int nt = host_threads((long long)cih.size());
+                parallel_for(nt, [&](int t) {
+                    const size_t k0 = cih.size() * t / nt, k1 = cih.size() * (t + 1) / nt;
+                    for (size_t k = k0; k < k1; ++k) {
+                        const int r = At_host_.ci[k];
+                        cih[k] = hot_id[r] >= 0 ? -1 - hot_id[r] : r;
+                    }
+                });
+                up(At_ci_hot_, cih.data(), cih.size() * sizeof(int));
+            }
+            PDAL_CUDA(cudaStreamSynchronize(stream_)); /* hot_id / cih leave scope */
             int dev = 0, sms = 0;
             PDAL_CUDA(cudaGetDevice(&dev));
             PDAL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

@@ -523,3 +523,41 @@ def test_persistent_loop_matches_graph_path(lp_lib, precision, opts):
     assert a.stats["fp32_iterations"] == b.stats["fp32_iterations"]
     assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
     assert b.stats["kernel_launches"] < a.stats["kernel_launches"]
+
+
+@pytest.mark.parametrize("case", ["zipf_panels_hot", "dense_columns", "random"])
+def test_device_transpose_is_the_host_transpose(lp_lib, case):
+    """A^T built on the device (atomic scatter, then every column sorted by
+    row: one thread for short columns, a block's bitonic sort for long ones)
+    is the host transpose exactly: bit-identical iterates with either, also
+    with the long rows' hot-index copy of A^T (FP64 panel path)."""
+    if case == "zipf_panels_hot":
+        d = I.zipf_lp(20_000, 40_000, 400_000, seed=1002)
+        opts = {"al_lambda": 0.0, "dual_panels": 1, "panel_width": 4096}
+    elif case == "dense_columns":
+        d = I.random_lp(2000, 5000, 8, seed=4)
+        rp, ci, v, (m, n) = d.csr()
+        rows = np.repeat(np.arange(m), np.diff(rp))
+        # columns 7, 11 and 13 get 600, 1,900 and 2,000 entries: the block sort
+        extra = [(7, np.arange(0, m, 3)[:600]), (11, np.arange(0, m, 1)[:1900]), (13, np.arange(0, m)[:2000])]
+        keep = ~np.isin(ci, [7, 11, 13])
+        rr, cc, vv = [rows[keep]], [ci[keep]], [v[keep]]
+        for col, rws in extra:
+            rr.append(rws)
+            cc.append(np.full(rws.size, col))
+            vv.append(np.random.default_rng(col).standard_normal(rws.size))
+        import scipy.sparse as sp
+
+        A = sp.csr_matrix((np.concatenate(vv), (np.concatenate(rr), np.concatenate(cc))), shape=(m, n))
+        A.sort_indices()
+        d.A = (A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data, (m, n))
+        opts = {}
+    else:
+        d = I.random_lp(300, 800, 6, seed=9)
+        opts = {}
+    p = {"eps": 1e-14, "iteration_limit": 600, "sv_max_iter": 200, "time_limit": 120}
+    a = lp.solve(d, p, {**opts, "device_transpose": 0})
+    b = lp.solve(d, p, {**opts, "device_transpose": 1})
+    assert a.iterations == b.iterations
+    assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
+    assert b.stats["h2d_bytes"] < a.stats["h2d_bytes"]

@@ -124,6 +124,10 @@ typedef struct {
                                      hot-row product, restart target selection, infeasibility detection or
                                      timing); 0 or -1 (default) = never (measured no faster than the
                                      graph path with programmatic launches, which hides the launches) */
+    int dual_fused_finish;        /* with the panel path: the group that writes a long row's last panel
+                                     partial also sums the row's partials (fixed order) and runs its
+                                     dual epilogue, instead of a separate launch.  0 = separate launch,
+                                     1 or -1 (default) = fused */
     int device_transpose;         /* A^T built on the device (scatter, then a sort by row per column;
                                      exactly the host transpose) when no column has more than 2,048
                                      nonzeros: -1 (default) or 1 = so, 0 = on the host threads */

@@ -202,6 +202,7 @@ class CpalOptions(C.Structure):
         ("infeasibility_detection", C.c_int),
         ("eps_infeasible", C.c_double),
         ("persistent_loop", C.c_int),
+        ("dual_fused_finish", C.c_int),
         ("device_transpose", C.c_int),
     ]
 

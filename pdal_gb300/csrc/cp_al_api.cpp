@@ -357,6 +357,7 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->infeasibility_detection = 0;
     o->eps_infeasible = 1e-8;
     o->persistent_loop = -1;
+    o->dual_fused_finish = -1;
     o->device_transpose = -1;
 }
 

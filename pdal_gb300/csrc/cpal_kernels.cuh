@@ -617,6 +617,10 @@ struct PanelDev {
     T *part;
     T *hot; /* the long rows' entries of the primal product's gathered vector (or null) */
     int H, P, W, nblocks;
+    /* the row's last segment finishes it (k_dual_panels with FUSE): arrivals
+     * per long row (zero between launches) and segments per long row */
+    unsigned *cnt;
+    const int *nseg;
 };
 
 constexpr int kPanelThreads = 512;
@@ -675,11 +679,20 @@ __device__ __forceinline__ void panel_stage(T *sx, const T *__restrict__ xbar, i
     for (int i = nvec * V + threadIdx.x; i < wlen; i += kPanelThreads) sx[i] = __ldcg(xbar + col0 + i);
 }
 
-template <typename T>
+/* The long rows' partial sums of one launch; with FUSE the group that writes
+ * a row's last partial (an arrival counter per row) also adds the row's P
+ * partials in FP64 in a fixed order -- 8 lanes over the panels, then a fixed
+ * shuffle tree -- and runs the dual epilogue, so that no separate launch is
+ * needed (k_dual_long_finish does the same in its own launch). */
+template <typename T, bool FUSE, bool MAJOR, bool BETA>
 __global__ void __launch_bounds__(kPanelThreads, sizeof(T) == 4 ? 2 : 1) k_dual_panels(PanelDev<T> pd,
                                                                                       const T *__restrict__ xbar,
                                                                                       int n,
-                                                                                      const CpalState *__restrict__ st) {
+                                                                                      const CpalState *__restrict__ st,
+                                                                                      DualArgs<T> a,
+                                                                                      const typename WeightT<T>::type
+                                                                                          *__restrict__ wt,
+                                                                                      int koff) {
     pdl_enter();
     if (st->status) return;
     extern __shared__ __align__(16) unsigned char panel_smem[];
@@ -691,6 +704,24 @@ __global__ void __launch_bounds__(kPanelThreads, sizeof(T) == 4 ? 2 : 1) k_dual_
     /* the groups of a warp may run different numbers of segments: each
      * shuffles among its own lanes only */
     const unsigned mask = ((1u << kPanelLanes) - 1u) << ((threadIdx.x & 31) & ~(kPanelLanes - 1));
+    auto finish_row = [&](int h) {
+        __threadfence();
+        double s = 0.0;
+        for (int q = li; q < pd.P; q += kPanelLanes) s += (double)__ldcg(&pd.part[(size_t)h * pd.P + q]);
+#pragma unroll
+        for (int o = kPanelLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(mask, s, o, kPanelLanes);
+        if (li == 0) {
+            DualEpi<T, MAJOR, BETA> epi;
+            epi.a = a;
+            load_coefs(st, epi.k);
+            epi.w = wt[koff].w;
+            epi.omw = wt[koff].omw;
+            const int i = pd.rows[h];
+            epi.finish(i, (T)s, epi.fetch(i));
+            if (pd.hot) pd.hot[h] = BETA ? a.u[i] : a.y[i];
+            pd.cnt[h] = 0u;
+        }
+    };
     for (int pc = c.x; pc < c.y; ++pc) {
         /* the segments of this block in panel p: [sbeg, send) */
         const int4 pie = pd.piece[pc];
@@ -739,9 +770,21 @@ __global__ void __launch_bounds__(kPanelThreads, sizeof(T) == 4 ? 2 : 1) k_dual_
                 acc_a += __shfl_xor_sync(mask, acc_a, o, kPanelLanes);
                 acc_b += __shfl_xor_sync(mask, acc_b, o, kPanelLanes);
             }
+            int last_a = 0, last_b = 0;
             if (li == 0) {
                 pd.part[(size_t)sa.x * pd.P + sa.w] = acc_a;
                 if (two) pd.part[(size_t)sb.x * pd.P + sb.w] = acc_b;
+                if (FUSE) {
+                    __threadfence();
+                    last_a = atomicAdd(&pd.cnt[sa.x], 1u) == (unsigned)(pd.nseg[sa.x] - 1);
+                    if (two) last_b = atomicAdd(&pd.cnt[sb.x], 1u) == (unsigned)(pd.nseg[sb.x] - 1);
+                }
+            }
+            if (FUSE) {
+                last_a = __shfl_sync(mask, last_a, 0, kPanelLanes);
+                last_b = __shfl_sync(mask, last_b, 0, kPanelLanes);
+                if (last_a) finish_row(sa.x);
+                if (last_b) finish_row(sb.x);
             }
         }
     }

@@ -257,6 +257,10 @@ class CpalSolver {
     int4 *pan_seg_ = nullptr, *pan_piece_ = nullptr, *pan_cta_ = nullptr;
     uint16_t *pan_off_ = nullptr;
     double *pan_v64_ = nullptr, *pan_part64_ = nullptr;
+    /* the fused finish of the long rows: arrivals and segments per long row */
+    bool fuse_finish_ = false;
+    unsigned *pan_cnt_ = nullptr;
+    int *pan_nseg_ = nullptr;
     float *pan_v32_ = nullptr, *pan_part32_ = nullptr;
     /* the same long rows' gathered values in shared memory in the primal
      * product (k_primal_hot): A^T's column indices with entry -1 - h for long
@@ -287,7 +291,9 @@ class CpalSolver {
     template <typename T>
     PanelDev<T> panel_dev() const;
     /* kernels one iteration launches */
-    int iter_launches() const { return 1 + (m_ == 0 ? 0 : use_panels_ ? (sh_b1_ + sh_b2_ + sh_b3_ > 0 ? 3 : 2) : 1); }
+    int iter_launches() const {
+        return 1 + (m_ == 0 ? 0 : use_panels_ ? (sh_b1_ + sh_b2_ + sh_b3_ > 0 ? 2 : 1) + (fuse_finish_ ? 0 : 1) : 1);
+    }
 
   public:
     int panel_rows() const { return use_panels_ ? pan_host_.H : 0; }
@@ -355,13 +361,15 @@ template <>
 PanelDev<double> CpalSolver::panel_dev<double>() const {
     return PanelDev<double>{pan_rows_, pan_seg_, pan_piece_, pan_cta_, pan_v64_, pan_off_, pan_part64_,
                             hot_in<double>() ? hot64_ : nullptr,
-                            pan_host_.H, pan_host_.P, pan_host_.W, (int)(pan_host_.cta.size() / 4)};
+                            pan_host_.H, pan_host_.P, pan_host_.W, (int)(pan_host_.cta.size() / 4), pan_cnt_,
+                            pan_nseg_};
 }
 template <>
 PanelDev<float> CpalSolver::panel_dev<float>() const {
     return PanelDev<float>{pan_rows_, pan_seg_, pan_piece_, pan_cta_, pan_v32_, pan_off_, pan_part32_,
                            hot_in<float>() ? hot32_ : nullptr,
-                           pan_host_.H, pan_host_.P, pan_host_.W, (int)(pan_host_.cta.size() / 4)};
+                           pan_host_.H, pan_host_.P, pan_host_.W, (int)(pan_host_.cta.size() / 4), pan_cnt_,
+                           pan_nseg_};
 }
 
 void CpalSolver::release() {
@@ -554,6 +562,8 @@ void CpalSolver::alloc_all() {
         }
         pan_v64_ = arena_.take<double>(len);
         pan_part64_ = arena_.take<double>(hp);
+        pan_cnt_ = arena_.take<unsigned>(std::max(pan_host_.H, 1));
+        pan_nseg_ = arena_.take<int>(std::max(pan_host_.H, 1));
         if (fp32_phase_) {
             pan_v32_ = arena_.take<float>(len);
             pan_part32_ = arena_.take<float>(hp);
@@ -811,6 +821,7 @@ void CpalSolver::upload() {
             sh_b2_ = blocks((long long)sh_r2_h.size(), kThreads / 8, 152 * 1);
             sh_b3_ = blocks((long long)sh_r3_h.size(), kThreads / 32, 152 * 2);
             use_panels_ = pan_host_.H > 0;
+            fuse_finish_ = O_.dual_fused_finish != 0;
         }
     }
     {
@@ -913,6 +924,14 @@ void CpalSolver::upload() {
         up(pan_off_, pan_host_.off.data(), len * sizeof(uint16_t));
         /* (row, panel) pairs without a segment keep a zero partial */
         PDAL_CUDA(cudaMemsetAsync(pan_part64_, 0, hp * sizeof(double), stream_));
+        {
+            /* segments per long row: a row's last one finishes it */
+            std::vector<int> nseg(std::max(pan_host_.H, 1), 0);
+            for (size_t q = 0; q + 3 < pan_host_.seg.size(); q += 4) nseg[pan_host_.seg[q]]++;
+            up(pan_nseg_, nseg.data(), nseg.size() * sizeof(int));
+            PDAL_CUDA(cudaMemsetAsync(pan_cnt_, 0, nseg.size() * sizeof(unsigned), stream_));
+            PDAL_CUDA(cudaStreamSynchronize(stream_)); /* nseg leaves scope */
+        }
         if (pan_part32_) PDAL_CUDA(cudaMemsetAsync(pan_part32_, 0, hp * sizeof(float), stream_));
     }
     up(c0_, prob_->objective_vector, n * sizeof(double));
@@ -1267,10 +1286,22 @@ void CpalSolver::setup_device() {
             k_panel_gather<double><<<grid_for(n1), kThreads, 0, stream_>>>(sh_p1_, A_.v, sh_v64_, n1);
             if (fp32_phase_) k_panel_gather<float><<<grid_for(n1), kThreads, 0, stream_>>>(sh_p1_, A_.v, sh_v32_, n1);
         }
-        PDAL_CUDA(cudaFuncSetAttribute(k_dual_panels<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)panel_smem_bytes<double>(pan_host_.W)));
-        PDAL_CUDA(cudaFuncSetAttribute(k_dual_panels<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)panel_smem_bytes<float>(pan_host_.W)));
+        {
+            const int s64 = (int)panel_smem_bytes<double>(pan_host_.W), s32 = (int)panel_smem_bytes<float>(pan_host_.W);
+            auto attr = [](auto kernel, int bytes) {
+                PDAL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            };
+            attr(k_dual_panels<double, false, false, false>, s64);
+            attr(k_dual_panels<double, true, false, false>, s64);
+            attr(k_dual_panels<double, true, false, true>, s64);
+            attr(k_dual_panels<double, true, true, false>, s64);
+            attr(k_dual_panels<double, true, true, true>, s64);
+            attr(k_dual_panels<float, false, false, false>, s32);
+            attr(k_dual_panels<float, true, false, false>, s32);
+            attr(k_dual_panels<float, true, false, true>, s32);
+            attr(k_dual_panels<float, true, true, false>, s32);
+            attr(k_dual_panels<float, true, true, true>, s32);
+        }
         PDAL_LAUNCH_CHECK();
         launches += fp32_phase_ ? 2 : 1;
     }
@@ -1572,7 +1603,29 @@ void CpalSolver::launch_dual(int koff, bool major, bool timed) {
      * the dual epilogue */
     if (timed) PDAL_CUDA(cudaEventRecordWithFlags(ev_[4], stream_, cudaEventRecordExternal));
     const PanelDev<T> pd = panel_dev<T>();
-    launch_pdl_cfg(k_dual_panels<T>, pd.nblocks, kPanelThreads, panel_smem_bytes<T>(pd.W), stream_, pd, xbar, n_, st);
+    const size_t psm = panel_smem_bytes<T>(pd.W);
+    if (fuse_finish_) {
+        /* the group that writes a long row's last partial finishes the row */
+        if (major) {
+            if (beta_on_)
+                launch_pdl_cfg(k_dual_panels<T, true, true, true>, pd.nblocks, kPanelThreads, psm, stream_, pd, xbar,
+                               n_, st, da, wt, koff);
+            else
+                launch_pdl_cfg(k_dual_panels<T, true, true, false>, pd.nblocks, kPanelThreads, psm, stream_, pd, xbar,
+                               n_, st, da, wt, koff);
+        } else {
+            if (beta_on_)
+                launch_pdl_cfg(k_dual_panels<T, true, false, true>, pd.nblocks, kPanelThreads, psm, stream_, pd, xbar,
+                               n_, st, da, wt, koff);
+            else
+                launch_pdl_cfg(k_dual_panels<T, true, false, false>, pd.nblocks, kPanelThreads, psm, stream_, pd, xbar,
+                               n_, st, da, wt, koff);
+        }
+        if (timed) PDAL_CUDA(cudaEventRecordWithFlags(ev_[5], stream_, cudaEventRecordExternal));
+        return;
+    }
+    launch_pdl_cfg(k_dual_panels<T, false, false, false>, pd.nblocks, kPanelThreads, psm, stream_, pd, xbar, n_, st, da,
+                   wt, koff);
     if (timed) PDAL_CUDA(cudaEventRecordWithFlags(ev_[5], stream_, cudaEventRecordExternal));
     const int gf = (pd.H * 32 + kThreads - 1) / kThreads;
     if (major) {

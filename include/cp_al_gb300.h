@@ -126,8 +126,10 @@ typedef struct {
                                      graph path with programmatic launches, which hides the launches) */
     int dual_fused_finish;        /* with the panel path: the group that writes a long row's last panel
                                      partial also sums the row's partials (fixed order) and runs its
-                                     dual epilogue, instead of a separate launch.  0 = separate launch,
-                                     1 or -1 (default) = fused */
+                                     dual epilogue, instead of a separate launch.  1 = fused; 0 or -1
+                                     (default) = a separate launch (measured twice as fast: the fused
+                                     form fences and counts once per segment, 160,000 times on the
+                                     large LP) */
     int device_transpose;         /* A^T built on the device (scatter, then a sort by row per column;
                                      exactly the host transpose) when no column has more than 2,048
                                      nonzeros: -1 (default) or 1 = so, 0 = on the host threads */

@@ -821,7 +821,7 @@ void CpalSolver::upload() {
             sh_b2_ = blocks((long long)sh_r2_h.size(), kThreads / 8, 152 * 1);
             sh_b3_ = blocks((long long)sh_r3_h.size(), kThreads / 32, 152 * 2);
             use_panels_ = pan_host_.H > 0;
-            fuse_finish_ = O_.dual_fused_finish != 0;
+            fuse_finish_ = O_.dual_fused_finish == 1;
         }
     }
     {

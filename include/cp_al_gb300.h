@@ -133,6 +133,31 @@ typedef struct {
     int device_transpose;         /* A^T built on the device (scatter, then a sort by row per column;
                                      exactly the host transpose) when no column has more than 2,048
                                      nonzeros: -1 (default) or 1 = so, 0 = on the host threads */
+
+    /* --- benchmark controllers of the reference (off by default there and here; single-LP
+     *     solver only) --- */
+    int alpha_direct_pulse;       /* CP_AL_ALPHA_DIRECT_PULSE (LP/CP_AL/src/solver.cu:885-1032): at the
+                                     first restart after 10,000 iterations with two recorded
+                                     zero-alpha epochs (evaluation frequency 200, at least 400
+                                     iterations left) the gate is evaluated once; when it passes, one
+                                     evaluation block runs at alpha = 0.002 outside sigma mode, then
+                                     alpha returns to 0 */
+    int pulse_force;              /* CP_AL_DETERMINISTIC_PULSE_FORCE: the gate passes (it never passes
+                                     otherwise, as in the reference) */
+    int pulse_trace;              /* CP_AL_ALPHA_DIRECT_PULSE_TRACE (the pulse's stderr lines are printed
+                                     whenever the pulse is enabled, as there) */
+    int pulse_test_limit;         /* CP_AL_ALPHA_DIRECT_PULSE_TEST_TRAJECTORY_LIMIT: > 0 ends the solve
+                                     (ITERATION_LIMIT) once the pulse is over and this many iterations
+                                     are done */
+    int sigma_trigger;            /* CP_AL_SIGMA_TRIGGER (solver.cu:1496-1527): outside sigma mode, at an
+                                     evaluation after sigma_trigger_min_iters, switch sigma mode on
+                                     (the sigma initialisation of solver.cu:3141-3164) and restart when
+                                     rel. primal >= sigma_trigger_primal, rel. dual <=
+                                     sigma_trigger_dual and their ratio >= sigma_trigger_ratio */
+    int sigma_trigger_min_iters;  /* CP_AL_SIGMA_TRIGGER_MIN_ITERS, 200 */
+    double sigma_trigger_primal;  /* CP_AL_SIGMA_TRIGGER_PRIMAL, 1e-2 */
+    double sigma_trigger_dual;    /* CP_AL_SIGMA_TRIGGER_DUAL, 1e-6 */
+    double sigma_trigger_ratio;   /* CP_AL_SIGMA_TRIGGER_RATIO, 1e6 */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */
@@ -181,6 +206,12 @@ typedef struct {
     double avg_dual_panels_ms;
     double avg_dual_rows32_ms;
     double avg_dual_panels32_ms;
+    /* benchmark controllers: iteration at which the alpha pulse's positive
+     * block started (-1: never), its gate (0 not evaluated, 1 passed, 2
+     * rejected), iteration at which the sigma trigger fired (0: never) */
+    int pulse_start_iteration;
+    int pulse_gate;
+    int sigma_trigger_iteration;
 } cp_al_gb300_stats_t;
 
 /* The reference defaults of every field, ignoring the environment. */
@@ -193,10 +224,8 @@ void cp_al_gb300_options_from_env(cp_al_gb300_options_t *opts);
 /* Name of the first CP_AL_* environment switch that turns on a controller of
  * the reference this library does not implement -- adaptive lambda
  * (CP_AL_ADAPTIVE_LAMBDA, the race / auto CP_AL_LAMBDA_PROFILE values),
- * dynamic evaluation frequency (CP_AL_DYNAMIC_EVAL), the sigma trigger
- * (CP_AL_SIGMA_TRIGGER outside sigma mode), the alpha rollback trial
- * (CP_AL_ALPHA_ROLLBACK_TRIAL) or the alpha pulse (CP_AL_ALPHA_DIRECT_PULSE)
- * -- or NULL.  solve_lp_problem
+ * dynamic evaluation frequency (CP_AL_DYNAMIC_EVAL) or the alpha rollback
+ * trial (CP_AL_ALPHA_ROLLBACK_TRIAL) -- or NULL.  solve_lp_problem
  * returns NULL with a message while one is set, instead of solving without
  * it.  Diagnostic and trace switches are ignored. */
 const char *cp_al_gb300_unbuilt_switch(void);

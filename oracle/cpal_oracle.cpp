@@ -45,6 +45,7 @@ namespace {
 int g_threads = 1;
 int g_polish_status[2] = {-1, -1};
 int g_restart_targets[3] = {0, 0, 0};
+int g_controllers[3] = {-1, 0, 0}; /* pulse start iteration, pulse gate, sigma trigger iteration */
 
 struct Csr {
     int nr = 0, nc = 0;
@@ -123,6 +124,68 @@ struct Solver {
     termination_reason_t reason = TERMINATION_REASON_UNSPECIFIED;
     int power_iters = 0, restarts = 0;
     int restarts_to[3] = {0, 0, 0}; /* restarts by target: current point, reflected, plain Halpern */
+    /* benchmark controllers (LP/CP_AL/src/solver.cu:198-272 state): the
+     * alpha pulse's phase (0 idle, 1 positive block, 2 over) and gate (0 not
+     * evaluated, 1 passed, 2 rejected), the epoch being measured and the last
+     * two zero-alpha epochs; the sigma trigger's iteration */
+    int pulse_phase = 0, pulse_gate = 0, pulse_start = -1;
+    bool epoch_valid = false;
+    int epoch_total = 0, hist_count = 0;
+    int hist_k[2] = {0, 0};
+    double hist_rate[2] = {0.0, 0.0};
+    double epoch_p = 0, epoch_d = 0, epoch_g = 0;
+    int trigger_iter = 0;
+
+    static double metric(double v) { return std::fmax(std::fabs(v), 1e-300); } /* solver.cu:415-418 */
+    static double log_rate(double a, double b, int k) {                        /* solver.cu:420-428 */
+        if (k <= 0 || !std::isfinite(a) || !std::isfinite(b)) return NAN;
+        const double r = std::log(metric(a) / metric(b)) / (double)k;
+        return std::isfinite(r) ? r : NAN;
+    }
+    /* solver.cu:616-678, at a restart before the restart itself */
+    void record_epoch() {
+        if (!epoch_valid || al_lambda > 0.0) return;
+        const int k = total - epoch_total;
+        const double fr = log_rate(fp0, fp, k);
+        const double pr = log_rate(epoch_p, rel_p, k), dr = log_rate(epoch_d, rel_d, k);
+        const double gr = log_rate(epoch_g, rel_gap, k);
+        const double kr = log_rate(std::fmax(epoch_p, std::fmax(epoch_d, epoch_g)),
+                                   std::fmax(metric(rel_p), std::fmax(metric(rel_d), metric(rel_gap))), k);
+        const bool ok = k > 0 && std::isfinite(fr) && std::isfinite(pr) && std::isfinite(dr) && std::isfinite(gr) &&
+                        std::isfinite(kr);
+        if (!ok) return;
+        if (hist_count < 2) {
+            hist_k[hist_count] = k;
+            hist_rate[hist_count] = fr;
+            ++hist_count;
+        } else {
+            hist_k[0] = hist_k[1];
+            hist_rate[0] = hist_rate[1];
+            hist_k[1] = k;
+            hist_rate[1] = fr;
+        }
+    }
+    void epoch_start() { /* solver.cu:605-614 */
+        epoch_valid = true;
+        epoch_total = total;
+        epoch_p = metric(rel_p);
+        epoch_d = metric(rel_d);
+        epoch_g = metric(rel_gap);
+    }
+    /* solver.cu:899-988: evaluated once, after a restart */
+    void pulse_gate_eval(int F, int limit) {
+        if (!O.alpha_direct_pulse || pulse_gate || pulse_phase || hist_count < 2 || total < 10000 || F != 200) return;
+        if (limit - total < 400) return;
+        for (int i = 0; i < 2; ++i)
+            if (hist_k[i] <= 0 || !std::isfinite(hist_rate[i])) return;
+        pulse_gate = O.pulse_force ? 1 : 2;
+        if (!O.pulse_force) return;
+        pulse_phase = 1;
+        pulse_start = total;
+        sigma_mode = false;
+        al_lambda = 0.002;
+        refresh_step_schedule();
+    }
 
     double kp() const { return std::isnan(O.sigma_kp) ? P->restart_params.k_p : O.sigma_kp; }
 
@@ -821,6 +884,15 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->persistent_loop = -1;
     o->dual_fused_finish = -1;
     o->device_transpose = -1;
+    o->alpha_direct_pulse = 0;
+    o->pulse_force = 0;
+    o->pulse_trace = 0;
+    o->pulse_test_limit = 0;
+    o->sigma_trigger = 0;
+    o->sigma_trigger_min_iters = 200;
+    o->sigma_trigger_primal = 1e-2;
+    o->sigma_trigger_dual = 1e-6;
+    o->sigma_trigger_ratio = 1e6;
 }
 
 /* LP/CP_AL/src/utils.cu:361-394 (reflection coefficient without the
@@ -955,10 +1027,41 @@ bool oracle_block(Solver &S, bool &do_restart, int &charged, double elapsed, int
     }
     S.check_termination(elapsed);
     if (S.reason == TERMINATION_REASON_UNSPECIFIED && charged >= limit) S.reason = TERMINATION_REASON_ITERATION_LIMIT;
+    const cp_al_gb300_options_t &O = S.O;
+    if (O.alpha_direct_pulse && S.pulse_phase == 1) {
+        /* solver.cu:990-1007: alpha back to 0 and the fixed-point error
+         * taken again with the refreshed steps, terminated or not */
+        S.sigma_mode = false;
+        S.al_lambda = 0.0;
+        S.refresh_step_schedule();
+        S.fixed_point_error();
+        S.pulse_phase = 2;
+    }
+    if (S.reason == TERMINATION_REASON_UNSPECIFIED && O.alpha_direct_pulse && O.pulse_test_limit > 0 &&
+        S.pulse_phase == 2 && S.total >= O.pulse_test_limit) /* solver.cu:1386-1391, 1418-1424 */
+        S.reason = TERMINATION_REASON_ITERATION_LIMIT;
     if (S.reason != TERMINATION_REASON_UNSPECIFIED) return true;
     S.choose_restart_candidate(elapsed);
-    do_restart = S.should_restart(F);
-    if (do_restart) S.perform_restart();
+    /* solver.cu:1496-1527: the sigma trigger; a forced restart skips the
+     * restart rule */
+    bool forced = false;
+    if (O.sigma_trigger && !S.sigma_mode && S.total >= O.sigma_trigger_min_iters) {
+        const double rpr = std::fmax(S.rel_p, 1e-300), rdr = std::fmax(S.rel_d, 1e-300);
+        if (rpr >= O.sigma_trigger_primal && rdr <= O.sigma_trigger_dual && rpr / rdr >= O.sigma_trigger_ratio) {
+            S.initialize_sigma_parameters();
+            S.trigger_iter = S.total;
+            forced = true;
+        }
+    }
+    do_restart = forced || S.should_restart(F);
+    if (do_restart) {
+        if (O.alpha_direct_pulse) S.record_epoch();
+        S.perform_restart();
+        if (O.alpha_direct_pulse) {
+            S.epoch_start();
+            S.pulse_gate_eval(F, limit);
+        }
+    }
     return false;
 }
 
@@ -1194,6 +1297,9 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
     }
     if (power_iterations_out) *power_iterations_out = S->power_iters;
     for (int t = 0; t < 3; ++t) g_restart_targets[t] = S->restarts_to[t];
+    g_controllers[0] = S->pulse_start;
+    g_controllers[1] = S->pulse_gate;
+    g_controllers[2] = S->trigger_iter;
     int polish_iters = 0, pst = -1, dst = -1;
     double polish_sec = 0.0;
     if (params->feasibility_polishing && S->reason != TERMINATION_REASON_PRIMAL_INFEASIBLE &&
@@ -1222,6 +1328,14 @@ void oracle_cpal_polish_status(int *primal, int *dual) {
  * Halpern iterate, the plain Halpern point */
 void oracle_cpal_restart_targets(int *counts) {
     for (int t = 0; t < 3; ++t) counts[t] = g_restart_targets[t];
+}
+
+/* benchmark controllers of the last solve: the iteration at which the alpha
+ * pulse's positive block started (-1: never), its gate (0 not evaluated, 1
+ * passed, 2 rejected), the iteration at which the sigma trigger fired (0:
+ * never) */
+void oracle_cpal_controllers(int *out) {
+    for (int t = 0; t < 3; ++t) out[t] = g_controllers[t];
 }
 
 /* Session form for timing: setup once, then blocks of iterations. */

@@ -111,6 +111,17 @@ def _restart_targets(L):
     return tuple(int(v) for v in counts)
 
 
+def _controllers(L):
+    """The benchmark controllers of the last oracle solve: the iteration at
+    which the alpha pulse's positive block started (-1: never), its gate (0
+    not evaluated, 1 passed, 2 rejected), the iteration at which the sigma
+    trigger fired (0: never)."""
+    out = (C.c_int * 3)()
+    L.oracle_cpal_controllers(out)
+    return {"pulse_start_iteration": int(out[0]), "pulse_gate": int(out[1]),
+            "sigma_trigger_iteration": int(out[2])}
+
+
 def solve_lp(data: LPData, params: dict | None = None, options: dict | None = None, threads: int = 1) -> LPResult:
     L = lib()
     p = apply_params(default_parameters(), params)
@@ -146,7 +157,7 @@ def solve_lp(data: LPData, params: dict | None = None, options: dict | None = No
                    "dual_ray_objective": r.dual_ray_objective,
                    "power_iterations": piters.value, "feasibility_iteration": r.feasibility_iteration,
                    "feasibility_polishing_time": r.feasibility_polishing_time, "polish_status": _polish_status(L),
-                   "restart_targets": _restart_targets(L)},
+                   "restart_targets": _restart_targets(L), **_controllers(L)},
         )
     finally:
         L.oracle_cpal_result_free(rp)

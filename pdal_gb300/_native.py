@@ -204,6 +204,15 @@ class CpalOptions(C.Structure):
         ("persistent_loop", C.c_int),
         ("dual_fused_finish", C.c_int),
         ("device_transpose", C.c_int),
+        ("alpha_direct_pulse", C.c_int),
+        ("pulse_force", C.c_int),
+        ("pulse_trace", C.c_int),
+        ("pulse_test_limit", C.c_int),
+        ("sigma_trigger", C.c_int),
+        ("sigma_trigger_min_iters", C.c_int),
+        ("sigma_trigger_primal", C.c_double),
+        ("sigma_trigger_dual", C.c_double),
+        ("sigma_trigger_ratio", C.c_double),
     ]
 
 
@@ -243,6 +252,9 @@ class CpalStats(C.Structure):
         ("avg_dual_panels_ms", C.c_double),
         ("avg_dual_rows32_ms", C.c_double),
         ("avg_dual_panels32_ms", C.c_double),
+        ("pulse_start_iteration", C.c_int),
+        ("pulse_gate", C.c_int),
+        ("sigma_trigger_iteration", C.c_int),
     ]
 
 

@@ -119,6 +119,10 @@ int run_batch(int count, lp_problem_t *const *problems, const cp_al_parameters_t
         p.pat = plan_rows(n, p.At.rp.data(), bs);
         p.cp = resolve_cpal_params(P, O, q);
         p.cp.infeas = 0; /* the batch controller evaluates no rays */
+        /* nor runs the alpha pulse or the sigma trigger (their step changes
+         * switch the iteration's kernel form, fixed per batch launch) */
+        p.cp.pulse = 0;
+        p.cp.trigger = 0;
     });
 
     /* image layout */

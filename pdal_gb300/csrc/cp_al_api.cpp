@@ -359,17 +359,25 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->persistent_loop = -1;
     o->dual_fused_finish = -1;
     o->device_transpose = -1;
+    o->alpha_direct_pulse = 0;
+    o->pulse_force = 0;
+    o->pulse_trace = 0;
+    o->pulse_test_limit = 0;
+    o->sigma_trigger = 0;
+    o->sigma_trigger_min_iters = 200;
+    o->sigma_trigger_primal = 1e-2;
+    o->sigma_trigger_dual = 1e-6;
+    o->sigma_trigger_ratio = 1e6;
 }
 
 /* Each variable is read the way the reference reads it
  * (LP/CP_AL/src/solver.cu:377-413: empty = unset, strtod/strtol, non-finite
  * ignored). */
-/* The enabling reads: LP/CP_AL/src/solver.cu:592 (rollback trial), 889
- * (pulse), 1235 (dynamic evaluation), 1497 (sigma trigger, outside sigma
- * mode), 3168-3180 (adaptive lambda and its profiles). */
+/* The enabling reads of the controllers not built: LP/CP_AL/src/solver.cu:592
+ * (rollback trial), 1235 (dynamic evaluation), 3168-3180 (adaptive lambda and
+ * its profiles). */
 const char *cp_al_gb300_unbuilt_switch(void) {
-    static const char *const kSwitches[] = {"CP_AL_ADAPTIVE_LAMBDA", "CP_AL_DYNAMIC_EVAL", "CP_AL_ALPHA_ROLLBACK_TRIAL",
-                                            "CP_AL_ALPHA_DIRECT_PULSE"};
+    static const char *const kSwitches[] = {"CP_AL_ADAPTIVE_LAMBDA", "CP_AL_DYNAMIC_EVAL", "CP_AL_ALPHA_ROLLBACK_TRIAL"};
     for (const char *name : kSwitches)
         if (env_int(name, 0) != 0) return name;
     if (const char *prof = getenv("CP_AL_LAMBDA_PROFILE")) {
@@ -377,8 +385,6 @@ const char *cp_al_gb300_unbuilt_switch(void) {
         for (const char *p : kProfiles)
             if (strcmp(prof, p) == 0) return "CP_AL_LAMBDA_PROFILE";
     }
-    if (env_int("CP_AL_SIGMA_TRIGGER", 0) != 0 && !(env_set("CP_AL_SIGMA") || env_int("CP_AL_SIGMA_MODE", 0) != 0))
-        return "CP_AL_SIGMA_TRIGGER";
     return nullptr;
 }
 
@@ -423,6 +429,16 @@ void cp_al_gb300_options_from_env(cp_al_gb300_options_t *o) {
     o->cr_early_stop = (cr_es && atoi(cr_es) != 0) ? 1 : 0;
     const char *cr_th = getenv("CP_AL_CR_EARLY_STOP_THRESHOLD");
     o->cr_early_stop_threshold = cr_th ? atof(cr_th) : 0.1;
+    /* LP/CP_AL/src/solver.cu:889-892, 1214-1216, 1497-1509 */
+    o->alpha_direct_pulse = env_int("CP_AL_ALPHA_DIRECT_PULSE", 0) != 0;
+    o->pulse_force = env_int("CP_AL_DETERMINISTIC_PULSE_FORCE", 0) != 0;
+    o->pulse_trace = env_int("CP_AL_ALPHA_DIRECT_PULSE_TRACE", 0) != 0;
+    o->pulse_test_limit = env_int("CP_AL_ALPHA_DIRECT_PULSE_TEST_TRAJECTORY_LIMIT", 0);
+    o->sigma_trigger = env_int("CP_AL_SIGMA_TRIGGER", 0) != 0;
+    o->sigma_trigger_min_iters = env_int("CP_AL_SIGMA_TRIGGER_MIN_ITERS", 200);
+    o->sigma_trigger_primal = env_double("CP_AL_SIGMA_TRIGGER_PRIMAL", 1e-2);
+    o->sigma_trigger_dual = env_double("CP_AL_SIGMA_TRIGGER_DUAL", 1e-6);
+    o->sigma_trigger_ratio = env_double("CP_AL_SIGMA_TRIGGER_RATIO", 1e6);
 }
 
 } // extern "C"

@@ -55,6 +55,20 @@ struct CpalParams {
      * evaluates them) */
     int infeas;
     double eps_infeas;
+    /* benchmark controllers of the reference, off by default there and here.
+     * Alpha pulse (LP/CP_AL/src/solver.cu:885-1032): once, at a restart after
+     * 10,000 iterations with two recorded zero-alpha epochs, run one
+     * evaluation block at alpha = 0.002 when the gate passes (pulse_force);
+     * pulse_test_limit ends the solve once the pulse is over and this many
+     * iterations are done. */
+    int pulse, pulse_force, pulse_test_limit;
+    /* sigma trigger (solver.cu:1496-1527): outside sigma mode, switch sigma
+     * mode on and restart when the primal residual lags the dual one */
+    int trigger, trigger_min_iters;
+    double trigger_p, trigger_d, trigger_ratio;
+    /* sigma initialisation the trigger repeats (solver.cu:3141-3164) */
+    int sigma_set;
+    double sigma_value, sigma_init_f, sigma_min_f, sigma_max_f;
 };
 
 /* Solver scalars, resident in device memory during the loop. */
@@ -93,6 +107,17 @@ struct CpalState {
     /* the last evaluation's ray quantities, normalised as the reference
      * reports them (infeasibility detection only) */
     double ray_pinf, ray_dinf, ray_pobj, ray_dobj;
+    /* alpha pulse: phase 0 idle, 1 running its positive block, 2 over; gate 0
+     * not evaluated, 1 passed, 2 rejected; the epoch being measured (valid
+     * after the first restart) and the last two zero-alpha epochs */
+    int pulse_phase, pulse_gate, pulse_start, pulse_status;
+    int epoch_valid, epoch_total, hist_count;
+    int hist_iters[2];
+    double hist_fp_rate[2];
+    double epoch_p, epoch_d, epoch_g;
+    double pulse_fp, pulse_p, pulse_d, pulse_g;
+    int trigger_iter; /* iteration at which the sigma trigger fired (0: never) */
+    int pad_ctl;
 };
 
 /* Reduction terms of one evaluation (finished sums / maxima). */
@@ -289,6 +314,144 @@ PDAL_HD void cpal_restart_scalars(CpalState &s, const CpalParams &p, double pd2,
     s.restarts++;
 }
 
+/* LP/CP_AL/src/solver.cu:415-428: the controllers' guarded magnitude and
+ * log-rate per iteration */
+PDAL_HD double ctl_metric(double v) { return fmax(fabs(v), 1e-300); }
+PDAL_HD double ctl_log_rate(double a, double b, int k) {
+    if (k <= 0 || !isfinite(a) || !isfinite(b)) return NAN;
+    const double r = log(ctl_metric(a) / ctl_metric(b)) / (double)k;
+    return isfinite(r) ? r : NAN;
+}
+
+/* LP/CP_AL/src/solver.cu:616-678: at a restart, an epoch run at alpha = 0 is
+ * kept (the last two) when all of its rates are finite */
+PDAL_HD void cpal_record_epoch(CpalState &s) {
+    if (!s.epoch_valid || s.al_lambda > 0.0) return;
+    const int k = s.total - s.epoch_total;
+    const double fr = ctl_log_rate(s.fp0, s.fp, k);
+    const double pr = ctl_log_rate(s.epoch_p, s.rel_p, k);
+    const double dr = ctl_log_rate(s.epoch_d, s.rel_d, k);
+    const double gr = ctl_log_rate(s.epoch_g, s.rel_gap, k);
+    const double k0 = fmax(s.epoch_p, fmax(s.epoch_d, s.epoch_g));
+    const double k1 = fmax(ctl_metric(s.rel_p), fmax(ctl_metric(s.rel_d), ctl_metric(s.rel_gap)));
+    const double kr = ctl_log_rate(k0, k1, k);
+    if (!(k > 0 && isfinite(fr) && isfinite(pr) && isfinite(dr) && isfinite(gr) && isfinite(kr))) return;
+    if (s.hist_count < 2) {
+        s.hist_iters[s.hist_count] = k;
+        s.hist_fp_rate[s.hist_count] = fr;
+        s.hist_count++;
+    } else {
+        s.hist_iters[0] = s.hist_iters[1];
+        s.hist_fp_rate[0] = s.hist_fp_rate[1];
+        s.hist_iters[1] = k;
+        s.hist_fp_rate[1] = fr;
+    }
+}
+
+/* solver.cu:605-614 */
+PDAL_HD void cpal_epoch_start(CpalState &s) {
+    s.epoch_valid = 1;
+    s.epoch_total = s.total;
+    s.epoch_p = ctl_metric(s.rel_p);
+    s.epoch_d = ctl_metric(s.rel_d);
+    s.epoch_g = ctl_metric(s.rel_gap);
+}
+
+/* solver.cu:899-966 (gate) and 968-988 (start), after a restart: the gate is
+ * evaluated once; with force it passes and the next block runs at alpha =
+ * 0.002 outside sigma mode */
+PDAL_HD void cpal_pulse_gate(CpalState &s, const CpalParams &p) {
+    if (!p.pulse || s.pulse_gate || s.pulse_phase != 0 || s.hist_count < 2 || s.total < 10000 || p.F != 200)
+        return;
+    if (s.iter_limit - s.total < 400) return;
+    for (int i = 0; i < 2; ++i)
+        if (s.hist_iters[i] <= 0 || !isfinite(s.hist_fp_rate[i])) return;
+    s.pulse_gate = p.pulse_force ? 1 : 2;
+    if (!p.pulse_force) return;
+    s.pulse_phase = 1;
+    s.pulse_start = s.total;
+    s.sigma_on = 0;
+    s.al_lambda = 0.002;
+    cpal_refresh_step_schedule(s, p);
+}
+
+/* solver.cu:3141-3164, as the sigma trigger runs it: the sigma parameters
+ * from the step's lambda estimate; the step sizes follow at the restart the
+ * trigger forces */
+PDAL_HD void cpal_init_sigma(CpalState &s, const CpalParams &p) {
+    const double le = fmax(s.lambda_est, 1e-12);
+    s.lambda_param = p.lambda_param_set ? p.lambda_param_opt : p.lambda_factor * le;
+    s.lambda_param = fmax(s.lambda_param, (2.0 + 1e-12) * le);
+    s.sigma_base = 1.0 / sqrt(fmax(s.lambda_param, 1e-16));
+    s.sigma_min = p.sigma_min_f * s.sigma_base;
+    s.sigma_max = p.sigma_max_f * s.sigma_base;
+    s.sigma = p.sigma_set ? p.sigma_value : p.sigma_init_f * s.sigma_base;
+    s.sigma = fmin(fmax(s.sigma, s.sigma_min), s.sigma_max);
+    s.sigma_best = s.sigma;
+    s.sigma_esum = 0.0;
+    s.sigma_last = 0.0;
+    s.sigma_adapt = p.sigma_adaptive;
+    s.sigma_on = 1;
+}
+
+/* Termination tests (LP/CP_AL/src/utils.cu:299-317, then the ray
+ * certificates, the iteration limit, the FP32 phase's switch and the time
+ * limit), then the end of an alpha pulse's positive block
+ * (LP/CP_AL/src/solver.cu:990-1032), which the reference runs whether or not
+ * that block ended the solve: alpha back to 0, the step schedule refreshed and
+ * the fixed-point error taken again with the new coefficients. */
+PDAL_HD bool cpal_terminated(CpalState &s, const CpalParams &p, const CpalEval &e) {
+    int st = 0;
+    if (s.rel_d < p.eps_feas && s.rel_p < p.eps_feas && s.rel_gap < p.eps_opt) st = 1; /* OPTIMAL */
+    if (!st && p.infeas) {
+        /* LP/CP_AL/src/utils.cu:919-1029 normalisation and 281-297 tests */
+        const double cs = s.cbr * s.ovr;
+        s.ray_pinf = e.ray_dxinf > 0.0 ? e.ray_pviol / e.ray_dxinf : e.ray_pviol;
+        s.ray_pobj = (e.ray_dxinf > 0.0 ? e.ray_cdx / e.ray_dxinf : e.ray_cdx) / cs;
+        const double sc = fmax(e.ray_dyinf, e.ray_dviol);
+        s.ray_dinf = sc > 0.0 ? e.ray_dviol / sc : 0.0;
+        s.ray_dobj = sc > 0.0 ? (e.ray_rowsum + e.ray_colsum) / cs / sc : 0.0;
+        if (s.ray_dobj > 0.0 && s.ray_dinf / s.ray_dobj <= p.eps_infeas)
+            st = 2; /* PRIMAL_INFEASIBLE */
+        else if (s.ray_pobj < 0.0 && s.ray_pinf / (-s.ray_pobj) <= p.eps_infeas)
+            st = 3; /* DUAL_INFEASIBLE */
+    }
+    if (!st && s.total >= s.iter_limit) st = 6; /* ITERATION_LIMIT */
+    if (!st) {
+        if (s.fp32_switch_tol > 0.0) {
+            /* the FP32 phase ends at its tolerance, or when the KKT error has
+             * not halved over fp32_stall_limit evaluations (FP32 rounding
+             * floor) */
+            const double kkt = fmax(s.rel_p, fmax(s.rel_d, s.rel_gap));
+            if (kkt < 0.5 * s.fp32_best_kkt) {
+                s.fp32_best_kkt = kkt;
+                s.fp32_stall = 0;
+            } else {
+                s.fp32_stall++;
+            }
+            if (kkt < s.fp32_switch_tol || (s.fp32_stall_limit > 0 && s.fp32_stall >= s.fp32_stall_limit))
+                s.phase_switch = 1;
+        }
+        if (s.elapsed >= p.time_limit) st = 5; /* TIME_LIMIT */
+    }
+    if (p.pulse && s.pulse_phase == 1) {
+        s.pulse_p = ctl_metric(s.rel_p);
+        s.pulse_d = ctl_metric(s.rel_d);
+        s.pulse_g = ctl_metric(s.rel_gap);
+        s.pulse_status = st;
+        s.sigma_on = 0;
+        s.al_lambda = 0.0;
+        cpal_refresh_step_schedule(s, p);
+        s.fp = cpal_fixed_point_error(s, e.dx2, e.dy2, e.adx2, e.cross);
+        s.pulse_fp = ctl_metric(s.fp);
+        s.pulse_phase = 2;
+    }
+    /* solver.cu:1386-1391, 1418-1424 */
+    if (!st && p.pulse && p.pulse_test_limit > 0 && s.pulse_phase == 2 && s.total >= p.pulse_test_limit) st = 6;
+    s.status = st;
+    return st != 0;
+}
+
 /*
  * Everything the reference does between two graph launches
  * (LP/CP_AL/src/solver.cu:1343-1697 with the default controllers off):
@@ -301,49 +464,7 @@ PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval
     s.inner += p.F;
     s.total += p.F;
     s.restart = 0;
-    /* LP/CP_AL/src/utils.cu:299-317 */
-    if (s.rel_d < p.eps_feas && s.rel_p < p.eps_feas && s.rel_gap < p.eps_opt) {
-        s.status = 1; /* TERMINATION_REASON_OPTIMAL */
-        return true;
-    }
-    if (p.infeas) {
-        /* LP/CP_AL/src/utils.cu:919-1029 normalisation and 281-297 tests */
-        const double cs = s.cbr * s.ovr;
-        s.ray_pinf = e.ray_dxinf > 0.0 ? e.ray_pviol / e.ray_dxinf : e.ray_pviol;
-        s.ray_pobj = (e.ray_dxinf > 0.0 ? e.ray_cdx / e.ray_dxinf : e.ray_cdx) / cs;
-        const double sc = fmax(e.ray_dyinf, e.ray_dviol);
-        s.ray_dinf = sc > 0.0 ? e.ray_dviol / sc : 0.0;
-        s.ray_dobj = sc > 0.0 ? (e.ray_rowsum + e.ray_colsum) / cs / sc : 0.0;
-        if (s.ray_dobj > 0.0 && s.ray_dinf / s.ray_dobj <= p.eps_infeas) {
-            s.status = 2; /* TERMINATION_REASON_PRIMAL_INFEASIBLE */
-            return true;
-        }
-        if (s.ray_pobj < 0.0 && s.ray_pinf / (-s.ray_pobj) <= p.eps_infeas) {
-            s.status = 3; /* TERMINATION_REASON_DUAL_INFEASIBLE */
-            return true;
-        }
-    }
-    if (s.total >= s.iter_limit) {
-        s.status = 6; /* TERMINATION_REASON_ITERATION_LIMIT */
-        return true;
-    }
-    if (s.fp32_switch_tol > 0.0) {
-        /* the FP32 phase ends at its tolerance, or when the KKT error has not
-         * halved over fp32_stall_limit evaluations (FP32 rounding floor) */
-        const double kkt = fmax(s.rel_p, fmax(s.rel_d, s.rel_gap));
-        if (kkt < 0.5 * s.fp32_best_kkt) {
-            s.fp32_best_kkt = kkt;
-            s.fp32_stall = 0;
-        } else {
-            s.fp32_stall++;
-        }
-        if (kkt < s.fp32_switch_tol || (s.fp32_stall_limit > 0 && s.fp32_stall >= s.fp32_stall_limit))
-            s.phase_switch = 1;
-    }
-    if (s.elapsed >= p.time_limit) {
-        s.status = 5; /* TERMINATION_REASON_TIME_LIMIT */
-        return true;
-    }
+    if (cpal_terminated(s, p, e)) return true;
     /* LP/CP_AL/src/solver.cu:2749-2819: the scores of the reflected Halpern
      * iterate (x, y) and, in the three-point mode, of the plain Halpern point
      * h = w x^ + (1 - w) x0 against (x^, y^), by the fixed-point error's
@@ -378,17 +499,33 @@ PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval
             }
         }
     }
-    if (cpal_should_restart(s, p)) {
+    /* LP/CP_AL/src/solver.cu:1496-1527: the sigma trigger forces a restart
+     * (the restart rule is then not evaluated) */
+    bool forced = false;
+    if (p.trigger && !s.sigma_on && s.total >= p.trigger_min_iters) {
+        const double rpr = fmax(s.rel_p, 1e-300), rdr = fmax(s.rel_d, 1e-300);
+        if (rpr >= p.trigger_p && rdr <= p.trigger_d && rpr / rdr >= p.trigger_ratio) {
+            cpal_init_sigma(s, p);
+            s.trigger_iter = s.total;
+            forced = true;
+        }
+    }
+    if (forced || cpal_should_restart(s, p)) {
         /* the PID distances run from the anchors to the restart point:
          * h - x0 = w (x^ - x0) for the plain Halpern point */
         const int tg = s.restart_target;
         const double w2 = w * w;
+        if (p.pulse) cpal_record_epoch(s);
         if (tg == 1)
             cpal_restart_scalars(s, p, e.cur_dx2, e.cur_dy2, e.cur_axd2);
         else if (tg == 2)
             cpal_restart_scalars(s, p, w2 * e.ddx2, w2 * e.ddy2, w2 * e.axd2);
         else
             cpal_restart_scalars(s, p, e.ddx2, e.ddy2, e.axd2);
+        if (p.pulse) {
+            cpal_epoch_start(s);
+            cpal_pulse_gate(s, p);
+        }
         s.restart = 1;
         /* the reference recomputes the fixed-point error of the unchanged
          * iterates with the new coefficients at the start of the next block

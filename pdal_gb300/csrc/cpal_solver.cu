@@ -323,7 +323,16 @@ class CpalSolver {
     int *lz_j_ = nullptr;
     CpalState *h_st_ = nullptr; /* pinned */
     PowerState *h_ps_ = nullptr;
-    cudaGraphExec_t exec64_ = nullptr, exec32_ = nullptr;
+    /* one graph per precision and predictor form (the alpha pulse and the
+     * sigma trigger switch the AL predictor on and off between blocks) */
+    cudaGraphExec_t exec64_[2] = {nullptr, nullptr}, exec32_[2] = {nullptr, nullptr};
+    /* the alpha pulse as the host last saw it, for its stderr lines */
+    int pulse_seen_gate_ = 0, pulse_seen_phase_ = 0, pulse_gate_iter_ = 0, pulse_gate_k_[2] = {0, 0};
+    double pulse_gate_rate_[2] = {0.0, 0.0};
+    void pulse_report();
+    /* evaluation blocks per graph launch: 1 while a controller may change the
+     * step form between blocks */
+    int graph_blocks() const { return (cp_.pulse || cp_.trigger) ? 1 : std::max(1, O_.graph_blocks); }
     int nmisc_ = 0;
     cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
@@ -375,9 +384,10 @@ PanelDev<float> CpalSolver::panel_dev<float>() const {
 void CpalSolver::release() {
     for (auto &e : ev_)
         if (e) cudaEventDestroy(e);
-    if (exec64_) cudaGraphExecDestroy(exec64_);
-    if (exec32_) cudaGraphExecDestroy(exec32_);
-    exec64_ = exec32_ = nullptr;
+    for (auto *e : {&exec64_[0], &exec64_[1], &exec32_[0], &exec32_[1]}) {
+        if (*e) cudaGraphExecDestroy(*e);
+        *e = nullptr;
+    }
     if (h_st_) cudaFreeHost(h_st_);
     if (h_ps_) cudaFreeHost(h_ps_);
     h_st_ = nullptr;
@@ -429,6 +439,19 @@ CpalParams resolve_cpal_params(const cp_al_parameters_t &P, const cp_al_gb300_op
     cp.restart_threepoint = O.restart_select != 0 && (O.restart_select == 3 || O.restart_select_threepoint != 0);
     cp.infeas = O.infeasibility_detection != 0;
     cp.eps_infeas = O.eps_infeasible;
+    cp.pulse = O.alpha_direct_pulse != 0;
+    cp.pulse_force = O.pulse_force != 0;
+    cp.pulse_test_limit = O.pulse_test_limit;
+    cp.trigger = O.sigma_trigger != 0;
+    cp.trigger_min_iters = O.sigma_trigger_min_iters;
+    cp.trigger_p = O.sigma_trigger_primal;
+    cp.trigger_d = O.sigma_trigger_dual;
+    cp.trigger_ratio = O.sigma_trigger_ratio;
+    cp.sigma_set = O.sigma_set;
+    cp.sigma_value = O.sigma;
+    cp.sigma_init_f = O.sigma_init_factor;
+    cp.sigma_min_f = O.sigma_min_factor;
+    cp.sigma_max_f = O.sigma_max_factor;
     cp.obj_const = prob->objective_constant;
     const int n = prob->num_variables, m = prob->num_constraints;
     const bool linf = cp.norm_linf;
@@ -711,7 +734,7 @@ void CpalSolver::setup_staged() {
 
 void CpalSolver::setup_loop() {
     const bool eligible = S_it_ <= 1024 && S_ev_ == S_it_ && !use_panels_ && !use_hot_ && !use_staged_ &&
-                          cp_.restart_select == 0 && !cp_.infeas && O_.timing == 0;
+                          cp_.restart_select == 0 && !cp_.infeas && O_.timing == 0 && !cp_.pulse && !cp_.trigger;
     const bool want = O_.persistent_loop == 1;
     use_loop_ = eligible && want;
     if (!use_loop_) return;
@@ -1342,6 +1365,15 @@ void CpalSolver::setup_device() {
     s.iter_limit = cp_.iteration_limit;
     cpal_set_coefficients(s);
     beta_on_ = s.beta > 0.0;
+    if (cp_.pulse) {
+        /* LP/CP_AL/src/solver.cu:893-900 */
+        fprintf(stderr,
+                "[alpha-direct-pulse-config] enabled=1 alpha=2.000000000000e-03 pulse_iterations=200 "
+                "history_epochs=2 deterministic_anchor_iter_ge=10000 wall_time_features=0 tail_only=1 "
+                "force_pulse=%d\n",
+                cp_.pulse_force);
+        fflush(stderr);
+    }
     host_state = s;
     *h_st_ = s;
     PDAL_CUDA(cudaMemcpyAsync(st_, h_st_, sizeof(CpalState), cudaMemcpyHostToDevice, stream_));
@@ -1718,7 +1750,7 @@ void CpalSolver::launch_eval() {
 template <typename T>
 void CpalSolver::capture_block(cudaGraphExec_t &exec) {
     const int F = cp_.F;
-    const int G = std::max(1, O_.graph_blocks);
+    const int G = graph_blocks();
     const bool timing = O_.timing != 0;
     if (timing && !ev_[0])
         for (auto &e : ev_) PDAL_CUDA(cudaEventCreate(&e));
@@ -2023,7 +2055,7 @@ void CpalSolver::run_loop() {
     const double t0 = now_sec();
     loop_t0_ = t0;
     const int F = cp_.F;
-    const int G = std::max(1, O_.graph_blocks);
+    const int G = graph_blocks();
     const int64_t per_block = (int64_t)iter_launches() * F + (m_ > 0 ? 4 : 3) + (cp_.infeas ? (m_ > 0 ? 2 : 1) : 0);
     k_start_clock<<<1, 1, 0, stream_>>>(st_);
     PDAL_LAUNCH_CHECK();
@@ -2046,11 +2078,11 @@ void CpalSolver::run_loop() {
         } else {
             cudaGraphExec_t *exec;
             if (fp32_phase_) {
-                if (!exec32_) capture_block<float>(exec32_);
-                exec = &exec32_;
+                exec = &exec32_[beta_on_ ? 1 : 0];
+                if (!*exec) capture_block<float>(*exec);
             } else {
-                if (!exec64_) capture_block<double>(exec64_);
-                exec = &exec64_;
+                exec = &exec64_[beta_on_ ? 1 : 0];
+                if (!*exec) capture_block<double>(*exec);
             }
             PDAL_CUDA(cudaGraphLaunch(*exec, stream_));
             launches += (per_block + ((fp32_phase_ ? hot_in<float>() : hot_in<double>()) ? 1 : 0)) * G;
@@ -2087,6 +2119,10 @@ void CpalSolver::run_loop() {
             fflush(stdout);
         }
         if (h_st_->status == kStatusDeviceError) check_device_error();
+        if (cp_.pulse) pulse_report();
+        if (cp_.trigger && h_st_->trigger_iter && P_.verbose && h_st_->restart && h_st_->trigger_iter == h_st_->total)
+            printf("sigma-trigger iter %d rpr %.12e rdr %.12e sigma %.12e base %.12e\n", h_st_->total, h_st_->rel_p,
+                   h_st_->rel_d, h_st_->sigma, h_st_->sigma_base);
         if (h_st_->status) break;
         /* the device enforces the time limit; this host guard only covers a
          * device clock that does not advance */
@@ -2094,7 +2130,20 @@ void CpalSolver::run_loop() {
             h_st_->status = TERMINATION_REASON_TIME_LIMIT;
             break;
         }
-        if (fp32_phase_ && (h_st_->phase_switch || (fp32_cap >= 0 && h_st_->total >= fp32_cap))) switch_to_fp64();
+        /* the alpha pulse and the sigma trigger change the AL penalty only at
+         * a restart (x = x0): the next block runs the iteration form of the
+         * new penalty, starting from A x0 and the predictor recomputed */
+        const bool beta_now = h_st_->beta > 0.0;
+        const bool beta_up = beta_now && !beta_on_;
+        beta_on_ = beta_now;
+        if (fp32_phase_ && (h_st_->phase_switch || (fp32_cap >= 0 && h_st_->total >= fp32_cap))) {
+            switch_to_fp64();
+        } else if (beta_up) {
+            if (fp32_phase_)
+                launch_init_ax<float>();
+            else
+                launch_init_ax<double>();
+        }
     }
     if (fp32_phase_) {
         /* finished inside the FP32 phase: promote the reported iterate */
@@ -2106,6 +2155,53 @@ void CpalSolver::run_loop() {
     }
     host_state = *h_st_;
     loop_sec = now_sec() - t0;
+    if (cp_.pulse) {
+        /* LP/CP_AL/src/solver.cu:1009-1032 */
+        const CpalState &q = host_state;
+        const int started = q.pulse_phase != 0, completed = q.pulse_phase == 2;
+        const int aborted = completed && q.pulse_status != 0 && q.pulse_status != TERMINATION_REASON_OPTIMAL;
+        fprintf(stderr,
+                "[alpha-direct-pulse-final] charged_iter=%d trajectory_iter=%d started=%d completed=%d aborted=%d "
+                "gate_evaluated=%d gate_passed=%d gate_rejected=%d gate_anchor_charged_iter=%d gate_previous_K=%d "
+                "gate_recent_K=%d gate_delta_fp_rate=%.12e positive_charged_iters=%d final_alpha=%.12e "
+                "final_penalty=%.12e\n",
+                q.total, q.total, started, completed, aborted, q.pulse_gate != 0, q.pulse_gate == 1, q.pulse_gate == 2,
+                pulse_gate_iter_, pulse_gate_k_[0], pulse_gate_k_[1], pulse_gate_rate_[1] - pulse_gate_rate_[0],
+                completed ? cp_.F : 0, q.al_lambda, q.beta);
+        fflush(stderr);
+    }
+}
+
+/* The alpha pulse's stderr lines (LP/CP_AL/src/solver.cu:893-988, 1017-1028),
+ * printed from the state after each evaluation block: the gate when it was
+ * evaluated, the start of the positive block and its end. */
+void CpalSolver::pulse_report() {
+    const CpalState &q = *h_st_;
+    if (q.pulse_gate && !pulse_seen_gate_) {
+        pulse_seen_gate_ = q.pulse_gate;
+        pulse_gate_iter_ = q.total;
+        for (int i = 0; i < 2; ++i) {
+            pulse_gate_k_[i] = q.hist_iters[i];
+            pulse_gate_rate_[i] = q.hist_fp_rate[i];
+        }
+        fprintf(stderr,
+                "[alpha-deterministic-tail-anchor] charged_iter=%d trajectory_iter=%d previous_K=%d recent_K=%d "
+                "previous_fp_rate=%.12e recent_fp_rate=%.12e delta_fp_rate=%.12e pass=%d force_pulse=%d\n",
+                q.total, q.total, q.hist_iters[0], q.hist_iters[1], q.hist_fp_rate[0], q.hist_fp_rate[1],
+                q.hist_fp_rate[1] - q.hist_fp_rate[0], q.pulse_gate == 1, cp_.pulse_force);
+    }
+    if (q.pulse_phase >= 1 && pulse_seen_phase_ < 1)
+        fprintf(stderr,
+                "[alpha-direct-pulse-start] charged_iter=%d trajectory_iter=%d alpha=2.000000000000e-03 "
+                "pulse_iterations=%d\n",
+                q.pulse_start, q.pulse_start, cp_.F);
+    if (q.pulse_phase == 2 && pulse_seen_phase_ < 2)
+        fprintf(stderr,
+                "[alpha-direct-pulse-complete] charged_iter=%d trajectory_iter=%d positive_iters=%d fp0map=%.12e "
+                "primal=%.12e dual=%.12e gap=%.12e term=%d\n",
+                q.total, q.total, cp_.F, q.pulse_fp, q.pulse_p, q.pulse_d, q.pulse_g, q.pulse_status);
+    pulse_seen_phase_ = q.pulse_phase;
+    fflush(stderr);
 }
 
 bool CpalSolver::extend(int n) {
@@ -2270,6 +2366,9 @@ static void fill_stats(const pdal::CpalSolver &s, double total) {
     }
     st.panel_rows = s.panel_rows();
     st.panels = s.panels();
+    st.pulse_start_iteration = s.host_state.pulse_phase ? s.host_state.pulse_start : -1;
+    st.pulse_gate = s.host_state.pulse_gate;
+    st.sigma_trigger_iteration = s.host_state.trigger_iter;
 }
 
 /* Options from the environment, unless a switch of a controller this library

@@ -58,6 +58,7 @@ def run_ref(bin_dir: Path, kind: str, data, env: dict, params: dict, vectors: bo
     line = [ln for ln in res.stdout.splitlines() if ln.startswith("{")][-1]
     out = json.loads(line)
     out["process_wall_sec"] = wall
+    out["controllers"] = RC.controller_events(res.stderr + "\n" + res.stdout)
     x = y = None
     if vectors:
         x = np.fromfile(tmp / "x.bin", dtype="<f8")

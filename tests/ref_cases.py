@@ -36,6 +36,13 @@ LAMBDA0_ENV = {"CP_AL_LAMBDA": "0"}
 C0 = ("random_lp", {"m": 2000, "n": 5000, "nnz_per_col": 8, "seed": 0})
 SMALL = ("random_lp", {"m": 300, "n": 800, "nnz_per_col": 6, "seed": 17})
 P8 = {"eps": 1e-8, "l_inf_ruiz_iterations": 4, "termination_evaluation_frequency": 200}
+NOSCALE = ("random_lp", {"m": 200, "n": 500, "nnz_per_col": 5, "seed": 5})
+NOSCALE_PARAMS = {"l_inf_ruiz_iterations": 0, "has_pock_chambolle_alpha": False, "bound_objective_rescaling": False}
+# the alpha pulse, its gate forced open as the structural tail's rescue solve sets it (LP/CP_AL/src/cli.c:760-763)
+PULSE_ENV = {"CP_AL_ALPHA_DIRECT_PULSE": "1", "CP_AL_DETERMINISTIC_PULSE_FORCE": "1"}
+# the sigma trigger with thresholds that always hold: it fires at the first evaluation after 2,000 iterations
+TRIGGER_ENV = {"CP_AL_SIGMA_TRIGGER": "1", "CP_AL_SIGMA_TRIGGER_MIN_ITERS": "2000", "CP_AL_SIGMA_TRIGGER_PRIMAL": "0",
+               "CP_AL_SIGMA_TRIGGER_DUAL": "1", "CP_AL_SIGMA_TRIGGER_RATIO": "0"}
 
 CASES = [
     # CP_AL, the plain FP64 form: status, objective and iteration parity at KKT 1e-8
@@ -68,6 +75,22 @@ CASES = [
     dict(name="lp_c4_transport_200x200", kind="lp",
          gen=("transport_lp", {"supplies": 200, "demands": 200, "seed": 4000}), env=SIGMA_PROTOCOL_ENV,
          params={"eps": 1e-6, "l_inf_ruiz_iterations": 4}, parity=True, timing="C4 cold start to 1e-6"),
+    # the benchmark controllers (LP/CP_AL/src/solver.cu:885-1032 alpha pulse, 1496-1527 sigma trigger): the
+    # iteration at which each acted is read from the reference's own log lines ("controllers" in the fixture)
+    dict(name="lp_noscale_pulse", kind="lp", gen=NOSCALE, env={**LAMBDA0_ENV, **PULSE_ENV},
+         params={**NOSCALE_PARAMS, "eps": 1e-14, "iteration_limit": 12000}, parity=True, vectors=True, oracle=True,
+         controllers=True),
+    dict(name="lp_noscale_pulse_gate", kind="lp", gen=NOSCALE,
+         env={**LAMBDA0_ENV, "CP_AL_ALPHA_DIRECT_PULSE": "1"},
+         params={**NOSCALE_PARAMS, "eps": 1e-14, "iteration_limit": 12000}, parity=True, vectors=True, oracle=True,
+         controllers=True),
+    dict(name="lp_c0_pulse", kind="lp", gen=C0, env={**LAMBDA0_ENV, **PULSE_ENV},
+         params={"eps": 1e-14, "iteration_limit": 13000, "l_inf_ruiz_iterations": 4}, parity=True, vectors=True,
+         controllers=True),
+    dict(name="lp_c0_pulse_1e-8", kind="lp", gen=C0, env={**LAMBDA0_ENV, **PULSE_ENV}, params=P8, parity=True,
+         vectors=True, controllers=True),
+    dict(name="lp_small_sigma_trigger", kind="lp", gen=SMALL, env={**LAMBDA0_ENV, **TRIGGER_ENV},
+         params={**P8, "verbose": True}, parity=True, vectors=True, oracle=True, controllers=True),
     # reference timing rows (time to relative KKT 1e-6, and per-iteration time on the large LP)
     dict(name="lp_c0_sigma_protocol_1e-6", kind="lp", gen=C0, env=SIGMA_PROTOCOL_ENV,
          params={"eps": 1e-6, "l_inf_ruiz_iterations": 4}, parity=True, timing="C0 to 1e-6"),
@@ -197,8 +220,32 @@ def driver_args(params: dict) -> list[str]:
             out.append(f"sigma_rule={SIGMA_RULES[v]}")
         elif k == "al_sigma":
             out.append(f"al_sigma={v!r}")
+        elif k == "verbose":
+            out.append(f"verbose={int(bool(v))}")
         else:
             raise KeyError(f"no driver key for {k!r}")
+    return out
+
+
+def controller_events(text: str) -> dict:
+    """The benchmark controllers' actions in a CP_AL log (the reference's
+    stderr and stdout, or this library's): the iteration at which the alpha
+    pulse started (-1: never), whether its gate was evaluated and passed
+    (None: not evaluated), and the iteration at which the sigma trigger fired
+    (0: never; printed with verbose output only)."""
+    import re
+
+    out = {"pulse_start": -1, "pulse_gate_pass": None, "pulse_gate_iteration": -1, "sigma_trigger": 0}
+    m = re.search(r"\[alpha-direct-pulse-start\] charged_iter=(\d+)", text)
+    if m:
+        out["pulse_start"] = int(m.group(1))
+    m = re.search(r"\[alpha-deterministic-tail-anchor\] charged_iter=(\d+).* pass=(\d)", text)
+    if m:
+        out["pulse_gate_iteration"] = int(m.group(1))
+        out["pulse_gate_pass"] = m.group(2) == "1"
+    m = re.search(r"sigma-trigger iter (\d+)", text)
+    if m:
+        out["sigma_trigger"] = int(m.group(1))
     return out
 
 

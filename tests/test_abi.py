@@ -220,17 +220,14 @@ def test_options_from_env_reads_reference_variables(lp_lib, monkeypatch):
     ("CP_AL_ADAPTIVE_LAMBDA", "1", {}),
     ("CP_AL_LAMBDA_PROFILE", "mp_race", {}),
     ("CP_AL_DYNAMIC_EVAL", "1", {}),
-    ("CP_AL_SIGMA_TRIGGER", "1", {}),
     ("CP_AL_ALPHA_ROLLBACK_TRIAL", "1", {}),
-    ("CP_AL_ALPHA_DIRECT_PULSE", "1", {}),
 ])
 def test_unbuilt_controller_switch_is_refused(lp_lib, monkeypatch, name, value, extra):
     """A CP_AL_* switch that turns on a controller this library does not
     implement makes solve_lp_problem (and cp_al_gb300_solve or
     cp_al_gb300_session_create without explicit options) return NULL with a
     message naming it (before any device work, so this runs without a GPU)
-    instead of solving without the controller; switched off, or the sigma
-    trigger inside sigma mode (where the reference ignores it), nothing is
+    instead of solving without the controller; switched off, nothing is
     refused."""
     for var in ("CP_AL_ADAPTIVE_LAMBDA", "CP_AL_LAMBDA_PROFILE", "CP_AL_DYNAMIC_EVAL", "CP_AL_SIGMA_TRIGGER",
                 "CP_AL_ALPHA_ROLLBACK_TRIAL", "CP_AL_ALPHA_DIRECT_PULSE", "CP_AL_SIGMA_MODE",
@@ -253,9 +250,30 @@ def test_unbuilt_controller_switch_is_refused(lp_lib, monkeypatch, name, value, 
         assert name in N.last_error(lp_lib)
     finally:
         prob.close()
-    if name == "CP_AL_SIGMA_TRIGGER":
-        monkeypatch.setenv("CP_AL_SIGMA_MODE", "1")
-        assert lp_lib.cp_al_gb300_unbuilt_switch() is None
+
+
+def test_pulse_and_trigger_options_from_env(lp_lib, monkeypatch):
+    """The alpha pulse and the sigma trigger are built: their switches are
+    read into the options (LP/CP_AL/src/solver.cu:889-892, 1214-1216,
+    1497-1509 defaults) and refuse nothing."""
+    names = ("CP_AL_ALPHA_DIRECT_PULSE", "CP_AL_DETERMINISTIC_PULSE_FORCE", "CP_AL_ALPHA_DIRECT_PULSE_TRACE",
+             "CP_AL_ALPHA_DIRECT_PULSE_TEST_TRAJECTORY_LIMIT", "CP_AL_SIGMA_TRIGGER", "CP_AL_SIGMA_TRIGGER_MIN_ITERS",
+             "CP_AL_SIGMA_TRIGGER_PRIMAL", "CP_AL_SIGMA_TRIGGER_DUAL", "CP_AL_SIGMA_TRIGGER_RATIO",
+             "CP_AL_ADAPTIVE_LAMBDA", "CP_AL_LAMBDA_PROFILE", "CP_AL_DYNAMIC_EVAL", "CP_AL_ALPHA_ROLLBACK_TRIAL")
+    for var in names:
+        monkeypatch.delenv(var, raising=False)
+    o = lp.default_options(lp_lib, from_env=True)
+    assert (o.alpha_direct_pulse, o.pulse_force, o.pulse_trace, o.pulse_test_limit, o.sigma_trigger) == (0,) * 5
+    assert (o.sigma_trigger_min_iters, o.sigma_trigger_primal, o.sigma_trigger_dual,
+            o.sigma_trigger_ratio) == (200, 1e-2, 1e-6, 1e6)
+    for var, val in zip(names[:9], ("1", "1", "1", "12000", "1", "400", "0.05", "1e-5", "1e3")):
+        monkeypatch.setenv(var, val)
+    o = lp.default_options(lp_lib, from_env=True)
+    assert (o.alpha_direct_pulse, o.pulse_force, o.pulse_trace, o.pulse_test_limit, o.sigma_trigger) == (
+        1, 1, 1, 12000, 1)
+    assert (o.sigma_trigger_min_iters, o.sigma_trigger_primal, o.sigma_trigger_dual,
+            o.sigma_trigger_ratio) == (400, 0.05, 1e-5, 1e3)
+    assert lp_lib.cp_al_gb300_unbuilt_switch() is None
 
 
 def test_curtis_reid_options_from_env(lp_lib, monkeypatch):

@@ -60,6 +60,30 @@ def test_fixture_instance_is_the_generated_one(name):
     assert RC.instance_sha256(RC.make_instance(case["gen"], case["kind"])) == fx["instance_sha256"]
 
 
+def _quiet(params: dict) -> dict:
+    return {k: v for k, v in params.items() if k != "verbose"}
+
+
+@pytest.mark.parametrize("name", [c["name"] for c in RC.CASES if c.get("oracle") and c.get("controllers")])
+def test_oracle_controllers_act_where_the_reference_does(lp_lib, name, monkeypatch):
+    """The oracle's alpha pulse and sigma trigger act at the iterations where
+    the reference's did (its log lines, recorded in the fixture), and its
+    solution vectors agree with the reference's to 1e-11 (1e-10 to 1e-6 apart
+    with the controllers off)."""
+    from oracle import oracle as O
+
+    fx, xr, yr = RC.load_fixture(name)
+    case = RC.BY_NAME[name]
+    data = RC.make_instance(case["gen"], case["kind"])
+    o = O.solve_lp(data, _quiet(case["params"]), _options_from_env(case["env"], monkeypatch))
+    ev = fx["ref"]["controllers"]
+    assert o.stats["pulse_start_iteration"] == ev["pulse_start"], (o.stats, ev)
+    assert o.stats["pulse_gate"] == {None: 0, True: 1, False: 2}[ev["pulse_gate_pass"]], (o.stats, ev)
+    assert o.stats["sigma_trigger_iteration"] == ev["sigma_trigger"], (o.stats, ev)
+    assert np.max(np.abs(o.x - xr)) / (1.0 + np.max(np.abs(xr))) <= 1e-11
+    assert np.max(np.abs(o.y - yr)) / (1.0 + np.max(np.abs(yr))) <= 1e-11
+
+
 @pytest.mark.parametrize("name", ORACLE_LP)
 def test_oracle_lp_matches_reference_solver(lp_lib, name, monkeypatch):
     from oracle import oracle as O
@@ -67,7 +91,7 @@ def test_oracle_lp_matches_reference_solver(lp_lib, name, monkeypatch):
     fx, xr, yr = RC.load_fixture(name)
     case = RC.BY_NAME[name]
     data = RC.make_instance(case["gen"], case["kind"])
-    o = O.solve_lp(data, case["params"], _options_from_env(case["env"], monkeypatch))
+    o = O.solve_lp(data, _quiet(case["params"]), _options_from_env(case["env"], monkeypatch))
     ref = fx["ref"]
     assert o.status_code == ref["termination_reason"], (o.status, ref["termination_reason"])
     assert _rel(o.primal_objective, ref["primal_objective"]) <= 1e-8, (o.primal_objective, ref["primal_objective"])

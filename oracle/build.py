@@ -50,8 +50,9 @@ def _cuda_include() -> str:
 
 def build_ref() -> list[Path]:
     """Compiles the reference's own MPS readers (LP/CP_AL/src/mps_parser.c and
-    QP/FA_CP/src/mps_parser.c) and its FA_CP equilibration
-    (QP/FA_CP/src/preconditioner.c), unmodified and read in place, into oracle/_ref/
+    QP/FA_CP/src/mps_parser.c), its FA_CP equilibration
+    (QP/FA_CP/src/preconditioner.c) and its CP_AL command's policy layer
+    (LP/CP_AL/src/cli.c, behind ref_shim/ref_cli_harness.c), unmodified and read in place, into oracle/_ref/
     with gcc, zlib and ref_shim/ (allocation helpers, the problem free
     functions and an empty PSLP_stats.h).  Their internal headers include the
     CUDA headers for declarations only; nothing of CUDA is linked.  Returns
@@ -87,6 +88,20 @@ def build_ref() -> list[Path]:
         if res.returncode != 0:
             raise RuntimeError("reference preconditioner build failed:\n" + " ".join(cmd) + "\n" + res.stderr)
     out.append(target)
+    # the CP_AL command's policy layer (LP/CP_AL/src/cli.c, host code) behind ref_cli_harness.c
+    proj = "LP/CP_AL"
+    src = REFERENCE / proj / "src" / "cli.c"
+    target = REF_OUT / "libref_cli_policy.so"
+    deps = [src, *SHIM.iterdir()]
+    if not (target.exists() and target.stat().st_mtime > max(p.stat().st_mtime for p in deps)):
+        cmd = ["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", "-w", "-DREF_LP", "-I", str(SHIM),
+               "-I", str(REFERENCE / proj / "src"), "-I", str(REFERENCE / proj / "include"),
+               "-I", str(REFERENCE / proj / "internal"), "-I", _cuda_include(), str(SHIM / "ref_cli_harness.c"),
+               str(SHIM / "ref_mps_shim.c"), "-lm", "-o", str(target)]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("reference policy layer build failed:\n" + " ".join(cmd) + "\n" + res.stderr)
+    out.append(target)
     return out
 
 
@@ -96,6 +111,9 @@ REF_SOLVERS = {
     "ref_fa_cp": ("QP/FA_CP", ["fa_cp.c", "preconditioner.c"],
                   ["solver.cu", "utils.cu", "solver_state.cu", "fa_cp_core_op.cu"], "REF_QP"),
 }
+# the reference's own CP_AL command (LP/CP_AL/src/cli.c with its MPS reader and
+# zlib): ref_cp_al's library objects (without the driver) plus these sources
+REF_CLI = ("ref_cp_al_cli", "ref_cp_al", ["cli.c", "mps_parser.c"])
 DRIVER = HERE / "ref_driver" / "ref_solve.c"
 
 
@@ -103,10 +121,11 @@ def build_ref_solvers(reference: Path | None = None, jobs: int | None = None) ->
     """Compiles the reference's own CP_AL and FA_CP solvers (their src/*.c and
     src/*.cu, unmodified, read where they lie) for sm_103a as the reference's
     CMake does (-O3, separable device compilation, cuSPARSE and cuBLAS), and
-    links each with the driver ref_driver/ref_solve.c into oracle/_ref/.
+    links each with the driver ref_driver/ref_solve.c into oracle/_ref/; and
+    the reference's CP_AL command itself (cli.c and its MPS reader with zlib
+    over the same CP_AL objects) as oracle/_ref/ref_cp_al_cli.
     CP_AL's presolve library (PSLP) is absent: ref_shim/ gives its header and
-    entry points, never reached with presolve off.  The MPS readers and the
-    command-line programs are not part of these builds.  `reference` (default:
+    entry points, never reached with presolve off.  `reference` (default:
     PDAL_REFERENCE_DIR, else the reference's usual location) must hold
     LP/CP_AL and QP/FA_CP.  Returns the executables, or [] where the sources
     are absent.  Test infrastructure: only the fixture script
@@ -142,6 +161,14 @@ def build_ref_solvers(reference: Path | None = None, jobs: int | None = None) ->
         if res.returncode != 0:
             raise RuntimeError("reference solver build failed:\n" + " ".join(cmd) + "\n" + res.stderr[-4000:])
 
+    cli, base, cli_srcs = REF_CLI
+    proj = REF_SOLVERS[base][0]
+    inc = ["-I", str(SHIM), "-I", str(ref / proj / "include"), "-I", str(ref / proj / "internal")]
+    for s in cli_srcs:
+        jobs_list.append((cli, objdir / f"{cli}_{Path(s).stem}.o",
+                          ["gcc", "-O3", "-std=gnu99", "-w", *inc, "-I", cuda_inc, "-c", str(ref / proj / "src" / s),
+                           "-o", str(objdir / f"{cli}_{Path(s).stem}.o")]))
+
     with cf.ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 2)) as ex:
         list(ex.map(run, [j[2] for j in jobs_list]))
     out = []
@@ -151,6 +178,11 @@ def build_ref_solvers(reference: Path | None = None, jobs: int | None = None) ->
         run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-rdc=true", *objs, "-lcusparse", "-lcublas",
              "-lm", "-o", str(target)])
         out.append(target)
+    objs = [str(o) for e, o, _ in jobs_list if e == cli or (e == base and DRIVER.stem not in o.name)]
+    target = REF_OUT / cli
+    run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-rdc=true", *objs, "-lcusparse", "-lcublas", "-lz",
+         "-lm", "-o", str(target)])
+    out.append(target)
     return out
 
 

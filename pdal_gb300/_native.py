@@ -293,8 +293,18 @@ class InstanceInfo(C.Structure):
     ]
 
 
-# name -> (restype, argtypes); every symbol include/cp_al.h and
-# include/cp_al_gb300.h declare
+class FeatureStats(C.Structure):
+    """cp_al_feature_stats_t (include/cp_al_policy.h)."""
+    _fields_ = [(f, C.c_double) for f in (
+        "coeff_log_range", "row_logmax_std", "col_logmax_std", "row_logspan_mean", "col_logspan_mean",
+        "row_span2_fraction", "col_span2_fraction", "row_nnz_cv", "col_nnz_cv", "equality_fraction",
+        "two_sided_variable_fraction", "objective_density")]
+
+
+SOLVE_FN = C.CFUNCTYPE(C.c_void_p, C.POINTER(LpProblem), C.POINTER(CpalParameters))
+
+# name -> (restype, argtypes); every symbol include/cp_al.h,
+# include/cp_al_gb300.h and include/cp_al_policy.h declare
 LP_SYMBOLS = {
     "create_lp_problem": (C.POINTER(LpProblem), [_dp, C.POINTER(MatrixDesc), _dp, _dp, _dp, _dp, _dp]),
     "set_start_values": (None, [C.POINTER(LpProblem), _dp, _dp]),
@@ -332,6 +342,12 @@ LP_SYMBOLS = {
         [C.c_int, C.POINTER(C.POINTER(LpProblem)), C.POINTER(CpalParameters), C.POINTER(CpalOptions),
          C.POINTER(BatchStats)],
     ),
+    "cp_al_feature_stats": (C.c_int, [C.POINTER(LpProblem), C.POINTER(FeatureStats)]),
+    "cp_al_unified_policy": (C.c_char_p, [C.POINTER(FeatureStats)]),
+    "cp_al_feature_policy": (C.c_int, [C.POINTER(LpProblem), C.POINTER(CpalParameters), C.POINTER(FeatureStats)]),
+    "cp_al_structural_tail": (
+        C.POINTER(CpalResult), [C.POINTER(LpProblem), C.POINTER(CpalParameters), C.POINTER(FeatureStats), C.c_int]),
+    "cp_al_policy_set_solver": (None, [SOLVE_FN]),
     "cp_al_gb300_primal_kkt_noalloc": (
         C.c_int,
         [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -27,7 +27,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 # library name -> sources
 LIBRARIES = {
     "libcp_al_gb300.so": ["cpal_solver.cu", "common.cpp", "cp_al_api.cpp", "noalloc.cu", "batch_solver.cu",
-                          "mps_reader.cpp"],
+                          "mps_reader.cpp", "cp_al_policy.cpp"],
     "libfa_cp_gb300.so": ["facp_solver.cu", "common.cpp", "fa_cp_api.cpp", "mps_reader.cpp"],
     "libpdal_learn_gb300.so": ["mlp.cu", "common.cpp"],
 }

@@ -8,14 +8,17 @@
  * <name>_primal_solution.txt and <name>_dual_solution.txt into output_dir in
  * the reference's formats (cli.c:472-586), <name> being the file name up to
  * its first dot.  The solver reads the CP_AL_* environment variables the way
- * solve_lp_problem does.  Not built: the feature / unified / structural-tail
- * policies the reference runs when CP_AL_UNIFIED_POLICY,
- * CP_AL_FEATURE_AUTO_POLICY, CP_AL_STRUCTURAL_TAIL_CUT or
- * CP_AL_FEATURE_AUDIT_ONLY is set (the command refuses to run with exit
- * code 2) and presolve (PSLP is not part of this build).
+ * solve_lp_problem does.  The benchmark policy layer runs as in the reference
+ * (cli.c:1031-1071, functions of include/cp_al_policy.h): with
+ * CP_AL_UNIFIED_POLICY, CP_AL_FEATURE_AUTO_POLICY or
+ * CP_AL_STRUCTURAL_TAIL_CUT set, the LP's features are computed, the
+ * unified decision list and then the feature policy set their variables,
+ * CP_AL_FEATURE_AUDIT_ONLY stops there, and the structural tail (when set)
+ * runs the solve.  Not built: presolve (PSLP is not part of this build).
  */
 #include "../../include/cp_al.h"
 #include "../../include/cp_al_mps_parser.h"
+#include "../../include/cp_al_policy.h"
 
 #include <getopt.h>
 
@@ -23,6 +26,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <ctime>
 #include <string>
 
 namespace {
@@ -227,20 +231,36 @@ int main(int argc, char *argv[]) {
     const char *filename = argv[optind];
     const char *output_dir = argv[optind + 1];
 
-    for (const char *flag : {"CP_AL_UNIFIED_POLICY", "CP_AL_FEATURE_AUTO_POLICY", "CP_AL_STRUCTURAL_TAIL_CUT",
-                             "CP_AL_FEATURE_AUDIT_ONLY"}) {
-        if (env_flag(flag)) {
-            fprintf(stderr, "Error: %s is set, but the benchmark policy layer is not part of this build.\n", flag);
-            return 2;
-        }
-    }
     const std::string name = instance_name(filename);
     lp_problem_t *problem = read_mps_file(filename);
     if (!problem) {
         fprintf(stderr, "Failed to read or parse the file.\n");
         return 1;
     }
-    cp_al_result_t *result = solve_lp_problem(problem, &params);
+    /* the policy layer, in the reference's order (cli.c:1031-1071) */
+    const bool need_stats = env_flag("CP_AL_UNIFIED_POLICY") || env_flag("CP_AL_FEATURE_AUTO_POLICY") ||
+                            env_flag("CP_AL_STRUCTURAL_TAIL_CUT");
+    cp_al_feature_stats_t stats;
+    memset(&stats, 0, sizeof(stats));
+    const clock_t policy_start = clock();
+    if (need_stats) cp_al_feature_stats(problem, &stats);
+    cp_al_unified_policy(need_stats ? &stats : nullptr);
+    const bool feature_policy = env_flag("CP_AL_FEATURE_AUTO_POLICY");
+    const bool tail = env_flag("CP_AL_STRUCTURAL_TAIL_CUT");
+    const bool tail_pulse = env_flag("CP_AL_TAIL_ONLY_PULSE");
+    if (need_stats)
+        fprintf(stderr, "[feature-matrix-stats] computed=1 feature_policy=%d structural_tail=%d\n",
+                feature_policy ? 1 : 0, tail ? 1 : 0);
+    cp_al_feature_policy(problem, &params, need_stats ? &stats : nullptr);
+    if (feature_policy)
+        fprintf(stderr, "[feature-auto-policy-time] seconds=%.12g\n",
+                (double)(clock() - policy_start) / CLOCKS_PER_SEC);
+    if (env_flag("CP_AL_FEATURE_AUDIT_ONLY")) {
+        lp_problem_free(problem);
+        return 0;
+    }
+    cp_al_result_t *result =
+        tail ? cp_al_structural_tail(problem, &params, &stats, tail_pulse ? 1 : 0) : solve_lp_problem(problem, &params);
     if (!result) {
         fprintf(stderr, "Solver failed.\n");
     } else {

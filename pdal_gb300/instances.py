@@ -11,6 +11,8 @@ the benchmark workloads (numpy default_rng; same seed -> same arrays).
   batch_lps(count)               uneven batch, m log-uniform in [50, 5000]
   transport_lp(S, D)             min-cost transportation LP on a complete
                                  bipartite graph with arc capacities
+  sparse_objective_lp(m, n)      feasibility-type LP: Zipf column lengths,
+                                 0.5% of the costs nonzero
 """
 from __future__ import annotations
 
@@ -158,6 +160,31 @@ def zipf_lp(m: int = 1_000_000, n: int = 2_000_000, nnz: int = 20_000_000, seed:
     lb[free] = -np.inf
     ubv[free] = np.inf
     c, cl, cu = _plant(rng, A, m, n, np.arange(m // 2), lb, ubv, free_mask=free)
+    return LPData(c, (A[0], A[1], A[2], (m, n)), cl, cu, lb, ubv)
+
+
+def sparse_objective_lp(m: int = 3000, n: int = 6000, nnz: int = 40_000, seed: int = 5000, priced: float = 0.005,
+                        max_col: int = 600) -> LPData:
+    """Feasibility-type LP: column lengths Zipf(1.5) capped at max_col and
+    rescaled to about nnz in total (a few dense columns, most with one or two
+    entries), values N(0,1), 0 <= x <= 10, half the rows equalities, b
+    planted, and only a `priced` fraction of the costs nonzero."""
+    rng = np.random.default_rng(seed)
+    z = rng.zipf(1.5, size=n).astype(np.float64)
+    cap = min(max_col, m)
+    lo, hi = 1e-9, 1.0
+    for _ in range(60):
+        f = np.sqrt(lo * hi)
+        tot = np.minimum(np.maximum(1.0, np.round(z * f)), cap).sum()
+        lo, hi = (f, hi) if tot < nnz else (lo, f)
+    k = np.minimum(np.maximum(1.0, np.round(z * np.sqrt(lo * hi))), cap).astype(np.int64)
+    rows, cols = _distinct_rows_per_col(rng, m, n, k)
+    vals = rng.standard_normal(rows.shape[0])
+    A = _csr_from_coo(rows, cols, vals, m, n)
+    lb = np.zeros(n)
+    ubv = np.full(n, 10.0)
+    c, cl, cu = _plant(rng, A, m, n, np.arange(m // 2), lb, ubv)
+    c = np.where(rng.random(n) < priced, c, 0.0)
     return LPData(c, (A[0], A[1], A[2], (m, n)), cl, cu, lb, ubv)
 
 

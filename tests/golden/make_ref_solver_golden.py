@@ -66,6 +66,38 @@ def run_ref(bin_dir: Path, kind: str, data, env: dict, params: dict, vectors: bo
     return out, x, y
 
 
+def run_cli_cases(bin_dir: Path, out_dir: Path, only: set, tmp: Path, meta: dict) -> None:
+    """The reference's own CP_AL command on each CLI case's MPS file: its
+    summary file and what its policy layer did (RC.cli_events of its
+    stderr)."""
+    import hashlib
+
+    from pdal_gb300 import mps
+
+    exe = bin_dir / "ref_cp_al_cli"
+    for case in RC.CLI_CASES:
+        if only and case["name"] not in only:
+            continue
+        data = RC.make_instance(case["gen"])
+        src = mps.write_lp(data, tmp / f"{case['name']}.mps")
+        outd = tmp / f"{case['name']}_out"
+        outd.mkdir(exist_ok=True)
+        t0 = time.perf_counter()
+        res = subprocess.run([str(exe), *case["args"], str(src), str(outd)], capture_output=True, text=True,
+                             env=_env(case["env"]), timeout=3600)
+        wall = time.perf_counter() - t0
+        if res.returncode != 0:
+            raise RuntimeError(f"{exe.name} failed ({res.returncode}):\n{res.stderr[-3000:]}")
+        rec = {"name": case["name"], "mps_sha256": hashlib.sha256(src.read_bytes()).hexdigest(), "gen": case["gen"],
+               "env": case["env"], "args": case["args"],
+               "summary": RC.read_summary(outd / f"{case['name']}_summary.txt"),
+               "events": RC.cli_events(res.stderr + "\n" + res.stdout), "process_wall_sec": wall,
+               "driver": "oracle/_ref/ref_cp_al_cli (LP/CP_AL/src/cli.c)", "gpu": meta["gpu"]}
+        (out_dir / f"{case['name']}.json").write_text(json.dumps(rec, indent=1) + "\n")
+        print(f"{case['name']}: {rec['summary']['Termination Reason']} iters={rec['summary']['Iterations Count']} "
+              f"events={rec['events']} wall={wall:.2f}s", flush=True)
+
+
 def gpu_name() -> str:
     try:
         return subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader"], capture_output=True,
@@ -80,6 +112,7 @@ def main() -> None:
     ap.add_argument("--out", type=Path, default=ROOT / "tests" / "golden" / "ref_solver")
     ap.add_argument("--only", default="")
     ap.add_argument("--timing", action="store_true")
+    ap.add_argument("--cli", action="store_true", help="only the reference command's cases (CLI_CASES)")
     a = ap.parse_args()
     a.out.mkdir(parents=True, exist_ok=True)
     only = set(filter(None, a.only.split(",")))
@@ -87,6 +120,9 @@ def main() -> None:
             "driver": "oracle/ref_driver/ref_solve.c"}
     with tempfile.TemporaryDirectory() as td:
         tmp = Path(td)
+        if a.cli:
+            run_cli_cases(a.bin, a.out, only, tmp, meta)
+            return
         for case in RC.CASES:
             if only and case["name"] not in only:
                 continue

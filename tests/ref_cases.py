@@ -125,6 +125,63 @@ CASES = [
          timing="C2 to 1e-8"),
 ]
 
+# The reference's own CP_AL command (oracle/_ref/ref_cp_al_cli) under the paper protocol's one switch
+# (LP/CP_AL/run_unified_full856.sbatch:87-89 environment, 110-113 arguments), on MPS files written by
+# pdal_gb300.mps.write_lp: one case per route of the unified decision list.  The tail case's iteration limit
+# ends the base solve long before its time share, so both phases are deterministic, and its rescue runs
+# the forced alpha pulse.
+UNIFIED_ENV = {"CP_AL_UNIFIED_POLICY": "1", "CP_AL_ALPHA_DIRECT_PULSE_TRACE": "1", "CP_AL_PROGRESS_LOG_FREQ": "0"}
+
+
+def _cli_args(eps: float, iters: int) -> list[str]:
+    return ["--time_limit", "3600", "--iter_limit", str(iters), "--eps_opt", repr(eps), "--eps_feas", repr(eps),
+            "--eval_freq", "200", "--no_presolve"]
+
+
+CLI_CASES = [
+    dict(name="cli_unified_tail_pulse", gen=("transport_lp", {"supplies": 200, "demands": 200, "seed": 4000}),
+         env=UNIFIED_ENV, args=_cli_args(1e-10, 12000)),
+    dict(name="cli_unified_base_c0", gen=C0, env=UNIFIED_ENV, args=_cli_args(1e-6, 100000)),
+    dict(name="cli_unified_zero_equality",
+         gen=("random_lp", {"m": 2000, "n": 5000, "nnz_per_col": 8, "seed": 7, "eq_fraction": 0.0}), env=UNIFIED_ENV,
+         args=_cli_args(1e-6, 100000)),
+    dict(name="cli_unified_lowobj", gen=("sparse_objective_lp", {}), env=UNIFIED_ENV, args=_cli_args(1e-6, 100000)),
+]
+CLI_BY_NAME = {c["name"]: c for c in CLI_CASES}
+
+
+def cli_events(text: str) -> dict:
+    """What the policy layer did, from a CP_AL command's stderr: the unified
+    route, the Curtis-Reid effort of each feature-policy application, the
+    structural tail's phases (status and iterations of each) and the alpha
+    pulse's events."""
+    import re
+
+    out = {"route": None, "cr_selected": [int(v) for v in re.findall(r"\[feature-auto-policy\] .*? cr_selected=(\d+)", text)]}
+    m = re.search(r"\[unified-policy\] version=2 route=(\S+)", text)
+    if m:
+        out["route"] = m.group(1)
+    for tag in ("base", "rescue"):
+        m = re.search(r"\[structural-tail-%s\] status=(\S+) .*? iterations=(\d+)" % tag, text)
+        out[tag] = [m.group(1), int(m.group(2))] if m else None
+    m = re.search(r"\[structural-tail-final\] phases=(\d) tail_started=(\d) status=(\S+) .*? total_iterations=(\d+)",
+                  text)
+    out["final"] = [int(m.group(1)), int(m.group(2)), m.group(3), int(m.group(4))] if m else None
+    out.update(controller_events(text))
+    return out
+
+
+def read_summary(path) -> dict:
+    """A CP_AL command's <name>_summary.txt (LP/CP_AL/src/cli.c:526-586)."""
+    from pathlib import Path
+
+    out = {}
+    for line in Path(path).read_text().splitlines():
+        k, v = line.split(": ", 1)
+        out[k] = v
+    return out
+
+
 # the large LP, reference time per iteration: two runs that differ only in the
 # iteration limit; (t[hi] - t[lo]) / (hi - lo) removes the setup
 C1_TIMING = dict(name="lp_c1_iteration_time", gen=("zipf_lp", {}), env=SIGMA_PROTOCOL_ENV,

@@ -13,7 +13,7 @@ from pdal_gb300 import _native as N
 from pdal_gb300 import lp
 
 ROOT = Path(__file__).resolve().parent.parent
-HEADERS = {"libcp_al_gb300.so": ["cp_al.h", "cp_al_gb300.h", "cp_al_mps_parser.h"],
+HEADERS = {"libcp_al_gb300.so": ["cp_al.h", "cp_al_gb300.h", "cp_al_mps_parser.h", "cp_al_policy.h"],
            "libfa_cp_gb300.so": ["fa_cp.h", "fa_cp_gb300.h", "fa_cp_mps_parser.h"],
            "libpdal_learn_gb300.so": ["pdal_learn.h"]}
 
@@ -37,11 +37,12 @@ PROBE = r"""
 #include <stddef.h>
 #include "cp_al_types.h"
 #include "cp_al_gb300.h"
+#include "cp_al_policy.h"
 #define S(T) printf(#T " %zu\n", sizeof(T));
 #define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
 int main(void) {
   S(lp_problem_t) S(cp_al_parameters_t) S(cp_al_result_t) S(matrix_desc_t) S(cp_al_gb300_options_t)
-  S(cp_al_gb300_stats_t) S(termination_criteria_t) S(restart_parameters_t)
+  S(cp_al_gb300_stats_t) S(termination_criteria_t) S(restart_parameters_t) S(cp_al_feature_stats_t)
   O(cp_al_parameters_t, termination_criteria) O(cp_al_parameters_t, restart_params)
   O(cp_al_parameters_t, optimality_norm) O(cp_al_parameters_t, matrix_zero_tol)
   O(cp_al_result_t, termination_reason) O(cp_al_result_t, feasibility_iteration)
@@ -62,6 +63,7 @@ def test_struct_layouts_match_c(tmp_path):
         "lp_problem_t": N.LpProblem, "cp_al_parameters_t": N.CpalParameters, "cp_al_result_t": N.CpalResult,
         "matrix_desc_t": N.MatrixDesc, "cp_al_gb300_options_t": N.CpalOptions, "cp_al_gb300_stats_t": N.CpalStats,
         "termination_criteria_t": N.TerminationCriteria, "restart_parameters_t": N.RestartParams,
+        "cp_al_feature_stats_t": N.FeatureStats,
     }
     for cname, ct in sizes.items():
         assert int(out[cname]) == C.sizeof(ct), cname

@@ -235,12 +235,29 @@ def test_cli_usage_and_argument_errors(name, tmp_path):
     assert r.returncode == 1 and "Failed to read or parse the file." in r.stderr
 
 
-def test_cli_sigma_rule_names_and_policy_refusal(tmp_path):
+def test_cli_sigma_rule_names(tmp_path):
     r = subprocess.run([str(_exe("fa_cp")), "--sigma_update", "bogus", "a", "b"], capture_output=True, text=True)
     assert r.returncode == 1 and "sigma_update must be" in r.stderr
-    env = {"PATH": "/usr/bin:/bin", "CP_AL_UNIFIED_POLICY": "1"}
-    r = subprocess.run([str(_exe("cp_al")), "a.mps", str(tmp_path)], capture_output=True, text=True, env=env)
-    assert r.returncode == 2 and "CP_AL_UNIFIED_POLICY" in r.stderr
+
+
+def test_cli_policy_audit_without_a_solve(tmp_path):
+    """The `cp_al` command's policy layer in the reference's order
+    (LP/CP_AL/src/cli.c:1031-1064): with CP_AL_UNIFIED_POLICY the features
+    are computed, the decision list picks the structural-tail route of a
+    transportation LP (all rows equalities, dense costs, unit coefficients),
+    the feature policy picks its Curtis-Reid effort, and
+    CP_AL_FEATURE_AUDIT_ONLY stops before any solve (so no GPU is needed)."""
+    from pdal_gb300 import instances, mps
+
+    src = mps.write_lp(instances.transport_lp(5, 6, seed=4001), tmp_path / "t.mps")
+    env = {"PATH": "/usr/bin:/bin", "CP_AL_UNIFIED_POLICY": "1", "CP_AL_FEATURE_AUDIT_ONLY": "1"}
+    r = subprocess.run([str(_exe("cp_al")), str(src), str(tmp_path)], capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stderr
+    assert "[unified-policy] version=2 route=high_equality_tail_or_base" in r.stderr
+    assert "[feature-matrix-stats] computed=1 feature_policy=1 structural_tail=1" in r.stderr
+    assert "variant=safe0" in r.stderr and "cr_selected=5" in r.stderr
+    assert "[feature-auto-policy-time] seconds=" in r.stderr
+    assert not (tmp_path / "t_summary.txt").exists()
 
 
 @pytest.mark.parametrize("quad", [False, True])

@@ -149,3 +149,63 @@ def test_qp_matches_reference_solver(qp_lib, name, monkeypatch):
     assert _rel(g.primal_objective, ref["primal_objective"]) <= OBJ_TOL, (g.primal_objective, ref["primal_objective"])
     assert abs(g.iterations - ref["iterations"]) <= ITER_TOL * ref["iterations"], (g.iterations, ref["iterations"])
     _check_vectors(g.x, g.y, xr, yr)
+
+
+def _cli_fixture(name):
+    import json
+    from pathlib import Path
+
+    f = Path(__file__).resolve().parent / "golden" / "ref_solver" / f"{name}.json"
+    if not f.exists():
+        pytest.fail(f"fixture {name} missing: run tests/golden/make_ref_solver_golden.py --cli")
+    return json.loads(f.read_text())
+
+
+@pytest.mark.parametrize("name", [c["name"] for c in RC.CLI_CASES])
+def test_cp_al_command_policy_matches_reference_command(tmp_path, lp_lib, name):
+    """The paper protocol end to end: this library's `cp_al` command and the
+    reference's own command (LP/CP_AL/src/cli.c, built from its sources, run
+    on a GB300; fixture) on the same MPS file with CP_AL_UNIFIED_POLICY=1 and
+    the runner's arguments take the same route of the unified decision list,
+    the same Curtis-Reid effort, the same structural-tail phases (status of
+    each, iterations within 2%) and alpha pulse (start iteration), and write
+    the same summary (status, iterations within 2%, objective to the printed
+    six digits, sizes)."""
+    import os
+    import subprocess
+
+    from pdal_gb300 import _native as N
+    from pdal_gb300 import mps
+
+    fx = _cli_fixture(name)
+    case = RC.CLI_BY_NAME[name]
+    src = mps.write_lp(RC.make_instance(case["gen"]), tmp_path / f"{name}.mps")
+    import hashlib
+
+    assert hashlib.sha256(src.read_bytes()).hexdigest() == fx["mps_sha256"], "MPS text differs from the fixture's"
+    out = tmp_path / "out"
+    out.mkdir()
+    env = {k: v for k, v in os.environ.items() if not k.startswith(("CP_AL_", "FA_CP_"))}
+    env.update(case["env"])
+    r = subprocess.run([str(N.LIBDIR / "cp_al"), *case["args"], str(src), str(out)], capture_output=True, text=True,
+                       env=env, timeout=1800)
+    assert r.returncode == 0, r.stderr[-3000:]
+    ev, ref = RC.cli_events(r.stderr + "\n" + r.stdout), fx["events"]
+    assert ev["route"] == ref["route"] and ev["cr_selected"] == ref["cr_selected"], (ev, ref)
+    for tag in ("base", "rescue"):
+        assert (ev[tag] is None) == (ref[tag] is None), (tag, ev, ref)
+        if ref[tag]:
+            assert ev[tag][0] == ref[tag][0], (tag, ev, ref)
+            assert abs(ev[tag][1] - ref[tag][1]) <= ITER_TOL * ref[tag][1], (tag, ev, ref)
+    assert (ev["final"] is None) == (ref["final"] is None)
+    if ref["final"]:
+        assert ev["final"][:3] == ref["final"][:3], (ev, ref)
+    for k in ("pulse_start", "pulse_gate_pass", "pulse_gate_iteration"):
+        assert ev[k] == ref[k], (k, ev, ref)
+    s, sr = RC.read_summary(out / f"{name}_summary.txt"), fx["summary"]
+    assert s["Termination Reason"] == sr["Termination Reason"]
+    it, itr = int(s["Iterations Count"]), int(sr["Iterations Count"])
+    assert abs(it - itr) <= ITER_TOL * itr, (it, itr)
+    assert _rel(float(s["Primal Objective Value"]), float(sr["Primal Objective Value"])) <= 1e-5
+    for k in ("Rows", "Columns", "Nonzeros"):
+        assert s[k] == sr[k]

@@ -158,6 +158,31 @@ typedef struct {
     double sigma_trigger_primal;  /* CP_AL_SIGMA_TRIGGER_PRIMAL, 1e-2 */
     double sigma_trigger_dual;    /* CP_AL_SIGMA_TRIGGER_DUAL, 1e-6 */
     double sigma_trigger_ratio;   /* CP_AL_SIGMA_TRIGGER_RATIO, 1e6 */
+    int dynamic_eval;             /* CP_AL_DYNAMIC_EVAL (solver.cu:1229-1255, 1529-1583): outside sigma mode,
+                                     once the iterations reach dynamic_eval_min_iters, evaluation blocks
+                                     of dynamic_eval_fast iterations instead of the evaluation frequency
+                                     from the first evaluation whose residuals are one-sided (the smaller
+                                     <= small_res, the larger >= large_res) or lopsided (ratio >= ratio,
+                                     the larger >= large_res); the switch is kept */
+    int dynamic_eval_fast;        /* CP_AL_DYNAMIC_EVAL_FAST, 50 (clamped to [3, evaluation frequency]) */
+    double dynamic_eval_after_sec;/* CP_AL_DYNAMIC_EVAL_AFTER_SEC, -1: > 0 switches after this many seconds
+                                     (unless Curtis-Reid stopped early) */
+    int dynamic_eval_after_iters; /* CP_AL_DYNAMIC_EVAL_AFTER_ITERS, -1: > 0 switches after this many
+                                     iterations (unless Curtis-Reid stopped early) */
+    int dynamic_eval_min_iters;   /* CP_AL_DYNAMIC_EVAL_MIN_ITERS, 0 = the evaluation frequency (at least
+                                     that) */
+    double dynamic_eval_small_res;/* CP_AL_DYNAMIC_EVAL_SMALL_RES, 1e-6 */
+    double dynamic_eval_large_res;/* CP_AL_DYNAMIC_EVAL_LARGE_RES, 1e-4 */
+    double dynamic_eval_ratio;    /* CP_AL_DYNAMIC_EVAL_RATIO, 1e4 */
+    int dynamic_eval_bootstrap_iters; /* CP_AL_DYNAMIC_EVAL_BOOTSTRAP_ITERS, 0: > 0 starts with short blocks
+                                     and returns to the evaluation frequency at this many iterations unless
+                                     the switch was taken */
+
+    /* --- options of this implementation (continued) --- */
+    int dual_concurrent;          /* with the panel path: the dual step's short-row launch and its
+                                     long rows' panel launch run concurrently on two streams (also in
+                                     the captured graphs).  1 = so, 0 or -1 (default) = one after
+                                     the other.  Results are bit-identical either way */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */
@@ -208,10 +233,12 @@ typedef struct {
     double avg_dual_panels32_ms;
     /* benchmark controllers: iteration at which the alpha pulse's positive
      * block started (-1: never), its gate (0 not evaluated, 1 passed, 2
-     * rejected), iteration at which the sigma trigger fired (0: never) */
+     * rejected), iteration at which the sigma trigger fired (0: never) and
+     * the dynamic evaluation frequency switched */
     int pulse_start_iteration;
     int pulse_gate;
     int sigma_trigger_iteration;
+    int dynamic_eval_iteration;   /* iteration at which the blocks became dynamic_eval_fast long (0: never) */
 } cp_al_gb300_stats_t;
 
 /* The reference defaults of every field, ignoring the environment. */
@@ -223,9 +250,9 @@ void cp_al_gb300_options_from_env(cp_al_gb300_options_t *opts);
 
 /* Name of the first CP_AL_* environment switch that turns on a controller of
  * the reference this library does not implement -- adaptive lambda
- * (CP_AL_ADAPTIVE_LAMBDA, the race / auto CP_AL_LAMBDA_PROFILE values),
- * dynamic evaluation frequency (CP_AL_DYNAMIC_EVAL) or the alpha rollback
- * trial (CP_AL_ALPHA_ROLLBACK_TRIAL) -- or NULL.  solve_lp_problem
+ * (CP_AL_ADAPTIVE_LAMBDA, the race / auto CP_AL_LAMBDA_PROFILE values) or
+ * the alpha rollback trial (CP_AL_ALPHA_ROLLBACK_TRIAL) -- or NULL.
+ * solve_lp_problem
  * returns NULL with a message while one is set, instead of solving without
  * it.  Diagnostic and trace switches are ignored. */
 const char *cp_al_gb300_unbuilt_switch(void);

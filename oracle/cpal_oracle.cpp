@@ -45,7 +45,7 @@ namespace {
 int g_threads = 1;
 int g_polish_status[2] = {-1, -1};
 int g_restart_targets[3] = {0, 0, 0};
-int g_controllers[3] = {-1, 0, 0}; /* pulse start iteration, pulse gate, sigma trigger iteration */
+int g_controllers[4] = {-1, 0, 0, 0}; /* pulse start iteration, pulse gate, sigma trigger and dynamic evaluation iterations */
 
 struct Csr {
     int nr = 0, nc = 0;
@@ -135,6 +135,48 @@ struct Solver {
     double hist_rate[2] = {0.0, 0.0};
     double epoch_p = 0, epoch_d = 0, epoch_g = 0;
     int trigger_iter = 0;
+    /* the dynamic evaluation frequency (solver.cu:1229-1255): the next
+     * block's length, whether the switch to short blocks was taken and at
+     * which iteration */
+    int F_cur = 0, dyn_iter = 0;
+    bool dyn_latched = false, cr_early_stopped = false;
+    struct Dyn {
+        bool on = false, resid = false;
+        int fast = 0, min_iters = 0, boot = 0, after_iters = -1;
+        double after_sec = -1.0, small = 0, large = 0, ratio = 0;
+    } dyn;
+    void dyn_setup() {
+        const int F = P->termination_evaluation_frequency;
+        dyn.fast = std::min(std::max(O.dynamic_eval_fast, 3), F);
+        dyn.resid = O.dynamic_eval != 0;
+        dyn.after_sec = O.dynamic_eval_after_sec;
+        dyn.after_iters = O.dynamic_eval_after_iters;
+        dyn.on = (dyn.resid || dyn.after_sec > 0.0 || dyn.after_iters > 0) && dyn.fast < F;
+        dyn.min_iters = std::max(O.dynamic_eval_min_iters > 0 ? O.dynamic_eval_min_iters : F, F);
+        dyn.small = O.dynamic_eval_small_res;
+        dyn.large = O.dynamic_eval_large_res;
+        dyn.ratio = O.dynamic_eval_ratio;
+        dyn.boot = std::max(O.dynamic_eval_bootstrap_iters, 0);
+        F_cur = (dyn.on && dyn.boot > 0) ? dyn.fast : F;
+    }
+    /* solver.cu:1529-1583, after an evaluation */
+    void dyn_update(double elapsed) {
+        if (!dyn.on || sigma_mode) return;
+        if (!(total >= dyn.min_iters || (dyn.boot > 0 && total >= dyn.boot))) return;
+        const double rpr = std::fmax(rel_p, 1e-300), rdr = std::fmax(rel_d, 1e-300);
+        const double lo = std::fmin(rpr, rdr), hi = std::fmax(rpr, rdr);
+        const bool one_sided = lo <= dyn.small && hi >= dyn.large;
+        const bool lag = hi / lo >= dyn.ratio && hi >= dyn.large;
+        const bool tgate = dyn.after_sec > 0.0 && !cr_early_stopped && elapsed >= dyn.after_sec;
+        const bool igate = dyn.after_iters > 0 && !cr_early_stopped && total >= dyn.after_iters;
+        if (tgate || igate || (dyn.resid && (one_sided || lag))) {
+            if (!dyn_latched) dyn_iter = total;
+            dyn_latched = true;
+            F_cur = dyn.fast;
+        } else if (!dyn_latched && dyn.boot > 0 && F_cur == dyn.fast && total >= dyn.boot) {
+            F_cur = P->termination_evaluation_frequency;
+        }
+    }
 
     static double metric(double v) { return std::fmax(std::fabs(v), 1e-300); } /* solver.cu:415-418 */
     static double log_rate(double a, double b, int k) {                        /* solver.cu:420-428 */
@@ -272,6 +314,7 @@ struct Solver {
                 if (mx <= O.cr_early_stop_threshold) break;
             }
         }
+        cr_early_stopped = early && cr_passes < iters; /* preconditioner.cu:246 */
         std::vector<double> rinv(m), dinv(n);
         for (int i = 0; i < m; ++i) {
             const double f = std::fmin(std::fmax(std::exp(lr[i]), 1e-30), 1e30);
@@ -893,6 +936,16 @@ void oracle_cpal_default_options(cp_al_gb300_options_t *o) {
     o->sigma_trigger_primal = 1e-2;
     o->sigma_trigger_dual = 1e-6;
     o->sigma_trigger_ratio = 1e6;
+    o->dynamic_eval = 0;
+    o->dynamic_eval_fast = 50;
+    o->dynamic_eval_after_sec = -1.0;
+    o->dynamic_eval_after_iters = -1;
+    o->dynamic_eval_min_iters = 0;
+    o->dynamic_eval_small_res = 1e-6;
+    o->dynamic_eval_large_res = 1e-4;
+    o->dynamic_eval_ratio = 1e4;
+    o->dynamic_eval_bootstrap_iters = 0;
+    o->dual_concurrent = -1;
 }
 
 /* LP/CP_AL/src/utils.cu:361-394 (reflection coefficient without the
@@ -995,13 +1048,14 @@ Solver *oracle_setup(const lp_problem_t *prob, const cp_al_parameters_t *params,
         S.bnd_norm = params->optimality_norm == NORM_TYPE_L_INF ? mx : std::sqrt(s);
     }
     S.initialize_step_size_and_primal_weight();
+    S.dyn_setup();
     return SP;
 }
 
 /* one evaluation block of the loop, solver.cu:1270-1697; returns true when
  * the solve has terminated */
 bool oracle_block(Solver &S, bool &do_restart, int &charged, double elapsed, int limit) {
-    const int F = S.P->termination_evaluation_frequency;
+    const int F = S.F_cur; /* this block's length */
     if (do_restart) {
         S.fixed_point_error();
         S.fp0 = S.fp;
@@ -1053,6 +1107,7 @@ bool oracle_block(Solver &S, bool &do_restart, int &charged, double elapsed, int
             forced = true;
         }
     }
+    S.dyn_update(elapsed);
     do_restart = forced || S.should_restart(F);
     if (do_restart) {
         if (O.alpha_direct_pulse) S.record_epoch();
@@ -1300,6 +1355,7 @@ cp_al_result_t *oracle_cpal_solve(const lp_problem_t *prob, const cp_al_paramete
     g_controllers[0] = S->pulse_start;
     g_controllers[1] = S->pulse_gate;
     g_controllers[2] = S->trigger_iter;
+    g_controllers[3] = S->dyn_iter;
     int polish_iters = 0, pst = -1, dst = -1;
     double polish_sec = 0.0;
     if (params->feasibility_polishing && S->reason != TERMINATION_REASON_PRIMAL_INFEASIBLE &&
@@ -1333,9 +1389,10 @@ void oracle_cpal_restart_targets(int *counts) {
 /* benchmark controllers of the last solve: the iteration at which the alpha
  * pulse's positive block started (-1: never), its gate (0 not evaluated, 1
  * passed, 2 rejected), the iteration at which the sigma trigger fired (0:
- * never) */
+ * never), the iteration at which the dynamic evaluation frequency switched to
+ * short blocks (0: never) */
 void oracle_cpal_controllers(int *out) {
-    for (int t = 0; t < 3; ++t) out[t] = g_controllers[t];
+    for (int t = 0; t < 4; ++t) out[t] = g_controllers[t];
 }
 
 /* Session form for timing: setup once, then blocks of iterations. */

@@ -115,11 +115,12 @@ def _controllers(L):
     """The benchmark controllers of the last oracle solve: the iteration at
     which the alpha pulse's positive block started (-1: never), its gate (0
     not evaluated, 1 passed, 2 rejected), the iteration at which the sigma
-    trigger fired (0: never)."""
-    out = (C.c_int * 3)()
+    trigger fired (0: never), the iteration at which the dynamic evaluation
+    frequency switched to short blocks (0: never)."""
+    out = (C.c_int * 4)()
     L.oracle_cpal_controllers(out)
     return {"pulse_start_iteration": int(out[0]), "pulse_gate": int(out[1]),
-            "sigma_trigger_iteration": int(out[2])}
+            "sigma_trigger_iteration": int(out[2]), "dynamic_eval_iteration": int(out[3])}
 
 
 def solve_lp(data: LPData, params: dict | None = None, options: dict | None = None, threads: int = 1) -> LPResult:

@@ -213,6 +213,16 @@ class CpalOptions(C.Structure):
         ("sigma_trigger_primal", C.c_double),
         ("sigma_trigger_dual", C.c_double),
         ("sigma_trigger_ratio", C.c_double),
+        ("dynamic_eval", C.c_int),
+        ("dynamic_eval_fast", C.c_int),
+        ("dynamic_eval_after_sec", C.c_double),
+        ("dynamic_eval_after_iters", C.c_int),
+        ("dynamic_eval_min_iters", C.c_int),
+        ("dynamic_eval_small_res", C.c_double),
+        ("dynamic_eval_large_res", C.c_double),
+        ("dynamic_eval_ratio", C.c_double),
+        ("dynamic_eval_bootstrap_iters", C.c_int),
+        ("dual_concurrent", C.c_int),
     ]
 
 
@@ -255,6 +265,7 @@ class CpalStats(C.Structure):
         ("pulse_start_iteration", C.c_int),
         ("pulse_gate", C.c_int),
         ("sigma_trigger_iteration", C.c_int),
+        ("dynamic_eval_iteration", C.c_int),
     ]
 
 

@@ -641,6 +641,7 @@ __device__ void blk_solve(const BInst &I, CpalParams p, const BOpts &o, BOut *ou
         s.fp32_stall_limit = o.fp32_stall_evals;
         s.fp32_best_kkt = INFINITY;
         s.iter_limit = p.iteration_limit;
+        s.F = p.F;
         cpal_set_coefficients(s);
         s.t_start_ns = globaltimer_ns();
         sh[3] = (double)(s.t_start_ns - t0) * 1e-9;

@@ -123,6 +123,7 @@ int run_batch(int count, lp_problem_t *const *problems, const cp_al_parameters_t
          * switch the iteration's kernel form, fixed per batch launch) */
         p.cp.pulse = 0;
         p.cp.trigger = 0;
+        p.cp.dyn = 0; /* nor a changing block length */
     });
 
     /* image layout */

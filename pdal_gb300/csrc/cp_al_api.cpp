@@ -368,16 +368,25 @@ void cp_al_gb300_default_options(cp_al_gb300_options_t *o) {
     o->sigma_trigger_primal = 1e-2;
     o->sigma_trigger_dual = 1e-6;
     o->sigma_trigger_ratio = 1e6;
+    o->dynamic_eval = 0;
+    o->dynamic_eval_fast = 50;
+    o->dynamic_eval_after_sec = -1.0;
+    o->dynamic_eval_after_iters = -1;
+    o->dynamic_eval_min_iters = 0;
+    o->dynamic_eval_small_res = 1e-6;
+    o->dynamic_eval_large_res = 1e-4;
+    o->dynamic_eval_ratio = 1e4;
+    o->dynamic_eval_bootstrap_iters = 0;
+    o->dual_concurrent = -1;
 }
 
 /* Each variable is read the way the reference reads it
  * (LP/CP_AL/src/solver.cu:377-413: empty = unset, strtod/strtol, non-finite
  * ignored). */
 /* The enabling reads of the controllers not built: LP/CP_AL/src/solver.cu:592
- * (rollback trial), 1235 (dynamic evaluation), 3168-3180 (adaptive lambda and
- * its profiles). */
+ * (rollback trial), 3168-3180 (adaptive lambda and its profiles). */
 const char *cp_al_gb300_unbuilt_switch(void) {
-    static const char *const kSwitches[] = {"CP_AL_ADAPTIVE_LAMBDA", "CP_AL_DYNAMIC_EVAL", "CP_AL_ALPHA_ROLLBACK_TRIAL"};
+    static const char *const kSwitches[] = {"CP_AL_ADAPTIVE_LAMBDA", "CP_AL_ALPHA_ROLLBACK_TRIAL"};
     for (const char *name : kSwitches)
         if (env_int(name, 0) != 0) return name;
     if (const char *prof = getenv("CP_AL_LAMBDA_PROFILE")) {
@@ -439,6 +448,16 @@ void cp_al_gb300_options_from_env(cp_al_gb300_options_t *o) {
     o->sigma_trigger_primal = env_double("CP_AL_SIGMA_TRIGGER_PRIMAL", 1e-2);
     o->sigma_trigger_dual = env_double("CP_AL_SIGMA_TRIGGER_DUAL", 1e-6);
     o->sigma_trigger_ratio = env_double("CP_AL_SIGMA_TRIGGER_RATIO", 1e6);
+    /* LP/CP_AL/src/solver.cu:1231-1255 */
+    o->dynamic_eval = env_int("CP_AL_DYNAMIC_EVAL", 0) != 0;
+    o->dynamic_eval_fast = env_int("CP_AL_DYNAMIC_EVAL_FAST", 50);
+    o->dynamic_eval_after_sec = env_double("CP_AL_DYNAMIC_EVAL_AFTER_SEC", -1.0);
+    o->dynamic_eval_after_iters = env_int("CP_AL_DYNAMIC_EVAL_AFTER_ITERS", -1);
+    o->dynamic_eval_min_iters = env_int("CP_AL_DYNAMIC_EVAL_MIN_ITERS", 0);
+    o->dynamic_eval_small_res = env_double("CP_AL_DYNAMIC_EVAL_SMALL_RES", 1e-6);
+    o->dynamic_eval_large_res = env_double("CP_AL_DYNAMIC_EVAL_LARGE_RES", 1e-4);
+    o->dynamic_eval_ratio = env_double("CP_AL_DYNAMIC_EVAL_RATIO", 1e4);
+    o->dynamic_eval_bootstrap_iters = env_int("CP_AL_DYNAMIC_EVAL_BOOTSTRAP_ITERS", 0);
 }
 
 } // extern "C"

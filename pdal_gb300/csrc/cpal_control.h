@@ -69,6 +69,13 @@ struct CpalParams {
     /* sigma initialisation the trigger repeats (solver.cu:3141-3164) */
     int sigma_set;
     double sigma_value, sigma_init_f, sigma_min_f, sigma_max_f;
+    /* dynamic evaluation frequency (solver.cu:1229-1255, 1529-1583): blocks
+     * of dyn_fast iterations instead of F once the residuals are lopsided
+     * (dyn_resid), after dyn_sec seconds or dyn_iters iterations (unless
+     * Curtis-Reid stopped early), or from the start until dyn_boot
+     * iterations */
+    int dyn, dyn_resid, dyn_fast, dyn_min_iters, dyn_boot, dyn_iters, cr_early_stopped;
+    double dyn_sec, dyn_small, dyn_large, dyn_ratio;
 };
 
 /* Solver scalars, resident in device memory during the loop. */
@@ -117,7 +124,9 @@ struct CpalState {
     double epoch_p, epoch_d, epoch_g;
     double pulse_fp, pulse_p, pulse_d, pulse_g;
     int trigger_iter; /* iteration at which the sigma trigger fired (0: never) */
-    int pad_ctl;
+    int F;            /* iterations of the next evaluation block */
+    int dyn_latched;  /* the dynamic evaluation frequency switched to its fast value */
+    int dyn_iter;     /* at this iteration (0: never) */
 };
 
 /* Reduction terms of one evaluation (finished sums / maxima). */
@@ -234,12 +243,12 @@ PDAL_HD void cpal_residual_scalars(CpalState &s, const CpalParams &p, const Cpal
     s.rel_gap = s.gap / (1.0 + fabs(s.pobj) + fabs(s.dobj));
 }
 
-/* LP/CP_AL/src/utils.cu:319-359 */
-PDAL_HD bool cpal_should_restart(CpalState &s, const CpalParams &p) {
+/* LP/CP_AL/src/utils.cu:319-359, F the iterations of the block just run */
+PDAL_HD bool cpal_should_restart(CpalState &s, const CpalParams &p, int F) {
     bool rs = false;
-    if (s.total == p.F) {
+    if (s.total == F) {
         rs = true;
-    } else if (s.total > p.F) {
+    } else if (s.total > F) {
         if (s.fp <= p.suff * s.fp0) rs = true;
         if (s.fp <= p.nec * s.fp0 && s.fp > s.fp_last) rs = true;
         if (s.inner >= p.art * s.total) rs = true;
@@ -360,9 +369,8 @@ PDAL_HD void cpal_epoch_start(CpalState &s) {
 /* solver.cu:899-966 (gate) and 968-988 (start), after a restart: the gate is
  * evaluated once; with force it passes and the next block runs at alpha =
  * 0.002 outside sigma mode */
-PDAL_HD void cpal_pulse_gate(CpalState &s, const CpalParams &p) {
-    if (!p.pulse || s.pulse_gate || s.pulse_phase != 0 || s.hist_count < 2 || s.total < 10000 || p.F != 200)
-        return;
+PDAL_HD void cpal_pulse_gate(CpalState &s, const CpalParams &p, int F) {
+    if (!p.pulse || s.pulse_gate || s.pulse_phase != 0 || s.hist_count < 2 || s.total < 10000 || F != 200) return;
     if (s.iter_limit - s.total < 400) return;
     for (int i = 0; i < 2; ++i)
         if (s.hist_iters[i] <= 0 || !isfinite(s.hist_fp_rate[i])) return;
@@ -459,10 +467,11 @@ PDAL_HD bool cpal_terminated(CpalState &s, const CpalParams &p, const CpalEval &
  * Returns true when the solve has terminated (s.status set).
  */
 PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval &e) {
+    const int F = s.F; /* this block's iterations */
     s.fp = cpal_fixed_point_error(s, e.dx2, e.dy2, e.adx2, e.cross);
     cpal_residual_scalars(s, p, e);
-    s.inner += p.F;
-    s.total += p.F;
+    s.inner += F;
+    s.total += F;
     s.restart = 0;
     if (cpal_terminated(s, p, e)) return true;
     /* LP/CP_AL/src/solver.cu:2749-2819: the scores of the reflected Halpern
@@ -510,7 +519,23 @@ PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval
             forced = true;
         }
     }
-    if (forced || cpal_should_restart(s, p)) {
+    /* LP/CP_AL/src/solver.cu:1529-1583: the next blocks' length */
+    if (p.dyn && !s.sigma_on && (s.total >= p.dyn_min_iters || (p.dyn_boot > 0 && s.total >= p.dyn_boot))) {
+        const double rpr = fmax(s.rel_p, 1e-300), rdr = fmax(s.rel_d, 1e-300);
+        const double lo = fmin(rpr, rdr), hi = fmax(rpr, rdr);
+        const bool one_sided = lo <= p.dyn_small && hi >= p.dyn_large;
+        const bool lag = hi / lo >= p.dyn_ratio && hi >= p.dyn_large;
+        const bool tgate = p.dyn_sec > 0.0 && !p.cr_early_stopped && s.elapsed >= p.dyn_sec;
+        const bool igate = p.dyn_iters > 0 && !p.cr_early_stopped && s.total >= p.dyn_iters;
+        if (tgate || igate || (p.dyn_resid && (one_sided || lag))) {
+            if (!s.dyn_latched) s.dyn_iter = s.total;
+            s.dyn_latched = 1;
+            s.F = p.dyn_fast;
+        } else if (!s.dyn_latched && p.dyn_boot > 0 && s.F == p.dyn_fast && s.total >= p.dyn_boot) {
+            s.F = p.F;
+        }
+    }
+    if (forced || cpal_should_restart(s, p, F)) {
         /* the PID distances run from the anchors to the restart point:
          * h - x0 = w (x^ - x0) for the plain Halpern point */
         const int tg = s.restart_target;
@@ -524,7 +549,7 @@ PDAL_HD bool cpal_end_of_block(CpalState &s, const CpalParams &p, const CpalEval
             cpal_restart_scalars(s, p, e.ddx2, e.ddy2, e.axd2);
         if (p.pulse) {
             cpal_epoch_start(s);
-            cpal_pulse_gate(s, p);
+            cpal_pulse_gate(s, p, F);
         }
         s.restart = 1;
         /* the reference recomputes the fixed-point error of the unchanged

@@ -190,7 +190,7 @@ class CpalSolver {
   private:
     void release();
     template <typename T>
-    void capture_block(cudaGraphExec_t &exec);
+    void capture_block(cudaGraphExec_t &exec, int F);
     template <typename T>
     void launch_iteration(int koff, bool major);
     template <typename T>
@@ -259,6 +259,11 @@ class CpalSolver {
     double *pan_v64_ = nullptr, *pan_part64_ = nullptr;
     /* the fused finish of the long rows: arrivals and segments per long row */
     bool fuse_finish_ = false;
+    /* the dual step's short-row and panel launches on two streams (forked and
+     * joined with events, also inside the captured graphs) */
+    bool dual_fork_ = false;
+    cudaStream_t side_ = nullptr;
+    cudaEvent_t fork_ev_ = nullptr, join_ev_ = nullptr;
     unsigned *pan_cnt_ = nullptr;
     int *pan_nseg_ = nullptr;
     float *pan_v32_ = nullptr, *pan_part32_ = nullptr;
@@ -323,16 +328,19 @@ class CpalSolver {
     int *lz_j_ = nullptr;
     CpalState *h_st_ = nullptr; /* pinned */
     PowerState *h_ps_ = nullptr;
-    /* one graph per precision and predictor form (the alpha pulse and the
-     * sigma trigger switch the AL predictor on and off between blocks) */
-    cudaGraphExec_t exec64_[2] = {nullptr, nullptr}, exec32_[2] = {nullptr, nullptr};
+    /* one graph per precision, predictor form and block length (the alpha
+     * pulse and the sigma trigger switch the AL predictor on and off between
+     * blocks, the dynamic evaluation frequency shortens the blocks):
+     * [predictor][short blocks] */
+    cudaGraphExec_t exec64_[2][2] = {}, exec32_[2][2] = {};
     /* the alpha pulse as the host last saw it, for its stderr lines */
     int pulse_seen_gate_ = 0, pulse_seen_phase_ = 0, pulse_gate_iter_ = 0, pulse_gate_k_[2] = {0, 0};
+    bool dyn_reported_ = false;
     double pulse_gate_rate_[2] = {0.0, 0.0};
     void pulse_report();
     /* evaluation blocks per graph launch: 1 while a controller may change the
      * step form between blocks */
-    int graph_blocks() const { return (cp_.pulse || cp_.trigger) ? 1 : std::max(1, O_.graph_blocks); }
+    int graph_blocks() const { return (cp_.pulse || cp_.trigger || cp_.dyn) ? 1 : std::max(1, O_.graph_blocks); }
     int nmisc_ = 0;
     cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
@@ -384,10 +392,18 @@ PanelDev<float> CpalSolver::panel_dev<float>() const {
 void CpalSolver::release() {
     for (auto &e : ev_)
         if (e) cudaEventDestroy(e);
-    for (auto *e : {&exec64_[0], &exec64_[1], &exec32_[0], &exec32_[1]}) {
-        if (*e) cudaGraphExecDestroy(*e);
+    for (auto *e : {&fork_ev_, &join_ev_}) {
+        if (*e) cudaEventDestroy(*e);
         *e = nullptr;
     }
+    if (side_) cudaStreamDestroy(side_);
+    side_ = nullptr;
+    for (auto *tab : {&exec64_, &exec32_})
+        for (auto &row : *tab)
+            for (auto &e : row) {
+                if (e) cudaGraphExecDestroy(e);
+                e = nullptr;
+            }
     if (h_st_) cudaFreeHost(h_st_);
     if (h_ps_) cudaFreeHost(h_ps_);
     h_st_ = nullptr;
@@ -452,6 +468,19 @@ CpalParams resolve_cpal_params(const cp_al_parameters_t &P, const cp_al_gb300_op
     cp.sigma_init_f = O.sigma_init_factor;
     cp.sigma_min_f = O.sigma_min_factor;
     cp.sigma_max_f = O.sigma_max_factor;
+    /* LP/CP_AL/src/solver.cu:1229-1255 */
+    const int F = cp.F;
+    cp.dyn_fast = std::min(std::max(O.dynamic_eval_fast, 3), F);
+    cp.dyn_resid = O.dynamic_eval != 0;
+    cp.dyn_sec = O.dynamic_eval_after_sec;
+    cp.dyn_iters = O.dynamic_eval_after_iters;
+    cp.dyn = (cp.dyn_resid || cp.dyn_sec > 0.0 || cp.dyn_iters > 0) && cp.dyn_fast < F;
+    cp.dyn_min_iters = std::max(O.dynamic_eval_min_iters > 0 ? O.dynamic_eval_min_iters : F, F);
+    cp.dyn_small = O.dynamic_eval_small_res;
+    cp.dyn_large = O.dynamic_eval_large_res;
+    cp.dyn_ratio = O.dynamic_eval_ratio;
+    cp.dyn_boot = std::max(O.dynamic_eval_bootstrap_iters, 0);
+    cp.cr_early_stopped = 0; /* set after the equilibration */
     cp.obj_const = prob->objective_constant;
     const int n = prob->num_variables, m = prob->num_constraints;
     const bool linf = cp.norm_linf;
@@ -734,7 +763,8 @@ void CpalSolver::setup_staged() {
 
 void CpalSolver::setup_loop() {
     const bool eligible = S_it_ <= 1024 && S_ev_ == S_it_ && !use_panels_ && !use_hot_ && !use_staged_ &&
-                          cp_.restart_select == 0 && !cp_.infeas && O_.timing == 0 && !cp_.pulse && !cp_.trigger;
+                          cp_.restart_select == 0 && !cp_.infeas && O_.timing == 0 && !cp_.pulse && !cp_.trigger &&
+                          !cp_.dyn;
     const bool want = O_.persistent_loop == 1;
     use_loop_ = eligible && want;
     if (!use_loop_) return;
@@ -845,6 +875,12 @@ void CpalSolver::upload() {
             sh_b3_ = blocks((long long)sh_r3_h.size(), kThreads / 32, 152 * 2);
             use_panels_ = pan_host_.H > 0;
             fuse_finish_ = O_.dual_fused_finish == 1;
+            dual_fork_ = use_panels_ && !fuse_finish_ && O_.dual_concurrent == 1;
+            if (dual_fork_ && !side_) {
+                PDAL_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+                PDAL_CUDA(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
+                PDAL_CUDA(cudaEventCreateWithFlags(&join_ev_, cudaEventDisableTiming));
+            }
         }
     }
     {
@@ -1259,6 +1295,7 @@ void CpalSolver::setup_device() {
                 if (mx <= O_.cr_early_stop_threshold) break;
             }
         }
+        cp_.cr_early_stopped = early && cr_passes < O_.cr_iterations; /* preconditioner.cu:246 */
         if (m) k_cr_exp<<<gm, kThreads, 0, stream_>>>(m_, lr, rinv, rsc_);
         k_cr_exp<<<gn, kThreads, 0, stream_>>>(n_, lc, dinv, dsc_);
         if (m)
@@ -1363,6 +1400,9 @@ void CpalSolver::setup_device() {
     s.fp32_stall_limit = O_.fp32_stall_evals;
     s.fp32_best_kkt = INFINITY;
     s.iter_limit = cp_.iteration_limit;
+    /* the dynamic evaluation frequency's bootstrap starts with short blocks
+     * (LP/CP_AL/src/solver.cu:1265-1268) */
+    s.F = (cp_.dyn && cp_.dyn_boot > 0) ? cp_.dyn_fast : cp_.F;
     cpal_set_coefficients(s);
     beta_on_ = s.beta > 0.0;
     if (cp_.pulse) {
@@ -1615,6 +1655,17 @@ void CpalSolver::launch_dual(int koff, bool major, bool timed) {
         });
         return;
     }
+    const PanelDev<T> pd = panel_dev<T>();
+    const size_t psm = panel_smem_bytes<T>(pd.W);
+    if (dual_fork_) {
+        /* the panel partials on the side stream, concurrently with the short
+         * rows: both only read x-bar and write disjoint outputs */
+        PDAL_CUDA(cudaEventRecord(fork_ev_, stream_));
+        PDAL_CUDA(cudaStreamWaitEvent(side_, fork_ev_, 0));
+        k_dual_panels<T, false, false, false><<<pd.nblocks, kPanelThreads, psm, side_>>>(pd, xbar, n_, st, da, wt, koff);
+        PDAL_LAUNCH_CHECK();
+        PDAL_CUDA(cudaEventRecord(join_ev_, side_));
+    }
     /* rows within the row-block budget, split by length */
     if (sh_b1_ + sh_b2_ + sh_b3_ > 0) {
         const ShortDev<T> sd = short_dev<T>();
@@ -1633,9 +1684,24 @@ void CpalSolver::launch_dual(int koff, bool major, bool timed) {
     }
     /* the long rows: panel partials, then one warp per row for the sum and
      * the dual epilogue */
+    const int gf = (pd.H * 32 + kThreads - 1) / kThreads;
+    if (dual_fork_) {
+        PDAL_CUDA(cudaStreamWaitEvent(stream_, join_ev_, 0));
+        if (major) {
+            if (beta_on_)
+                k_dual_long_finish<T, true, true><<<gf, kThreads, 0, stream_>>>(pd, da, st, wt, koff);
+            else
+                k_dual_long_finish<T, true, false><<<gf, kThreads, 0, stream_>>>(pd, da, st, wt, koff);
+        } else {
+            if (beta_on_)
+                k_dual_long_finish<T, false, true><<<gf, kThreads, 0, stream_>>>(pd, da, st, wt, koff);
+            else
+                k_dual_long_finish<T, false, false><<<gf, kThreads, 0, stream_>>>(pd, da, st, wt, koff);
+        }
+        PDAL_LAUNCH_CHECK();
+        return;
+    }
     if (timed) PDAL_CUDA(cudaEventRecordWithFlags(ev_[4], stream_, cudaEventRecordExternal));
-    const PanelDev<T> pd = panel_dev<T>();
-    const size_t psm = panel_smem_bytes<T>(pd.W);
     if (fuse_finish_) {
         /* the group that writes a long row's last partial finishes the row */
         if (major) {
@@ -1659,7 +1725,6 @@ void CpalSolver::launch_dual(int koff, bool major, bool timed) {
     launch_pdl_cfg(k_dual_panels<T, false, false, false>, pd.nblocks, kPanelThreads, psm, stream_, pd, xbar, n_, st, da,
                    wt, koff);
     if (timed) PDAL_CUDA(cudaEventRecordWithFlags(ev_[5], stream_, cudaEventRecordExternal));
-    const int gf = (pd.H * 32 + kThreads - 1) / kThreads;
     if (major) {
         if (beta_on_)
             launch_pdl(k_dual_long_finish<T, true, true>, gf, stream_, pd, da, st, wt, koff);
@@ -1748,8 +1813,7 @@ void CpalSolver::launch_eval() {
 }
 
 template <typename T>
-void CpalSolver::capture_block(cudaGraphExec_t &exec) {
-    const int F = cp_.F;
+void CpalSolver::capture_block(cudaGraphExec_t &exec, int F) {
     const int G = graph_blocks();
     const bool timing = O_.timing != 0;
     if (timing && !ev_[0])
@@ -1973,7 +2037,7 @@ void CpalSolver::polish() {
                 status = TERMINATION_REASON_TIME_LIMIT;
                 break;
             }
-            do_restart = cpal_should_restart(s, cp_);
+            do_restart = cpal_should_restart(s, cp_, cp_.F);
             if (do_restart) { /* solver.cu:4376-4404 */
                 if (primal) {
                     cp(v.x, v.xh, n);
@@ -2056,7 +2120,7 @@ void CpalSolver::run_loop() {
     loop_t0_ = t0;
     const int F = cp_.F;
     const int G = graph_blocks();
-    const int64_t per_block = (int64_t)iter_launches() * F + (m_ > 0 ? 4 : 3) + (cp_.infeas ? (m_ > 0 ? 2 : 1) : 0);
+    const int F0 = h_st_->F;
     k_start_clock<<<1, 1, 0, stream_>>>(st_);
     PDAL_LAUNCH_CHECK();
     launches += 1;
@@ -2076,13 +2140,16 @@ void CpalSolver::run_loop() {
             else
                 launch_loop<double>(chunk);
         } else {
+            const int Fb = h_st_->F; /* this block's length (the dynamic evaluation frequency may shorten it) */
+            const int64_t per_block = (int64_t)iter_launches() * Fb + (m_ > 0 ? 4 : 3) +
+                                      (cp_.infeas ? (m_ > 0 ? 2 : 1) : 0);
             cudaGraphExec_t *exec;
             if (fp32_phase_) {
-                exec = &exec32_[beta_on_ ? 1 : 0];
-                if (!*exec) capture_block<float>(*exec);
+                exec = &exec32_[beta_on_ ? 1 : 0][Fb != F ? 1 : 0];
+                if (!*exec) capture_block<float>(*exec, Fb);
             } else {
-                exec = &exec64_[beta_on_ ? 1 : 0];
-                if (!*exec) capture_block<double>(*exec);
+                exec = &exec64_[beta_on_ ? 1 : 0][Fb != F ? 1 : 0];
+                if (!*exec) capture_block<double>(*exec, Fb);
             }
             PDAL_CUDA(cudaGraphLaunch(*exec, stream_));
             launches += (per_block + ((fp32_phase_ ? hot_in<float>() : hot_in<double>()) ? 1 : 0)) * G;
@@ -2099,7 +2166,7 @@ void CpalSolver::run_loop() {
             sum_ms[ph][0] += a;
             sum_ms[ph][1] += b;
             sum_ms[ph][2] += c;
-            if (use_panels_) {
+            if (use_panels_ && !dual_fork_) {
                 float d = 0, e = 0;
                 PDAL_CUDA(cudaEventElapsedTime(&d, ev_[1], ev_[4]));
                 PDAL_CUDA(cudaEventElapsedTime(&e, ev_[4], ev_[5]));
@@ -2120,6 +2187,14 @@ void CpalSolver::run_loop() {
         }
         if (h_st_->status == kStatusDeviceError) check_device_error();
         if (cp_.pulse) pulse_report();
+        if (cp_.dyn && h_st_->F != F0 && !dyn_reported_) {
+            /* LP/CP_AL/src/solver.cu:1557-1569 */
+            dyn_reported_ = true;
+            if (P_.verbose || cp_.dyn_sec > 0.0 || cp_.dyn_iters > 0)
+                printf("[dynamic-eval] iter=%d solve_sec=%.12e eval_frequency=%d->%d relative_primal=%.12e "
+                       "relative_dual=%.12e\n",
+                       h_st_->total, h_st_->elapsed, F0, h_st_->F, h_st_->rel_p, h_st_->rel_d);
+        }
         if (cp_.trigger && h_st_->trigger_iter && P_.verbose && h_st_->restart && h_st_->trigger_iter == h_st_->total)
             printf("sigma-trigger iter %d rpr %.12e rdr %.12e sigma %.12e base %.12e\n", h_st_->total, h_st_->rel_p,
                    h_st_->rel_d, h_st_->sigma, h_st_->sigma_base);
@@ -2369,6 +2444,7 @@ static void fill_stats(const pdal::CpalSolver &s, double total) {
     st.pulse_start_iteration = s.host_state.pulse_phase ? s.host_state.pulse_start : -1;
     st.pulse_gate = s.host_state.pulse_gate;
     st.sigma_trigger_iteration = s.host_state.trigger_iter;
+    st.dynamic_eval_iteration = s.host_state.dyn_iter;
 }
 
 /* Options from the environment, unless a switch of a controller this library

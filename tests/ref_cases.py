@@ -91,6 +91,18 @@ CASES = [
          vectors=True, controllers=True),
     dict(name="lp_small_sigma_trigger", kind="lp", gen=SMALL, env={**LAMBDA0_ENV, **TRIGGER_ENV},
          params={**P8, "verbose": True}, parity=True, vectors=True, oracle=True, controllers=True),
+    # the dynamic evaluation frequency (solver.cu:1229-1255, 1529-1583): by the residual test, by the
+    # iteration gate, and the bootstrap's short blocks
+    dict(name="lp_small_dynamic_eval", kind="lp", gen=SMALL,
+         env={**LAMBDA0_ENV, "CP_AL_DYNAMIC_EVAL": "1", "CP_AL_DYNAMIC_EVAL_RATIO": "3",
+              "CP_AL_DYNAMIC_EVAL_LARGE_RES": "1e-6"},
+         params={**P8, "verbose": True}, parity=True, vectors=True, oracle=True, controllers=True),
+    dict(name="lp_small_dynamic_eval_iters", kind="lp", gen=SMALL,
+         env={**LAMBDA0_ENV, "CP_AL_DYNAMIC_EVAL_AFTER_ITERS": "1500"}, params=P8, parity=True, vectors=True,
+         oracle=True, controllers=True),
+    dict(name="lp_small_dynamic_eval_bootstrap", kind="lp", gen=SMALL,
+         env={**LAMBDA0_ENV, "CP_AL_DYNAMIC_EVAL": "1", "CP_AL_DYNAMIC_EVAL_BOOTSTRAP_ITERS": "1000"}, params=P8,
+         parity=True, vectors=True, oracle=True, controllers=True),
     # reference timing rows (time to relative KKT 1e-6, and per-iteration time on the large LP)
     dict(name="lp_c0_sigma_protocol_1e-6", kind="lp", gen=C0, env=SIGMA_PROTOCOL_ENV,
          params={"eps": 1e-6, "l_inf_ruiz_iterations": 4}, parity=True, timing="C0 to 1e-6"),
@@ -289,10 +301,13 @@ def controller_events(text: str) -> dict:
     stderr and stdout, or this library's): the iteration at which the alpha
     pulse started (-1: never), whether its gate was evaluated and passed
     (None: not evaluated), and the iteration at which the sigma trigger fired
-    (0: never; printed with verbose output only)."""
+    (0: never; printed with verbose output only) and the dynamic evaluation
+    frequency switched to short blocks (0: never; printed with verbose output
+    or an iteration or time gate)."""
     import re
 
-    out = {"pulse_start": -1, "pulse_gate_pass": None, "pulse_gate_iteration": -1, "sigma_trigger": 0}
+    out = {"pulse_start": -1, "pulse_gate_pass": None, "pulse_gate_iteration": -1, "sigma_trigger": 0,
+           "dynamic_eval": 0}
     m = re.search(r"\[alpha-direct-pulse-start\] charged_iter=(\d+)", text)
     if m:
         out["pulse_start"] = int(m.group(1))
@@ -303,6 +318,9 @@ def controller_events(text: str) -> dict:
     m = re.search(r"sigma-trigger iter (\d+)", text)
     if m:
         out["sigma_trigger"] = int(m.group(1))
+    m = re.search(r"\[dynamic-eval\] iter=(\d+)", text)
+    if m:
+        out["dynamic_eval"] = int(m.group(1))
     return out
 
 

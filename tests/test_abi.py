@@ -221,7 +221,6 @@ def test_options_from_env_reads_reference_variables(lp_lib, monkeypatch):
 @pytest.mark.parametrize("name,value,extra", [
     ("CP_AL_ADAPTIVE_LAMBDA", "1", {}),
     ("CP_AL_LAMBDA_PROFILE", "mp_race", {}),
-    ("CP_AL_DYNAMIC_EVAL", "1", {}),
     ("CP_AL_ALPHA_ROLLBACK_TRIAL", "1", {}),
 ])
 def test_unbuilt_controller_switch_is_refused(lp_lib, monkeypatch, name, value, extra):

@@ -221,6 +221,25 @@ def test_staged_primal_product_changes_nothing(lp_lib, precision, budget):
         assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refine"])
+def test_concurrent_dual_launches_change_nothing(lp_lib, precision):
+    """The dual step's short-row and panel launches on two streams
+    (dual_concurrent) write disjoint outputs from the same x-bar: iterates
+    bit-identical to the launches one after the other, also with the timing
+    events bracketing the forked step."""
+    d = _lp_with_dense_rows()
+    p = {"eps": 1e-14, "iteration_limit": 2000, "time_limit": 120, "l_inf_ruiz_iterations": 4}
+    base = {"precision": precision, "spmv_nnz_per_block": 256, "dual_panels": 1, "panel_width": 1024,
+            "fp32_switch_tol": 1e-4, "fp32_stall_evals": 2}
+    a = lp.solve(d, p, {**base, "dual_concurrent": 0})
+    for extra in ({}, {"timing": 1}):
+        b = lp.solve(d, p, {**base, "dual_concurrent": 1, **extra})
+        assert b.stats["panel_rows"] == 3
+        assert a.iterations == b.iterations and a.stats["fp32_iterations"] == b.stats["fp32_iterations"]
+        assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
+    assert b.stats["avg_dual_ms" if precision == "fp64" else "avg_dual32_ms"] > 0
+
+
 def test_panels_fp32_form_reaches_tolerance(lp_lib):
     """Chosen form (FP32 phase, then FP64) with the panel path: same status and
     objective as the oracle at relative KKT 1e-7."""

@@ -80,10 +80,11 @@ GATE = {None: 0, True: 1, False: 2}
 
 @pytest.mark.parametrize("name", [c["name"] for c in RC.CASES if c.get("controllers")])
 def test_controllers_act_where_the_reference_does(lp_lib, name, monkeypatch, capfd):
-    """The alpha pulse (LP/CP_AL/src/solver.cu:885-1032) and the sigma
-    trigger (1496-1527) act at the iterations where the reference's acted, as
-    its log lines record them: the pulse's gate evaluation and pass/reject,
-    the start of its positive block, the trigger's iteration.  This library's
+    """The alpha pulse (LP/CP_AL/src/solver.cu:885-1032), the sigma trigger
+    (1496-1527) and the dynamic evaluation frequency (1529-1583) act at the
+    iterations where the reference's acted, as its log lines record them: the
+    pulse's gate evaluation and pass/reject, the start of its positive block,
+    the trigger's iteration, the switch to short blocks.  This library's
     own pulse lines say the same.  The solution vectors agree with the
     reference's to CTL_VEC_TOL: with the controllers off the same runs end
     1e-10 to 1e-6 away from them, so the check sees what the controllers did.
@@ -103,6 +104,7 @@ def test_controllers_act_where_the_reference_does(lp_lib, name, monkeypatch, cap
     assert g.stats["pulse_start_iteration"] == ev["pulse_start"], (g.stats["pulse_start_iteration"], ev)
     assert g.stats["pulse_gate"] == GATE[ev["pulse_gate_pass"]], (g.stats["pulse_gate"], ev)
     assert g.stats["sigma_trigger_iteration"] == ev["sigma_trigger"], (g.stats["sigma_trigger_iteration"], ev)
+    assert g.stats["dynamic_eval_iteration"] == ev.get("dynamic_eval", 0), (g.stats["dynamic_eval_iteration"], ev)
     if case["env"].get("CP_AL_ALPHA_DIRECT_PULSE") == "1":
         mine = RC.controller_events(err)
         for k in ("pulse_start", "pulse_gate_pass", "pulse_gate_iteration"):

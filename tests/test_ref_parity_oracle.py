@@ -66,8 +66,8 @@ def _quiet(params: dict) -> dict:
 
 @pytest.mark.parametrize("name", [c["name"] for c in RC.CASES if c.get("oracle") and c.get("controllers")])
 def test_oracle_controllers_act_where_the_reference_does(lp_lib, name, monkeypatch):
-    """The oracle's alpha pulse and sigma trigger act at the iterations where
-    the reference's did (its log lines, recorded in the fixture), and its
+    """The oracle's alpha pulse, sigma trigger and dynamic evaluation frequency
+    act at the iterations where the reference's did (its log lines, recorded in the fixture), and its
     solution vectors agree with the reference's to 1e-11 (1e-10 to 1e-6 apart
     with the controllers off)."""
     from oracle import oracle as O
@@ -80,6 +80,7 @@ def test_oracle_controllers_act_where_the_reference_does(lp_lib, name, monkeypat
     assert o.stats["pulse_start_iteration"] == ev["pulse_start"], (o.stats, ev)
     assert o.stats["pulse_gate"] == {None: 0, True: 1, False: 2}[ev["pulse_gate_pass"]], (o.stats, ev)
     assert o.stats["sigma_trigger_iteration"] == ev["sigma_trigger"], (o.stats, ev)
+    assert o.stats["dynamic_eval_iteration"] == ev.get("dynamic_eval", 0), (o.stats, ev)
     assert np.max(np.abs(o.x - xr)) / (1.0 + np.max(np.abs(xr))) <= 1e-11
     assert np.max(np.abs(o.y - yr)) / (1.0 + np.max(np.abs(yr))) <= 1e-11
 

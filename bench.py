@@ -337,8 +337,9 @@ def run_ours(args, rank, world, local):
                            "us_per_iteration": dt64 / max(r64.iterations - i0, 1) * 1e6},
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": int(re.stats["h2d_bytes"]),
                     "d2h_bytes_per_step": int(re.stats["d2h_bytes"]), "s_per_step": dte / len(rese),
-                    "phases_s": {k: re.stats[k] for k in ("prepare_sec", "upload_sec", "equilibration_sec",
-                                                          "power_sec", "setup_sec", "loop_sec", "total_sec")},
+                    "phases_s": {k: re.stats[k] for k in ("prepare_sec", "upload_sec", "upload_plan_sec",
+                                                          "upload_alloc_sec", "equilibration_sec", "power_sec",
+                                                          "setup_sec", "loop_sec", "total_sec")},
                     "power_iterations": re.stats["power_iterations"]},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",

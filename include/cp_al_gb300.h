@@ -239,6 +239,11 @@ typedef struct {
     int pulse_gate;
     int sigma_trigger_iteration;
     int dynamic_eval_iteration;   /* iteration at which the blocks became dynamic_eval_fast long (0: never) */
+    /* parts of upload_sec: the host-side row-block and panel plans, and the
+     * device arena's allocation (the rest is copies and the device
+     * transpose) */
+    double upload_plan_sec;
+    double upload_alloc_sec;
 } cp_al_gb300_stats_t;
 
 /* The reference defaults of every field, ignoring the environment. */

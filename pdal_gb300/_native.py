@@ -266,6 +266,8 @@ class CpalStats(C.Structure):
         ("pulse_gate", C.c_int),
         ("sigma_trigger_iteration", C.c_int),
         ("dynamic_eval_iteration", C.c_int),
+        ("upload_plan_sec", C.c_double),
+        ("upload_alloc_sec", C.c_double),
     ]
 
 

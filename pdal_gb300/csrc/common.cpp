@@ -214,6 +214,9 @@ HostPanels plan_panels(int nr, int nc, const int *rp, const int *ci, int S, int 
         }
     });
     std::vector<long long> start((size_t)H * P, 0);
+    size_t used = 0; /* (row, panel) pairs with entries: the segments */
+    for (int c : cnt) used += c > 0 ? 1 : 0;
+    Q.seg.reserve(4 * used);
     long long pos = 0;
     for (int p = 0; p < P; ++p)
         for (int h = 0; h < H; ++h) {
@@ -226,8 +229,10 @@ HostPanels plan_panels(int nr, int nc, const int *rp, const int *ci, int S, int 
         }
     if (pos > (long long)INT32_MAX - 16) throw Error("long rows too large for the panel plan");
     Q.len = pos;
-    Q.pmap.assign((size_t)pos, -1);
-    Q.off.assign((size_t)pos, 0);
+    /* every position is written once below, by the thread that owns its
+     * row: the entries, then the segment's padding (-1, offset 0) */
+    Q.pmap.resize((size_t)pos);
+    Q.off.resize((size_t)pos);
     parallel_for(nt, [&](int t) {
         std::vector<long long> at((size_t)P);
         for (int h = t; h < H; h += nt) {
@@ -238,6 +243,14 @@ HostPanels plan_panels(int nr, int nc, const int *rp, const int *ci, int S, int 
                 const long long q = at[p]++;
                 Q.pmap[(size_t)q] = k;
                 Q.off[(size_t)q] = (uint16_t)(ci[k] - p * W);
+            }
+            for (int p = 0; p < P; ++p) {
+                const int c = cnt[(size_t)h * P + p];
+                const long long end = start[(size_t)h * P + p] + ((c + 3) & ~3);
+                for (long long q = at[p]; q < end; ++q) {
+                    Q.pmap[(size_t)q] = -1;
+                    Q.off[(size_t)q] = 0;
+                }
             }
         }
     });

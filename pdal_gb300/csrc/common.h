@@ -10,8 +10,10 @@
 #include <cstdint>
 #include <cstdio>
 #include <functional>
+#include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace pdal {
@@ -129,11 +131,31 @@ HostPlan plan_rows(int nr, const int *rp, int S);
  * sum of its P partials in panel order (zeros where the row has no entry in
  * a panel), so the result is deterministic.
  */
+/* An allocator that leaves new elements uninitialised, so that a large host
+ * array is first touched by the threads that fill it (in parallel) instead
+ * of being zeroed on one thread. */
+template <typename T>
+struct UninitAlloc : std::allocator<T> {
+    template <typename U>
+    struct rebind {
+        using other = UninitAlloc<U>;
+    };
+    UninitAlloc() = default;
+    template <typename U>
+    UninitAlloc(const UninitAlloc<U> &) {}
+    template <typename U>
+    void construct(U *) noexcept {}
+    template <typename U, typename... A>
+    void construct(U *p, A &&...a) {
+        ::new ((void *)p) U(std::forward<A>(a)...);
+    }
+};
+
 struct HostPanels {
     int W = 0, P = 0, H = 0;
     std::vector<int> rows;      /* H long rows (ascending) */
-    std::vector<int> pmap;      /* panel-array position -> CSR position, -1 for padding */
-    std::vector<uint16_t> off;  /* column - p * W */
+    std::vector<int, UninitAlloc<int>> pmap;          /* panel-array position -> CSR position, -1 for padding */
+    std::vector<uint16_t, UninitAlloc<uint16_t>> off; /* column - p * W (0 for padding) */
     std::vector<int> seg;       /* 4 ints per segment: {h, k0, k1, p} (k0, k1 multiples of 4) */
     std::vector<int> piece;     /* 4 ints per piece: {panel, first segment, end segment, 0} */
     std::vector<int> cta;       /* 4 ints per block: {first piece, end piece, 0, 0} */

@@ -10,6 +10,7 @@
  */
 #include "../../include/cp_al.h"
 #include "../../include/cp_al_gb300.h"
+#include "common.h"
 
 #include <cerrno>
 #include <cmath>
@@ -19,11 +20,26 @@
 
 namespace {
 
+/* memcpy of a large array by the host threads (the destination's pages are
+ * first touched in parallel too): the deep copies of a 20M-nonzero problem
+ * are ~300 MB */
+void copy_bytes(void *dst, const void *src, size_t bytes) {
+    const int nt = bytes >= (8u << 20) ? pdal::host_threads((long long)(bytes >> 4)) : 1;
+    if (nt <= 1) {
+        memcpy(dst, src, bytes);
+        return;
+    }
+    pdal::parallel_for(nt, [&](int t) {
+        const size_t b0 = bytes * t / nt & ~size_t(63), b1 = t + 1 == nt ? bytes : bytes * (t + 1) / nt & ~size_t(63);
+        memcpy(static_cast<char *>(dst) + b0, static_cast<const char *>(src) + b0, b1 - b0);
+    });
+}
+
 double *fill_or_copy(int n, const double *src, double fill) {
     double *d = (double *)malloc(sizeof(double) * (n > 0 ? n : 1));
     if (!d) return nullptr;
     if (src)
-        memcpy(d, src, sizeof(double) * (size_t)n);
+        copy_bytes(d, src, sizeof(double) * (size_t)n);
     else
         for (int i = 0; i < n; ++i) d[i] = fill;
     return d;
@@ -173,12 +189,12 @@ lp_problem_t *create_lp_problem(const double *objective_c, const matrix_desc_t *
             break;
         }
         if (A_desc->data.csr.row_ptr)
-            memcpy(rp, A_desc->data.csr.row_ptr, sizeof(int) * ((size_t)m + 1));
+            copy_bytes(rp, A_desc->data.csr.row_ptr, sizeof(int) * ((size_t)m + 1));
         else
             rp[0] = 0;
         if (nnz) {
-            memcpy(ci, A_desc->data.csr.col_ind, sizeof(int) * (size_t)nnz);
-            memcpy(vv, A_desc->data.csr.vals, sizeof(double) * (size_t)nnz);
+            copy_bytes(ci, A_desc->data.csr.col_ind, sizeof(int) * (size_t)nnz);
+            copy_bytes(vv, A_desc->data.csr.vals, sizeof(double) * (size_t)nnz);
         }
         p->constraint_matrix_row_pointers = rp;
         p->constraint_matrix_col_indices = ci;

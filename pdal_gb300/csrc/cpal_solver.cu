@@ -177,6 +177,7 @@ class CpalSolver {
     CpalState host_state{};
     double setup_sec = 0, loop_sec = 0;
     double prepare_sec = 0, upload_sec = 0, equil_sec = 0, power_sec = 0;
+    double upload_plan_sec = 0, upload_alloc_sec = 0; /* parts of upload_sec */
     int64_t launches = 0;
     int64_t h2d = 0, d2h = 0;
     int power_iters = 0;
@@ -848,6 +849,20 @@ void CpalSolver::upload() {
             sh_r2_h.clear();
             sh_r3_h.clear();
             const int *cip = prob_->constraint_matrix_col_indices;
+            {
+                size_t n1 = 0, n2 = 0, n3 = 0;
+                for (int r = 0; r < m_; ++r) {
+                    const int len = rp[r + 1] - rp[r];
+                    n1 += len <= 1;
+                    n2 += len > 1 && len <= kShortMidLen;
+                    n3 += len > kShortMidLen && len <= S_it_;
+                }
+                sh_r1_h.reserve(n1);
+                sh_p1_h.reserve(n1);
+                sh_c1_h.reserve(n1);
+                sh_r2_h.reserve(n2);
+                sh_r3_h.reserve(n3);
+            }
             for (int r = 0; r < m_; ++r) {
                 const int len = rp[r + 1] - rp[r];
                 if (len <= 1) {
@@ -863,9 +878,17 @@ void CpalSolver::upload() {
             use_hot_ = O_.primal_hot_rows != 0 && pan_host_.H > 0 &&
                        pan_host_.H <= kHotRows;
             /* the warp rows longest first, so that the longest start in the
-             * first round of the grid-stride loop */
-            std::stable_sort(sh_r3_h.begin(), sh_r3_h.end(),
-                             [&](int a, int b) { return rp[a + 1] - rp[a] > rp[b + 1] - rp[b]; });
+             * first round of the grid-stride loop (a counting sort by length:
+             * rows of equal length keep their order) */
+            {
+                const int span = S_it_ - kShortMidLen; /* lengths kShortMidLen + 1 .. S_it_ */
+                std::vector<int> at((size_t)span + 1, 0);
+                for (int r : sh_r3_h) at[(size_t)(S_it_ - (rp[r + 1] - rp[r])) + 1]++;
+                for (int q = 0; q < span; ++q) at[q + 1] += at[q];
+                std::vector<int> sorted(sh_r3_h.size());
+                for (int r : sh_r3_h) sorted[(size_t)at[(size_t)(S_it_ - (rp[r + 1] - rp[r]))]++] = r;
+                sh_r3_h.swap(sorted);
+            }
             /* a fixed number of blocks per part, each looping over its rows */
             auto blocks = [](long long rows, long long per_block, long long cap) {
                 return (int)std::min<long long>((rows + per_block - 1) / per_block, cap);
@@ -892,10 +915,13 @@ void CpalSolver::upload() {
         longs(m_, prob_->constraint_matrix_row_pointers, eq_long_h_[0]);
         longs(n_, At_host_.rp.data(), eq_long_h_[1]);
     }
+    const double t_alloc = now_sec();
+    upload_plan_sec = t_alloc - t_up;
     arena_.begin_measure();
     alloc_all();
     arena_.reserve_measured();
     alloc_all();
+    upload_alloc_sec = now_sec() - t_alloc;
     PDAL_CUDA(cudaMemsetAsync(dev_err_, 0, sizeof(int), stream_));
     for (int q = 0; q < 2; ++q)
         if (!eq_long_h_[q].empty())
@@ -1008,8 +1034,8 @@ void CpalSolver::upload() {
         PDAL_CUDA(cudaMemsetAsync(y00_, 0, std::max<size_t>(m, 1) * sizeof(double), stream_));
     PDAL_CUDA(cudaStreamSynchronize(stream_));
     At_host_ = HostCsr(); /* host transpose no longer needed */
-    pan_host_.pmap = std::vector<int>();
-    pan_host_.off = std::vector<uint16_t>();
+    pan_host_.pmap = decltype(pan_host_.pmap)();
+    pan_host_.off = decltype(pan_host_.off)();
     upload_sec = now_sec() - t_up;
 }
 
@@ -2426,6 +2452,8 @@ static void fill_stats(const pdal::CpalSolver &s, double total) {
     st.al_penalty = s.host_state.beta;
     st.prepare_sec = s.prepare_sec;
     st.upload_sec = s.upload_sec;
+    st.upload_plan_sec = s.upload_plan_sec;
+    st.upload_alloc_sec = s.upload_alloc_sec;
     st.equilibration_sec = s.equil_sec;
     st.power_sec = s.power_sec;
     st.polish_primal_status = s.polish_status[0];

@@ -158,6 +158,14 @@ CLI_CASES = [
          gen=("random_lp", {"m": 2000, "n": 5000, "nnz_per_col": 8, "seed": 7, "eq_fraction": 0.0}), env=UNIFIED_ENV,
          args=_cli_args(1e-6, 100000)),
     dict(name="cli_unified_lowobj", gen=("sparse_objective_lp", {}), env=UNIFIED_ENV, args=_cli_args(1e-6, 100000)),
+    # the feature policy alone, variant trigger_select: the sigma trigger, the dynamic evaluation frequency
+    # (which switches to short blocks at 5,200 iterations on this LP) and three-point restart selection at
+    # lambda = 0.  The policy's 50 Curtis-Reid passes leave this LP ill-conditioned: rounding differences
+    # between any two implementations grow (1e-13 at 1,000 iterations, 1e-9 at 6,000) until a restart decision
+    # flips near 20,000, so the case stops at 6,000.
+    dict(name="cli_feature_trigger_select", gen=("zipf_lp", {"m": 2000, "n": 4000, "nnz": 40000, "seed": 1000}),
+         env={"CP_AL_FEATURE_AUTO_POLICY": "1", "CP_AL_FEATURE_POLICY_VARIANT": "trigger_select",
+              "CP_AL_PROGRESS_LOG_FREQ": "0"}, args=_cli_args(1e-6, 6000)),
 ]
 CLI_BY_NAME = {c["name"]: c for c in CLI_CASES}
 

@@ -362,6 +362,10 @@ int run_batch(int count, lp_problem_t *const *problems, const cp_al_parameters_t
     CpalParams cp = prep[0].cp; /* instance-specific norms are overridden per instance in the kernel */
     if (cp.restart_select != 0) throw Error("batch_solve: restart_select is not supported by the batched solver");
     if (O.cr_iterations > 0) throw Error("batch_solve: Curtis-Reid scaling is not supported by the batched solver");
+    if (O.alpha_direct_pulse || O.sigma_trigger || O.dynamic_eval || O.dynamic_eval_after_sec > 0.0 ||
+        O.dynamic_eval_after_iters > 0)
+        throw Error("batch_solve: the alpha pulse, the sigma trigger and the dynamic evaluation frequency are not "
+                    "supported by the batched solver");
 
     int dev_id = 0, sms = 0, per_sm = 0;
     PDAL_CUDA(cudaGetDevice(&dev_id));

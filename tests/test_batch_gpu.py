@@ -125,3 +125,16 @@ def test_schedule_autotuner_and_fixed_schedules():
     assert st3["tune_sec"] == 0.0 and (st3["block_nnz"], st3["blocks_per_sm"]) == (t["block_nnz"], t["blocks_per_sm"])
     with pytest.raises(RuntimeError):
         lp.solve_batch(items, params, {"spmv_nnz_per_block": 2048, "batch_blocks_per_sm": 4})
+
+
+@pytest.mark.parametrize("opts", [{"restart_select": 1}, {"cr_iterations": 5}, {"alpha_direct_pulse": 1},
+                                  {"sigma_trigger": 1}, {"dynamic_eval": 1}, {"dynamic_eval_after_iters": 400}],
+                         ids=["restart_select", "curtis_reid", "pulse", "trigger", "dynamic_eval", "dynamic_eval_iters"])
+def test_batch_refuses_single_solve_options(lp_lib, opts):
+    """Options the batched launch cannot honour are refused with a message
+    (an error, not a silent skip): restart target selection, Curtis-Reid
+    scaling, and the benchmark controllers whose step or block-length changes
+    would switch the kernel form a batch launch fixes."""
+    items = [random_lp(30, 60, 3, seed=s) for s in range(2)]
+    with pytest.raises(RuntimeError, match="not supported by the batched solver"):
+        lp.solve_batch(items, {"eps": 1e-6}, {"device": 0, **opts})

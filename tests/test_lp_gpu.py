@@ -580,3 +580,32 @@ def test_device_transpose_is_the_host_transpose(lp_lib, case):
     assert a.iterations == b.iterations
     assert np.array_equal(a.x, b.x) and np.array_equal(a.y, b.y)
     assert b.stats["h2d_bytes"] < a.stats["h2d_bytes"]
+
+
+def test_controllers_in_the_fp32_phase(lp_lib):
+    """The sigma trigger and the alpha pulse switch the AL penalty on inside
+    the chosen form's FP32 phase (the host then recomputes A x0 and the
+    predictor in FP32 before the predictor form's graph): the trigger fires
+    where the FP64 form's does and the solve reaches the oracle's optimum; the
+    pulse runs its positive block inside a long FP32 phase and the iterate
+    stays close to the FP64 form's."""
+    trig = {"al_lambda": 0.0, "sigma_trigger": 1, "sigma_trigger_min_iters": 2000, "sigma_trigger_primal": 0.0,
+            "sigma_trigger_dual": 1.0, "sigma_trigger_ratio": 0.0}
+    d = I.random_lp(300, 800, 6, seed=17)
+    p = {"eps": 1e-8, "l_inf_ruiz_iterations": 4}
+    g = lp.solve(d, p, {**trig, "precision": "fp32_refine", "fp32_switch_tol": 1e-7})
+    o = O.solve_lp(d, p, trig)
+    assert g.status == o.status == "OPTIMAL"
+    assert g.stats["sigma_trigger_iteration"] == o.stats["sigma_trigger_iteration"] == 2000
+    assert g.stats["fp32_iterations"] > 2000
+    assert rel(g.primal_objective, o.primal_objective) <= 1e-7
+    d = I.random_lp(200, 500, 5, seed=5)
+    p = {"eps": 1e-14, "iteration_limit": 12000, "l_inf_ruiz_iterations": 0, "has_pock_chambolle_alpha": False,
+         "bound_objective_rescaling": False}
+    pulse = {"al_lambda": 0.0, "alpha_direct_pulse": 1, "pulse_force": 1}
+    g32 = lp.solve(d, p, {**pulse, "precision": "fp32_refine", "fp32_switch_tol": 1e-12,
+                          "fp32_stall_evals": 1_000_000})
+    g64 = lp.solve(d, p, pulse)
+    assert g32.stats["fp32_iterations"] == 12000 and g32.stats["pulse_gate"] == 1
+    assert 10000 <= g32.stats["pulse_start_iteration"] <= 11800
+    assert np.all(np.isfinite(g32.x)) and rel(g32.primal_objective, g64.primal_objective) <= 1e-5

@@ -189,6 +189,9 @@ void usage(const char *prog) {
             fprintf(stderr, "      %-34s %s\n", head, o.help);
     }
     fprintf(stderr, "\nCP_AL_* environment variables are read as the solver library reads them.\n");
+    fprintf(stderr, "CP_AL_UNIFIED_POLICY, CP_AL_FEATURE_AUTO_POLICY and CP_AL_STRUCTURAL_TAIL_CUT switch on the\n"
+                    "benchmark policy layer (features of the LP pick the settings; CP_AL_FEATURE_AUDIT_ONLY stops\n"
+                    "after printing them).\n");
 }
 
 } // namespace

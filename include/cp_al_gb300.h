@@ -181,8 +181,9 @@ typedef struct {
     /* --- options of this implementation (continued) --- */
     int dual_concurrent;          /* with the panel path: the dual step's short-row launch and its
                                      long rows' panel launch run concurrently on two streams (also in
-                                     the captured graphs).  1 = so, 0 or -1 (default) = one after
-                                     the other.  Results are bit-identical either way */
+                                     the captured graphs).  1 = in both phases, -1 (default) = in the
+                                     FP64 phase only (measured faster there, no faster in FP32), 0 =
+                                     one after the other.  Results are bit-identical either way */
 } cp_al_gb300_options_t;
 
 /* Statistics of the last solve on this thread (for benchmarks and tests). */

@@ -1410,10 +1410,10 @@ void *oracle_cpal_session_create(const lp_problem_t *prob, const cp_al_parameter
 int oracle_cpal_session_iterate(void *h, int iterations) {
     OracleSession *s = (OracleSession *)h;
     if (!s) return -1;
-    const int F = s->P.termination_evaluation_frequency;
     int done = 0;
     while (done < iterations) {
         s->S->reason = TERMINATION_REASON_UNSPECIFIED;
+        const int F = s->S->F_cur; /* this block's length */
         if (oracle_block(*s->S, s->do_restart, s->charged, 0.0, 2147483647) &&
             s->S->reason == TERMINATION_REASON_OPTIMAL)
             break;
